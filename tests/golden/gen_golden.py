@@ -1,0 +1,120 @@
+"""Generate the golden fixtures that pin the oracle to the reference.
+
+Run in a checkout that has the reference mounted (REF, default
+/root/reference) after `make -C oracle ref`, which compiles the unmodified
+reference sources (ref/ variant) with oracle/ref_harness.cpp into
+oracle/_ref/ref_harness.  Writes:
+
+  tests/golden/minife_golden.npz   full arrays for small boxes
+  tests/golden/golden_hashes.json  sha256 of every array for larger boxes
+
+The legacy unit test's known-answer element matrix (ref/basic/utest_cases.hpp,
+get_test_elem_mat) is read from the reference source as text and stored too.
+The GPU machine never runs this script; tests only read its outputs.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+import re
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("REF", "/root/reference")
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+EPS = 2.220446049250313e-16
+
+FULL_CASES = [  # (nx, ny, nz, max_iter, tol_mode, tol)
+    (1, 1, 2, 200, 0, EPS),
+    (2, 2, 2, 200, 0, EPS),
+    (4, 5, 6, 200, 0, EPS),
+    (17, 3, 5, 200, 0, EPS),
+    (10, 10, 10, 200, 0, EPS),
+    (10, 10, 10, 200, 1, 1e-8),
+    (7, 9, 4, 200, 1, 1e-8),
+]
+HASH_CASES = [
+    (20, 30, 40, 200, 0, EPS),
+    (30, 30, 30, 200, 0, EPS),
+    (30, 30, 30, 200, 1, 1e-8),
+    (24, 16, 8, 200, 1, 1e-8),
+]
+ARRAYS = [("row_offsets", "i32", np.int32), ("cols", "i32", np.int32),
+          ("vals_prebc", "f64", np.float64), ("b_prebc", "f64", np.float64),
+          ("vals", "f64", np.float64), ("b", "f64", np.float64), ("x", "f64", np.float64)]
+
+
+def run_case(case, tmp):
+    nx, ny, nz, mi, mode, tol = case
+    d = os.path.join(tmp, "c_%d_%d_%d_%d" % (nx, ny, nz, mode))
+    os.makedirs(d, exist_ok=True)
+    subprocess.run([HARNESS, str(nx), str(ny), str(nz), str(mi), str(mode), repr(tol), d],
+                   check=True, capture_output=True)
+    arrs = {name: np.fromfile(os.path.join(d, "%s.%s" % (name, ext)), dt)
+            for name, ext, dt in ARRAYS}
+    meta = {}
+    for line in open(os.path.join(d, "meta.txt")):
+        k, v = line.split()
+        meta[k] = float(v) if "." in v or "e" in v else int(v)
+    return arrs, meta
+
+
+def key(case):
+    nx, ny, nz, mi, mode, tol = case
+    return "%dx%dx%d_mode%d" % (nx, ny, nz, mode)
+
+
+def utest_known_answer():
+    path = os.path.join(REF, "ref", "basic", "utest_cases.hpp")
+    text = open(path).read()
+    body = text[text.index("void get_test_elem_mat"):]
+    body = body[: body.index("}")]
+    vals = np.zeros(36)
+    for idx, val in re.findall(r"elem_mat\[(\d+)\]\s*=\s*([-0-9.e]+);", body):
+        vals[int(idx)] = float(val)
+    return vals
+
+
+def main():
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: make -C oracle ref")
+    out = {}
+    hashes = {}
+    with tempfile.TemporaryDirectory() as tmp:
+        for case in FULL_CASES:
+            arrs, meta = run_case(case, tmp)
+            k = key(case)
+            for name, arr in arrs.items():
+                out["%s/%s" % (k, name)] = arr
+            out["%s/meta" % k] = np.array([meta["num_iters"], meta["normr"], meta["verify"],
+                                           meta["abs_tol"], case[3], case[4], case[5]])
+        for case in HASH_CASES:
+            arrs, meta = run_case(case, tmp)
+            hashes[key(case)] = {
+                "dims": list(case[:3]), "max_iter": case[3], "tol_mode": case[4], "tol": case[5],
+                "num_iters": meta["num_iters"], "normr": meta["normr"], "verify": meta["verify"],
+                "nrows": meta["nrows"], "nnz": meta["nnz"],
+                "sha256": {n: hashlib.sha256(a.tobytes()).hexdigest() for n, a in arrs.items()},
+                "x_l2": float(np.linalg.norm(arrs["x"])),
+            }
+        d = os.path.join(tmp, "elem")
+        os.makedirs(d)
+        subprocess.run([HARNESS, "element", d], check=True)
+        out["element/ref_elem_mat"] = np.fromfile(os.path.join(d, "elem_mat.f64"), np.float64)
+        out["element/ref_elem_vec"] = np.fromfile(os.path.join(d, "elem_vec.f64"), np.float64)
+        out["element/ref_grad_vals"] = np.fromfile(os.path.join(d, "grad_vals.f64"), np.float64)
+    out["element/utest_elem_mat"] = utest_known_answer()
+    np.savez_compressed(os.path.join(HERE, "minife_golden.npz"), **out)
+    with open(os.path.join(HERE, "golden_hashes.json"), "w") as f:
+        json.dump(hashes, f, indent=1, sort_keys=True)
+    print("wrote", len(out), "arrays and", len(hashes), "hashed cases")
+
+
+if __name__ == "__main__":
+    main()

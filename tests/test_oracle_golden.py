@@ -1,0 +1,103 @@
+"""Pin the oracle (CPU restatement) to the reference's own outputs.
+
+The fixtures under tests/golden/ were produced by the unmodified reference
+(ref/ variant) through oracle/ref_harness.cpp; see tests/golden/gen_golden.py.
+Every array must agree bit for bit: the restatement follows the reference's
+floating-point operation order exactly.
+"""
+import hashlib
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+FULL = ["1x1x2_mode0", "2x2x2_mode0", "4x5x6_mode0", "17x3x5_mode0", "10x10x10_mode0",
+        "10x10x10_mode1", "7x9x4_mode1"]
+
+
+def _dims(key):
+    d = key.split("_")[0]
+    return tuple(int(v) for v in d.split("x"))
+
+
+def _bits_equal(a, b):
+    return a.shape == b.shape and np.array_equal(a.view(np.int64), b.view(np.int64))
+
+
+@pytest.mark.parametrize("key", FULL)
+def test_structure_assembly_bc_bitexact(golden, key):
+    nx, ny, nz = _dims(key)
+    ro, cols, vals, b = O.assemble(nx, ny, nz)
+    assert np.array_equal(ro, golden[key + "/row_offsets"])
+    assert np.array_equal(cols, golden[key + "/cols"])
+    assert _bits_equal(vals, golden[key + "/vals_prebc"])
+    assert _bits_equal(b, golden[key + "/b_prebc"])
+    ro, cols, vals, b = O.build_system(nx, ny, nz)
+    assert _bits_equal(vals, golden[key + "/vals"])
+    assert _bits_equal(b, golden[key + "/b"])
+
+
+@pytest.mark.parametrize("key", FULL)
+def test_cg_bitexact(golden, key):
+    nx, ny, nz = _dims(key)
+    meta = golden[key + "/meta"]
+    num_iters, normr, verify, abs_tol, max_iter, mode, tol = meta
+    ro, cols, vals, b = O.build_system(nx, ny, nz)
+    x, it, nr, st = O.cg_solve(ro, cols, vals, b, max_iter=int(max_iter), tol=tol,
+                               tol_mode=int(mode))
+    # st == 1 (breakdown) happens when the residual is already exactly zero
+    # (e.g. 1x1x2: every node is a boundary node); the reference then prints
+    # its breakdown message and returns the same iterate
+    assert st == 0 or nr == 0.0
+    assert it == int(num_iters)
+    assert nr == normr
+    assert _bits_equal(x, golden[key + "/x"])
+    rc, err = O.verify_solution(nx, ny, nz, x)
+    assert rc == int(verify)
+
+
+def test_hashed_cases(golden_hashes):
+    for key, h in golden_hashes.items():
+        nx, ny, nz = h["dims"]
+        ro, cols, vals, b = O.build_system(nx, ny, nz)
+        assert ro.size - 1 == h["nrows"] and cols.size == h["nnz"]
+        sha = lambda a: hashlib.sha256(a.tobytes()).hexdigest()
+        assert sha(ro) == h["sha256"]["row_offsets"], key
+        assert sha(cols) == h["sha256"]["cols"], key
+        assert sha(vals) == h["sha256"]["vals"], key
+        assert sha(b) == h["sha256"]["b"], key
+        x, it, nr, st = O.cg_solve(ro, cols, vals, b, max_iter=h["max_iter"], tol=h["tol"],
+                                   tol_mode=h["tol_mode"])
+        assert it == h["num_iters"], key
+        assert sha(x) == h["sha256"]["x"], key
+
+
+def test_element_known_answers(golden):
+    """Unit cube at the origin: ref/src element math, bit for bit, and the
+    legacy unit test's pasted values (ref/basic/utest_cases.hpp:233-317).
+
+    The legacy matrix was pasted from the older basic/ element code, whose
+    diffusion matrix is that of ref/src for an element of side 2 (stiffness
+    scales with h); its source vector is that of the unit cube.  Both are
+    compared with the legacy test's own tolerances (1e-6, 1e-13)."""
+    coords = np.array([0, 0, 0, 1, 0, 0, 1, 1, 0, 0, 1, 0, 0, 0, 1, 1, 0, 1, 1, 1, 1, 0, 1, 1],
+                      np.float64)
+    em, ev = O.element_matrix(coords)
+    assert _bits_equal(em, golden["element/ref_elem_mat"])
+    assert _bits_equal(ev, golden["element/ref_elem_vec"])
+    assert _bits_equal(O.gradient_values(), golden["element/ref_grad_vals"])
+    em2, _ = O.element_matrix(2.0 * coords)
+    assert np.max(np.abs(em2 - golden["element/utest_elem_mat"])) < 1e-6
+    assert np.max(np.abs(ev - 0.125)) < 1e-13
+
+
+def test_row_lengths_and_counts():
+    for dims in [(1, 1, 1), (3, 4, 5), (30, 30, 30)]:
+        n, nnz = O.dims_rows_nnz(*dims)
+        Nx, Ny, Nz = (d + 1 for d in dims)
+        assert n == Nx * Ny * Nz
+        assert nnz == (3 * Nx - 2) * (3 * Ny - 2) * (3 * Nz - 2)
+        ro, cols = O.structure(*dims)
+        lens = np.diff(ro)
+        assert set(np.unique(lens)) <= {8, 12, 18, 27}
