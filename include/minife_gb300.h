@@ -1,0 +1,283 @@
+/*
+ * minife_gb300 -- C ABI of the GB300 (sm_103a) implementation of miniFE's
+ * assemble-and-solve path.
+ *
+ * The reference (Mantevo miniFE, ref/ variant) binds this path at compile time
+ * through C++ templates: cg_solve takes the matvec as a functor argument and
+ * the CSRMatrix / Vector types by macro.  This header is the drop-in boundary
+ * for that path as plain C: every entry point takes POD structs, raw pointers
+ * and sizes, runs hand-written CUDA kernels on one GPU, and returns an
+ * mfe_status.  Each declaration names the reference interface it replaces
+ * (file:line in the reference repository).  There is no CPU fallback: a call
+ * without a usable GPU returns MFE_CUDA_ERR.
+ *
+ * Conventions
+ *  - "device" pointers are CUDA device addresses (cudaMalloc, or the data
+ *    pointer of a CUDA tensor); "host" pointers are ordinary host memory
+ *    (pinned memory gives the fastest copies).
+ *  - One context = one CUDA stream on one device.  Calls on one context are
+ *    ordered on its stream; a context is not thread-safe, distinct contexts
+ *    are independent.  Entry points that return a value to the host
+ *    (mfe_dot, mfe_cg_solve) synchronise the stream before returning.
+ *  - Indices are 32-bit like the reference's LocalOrdinal/GlobalOrdinal = int
+ *    (ref/src/Makefile:3-6); boxes whose nonzero count reaches 2^31 are
+ *    rejected with MFE_BAD_ARG.
+ */
+#ifndef MINIFE_GB300_H
+#define MINIFE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MFE_ABI_VERSION 1
+
+typedef enum mfe_status {
+  MFE_OK = 0,
+  MFE_BAD_ARG = 1,       /* invalid dimensions, null pointers, size overflow */
+  MFE_OOM = 2,           /* device allocation failed */
+  MFE_CUDA_ERR = 3,      /* CUDA runtime error (no device, launch failure) */
+  MFE_BREAKDOWN = 4,     /* CG breakdown test fired (cg_solve.hpp:186-198) */
+  MFE_MAXITER = 5,       /* returned by the refinement solver only: the target
+                            residual was not reached within its limits */
+  MFE_TIMEOUT = 6,       /* a bounded device-side wait gave up */
+  MFE_NOT_SUPPORTED = 7  /* valid request the library does not implement */
+} mfe_status;
+
+typedef enum mfe_dtype { MFE_F64 = 0, MFE_F32 = 1 } mfe_dtype;
+
+typedef struct mfe_ctx mfe_ctx;
+
+/* CSR matrix in device memory, one rank: row i of the reference's
+ * CSRMatrix (ref/src/CSRMatrix.hpp:43-129) with rows[i] == i,
+ * row_offsets == CSRMatrix::row_offsets, cols == packed_cols,
+ * vals == packed_coefs (double for MFE_F64, float for MFE_F32). */
+typedef struct mfe_csr {
+  int64_t nrows;
+  int64_t ncols;
+  int64_t nnz;
+  int32_t* row_offsets; /* device, nrows + 1 */
+  int32_t* cols;        /* device, nnz */
+  void* vals;           /* device, nnz of dtype */
+  int32_t dtype;        /* mfe_dtype */
+  int32_t max_row_len;  /* 0 = unknown (computed on first use) */
+  /* box the matrix was assembled on (0 if not an assembled box); lets the
+   * solver use the 27-point stencil layout of those rows */
+  int32_t box_nx, box_ny, box_nz;
+  int32_t owned;        /* 1 if allocated by mfe_csr_alloc */
+} mfe_csr;
+
+/* ------------------------------------------------------------------ */
+/* context, memory, errors                                             */
+/* ------------------------------------------------------------------ */
+int mfe_abi_version(void);
+mfe_status mfe_ctx_create(int device, mfe_ctx** out);
+mfe_status mfe_ctx_destroy(mfe_ctx* ctx);
+/* Run this context's work on an existing CUDA stream (cudaStream_t); NULL
+ * restores the context's own stream. */
+mfe_status mfe_set_stream(mfe_ctx* ctx, void* stream);
+mfe_status mfe_synchronize(mfe_ctx* ctx);
+const char* mfe_last_error_string(const mfe_ctx* ctx);
+const char* mfe_status_string(mfe_status s);
+/* Number of SMs of the context's device (the grid-size unit). */
+int mfe_device_sm_count(const mfe_ctx* ctx);
+
+mfe_status mfe_device_alloc(mfe_ctx* ctx, size_t bytes, void** out);
+mfe_status mfe_device_free(mfe_ctx* ctx, void* ptr);
+mfe_status mfe_memcpy_h2d(mfe_ctx* ctx, void* dst, const void* src, size_t bytes);
+mfe_status mfe_memcpy_d2h(mfe_ctx* ctx, void* dst, const void* src, size_t bytes);
+
+/* Allocate device arrays for an nrows x nrows CSR with nnz nonzeros. */
+mfe_status mfe_csr_alloc(mfe_ctx* ctx, int64_t nrows, int64_t nnz, mfe_dtype dtype,
+                         mfe_csr* out);
+mfe_status mfe_csr_free(mfe_ctx* ctx, mfe_csr* A);
+
+/* ------------------------------------------------------------------ */
+/* mesh, structure, assembly, boundary conditions                      */
+/* ------------------------------------------------------------------ */
+
+/* Rows and nonzeros of the nx x ny x nz element box (nodes = elements + 1
+ * per dimension, 27-point rows): the sizes generate_matrix_structure
+ * reserves (ref/src/generate_matrix_structure.hpp:63-130). */
+mfe_status mfe_box_dims(int nx, int ny, int nz, int64_t* nrows, int64_t* nnz);
+
+/* generate_matrix_structure + MatrixInitOp<CSR>
+ * (ref/src/generate_matrix_structure.hpp:47-149, MatrixInitOp.hpp:127-156):
+ * fills A->row_offsets and A->cols (ascending 27-point columns) and zeroes
+ * A->vals.  A must be allocated for mfe_box_dims rows/nonzeros. */
+mfe_status mfe_generate_structure(mfe_ctx* ctx, int nx, int ny, int nz, mfe_csr* A);
+
+/* assemble_FE_data -> perform_element_loop -> sum_into_global_linear_system
+ * (ref/src/assemble_FE_data.hpp:38-73, perform_element_loop.hpp:40-104,
+ * SparseMatrix_functions.hpp:183-255): structure, Hex8 element matrices and
+ * source vectors (ref/fem/Hex8.hpp:260-410), summed per coefficient in
+ * ascending element order, so values match the reference bit for bit.
+ * kappa (device, nullable): one conductivity per element in element-id order
+ * replacing the constant k = 1.0 of Hex8.hpp:273; NULL = the reference.
+ * impose_bc != 0 also applies both impose_dirichlet passes of
+ * driver.hpp:214-218 (value 0 on faces x=0,y=0,z=0,y=1,z=1, then value 1 on
+ * face x=1), fused into the same kernel.  b (device, nrows doubles) is
+ * overwritten.  A->dtype must be MFE_F64. */
+mfe_status mfe_assemble(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,
+                        mfe_csr* A, double* b, int impose_bc);
+
+/* impose_dirichlet (ref/src/SparseMatrix_functions.hpp:434-480) for an
+ * arbitrary CSR: bc_rows (device, sorted ascending, n_bc entries) replaces
+ * the std::set.  Rows in the set become identity rows with b = value; every
+ * other row moves value * (its coefficients in bc columns) to b and zeroes
+ * those coefficients, keeping them as explicit zeros. */
+mfe_status mfe_impose_dirichlet(mfe_ctx* ctx, mfe_csr* A, double* b, double value,
+                                const int32_t* bc_rows, int64_t n_bc);
+
+/* The boundary row sets of simple_mesh_description
+ * (ref/src/simple_mesh_description.hpp:62-224) as ascending device arrays:
+ * set 0 (faces x=0,y=0,z=0,y=1,z=1) or set 1 (face x=1).  count_out
+ * receives the size; rows may be NULL to query the size only. */
+mfe_status mfe_box_bc_rows(mfe_ctx* ctx, int nx, int ny, int nz, int which,
+                           int32_t* rows, int64_t* count_out);
+
+/* Convert the values of an FP64 CSR into an FP32 copy sharing its structure
+ * (dst->row_offsets/cols may alias src's). */
+mfe_status mfe_csr_convert_f32(mfe_ctx* ctx, const mfe_csr* src, mfe_csr* dst);
+
+/* ------------------------------------------------------------------ */
+/* kernels: matvec, dot, waxpby                                        */
+/* ------------------------------------------------------------------ */
+
+/* matvec_std<CSR>::operator() (ref/src/SparseMatrix_functions.hpp:545-578):
+ * y = A x.  x and y have A->dtype. */
+mfe_status mfe_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y);
+
+/* matvec_and_dot (ref/src/SparseMatrix_functions.hpp:491-536): y = A x and
+ * *result = x . y (double, host), accumulated in FP64. */
+mfe_status mfe_matvec_and_dot(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
+                              double* result);
+
+/* dot (ref/src/Vector_functions.hpp:194-226): *result (host) = x . y. */
+mfe_status mfe_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
+                   double* result);
+
+/* waxpby (ref/src/Vector_functions.hpp:127-150): w = alpha x + beta y. */
+mfe_status mfe_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x,
+                      double beta, const double* y, double* w);
+
+/* fused_waxpby (ref/src/Vector_functions.hpp:154-185). */
+mfe_status mfe_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x,
+                            double beta, const double* y, double* w, double alpha2,
+                            const double* x2, double beta2, const double* y2, double* w2);
+
+/* ------------------------------------------------------------------ */
+/* CG                                                                  */
+/* ------------------------------------------------------------------ */
+typedef enum mfe_precision {
+  MFE_PREC_F64 = 0,   /* the reference's FP64 CG */
+  MFE_PREC_MIXED = 1  /* FP32 inner CG (FP32 matrix and vectors, FP64 dots)
+                         inside FP64 iterative refinement */
+} mfe_precision;
+
+typedef enum mfe_tol_mode {
+  MFE_TOL_ABSOLUTE = 0, /* the reference's test normr > tol (cg_solve.hpp:152) */
+  MFE_TOL_RELATIVE = 1  /* normr > tol * ||b - A x0|| */
+} mfe_tol_mode;
+
+typedef struct mfe_cg_opts {
+  int32_t max_iter;     /* reference: 200 (driver.hpp:241) */
+  int32_t tol_mode;     /* mfe_tol_mode */
+  double tol;           /* reference: DBL_EPSILON absolute (driver.hpp:245) */
+  int32_t precision;    /* mfe_precision */
+  int32_t refine_k;     /* mixed: max inner iterations per refinement sweep
+                           (0 = library default) */
+  double inner_tol;     /* mixed: inner relative reduction per sweep (0 = default) */
+  int32_t max_refine;   /* mixed: max refinement sweeps (0 = default) */
+  int32_t record_history; /* 1: keep normr of every iteration (see
+                             mfe_cg_history) */
+  const mfe_csr* A32;   /* mixed: optional prepared FP32 copy of A (NULL: the
+                           library converts and caches one) */
+} mfe_cg_opts;
+
+/* Fill opts with the reference's defaults (max_iter 200, absolute tol
+ * DBL_EPSILON, FP64). */
+void mfe_cg_opts_default(mfe_cg_opts* opts);
+
+typedef struct mfe_cg_result {
+  int32_t num_iters;    /* cg_solve's num_iters (total inner iterations for
+                           the mixed solver) */
+  int32_t status;       /* mfe_status of the solve */
+  double normr;         /* cg_solve's normr: residual norm at the top of the
+                           last iteration (FP64 true residual for mixed) */
+  double normr0;        /* initial residual norm */
+  double final_resid;   /* ||b - A x|| of the returned x, FP64 */
+  double times[5];      /* seconds: WAXPY, DOT, MATVEC, MATVECDOT, TOTAL
+                           (mytimer.hpp:37-43 order); fused kernels are
+                           accounted to MATVECDOT and WAXPY */
+  int32_t refinements;  /* mixed: outer refinement sweeps */
+  int32_t fp64_spmvs;   /* number of FP64 matvecs performed */
+} mfe_cg_result;
+
+/* cg_solve (ref/src/cg_solve.hpp:69-229) with matvec_std: solves A x = b
+ * from the initial guess in x (device).  FP64 precision follows the
+ * reference's loop exactly (x0 copied to p, r = b - A p, then per iteration
+ * p update, A p, p.Ap, breakdown test, x and r updates); the loop runs on the
+ * device inside one CUDA graph (a conditional while node), with no host
+ * round trip per iteration. */
+mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
+                        const mfe_cg_opts* opts, mfe_cg_result* result);
+
+/* Drop-in for the reference's host-side call: CSR and vectors in HOST
+ * memory (CSRMatrix/Vector storage), copied to the device, solved with
+ * mfe_cg_solve, and x copied back. */
+mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz,
+                             const int32_t* row_offsets, const int32_t* cols,
+                             const double* vals, const double* b, double* x,
+                             const mfe_cg_opts* opts, mfe_cg_result* result);
+
+/* History of normr recorded by the last mfe_cg_solve on ctx with
+ * record_history = 1: up to cap values (host), index 0 = initial residual. */
+mfe_status mfe_cg_history(mfe_ctx* ctx, double* out, int32_t cap, int32_t* count);
+
+/* ------------------------------------------------------------------ */
+/* verification, adjoint, batching                                     */
+/* ------------------------------------------------------------------ */
+
+/* verify_solution (ref/fem/verify_solution.hpp:55-174, analytic_soln.hpp):
+ * max |x - analytic| over nodes within 0.05 of the centre (all nodes when
+ * whole_domain), 300 x 300 series terms, evaluated on the device.
+ * *passed = max_err <= tolerance. */
+mfe_status mfe_verify_solution(mfe_ctx* ctx, int nx, int ny, int nz, const double* x,
+                               double tolerance, int whole_domain, double* max_err,
+                               int* passed);
+
+/* Adjoint contraction for per-element conductivity (extension of
+ * Hex8.hpp:273): g[e] = -lambda_e^T Khat_e u_e, Khat_e the k = 1 element
+ * matrix of element e, u and lambda nodal (device), g per element (device). */
+mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
+                                const double* lambda, double* g);
+
+/* Multi-RHS: Y = A X for nrhs column vectors stored row-major (X[i*nrhs + j]),
+ * reading A once per product.  FP64 or FP32 by A->dtype (X, Y same type). */
+mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X, void* Y);
+
+/* Multi-RHS CG on one matrix: nrhs independent CG solves (each with its own
+ * alpha/beta and stopping test) advanced together so every iteration reads A
+ * once.  B, X row-major (i*nrhs + j), device, FP64; opts as for mfe_cg_solve
+ * (FP64 or MIXED).  results: nrhs entries (host). */
+mfe_status mfe_cg_solve_multi(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const double* B,
+                              double* X, const mfe_cg_opts* opts, mfe_cg_result* results);
+
+/* Batched uneven boxes: nbox independent miniFE problems (dims[3*i..3*i+2]),
+ * each assembled (k = 1, reference BCs) and solved with CG in one persistent
+ * launch per iteration block, all boxes advancing together.  x_out (device)
+ * receives the concatenated solutions (offsets: prefix sums of the boxes'
+ * rows); results: nbox entries (host). */
+mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims,
+                                 const mfe_cg_opts* opts, double* x_out,
+                                 mfe_cg_result* results);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* MINIFE_GB300_H */

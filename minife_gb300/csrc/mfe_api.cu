@@ -1,0 +1,573 @@
+// C ABI entry points (include/minife_gb300.h): context, memory, argument
+// checking, and dispatch to the kernels of mfe_assemble.cu, mfe_spmv.cu and
+// mfe_cg.cu.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mfe_internal.h"
+
+namespace mfe {
+
+mfe_status fail(mfe_ctx* ctx, mfe_status st, const std::string& msg)
+{
+  if (ctx) ctx->err = msg;
+  return st;
+}
+
+mfe_status cuda_fail(mfe_ctx* ctx, cudaError_t e, const char* where)
+{
+  std::string m = std::string(where) + ": " + cudaGetErrorString(e);
+  if (e == cudaErrorMemoryAllocation) return fail(ctx, MFE_OOM, m);
+  return fail(ctx, MFE_CUDA_ERR, m);
+}
+
+mfe_status check_launch(mfe_ctx* ctx, const char* where)
+{
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_fail(ctx, e, where);
+  return MFE_OK;
+}
+
+void* workspace(mfe_ctx* ctx, const char* name, size_t bytes)
+{
+  mfe_ctx::Buf& b = ctx->ws[name];
+  if (b.bytes >= bytes && b.ptr) return b.ptr;
+  if (b.ptr) {
+    // the old buffer may still be in use by queued work
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+  }
+  void* p = nullptr;
+  if (cudaMalloc(&p, std::max<size_t>(bytes, 256)) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  b.ptr = p;
+  b.bytes = std::max<size_t>(bytes, 256);
+  return p;
+}
+
+void* host_scratch(mfe_ctx* ctx, size_t bytes)
+{
+  if (ctx->host_scratch_bytes >= bytes) return ctx->host_scratch;
+  if (ctx->host_scratch) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFreeHost(ctx->host_scratch);
+  }
+  ctx->host_scratch = nullptr;
+  ctx->host_scratch_bytes = 0;
+  const size_t sz = std::max<size_t>(bytes, 4096);
+  if (cudaMallocHost(&ctx->host_scratch, sz) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  ctx->host_scratch_bytes = sz;
+  return ctx->host_scratch;
+}
+
+static mfe_status set_device(mfe_ctx* ctx)
+{
+  MFE_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  return MFE_OK;
+}
+
+static bool box_ok(int nx, int ny, int nz)
+{
+  if (nx < 1 || ny < 1 || nz < 1) return false;
+  return box_nnz(nx, ny, nz) < ((int64_t)1 << 31);
+}
+
+static mfe_status check_csr(mfe_ctx* ctx, const mfe_csr* A)
+{
+  if (!A) return fail(ctx, MFE_BAD_ARG, "null matrix");
+  if (A->nrows < 0 || A->nnz < 0 || A->nnz >= ((int64_t)1 << 31) || A->nrows >= ((int64_t)1 << 31))
+    return fail(ctx, MFE_BAD_ARG, "matrix sizes out of range for 32-bit indices");
+  if (A->nrows > 0 && (!A->row_offsets || (A->nnz > 0 && (!A->cols || !A->vals))))
+    return fail(ctx, MFE_BAD_ARG, "null matrix array");
+  if (A->dtype != MFE_F64 && A->dtype != MFE_F32) return fail(ctx, MFE_BAD_ARG, "bad dtype");
+  return MFE_OK;
+}
+
+}  // namespace mfe
+
+using namespace mfe;
+
+extern "C" {
+
+int mfe_abi_version(void) { return MFE_ABI_VERSION; }
+
+const char* mfe_status_string(mfe_status s)
+{
+  switch (s) {
+    case MFE_OK: return "ok";
+    case MFE_BAD_ARG: return "bad argument";
+    case MFE_OOM: return "out of device memory";
+    case MFE_CUDA_ERR: return "CUDA error";
+    case MFE_BREAKDOWN: return "numerical breakdown";
+    case MFE_MAXITER: return "iteration limit reached";
+    case MFE_TIMEOUT: return "device wait timed out";
+    case MFE_NOT_SUPPORTED: return "not supported";
+  }
+  return "unknown status";
+}
+
+mfe_status mfe_ctx_create(int device, mfe_ctx** out)
+{
+  if (!out) return MFE_BAD_ARG;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count == 0) {
+    cudaGetLastError();
+    return MFE_CUDA_ERR;
+  }
+  if (device < 0 || device >= count) return MFE_BAD_ARG;
+  mfe_ctx* ctx = new mfe_ctx();
+  ctx->device = device;
+  if (cudaSetDevice(device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, device) !=
+          cudaSuccess ||
+      cudaStreamCreateWithFlags(&ctx->own_stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess) {
+    cudaGetLastError();
+    delete ctx;
+    return MFE_CUDA_ERR;
+  }
+  ctx->stream = ctx->own_stream;
+  *out = ctx;
+  return MFE_OK;
+}
+
+mfe_status mfe_ctx_destroy(mfe_ctx* ctx)
+{
+  if (!ctx) return MFE_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  cg_graph_destroy(ctx->cg_graph);
+  for (auto& kv : ctx->ws)
+    if (kv.second.ptr) cudaFree(kv.second.ptr);
+  if (ctx->f32_copy.owned) {
+    cudaFree(ctx->f32_copy.vals);
+  }
+  if (ctx->host_scratch) cudaFreeHost(ctx->host_scratch);
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
+  delete ctx;
+  return MFE_OK;
+}
+
+mfe_status mfe_set_stream(mfe_ctx* ctx, void* stream)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
+  if (s != ctx->stream) {
+    cudaStreamSynchronize(ctx->stream);
+    ctx->stream = s;
+  }
+  return MFE_OK;
+}
+
+mfe_status mfe_synchronize(mfe_ctx* ctx)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return MFE_OK;
+}
+
+const char* mfe_last_error_string(const mfe_ctx* ctx)
+{
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+int mfe_device_sm_count(const mfe_ctx* ctx) { return ctx ? ctx->sm_count : 0; }
+
+mfe_status mfe_device_alloc(mfe_ctx* ctx, size_t bytes, void** out)
+{
+  if (!ctx || !out) return MFE_BAD_ARG;
+  MFE_TRY(set_device(ctx));
+  *out = nullptr;
+  MFE_CUDA_TRY(ctx, cudaMalloc(out, std::max<size_t>(bytes, 16)));
+  return MFE_OK;
+}
+
+mfe_status mfe_device_free(mfe_ctx* ctx, void* ptr)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  if (!ptr) return MFE_OK;
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaFree(ptr));
+  return MFE_OK;
+}
+
+mfe_status mfe_memcpy_h2d(mfe_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+  if (!ctx || (bytes && (!dst || !src))) return MFE_BAD_ARG;
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, ctx->stream));
+  return MFE_OK;
+}
+
+mfe_status mfe_memcpy_d2h(mfe_ctx* ctx, void* dst, const void* src, size_t bytes)
+{
+  if (!ctx || (bytes && (!dst || !src))) return MFE_BAD_ARG;
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return MFE_OK;
+}
+
+mfe_status mfe_csr_alloc(mfe_ctx* ctx, int64_t nrows, int64_t nnz, mfe_dtype dtype, mfe_csr* out)
+{
+  if (!ctx || !out || nrows < 0 || nnz < 0 || nnz >= ((int64_t)1 << 31) ||
+      (dtype != MFE_F64 && dtype != MFE_F32))
+    return fail(ctx, MFE_BAD_ARG, "mfe_csr_alloc: bad arguments");
+  MFE_TRY(set_device(ctx));
+  memset(out, 0, sizeof(*out));
+  const size_t vb = dtype == MFE_F64 ? 8 : 4;
+  void *ro = nullptr, *cols = nullptr, *vals = nullptr;
+  // values and columns are padded to a 16-byte multiple (bulk-copy granule)
+  if (cudaMalloc(&ro, sizeof(int32_t) * (size_t)(nrows + 1)) != cudaSuccess ||
+      cudaMalloc(&cols, sizeof(int32_t) * (size_t)(nnz + 4)) != cudaSuccess ||
+      cudaMalloc(&vals, vb * (size_t)(nnz + 4)) != cudaSuccess) {
+    cudaGetLastError();
+    if (ro) cudaFree(ro);
+    if (cols) cudaFree(cols);
+    if (vals) cudaFree(vals);
+    return fail(ctx, MFE_OOM, "mfe_csr_alloc: device allocation failed");
+  }
+  out->nrows = nrows;
+  out->ncols = nrows;
+  out->nnz = nnz;
+  out->row_offsets = static_cast<int32_t*>(ro);
+  out->cols = static_cast<int32_t*>(cols);
+  out->vals = vals;
+  out->dtype = dtype;
+  out->owned = 1;
+  return MFE_OK;
+}
+
+mfe_status mfe_csr_free(mfe_ctx* ctx, mfe_csr* A)
+{
+  if (!ctx || !A) return MFE_BAD_ARG;
+  if (!A->owned) return fail(ctx, MFE_BAD_ARG, "matrix was not allocated by mfe_csr_alloc");
+  cudaStreamSynchronize(ctx->stream);
+  if (A->row_offsets) cudaFree(A->row_offsets);
+  if (A->cols) cudaFree(A->cols);
+  if (A->vals) cudaFree(A->vals);
+  if (ctx->f32_src_vals == A->vals) ctx->f32_src_vals = nullptr;
+  memset(A, 0, sizeof(*A));
+  return MFE_OK;
+}
+
+mfe_status mfe_box_dims(int nx, int ny, int nz, int64_t* nrows, int64_t* nnz)
+{
+  if (!box_ok(nx, ny, nz)) return MFE_BAD_ARG;
+  if (nrows) *nrows = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+  if (nnz) *nnz = box_nnz(nx, ny, nz);
+  return MFE_OK;
+}
+
+static mfe_status check_box_matrix(mfe_ctx* ctx, int nx, int ny, int nz, const mfe_csr* A)
+{
+  if (!box_ok(nx, ny, nz)) return fail(ctx, MFE_BAD_ARG, "box dimensions must be >= 1 and give < 2^31 nonzeros");
+  MFE_TRY(check_csr(ctx, A));
+  int64_t n, nnz;
+  mfe_box_dims(nx, ny, nz, &n, &nnz);
+  if (A->nrows != n || A->nnz != nnz)
+    return fail(ctx, MFE_BAD_ARG, "matrix is not sized for this box (see mfe_box_dims)");
+  return MFE_OK;
+}
+
+mfe_status mfe_generate_structure(mfe_ctx* ctx, int nx, int ny, int nz, mfe_csr* A)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_box_matrix(ctx, nx, ny, nz, A));
+  MFE_TRY(set_device(ctx));
+  MFE_TRY(launch_structure(ctx, nx, ny, nz, A->row_offsets, A->cols));
+  const size_t vb = A->dtype == MFE_F64 ? 8 : 4;
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(A->vals, 0, vb * (size_t)A->nnz, ctx->stream));
+  A->max_row_len = 27;  // upper bound of the 27-point rows
+  A->box_nx = nx;
+  A->box_ny = ny;
+  A->box_nz = nz;
+  return MFE_OK;
+}
+
+mfe_status mfe_assemble(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa, mfe_csr* A,
+                        double* b, int impose_bc)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_box_matrix(ctx, nx, ny, nz, A));
+  if (A->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "assembly needs an FP64 matrix");
+  if (!b) return fail(ctx, MFE_BAD_ARG, "null b");
+  MFE_TRY(set_device(ctx));
+  MFE_TRY(launch_structure(ctx, nx, ny, nz, A->row_offsets, A->cols));
+  MFE_TRY(launch_assemble(ctx, nx, ny, nz, kappa, A->row_offsets, static_cast<double*>(A->vals),
+                          b, impose_bc));
+  A->max_row_len = 27;  // upper bound of the 27-point rows
+  A->box_nx = nx;
+  A->box_ny = ny;
+  A->box_nz = nz;
+  return MFE_OK;
+}
+
+mfe_status mfe_impose_dirichlet(mfe_ctx* ctx, mfe_csr* A, double* b, double value,
+                                const int32_t* bc_rows, int64_t n_bc)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, A));
+  if (A->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "impose_dirichlet needs an FP64 matrix");
+  if (!b || n_bc < 0 || (n_bc > 0 && !bc_rows)) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  return launch_impose_dirichlet(ctx, A, b, value, bc_rows, n_bc);
+}
+
+mfe_status mfe_box_bc_rows(mfe_ctx* ctx, int nx, int ny, int nz, int which, int32_t* rows,
+                           int64_t* count_out)
+{
+  if (!ctx || !count_out || (which != 0 && which != 1)) return MFE_BAD_ARG;
+  if (!box_ok(nx, ny, nz)) return fail(ctx, MFE_BAD_ARG, "bad box");
+  const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
+  // simple_mesh_description.hpp:62-224 on one rank, ascending (std::set order)
+  std::vector<int32_t> v;
+  for (int iz = 0; iz < Nz; ++iz)
+    for (int iy = 0; iy < Ny; ++iy)
+      for (int ix = 0; ix < Nx; ++ix) {
+        const bool in = which == 1 ? (ix == Nx - 1)
+                                   : (ix == 0 || iy == 0 || iz == 0 || iy == Ny - 1 || iz == Nz - 1);
+        if (in) v.push_back((int32_t)(ix + (int64_t)Nx * (iy + (int64_t)Ny * iz)));
+      }
+  *count_out = (int64_t)v.size();
+  if (rows && !v.empty()) {
+    MFE_TRY(set_device(ctx));
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(rows, v.data(), sizeof(int32_t) * v.size(),
+                                      cudaMemcpyHostToDevice, ctx->stream));
+    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  }
+  return MFE_OK;
+}
+
+mfe_status mfe_csr_convert_f32(mfe_ctx* ctx, const mfe_csr* src, mfe_csr* dst)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, src));
+  if (!dst || src->dtype != MFE_F64 || dst->dtype != MFE_F32 || dst->nnz != src->nnz ||
+      dst->nrows != src->nrows || !dst->vals)
+    return fail(ctx, MFE_BAD_ARG, "mfe_csr_convert_f32: dst must be an FP32 CSR of src's size");
+  MFE_TRY(set_device(ctx));
+  if (dst->row_offsets != src->row_offsets)
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst->row_offsets, src->row_offsets,
+                                      sizeof(int32_t) * (size_t)(src->nrows + 1),
+                                      cudaMemcpyDeviceToDevice, ctx->stream));
+  if (dst->cols != src->cols)
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst->cols, src->cols, sizeof(int32_t) * (size_t)src->nnz,
+                                      cudaMemcpyDeviceToDevice, ctx->stream));
+  dst->max_row_len = src->max_row_len;
+  dst->box_nx = src->box_nx;
+  dst->box_ny = src->box_ny;
+  dst->box_nz = src->box_nz;
+  return launch_convert_f32(ctx, static_cast<const double*>(src->vals),
+                            static_cast<float*>(dst->vals), src->nnz);
+}
+
+mfe_status mfe_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, A));
+  if (A->nrows > 0 && (!x || !y)) return fail(ctx, MFE_BAD_ARG, "null vector");
+  MFE_TRY(set_device(ctx));
+  return launch_spmv(ctx, A, x, y, nullptr, nullptr, nullptr);
+}
+
+static double* dev_scalar(mfe_ctx* ctx)
+{
+  return static_cast<double*>(workspace(ctx, "api.scalar", sizeof(double) * 4));
+}
+
+static mfe_status read_scalar(mfe_ctx* ctx, const double* d, double* out)
+{
+  double* h = static_cast<double*>(host_scratch(ctx, sizeof(double)));
+  if (!h) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(h, d, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  *out = *h;
+  return MFE_OK;
+}
+
+mfe_status mfe_matvec_and_dot(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
+                              double* result)
+{
+  if (!ctx || !result) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, A));
+  if (A->nrows > 0 && (!x || !y)) return fail(ctx, MFE_BAD_ARG, "null vector");
+  MFE_TRY(set_device(ctx));
+  if (A->nrows == 0) {
+    *result = 0.0;
+    return MFE_OK;
+  }
+  double* d = dev_scalar(ctx);
+  double* partials = static_cast<double*>(workspace(ctx, "api.partials", sizeof(double) * 8192));
+  const bool fresh = ctx->ws.find("api.ticket") == ctx->ws.end();
+  unsigned* ticket = static_cast<unsigned*>(workspace(ctx, "api.ticket", sizeof(unsigned)));
+  if (!d || !partials || !ticket) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  if (fresh) MFE_CUDA_TRY(ctx, cudaMemsetAsync(ticket, 0, sizeof(unsigned), ctx->stream));
+  DotSink sink;
+  sink.partials = partials;
+  sink.ticket = ticket;
+  sink.out = d;
+  MFE_TRY(launch_spmv(ctx, A, x, y, &sink, nullptr, nullptr));
+  return read_scalar(ctx, d, result);
+}
+
+mfe_status mfe_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y, double* result)
+{
+  if (!ctx || !result || n < 0 || (n > 0 && (!x || !y))) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  if (n == 0) {
+    *result = 0.0;
+    return MFE_OK;
+  }
+  double* d = dev_scalar(ctx);
+  if (!d) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  MFE_TRY(launch_dot(ctx, n, x, y, d));
+  return read_scalar(ctx, d, result);
+}
+
+mfe_status mfe_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
+                      const double* y, double* w)
+{
+  if (!ctx || n < 0 || (n > 0 && (!x || !y || !w))) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  return launch_waxpby(ctx, n, alpha, x, beta, y, w);
+}
+
+mfe_status mfe_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
+                            const double* y, double* w, double alpha2, const double* x2,
+                            double beta2, const double* y2, double* w2)
+{
+  MFE_TRY(mfe_waxpby(ctx, n, alpha, x, beta, y, w));
+  return mfe_waxpby(ctx, n, alpha2, x2, beta2, y2, w2);
+}
+
+void mfe_cg_opts_default(mfe_cg_opts* o)
+{
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->max_iter = 200;
+  o->tol_mode = MFE_TOL_ABSOLUTE;
+  o->tol = 2.220446049250313e-16;
+  o->precision = MFE_PREC_F64;
+}
+
+mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
+                        const mfe_cg_opts* opts, mfe_cg_result* result)
+{
+  if (!ctx || !result) return MFE_BAD_ARG;
+  memset(result, 0, sizeof(*result));
+  MFE_TRY(check_csr(ctx, A));
+  if (A->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "cg_solve needs the FP64 matrix");
+  if (A->nrows > 0 && (!b || !x)) return fail(ctx, MFE_BAD_ARG, "null vector");
+  mfe_cg_opts o;
+  if (opts) o = *opts;
+  else mfe_cg_opts_default(&o);
+  if (o.max_iter < 0 || !(o.tol >= 0.0) ||
+      (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED))
+    return fail(ctx, MFE_BAD_ARG, "bad CG options");
+  MFE_TRY(set_device(ctx));
+  if (A->nrows == 0) return MFE_OK;
+  mfe_status st = cg_solve_impl(ctx, A, b, x, &o, result);
+  result->status = st;
+  return st;
+}
+
+mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz, const int32_t* ro,
+                             const int32_t* cols, const double* vals, const double* b, double* x,
+                             const mfe_cg_opts* opts, mfe_cg_result* result)
+{
+  if (!ctx || !result || nrows < 0 || nnz < 0 || nnz >= ((int64_t)1 << 31) ||
+      (nrows > 0 && (!ro || !b || !x || (nnz > 0 && (!cols || !vals)))))
+    return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  mfe_csr A;
+  memset(&A, 0, sizeof(A));
+  A.nrows = nrows;
+  A.ncols = nrows;
+  A.nnz = nnz;
+  A.dtype = MFE_F64;
+  A.row_offsets = static_cast<int32_t*>(workspace(ctx, "host.ro", sizeof(int32_t) * (size_t)(nrows + 1)));
+  A.cols = static_cast<int32_t*>(workspace(ctx, "host.cols", sizeof(int32_t) * (size_t)(nnz + 4)));
+  A.vals = workspace(ctx, "host.vals", sizeof(double) * (size_t)(nnz + 4));
+  double* db = static_cast<double*>(workspace(ctx, "host.b", sizeof(double) * (size_t)std::max<int64_t>(nrows, 1)));
+  double* dx = static_cast<double*>(workspace(ctx, "host.x", sizeof(double) * (size_t)std::max<int64_t>(nrows, 1)));
+  if (!A.row_offsets || !A.cols || !A.vals || !db || !dx)
+    return fail(ctx, MFE_OOM, "device allocation for host operands failed");
+  cudaStream_t s = ctx->stream;
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.row_offsets, ro, sizeof(int32_t) * (size_t)(nrows + 1), cudaMemcpyHostToDevice, s));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.cols, cols, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
+  mfe_status st = mfe_cg_solve(ctx, &A, db, dx, opts, result);
+  if (st != MFE_OK && st != MFE_BREAKDOWN && st != MFE_MAXITER) return st;
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)nrows, cudaMemcpyDeviceToHost, s));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+  return st;
+}
+
+mfe_status mfe_cg_history(mfe_ctx* ctx, double* out, int32_t cap, int32_t* count)
+{
+  if (!ctx || !count) return MFE_BAD_ARG;
+  const int32_t n = (int32_t)ctx->history.size();
+  *count = n;
+  if (out) memcpy(out, ctx->history.data(), sizeof(double) * (size_t)std::min(n, std::max(cap, 0)));
+  return MFE_OK;
+}
+
+mfe_status mfe_verify_solution(mfe_ctx* ctx, int nx, int ny, int nz, const double* x,
+                               double tolerance, int whole_domain, double* max_err, int* passed)
+{
+  if (!ctx || !x || !max_err) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  if (!box_ok(nx, ny, nz)) return fail(ctx, MFE_BAD_ARG, "bad box");
+  MFE_TRY(set_device(ctx));
+  MFE_TRY(launch_verify(ctx, nx, ny, nz, x, whole_domain, max_err));
+  if (passed) *passed = *max_err <= tolerance ? 1 : 0;
+  return MFE_OK;
+}
+
+mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
+                                const double* lambda, double* g)
+{
+  if (!ctx || !u || !lambda || !g) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  if (!box_ok(nx, ny, nz)) return fail(ctx, MFE_BAD_ARG, "bad box");
+  MFE_TRY(set_device(ctx));
+  return launch_element_gradient(ctx, nx, ny, nz, u, lambda, g);
+}
+
+mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X, void* Y)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, A));
+  if (nrhs < 1 || (A->nrows > 0 && (!X || !Y))) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  return launch_spmm(ctx, A, nrhs, X, Y);
+}
+
+mfe_status mfe_cg_solve_multi(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const double* B,
+                              double* X, const mfe_cg_opts* opts, mfe_cg_result* results)
+{
+  (void)A; (void)nrhs; (void)B; (void)X; (void)opts; (void)results;
+  return fail(ctx, MFE_NOT_SUPPORTED, "multi-RHS CG is not built yet");
+}
+
+mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims,
+                                 const mfe_cg_opts* opts, double* x_out, mfe_cg_result* results)
+{
+  (void)nbox; (void)dims; (void)opts; (void)x_out; (void)results;
+  return fail(ctx, MFE_NOT_SUPPORTED, "batched boxes are not built yet");
+}
+
+}  // extern "C"

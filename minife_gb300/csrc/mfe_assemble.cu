@@ -1,0 +1,483 @@
+// Structure generation, FE assembly, Dirichlet conditions, verification and
+// the adjoint element contraction.
+//
+// This translation unit is compiled with -fmad=false: the Hex8 element math
+// must round every multiply and add separately, as the reference does, so the
+// assembled matrix and right-hand side are bit-identical to the reference's.
+//
+// Assembly is split in two passes (the reference's perform_element_loop does
+// both in one serial loop with binary-search scatter, perform_element_loop.hpp
+// :80-100, SparseMatrix_functions.hpp:183-255):
+//   1. element pass: one thread per element computes its 36-entry symmetric
+//      diffusion matrix and 8-entry source vector into a structure-of-arrays
+//      scratch (coalesced writes);
+//   2. node gather: one thread per node row reads the rows of its (up to) 8
+//      adjacent element matrices, in ascending element order, into 27 stencil
+//      accumulators, applies both Dirichlet passes in registers, and writes
+//      the CSR row (staged through shared memory for coalescing).
+// No atomics: every coefficient is summed in the reference's element order.
+#include <cstdio>
+#include <vector>
+
+#include "mfe_common.cuh"
+#include "mfe_hex8.cuh"
+#include "mfe_internal.h"
+
+namespace mfe {
+
+__constant__ Hex8Tables c_hex8;
+
+// ---------------------------------------------------------------------------
+// closed-form 27-point structure
+// ---------------------------------------------------------------------------
+// Nonzeros contributed by rows with coordinate < i along a dimension of n
+// nodes: sum_{j<i} (1 + [j>0] + [j<n-1]).
+__host__ __device__ __forceinline__ int64_t pre_count(int64_t i, int64_t n)
+{
+  return i + (i > 0 ? i - 1 : 0) + (i < n - 1 ? i : n - 1);
+}
+__host__ __device__ __forceinline__ int nbr(int i, int n)
+{
+  return 1 + (i > 0) + (i < n - 1);
+}
+// CSR offset of node (ix, iy, iz) in the Nx x Ny x Nz node box
+// (generate_matrix_structure.hpp:98-125 counts these one row at a time).
+__host__ __device__ __forceinline__ int64_t row_offset(int ix, int iy, int iz, int Nx, int Ny,
+                                                       int Nz)
+{
+  const int64_t Sx = 3 * (int64_t)Nx - 2, Sy = 3 * (int64_t)Ny - 2;
+  return pre_count(iz, Nz) * Sy * Sx + (int64_t)nbr(iz, Nz) * pre_count(iy, Ny) * Sx +
+         (int64_t)nbr(iz, Nz) * nbr(iy, Ny) * pre_count(ix, Nx);
+}
+
+int64_t box_nnz(int nx, int ny, int nz)
+{
+  return (3 * (int64_t)(nx + 1) - 2) * (3 * (int64_t)(ny + 1) - 2) * (3 * (int64_t)(nz + 1) - 2);
+}
+
+constexpr int kStructRows = 128;
+
+// One thread per row: row offset (closed form) and the ascending in-box
+// 27-point columns (MatrixInitOp.hpp:127-156), staged in shared memory so the
+// block writes its contiguous column range coalesced.  vals are zeroed.
+__global__ void __launch_bounds__(kStructRows)
+    k_structure(int Nx, int Ny, int Nz, int64_t N, int32_t* __restrict__ ro,
+                int32_t* __restrict__ cols)
+{
+  __shared__ int32_t s_cols[kStructRows * 27];
+  const int64_t r0 = (int64_t)blockIdx.x * kStructRows;
+  const int64_t r = r0 + threadIdx.x;
+  const int64_t NxNy = (int64_t)Nx * Ny;
+  const int64_t rend = min(r0 + (int64_t)kStructRows, N);
+  const int64_t base =
+      row_offset((int)(r0 % Nx), (int)((r0 / Nx) % Ny), (int)(r0 / NxNy), Nx, Ny, Nz);
+  const int64_t endoff =
+      rend == N ? (3 * (int64_t)Nx - 2) * (3 * (int64_t)Ny - 2) * (3 * (int64_t)Nz - 2)
+                : row_offset((int)(rend % Nx), (int)((rend / Nx) % Ny), (int)(rend / NxNy), Nx,
+                             Ny, Nz);
+  if (r < N) {
+    const int ix = (int)(r % Nx), iy = (int)((r / Nx) % Ny), iz = (int)(r / NxNy);
+    const int64_t off = row_offset(ix, iy, iz, Nx, Ny, Nz);
+    ro[r] = (int32_t)off;
+    int k = (int)(off - base);
+#pragma unroll
+    for (int sz = -1; sz <= 1; ++sz)
+#pragma unroll
+      for (int sy = -1; sy <= 1; ++sy)
+#pragma unroll
+        for (int sx = -1; sx <= 1; ++sx) {
+          const int jx = ix + sx, jy = iy + sy, jz = iz + sz;
+          if (jx >= 0 && jx < Nx && jy >= 0 && jy < Ny && jz >= 0 && jz < Nz)
+            s_cols[k++] = (int32_t)(r + sx + sy * (int64_t)Nx + sz * NxNy);
+        }
+    if (r == N - 1) ro[N] = (int32_t)endoff;
+  }
+  __syncthreads();
+  const int total = (int)(endoff - base);
+  for (int i = threadIdx.x; i < total; i += kStructRows) cols[base + i] = s_cols[i];
+}
+
+// ---------------------------------------------------------------------------
+// element pass
+// ---------------------------------------------------------------------------
+constexpr int kElemThreads = 128;
+
+// Element e = (ex, ey, ez) in BoxIterator order (x fastest).  Writes
+// ke[k * E + e] (k < 36, upper triangle) and fe[k * E + e] (k < 8).
+__global__ void __launch_bounds__(kElemThreads)
+    k_element(int nx, int ny, int nz, int64_t E, const double* __restrict__ kappa,
+              double* __restrict__ ke, double* __restrict__ fe)
+{
+  const int64_t e = (int64_t)blockIdx.x * kElemThreads + threadIdx.x;
+  if (e >= E) return;
+  const int ex = (int)(e % nx);
+  const int ey = (int)((e / nx) % ny);
+  const int ez = (int)(e / ((int64_t)nx * ny));
+  const ElemCorner c = elem_corner(ex, ey, ez, nx, ny, nz);
+  const double k = kappa ? kappa[e] : 1.0;
+  double em[36], ev[8];
+  element_matrix_vector(c_hex8, c, k, em, ev);
+#pragma unroll
+  for (int i = 0; i < 36; ++i) ke[i * E + e] = em[i];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) fe[i * E + e] = ev[i];
+}
+
+// ---------------------------------------------------------------------------
+// node gather + both Dirichlet passes
+// ---------------------------------------------------------------------------
+constexpr int kGatherRows = 128;
+
+__global__ void __launch_bounds__(kGatherRows)
+    k_gather(int nx, int ny, int nz, int64_t E, const double* __restrict__ ke,
+             const double* __restrict__ fe, const int32_t* __restrict__ ro,
+             double* __restrict__ vals, double* __restrict__ b, int impose_bc)
+{
+  __shared__ double s_vals[kGatherRows * 27];
+  const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
+  const int64_t NxNy = (int64_t)Nx * Ny;
+  const int64_t N = NxNy * Nz;
+  const int64_t r0 = (int64_t)blockIdx.x * kGatherRows;
+  const int64_t r = r0 + threadIdx.x;
+  const int64_t rend = min(r0 + (int64_t)kGatherRows, N);
+  const int64_t base = ro[r0];
+  if (r < N) {
+    const int ix = (int)(r % Nx), iy = (int)((r / Nx) % Ny), iz = (int)(r / NxNy);
+    const bool bc1 = (ix == Nx - 1);
+    const bool bc0 = (ix == 0 || iy == 0 || iz == 0 || iy == Ny - 1 || iz == Nz - 1);
+    const int64_t off = ro[r] - base;
+    if (impose_bc && (bc0 || bc1)) {
+      // zero_row_and_put_1_on_diagonal (SparseMatrix_functions.hpp:413-428),
+      // b = prescribed value; the x=1 face (second pass) wins on shared edges
+      int k = 0;
+#pragma unroll
+      for (int s = 0; s < 27; ++s) {
+        const int jx = ix + s % 3 - 1, jy = iy + (s / 3) % 3 - 1, jz = iz + s / 9 - 1;
+        if (jx >= 0 && jx < Nx && jy >= 0 && jy < Ny && jz >= 0 && jz < Nz)
+          s_vals[off + k++] = (s == 13) ? 1.0 : 0.0;
+      }
+      b[r] = bc1 ? 1.0 : 0.0;
+    } else {
+      double acc[27];
+#pragma unroll
+      for (int s = 0; s < 27; ++s) acc[s] = 0.0;
+      double bsum = 0.0;
+      // adjacent elements in ascending element id: (ez, ey, ex) lexicographic
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int ez = iz - 1 + c;
+#pragma unroll
+        for (int bb = 0; bb < 2; ++bb) {
+          const int ey = iy - 1 + bb;
+#pragma unroll
+          for (int a = 0; a < 2; ++a) {
+            const int ex = ix - 1 + a;
+            if (ex < 0 || ex >= nx || ey < 0 || ey >= ny || ez < 0 || ez >= nz) continue;
+            const int64_t e = ex + (int64_t)nx * (ey + (int64_t)ny * ez);
+            const int lr = local_node(1 - a, 1 - bb, 1 - c);
+#pragma unroll
+            for (int m = 0; m < 8; ++m) {
+              const int mx = (m == 1 || m == 2 || m == 5 || m == 6);
+              const int my = (m == 2 || m == 3 || m == 6 || m == 7);
+              const int mz = (m >= 4);
+              const int slot = (c + mz) * 9 + (bb + my) * 3 + (a + mx);
+              acc[slot] += __ldg(&ke[(int64_t)sym_index(lr, m) * E + e]);
+            }
+            bsum += __ldg(&fe[(int64_t)lr * E + e]);
+          }
+        }
+      }
+      if (!impose_bc) {
+        int k = 0;
+#pragma unroll
+        for (int s = 0; s < 27; ++s) {
+          const int jx = ix + s % 3 - 1, jy = iy + (s / 3) % 3 - 1, jz = iz + s / 9 - 1;
+          if (jx >= 0 && jx < Nx && jy >= 0 && jy < Ny && jz >= 0 && jz < Nz)
+            s_vals[off + k++] = acc[s];
+        }
+        b[r] = bsum;
+      } else {
+        // interior row: all 27 columns exist.  impose_dirichlet pass 1
+        // (value 0, faces x=0,y=0,z=0,y=1,z=1) then pass 2 (value 1, face
+        // x=1), SparseMatrix_functions.hpp:460-479, in ascending column order
+        double s0 = 0.0, s1 = 0.0;
+#pragma unroll
+        for (int s = 0; s < 27; ++s) {
+          const int jx = ix + s % 3 - 1, jy = iy + (s / 3) % 3 - 1, jz = iz + s / 9 - 1;
+          const bool c0 = (jx == 0 || jy == 0 || jz == 0 || jy == Ny - 1 || jz == Nz - 1);
+          const bool c1 = (jx == Nx - 1);
+          if (c0) s0 += acc[s];
+          if (c1) s1 += c0 ? 0.0 : acc[s];  // pass 1 already zeroed c0 columns
+          s_vals[off + s] = (c0 || c1) ? 0.0 : acc[s];
+        }
+        double bv = bsum;
+        bv -= s0 * 0.0;
+        bv -= s1 * 1.0;
+        b[r] = bv;
+      }
+    }
+  }
+  __syncthreads();
+  const int total = (int)(ro[rend] - base);
+  for (int i = threadIdx.x; i < total; i += kGatherRows) vals[base + i] = s_vals[i];
+}
+
+// ---------------------------------------------------------------------------
+// generic impose_dirichlet for any CSR (SparseMatrix_functions.hpp:434-480)
+// ---------------------------------------------------------------------------
+__global__ void k_bc_mark(int64_t n_bc, const int32_t* __restrict__ bc_rows, int64_t nrows,
+                          uint8_t* __restrict__ mask, const int32_t* __restrict__ ro,
+                          const int32_t* __restrict__ cols, double* __restrict__ vals,
+                          double* __restrict__ b, double value)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n_bc) return;
+  const int32_t row = bc_rows[i];
+  if (row < 0 || row >= nrows) return;  // rows outside the matrix are ignored
+  mask[row] = 1;
+  b[row] = value;
+  for (int32_t j = ro[row]; j < ro[row + 1]; ++j) vals[j] = (cols[j] == row) ? 1.0 : 0.0;
+}
+
+__global__ void k_bc_lift(int64_t nrows, const uint8_t* __restrict__ mask,
+                          const int32_t* __restrict__ ro, const int32_t* __restrict__ cols,
+                          double* __restrict__ vals, double* __restrict__ b, double value)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nrows || mask[i]) return;
+  double sum = 0.0;
+  for (int32_t j = ro[i]; j < ro[i + 1]; ++j) {
+    const int32_t c = cols[j];
+    if (c >= 0 && c < nrows && mask[c]) {
+      sum += vals[j];
+      vals[j] = 0.0;
+    }
+  }
+  b[i] -= sum * value;
+}
+
+__global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst, int64_t n)
+{
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    dst[i] = (float)src[i];
+}
+
+// ---------------------------------------------------------------------------
+// verify_solution (ref/fem/verify_solution.hpp:55-174) with the series of
+// ref/fem/analytic_soln.hpp:66-112
+// ---------------------------------------------------------------------------
+__device__ double analytic_soln(double x, double y, double z, int max_p, int max_q)
+{
+  const double PI = 3.141592653589793238462;
+  const double PI_SQR = PI * PI;
+  const double term0 = 16.0 / (PI_SQR);
+  double sum = 0;
+  for (int p = 0; p <= max_p; ++p) {
+    const double p21y = (2 * p + 1) * PI * y;
+    const double sin_py = sin(p21y) / (2 * p + 1);
+    for (int q = 0; q <= max_q; ++q) {
+      const double q21z = (2 * q + 1) * PI * z;
+      const double sin_qz = sin(q21z) / (2 * q + 1);
+      const double l = sqrt((2 * p + 1) * (2 * p + 1) * PI_SQR + (2 * q + 1) * (2 * q + 1) * PI_SQR);
+      const double sinh1 = sinh(l * x);
+      const double sinh2 = sinh(l);
+      const double tmp = (sinh1 * sin_py) * (sin_qz / sinh2);
+      if (tmp == tmp) sum += tmp;
+      else break;
+    }
+  }
+  return term0 * sum;
+}
+
+__global__ void k_verify(int Nx, int Ny, int Nz, const double* __restrict__ xv, int whole,
+                         unsigned long long* __restrict__ max_bits)
+{
+  const int64_t N = (int64_t)Nx * Ny * Nz;
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= N) return;
+  const int64_t NxNy = (int64_t)Nx * Ny;
+  const int xdiv = Nx > 1 ? Nx - 1 : 1, ydiv = Ny > 1 ? Ny - 1 : 1, zdiv = Nz > 1 ? Nz - 1 : 1;
+  const double z = (1.0 * (double)(r / NxNy)) / zdiv;
+  const double y = 1.0 * (double)((r % NxNy) / Nx) / ydiv;
+  const double x = 1.0 * (double)(r % Nx) / xdiv;
+  const bool check =
+      whole || (fabs(x - 0.5) < 0.05 && fabs(y - 0.5) < 0.05 && fabs(z - 0.5) < 0.05);
+  if (!check) return;
+  double a;
+  if (x == 1.0) a = 1;
+  else if (x == 0.0 || y == 0.0 || z == 0.0) a = 0;
+  else if (y == 1.0 || z == 1.0) a = 0;
+  else a = analytic_soln(x, y, z, 300, 300);
+  const double err = fabs(a - xv[r]);
+  // non-negative doubles order like their bit patterns
+  atomicMax(max_bits, (unsigned long long)__double_as_longlong(err));
+}
+
+// ---------------------------------------------------------------------------
+// adjoint contraction: g[e] = -lambda_e^T Khat_e u_e (k = 1 element matrix)
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kElemThreads)
+    k_elem_grad(int nx, int ny, int nz, int64_t E, const double* __restrict__ u,
+                const double* __restrict__ lam, double* __restrict__ g)
+{
+  const int64_t e = (int64_t)blockIdx.x * kElemThreads + threadIdx.x;
+  if (e >= E) return;
+  const int ex = (int)(e % nx);
+  const int ey = (int)((e / nx) % ny);
+  const int ez = (int)(e / ((int64_t)nx * ny));
+  const int Nx = nx + 1;
+  const int64_t NxNy = (int64_t)Nx * (ny + 1);
+  const int64_t n0 = ex + (int64_t)Nx * ey + NxNy * ez;
+  const int64_t ids[8] = {n0, n0 + 1, n0 + Nx + 1, n0 + Nx,
+                          n0 + NxNy, n0 + 1 + NxNy, n0 + Nx + NxNy + 1, n0 + Nx + NxNy};
+  const ElemCorner c = elem_corner(ex, ey, ez, nx, ny, nz);
+  double em[36], ev[8];
+  element_matrix_vector(c_hex8, c, 1.0, em, ev);
+  double ue[8], le[8];
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    ue[i] = u[ids[i]];
+    le[i] = lam[ids[i]];
+  }
+  double s = 0.0;
+#pragma unroll
+  for (int m = 0; m < 8; ++m) {
+    double t = 0.0;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) t += em[sym_index(m, n)] * ue[n];
+    s += le[m] * t;
+  }
+  g[e] = -s;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+static bool g_tables_ready[64] = {};
+
+// Hex8::gradients / shape_fns at the 2x2x2 Gauss points (Hex8.hpp:44-113,
+// Hex8_ElemData.hpp:37-61).  Products and differences of constants only.
+static void fill_tables(Hex8Tables& T)
+{
+  const double gpts[2] = {-kGaussPt, kGaussPt};
+  for (int ig = 0; ig < 2; ++ig)
+    for (int jg = 0; jg < 2; ++jg)
+      for (int kg = 0; kg < 2; ++kg) {
+        const int gp = ig * 4 + jg * 2 + kg;
+        const double x0 = gpts[ig], x1 = gpts[jg], x2 = gpts[kg];
+        const double u = 1.0 - x0, v = 1.0 - x1, w = 1.0 - x2;
+        const double up1 = 1.0 + x0, vp1 = 1.0 + x1, wp1 = 1.0 + x2;
+        double* g = &T.grad[gp][0][0];
+        g[0] = -0.125 * v * w;     g[1] = -0.125 * u * w;     g[2] = -0.125 * u * v;
+        g[3] = 0.125 * v * w;      g[4] = -0.125 * up1 * w;   g[5] = -0.125 * up1 * v;
+        g[6] = 0.125 * vp1 * w;    g[7] = 0.125 * up1 * w;    g[8] = -0.125 * up1 * vp1;
+        g[9] = -0.125 * vp1 * w;   g[10] = 0.125 * u * w;     g[11] = -0.125 * u * vp1;
+        g[12] = -0.125 * v * wp1;  g[13] = -0.125 * u * wp1;  g[14] = 0.125 * u * v;
+        g[15] = 0.125 * v * wp1;   g[16] = -0.125 * up1 * wp1; g[17] = 0.125 * up1 * v;
+        g[18] = 0.125 * vp1 * wp1; g[19] = 0.125 * up1 * wp1; g[20] = 0.125 * up1 * vp1;
+        g[21] = -0.125 * vp1 * wp1; g[22] = 0.125 * u * wp1;  g[23] = 0.125 * u * vp1;
+        double* p = T.psi[gp];
+        p[0] = 0.125 * u * v * w;
+        p[1] = 0.125 * up1 * v * w;
+        p[2] = 0.125 * up1 * vp1 * w;
+        p[3] = 0.125 * u * vp1 * w;
+        p[4] = 0.125 * u * v * wp1;
+        p[5] = 0.125 * up1 * v * wp1;
+        p[6] = 0.125 * up1 * vp1 * wp1;
+        p[7] = 0.125 * u * vp1 * wp1;
+      }
+}
+
+static mfe_status ensure_tables(mfe_ctx* ctx)
+{
+  if (ctx->device >= 0 && ctx->device < 64 && g_tables_ready[ctx->device]) return MFE_OK;
+  Hex8Tables T;
+  fill_tables(T);
+  MFE_CUDA_TRY(ctx, cudaMemcpyToSymbol(c_hex8, &T, sizeof(T)));
+  if (ctx->device >= 0 && ctx->device < 64) g_tables_ready[ctx->device] = true;
+  return MFE_OK;
+}
+
+mfe_status launch_structure(mfe_ctx* ctx, int nx, int ny, int nz, int32_t* ro, int32_t* cols)
+{
+  const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
+  const int64_t N = (int64_t)Nx * Ny * Nz;
+  const int64_t blocks = ceil_div(N, kStructRows);
+  k_structure<<<(unsigned)blocks, kStructRows, 0, ctx->stream>>>(Nx, Ny, Nz, N, ro, cols);
+  return check_launch(ctx, "k_structure");
+}
+
+mfe_status launch_assemble(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,
+                           const int32_t* ro, double* vals, double* b, int impose_bc)
+{
+  MFE_TRY(ensure_tables(ctx));
+  const int64_t E = (int64_t)nx * ny * nz;
+  const int64_t N = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+  double* ke = static_cast<double*>(workspace(ctx, "assembly.ke", sizeof(double) * 44 * E));
+  if (!ke) return fail(ctx, MFE_OOM, "assembly scratch allocation failed");
+  double* fe = ke + 36 * E;
+  k_element<<<(unsigned)ceil_div(E, kElemThreads), kElemThreads, 0, ctx->stream>>>(
+      nx, ny, nz, E, kappa, ke, fe);
+  MFE_TRY(check_launch(ctx, "k_element"));
+  k_gather<<<(unsigned)ceil_div(N, kGatherRows), kGatherRows, 0, ctx->stream>>>(
+      nx, ny, nz, E, ke, fe, ro, vals, b, impose_bc);
+  return check_launch(ctx, "k_gather");
+}
+
+mfe_status launch_impose_dirichlet(mfe_ctx* ctx, const mfe_csr* A, double* b, double value,
+                                   const int32_t* bc_rows, int64_t n_bc)
+{
+  uint8_t* mask = static_cast<uint8_t*>(workspace(ctx, "bc.mask", (size_t)A->nrows + 1));
+  if (!mask) return fail(ctx, MFE_OOM, "bc mask allocation failed");
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(mask, 0, (size_t)A->nrows, ctx->stream));
+  double* vals = static_cast<double*>(A->vals);
+  if (n_bc > 0) {
+    k_bc_mark<<<(unsigned)ceil_div(n_bc, 256), 256, 0, ctx->stream>>>(
+        n_bc, bc_rows, A->nrows, mask, A->row_offsets, A->cols, vals, b, value);
+    MFE_TRY(check_launch(ctx, "k_bc_mark"));
+  }
+  k_bc_lift<<<(unsigned)ceil_div(A->nrows, 256), 256, 0, ctx->stream>>>(
+      A->nrows, mask, A->row_offsets, A->cols, vals, b, value);
+  return check_launch(ctx, "k_bc_lift");
+}
+
+mfe_status launch_convert_f32(mfe_ctx* ctx, const double* src, float* dst, int64_t n)
+{
+  const int64_t blocks = std::min<int64_t>(ceil_div(n, 256), (int64_t)ctx->sm_count * 16);
+  k_to_f32<<<(unsigned)std::max<int64_t>(blocks, 1), 256, 0, ctx->stream>>>(src, dst, n);
+  return check_launch(ctx, "k_to_f32");
+}
+
+mfe_status launch_verify(mfe_ctx* ctx, int nx, int ny, int nz, const double* x, int whole,
+                         double* max_err_host)
+{
+  const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
+  const int64_t N = (int64_t)Nx * Ny * Nz;
+  unsigned long long* d = static_cast<unsigned long long*>(workspace(ctx, "verify.max", 8));
+  if (!d) return fail(ctx, MFE_OOM, "verify scratch allocation failed");
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(d, 0, 8, ctx->stream));
+  k_verify<<<(unsigned)ceil_div(N, 128), 128, 0, ctx->stream>>>(Nx, Ny, Nz, x, whole, d);
+  MFE_TRY(check_launch(ctx, "k_verify"));
+  unsigned long long* h = static_cast<unsigned long long*>(host_scratch(ctx, 8));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  unsigned long long bits = *h;
+  double v;
+  static_assert(sizeof(v) == sizeof(bits), "");
+  memcpy(&v, &bits, sizeof(v));
+  *max_err_host = v;
+  return MFE_OK;
+}
+
+mfe_status launch_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
+                                   const double* lambda, double* g)
+{
+  MFE_TRY(ensure_tables(ctx));
+  const int64_t E = (int64_t)nx * ny * nz;
+  k_elem_grad<<<(unsigned)ceil_div(E, kElemThreads), kElemThreads, 0, ctx->stream>>>(
+      nx, ny, nz, E, u, lambda, g);
+  return check_launch(ctx, "k_elem_grad");
+}
+
+}  // namespace mfe

@@ -1,0 +1,154 @@
+// Shared device helpers for the minife_gb300 kernels (sm_103a).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "minife_gb300.h"
+
+namespace mfe {
+
+// ---------------------------------------------------------------------------
+// error flags written by kernels instead of trapping: bit 0 = a bounded
+// mbarrier wait gave up, bit 1 = a tile did not fit its shared-memory stage
+// ---------------------------------------------------------------------------
+enum : unsigned { ERR_WAIT_TIMEOUT = 1u, ERR_TILE_OVERFLOW = 2u };
+
+// Upper bound on mbarrier polls before a wait gives up (each try_wait may
+// suspend the thread for a hardware-chosen interval, so this is >> 1 s).
+constexpr unsigned kMaxPolls = 1u << 26;
+
+// ---------------------------------------------------------------------------
+// reductions (deterministic for a fixed launch shape)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double warp_sum(double v)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Sum over the block; result valid in thread 0.  scratch: >= 32 doubles.
+__device__ __forceinline__ double block_sum(double v, double* scratch)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  v = warp_sum(v);
+  __syncthreads();  // scratch may be reused across calls
+  if (lane == 0) scratch[wid] = v;
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  double s = 0.0;
+  if (wid == 0) {
+    s = lane < nw ? scratch[lane] : 0.0;
+    s = warp_sum(s);
+  }
+  return s;
+}
+
+// Grid-level reduction tail: block partial -> partials[blockIdx.x]; the last
+// block to finish (atomic ticket) sums the partials in block order and
+// returns true with the total in *total (thread 0 only).  The ticket counter
+// is re-armed to 0 by the last block, so consecutive launches reuse it.
+__device__ __forceinline__ bool grid_reduce_last(double block_total, double* partials,
+                                                 unsigned* ticket, double* scratch,
+                                                 double* total)
+{
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+    partials[blockIdx.x] = block_total;
+    __threadfence();
+    unsigned t = atomicAdd(ticket, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  double s = 0.0;
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x)
+    s += __ldcg(&partials[i]);
+  s = block_sum(s, scratch);
+  if (threadIdx.x == 0) {
+    *total = s;
+    *ticket = 0u;
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// mbarrier + bulk async copy (TMA, non-tensor form), inline PTX
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_u32(const void* p)
+{
+  return static_cast<uint32_t>(__cvta_generic_to_shared(p));
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count)
+{
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+}
+
+__device__ __forceinline__ void fence_mbar_init()
+{
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+__device__ __forceinline__ void fence_proxy_async_smem()
+{
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(
+                   smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
+{
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait; returns false (and the caller records ERR_WAIT_TIMEOUT) if
+// the phase did not complete within kMaxPolls polls.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity)
+{
+  for (unsigned i = 0; i < kMaxPolls; ++i)
+    if (mbar_try_wait(bar, parity)) return true;
+  return false;
+}
+
+// 1-D bulk copy global -> shared, completion counted on bar (bytes, smem and
+// gmem addresses must be multiples of 16).
+__device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, unsigned bytes,
+                                         uint64_t* bar)
+{
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(smem_dst)),
+      "l"(gmem_src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// misc
+// ---------------------------------------------------------------------------
+template <typename T>
+__device__ __forceinline__ T ldg(const T* p) { return __ldg(p); }
+
+__host__ __device__ __forceinline__ int64_t ceil_div(int64_t a, int64_t b)
+{
+  return (a + b - 1) / b;
+}
+
+}  // namespace mfe

@@ -1,0 +1,100 @@
+// Internal declarations shared by the minife_gb300 translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "minife_gb300.h"
+
+struct mfe_cg_graph;  // cached CUDA graph of the CG loop (mfe_cg.cu)
+
+struct mfe_ctx {
+  int device = 0;
+  int sm_count = 0;
+  cudaStream_t own_stream = nullptr;
+  cudaStream_t stream = nullptr;
+  std::string err;
+  // named device workspace, grown on demand and owned by the context
+  struct Buf {
+    void* ptr = nullptr;
+    size_t bytes = 0;
+  };
+  std::map<std::string, Buf> ws;
+  // pinned host scratch for small device->host reads
+  void* host_scratch = nullptr;
+  size_t host_scratch_bytes = 0;
+  mfe_cg_graph* cg_graph = nullptr;
+  std::vector<double> history;
+  // cached FP32 copy of a matrix for the mixed-precision solver
+  const void* f32_src_vals = nullptr;
+  int64_t f32_src_nnz = 0;
+  mfe_csr f32_copy{};
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+};
+
+namespace mfe {
+
+// Record a failure on ctx and return its status.
+mfe_status fail(mfe_ctx* ctx, mfe_status st, const std::string& msg);
+mfe_status cuda_fail(mfe_ctx* ctx, cudaError_t e, const char* where);
+// Check the last launch; returns MFE_OK or MFE_CUDA_ERR.
+mfe_status check_launch(mfe_ctx* ctx, const char* where);
+
+// Named workspace buffer of at least `bytes` (contents undefined when grown).
+void* workspace(mfe_ctx* ctx, const char* name, size_t bytes);
+// Pinned host scratch of at least `bytes`.
+void* host_scratch(mfe_ctx* ctx, size_t bytes);
+
+// ---- assembly (mfe_assemble.cu) ----
+mfe_status launch_structure(mfe_ctx* ctx, int nx, int ny, int nz, int32_t* ro, int32_t* cols);
+mfe_status launch_assemble(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,
+                           const int32_t* ro, double* vals, double* b, int impose_bc);
+mfe_status launch_impose_dirichlet(mfe_ctx* ctx, const mfe_csr* A, double* b, double value,
+                                   const int32_t* bc_rows, int64_t n_bc);
+mfe_status launch_convert_f32(mfe_ctx* ctx, const double* src, float* dst, int64_t n);
+mfe_status launch_verify(mfe_ctx* ctx, int nx, int ny, int nz, const double* x, int whole,
+                         double* max_err_host);
+mfe_status launch_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
+                                   const double* lambda, double* g);
+int64_t box_nnz(int nx, int ny, int nz);
+
+// ---- SpMV (mfe_spmv.cu) ----
+struct DotSink {
+  double* partials = nullptr;  // >= grid blocks
+  unsigned* ticket = nullptr;
+  double* out = nullptr;       // device scalar receiving the dot
+};
+int spmv_grid(mfe_ctx* ctx, const mfe_csr* A);
+mfe_status ensure_max_row_len(mfe_ctx* ctx, const mfe_csr* A, int* max_len);
+// y = A x, optionally with x.y (FP64-accumulated) into sink.out.  When
+// resid_b != nullptr the kernel instead writes y = b - A x and the dot is y.y.
+mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
+                       const DotSink* sink, const double* resid_b, void* cg_state);
+mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y);
+
+// ---- BLAS-1 and CG (mfe_cg.cu) ----
+mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
+                      double* dev_out);
+mfe_status launch_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
+                         const double* y, double* w);
+mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
+                         const mfe_cg_opts* opts, mfe_cg_result* res);
+void cg_graph_destroy(mfe_cg_graph* g);
+
+}  // namespace mfe
+
+#define MFE_CUDA_TRY(ctx, expr)                                      \
+  do {                                                               \
+    cudaError_t _e = (expr);                                         \
+    if (_e != cudaSuccess) return ::mfe::cuda_fail((ctx), _e, #expr); \
+  } while (0)
+
+#define MFE_TRY(expr)                  \
+  do {                                 \
+    mfe_status _s = (expr);            \
+    if (_s != MFE_OK) return _s;       \
+  } while (0)

@@ -1,0 +1,453 @@
+// CSR matrix-vector products on sm_103a.
+//
+// GB300 has a reduced FP64 pipe (about 2 FP64 FMA per clock per SM), which
+// puts an FP64 CSR SpMV close to the FP64 issue limit as well as the HBM
+// limit.  The main kernel therefore spends exactly one FP64 FMA per nonzero:
+// one thread owns one row and accumulates it sequentially (no shuffle-add
+// trees, which would cost 5 extra FP64 adds per lane), while the row's values
+// and column indices arrive through shared memory so the HBM reads stay fully
+// coalesced:
+//   - a persistent grid walks tiles of ROWS consecutive rows; the nonzeros of
+//     a tile are contiguous in CSR, so one thread issues two 1-D bulk async
+//     copies (TMA, cp.async.bulk) for the tile's values and columns into a
+//     shared-memory stage, completion tracked by an mbarrier;
+//   - S stages are in flight per CTA, so the copies for the next tiles
+//     overlap the current tile's FMAs;
+//   - x is gathered through the read-only path (27-point rows touch three
+//     x-planes, which stay L1/L2 resident).
+// Epilogues: plain y = A x; y = A x with x.y (matvec_and_dot); and the CG
+// residual r = b - A x with r.r.  Dots accumulate in FP64 and reduce
+// deterministically (fixed grid, last block sums the block partials in order).
+// Matrices with rows longer than kMaxTileRowLen use a warp-per-row kernel.
+#include <algorithm>
+#include <cstdio>
+#include <cstdlib>
+
+#include "mfe_cgstate.cuh"
+#include "mfe_common.cuh"
+#include "mfe_internal.h"
+
+namespace mfe {
+
+constexpr int kMaxTileRowLen = 32;
+
+enum SpmvMode { SPMV_PLAIN = 0, SPMV_DOT = 1, SPMV_RESID = 2 };
+
+template <typename T>
+struct SpmvParams {
+  int64_t n;
+  int64_t nnz;
+  const int32_t* __restrict__ ro;
+  const int32_t* __restrict__ cols;
+  const T* __restrict__ vals;
+  const T* __restrict__ x;
+  T* __restrict__ y;
+  const double* __restrict__ b;  // SPMV_RESID: y = b - A x
+  int cap;                       // elements per stage (multiple of 4)
+  double* partials;
+  unsigned* ticket;
+  double* dot_out;  // used when cg == nullptr
+  CgState* cg;      // CG bookkeeping in the last block (nullable)
+  unsigned* err;
+};
+
+// Row sum: exactly one FMA per nonzero, in column order.
+template <typename T>
+__device__ __forceinline__ T row_dot(const T* __restrict__ rv, const int32_t* __restrict__ rc,
+                                     int len, const T* __restrict__ x)
+{
+  T sum = T(0);
+  if (len == 27) {
+    T xv[27];
+#pragma unroll
+    for (int k = 0; k < 27; ++k) xv[k] = __ldg(&x[rc[k]]);
+#pragma unroll
+    for (int k = 0; k < 27; ++k) sum = fma(rv[k], xv[k], sum);
+  } else {
+#pragma unroll 4
+    for (int k = 0; k < len; ++k) sum = fma(rv[k], __ldg(&x[rc[k]]), sum);
+  }
+  return sum;
+}
+
+template <int MODE>
+__device__ __forceinline__ void spmv_epilogue(double total, CgState* cg, double* dot_out)
+{
+  if (cg == nullptr) {
+    if (MODE != SPMV_PLAIN) *dot_out = total;
+    return;
+  }
+  if (MODE == SPMV_DOT) {
+    // cg_solve.hpp:179-200: p.Ap and the breakdown pre-test
+    cg->pAp = total;
+    if (total < cg->brkdown_tol) cg->check_pending = 1;
+  } else if (MODE == SPMV_RESID) {
+    // cg_solve.hpp:124-144: r = b - A x, rtrans, normr, loop condition
+    const double normr = sqrt(total);
+    cg->rtrans = total;
+    cg->rr_new = total;
+    cg->normr = normr;
+    cg->normr0 = normr;
+    const double tol_abs = cg->tol_mode ? cg->tol_abs * normr : cg->tol_abs;
+    cg->tol_abs = tol_abs;
+    cg->k = 1;
+    cg->num_iters = 0;
+    cg->cont = (1 <= cg->max_iter) && (normr > tol_abs);
+    if (cg->record) cg->history[0] = normr;
+  }
+}
+
+template <typename T, int ROWS, int S, int MODE>
+__global__ void __launch_bounds__(ROWS) k_spmv_tiled(SpmvParams<T> P)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar[S];
+  __shared__ int64_t s_base_v[S], s_base_c[S];
+  __shared__ double red[32];
+  constexpr int VA = 16 / sizeof(T);  // values per 16 bytes
+  T* sv = reinterpret_cast<T*>(smem);
+  int32_t* sc = reinterpret_cast<int32_t*>(smem + (size_t)S * P.cap * sizeof(T));
+
+  const int tid = threadIdx.x;
+  const int64_t ntiles = (P.n + ROWS - 1) / ROWS;
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // producer (thread 0): stage nonzeros [a, e) of one tile into stage s
+  auto issue = [&](int64_t a, int64_t e, int s) {
+    const int64_t av = a & ~(int64_t)(VA - 1);
+    const int64_t ac = a & ~(int64_t)3;
+    int64_t bv = min((e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
+    int64_t bc = min((e + 3) & ~(int64_t)3, P.nnz & ~(int64_t)3);
+    if (bv < av) bv = av;
+    if (bc < ac) bc = ac;
+    if (max(bv, e) - av > P.cap || max(bc, e) - ac > P.cap) {
+      // cannot happen when every row has <= max_len nonzeros (the host sizes
+      // cap from max_len); record it and stage nothing
+      atomicOr(P.err, ERR_TILE_OVERFLOW);
+      s_base_v[s] = a;
+      s_base_c[s] = a;
+      mbar_arrive_expect_tx(&bar[s], 0);
+      return;
+    }
+    s_base_v[s] = av;
+    s_base_c[s] = ac;
+    T* dv = sv + (size_t)s * P.cap;
+    int32_t* dc = sc + (size_t)s * P.cap;
+    // ragged tail past the last 16-byte boundary of the arrays: plain loads
+    for (int64_t k = bv; k < e; ++k) dv[k - av] = P.vals[k];
+    for (int64_t k = bc; k < e; ++k) dc[k - ac] = P.cols[k];
+    fence_proxy_async_smem();
+    const unsigned bytes_v = (unsigned)((bv - av) * sizeof(T));
+    const unsigned bytes_c = (unsigned)((bc - ac) * sizeof(int32_t));
+    mbar_arrive_expect_tx(&bar[s], bytes_v + bytes_c);
+    if (bytes_v) bulk_g2s(dv, P.vals + av, bytes_v, &bar[s]);
+    if (bytes_c) bulk_g2s(dc, P.cols + ac, bytes_c, &bar[s]);
+  };
+  auto tile_bounds = [&](int64_t t, int64_t& a, int64_t& e) {
+    a = __ldg(&P.ro[t * ROWS]);
+    e = __ldg(&P.ro[min(P.n, t * ROWS + ROWS)]);
+  };
+
+  if (tid == 0) {
+    for (int s = 0; s < S; ++s) {
+      const int64_t t = blockIdx.x + (int64_t)s * gridDim.x;
+      if (t < ntiles) {
+        int64_t a, e;
+        tile_bounds(t, a, e);
+        issue(a, e, s);
+      }
+    }
+  }
+
+  double dacc = 0.0;
+  int it = 0;
+  int64_t tile = blockIdx.x;
+  // row offsets of this thread's row in the current tile (prefetched)
+  int32_t ra = 0, rb = 0;
+  {
+    const int64_t r = tile * ROWS + tid;
+    if (tile < ntiles && r < P.n) {
+      ra = __ldg(&P.ro[r]);
+      rb = __ldg(&P.ro[r + 1]);
+    }
+  }
+  bool ok = true;
+  for (; tile < ntiles; tile += gridDim.x, ++it) {
+    const int s = it % S;
+    const unsigned parity = (unsigned)((it / S) & 1);
+    // prefetch the next tile's row offsets into registers
+    const int64_t ntile = tile + gridDim.x;
+    const int64_t nr = ntile * ROWS + tid;
+    int32_t na = 0, nb = 0;
+    if (ntile < ntiles && nr < P.n) {
+      na = __ldg(&P.ro[nr]);
+      nb = __ldg(&P.ro[nr + 1]);
+    }
+    // thread 0: bounds of the tile it will stage into s after this one
+    const int64_t itile = tile + (int64_t)S * gridDim.x;
+    int64_t ia = 0, ie = 0;
+    if (tid == 0 && itile < ntiles) tile_bounds(itile, ia, ie);
+    ok = mbar_wait_bounded(&bar[s], parity);
+    ok = __syncthreads_and(ok);
+    if (!ok) break;
+    const int64_t r = tile * ROWS + tid;
+    if (r < P.n) {
+      const int len = rb - ra;
+      const T* rv = sv + (size_t)s * P.cap + (ra - s_base_v[s]);
+      const int32_t* rc = sc + (size_t)s * P.cap + (ra - s_base_c[s]);
+      const T sum = row_dot<T>(rv, rc, len, P.x);
+      if (MODE == SPMV_RESID) {
+        const double rr = P.b[r] - (double)sum;
+        P.y[r] = (T)rr;
+        dacc = fma(rr, rr, dacc);
+      } else {
+        P.y[r] = sum;
+        if (MODE == SPMV_DOT) dacc = fma((double)sum, (double)__ldg(&P.x[r]), dacc);
+      }
+    }
+    ra = na;
+    rb = nb;
+    __syncthreads();  // every thread is done reading stage s
+    if (tid == 0 && itile < ntiles) issue(ia, ie, s);
+  }
+  if (!ok) {
+    if (tid == 0) {
+      atomicOr(P.err, ERR_WAIT_TIMEOUT);
+      // drain: give every stage that may still have copies in flight a
+      // bounded chance to complete before the block exits
+      for (int s = 0; s < S; ++s) {
+        const int j = it + s;
+        mbar_wait_bounded(&bar[j % S], (unsigned)((j / S) & 1));
+      }
+    }
+    return;
+  }
+  if (MODE != SPMV_PLAIN) {
+    const double bt = block_sum(dacc, red);
+    double total;
+    if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && tid == 0)
+      spmv_epilogue<MODE>(total, P.cg, P.dot_out);
+  }
+}
+
+// Warp-per-row fallback for long rows (shuffle-reduced).
+template <typename T, int MODE>
+__global__ void __launch_bounds__(256) k_spmv_warp(SpmvParams<T> P)
+{
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t warp = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+  double dacc = 0.0;
+  for (int64_t r = warp; r < P.n; r += nwarps) {
+    const int32_t a = P.ro[r], e = P.ro[r + 1];
+    T sum = T(0);
+    for (int32_t k = a + lane; k < e; k += 32) sum = fma(P.vals[k], __ldg(&P.x[P.cols[k]]), sum);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) sum += __shfl_xor_sync(0xffffffffu, sum, o);
+    if (lane == 0) {
+      if (MODE == SPMV_RESID) {
+        const double rr = P.b[r] - (double)sum;
+        P.y[r] = (T)rr;
+        dacc = fma(rr, rr, dacc);
+      } else {
+        P.y[r] = sum;
+        if (MODE == SPMV_DOT) dacc = fma((double)sum, (double)P.x[r], dacc);
+      }
+    }
+  }
+  if (MODE != SPMV_PLAIN) {
+    const double bt = block_sum(dacc, red);
+    double total;
+    if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0)
+      spmv_epilogue<MODE>(total, P.cg, P.dot_out);
+  }
+}
+
+__global__ void k_max_row_len(int64_t n, const int32_t* __restrict__ ro, int* out)
+{
+  int m = 0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * blockDim.x)
+    m = max(m, ro[i + 1] - ro[i]);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+  if ((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+// ---------------------------------------------------------------------------
+// multi-RHS: Y = A X, X and Y row-major with nrhs columns; one thread per
+// (row, rhs) pair walks the row, so A is read once per product through L1.
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void __launch_bounds__(256)
+    k_spmm(int64_t n, int nrhs, const int32_t* __restrict__ ro, const int32_t* __restrict__ cols,
+           const T* __restrict__ vals, const T* __restrict__ X, T* __restrict__ Y)
+{
+  const int64_t total = n * nrhs;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < total;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / nrhs;
+    const int j = (int)(t - r * nrhs);
+    const int32_t a = ro[r], e = ro[r + 1];
+    T sum = T(0);
+    for (int32_t k = a; k < e; ++k) sum = fma(vals[k], __ldg(&X[(int64_t)cols[k] * nrhs + j]), sum);
+    Y[t] = sum;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+constexpr int kTileRows = 128;
+constexpr int kStages = 2;
+
+// Stage capacity (elements) for rows of at most max_len nonzeros: the tile's
+// nonzeros plus the 16-byte alignment slack at both ends, kept a multiple of 4
+// so every stage starts 16-byte aligned.
+static int tile_cap(int max_len)
+{
+  return ((kTileRows * max_len + 8) + 3) & ~3;
+}
+
+template <typename T>
+static size_t tiled_smem(int max_len)
+{
+  return (size_t)kStages * tile_cap(max_len) * (sizeof(T) + sizeof(int32_t));
+}
+
+template <typename T, int MODE>
+static cudaError_t configure_tiled()
+{
+  static bool done = false;
+  if (done) return cudaSuccess;
+  cudaError_t e = cudaFuncSetAttribute(k_spmv_tiled<T, kTileRows, kStages, MODE>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)tiled_smem<T>(kMaxTileRowLen));
+  if (e == cudaSuccess) done = true;
+  return e;
+}
+
+// CTAs per SM for the tiled kernel (MFE_SPMV_CTAS_PER_SM overrides, for
+// launch-shape sweeps); limited by shared memory.
+static int tiled_ctas_per_sm(size_t smem)
+{
+  int per_sm = (int)((227 * 1024) / (smem + 1024));
+  if (const char* v = getenv("MFE_SPMV_CTAS_PER_SM")) {
+    const int o = atoi(v);
+    if (o > 0 && o < per_sm) per_sm = o;
+  }
+  return std::max(1, per_sm);
+}
+
+int spmv_grid(mfe_ctx* ctx, const mfe_csr* A)
+{
+  const int64_t ntiles = ceil_div(A->nrows, kTileRows);
+  const int max_len = A->max_row_len > 0 ? A->max_row_len : kMaxTileRowLen;
+  const size_t smem =
+      A->dtype == MFE_F32 ? tiled_smem<float>(max_len) : tiled_smem<double>(max_len);
+  const int per_sm = tiled_ctas_per_sm(smem);
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * per_sm));
+}
+
+mfe_status ensure_max_row_len(mfe_ctx* ctx, const mfe_csr* A, int* max_len)
+{
+  if (A->max_row_len > 0) {
+    *max_len = A->max_row_len;
+    return MFE_OK;
+  }
+  int* d = static_cast<int*>(workspace(ctx, "spmv.maxlen", sizeof(int)));
+  if (!d) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(d, 0, sizeof(int), ctx->stream));
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(A->nrows, 256),
+                                                                (int64_t)ctx->sm_count * 8));
+  k_max_row_len<<<(unsigned)blocks, 256, 0, ctx->stream>>>(A->nrows, A->row_offsets, d);
+  MFE_TRY(check_launch(ctx, "k_max_row_len"));
+  int* h = static_cast<int*>(host_scratch(ctx, sizeof(int)));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(h, d, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  *max_len = *h;
+  return MFE_OK;
+}
+
+template <typename T, int MODE>
+static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, const DotSink* sink,
+                           const double* b, CgState* cg, int max_len)
+{
+  SpmvParams<T> P;
+  P.n = A->nrows;
+  P.nnz = A->nnz;
+  P.ro = A->row_offsets;
+  P.cols = A->cols;
+  P.vals = static_cast<const T*>(A->vals);
+  P.x = x;
+  P.y = y;
+  P.b = b;
+  P.cap = tile_cap(std::max(max_len, 1));
+  P.partials = sink ? sink->partials : nullptr;
+  P.ticket = sink ? sink->ticket : nullptr;
+  P.dot_out = sink ? sink->out : nullptr;
+  P.cg = cg;
+  P.err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
+  if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  if (cg) P.err = &cg->err;
+  if (A->nrows == 0) return MFE_OK;
+  if (max_len <= kMaxTileRowLen) {
+    MFE_CUDA_TRY(ctx, (configure_tiled<T, MODE>()));
+    const size_t smem = tiled_smem<T>(std::max(max_len, 1));
+    const int64_t ntiles = ceil_div(A->nrows, kTileRows);
+    const int grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * tiled_ctas_per_sm(smem)));
+    k_spmv_tiled<T, kTileRows, kStages, MODE><<<grid, kTileRows, smem, ctx->stream>>>(P);
+    return check_launch(ctx, "k_spmv_tiled");
+  }
+  const int grid = (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(A->nrows * 32, 256), (int64_t)ctx->sm_count * 8));
+  k_spmv_warp<T, MODE><<<grid, 256, 0, ctx->stream>>>(P);
+  return check_launch(ctx, "k_spmv_warp");
+}
+
+mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
+                       const DotSink* sink, const double* resid_b, void* cg_state)
+{
+  int max_len = 0;
+  MFE_TRY(ensure_max_row_len(ctx, A, &max_len));
+  CgState* cg = static_cast<CgState*>(cg_state);
+  if (A->dtype == MFE_F64) {
+    const double* xd = static_cast<const double*>(x);
+    double* yd = static_cast<double*>(y);
+    if (resid_b) return launch_t<double, SPMV_RESID>(ctx, A, xd, yd, sink, resid_b, cg, max_len);
+    if (sink) return launch_t<double, SPMV_DOT>(ctx, A, xd, yd, sink, nullptr, cg, max_len);
+    return launch_t<double, SPMV_PLAIN>(ctx, A, xd, yd, nullptr, nullptr, cg, max_len);
+  }
+  if (A->dtype == MFE_F32) {
+    const float* xf = static_cast<const float*>(x);
+    float* yf = static_cast<float*>(y);
+    if (resid_b) return fail(ctx, MFE_NOT_SUPPORTED, "FP32 residual SpMV is not provided");
+    if (sink) return launch_t<float, SPMV_DOT>(ctx, A, xf, yf, sink, nullptr, cg, max_len);
+    return launch_t<float, SPMV_PLAIN>(ctx, A, xf, yf, nullptr, nullptr, cg, max_len);
+  }
+  return fail(ctx, MFE_BAD_ARG, "unknown matrix dtype");
+}
+
+mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y)
+{
+  const int64_t total = A->nrows * (int64_t)nrhs;
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256),
+                                                                (int64_t)ctx->sm_count * 16));
+  if (A->dtype == MFE_F64)
+    k_spmm<double><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
+        A->nrows, nrhs, A->row_offsets, A->cols, static_cast<const double*>(A->vals),
+        static_cast<const double*>(X), static_cast<double*>(Y));
+  else
+    k_spmm<float><<<(unsigned)blocks, 256, 0, ctx->stream>>>(
+        A->nrows, nrhs, A->row_offsets, A->cols, static_cast<const float*>(A->vals),
+        static_cast<const float*>(X), static_cast<float*>(Y));
+  return check_launch(ctx, "k_spmm");
+}
+
+}  // namespace mfe
