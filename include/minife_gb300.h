@@ -76,9 +76,11 @@ typedef struct mfe_csr {
 int mfe_abi_version(void);
 mfe_status mfe_ctx_create(int device, mfe_ctx** out);
 mfe_status mfe_ctx_destroy(mfe_ctx* ctx);
-/* Run this context's work on an existing CUDA stream (cudaStream_t); NULL
- * restores the context's own stream. */
+/* Run this context's work on an existing CUDA stream (cudaStream_t).  NULL
+ * selects the CUDA default stream, as it does for CUDA runtime calls. */
 mfe_status mfe_set_stream(mfe_ctx* ctx, void* stream);
+/* Return to the context's own (non-blocking) stream. */
+mfe_status mfe_use_own_stream(mfe_ctx* ctx);
 mfe_status mfe_synchronize(mfe_ctx* ctx);
 const char* mfe_last_error_string(const mfe_ctx* ctx);
 const char* mfe_status_string(mfe_status s);

@@ -68,7 +68,7 @@ class Context:
             raise MiniFEError(st, "mfe_ctx_create(device=%d) failed" % device)
         self.h = h
         self.device = int(device)
-        self._bound_stream = None
+        self._bound_stream = -1
 
     def close(self):
         if getattr(self, "h", None):

@@ -59,6 +59,7 @@ SIGNATURES = {
     "mfe_ctx_create": (ctypes.c_int, [ctypes.c_int, _P(c_void_p)]),
     "mfe_ctx_destroy": (ctypes.c_int, [c_void_p]),
     "mfe_set_stream": (ctypes.c_int, [c_void_p, c_void_p]),
+    "mfe_use_own_stream": (ctypes.c_int, [c_void_p]),
     "mfe_synchronize": (ctypes.c_int, [c_void_p]),
     "mfe_last_error_string": (ctypes.c_char_p, [c_void_p]),
     "mfe_status_string": (ctypes.c_char_p, [ctypes.c_int]),

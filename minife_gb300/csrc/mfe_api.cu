@@ -162,14 +162,26 @@ mfe_status mfe_ctx_destroy(mfe_ctx* ctx)
   return MFE_OK;
 }
 
-mfe_status mfe_set_stream(mfe_ctx* ctx, void* stream)
+static void switch_stream(mfe_ctx* ctx, cudaStream_t s)
 {
-  if (!ctx) return MFE_BAD_ARG;
-  cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->own_stream;
   if (s != ctx->stream) {
+    // work already queued on the old stream completes before the switch
     cudaStreamSynchronize(ctx->stream);
     ctx->stream = s;
   }
+}
+
+mfe_status mfe_set_stream(mfe_ctx* ctx, void* stream)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  switch_stream(ctx, static_cast<cudaStream_t>(stream));
+  return MFE_OK;
+}
+
+mfe_status mfe_use_own_stream(mfe_ctx* ctx)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  switch_stream(ctx, ctx->own_stream);
   return MFE_OK;
 }
 
