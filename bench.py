@@ -1,0 +1,384 @@
+"""Benchmark: miniFE CG solve to a 1e-8 relative residual on one GB300.
+
+Workload (the FP64 GPU configuration): nx = ny = nz = 256 Hex8 box, 16,974,593
+unknowns, 454,756,609 CSR nonzeros (FP64 values, int32 columns), reference
+boundary conditions, unpreconditioned CG from x0 = 0 to ||r|| <= 1e-8 ||r0||.
+A "step" is one full CG solve on the assembled system (assembly is timed
+separately and reported beside it).  The matrix (5.5 GB) is far larger than
+the 129 MB L2, so no L2 flush is needed between steps.
+
+Keys beyond the base contract:
+  e2e          the same solve through the host drop-in call
+               (mfe_cg_solve_host: host CSR and b in pinned memory copied to the
+               device inside the timed region, x copied back)
+  roofline     the dominant kernel (the CSR SpMV with fused p.Ap) timed with
+               CUDA events on its stream against MEASURED_PEAKS.json's HBM copy
+               bandwidth; traffic from the committed ncu summary
+  cpu_baseline the OpenMP CG port (oracle/cpu_baseline.c) on the host cores,
+               a bounded sample of iterations scaled to the solve's count
+  --impl reference  times that CPU baseline as the reference arm.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+DIMS = (256, 256, 256)
+TOL = 1e-8
+METRIC = "CG time to 1e-8 rel. residual, mixed vs FP64 on GB300; SpMV GB/s vs HBM roof"
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def traffic_from_profile():
+    """Per-launch DRAM bytes of the SpMV kernel from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "spmv_traffic.json")
+    try:
+        with open(path) as f:
+            d = json.load(f)
+        return float(d["bytes_per_launch_256"])
+    except Exception:
+        return None
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled while the timed region runs."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        sm.sort()
+        med = sm[len(sm) // 2] if sm else None
+        return {"sm_mhz": med, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(ngpus):
+    import torch
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if torch.cuda.is_available():
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    elif torch.cuda.is_available():
+        torch.cuda.set_device(0)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, v):
+    if world == 1:
+        return v
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# --------------------------------------------------------------------------
+# CPU baseline (oracle/cpu_baseline.c, OpenMP port of the openmp/ variant)
+# --------------------------------------------------------------------------
+def cpu_cg_sample(ro, cols, vals, b, iters):
+    """Run `iters` CG iterations with the OpenMP baseline; returns (seconds,
+    threads)."""
+    import numpy as np
+    from oracle import oracle as O
+    L = O.cpubase()
+    x = np.zeros(b.size)
+    import ctypes
+    nr = ctypes.c_double()
+    t0 = time.perf_counter()
+    L.cpub_cg_solve(b.size, ro, cols, vals, b, x, int(iters), 0.0, 0, ctypes.byref(nr))
+    t1 = time.perf_counter()
+    return t1 - t0, int(L.cpub_num_threads())
+
+
+def host_system(A, b):
+    """Copy the device system to host numpy arrays (bit-identical to the
+    oracle's assembly, which the parity tests establish)."""
+    import numpy as np
+    ro = A.row_offsets.cpu().numpy()
+    cols = A.packed_cols.cpu().numpy()
+    vals = A.packed_coefs.cpu().numpy()
+    bh = b.cpu().numpy()
+    return (np.ascontiguousarray(ro), np.ascontiguousarray(cols), np.ascontiguousarray(vals),
+            np.ascontiguousarray(bh))
+
+
+def run_reference(args):
+    """Reference arm: the CPU CG on the host cores, bounded samples scaled to
+    the full solve's iteration count."""
+    import numpy as np
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    if rank != 0:
+        return 0
+    import minife_gb300 as M
+    from oracle import oracle as O
+    O.build()
+    A, b = M.build_system(*DIMS)
+    ro, cols, vals, bh = host_system(A, b)
+    iters_full = args.ref_iters
+    del A, b
+    torch.cuda.empty_cache()
+    per = []
+    threads = 1
+    for i in range(args.warmup + args.steps):
+        dt, threads = cpu_cg_sample(ro, cols, vals, bh, args.ref_sample)
+        if i >= args.warmup:
+            per.append(dt / args.ref_sample)
+    per_it = sum(per) / len(per)
+    value = per_it * iters_full
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (miniFE box, generated)",
+        "config": {"workload": "cg_f64_256^3_to_1e-8_rel", "nx": DIMS[0], "ny": DIMS[1],
+                   "nz": DIMS[2], "iterations": iters_full},
+        "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
+                         "sample": "%d CG iterations per step on the 256^3 system, %d steps, "
+                                   "scaled to %d iterations" % (args.ref_sample, args.steps,
+                                                                iters_full)},
+        "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# --------------------------------------------------------------------------
+# GPU arm
+# --------------------------------------------------------------------------
+def run_gpu(args):
+    import numpy as np
+    import torch
+    world, rank, local = dist_setup(args.gpus)
+    import minife_gb300 as M
+    dev = torch.cuda.current_device()
+    n, nnz = M.box_dims(*DIMS)
+    stream = torch.cuda.current_stream()
+
+    # assembly (timed separately, like the reference's "FE assembly Time")
+    A = M.CSRMatrix.empty_box(*DIMS)
+    b = torch.empty(n, dtype=torch.float64, device="cuda")
+    M.assemble_FE_data(*DIMS, A, b, impose_bc=True)
+    torch.cuda.synchronize()
+    ta = []
+    for _ in range(2):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        M.assemble_FE_data(*DIMS, A, b, impose_bc=True)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ta.append(e0.elapsed_time(e1) * 1e-3)
+    t_assembly = min(ta)
+
+    x = torch.zeros_like(b)
+    for _ in range(args.warmup):
+        x.zero_()
+        res = M.cg_solve(A, b, x, max_iter=5000, tol=TOL, tol_mode="relative")
+    torch.cuda.synchronize()
+
+    sampler = ClockSampler(dev) if rank == 0 else None
+    if sampler:
+        sampler.start()
+    barrier(world)
+    torch.cuda.synchronize()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    iters = []
+    for _ in range(args.steps):
+        x.zero_()
+        res = M.cg_solve(A, b, x, max_iter=5000, tol=TOL, tol_mode="relative")
+        iters.append(res.num_iters)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier(world)
+    t_total = e0.elapsed_time(e1) * 1e-3
+    t_step = max_over_ranks(world, t_total / args.steps)
+    rel = res.normr / res.normr0
+    final_rel = res.final_resid / res.normr0
+    rc, err = M.verify_solution(*DIMS, x)
+
+    # dominant kernel: the CG's SpMV (with fused p.Ap), timed alone on the
+    # same stream with CUDA events
+    p = torch.randn(n, dtype=torch.float64, device="cuda")
+    Ap = torch.empty_like(p)
+    for _ in range(3):
+        M.matvec_and_dot(A, p, Ap)
+    torch.cuda.synchronize()
+    R = 20
+    k0 = torch.cuda.Event(enable_timing=True)
+    k1 = torch.cuda.Event(enable_timing=True)
+    k0.record(stream)
+    for _ in range(R):
+        M.matvec(A, p, Ap)
+    k1.record(stream)
+    torch.cuda.synchronize()
+    t_spmv = k0.elapsed_time(k1) * 1e-3 / R
+    clocks = sampler.stop() if sampler else None
+    spmv_bytes = nnz * (8 + 4) + (n + 1) * 4 + 2 * n * 8
+    iter_bytes = nnz * (8 + 4) + (n + 1) * 4 + 11 * n * 8
+    peak, peak_kind = peaks()
+    achieved = spmv_bytes / t_spmv / 1e9
+    traffic = traffic_from_profile()
+
+    # e2e through the host drop-in call (pinned host CSR, copies inside)
+    e2e = None
+    if not args.no_e2e:
+        ro_h = A.row_offsets.cpu().pin_memory()
+        cols_h = A.packed_cols.cpu().pin_memory()
+        vals_h = A.packed_coefs.cpu().pin_memory()
+        b_h = b.cpu().pin_memory()
+        x_h = torch.zeros(n, dtype=torch.float64).pin_memory()
+        M.cg_solve_host(ro_h, cols_h, vals_h, b_h, x_h, max_iter=5000, tol=TOL,
+                        tol_mode="relative")
+        barrier(world)
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            x_h.zero_()
+            r2 = M.cg_solve_host(ro_h, cols_h, vals_h, b_h, x_h, max_iter=5000, tol=TOL,
+                                 tol_mode="relative")
+        t1 = time.perf_counter()
+        barrier(world)
+        t_e2e = max_over_ranks(world, (t1 - t0) / args.steps)
+        h2d = 4 * (n + 1) + 4 * nnz + 8 * nnz + 8 * n + 8 * n
+        e2e = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": 8 * n, "iterations": r2.num_iters}
+        del ro_h, cols_h, vals_h
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ro, cols, vals, bh = host_system(A, b)
+        dt, threads = cpu_cg_sample(ro, cols, vals, bh, args.cpu_sample)
+        per_it = dt / args.cpu_sample
+        cpu = {"value": per_it * res.num_iters, "unit": "s", "cores": threads, "kind": "port",
+               "sample": "%d OpenMP CG iterations on the 256^3 system, scaled to %d iterations"
+                         % (args.cpu_sample, res.num_iters)}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": t_step, "unit": "s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_step * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (miniFE 256^3 box generated on the device; matrix 5.5 GB > L2, "
+                    "no flush needed)",
+            "config": {"workload": "cg_f64_256^3_to_1e-8_rel", "nx": DIMS[0], "ny": DIMS[1],
+                       "nz": DIMS[2], "rows": n, "nnz": nnz, "tol_rel": TOL,
+                       "l2": "inputs larger than L2", "parallelism": "replicas" if world > 1
+                       else "single"},
+            "iterations": res.num_iters,
+            "final_rel_resid": final_rel, "reported_rel_normr": rel,
+            "analytic_check": {"max_err": err, "passed": rc == 0},
+            "ms_per_iter": t_step / res.num_iters * 1e3,
+            "cg_effective_gbs": iter_bytes * res.num_iters / t_step / 1e9,
+            "assembly_s": t_assembly,
+            "spmv_f64_gbs": achieved,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": traffic,
+                         "kernel": "k_spmv_tiled<double> (FP64 CSR SpMV)",
+                         "algorithmic_bytes": spmv_bytes, "peak_kind": peak_kind},
+            "e2e": e2e,
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps * (3 * res.num_iters + 2),
+            "clocks": clocks,
+        }
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--cpu-sample", type=int, default=20)
+    ap.add_argument("--ref-sample", type=int, default=10)
+    ap.add_argument("--ref-iters", type=int, default=401,
+                    help="CG iterations of the 256^3 solve to 1e-8 (the GPU solve's count)")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

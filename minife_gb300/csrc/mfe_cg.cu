@@ -296,13 +296,18 @@ static mfe_status build_graph(mfe_ctx* ctx, const mfe_csr* A, double* x, const C
 {
   mfe_cg_graph* g = new mfe_cg_graph();
   const int64_t n = A->nrows;
-  cudaStream_t s = ctx->stream;
+  // capture on the context's own stream (the legacy default stream cannot be
+  // captured); the executable graph is launched on ctx->stream afterwards
+  cudaStream_t run_stream = ctx->stream;
+  cudaStream_t s = ctx->own_stream;
+  ctx->stream = s;
   auto bail = [&](cudaError_t e, const char* where) {
     cudaStreamCaptureStatus cs;
     if (cudaStreamIsCapturing(s, &cs) == cudaSuccess && cs != cudaStreamCaptureStatusNone) {
       cudaGraph_t tmp;
       cudaStreamEndCapture(s, &tmp);
     }
+    ctx->stream = run_stream;
     cg_graph_destroy(g);
     cudaGetLastError();
     return cuda_fail(ctx, e, where);
@@ -344,12 +349,14 @@ static mfe_status build_graph(mfe_ctx* ctx, const mfe_csr* A, double* x, const C
   if (st == MFE_OK) st = launch_cg_update(ctx, n, x, B, rb, g->handle, 1);
   e = cudaStreamEndCapture(s, &body);
   if (st != MFE_OK) {
+    ctx->stream = run_stream;
     cg_graph_destroy(g);
     return st;
   }
   if (e != cudaSuccess) return bail(e, "cudaStreamEndCapture(body)");
   e = cudaGraphInstantiate(&g->exec, g->graph, 0);
   if (e != cudaSuccess) return bail(e, "cudaGraphInstantiate");
+  ctx->stream = run_stream;
   *out = g;
   return MFE_OK;
 }

@@ -51,23 +51,24 @@ struct SpmvParams {
   unsigned* err;
 };
 
-// Row sum: exactly one FMA per nonzero, in column order.
-template <typename T>
+// Row sum with one FMA per nonzero.  Rows of up to LMAX entries run the same
+// fully unrolled, predicated code (no divergence between the 27-entry
+// interior rows and the 8/12/18-entry boundary rows of a warp), and two
+// interleaved partial sums (even / odd entries) halve the dependent-FMA
+// chain, which the FP64 pipe's long latency otherwise exposes; one extra add
+// joins them.  Longer rows continue in a plain loop.
+template <typename T, int LMAX>
 __device__ __forceinline__ T row_dot(const T* __restrict__ rv, const int32_t* __restrict__ rc,
                                      int len, const T* __restrict__ x)
 {
-  T sum = T(0);
-  if (len == 27) {
-    T xv[27];
+  T s0 = T(0), s1 = T(0);
 #pragma unroll
-    for (int k = 0; k < 27; ++k) xv[k] = __ldg(&x[rc[k]]);
-#pragma unroll
-    for (int k = 0; k < 27; ++k) sum = fma(rv[k], xv[k], sum);
-  } else {
-#pragma unroll 4
-    for (int k = 0; k < len; ++k) sum = fma(rv[k], __ldg(&x[rc[k]]), sum);
+  for (int k = 0; k < LMAX; k += 2) {
+    if (k < len) s0 = fma(rv[k], __ldg(&x[rc[k]]), s0);
+    if (k + 1 < LMAX && k + 1 < len) s1 = fma(rv[k + 1], __ldg(&x[rc[k + 1]]), s1);
   }
-  return sum;
+  for (int k = LMAX; k < len; ++k) s0 = fma(rv[k], __ldg(&x[rc[k]]), s0);
+  return s0 + s1;
 }
 
 template <int MODE>
@@ -199,7 +200,7 @@ __global__ void __launch_bounds__(ROWS) k_spmv_tiled(SpmvParams<T> P)
       const int len = rb - ra;
       const T* rv = sv + (size_t)s * P.cap + (ra - s_base_v[s]);
       const int32_t* rc = sc + (size_t)s * P.cap + (ra - s_base_c[s]);
-      const T sum = row_dot<T>(rv, rc, len, P.x);
+      const T sum = row_dot<T, 27>(rv, rc, len, P.x);
       if (MODE == SPMV_RESID) {
         const double rr = P.b[r] - (double)sum;
         P.y[r] = (T)rr;
@@ -321,14 +322,25 @@ static size_t tiled_smem(int max_len)
 }
 
 template <typename T, int MODE>
-static cudaError_t configure_tiled()
+static cudaError_t configure_one()
 {
-  static bool done = false;
-  if (done) return cudaSuccess;
-  cudaError_t e = cudaFuncSetAttribute(k_spmv_tiled<T, kTileRows, kStages, MODE>,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)tiled_smem<T>(kMaxTileRowLen));
-  if (e == cudaSuccess) done = true;
+  return cudaFuncSetAttribute(k_spmv_tiled<T, kTileRows, kStages, MODE>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)tiled_smem<T>(kMaxTileRowLen));
+}
+
+// Shared-memory opt-in for every tiled instantiation, once per device (a
+// function attribute, so it is set before any stream capture uses them).
+static cudaError_t configure_tiled(int device)
+{
+  static bool done[64] = {};
+  if (device >= 0 && device < 64 && done[device]) return cudaSuccess;
+  cudaError_t e = configure_one<double, SPMV_PLAIN>();
+  if (e == cudaSuccess) e = configure_one<double, SPMV_DOT>();
+  if (e == cudaSuccess) e = configure_one<double, SPMV_RESID>();
+  if (e == cudaSuccess) e = configure_one<float, SPMV_PLAIN>();
+  if (e == cudaSuccess) e = configure_one<float, SPMV_DOT>();
+  if (e == cudaSuccess && device >= 0 && device < 64) done[device] = true;
   return e;
 }
 
@@ -397,7 +409,7 @@ static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, con
   if (cg) P.err = &cg->err;
   if (A->nrows == 0) return MFE_OK;
   if (max_len <= kMaxTileRowLen) {
-    MFE_CUDA_TRY(ctx, (configure_tiled<T, MODE>()));
+    MFE_CUDA_TRY(ctx, configure_tiled(ctx->device));
     const size_t smem = tiled_smem<T>(std::max(max_len, 1));
     const int64_t ntiles = ceil_div(A->nrows, kTileRows);
     const int grid = (int)std::max<int64_t>(
