@@ -26,6 +26,7 @@ SOURCES = {
     "mfe_api.cu": [],
     "mfe_assemble.cu": ["-fmad=false"],
     "mfe_spmv.cu": [],
+    "mfe_spmv_box.cu": [],
     "mfe_cg.cu": [],
 }
 

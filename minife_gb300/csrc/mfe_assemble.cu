@@ -16,9 +16,12 @@
 //      accumulators, applies both Dirichlet passes in registers, and writes
 //      the CSR row (staged through shared memory for coalescing).
 // No atomics: every coefficient is summed in the reference's element order.
+#include <algorithm>
 #include <cstdio>
+#include <cstring>
 #include <vector>
 
+#include "mfe_box.cuh"
 #include "mfe_common.cuh"
 #include "mfe_hex8.cuh"
 #include "mfe_internal.h"
@@ -28,28 +31,8 @@ namespace mfe {
 __constant__ Hex8Tables c_hex8;
 
 // ---------------------------------------------------------------------------
-// closed-form 27-point structure
+// closed-form 27-point structure (offsets: mfe_box.cuh)
 // ---------------------------------------------------------------------------
-// Nonzeros contributed by rows with coordinate < i along a dimension of n
-// nodes: sum_{j<i} (1 + [j>0] + [j<n-1]).
-__host__ __device__ __forceinline__ int64_t pre_count(int64_t i, int64_t n)
-{
-  return i + (i > 0 ? i - 1 : 0) + (i < n - 1 ? i : n - 1);
-}
-__host__ __device__ __forceinline__ int nbr(int i, int n)
-{
-  return 1 + (i > 0) + (i < n - 1);
-}
-// CSR offset of node (ix, iy, iz) in the Nx x Ny x Nz node box
-// (generate_matrix_structure.hpp:98-125 counts these one row at a time).
-__host__ __device__ __forceinline__ int64_t row_offset(int ix, int iy, int iz, int Nx, int Ny,
-                                                       int Nz)
-{
-  const int64_t Sx = 3 * (int64_t)Nx - 2, Sy = 3 * (int64_t)Ny - 2;
-  return pre_count(iz, Nz) * Sy * Sx + (int64_t)nbr(iz, Nz) * pre_count(iy, Ny) * Sx +
-         (int64_t)nbr(iz, Nz) * nbr(iy, Ny) * pre_count(ix, Nx);
-}
-
 int64_t box_nnz(int nx, int ny, int nz)
 {
   return (3 * (int64_t)(nx + 1) - 2) * (3 * (int64_t)(ny + 1) - 2) * (3 * (int64_t)(nz + 1) - 2);

@@ -372,6 +372,15 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   int max_len = 0;
   MFE_TRY(ensure_max_row_len(ctx, &A, &max_len));
   A.max_row_len = max_len;
+  if (!csr_is_box(&A)) {
+    // a CSR without box dimensions may still be a miniFE box matrix (e.g. one
+    // handed over through the host drop-in call): recognise it once per solve
+    int bx, by, bz;
+    MFE_TRY(detect_box(ctx, &A, &bx, &by, &bz));
+    A.box_nx = bx;
+    A.box_ny = by;
+    A.box_nz = bz;
+  }
 
   CgBufs B;
   B.r = static_cast<double*>(workspace(ctx, "cg.r", sizeof(double) * std::max<int64_t>(n, 1)));
@@ -415,14 +424,17 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   }
 
   // (re)build the graph when the operands changed
-  const void* key[10] = {A.row_offsets, A.cols, A.vals, x, b, B.r, B.p, B.Ap, B.st, ctx->stream};
+  const void* key[10] = {A.row_offsets, A.cols, A.vals, x, b, B.r, B.p, B.Ap, B.st,
+                         (const void*)(uintptr_t)(((int64_t)A.box_nx << 42) ^
+                                                  ((int64_t)A.box_ny << 21) ^ A.box_nz)};
   mfe_cg_graph* g = ctx->cg_graph;
-  if (!g || g->n != n || memcmp(g->key, key, sizeof(key)) != 0) {
+  if (!g || g->n != n || g->stream != ctx->stream || memcmp(g->key, key, sizeof(key)) != 0) {
     cg_graph_destroy(g);
     ctx->cg_graph = nullptr;
     MFE_TRY(build_graph(ctx, &A, x, B, rb, &g));
     memcpy(g->key, key, sizeof(key));
     g->n = n;
+    g->stream = ctx->stream;
     ctx->cg_graph = g;
   }
 

@@ -76,6 +76,16 @@ mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
                        const DotSink* sink, const double* resid_b, void* cg_state);
 mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y);
 
+// ---- box-structured SpMV (mfe_spmv_box.cu) ----
+// True when A carries box dimensions consistent with its sizes (the caller
+// vouches that its CSR layout is the 27-point box's).
+bool csr_is_box(const mfe_csr* A);
+// Infer box dimensions from row 0 and verify every row offset and column
+// against the closed form; *nx = *ny = *nz = 0 when A is not a box matrix.
+mfe_status detect_box(mfe_ctx* ctx, const mfe_csr* A, int* nx, int* ny, int* nz);
+mfe_status launch_spmv_box(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
+                           const DotSink* sink, const double* resid_b, void* cg_state);
+
 // ---- BLAS-1 and CG (mfe_cg.cu) ----
 mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
                       double* dev_out);

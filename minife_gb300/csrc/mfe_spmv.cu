@@ -31,6 +31,8 @@ namespace mfe {
 
 constexpr int kMaxTileRowLen = 32;
 
+static bool aligned16(const void* p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
 enum SpmvMode { SPMV_PLAIN = 0, SPMV_DOT = 1, SPMV_RESID = 2 };
 
 template <typename T>
@@ -57,15 +59,51 @@ struct SpmvParams {
 // interleaved partial sums (even / odd entries) halve the dependent-FMA
 // chain, which the FP64 pipe's long latency otherwise exposes; one extra add
 // joins them.  Longer rows continue in a plain loop.
+//
+// All LMAX column/value/x loads are issued unconditionally before the first
+// FMA (indices past the row end are clamped to its last entry, so every load
+// stays inside the row), letting the 27 x-gathers overlap; the FMAs past the
+// row end are discarded by a select, so the sum is exactly that of the row's
+// own entries.
+// Read-only-path gathers written as volatile asm: the compiler treats
+// __ldg results as rematerialisable and sinks each gather next to its FMA,
+// which serialises the gathers' latency; volatile loads stay where they are
+// issued, so all of a row's gathers are in flight together.
+__device__ __forceinline__ double ld_gather(const double* p)
+{
+  double v;
+  asm volatile("ld.global.nc.f64 %0, [%1];" : "=d"(v) : "l"(p));
+  return v;
+}
+__device__ __forceinline__ float ld_gather(const float* p)
+{
+  float v;
+  asm volatile("ld.global.nc.f32 %0, [%1];" : "=f"(v) : "l"(p));
+  return v;
+}
+
 template <typename T, int LMAX>
 __device__ __forceinline__ T row_dot(const T* __restrict__ rv, const int32_t* __restrict__ rc,
                                      int len, const T* __restrict__ x)
 {
+  if (len <= 0) return T(0);
+  int32_t c[LMAX];
+  T xv[LMAX], v[LMAX];
+#pragma unroll
+  for (int k = 0; k < LMAX; ++k) c[k] = rc[min(k, len - 1)];
+#pragma unroll
+  for (int k = 0; k < LMAX; ++k) xv[k] = ld_gather(&x[c[k]]);
+#pragma unroll
+  for (int k = 0; k < LMAX; ++k) v[k] = rv[min(k, len - 1)];
   T s0 = T(0), s1 = T(0);
 #pragma unroll
   for (int k = 0; k < LMAX; k += 2) {
-    if (k < len) s0 = fma(rv[k], __ldg(&x[rc[k]]), s0);
-    if (k + 1 < LMAX && k + 1 < len) s1 = fma(rv[k + 1], __ldg(&x[rc[k + 1]]), s1);
+    const T t0 = fma(v[k], xv[k], s0);
+    s0 = (k < len) ? t0 : s0;
+    if (k + 1 < LMAX) {
+      const T t1 = fma(v[k + 1], xv[k + 1], s1);
+      s1 = (k + 1 < len) ? t1 : s1;
+    }
   }
   for (int k = LMAX; k < len; ++k) s0 = fma(rv[k], __ldg(&x[rc[k]]), s0);
   return s0 + s1;
@@ -304,29 +342,54 @@ __global__ void __launch_bounds__(256)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-constexpr int kTileRows = 128;
 constexpr int kStages = 2;
+
+// Rows per tile (= threads per CTA): 128 by default; MFE_SPMV_ROWS selects
+// 64 or 256 for launch-shape sweeps.
+static int tile_rows()
+{
+  static int rows = 0;
+  if (rows == 0) {
+    rows = 128;
+    if (const char* v = getenv("MFE_SPMV_ROWS")) {
+      const int r = atoi(v);
+      if (r == 64 || r == 128 || r == 256) rows = r;
+    }
+  }
+  return rows;
+}
 
 // Stage capacity (elements) for rows of at most max_len nonzeros: the tile's
 // nonzeros plus the 16-byte alignment slack at both ends, kept a multiple of 4
 // so every stage starts 16-byte aligned.
-static int tile_cap(int max_len)
+static int tile_cap(int rows, int max_len)
 {
-  return ((kTileRows * max_len + 8) + 3) & ~3;
+  return ((rows * max_len + 8) + 3) & ~3;
 }
 
 template <typename T>
-static size_t tiled_smem(int max_len)
+static size_t tiled_smem(int rows, int max_len)
 {
-  return (size_t)kStages * tile_cap(max_len) * (sizeof(T) + sizeof(int32_t));
+  return (size_t)kStages * tile_cap(rows, max_len) * (sizeof(T) + sizeof(int32_t));
 }
 
-template <typename T, int MODE>
+template <typename T, int ROWS, int MODE>
 static cudaError_t configure_one()
 {
-  return cudaFuncSetAttribute(k_spmv_tiled<T, kTileRows, kStages, MODE>,
+  return cudaFuncSetAttribute(k_spmv_tiled<T, ROWS, kStages, MODE>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              (int)tiled_smem<T>(kMaxTileRowLen));
+                              (int)tiled_smem<T>(ROWS, kMaxTileRowLen));
+}
+
+template <int ROWS>
+static cudaError_t configure_rows()
+{
+  cudaError_t e = configure_one<double, ROWS, SPMV_PLAIN>();
+  if (e == cudaSuccess) e = configure_one<double, ROWS, SPMV_DOT>();
+  if (e == cudaSuccess) e = configure_one<double, ROWS, SPMV_RESID>();
+  if (e == cudaSuccess) e = configure_one<float, ROWS, SPMV_PLAIN>();
+  if (e == cudaSuccess) e = configure_one<float, ROWS, SPMV_DOT>();
+  return e;
 }
 
 // Shared-memory opt-in for every tiled instantiation, once per device (a
@@ -335,11 +398,9 @@ static cudaError_t configure_tiled(int device)
 {
   static bool done[64] = {};
   if (device >= 0 && device < 64 && done[device]) return cudaSuccess;
-  cudaError_t e = configure_one<double, SPMV_PLAIN>();
-  if (e == cudaSuccess) e = configure_one<double, SPMV_DOT>();
-  if (e == cudaSuccess) e = configure_one<double, SPMV_RESID>();
-  if (e == cudaSuccess) e = configure_one<float, SPMV_PLAIN>();
-  if (e == cudaSuccess) e = configure_one<float, SPMV_DOT>();
+  cudaError_t e = configure_rows<64>();
+  if (e == cudaSuccess) e = configure_rows<128>();
+  if (e == cudaSuccess) e = configure_rows<256>();
   if (e == cudaSuccess && device >= 0 && device < 64) done[device] = true;
   return e;
 }
@@ -358,10 +419,11 @@ static int tiled_ctas_per_sm(size_t smem)
 
 int spmv_grid(mfe_ctx* ctx, const mfe_csr* A)
 {
-  const int64_t ntiles = ceil_div(A->nrows, kTileRows);
+  const int rows = tile_rows();
+  const int64_t ntiles = ceil_div(A->nrows, rows);
   const int max_len = A->max_row_len > 0 ? A->max_row_len : kMaxTileRowLen;
-  const size_t smem =
-      A->dtype == MFE_F32 ? tiled_smem<float>(max_len) : tiled_smem<double>(max_len);
+  const size_t smem = A->dtype == MFE_F32 ? tiled_smem<float>(rows, max_len)
+                                          : tiled_smem<double>(rows, max_len);
   const int per_sm = tiled_ctas_per_sm(smem);
   return (int)std::max<int64_t>(1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * per_sm));
 }
@@ -399,7 +461,8 @@ static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, con
   P.x = x;
   P.y = y;
   P.b = b;
-  P.cap = tile_cap(std::max(max_len, 1));
+  const int rows = tile_rows();
+  P.cap = tile_cap(rows, std::max(max_len, 1));
   P.partials = sink ? sink->partials : nullptr;
   P.ticket = sink ? sink->ticket : nullptr;
   P.dot_out = sink ? sink->out : nullptr;
@@ -408,13 +471,18 @@ static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, con
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
   if (A->nrows == 0) return MFE_OK;
-  if (max_len <= kMaxTileRowLen) {
+  if (max_len <= kMaxTileRowLen && aligned16(A->vals) && aligned16(A->cols)) {
     MFE_CUDA_TRY(ctx, configure_tiled(ctx->device));
-    const size_t smem = tiled_smem<T>(std::max(max_len, 1));
-    const int64_t ntiles = ceil_div(A->nrows, kTileRows);
+    const size_t smem = tiled_smem<T>(rows, std::max(max_len, 1));
+    const int64_t ntiles = ceil_div(A->nrows, rows);
     const int grid = (int)std::max<int64_t>(
         1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * tiled_ctas_per_sm(smem)));
-    k_spmv_tiled<T, kTileRows, kStages, MODE><<<grid, kTileRows, smem, ctx->stream>>>(P);
+    if (rows == 64)
+      k_spmv_tiled<T, 64, kStages, MODE><<<grid, 64, smem, ctx->stream>>>(P);
+    else if (rows == 256)
+      k_spmv_tiled<T, 256, kStages, MODE><<<grid, 256, smem, ctx->stream>>>(P);
+    else
+      k_spmv_tiled<T, 128, kStages, MODE><<<grid, 128, smem, ctx->stream>>>(P);
     return check_launch(ctx, "k_spmv_tiled");
   }
   const int grid = (int)std::max<int64_t>(
@@ -426,6 +494,10 @@ static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, con
 mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
                        const DotSink* sink, const double* resid_b, void* cg_state)
 {
+  // bulk async copies need 16-byte aligned sources
+  if (csr_is_box(A) && aligned16(A->vals) && aligned16(x) &&
+      getenv("MFE_SPMV_GENERIC") == nullptr)
+    return launch_spmv_box(ctx, A, x, y, sink, resid_b, cg_state);
   int max_len = 0;
   MFE_TRY(ensure_max_row_len(ctx, A, &max_len));
   CgState* cg = static_cast<CgState*>(cg_state);

@@ -275,3 +275,50 @@ def test_assembly_256_properties():
     assert abs(bv - (1.0 / 256) ** 3) <= 1e-15
     del A, b
     torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("dims", [(17, 9, 11), (1, 1, 1), (2, 3, 1), (30, 30, 30)])
+def test_box_and_generic_spmv_agree(dims):
+    """The box-structured kernel (closed-form columns, staged x segments)
+    against the generic CSR kernel on the same arrays, FP64 and FP32."""
+    A, b = M.build_system(*dims)
+    G = M.CSRMatrix(A.row_offsets, A.packed_cols, A.packed_coefs)  # no box dims
+    ro, cols, vals, bo = O.build_system(*dims)
+    x = torch.randn(A.nrows, dtype=torch.float64, device=DEV)
+    y1 = M.matvec(A, x, torch.empty_like(x))
+    y2 = M.matvec(G, x, torch.empty_like(x))
+    yo = O.matvec(ro, cols, vals, host(x))
+    scale = O.matvec(ro, cols, np.abs(vals), np.abs(host(x))) + 1e-300
+    assert np.all(np.abs(host(y1) - yo) <= 30 * 2.0 ** -53 * scale)
+    assert np.all(np.abs(host(y2) - yo) <= 30 * 2.0 ** -53 * scale)
+    d1 = M.matvec_and_dot(A, x, y1)
+    assert abs(d1 - float(host(x) @ yo)) <= 1e-12 * float(np.abs(host(x)) @ np.abs(yo))
+    A32 = M.to_f32(A)
+    G32 = M.CSRMatrix(A32.row_offsets, A32.packed_cols, A32.packed_coefs)
+    x32 = x.float()
+    z1 = M.matvec(A32, x32, torch.empty_like(x32))
+    z2 = M.matvec(G32, x32, torch.empty_like(x32))
+    assert torch.allclose(z1, z2, rtol=1e-5, atol=1e-6 * float(z2.abs().max()))
+
+
+def test_box_detection_through_host_call():
+    """A box matrix handed over without dimensions (host drop-in call) is
+    recognised and solved; a perturbed column pattern is not mistaken for one."""
+    dims = (9, 7, 5)
+    ro, cols, vals, bo = O.build_system(*dims)
+    x = np.zeros(ro.size - 1)
+    res = M.cg_solve_host(ro, cols, vals, bo, x, max_iter=500, tol=1e-10, tol_mode="relative")
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=500, tol=1e-10, tol_mode=1)
+    assert abs(res.num_iters - it) <= 1
+    assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)
+    # swap two columns of one interior row (values swapped too): same
+    # operator, not the closed-form layout -> the generic kernel must be used
+    cols2, vals2 = cols.copy(), vals.copy()
+    r = 1 + (7 + 1) + (9 + 1) * (8 + 1)  # an interior-ish row
+    a = ro[r]
+    cols2[a], cols2[a + 1] = cols2[a + 1], cols2[a]
+    vals2[a], vals2[a + 1] = vals2[a + 1], vals2[a]
+    x2 = np.zeros(ro.size - 1)
+    res2 = M.cg_solve_host(ro, cols2, vals2, bo, x2, max_iter=500, tol=1e-10, tol_mode="relative")
+    assert abs(res2.num_iters - it) <= 1
+    assert np.linalg.norm(x2 - xo) <= 1e-9 * np.linalg.norm(xo)
