@@ -41,4 +41,15 @@ __host__ __device__ __forceinline__ int64_t row_offset_of(int64_t r, int Nx, int
   return row_offset((int)(r % Nx), (int)((r / Nx) % Ny), (int)(r / NxNy), Nx, Ny, Nz);
 }
 
+// 32-bit variant for rows < 2^31 (every box the library accepts).
+__host__ __device__ __forceinline__ int64_t row_offset_of32(int r, int Nx, int Ny, int Nz, int NxNy)
+{
+  if (r >= NxNy * Nz)
+    return (3 * (int64_t)Nx - 2) * (3 * (int64_t)Ny - 2) * (3 * (int64_t)Nz - 2);
+  const int iz = r / NxNy;
+  const int rem = r - iz * NxNy;
+  const int iy = rem / Nx;
+  return row_offset(rem - iy * Nx, iy, iz, Nx, Ny, Nz);
+}
+
 }  // namespace mfe

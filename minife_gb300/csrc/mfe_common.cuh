@@ -106,6 +106,14 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
                : "memory");
 }
 
+// Plain arrival (count 1), release semantics: prior shared-memory reads by
+// this thread are ordered before the phase can complete.
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar)
+{
+  asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar))
+               : "memory");
+}
+
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
 {
   uint32_t ok;
@@ -119,12 +127,26 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity)
   return ok != 0;
 }
 
+__device__ __forceinline__ uint64_t global_ns()
+{
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Longest a bounded wait may take before it gives up (nanoseconds).
+constexpr uint64_t kWaitLimitNs = 2000000000ull;
+
 // Bounded wait; returns false (and the caller records ERR_WAIT_TIMEOUT) if
-// the phase did not complete within kMaxPolls polls.
+// the phase did not complete within kWaitLimitNs (or kMaxPolls polls).
 __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity)
 {
-  for (unsigned i = 0; i < kMaxPolls; ++i)
+  if (mbar_try_wait(bar, parity)) return true;
+  const uint64_t t0 = global_ns();
+  for (unsigned i = 1; i < kMaxPolls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
+    if ((i & 63u) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
+  }
   return false;
 }
 

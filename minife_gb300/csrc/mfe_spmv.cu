@@ -132,7 +132,7 @@ __device__ __forceinline__ void spmv_epilogue(double total, CgState* cg, double*
     cg->k = 1;
     cg->num_iters = 0;
     cg->cont = (1 <= cg->max_iter) && (normr > tol_abs);
-    if (cg->record) cg->history[0] = normr;
+    if (cg->record) cg->history[0] = cg->history[1] = normr;
   }
 }
 

@@ -69,184 +69,197 @@ __device__ __forceinline__ void box_epilogue(double total, CgState* cg, double* 
     cg->k = 1;
     cg->num_iters = 0;
     cg->cont = (1 <= cg->max_iter) && (normr > tol_abs);
-    if (cg->record) cg->history[0] = normr;
+    if (cg->record) cg->history[0] = cg->history[1] = normr;
   }
 }
 
+// Warp-specialised pipeline: warp 0 is the producer (lane 0 stages tiles),
+// warps 1..C are consumers, one row per consumer thread (ROWS = 32 * C).
+// full[s] completes when stage s holds its tile (expect_tx + bulk copies);
+// empty[s] completes when all C consumer warps have finished reading it, so
+// the producer runs up to S tiles ahead without any CTA-wide barrier.
 template <typename T, int ROWS, int S, int MODE>
-__global__ void __launch_bounds__(ROWS) k_spmv_box(BoxParams<T> P)
+__global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
 {
+  constexpr int C = ROWS / 32;  // consumer warps
   extern __shared__ __align__(128) unsigned char smem[];
-  __shared__ uint64_t bar[S];
-  __shared__ int s_vbase[S];       // first staged value index of each stage
-  __shared__ int s_xbase[S][9];    // first staged x index of each segment
+  __shared__ uint64_t full[S], empty[S];
+  __shared__ int s_vbase[S];     // first staged value index of each stage
+  __shared__ int s_xbase[S][9];  // first staged x index of each segment
   __shared__ double red[32];
   constexpr int VA = 16 / sizeof(T);
   const size_t stage_elems = (size_t)P.capv + 9 * (size_t)P.capx;
   T* const st0 = reinterpret_cast<T*>(smem);
 
-  const int tid = threadIdx.x;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = (P.n + ROWS - 1) / ROWS;
-  if (tid == 0) {
-    for (int s = 0; s < S; ++s) mbar_init(&bar[s], 1);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], C);
+    }
     fence_mbar_init();
   }
   __syncthreads();
 
-  // producer: stage tile t (values + nine x segments) into stage s
-  auto issue = [&](int t, int s) {
-    T* sv = st0 + (size_t)s * stage_elems;
-    T* sx = sv + P.capv;
-    const int r0 = t * ROWS, r1 = min(P.n, r0 + ROWS);
-    const int64_t a = row_offset_of(r0, P.Nx, P.Ny, P.Nz);
-    const int64_t e = row_offset_of(r1, P.Nx, P.Ny, P.Nz);
-    const int64_t av = a & ~(int64_t)(VA - 1);
-    int64_t bv = min((e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
-    if (bv < av) bv = av;
-    unsigned bytes = 0;
-    bool ok = (max(bv, e) - av <= P.capv);
-    int64_t xlo[9], xbl[9], xhi[9];
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-      const int64_t off = (int64_t)(j / 3 - 1) * P.NxNy + (int64_t)(j % 3 - 1) * P.Nx;
-      int64_t lo = max((int64_t)r0 + off - 1, (int64_t)0);
-      int64_t hi = min((int64_t)r1 + off + 1, (int64_t)P.n);
-      if (hi < lo) hi = lo;
-      const int64_t lal = lo & ~(int64_t)(VA - 1);
-      int64_t bl = min((hi + VA - 1) & ~(int64_t)(VA - 1), (int64_t)P.n & ~(int64_t)(VA - 1));
-      if (bl < lal) bl = lal;
-      xlo[j] = lal;
-      xbl[j] = bl;
-      xhi[j] = hi;
-      ok = ok && (max(bl, hi) - lal <= P.capx);
-    }
-    if (!ok) {
-      atomicOr(P.err, ERR_TILE_OVERFLOW);
-      s_vbase[s] = (int)a;
-      for (int j = 0; j < 9; ++j) s_xbase[s][j] = 0;
-      mbar_arrive_expect_tx(&bar[s], 0);
-      return;
-    }
-    s_vbase[s] = (int)av;
-    for (int64_t k = bv; k < e; ++k) sv[k - av] = P.vals[k];
-    bytes += (unsigned)((bv - av) * sizeof(T));
-#pragma unroll
-    for (int j = 0; j < 9; ++j) {
-      s_xbase[s][j] = (int)xlo[j];
-      T* dx = sx + (size_t)j * P.capx;
-      for (int64_t k = xbl[j]; k < xhi[j]; ++k) dx[k - xlo[j]] = P.x[k];
-      bytes += (unsigned)((xbl[j] - xlo[j]) * sizeof(T));
-    }
-    fence_proxy_async_smem();
-    mbar_arrive_expect_tx(&bar[s], bytes);
-    if (bv > av) bulk_g2s(sv, P.vals + av, (unsigned)((bv - av) * sizeof(T)), &bar[s]);
-#pragma unroll
-    for (int j = 0; j < 9; ++j)
-      if (xbl[j] > xlo[j])
-        bulk_g2s(sx + (size_t)j * P.capx, P.x + xlo[j],
-                 (unsigned)((xbl[j] - xlo[j]) * sizeof(T)), &bar[s]);
-  };
-
-  if (tid == 0) {
-    for (int s = 0; s < S; ++s) {
-      const int t = blockIdx.x + s * gridDim.x;
-      if (t < ntiles) issue(t, s);
-    }
-  }
-
   double dacc = 0.0;
-  int it = 0;
   bool ok = true;
-  for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
-    const int s = it % S;
-    const unsigned parity = (unsigned)((it / S) & 1);
-    // row coordinates and offsets do not depend on the staged data
-    const int r = tile * ROWS + tid;
-    const bool active = r < P.n;
-    const int rr = active ? r : P.n - 1;
-    const int iz = rr / P.NxNy;
-    const int rem = rr - iz * P.NxNy;
-    const int iy = rem / P.Nx;
-    const int ix = rem - iy * P.Nx;
-    const int64_t roff = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
-    ok = mbar_wait_bounded(&bar[s], parity);
-    ok = __syncthreads_and(ok);
-    if (!ok) break;
-    if (active) {
-      const T* sv = st0 + (size_t)s * stage_elems;
-      const T* sx = sv + P.capv;
-      const T* rowv = sv + (roff - s_vbase[s]);
-      const bool vxm = ix > 0, vxp = ix < P.Nx - 1;
-      const bool vym = iy > 0, vyp = iy < P.Ny - 1;
-      const bool vzm = iz > 0, vzp = iz < P.Nz - 1;
-      const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp;
-      const int cxy = cx * cy;
-      // x[r] lives in the centre segment (j = 4) of every tile
-      const T* xc = sx + 4 * (size_t)P.capx + (r - s_xbase[s][4]);
-      T s0 = T(0), s1 = T(0);
-      int slot = 0;
+  if (warp == 0) {
+    // ---------------- producer ----------------
+    if (lane == 0) {
+      int it = 0;
+      unsigned issued[S];
+      for (int s = 0; s < S; ++s) issued[s] = 0;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
+        const int s = it % S;
+        if (it >= S) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / S) - 1) & 1));
+        if (!ok) break;
+        T* sv = st0 + (size_t)s * stage_elems;
+        T* sx = sv + P.capv;
+        const int r0 = tile * ROWS, r1 = min(P.n, r0 + ROWS);
+        const int64_t a = row_offset_of32(r0, P.Nx, P.Ny, P.Nz, P.NxNy);
+        const int64_t e = row_offset_of32(r1, P.Nx, P.Ny, P.Nz, P.NxNy);
+        const int64_t av = a & ~(int64_t)(VA - 1);
+        int64_t bv = min((e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
+        if (bv < av) bv = av;
+        bool fits = (max(bv, e) - av <= P.capv);
+        int xlo[9], xbl[9], xhi[9];
 #pragma unroll
-      for (int dz = -1; dz <= 1; ++dz) {
-        const bool vz = dz < 0 ? vzm : (dz > 0 ? vzp : true);
-        const int bz = dz < 0 ? 0 : (dz == 0 ? (int)vzm : (int)vzm + 1);
+        for (int j = 0; j < 9; ++j) {
+          const int off = (j / 3 - 1) * P.NxNy + (j % 3 - 1) * P.Nx;
+          const int lo = max(r0 + off - 1, 0);
+          int hi = min(r1 + off + 1, P.n);
+          if (hi < lo) hi = lo;
+          const int lal = lo & ~(VA - 1);
+          int bl = min((hi + VA - 1) & ~(VA - 1), P.n & ~(VA - 1));
+          if (bl < lal) bl = lal;
+          xlo[j] = lal;
+          xbl[j] = bl;
+          xhi[j] = hi;
+          fits = fits && (max(bl, hi) - lal <= P.capx);
+        }
+        ++issued[s];
+        if (!fits) {
+          // cannot happen for box dimensions the host accepted; record it
+          atomicOr(P.err, ERR_TILE_OVERFLOW);
+          s_vbase[s] = (int)a;
+          for (int j = 0; j < 9; ++j) s_xbase[s][j] = 0;
+          mbar_arrive_expect_tx(&full[s], 0);
+          continue;
+        }
+        s_vbase[s] = (int)av;
+        unsigned bytes = (unsigned)((bv - av) * sizeof(T));
+        for (int64_t k = bv; k < e; ++k) sv[k - av] = P.vals[k];
 #pragma unroll
-        for (int dy = -1; dy <= 1; ++dy) {
-          const bool vy = dy < 0 ? vym : (dy > 0 ? vyp : true);
-          const int by = dy < 0 ? 0 : (dy == 0 ? (int)vym : (int)vym + 1);
-          const int j = (dz + 1) * 3 + (dy + 1);
-          const int64_t off = (int64_t)dz * P.NxNy + (int64_t)dy * P.Nx;
-          const T* seg = sx + (size_t)j * P.capx + ((int64_t)r + off - s_xbase[s][j]);
-          const int pbase = bz * cxy + by * cx;
+        for (int j = 0; j < 9; ++j) {
+          s_xbase[s][j] = xlo[j];
+          T* dx = sx + (size_t)j * P.capx;
+          for (int k = xbl[j]; k < xhi[j]; ++k) dx[k - xlo[j]] = P.x[k];
+          bytes += (unsigned)((xbl[j] - xlo[j]) * sizeof(T));
+        }
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&full[s], bytes);
+        if (bv > av) bulk_g2s(sv, P.vals + av, (unsigned)((bv - av) * sizeof(T)), &full[s]);
 #pragma unroll
-          for (int dx = -1; dx <= 1; ++dx) {
-            const bool vx = dx < 0 ? vxm : (dx > 0 ? vxp : true);
-            const int bx = dx < 0 ? 0 : (dx == 0 ? (int)vxm : (int)vxm + 1);
-            const bool valid = vz && vy && vx;
-            // masked slots read the row's first value and x[r], both staged
-            // (the addresses are selected, so every load stays in bounds)
-            const T v = rowv[valid ? pbase + bx : 0];
-            const T xv = *(valid ? seg + dx : xc);
-            if (slot & 1) {
-              const T t1 = fma(v, xv, s1);
-              s1 = valid ? t1 : s1;
-            } else {
-              const T t0 = fma(v, xv, s0);
-              s0 = valid ? t0 : s0;
+        for (int j = 0; j < 9; ++j)
+          if (xbl[j] > xlo[j])
+            bulk_g2s(sx + (size_t)j * P.capx, P.x + xlo[j],
+                     (unsigned)((xbl[j] - xlo[j]) * sizeof(T)), &full[s]);
+      }
+      if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        // bounded drain: let the last copies issued into each stage land
+        for (int s = 0; s < S; ++s)
+          if (issued[s]) mbar_wait_bounded(&full[s], (issued[s] - 1) & 1u);
+      }
+    }
+  } else {
+    // ---------------- consumers ----------------
+    const int lr = (warp - 1) * 32 + lane;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int s = it % S;
+      // row coordinates and offsets do not depend on the staged data
+      const int r = tile * ROWS + lr;
+      const bool active = r < P.n;
+      const int rr = active ? r : P.n - 1;
+      const int iz = rr / P.NxNy;
+      const int rem = rr - iz * P.NxNy;
+      const int iy = rem / P.Nx;
+      const int ix = rem - iy * P.Nx;
+      const int64_t roff = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
+      if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        ok = false;
+        break;
+      }
+      if (active) {
+        const T* sv = st0 + (size_t)s * stage_elems;
+        const T* sx = sv + P.capv;
+        const T* rowv = sv + (roff - s_vbase[s]);
+        const bool vxm = ix > 0, vxp = ix < P.Nx - 1;
+        const bool vym = iy > 0, vyp = iy < P.Ny - 1;
+        const bool vzm = iz > 0, vzp = iz < P.Nz - 1;
+        const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp;
+        const int cxy = cx * cy;
+        // x[r] lives in the centre segment (j = 4) of every tile
+        const T* xc = sx + 4 * (size_t)P.capx + (r - s_xbase[s][4]);
+        T s0 = T(0), s1 = T(0);
+        int slot = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz) {
+          const bool vz = dz < 0 ? vzm : (dz > 0 ? vzp : true);
+          const int bz = dz < 0 ? 0 : (dz == 0 ? (int)vzm : (int)vzm + 1);
+#pragma unroll
+          for (int dy = -1; dy <= 1; ++dy) {
+            const bool vy = dy < 0 ? vym : (dy > 0 ? vyp : true);
+            const int by = dy < 0 ? 0 : (dy == 0 ? (int)vym : (int)vym + 1);
+            const int j = (dz + 1) * 3 + (dy + 1);
+            const int off = dz * P.NxNy + dy * P.Nx;
+            const T* seg = sx + (size_t)j * P.capx + (r + off - s_xbase[s][j]);
+            const int pbase = bz * cxy + by * cx;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+              const bool vx = dx < 0 ? vxm : (dx > 0 ? vxp : true);
+              const int bx = dx < 0 ? 0 : (dx == 0 ? (int)vxm : (int)vxm + 1);
+              const bool valid = vz && vy && vx;
+              // masked slots read the row's first value and x[r], both
+              // staged (the addresses are selected: every load is in bounds)
+              const T v = rowv[valid ? pbase + bx : 0];
+              const T xv = *(valid ? seg + dx : xc);
+              if (slot & 1) {
+                const T t1 = fma(v, xv, s1);
+                s1 = valid ? t1 : s1;
+              } else {
+                const T t0 = fma(v, xv, s0);
+                s0 = valid ? t0 : s0;
+              }
+              ++slot;
             }
-            ++slot;
           }
         }
-      }
-      const T sum = s0 + s1;
-      if (MODE == BOX_RESID) {
-        const double res = P.b[r] - (double)sum;
-        P.y[r] = (T)res;
-        dacc = fma(res, res, dacc);
+        const T sum = s0 + s1;
+        const T xr = xc[0];
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);  // stage s no longer read by this warp
+        if (MODE == BOX_RESID) {
+          const double res = P.b[r] - (double)sum;
+          P.y[r] = (T)res;
+          dacc = fma(res, res, dacc);
+        } else {
+          P.y[r] = sum;
+          if (MODE == BOX_DOT) dacc = fma((double)sum, (double)xr, dacc);
+        }
       } else {
-        P.y[r] = sum;
-        if (MODE == BOX_DOT) dacc = fma((double)sum, (double)xc[0], dacc);
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
       }
     }
-    __syncthreads();  // stage s fully consumed
-    if (tid == 0) {
-      const int t = tile + S * gridDim.x;
-      if (t < ntiles) issue(t, s);
-    }
-  }
-  if (!ok) {
-    if (tid == 0) {
-      atomicOr(P.err, ERR_WAIT_TIMEOUT);
-      for (int s = 0; s < S; ++s) {
-        const int j = it + s;
-        mbar_wait_bounded(&bar[j % S], (unsigned)((j / S) & 1));
-      }
-    }
-    return;
   }
   if (MODE != BOX_PLAIN) {
     const double bt = block_sum(dacc, red);
     double total;
-    if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && tid == 0)
+    if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0)
       box_epilogue<MODE>(total, P.cg, P.dot_out);
   }
 }
@@ -280,7 +293,7 @@ __global__ void k_check_box(int n, int Nx, int Ny, int Nz, const int32_t* __rest
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-constexpr int kBoxStages = 2;
+constexpr int kBoxStages = 3;
 
 static int box_rows()
 {
@@ -414,11 +427,11 @@ static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
   const int grid = (int)std::max<int64_t>(
       1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * box_ctas_per_sm(smem)));
   if (rows == 64)
-    k_spmv_box<T, 64, kBoxStages, MODE><<<grid, 64, smem, ctx->stream>>>(P);
+    k_spmv_box<T, 64, kBoxStages, MODE><<<grid, 64 + 32, smem, ctx->stream>>>(P);
   else if (rows == 256)
-    k_spmv_box<T, 256, kBoxStages, MODE><<<grid, 256, smem, ctx->stream>>>(P);
+    k_spmv_box<T, 256, kBoxStages, MODE><<<grid, 256 + 32, smem, ctx->stream>>>(P);
   else
-    k_spmv_box<T, 128, kBoxStages, MODE><<<grid, 128, smem, ctx->stream>>>(P);
+    k_spmv_box<T, 128, kBoxStages, MODE><<<grid, 128 + 32, smem, ctx->stream>>>(P);
   return check_launch(ctx, "k_spmv_box");
 }
 

@@ -234,8 +234,11 @@ def test_cg_nonzero_initial_guess_and_max_iter():
     res = M.cg_solve(A, b, x, max_iter=7)
     xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, x0=x0, max_iter=7)
     assert res.num_iters == it == 7
-    assert np.allclose(host(x), xo, rtol=1e-11, atol=1e-11)
-    assert abs(res.normr - nr) <= 1e-10 * nr
+    # an unconverged CG iterate amplifies rounding differences (FMA vs
+    # separate multiply-add, reduction order) by a few times per iteration;
+    # the converged solutions above agree to ~1e-15
+    assert np.allclose(host(x), xo, rtol=1e-9, atol=1e-9)
+    assert abs(res.normr - nr) <= 1e-9 * nr
 
 
 def test_element_gradient():
