@@ -293,55 +293,83 @@ __global__ void k_check_box(int n, int Nx, int Ny, int Nz, const int32_t* __rest
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
-constexpr int kBoxStages = 3;
+// Launch shape: rows per tile (64/128/256 = 2/4/8 consumer warps) and
+// pipeline stages (2..4).  Defaults per value type come from launch-shape
+// sweeps at 256^3; MFE_BOX_ROWS / MFE_BOX_STAGES override them for sweeps.
+struct BoxShape {
+  int rows, stages;
+};
 
-static int box_rows()
+template <typename T>
+static BoxShape box_shape()
 {
-  static int rows = 0;
-  if (rows == 0) {
-    rows = 128;
-    if (const char* v = getenv("MFE_BOX_ROWS")) {
-      const int r = atoi(v);
-      if (r == 64 || r == 128 || r == 256) rows = r;
-    }
+  BoxShape sh = sizeof(T) == 8 ? BoxShape{128, 3} : BoxShape{128, 3};
+  if (const char* v = getenv("MFE_BOX_ROWS")) {
+    const int r = atoi(v);
+    if (r == 64 || r == 128 || r == 256) sh.rows = r;
   }
-  return rows;
+  if (const char* v = getenv("MFE_BOX_STAGES")) {
+    const int st = atoi(v);
+    if (st >= 2 && st <= 4) sh.stages = st;
+  }
+  if (sh.rows == 256 && sh.stages > 3) sh.stages = 3;
+  return sh;
 }
 
 static int box_capv(int rows) { return ((rows * 27 + 8) + 3) & ~3; }
 static int box_capx(int rows) { return ((rows + 2 + 8) + 3) & ~3; }
 
 template <typename T>
-static size_t box_smem(int rows)
+static size_t box_smem(int rows, int stages)
 {
-  return (size_t)kBoxStages * ((size_t)box_capv(rows) + 9 * (size_t)box_capx(rows)) * sizeof(T);
+  return (size_t)stages * ((size_t)box_capv(rows) + 9 * (size_t)box_capx(rows)) * sizeof(T);
 }
 
-template <typename T, int ROWS, int MODE>
-static cudaError_t box_configure_one()
+// Calls F.template operator()<ROWS, S>() for the instantiated shape.
+template <typename F>
+static auto box_dispatch(BoxShape sh, F&& f)
 {
-  return cudaFuncSetAttribute(k_spmv_box<T, ROWS, kBoxStages, MODE>,
-                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)box_smem<T>(ROWS));
+  if (sh.rows == 64) {
+    if (sh.stages == 2) return f.template operator()<64, 2>();
+    if (sh.stages == 4) return f.template operator()<64, 4>();
+    return f.template operator()<64, 3>();
+  }
+  if (sh.rows == 256) {
+    if (sh.stages == 2) return f.template operator()<256, 2>();
+    return f.template operator()<256, 3>();
+  }
+  if (sh.stages == 2) return f.template operator()<128, 2>();
+  if (sh.stages == 4) return f.template operator()<128, 4>();
+  return f.template operator()<128, 3>();
 }
 
-template <int ROWS>
-static cudaError_t box_configure_rows()
+template <typename T, int MODE>
+static cudaError_t box_configure_mode()
 {
-  cudaError_t e = box_configure_one<double, ROWS, BOX_PLAIN>();
-  if (e == cudaSuccess) e = box_configure_one<double, ROWS, BOX_DOT>();
-  if (e == cudaSuccess) e = box_configure_one<double, ROWS, BOX_RESID>();
-  if (e == cudaSuccess) e = box_configure_one<float, ROWS, BOX_PLAIN>();
-  if (e == cudaSuccess) e = box_configure_one<float, ROWS, BOX_DOT>();
-  return e;
+  const int shapes[8][2] = {{64, 2},  {64, 3},  {64, 4},  {128, 2},
+                            {128, 3}, {128, 4}, {256, 2}, {256, 3}};
+  for (auto& rs : shapes) {
+    BoxShape sh{rs[0], rs[1]};
+    const size_t smem = box_smem<T>(sh.rows, sh.stages);
+    if (smem > 227 * 1024) continue;
+    cudaError_t e = box_dispatch(sh, [&]<int R, int S>() {
+      return cudaFuncSetAttribute(k_spmv_box<T, R, S, MODE>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    });
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
 }
 
 static cudaError_t box_configure(int device)
 {
   static bool done[64] = {};
   if (device >= 0 && device < 64 && done[device]) return cudaSuccess;
-  cudaError_t e = box_configure_rows<64>();
-  if (e == cudaSuccess) e = box_configure_rows<128>();
-  if (e == cudaSuccess) e = box_configure_rows<256>();
+  cudaError_t e = box_configure_mode<double, BOX_PLAIN>();
+  if (e == cudaSuccess) e = box_configure_mode<double, BOX_DOT>();
+  if (e == cudaSuccess) e = box_configure_mode<double, BOX_RESID>();
+  if (e == cudaSuccess) e = box_configure_mode<float, BOX_PLAIN>();
+  if (e == cudaSuccess) e = box_configure_mode<float, BOX_DOT>();
   if (e == cudaSuccess && device >= 0 && device < 64) done[device] = true;
   return e;
 }
@@ -411,9 +439,9 @@ static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
   P.x = x;
   P.y = y;
   P.b = b;
-  const int rows = box_rows();
-  P.capv = box_capv(rows);
-  P.capx = box_capx(rows);
+  const BoxShape sh = box_shape<T>();
+  P.capv = box_capv(sh.rows);
+  P.capx = box_capx(sh.rows);
   P.partials = sink ? sink->partials : nullptr;
   P.ticket = sink ? sink->ticket : nullptr;
   P.dot_out = sink ? sink->out : nullptr;
@@ -422,16 +450,14 @@ static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
   MFE_CUDA_TRY(ctx, box_configure(ctx->device));
-  const size_t smem = box_smem<T>(rows);
-  const int64_t ntiles = ceil_div(A->nrows, rows);
+  const size_t smem = box_smem<T>(sh.rows, sh.stages);
+  const int64_t ntiles = ceil_div(A->nrows, sh.rows);
   const int grid = (int)std::max<int64_t>(
       1, std::min<int64_t>(ntiles, (int64_t)ctx->sm_count * box_ctas_per_sm(smem)));
-  if (rows == 64)
-    k_spmv_box<T, 64, kBoxStages, MODE><<<grid, 64 + 32, smem, ctx->stream>>>(P);
-  else if (rows == 256)
-    k_spmv_box<T, 256, kBoxStages, MODE><<<grid, 256 + 32, smem, ctx->stream>>>(P);
-  else
-    k_spmv_box<T, 128, kBoxStages, MODE><<<grid, 128 + 32, smem, ctx->stream>>>(P);
+  box_dispatch(sh, [&]<int R, int S>() {
+    k_spmv_box<T, R, S, MODE><<<grid, R + 32, smem, ctx->stream>>>(P);
+    return 0;
+  });
   return check_launch(ctx, "k_spmv_box");
 }
 
