@@ -34,6 +34,9 @@ sys.path.insert(0, ROOT)
 DIMS = (256, 256, 256)
 TOL = 1e-8
 METRIC = "CG time to 1e-8 rel. residual, mixed vs FP64 on GB300; SpMV GB/s vs HBM roof"
+# FP64 FMA throughput of this machine's GB300 (597 G FMA/s = 1.19 TFLOP/s, 1.90
+# FMA/clk/SM), measured with an FMA-only kernel; see profiles/.
+FP64_PEAK_TFLOPS = 1.194
 
 
 def log(*a):
@@ -292,8 +295,11 @@ def run_gpu(args):
     torch.cuda.synchronize()
     t_spmv = k0.elapsed_time(k1) * 1e-3 / R
     clocks = sampler.stop() if sampler else None
-    spmv_bytes = nnz * (8 + 4) + (n + 1) * 4 + 2 * n * 8
-    iter_bytes = nnz * (8 + 4) + (n + 1) * 4 + 11 * n * 8
+    # the box-structured kernel reads the values only (columns and row
+    # offsets follow from the box): 8 bytes per nonzero + x and y once
+    spmv_bytes = nnz * 8 + 2 * n * 8
+    iter_bytes = nnz * 8 + 11 * n * 8
+    csr_equiv_bytes = nnz * (8 + 4) + (n + 1) * 4 + 2 * n * 8
     peak, peak_kind = peaks()
     achieved = spmv_bytes / t_spmv / 1e9
     traffic = traffic_from_profile()
@@ -351,8 +357,14 @@ def run_gpu(args):
             "spmv_f64_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_spmv_tiled<double> (FP64 CSR SpMV)",
-                         "algorithmic_bytes": spmv_bytes, "peak_kind": peak_kind},
+                         "kernel": "k_spmv_box<double> (FP64 box-structured CSR SpMV)",
+                         "algorithmic_bytes": spmv_bytes, "peak_kind": peak_kind + " (HBM copy)",
+                         "csr_equivalent_gbs": csr_equiv_bytes / t_spmv / 1e9,
+                         "fp64_fma": {"achieved_tflops": 2 * nnz / t_spmv / 1e12,
+                                      "peak_tflops": FP64_PEAK_TFLOPS,
+                                      "frac": 2 * nnz / t_spmv / 1e12 / FP64_PEAK_TFLOPS,
+                                      "note": "FP64 FMA pipe, the binding limit on GB300; "
+                                              "peak measured with an FMA-only kernel"}},
             "e2e": e2e,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps * (3 * res.num_iters + 2),

@@ -127,7 +127,9 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
           const int off = (j / 3 - 1) * P.NxNy + (j % 3 - 1) * P.Nx;
-          const int lo = max(r0 + off - 1, 0);
+          // the segment [lo, hi) is clamped to [0, n] at both ends: near the
+          // last rows r0 + off can lie past the end of x
+          const int lo = min(max(r0 + off - 1, 0), P.n);
           int hi = min(r1 + off + 1, P.n);
           if (hi < lo) hi = lo;
           const int lal = lo & ~(VA - 1);
@@ -303,7 +305,9 @@ struct BoxShape {
 template <typename T>
 static BoxShape box_shape()
 {
-  BoxShape sh = sizeof(T) == 8 ? BoxShape{128, 3} : BoxShape{128, 3};
+  // measured at 256^3 on GB300: FP64 0.833 ms at {128, 2} (3 CTAs/SM keep
+  // 12 consumer warps issuing FP64 FMAs), FP32 0.366 ms at {256, 2}
+  BoxShape sh = sizeof(T) == 8 ? BoxShape{128, 2} : BoxShape{256, 2};
   if (const char* v = getenv("MFE_BOX_ROWS")) {
     const int r = atoi(v);
     if (r == 64 || r == 128 || r == 256) sh.rows = r;
