@@ -17,6 +17,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "mfe_cgstate.cuh"
@@ -439,8 +440,24 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   }
 
   int status = MFE_OK;
+  // MFE_CG_EAGER=1 issues the same three kernels per iteration as ordinary
+  // launches from the host (one small state read per iteration) instead of
+  // the graph's device-side loop: identical work, visible to per-kernel
+  // profilers that do not descend into conditional graph nodes
+  const bool eager = getenv("MFE_CG_EAGER") != nullptr;
   for (int round = 0;; ++round) {
-    MFE_CUDA_TRY(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+    if (eager) {
+      for (;;) {
+        MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+        MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!hs->cont || hs->check_pending || hs->err) break;
+        MFE_TRY(launch_cg_p(ctx, n, B));
+        MFE_TRY(launch_cg_spmv(ctx, &A, B, rb));
+        MFE_TRY(launch_cg_update(ctx, n, x, B, rb, 0, 0));
+      }
+    } else {
+      MFE_CUDA_TRY(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+    }
     MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
     MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     if (hs->err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during CG");
