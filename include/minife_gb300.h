@@ -162,6 +162,28 @@ mfe_status mfe_matvec_and_dot(mfe_ctx* ctx, const mfe_csr* A, const void* x, voi
 mfe_status mfe_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
                    double* result);
 
+/* Allocation-free dot product, for callers that may not allocate device
+ * memory: applications whose GPU memory belongs to another allocator (a host
+ * program or framework that reserves the device in its own pool and lets no
+ * plugin allocate beside it) and latency-critical loops that cannot take the
+ * implicit synchronisation of cudaMalloc/cudaFree.  No counterpart in the
+ * reference (its dot, Vector_functions.hpp:194-226, runs on the host).
+ *
+ * *result (DEVICE pointer, one double) = x . y, accumulated in FP64 in fixed
+ * 8192-element chunks (deterministic for a given n), computed on the calling
+ * thread's current device and on `stream` (cudaStream_t, NULL = default
+ * stream); the call returns once the work is queued.  No context is needed
+ * and nothing is allocated: the chunk partial sums live in a 512 KiB device
+ * array inside the library (held by every GPU that loads the library until
+ * the process exits).  The first call on each device resolves that array's
+ * device address (cudaGetSymbolAddress) and should come before any stream
+ * capture.  n > MFE_DOT_NOALLOC_MAX_N returns MFE_BAD_ARG and launches
+ * nothing.  All calls share the array, so calls that overlap on the GPU race:
+ * order them on one stream. */
+#define MFE_DOT_NOALLOC_MAX_N ((int64_t)536870912) /* 2^29 elements */
+mfe_status mfe_dot_noalloc(int64_t n, const double* x, const double* y, double* result,
+                           void* stream);
+
 /* waxpby (ref/src/Vector_functions.hpp:127-150): w = alpha x + beta y. */
 mfe_status mfe_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x,
                       double beta, const double* y, double* w);

@@ -82,6 +82,7 @@ SIGNATURES = {
     "mfe_matvec_and_dot": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_void_p, c_void_p,
                                           _P(c_double)]),
     "mfe_dot": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p, _P(c_double)]),
+    "mfe_dot_noalloc": (ctypes.c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfe_waxpby": (ctypes.c_int, [c_void_p, c_int64, c_double, c_void_p, c_double, c_void_p,
                                   c_void_p]),
     "mfe_fused_waxpby": (ctypes.c_int, [c_void_p, c_int64, c_double, c_void_p, c_double,

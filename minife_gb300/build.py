@@ -27,6 +27,7 @@ SOURCES = {
     "mfe_assemble.cu": ["-fmad=false"],
     "mfe_spmv.cu": [],
     "mfe_spmv_box.cu": [],
+    "mfe_noalloc.cu": [],
     "mfe_cg.cu": [],
 }
 
