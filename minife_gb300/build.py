@@ -28,6 +28,7 @@ SOURCES = {
     "mfe_spmv.cu": [],
     "mfe_spmv_box.cu": [],
     "mfe_noalloc.cu": [],
+    "mfe_mixed.cu": [],
     "mfe_cg.cu": [],
 }
 

@@ -514,7 +514,7 @@ mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double
                          const mfe_cg_opts* opts, mfe_cg_result* res)
 {
   if (opts->precision == MFE_PREC_F64) return cg_f64(ctx, A, b, x, opts, res);
-  return fail(ctx, MFE_NOT_SUPPORTED, "mixed precision solver not built yet");
+  return cg_mixed(ctx, A, b, x, opts, res);
 }
 
 }  // namespace mfe

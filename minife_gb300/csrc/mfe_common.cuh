@@ -163,6 +163,31 @@ __device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, u
 }
 
 // ---------------------------------------------------------------------------
+// exact float -> double widening with integer operations only: on GB300 the
+// FP64 pipe (which also executes F2F.F64.F32) is the scarce resource, so the
+// FP64-accumulated dots of FP32 vectors spend their one FP64 operation per
+// element on the FMA.  Built from the IEEE-754 binary32/binary64 layouts:
+// the exponent is rebiased by 1023 - 127 = 896 and the 23-bit fraction moves
+// to the top of the 52-bit one.  Subnormal floats (magnitude < 2^-126)
+// contribute a signed zero.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double f2d_exact(float f)
+{
+  const uint32_t u = __float_as_uint(f);
+  const uint32_t e = (u >> 23) & 0xffu;
+  const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
+  const uint64_t frac = (uint64_t)(u & 0x7fffffu) << 29;
+  uint64_t bits;
+  if (e == 0u) bits = sign;
+  else if (e == 0xffu) bits = sign | 0x7ff0000000000000ull | frac;
+  else bits = sign | ((uint64_t)(e + 896u) << 52) | frac;
+  return __longlong_as_double((long long)bits);
+}
+
+__device__ __forceinline__ double widen(double v) { return v; }
+__device__ __forceinline__ double widen(float v) { return f2d_exact(v); }
+
+// ---------------------------------------------------------------------------
 // misc
 // ---------------------------------------------------------------------------
 template <typename T>

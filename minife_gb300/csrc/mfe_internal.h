@@ -85,6 +85,15 @@ bool csr_is_box(const mfe_csr* A);
 mfe_status detect_box(mfe_ctx* ctx, const mfe_csr* A, int* nx, int* ny, int* nz);
 mfe_status launch_spmv_box(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
                            const DotSink* sink, const double* resid_b, void* cg_state);
+// r32 = (float)(b - A64 x), ||b - A64 x||^2 (FP64) into sink->out; when gate
+// is set the launch does nothing unless *gate != 0 (read on the device).
+mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const double* x,
+                                   const double* b, float* r32, const DotSink* sink,
+                                   const int* gate);
+
+// ---- mixed-precision CG (mfe_mixed.cu) ----
+mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,
+                    const mfe_cg_opts* opts, mfe_cg_result* res);
 
 // ---- BLAS-1 and CG (mfe_cg.cu) ----
 mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,

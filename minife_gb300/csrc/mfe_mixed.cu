@@ -1,0 +1,424 @@
+// Mixed-precision CG: FP32 matrix, vectors and FMAs, FP64 dots, scalars and
+// solution, with reliable updates against the FP64 matrix.
+//
+// The reference solves in FP64 only (ref/src/cg_solve.hpp).  Here the inner
+// recurrence runs the reference's CG steps (p update, A p, p.Ap, alpha, x and
+// r updates, r.r, beta) on an FP32 copy of the matrix with FP32 vectors --
+// half the bytes of every pass -- while every reduction accumulates in FP64
+// (widened with integer operations, mfe_common.cuh) and alpha / beta stay
+// FP64.  The FP32 iterate is a correction x32 to the FP64 solution x.  A
+// reliable update -- x += x32, x32 = 0, r = b - A x in FP64 (the box SpMV
+// writing the residual straight into the FP32 r) -- replaces the drifting
+// recursive residual with the true one; the search direction p is kept, so
+// the recurrence continues instead of restarting and the iteration count stays
+// close to the FP64 solver's.  Updates happen every refine_k iterations, when
+// the recursive residual has dropped tenfold since the last update, and
+// whenever the recursive residual claims convergence; the solve stops only
+// when the true FP64 residual meets the tolerance.
+//
+// One iteration is three kernels (k_mx_p, the FP32 box SpMV with p.Ap,
+// k_mx_update) plus three that only work when an update is due (the graph
+// cannot branch cheaply per iteration, so k_mx_xupdate and the FP64 residual
+// SpMV check a device-side gate and return at once when it is closed) and a
+// one-thread bookkeeping kernel that sets the loop condition.  The whole
+// solve is one CUDA graph launch with a conditional while node.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+
+#include "mfe_common.cuh"
+#include "mfe_internal.h"
+
+namespace mfe {
+
+struct MixState {
+  double rr;            // r.r of the current recursive residual (FP64 accumulated)
+  double rr_new;        // r.r after this iteration's update
+  double pAp;           // written by the FP32 SpMV's epilogue
+  double beta;
+  double rr_true;       // ||b - A x||^2 from the gated FP64 residual SpMV
+  double rr_at_update;  // rr right after the last reliable update
+  double normr0, tol_abs, normr_true;
+  double delta2;        // update when rr_new < delta2 * rr_at_update
+  int k;                // inner iterations done
+  int max_iter;
+  int since;            // iterations since the last reliable update
+  int refine_k;         // update at least every refine_k iterations
+  int gate;             // 1: a reliable update runs in this iteration
+  int cont;             // loop condition
+  int first;            // next p update is p = r
+  int updates;          // reliable updates done
+  int status;           // 0 ok, MFE_BREAKDOWN
+  int record;
+  unsigned err;
+  int pad;
+  double* history;      // recursive normr per iteration (record)
+};
+
+constexpr int kT = 256;
+constexpr int kMaxPart = 8192;
+
+// p = r (first) or p = r + beta p, FP32 (cg_solve.hpp:153-161)
+__global__ void __launch_bounds__(kT)
+    k_mx_p(int64_t n, const float* __restrict__ r, float* __restrict__ p, const MixState* st)
+{
+  const bool first = st->first != 0;
+  const float beta = (float)st->beta;
+  const int64_t stride = (int64_t)gridDim.x * kT;
+  const int64_t n4 = n >> 2;
+  const float4* r4 = reinterpret_cast<const float4*>(r);
+  float4* p4 = reinterpret_cast<float4*>(p);
+  for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n4; i += stride) {
+    const float4 rv = r4[i];
+    float4 pv;
+    if (first) pv = rv;
+    else {
+      pv = p4[i];
+      pv.x = fmaf(beta, pv.x, rv.x);
+      pv.y = fmaf(beta, pv.y, rv.y);
+      pv.z = fmaf(beta, pv.z, rv.z);
+      pv.w = fmaf(beta, pv.w, rv.w);
+    }
+    p4[i] = pv;
+  }
+  const int64_t t = (n4 << 2) + (int64_t)blockIdx.x * kT + threadIdx.x;
+  if (blockIdx.x == 0 && t < n) p[t] = first ? r[t] : fmaf(beta, p[t], r[t]);
+}
+
+// x32 += alpha p, r -= alpha Ap, r.r in FP64 (cg_solve.hpp:201-213, :158);
+// the last block decides whether a reliable update is due.
+__global__ void __launch_bounds__(kT)
+    k_mx_update(int64_t n, float* __restrict__ x32, float* __restrict__ r,
+                const float* __restrict__ p, const float* __restrict__ Ap, MixState* st,
+                double* partials, unsigned* ticket)
+{
+  __shared__ double red[32];
+  __shared__ float s_alpha;
+  if (threadIdx.x == 0) s_alpha = (float)(st->rr / st->pAp);
+  __syncthreads();
+  const float alpha = s_alpha;
+  double acc = 0.0;
+  const int64_t stride = (int64_t)gridDim.x * kT;
+  const int64_t n4 = n >> 2;
+  float4* x4 = reinterpret_cast<float4*>(x32);
+  float4* r4 = reinterpret_cast<float4*>(r);
+  const float4* p4 = reinterpret_cast<const float4*>(p);
+  const float4* a4 = reinterpret_cast<const float4*>(Ap);
+  for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n4; i += stride) {
+    float4 xv = x4[i], rv = r4[i];
+    const float4 pv = p4[i], av = a4[i];
+    xv.x = fmaf(alpha, pv.x, xv.x);
+    xv.y = fmaf(alpha, pv.y, xv.y);
+    xv.z = fmaf(alpha, pv.z, xv.z);
+    xv.w = fmaf(alpha, pv.w, xv.w);
+    rv.x = fmaf(-alpha, av.x, rv.x);
+    rv.y = fmaf(-alpha, av.y, rv.y);
+    rv.z = fmaf(-alpha, av.z, rv.z);
+    rv.w = fmaf(-alpha, av.w, rv.w);
+    x4[i] = xv;
+    r4[i] = rv;
+    double d;
+    d = f2d_exact(rv.x); acc = fma(d, d, acc);
+    d = f2d_exact(rv.y); acc = fma(d, d, acc);
+    d = f2d_exact(rv.z); acc = fma(d, d, acc);
+    d = f2d_exact(rv.w); acc = fma(d, d, acc);
+  }
+  const int64_t t = (n4 << 2) + (int64_t)blockIdx.x * kT + threadIdx.x;
+  if (blockIdx.x == 0 && t < n) {
+    x32[t] = fmaf(alpha, p[t], x32[t]);
+    const float rv = fmaf(-alpha, Ap[t], r[t]);
+    r[t] = rv;
+    const double d = f2d_exact(rv);
+    acc = fma(d, d, acc);
+  }
+  const double bt = block_sum(acc, red);
+  double total;
+  if (grid_reduce_last(bt, partials, ticket, red, &total) && threadIdx.x == 0) {
+    st->rr_new = total;
+    st->k += 1;
+    st->since += 1;
+    st->first = 0;
+    if (st->record) st->history[st->k] = sqrt(total);
+    if (!(st->pAp > 0.0)) st->status = MFE_BREAKDOWN;  // cg_solve.hpp:187
+    st->gate = st->status == 0 &&
+               (st->since >= st->refine_k || total < st->delta2 * st->rr_at_update ||
+                total <= st->tol_abs * st->tol_abs || st->k >= st->max_iter);
+  }
+}
+
+// reliable update, part 1 (gated): x += x32, x32 = 0
+__global__ void __launch_bounds__(kT)
+    k_mx_xupdate(int64_t n, double* __restrict__ x, float* __restrict__ x32, const MixState* st)
+{
+  if (st->gate == 0) return;
+  for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
+    x[i] += f2d_exact(x32[i]);
+    x32[i] = 0.0f;
+  }
+}
+
+// bookkeeping (one thread): finish a reliable update, set the loop condition
+__global__ void k_mx_after(MixState* st, cudaGraphConditionalHandle h, int in_graph)
+{
+  if (st->status != 0) {
+    st->cont = 0;
+  } else if (st->gate) {
+    st->updates += 1;
+    st->since = 0;
+    st->normr_true = sqrt(st->rr_true);
+    if (st->normr_true <= st->tol_abs || st->k >= st->max_iter) {
+      st->cont = 0;
+    } else {
+      // continue the recurrence from the true residual, keeping p
+      st->beta = st->rr_true / st->rr;
+      st->rr = st->rr_true;
+      st->rr_at_update = st->rr_true;
+      st->cont = 1;
+    }
+  } else {
+    st->beta = st->rr_new / st->rr;
+    st->rr = st->rr_new;
+    st->cont = st->k < st->max_iter;
+  }
+  st->gate = 0;
+  if (in_graph) cudaGraphSetConditional(h, st->cont ? 1u : 0u);
+}
+
+__global__ void k_mx_init(MixState* st)
+{
+  // after the first FP64 residual: r32 = b - A x0, rr_true = ||r||^2
+  const double nr = sqrt(st->rr_true);
+  st->normr0 = nr;
+  st->normr_true = nr;
+  if (st->gate) st->tol_abs *= nr;  // relative tolerance (gate carries tol_mode here)
+  st->gate = 0;
+  st->rr = st->rr_true;
+  st->rr_at_update = st->rr_true;
+  st->cont = (st->max_iter > 0) && (nr > st->tol_abs);
+  if (st->record) st->history[0] = nr;
+}
+
+__global__ void k_mx_begin(const MixState* st, cudaGraphConditionalHandle h)
+{
+  cudaGraphSetConditional(h, st->cont ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
+// host
+// ---------------------------------------------------------------------------
+namespace {
+
+struct MixBufs {
+  float *r, *p, *Ap, *x32;
+  MixState* st;
+  double* history;
+  double* partials;  // 2 * kMaxPart
+  unsigned* tickets; // 2
+};
+
+int grid_for(mfe_ctx* ctx, int64_t n)
+{
+  return (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(std::max<int64_t>(n, 1), kT), (int64_t)ctx->sm_count * 8));
+}
+
+mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, const double* b,
+                       double* x, const MixBufs& B, cudaGraphConditionalHandle h, int in_graph)
+{
+  const int64_t n = A64.nrows;
+  k_mx_p<<<grid_for(ctx, n / 4), kT, 0, ctx->stream>>>(n, B.r, B.p, B.st);
+  MFE_TRY(check_launch(ctx, "k_mx_p"));
+  DotSink s1;
+  s1.partials = B.partials;
+  s1.ticket = B.tickets;
+  s1.out = &B.st->pAp;
+  MFE_TRY(launch_spmv(ctx, &A32, B.p, B.Ap, &s1, nullptr, nullptr));
+  k_mx_update<<<grid_for(ctx, n / 4), kT, 0, ctx->stream>>>(n, B.x32, B.r, B.p, B.Ap, B.st,
+                                                             B.partials + kMaxPart, B.tickets + 1);
+  MFE_TRY(check_launch(ctx, "k_mx_update"));
+  k_mx_xupdate<<<grid_for(ctx, n), kT, 0, ctx->stream>>>(n, x, B.x32, B.st);
+  MFE_TRY(check_launch(ctx, "k_mx_xupdate"));
+  DotSink s2;
+  s2.partials = B.partials;
+  s2.ticket = B.tickets;
+  s2.out = &B.st->rr_true;
+  MFE_TRY(launch_box_resid_f32out(ctx, &A64, x, b, B.r, &s2, &B.st->gate));
+  k_mx_after<<<1, 1, 0, ctx->stream>>>(B.st, h, in_graph);
+  return check_launch(ctx, "k_mx_after");
+}
+
+}  // namespace
+
+mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double* x,
+                    const mfe_cg_opts* o, mfe_cg_result* res)
+{
+  const int64_t n = A64_in->nrows;
+  mfe_csr A64 = *A64_in;
+  if (!csr_is_box(&A64)) {
+    int bx, by, bz;
+    MFE_TRY(detect_box(ctx, &A64, &bx, &by, &bz));
+    A64.box_nx = bx;
+    A64.box_ny = by;
+    A64.box_nz = bz;
+  }
+  if (!csr_is_box(&A64))
+    return fail(ctx, MFE_NOT_SUPPORTED,
+                "the mixed-precision solver needs a box-structured matrix (miniFE assembly)");
+  if (((uintptr_t)A64.vals & 15u) || ((uintptr_t)x & 15u))
+    return fail(ctx, MFE_BAD_ARG, "mixed solver: matrix values and x must be 16-byte aligned");
+  A64.max_row_len = 27;
+
+  // FP32 copy of the values (cached per source matrix on the context)
+  mfe_csr A32;
+  if (o->A32 != nullptr) {
+    A32 = *o->A32;
+    if (A32.dtype != MFE_F32 || A32.nnz != A64.nnz || A32.nrows != n)
+      return fail(ctx, MFE_BAD_ARG, "opts->A32 does not match A");
+  } else {
+    float* v32 = static_cast<float*>(workspace(ctx, "mixed.vals32", sizeof(float) * (size_t)(A64.nnz + 4)));
+    if (!v32) return fail(ctx, MFE_OOM, "FP32 matrix copy allocation failed");
+    if (ctx->f32_src_vals != A64.vals || ctx->f32_src_nnz != A64.nnz) {
+      MFE_TRY(launch_convert_f32(ctx, static_cast<const double*>(A64.vals), v32, A64.nnz));
+      ctx->f32_src_vals = A64.vals;
+      ctx->f32_src_nnz = A64.nnz;
+    }
+    A32 = A64;
+    A32.vals = v32;
+    A32.dtype = MFE_F32;
+  }
+  A32.box_nx = A64.box_nx;
+  A32.box_ny = A64.box_ny;
+  A32.box_nz = A64.box_nz;
+  A32.max_row_len = 27;
+
+  MixBufs B;
+  const size_t vb = sizeof(float) * (size_t)std::max<int64_t>(n + 4, 4);
+  B.r = static_cast<float*>(workspace(ctx, "mixed.r", vb));
+  B.p = static_cast<float*>(workspace(ctx, "mixed.p", vb));
+  B.Ap = static_cast<float*>(workspace(ctx, "mixed.Ap", vb));
+  B.x32 = static_cast<float*>(workspace(ctx, "mixed.x32", vb));
+  B.st = static_cast<MixState*>(workspace(ctx, "mixed.state", sizeof(MixState)));
+  const int max_iter = std::max(0, o->max_iter);
+  B.history = static_cast<double*>(workspace(ctx, "mixed.history", sizeof(double) * ((size_t)max_iter + 2)));
+  B.partials = static_cast<double*>(workspace(ctx, "mixed.partials", sizeof(double) * 2 * kMaxPart));
+  const bool fresh = ctx->ws.find("mixed.tickets") == ctx->ws.end();
+  B.tickets = static_cast<unsigned*>(workspace(ctx, "mixed.tickets", sizeof(unsigned) * 4));
+  if (!B.r || !B.p || !B.Ap || !B.x32 || !B.st || !B.history || !B.partials || !B.tickets)
+    return fail(ctx, MFE_OOM, "mixed solver workspace allocation failed");
+  if (fresh) MFE_CUDA_TRY(ctx, cudaMemsetAsync(B.tickets, 0, sizeof(unsigned) * 4, ctx->stream));
+  if (!workspace(ctx, "spmv.err", sizeof(unsigned))) return fail(ctx, MFE_OOM, "workspace");
+
+  char* hbuf = static_cast<char*>(host_scratch(ctx, 4096));
+  if (!hbuf) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
+  MixState* hs = reinterpret_cast<MixState*>(hbuf);
+  memset(hs, 0, sizeof(MixState));
+  hs->max_iter = max_iter;
+  hs->tol_abs = o->tol;
+  hs->gate = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;  // consumed by k_mx_init
+  hs->refine_k = o->refine_k > 0 ? o->refine_k : 25;
+  hs->delta2 = 1e-2;
+  hs->record = o->record_history ? 1 : 0;
+  hs->history = B.history;
+  hs->first = 1;
+
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(B.st, hs, sizeof(MixState), cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(B.x32, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(B.p, 0, vb, ctx->stream));
+  {
+    DotSink s;
+    s.partials = B.partials;
+    s.ticket = B.tickets;
+    s.out = &B.st->rr_true;
+    MFE_TRY(launch_box_resid_f32out(ctx, &A64, x, b, B.r, &s, nullptr));
+  }
+  k_mx_init<<<1, 1, 0, ctx->stream>>>(B.st);
+  MFE_TRY(check_launch(ctx, "k_mx_init"));
+
+  if (getenv("MFE_CG_EAGER") != nullptr) {
+    for (;;) {
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(MixState), cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!hs->cont || hs->err) break;
+      MFE_TRY(launch_iter(ctx, A32, A64, b, x, B, 0, 0));
+    }
+  } else {
+    // graph: begin kernel, then while(cont) { one iteration }
+    cudaStream_t run_stream = ctx->stream;
+    cudaStream_t s = ctx->own_stream;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    mfe_status st = MFE_OK;
+    if (e == cudaSuccess) {
+      ctx->stream = s;
+      e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        k_mx_begin<<<1, 1, 0, s>>>(B.st, h);
+        e = cudaStreamEndCapture(s, &g);
+      }
+      cudaGraphNode_t nodes[4];
+      size_t nn = 4;
+      if (e == cudaSuccess) e = cudaGraphGetNodes(g, nodes, &nn);
+      alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+      memset(cp_buf, 0, sizeof(cp_buf));
+      cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+      cp->type = cudaGraphNodeTypeConditional;
+      cp->conditional.handle = h;
+      cp->conditional.type = cudaGraphCondTypeWhile;
+      cp->conditional.size = 1;
+      cudaGraphNode_t cnode;
+      if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
+      if (e == cudaSuccess) {
+        cudaGraph_t body = cp->conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+          st = launch_iter(ctx, A32, A64, b, x, B, h, 1);
+          cudaGraph_t tmp;
+          cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+          if (e == cudaSuccess) e = e2;
+        }
+      }
+      ctx->stream = run_stream;
+      if (e == cudaSuccess && st == MFE_OK) e = cudaGraphInstantiate(&ex, g, 0);
+      if (e == cudaSuccess && st == MFE_OK) e = cudaGraphLaunch(ex, ctx->stream);
+    }
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    if (st != MFE_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "mixed CG graph");
+  }
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(MixState), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  if (hs->err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during mixed CG");
+  res->num_iters = hs->k;
+  res->normr = hs->normr_true;
+  res->normr0 = hs->normr0;
+  res->final_resid = hs->normr_true;
+  for (double& t : res->times) t = 0.0;
+  res->times[4] = ms * 1e-3;
+  res->refinements = hs->updates;
+  res->fp64_spmvs = hs->updates + 1;
+  mfe_status status = MFE_OK;
+  if (hs->status != 0) status = MFE_BREAKDOWN;
+  else if (hs->normr_true > hs->tol_abs) status = MFE_MAXITER;
+  res->status = status;
+  if (o->record_history) {
+    const int cnt = hs->k + 1;
+    ctx->history.resize(cnt);
+    MFE_CUDA_TRY(ctx, cudaMemcpy(ctx->history.data(), B.history, sizeof(double) * cnt,
+                                 cudaMemcpyDeviceToHost));
+  } else {
+    ctx->history.clear();
+  }
+  return status;
+}
+
+}  // namespace mfe

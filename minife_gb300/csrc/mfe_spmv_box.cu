@@ -46,6 +46,8 @@ struct BoxParams {
   double* dot_out;
   CgState* cg;
   unsigned* err;
+  float* y32;          // BOX_RESID: when set, the residual is written as FP32 here
+  const int* gate;     // when set and *gate == 0 the launch does nothing
 };
 
 template <int MODE>
@@ -93,6 +95,9 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = (P.n + ROWS - 1) / ROWS;
+  // gated launches (the mixed solver's reliable update inside its graph)
+  // return at once, uniformly for the whole grid, when the gate is closed
+  if (P.gate != nullptr && *P.gate == 0) return;
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
@@ -245,12 +250,13 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
         __syncwarp();
         if (lane == 0) mbar_arrive(&empty[s]);  // stage s no longer read by this warp
         if (MODE == BOX_RESID) {
-          const double res = P.b[r] - (double)sum;
-          P.y[r] = (T)res;
+          const double res = P.b[r] - widen(sum);
+          if (P.y32 != nullptr) P.y32[r] = (float)res;
+          else P.y[r] = (T)res;
           dacc = fma(res, res, dacc);
         } else {
           P.y[r] = sum;
-          if (MODE == BOX_DOT) dacc = fma((double)sum, (double)xr, dacc);
+          if (MODE == BOX_DOT) dacc = fma(widen(sum), widen(xr), dacc);
         }
       } else {
         __syncwarp();
@@ -430,9 +436,12 @@ mfe_status detect_box(mfe_ctx* ctx, const mfe_csr* A, int* nx, int* ny, int* nz)
 
 template <typename T, int MODE>
 static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
-                               const DotSink* sink, const double* b, CgState* cg)
+                               const DotSink* sink, const double* b, CgState* cg,
+                               float* y32 = nullptr, const int* gate = nullptr)
 {
   BoxParams<T> P;
+  P.y32 = y32;
+  P.gate = gate;
   P.Nx = A->box_nx + 1;
   P.Ny = A->box_ny + 1;
   P.Nz = A->box_nz + 1;
@@ -482,6 +491,14 @@ mfe_status launch_spmv_box(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* 
   if (resid_b) return fail(ctx, MFE_NOT_SUPPORTED, "FP32 residual SpMV is not provided");
   if (sink) return box_launch_t<float, BOX_DOT>(ctx, A, xf, yf, sink, nullptr, cg);
   return box_launch_t<float, BOX_PLAIN>(ctx, A, xf, yf, nullptr, nullptr, cg);
+}
+
+mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const double* x,
+                                   const double* b, float* r32, const DotSink* sink,
+                                   const int* gate)
+{
+  if (A64->nrows == 0) return MFE_OK;
+  return box_launch_t<double, BOX_RESID>(ctx, A64, x, nullptr, sink, b, nullptr, r32, gate);
 }
 
 }  // namespace mfe

@@ -1,0 +1,75 @@
+"""Mixed-precision CG (FP32 matrix and vectors, FP64 dots, FP64 reliable
+updates) against the FP64 oracle.
+
+Bars: the solver stops only on the TRUE FP64 residual, so ||b - A x|| / ||b||
+<= tol is checked here with the oracle's own matvec on the host; the solution
+is compared with the oracle's FP64 solution solved to 1e-12 (relative L2 and
+max-abs error); the analytic check passes as in the reference.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+import minife_gb300 as M  # noqa: E402
+
+
+def host(t):
+    return t.detach().cpu().numpy()
+
+
+@pytest.mark.parametrize("dims,refine_k", [((30, 30, 30), 0), ((24, 16, 8), 10),
+                                           ((40, 30, 20), 50), ((17, 9, 11), 25)])
+def test_mixed_reaches_fp64_verified_tolerance(dims, refine_k):
+    A, b = M.build_system(*dims)
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=3000, tol=1e-8, tol_mode="relative",
+                     precision="mixed", refine_k=refine_k)
+    assert res.status == 0
+    ro, cols, vals, bo = O.build_system(*dims)
+    xg = host(x)
+    rel_res = np.linalg.norm(bo - O.matvec(ro, cols, vals, xg)) / np.linalg.norm(bo)
+    assert rel_res <= 1e-8, rel_res
+    assert abs(res.final_resid / res.normr0 - rel_res) <= 1e-3 * rel_res + 1e-15
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=5000, tol=1e-12, tol_mode=1)
+    rel_err = np.linalg.norm(xg - xo) / np.linalg.norm(xo)
+    max_abs = np.abs(xg - xo).max()
+    assert rel_err <= 1e-6, rel_err
+    assert max_abs <= 1e-6, max_abs
+    # iteration count stays close to the FP64 solver's
+    x64 = torch.zeros_like(b)
+    r64 = M.cg_solve(A, b, x64, max_iter=3000, tol=1e-8, tol_mode="relative")
+    assert res.num_iters <= 1.35 * r64.num_iters + 10, (res.num_iters, r64.num_iters)
+    rc, err = M.verify_solution(*dims, x)
+    rco, erro = O.verify_solution(*dims, xo)
+    assert rc == rco and abs(err - erro) <= 1e-5
+
+
+def test_mixed_max_iter_reports_maxiter():
+    A, b = M.build_system(20, 20, 20)
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=5, tol=1e-8, tol_mode="relative", precision="mixed")
+    assert res.status == 5  # MFE_MAXITER
+    assert res.num_iters == 5
+    # the returned x is the reliably updated FP64 iterate: its residual is the
+    # one reported
+    ro, cols, vals, bo = O.build_system(20, 20, 20)
+    r = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x)))
+    assert abs(r - res.final_resid) <= 1e-9 * r
+
+
+def test_mixed_with_prepared_f32_copy_and_history():
+    A, b = M.build_system(16, 16, 16)
+    A32 = M.to_f32(A)
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=2000, tol=1e-9, tol_mode="relative", precision="mixed",
+                     A32=A32, record_history=True)
+    assert res.status == 0 and res.final_resid <= 1e-9 * res.normr0
+    assert len(res.history) == res.num_iters + 1
+    assert res.refinements >= 1
