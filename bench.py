@@ -328,6 +328,42 @@ def run_gpu(args):
                "d2h_bytes_per_step": 8 * n, "iterations": r2.num_iters}
         del ro_h, cols_h, vals_h
 
+    # mixed precision (FP32 matrix/vectors, FP64 dots and reliable updates) to
+    # the same FP64-verified tolerance, same system, same timing rules
+    mixed = None
+    if not args.no_mixed:
+        x64 = x.clone()
+        xm = torch.zeros_like(b)
+        A32 = M.to_f32(A)
+        for _ in range(args.warmup):
+            xm.zero_()
+            rm = M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
+                            precision="mixed", refine_k=args.refine_k, A32=A32)
+        torch.cuda.synchronize()
+        barrier(world)
+        m0 = torch.cuda.Event(enable_timing=True)
+        m1 = torch.cuda.Event(enable_timing=True)
+        m0.record(stream)
+        for _ in range(args.steps):
+            xm.zero_()
+            rm = M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
+                            precision="mixed", refine_k=args.refine_k, A32=A32)
+        m1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        t_mixed = max_over_ranks(world, m0.elapsed_time(m1) * 1e-3 / args.steps)
+        rcm, errm = M.verify_solution(*DIMS, xm)
+        diff = xm - x64
+        mixed = {"value": t_mixed, "unit": "s", "speedup_vs_fp64": t_step / t_mixed,
+                 "inner_iterations": rm.num_iters, "reliable_updates": rm.refinements,
+                 "refine_k": args.refine_k, "status": rm.status,
+                 "final_rel_resid_fp64": rm.final_resid / rm.normr0,
+                 "err_vs_fp64_solution": {"rel_l2": float(diff.norm() / x64.norm()),
+                                          "max_abs": float(diff.abs().max())},
+                 "analytic_check": {"max_err": errm, "passed": rcm == 0},
+                 "dtype": "f32 matrix/vectors, f64 dots/scalars/solution"}
+        del A32, xm, x64
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         ro, cols, vals, bh = host_system(A, b)
@@ -354,6 +390,7 @@ def run_gpu(args):
             "ms_per_iter": t_step / res.num_iters * 1e3,
             "cg_effective_gbs": iter_bytes * res.num_iters / t_step / 1e9,
             "assembly_s": t_assembly,
+            "mixed": mixed,
             "spmv_f64_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -382,6 +419,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--refine-k", type=int, default=50,
+                    help="mixed solver: reliable update at least every k inner iterations")
     ap.add_argument("--cpu-sample", type=int, default=20)
     ap.add_argument("--ref-sample", type=int, default=10)
     ap.add_argument("--ref-iters", type=int, default=401,
