@@ -280,6 +280,11 @@ mfe_status mfe_verify_solution(mfe_ctx* ctx, int nx, int ny, int nz, const doubl
 mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
                                 const double* lambda, double* g);
 
+/* v[r] = 0 on every Dirichlet row of the box (faces of both boundary sets of
+ * simple_mesh_description.hpp:62-224).  Used to form the adjoint right-hand
+ * side of a box solve, which must vanish on the prescribed rows. */
+mfe_status mfe_box_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v);
+
 /* Multi-RHS: Y = A X for nrhs column vectors stored row-major (X[i*nrhs + j]),
  * reading A once per product.  FP64 or FP32 by A->dtype (X, Y same type). */
 mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X, void* Y);

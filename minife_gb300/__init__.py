@@ -425,3 +425,10 @@ def element_gradient(nx, ny, nz, u, lam, g=None, ctx: Context | None = None):
     ctx.check(ctx.lib.mfe_element_gradient(ctx.h, nx, ny, nz, _ptr(u), _ptr(lam), _ptr(g)),
               "mfe_element_gradient")
     return g
+
+
+def box_zero_boundary(nx, ny, nz, v, ctx: Context | None = None):
+    """v[r] = 0 on every Dirichlet row of the box (in place)."""
+    ctx = ctx or default_context()
+    ctx.check(ctx.lib.mfe_box_zero_boundary(ctx.h, nx, ny, nz, _ptr(v)), "mfe_box_zero_boundary")
+    return v

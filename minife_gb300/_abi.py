@@ -100,6 +100,7 @@ SIGNATURES = {
                              _P(ctypes.c_int)]),
     "mfe_element_gradient": (ctypes.c_int, [c_void_p] + [ctypes.c_int] * 3 +
                              [c_void_p, c_void_p, c_void_p]),
+    "mfe_box_zero_boundary": (ctypes.c_int, [c_void_p] + [ctypes.c_int] * 3 + [c_void_p]),
     "mfe_spmm": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_int32, c_void_p, c_void_p]),
     "mfe_cg_solve_multi": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_int32, c_void_p, c_void_p,
                                           _P(MfeCgOpts), _P(MfeCgResult)]),

@@ -559,6 +559,14 @@ mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const doub
   return launch_element_gradient(ctx, nx, ny, nz, u, lambda, g);
 }
 
+mfe_status mfe_box_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v)
+{
+  if (!ctx || !v) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  if (!box_ok(nx, ny, nz)) return fail(ctx, MFE_BAD_ARG, "bad box");
+  MFE_TRY(set_device(ctx));
+  return launch_zero_boundary(ctx, nx, ny, nz, v);
+}
+
 mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X, void* Y)
 {
   if (!ctx) return MFE_BAD_ARG;

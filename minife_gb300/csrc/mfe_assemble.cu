@@ -334,6 +334,18 @@ __global__ void __launch_bounds__(kElemThreads)
   g[e] = -s;
 }
 
+// v[r] = 0 on every Dirichlet row of the box (both boundary sets): the adjoint
+// right-hand side must vanish there so that lambda_D = 0.
+__global__ void k_zero_boundary(int Nx, int Ny, int Nz, double* __restrict__ v)
+{
+  const int64_t NxNy = (int64_t)Nx * Ny, N = NxNy * Nz;
+  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < N;
+       r += (int64_t)gridDim.x * blockDim.x) {
+    const int ix = (int)(r % Nx), iy = (int)((r / Nx) % Ny), iz = (int)(r / NxNy);
+    if (ix == 0 || ix == Nx - 1 || iy == 0 || iy == Ny - 1 || iz == 0 || iz == Nz - 1) v[r] = 0.0;
+  }
+}
+
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
@@ -451,6 +463,15 @@ mfe_status launch_verify(mfe_ctx* ctx, int nx, int ny, int nz, const double* x, 
   memcpy(&v, &bits, sizeof(v));
   *max_err_host = v;
   return MFE_OK;
+}
+
+mfe_status launch_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v)
+{
+  const int64_t N = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
+  const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(N, 256),
+                                                                (int64_t)ctx->sm_count * 8));
+  k_zero_boundary<<<(unsigned)blocks, 256, 0, ctx->stream>>>(nx + 1, ny + 1, nz + 1, v);
+  return check_launch(ctx, "k_zero_boundary");
 }
 
 mfe_status launch_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,

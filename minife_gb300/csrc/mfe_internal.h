@@ -60,6 +60,7 @@ mfe_status launch_verify(mfe_ctx* ctx, int nx, int ny, int nz, const double* x, 
                          double* max_err_host);
 mfe_status launch_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
                                    const double* lambda, double* g);
+mfe_status launch_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v);
 int64_t box_nnz(int nx, int ny, int nz);
 
 // ---- SpMV (mfe_spmv.cu) ----
