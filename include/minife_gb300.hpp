@@ -1,0 +1,297 @@
+// minife_gb300.hpp -- header-only C++ shim over the C ABI (minife_gb300.h)
+// with the reference's operator interface for the solve path.
+//
+// The reference (Mantevo miniFE, ref/ variant) binds this path through C++
+// templates; this header keeps those types and signatures so reference-style
+// host code compiles against the GB300 implementation unchanged:
+//
+//   CSRMatrix<S,LO,GO>   ref/src/CSRMatrix.hpp:43-129   (same fields)
+//   Vector<S,LO,GO>      ref/src/Vector.hpp:36-61       (same fields)
+//   matvec_std<M,V>      ref/src/SparseMatrix_functions.hpp:545-578
+//   matvec_and_dot       ref/src/SparseMatrix_functions.hpp:491-536
+//   dot, waxpby, fused_waxpby  ref/src/Vector_functions.hpp:127-226
+//   impose_dirichlet     ref/src/SparseMatrix_functions.hpp:434-480
+//   cg_solve             ref/src/cg_solve.hpp:69-229
+//
+// The containers stay in host std::vectors like the reference's; each call
+// copies its operands to the device, runs the library's CUDA kernels and
+// copies results back (cg_solve does this once for the whole solve).  Only
+// Scalar = double, LocalOrdinal = GlobalOrdinal = int -- the reference's
+// default build (ref/src/Makefile:3-6) -- is supported.
+#pragma once
+
+#include <cmath>
+#include <cstring>
+#include <set>
+#include <stdexcept>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include "minife_gb300.h"
+
+namespace minife_gb300 {
+
+typedef double timer_type;
+enum CG_TIMES { WAXPY = 0, DOT = 1, MATVEC = 2, MATVECDOT = 3, TOTAL = 4, NUM_TIMERS = 5 };
+
+class Error : public std::runtime_error {
+ public:
+  Error(mfe_status s, const std::string& what)
+      : std::runtime_error(what + ": " + mfe_status_string(s)), status(s) {}
+  mfe_status status;
+};
+
+// Process-wide context on device 0 (one stream), created on first use.
+class Context {
+ public:
+  static Context& get()
+  {
+    static Context c;
+    return c;
+  }
+  mfe_ctx* h() { return ctx_; }
+  void check(mfe_status s, const char* what)
+  {
+    if (s != MFE_OK) throw Error(s, std::string(what) + " (" + mfe_last_error_string(ctx_) + ")");
+  }
+  // device buffer cache by role, grown on demand
+  void* buf(int slot, size_t bytes)
+  {
+    if (bytes > cap_[slot]) {
+      if (ptr_[slot]) mfe_device_free(ctx_, ptr_[slot]);
+      ptr_[slot] = nullptr;
+      check(mfe_device_alloc(ctx_, bytes, &ptr_[slot]), "mfe_device_alloc");
+      cap_[slot] = bytes;
+    }
+    return ptr_[slot];
+  }
+  ~Context()
+  {
+    for (int i = 0; i < kSlots; ++i)
+      if (ptr_[i]) mfe_device_free(ctx_, ptr_[i]);
+    mfe_ctx_destroy(ctx_);
+  }
+
+ private:
+  Context()
+  {
+    mfe_status s = mfe_ctx_create(0, &ctx_);
+    if (s != MFE_OK) throw Error(s, "mfe_ctx_create(0)");
+  }
+  static constexpr int kSlots = 8;
+  mfe_ctx* ctx_ = nullptr;
+  void* ptr_[kSlots] = {};
+  size_t cap_[kSlots] = {};
+};
+
+template <typename Scalar, typename LocalOrdinal, typename GlobalOrdinal>
+struct CSRMatrix {
+  static_assert(std::is_same<Scalar, double>::value && std::is_same<LocalOrdinal, int>::value &&
+                    std::is_same<GlobalOrdinal, int>::value,
+                "minife_gb300 supports CSRMatrix<double,int,int>");
+  typedef Scalar ScalarType;
+  typedef LocalOrdinal LocalOrdinalType;
+  typedef GlobalOrdinal GlobalOrdinalType;
+
+  bool has_local_indices = false;
+  std::vector<GlobalOrdinal> rows;
+  std::vector<LocalOrdinal> row_offsets;
+  std::vector<LocalOrdinal> row_offsets_external;
+  std::vector<GlobalOrdinal> packed_cols;
+  std::vector<Scalar> packed_coefs;
+  LocalOrdinal num_cols = 0;
+
+  size_t num_nonzeros() const { return row_offsets.empty() ? 0 : row_offsets.back(); }
+  void reserve_space(unsigned nrows, unsigned ncols_per_row)
+  {
+    rows.resize(nrows);
+    row_offsets.resize(nrows + 1);
+    packed_cols.reserve((size_t)nrows * ncols_per_row);
+    packed_coefs.reserve((size_t)nrows * ncols_per_row);
+  }
+  // one rank: rows[i] == i, so the row pointer is a direct index
+  void get_row_pointers(GlobalOrdinal row, size_t& row_length, GlobalOrdinal*& cols,
+                        Scalar*& coefs)
+  {
+    if (row < 0 || (size_t)row + 1 >= row_offsets.size()) {
+      row_length = 0;
+      return;
+    }
+    const LocalOrdinal off = row_offsets[row];
+    row_length = (size_t)(row_offsets[row + 1] - off);
+    cols = &packed_cols[off];
+    coefs = &packed_coefs[off];
+  }
+};
+
+template <typename Scalar, typename LocalOrdinal, typename GlobalOrdinal>
+struct Vector {
+  typedef Scalar ScalarType;
+  typedef LocalOrdinal LocalOrdinalType;
+  typedef GlobalOrdinal GlobalOrdinalType;
+  Vector(GlobalOrdinal startIdx, LocalOrdinal local_sz)
+      : startIndex(startIdx), local_size(local_sz), coefs(local_sz, 0.0) {}
+  GlobalOrdinal startIndex;
+  LocalOrdinal local_size;
+  std::vector<Scalar> coefs;
+};
+
+namespace detail {
+enum { SLOT_RO = 0, SLOT_COLS, SLOT_VALS, SLOT_X, SLOT_Y, SLOT_W, SLOT_ROWS };
+
+inline void h2d(void* d, const void* h, size_t bytes)
+{
+  Context& c = Context::get();
+  c.check(mfe_memcpy_h2d(c.h(), d, h, bytes), "mfe_memcpy_h2d");
+}
+inline void d2h(void* h, const void* d, size_t bytes)
+{
+  Context& c = Context::get();
+  c.check(mfe_memcpy_d2h(c.h(), h, d, bytes), "mfe_memcpy_d2h");
+}
+
+template <typename M>
+mfe_csr upload(const M& A)
+{
+  Context& c = Context::get();
+  mfe_csr m;
+  std::memset(&m, 0, sizeof(m));
+  m.nrows = (int64_t)A.rows.size();
+  m.ncols = m.nrows;
+  m.nnz = (int64_t)A.packed_cols.size();
+  m.dtype = MFE_F64;
+  m.row_offsets = static_cast<int32_t*>(c.buf(SLOT_RO, 4 * (size_t)(m.nrows + 1)));
+  m.cols = static_cast<int32_t*>(c.buf(SLOT_COLS, 4 * (size_t)(m.nnz + 4)));
+  m.vals = c.buf(SLOT_VALS, 8 * (size_t)(m.nnz + 4));
+  h2d(m.row_offsets, A.row_offsets.data(), 4 * (size_t)(m.nrows + 1));
+  h2d(m.cols, A.packed_cols.data(), 4 * (size_t)m.nnz);
+  h2d(m.vals, A.packed_coefs.data(), 8 * (size_t)m.nnz);
+  return m;
+}
+}  // namespace detail
+
+// matvec_std<CSR>: y = A x (SparseMatrix_functions.hpp:548-577)
+template <typename MatrixType, typename VectorType>
+struct matvec_std {
+  void operator()(MatrixType& A, VectorType& x, VectorType& y)
+  {
+    Context& c = Context::get();
+    mfe_csr m = detail::upload(A);
+    const size_t n = A.rows.size();
+    double* dx = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+    double* dy = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
+    detail::h2d(dx, x.coefs.data(), 8 * n);
+    c.check(mfe_spmv(c.h(), &m, dx, dy), "mfe_spmv");
+    detail::d2h(y.coefs.data(), dy, 8 * n);
+  }
+};
+
+template <typename MatrixType, typename VectorType>
+void matvec(MatrixType& A, VectorType& x, VectorType& y)
+{
+  matvec_std<MatrixType, VectorType>()(A, x, y);
+}
+
+template <typename MatrixType, typename VectorType>
+double matvec_and_dot(MatrixType& A, VectorType& x, VectorType& y)
+{
+  Context& c = Context::get();
+  mfe_csr m = detail::upload(A);
+  const size_t n = A.rows.size();
+  double* dx = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+  double* dy = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
+  detail::h2d(dx, x.coefs.data(), 8 * n);
+  double r = 0;
+  c.check(mfe_matvec_and_dot(c.h(), &m, dx, dy, &r), "mfe_matvec_and_dot");
+  detail::d2h(y.coefs.data(), dy, 8 * n);
+  return r;
+}
+
+// dot (Vector_functions.hpp:194-226)
+template <typename VectorType>
+double dot(const VectorType& x, const VectorType& y)
+{
+  Context& c = Context::get();
+  const size_t n = x.coefs.size();
+  double* dx = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+  double* dy = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
+  detail::h2d(dx, x.coefs.data(), 8 * n);
+  detail::h2d(dy, y.coefs.data(), 8 * n);
+  double r = 0;
+  c.check(mfe_dot(c.h(), (int64_t)n, dx, dy, &r), "mfe_dot");
+  return r;
+}
+
+// waxpby (Vector_functions.hpp:127-150): w = alpha x + beta y
+template <typename VectorType>
+void waxpby(double alpha, const VectorType& x, double beta, const VectorType& y, VectorType& w)
+{
+  Context& c = Context::get();
+  const size_t n = x.coefs.size();
+  double* dx = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+  double* dy = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
+  double* dw = static_cast<double*>(c.buf(detail::SLOT_W, 8 * n + 16));
+  detail::h2d(dx, x.coefs.data(), 8 * n);
+  detail::h2d(dy, y.coefs.data(), 8 * n);
+  c.check(mfe_waxpby(c.h(), (int64_t)n, alpha, dx, beta, dy, dw), "mfe_waxpby");
+  detail::d2h(w.coefs.data(), dw, 8 * n);
+}
+
+template <typename VectorType>
+void fused_waxpby(double alpha, const VectorType& x, double beta, const VectorType& y,
+                  VectorType& w, double alpha2, const VectorType& x2, double beta2,
+                  const VectorType& y2, VectorType& w2)
+{
+  waxpby(alpha, x, beta, y, w);
+  waxpby(alpha2, x2, beta2, y2, w2);
+}
+
+// impose_dirichlet (SparseMatrix_functions.hpp:434-480)
+template <typename MatrixType, typename VectorType>
+void impose_dirichlet(double prescribed_value, MatrixType& A, VectorType& b, int /*global_nx*/,
+                      int /*global_ny*/, int /*global_nz*/, const std::set<int>& bc_rows)
+{
+  Context& c = Context::get();
+  mfe_csr m = detail::upload(A);
+  const size_t n = A.rows.size();
+  double* db = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+  detail::h2d(db, b.coefs.data(), 8 * n);
+  std::vector<int32_t> rows(bc_rows.begin(), bc_rows.end());  // std::set is ascending
+  int32_t* drows = static_cast<int32_t*>(c.buf(detail::SLOT_ROWS, 4 * rows.size() + 16));
+  if (!rows.empty()) detail::h2d(drows, rows.data(), 4 * rows.size());
+  c.check(mfe_impose_dirichlet(c.h(), &m, db, prescribed_value, drows, (int64_t)rows.size()),
+          "mfe_impose_dirichlet");
+  detail::d2h(A.packed_coefs.data(), m.vals, 8 * A.packed_coefs.size());
+  detail::d2h(b.coefs.data(), db, 8 * n);
+}
+
+// cg_solve (cg_solve.hpp:69-229).  The Matvec argument is accepted for
+// signature compatibility; the solve always uses the library's kernels.
+template <typename OperatorType, typename VectorType, typename Matvec>
+void cg_solve(OperatorType& A, const VectorType& b, VectorType& x, Matvec /*matvec*/,
+              typename OperatorType::LocalOrdinalType max_iter, double& tolerance,
+              typename OperatorType::LocalOrdinalType& num_iters, double& normr,
+              timer_type* my_cg_times)
+{
+  Context& c = Context::get();
+  mfe_cg_opts o;
+  mfe_cg_opts_default(&o);
+  o.max_iter = max_iter;
+  o.tol = tolerance;
+  mfe_cg_result r;
+  const mfe_status s = mfe_cg_solve_host(
+      c.h(), (int64_t)A.rows.size(), (int64_t)A.packed_cols.size(), A.row_offsets.data(),
+      A.packed_cols.data(), A.packed_coefs.data(), b.coefs.data(), x.coefs.data(), &o, &r);
+  if (s == MFE_BREAKDOWN) {
+    // the reference reports breakdown on std::cerr and returns (cg_solve.hpp:188)
+  } else if (s != MFE_OK && s != MFE_MAXITER) {
+    c.check(s, "mfe_cg_solve_host");
+  }
+  num_iters = r.num_iters;
+  normr = r.normr;
+  if (my_cg_times)
+    for (int t = 0; t < NUM_TIMERS; ++t) my_cg_times[t] = r.times[t];
+}
+
+}  // namespace minife_gb300

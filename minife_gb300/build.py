@@ -54,10 +54,11 @@ def _compile(src: str, extra: list[str], verbose: bool) -> str:
 
 
 def _stale() -> bool:
-    if not os.path.exists(LIB):
+    if not os.path.exists(LIB) or not os.path.exists(os.path.join(HERE, "miniFE.x")):
         return True
-    t = os.path.getmtime(LIB)
+    t = min(os.path.getmtime(LIB), os.path.getmtime(os.path.join(HERE, "miniFE.x")))
     deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
+    deps += [os.path.join(HERE, "host", f) for f in os.listdir(os.path.join(HERE, "host"))]
     deps.append(os.path.join(ROOT, "include", "minife_gb300.h"))
     deps.append(os.path.abspath(__file__))
     return any(os.path.getmtime(d) > t for d in deps)
@@ -76,7 +77,24 @@ def build(force: bool = False, verbose: bool = False) -> str:
     if res.returncode != 0:
         raise RuntimeError("link failed:\n%s\n%s" % (res.stdout, res.stderr))
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
+
+
+DRIVER = os.path.join(HERE, "miniFE.x")
+
+
+def build_driver() -> str:
+    """The miniFE.x command-line driver (host C++ over the C ABI)."""
+    src = os.path.join(HERE, "host", "main.cpp")
+    cxx = shutil.which("g++") or "g++"
+    cmd = [cxx, "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), src, "-L", HERE,
+           "-lminife_gb300", "-Wl,-rpath,$ORIGIN", "-o", DRIVER + ".tmp"]
+    res = subprocess.run(cmd, capture_output=True, text=True)
+    if res.returncode != 0:
+        raise RuntimeError("driver build failed:\n%s\n%s" % (res.stdout, res.stderr))
+    os.replace(DRIVER + ".tmp", DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":

@@ -1,0 +1,360 @@
+// miniFE.x for GB300: the reference's command line, phases and YAML report
+// (ref/src/main.cpp:86-247, ref/src/driver.hpp:120-404) driving the GPU path
+// through the C ABI (include/minife_gb300.h).
+//
+//   miniFE.x nx=256 ny=256 nz=256 verify_solution=1
+//   miniFE.x -nx 64 -ny 64 -nz 64 precision=mixed rel_tol=1e-8 max_iters=5000
+//
+// Parameters are found by the reference's string scan
+// (ref/utils/param_utils.hpp:116-155): the first occurrence of the name, then
+// ' ', '=' or ':' separators, then the value.  Reference keys: nx (default
+// 10), ny (default nx), nz (default ny), verify_solution, name, load_imbalance,
+// mv_overlap_comm_comp, input_file, numthreads, use_locking, elem_group_size,
+// use_elem_mat_fields, device, num_devices, skip_device, numa (accepted; the
+// multi-rank ones have no effect on one GPU).  GB300 keys: precision (f64 |
+// mixed), max_iters (default 200, driver.hpp:241), abs_tol (default
+// DBL_EPSILON, driver.hpp:245), rel_tol (overrides abs_tol: stop at
+// ||r|| <= rel_tol ||r0||), refine_k (mixed solver).
+#include <sys/utsname.h>
+#include <unistd.h>
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <limits>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "minife_gb300.h"
+#include "yaml_doc.hpp"
+
+namespace {
+
+double now()
+{
+  return std::chrono::duration<double>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+// read_args_into_string / read_file_into_string (ref/utils/param_utils.cpp:36-55)
+std::string args_string(int argc, char** argv)
+{
+  std::string s = argv[0];
+  for (int i = 1; i < argc; ++i) s += " " + std::string(argv[i]);
+  return s;
+}
+
+std::string file_string(const std::string& fn)
+{
+  std::string out;
+  std::ifstream f(fn.c_str());
+  std::string line;
+  while (std::getline(f, line)) out += " " + line;
+  return out;
+}
+
+// parse_parameter (ref/utils/param_utils.hpp:116-155)
+template <typename T>
+T parse_parameter(const std::string& s, const std::string& name, const T& def)
+{
+  std::string::size_type pos = s.find(name);
+  if (pos == std::string::npos) return def;
+  pos += name.size();
+  if (s.size() <= pos) return def;
+  while (pos < s.size() && (s[pos] == ' ' || s[pos] == '=' || s[pos] == ':')) ++pos;
+  if (pos < s.size() && (s[pos] == '=' || s[pos] == ':')) ++pos;
+  std::istringstream is(s.substr(pos));
+  T v = def;
+  is >> v;
+  if (!is) return def;
+  return v;
+}
+
+void check(mfe_ctx* ctx, mfe_status s, const char* what)
+{
+  if (s != MFE_OK) {
+    std::cerr << "miniFE.x: " << what << " failed: " << mfe_status_string(s) << " ("
+              << (ctx ? mfe_last_error_string(ctx) : "") << ")" << std::endl;
+    std::exit(2);
+  }
+}
+
+struct Params {
+  int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads;
+  float load_imbalance;
+  std::string name, precision;
+  int max_iters, refine_k;
+  double abs_tol, rel_tol;
+};
+
+void print_timed(const char* msg, double t, double total)
+{
+  std::cout.width(30);
+  std::cout << msg << t << "s, total time: " << total << std::endl;
+}
+
+}  // namespace
+
+int main(int argc, char** argv)
+{
+  using minife_gb300::YamlDoc;
+  const double t_program = now();
+  std::string as = args_string(argc, argv);
+  const int print_params = parse_parameter<int>(as, "print_params", 0);
+  const std::string garbage("garbage");
+  const std::string fname = parse_parameter<std::string>(as, "input_file", garbage);
+  if (fname != garbage) as = file_string(fname);
+
+  Params p;
+  p.nx = parse_parameter<int>(as, "nx", 10);
+  p.ny = parse_parameter<int>(as, "ny", p.nx);
+  p.nz = parse_parameter<int>(as, "nz", p.ny);
+  p.load_imbalance = parse_parameter<float>(as, "load_imbalance", 0);
+  p.numthreads = parse_parameter<int>(as, "numthreads", 1);
+  p.mv_overlap_comm_comp = parse_parameter<int>(as, "mv_overlap_comm_comp", 0);
+  p.name = parse_parameter<std::string>(as, "name", "");
+  p.verify_solution = parse_parameter<int>(as, "verify_solution", 0);
+  p.precision = parse_parameter<std::string>(as, "precision", "f64");
+  p.max_iters = parse_parameter<int>(as, "max_iters", 200);
+  p.abs_tol = parse_parameter<double>(as, "abs_tol", std::numeric_limits<double>::epsilon());
+  p.rel_tol = parse_parameter<double>(as, "rel_tol", 0.0);
+  p.refine_k = parse_parameter<int>(as, "refine_k", 0);
+
+  // print_params=1 on the command line: print the parsed parameters and stop
+  // (no GPU needed); an input_file replaces the other arguments, as in the
+  // reference (utils.cpp:58-64)
+  if (print_params == 1) {
+    std::cout << "nx " << p.nx << "\nny " << p.ny << "\nnz " << p.nz << "\nverify_solution "
+              << p.verify_solution << "\nname " << p.name << "\nload_imbalance "
+              << p.load_imbalance << "\nprecision " << p.precision << "\nmax_iters "
+              << p.max_iters << "\nabs_tol " << p.abs_tol << "\nrel_tol " << p.rel_tol
+              << "\nrefine_k " << p.refine_k << std::endl;
+    return 0;
+  }
+
+  // main.cpp:116-130
+  if ((long long)p.nx * p.ny * p.nz <= 0 || p.nx < 0 || p.ny < 0 || p.nz < 0) {
+    std::cout << "One or more processors have 0 equations. Not currently supported. Exiting."
+              << std::endl;
+    return 1;
+  }
+
+  std::ostringstream prefix;
+  prefix << "miniFE." << p.nx << "x" << p.ny << "x" << p.nz << ".";
+  if (!p.name.empty()) prefix << p.name << ".";
+  YamlDoc doc("miniFE", "2.0", prefix.str());
+
+  // add_params_to_yaml / add_configuration_to_yaml / add_timestring_to_yaml
+  // (main.cpp:190-247)
+  auto* grp = doc.add("Global Run Parameters", "");
+  auto* dims = grp->add("dimensions", "");
+  dims->add("nx", p.nx);
+  dims->add("ny", p.ny);
+  dims->add("nz", p.nz);
+  grp->add("load_imbalance", p.load_imbalance);
+  grp->add("mv_overlap_comm_comp", p.mv_overlap_comm_comp == 1 ? "1 (yes)" : "0 (no)");
+  grp->add("number of processors", 1);
+  struct utsname un;
+  const bool have_un = uname(&un) == 0;
+  char host[256] = "unknown";
+  gethostname(host, sizeof(host) - 1);
+  auto* plat = doc.add("Platform", "");
+  plat->add("hostname", host);
+  plat->add("kernel name", have_un ? un.sysname : "unknown");
+  plat->add("kernel release", have_un ? un.release : "unknown");
+  plat->add("processor", have_un ? un.machine : "unknown");
+  auto* build = doc.add("Build", "");
+  build->add("CXX", "g++ (host), nvcc sm_103a (device)");
+  build->add("CXXFLAGS", "-O2 -std=c++17");
+  build->add("using MPI", "no");
+  {
+    std::time_t raw = std::time(nullptr);
+    std::tm* t = std::localtime(&raw);
+    char ts[64];
+    std::snprintf(ts, sizeof(ts), "%04d-%02d-%02d, %02d-%02d-%02d", t->tm_year + 1900,
+                  t->tm_mon + 1, t->tm_mday, t->tm_hour, t->tm_min, t->tm_sec);
+    doc.add("Run Date/Time", ts);
+  }
+  // compute_imbalance on one rank (ref/utils/imbalance.hpp:167)
+  auto* imb = doc.add("Rows-per-proc Load Imbalance", "");
+  imb->add("Largest (from avg, %)", 0);
+  imb->add("Std Dev (%)", 0);
+
+  mfe_ctx* ctx = nullptr;
+  check(nullptr, mfe_ctx_create(0, &ctx), "mfe_ctx_create");
+
+  double t_total = 0, t0 = now();
+  std::cout.width(30);
+  std::cout << "creating/filling mesh...";
+  const double t_mesh = now() - t0;  // the mesh is implicit in the box dimensions
+  t_total += t_mesh;
+  std::cout << t_mesh << "s, total time: " << t_total << std::endl;
+
+  int64_t nrows = 0, nnz = 0;
+  check(ctx, mfe_box_dims(p.nx, p.ny, p.nz, &nrows, &nnz), "mfe_box_dims");
+  mfe_csr A;
+  check(ctx, mfe_csr_alloc(ctx, nrows, nnz, MFE_F64, &A), "mfe_csr_alloc");
+  double *b = nullptr, *x = nullptr;
+  check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&b), "mfe_device_alloc");
+  check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&x), "mfe_device_alloc");
+
+  t0 = now();
+  check(ctx, mfe_generate_structure(ctx, p.nx, p.ny, p.nz, &A), "mfe_generate_structure");
+  check(ctx, mfe_synchronize(ctx), "mfe_synchronize");
+  const double gen_structure = now() - t0;
+  t_total += gen_structure;
+  print_timed("generating matrix structure...", gen_structure, t_total);
+
+  t0 = now();
+  check(ctx, mfe_assemble(ctx, p.nx, p.ny, p.nz, nullptr, &A, b, 1), "mfe_assemble");
+  check(ctx, mfe_synchronize(ctx), "mfe_synchronize");
+  const double fe_assembly = now() - t0;
+  t_total += fe_assembly;
+  print_timed("assembling FE data...", fe_assembly, t_total);
+  // both impose_dirichlet passes run inside the assembly kernel
+  print_timed("imposing Dirichlet BC...", 0.0, t_total);
+  print_timed("imposing Dirichlet BC...", 0.0, t_total);
+  print_timed("making matrix indices local...", 0.0, t_total);
+
+  doc.add("Matrix structure generation", "")->add("Mat-struc-gen Time", gen_structure);
+  doc.add("FE assembly", "")->add("FE assembly Time", fe_assembly);
+
+  // compute_matrix_stats (ref/utils/compute_matrix_stats.hpp:44-111), one rank
+  {
+    auto* ma = doc.add("Matrix attributes", "");
+    ma->add("Global Nrows", (size_t)nrows);
+    ma->add("Global NNZ", (size_t)nnz);
+    const double invGB = 1.0 / (1024 * 1024 * 1024);
+    double memGB = invGB * nrows * sizeof(int);
+    memGB += invGB * nrows * sizeof(int);
+    memGB += invGB * nnz * sizeof(int);
+    memGB += invGB * nnz * sizeof(double);
+    ma->add("Global Memory (GB)", memGB);
+    ma->add("Pll Memory Overhead (MB)", 0);
+    ma->add("Rows per proc MIN", (size_t)nrows);
+    ma->add("Rows per proc MAX", (size_t)nrows);
+    ma->add("Rows per proc AVG", (double)nrows);
+    ma->add("NNZ per proc MIN", (size_t)nnz);
+    ma->add("NNZ per proc MAX", (size_t)nnz);
+    ma->add("NNZ per proc AVG", (double)nnz);
+  }
+
+  // x = 0 (Vector is zero-filled, ref/src/Vector.hpp:49-51)
+  check(ctx, mfe_waxpby(ctx, nrows, 0.0, b, 0.0, b, x), "mfe_waxpby");
+
+  mfe_cg_opts o;
+  mfe_cg_opts_default(&o);
+  o.max_iter = p.max_iters;
+  o.tol = p.abs_tol;
+  if (p.rel_tol > 0) {
+    o.tol = p.rel_tol;
+    o.tol_mode = MFE_TOL_RELATIVE;
+  }
+  o.precision = p.precision == "mixed" ? MFE_PREC_MIXED : MFE_PREC_F64;
+  o.refine_k = p.refine_k;
+  std::cout << "Starting CG solver ... " << std::endl;
+  mfe_cg_result r;
+  const mfe_status st = mfe_cg_solve(ctx, &A, b, x, &o, &r);
+  if (st == MFE_BREAKDOWN) std::cerr << "miniFE::cg_solve ERROR, numerical breakdown!" << std::endl;
+  else if (st != MFE_OK && st != MFE_MAXITER) check(ctx, st, "mfe_cg_solve");
+  std::cout << "Initial Residual = " << r.normr0 << std::endl;
+  std::cout << "Final Resid Norm: " << r.normr << std::endl;
+
+  int verify_result = 0;
+  if (p.verify_solution > 0) {
+    std::cout << "verifying solution at ~ (0.5, 0.5, 0.5) ..." << std::endl;
+    double max_err = 0;
+    int passed = 0;
+    check(ctx, mfe_verify_solution(ctx, p.nx, p.ny, p.nz, x, 0.06, 0, &max_err, &passed),
+          "mfe_verify_solution");
+    if (passed) std::cout << "solution matches analytic solution to within 0.06 or better." << std::endl;
+    else std::cout << "max absolute error is " << max_err << ":" << std::endl;
+    verify_result = passed ? 0 : 1;
+  }
+
+  // per-operation times: the solve fuses the operations into three kernels
+  // per iteration, so each operation is timed alone on the solved system and
+  // scaled by the reference's operation counts (driver.hpp:331-335)
+  const int it = r.num_iters;
+  double t_mv = 0, t_dot = 0, t_wax = 0;
+  {
+    double* w = nullptr;
+    check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&w), "mfe_device_alloc");
+    double d = 0;
+    const int reps = 5;
+    check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+    check(ctx, mfe_synchronize(ctx), "sync");
+    double s0 = now();
+    for (int i = 0; i < reps; ++i) check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+    check(ctx, mfe_synchronize(ctx), "sync");
+    t_mv = (now() - s0) / reps;
+    s0 = now();
+    for (int i = 0; i < reps; ++i) check(ctx, mfe_dot(ctx, nrows, x, w, &d), "mfe_dot");
+    t_dot = (now() - s0) / reps;
+    s0 = now();
+    for (int i = 0; i < reps; ++i) check(ctx, mfe_waxpby(ctx, nrows, 1.0, x, 0.5, w, w), "mfe_waxpby");
+    check(ctx, mfe_synchronize(ctx), "sync");
+    t_wax = (now() - s0) / reps;
+    mfe_device_free(ctx, w);
+  }
+  const double total = r.times[4];
+  // driver.hpp:314-401, with global_nrows = nx*ny*nz as in the reference
+  grp->add("ScalarType", "double");
+  grp->add("GlobalOrdinalType", "int");
+  grp->add("LocalOrdinalType", "int");
+  auto* cg = doc.add("CG solve", "");
+  cg->add("Iterations", it);
+  cg->add("Final Resid Norm", r.normr);
+  const double global_nrows = (double)p.nx * p.ny * p.nz;
+  double mv_flops = (double)nnz * 2.0 * (it + 1);
+  double dot_flops = global_nrows * 2.0 * (2 * it);
+  double waxpy_flops = global_nrows * 3.0 * (3 * it + 2);
+  const double tw = t_wax * (3 * it + 2), td = t_dot * (2 * it), tm = t_mv * (it + 1);
+  auto mflops = [](double f, double t) { return t > 1e-4 ? 1e-6 * f / t : -1.0; };
+  auto add_rate = [&](const char* key, double f, double t) {
+    const double m = mflops(f, t);
+    if (m >= 0) cg->add(key, m);
+    else cg->add(key, "inf");
+  };
+  cg->add("WAXPY Time", tw);
+  cg->add("WAXPY Flops", waxpy_flops);
+  add_rate("WAXPY Mflops", waxpy_flops, tw);
+  cg->add("DOT Time", td);
+  cg->add("DOT Flops", dot_flops);
+  add_rate("DOT Mflops", dot_flops, td);
+  cg->add("MATVEC Time", tm);
+  cg->add("MATVEC Flops", mv_flops);
+  add_rate("MATVEC Mflops", mv_flops, tm);
+  auto* tot = cg->add("Total", "");
+  const double total_flops = mv_flops + dot_flops + waxpy_flops;
+  tot->add("Total CG Time", total);
+  tot->add("Total CG Flops", total_flops);
+  const double tm_rate = mflops(total_flops, total);
+  if (tm_rate >= 0) tot->add("Total CG Mflops", tm_rate);
+  else tot->add("Total CG Mflops", "inf");
+  cg->add("Time per iteration", it > 0 ? total / it : 0.0);
+
+  auto* gpu = doc.add("GB300", "");
+  gpu->add("precision", p.precision);
+  gpu->add("tolerance mode", p.rel_tol > 0 ? "relative" : "absolute");
+  gpu->add("tolerance", o.tol);
+  gpu->add("Initial Resid Norm", r.normr0);
+  gpu->add("True Final Resid Norm", r.final_resid);
+  gpu->add("reliable updates", r.refinements);
+  gpu->add("op times", "standalone kernels scaled by operation counts");
+  gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) / t_mv * 1e-9);
+  if (p.verify_solution > 0) gpu->add("verification", verify_result == 0 ? "passed" : "failed");
+
+  mfe_device_free(ctx, b);
+  mfe_device_free(ctx, x);
+  mfe_csr_free(ctx, &A);
+  mfe_ctx_destroy(ctx);
+  doc.add("Total Program Time", now() - t_program);
+  doc.generate();
+  return verify_result;
+}

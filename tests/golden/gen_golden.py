@@ -110,6 +110,23 @@ def main():
         out["element/ref_elem_vec"] = np.fromfile(os.path.join(d, "elem_vec.f64"), np.float64)
         out["element/ref_grad_vals"] = np.fromfile(os.path.join(d, "grad_vals.f64"), np.float64)
     out["element/utest_elem_mat"] = utest_known_answer()
+    # the reference's own YAML report (oracle/_ref/miniFE.x nx=10
+    # verify_solution=1): its key tree, one "indent:key" line per entry
+    with tempfile.TemporaryDirectory() as tmp:
+        exe = os.path.join(ROOT, "oracle", "_ref", "miniFE.x")
+        run = subprocess.run([exe, "nx=10", "verify_solution=1"], cwd=tmp, capture_output=True,
+                             text=True, check=True)
+        yml = [f for f in os.listdir(tmp) if f.endswith(".yaml")][0]
+        keys = []
+        for line in open(os.path.join(tmp, yml)):
+            if ":" not in line:
+                continue
+            indent = len(line) - len(line.lstrip(" "))
+            keys.append("%d:%s" % (indent, line.strip().split(":")[0]))
+        with open(os.path.join(HERE, "ref_yaml_keys.txt"), "w") as f:
+            f.write("\n".join(keys) + "\n")
+        with open(os.path.join(HERE, "ref_stdout_nx10.txt"), "w") as f:
+            f.write(run.stdout)
     np.savez_compressed(os.path.join(HERE, "minife_golden.npz"), **out)
     with open(os.path.join(HERE, "golden_hashes.json"), "w") as f:
         json.dump(hashes, f, indent=1, sort_keys=True)

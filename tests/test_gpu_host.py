@@ -1,0 +1,94 @@
+"""GPU tests of the host-side drop-in: miniFE.x (the reference's CLI, phases
+and YAML report) and the C++ shim header (reference types and signatures)."""
+import os
+import subprocess
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # pragma: no cover
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+DRIVER = os.path.join(ROOT, "minife_gb300", "miniFE.x")
+
+
+def yaml_keys(path):
+    keys = []
+    for line in open(path):
+        if ":" not in line:
+            continue
+        indent = len(line) - len(line.lstrip(" "))
+        keys.append("%d:%s" % (indent, line.strip().split(":")[0]))
+    return keys
+
+
+def yaml_value(path, key):
+    for line in open(path):
+        if line.strip().startswith(key + ":"):
+            return line.split(":", 1)[1].strip()
+    return None
+
+
+def run_driver(tmp_path, *args):
+    from minife_gb300 import build
+    build.build()
+    r = subprocess.run([DRIVER, *args], cwd=tmp_path, capture_output=True, text=True)
+    ymls = [f for f in os.listdir(tmp_path) if f.endswith(".yaml")]
+    return r, (os.path.join(tmp_path, ymls[0]) if ymls else None)
+
+
+def test_minife_x_reference_run(tmp_path):
+    """./miniFE.x nx=10 verify_solution=1 (ref/src/run_test:3): exit 0, the
+    reference's YAML key tree, iterations and residual like the reference."""
+    r, yml = run_driver(tmp_path, "nx=10", "verify_solution=1")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "solution matches analytic solution" in r.stdout
+    ref = open(os.path.join(ROOT, "tests", "golden", "ref_yaml_keys.txt")).read().split("\n")
+    ref = [k for k in ref if k]
+    ours = yaml_keys(yml)
+    missing = [k for k in ref if k not in ours]
+    assert not missing, missing
+    assert os.path.basename(yml).startswith("miniFE.10x10x10.")
+    it = int(yaml_value(yml, "Iterations"))
+    assert abs(it - 31) <= 2  # reference: 31 iterations (tests/golden, 10x10x10)
+    assert float(yaml_value(yml, "Final Resid Norm")) < 1e-14
+    assert int(yaml_value(yml, "Global NNZ")) == 29791
+
+
+def test_minife_x_mixed_relative(tmp_path):
+    r, yml = run_driver(tmp_path, "-nx", "24", "-ny", "20", "-nz", "16", "precision=mixed",
+                        "rel_tol=1e-8", "max_iters=3000", "verify_solution=1", "name=mx")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert os.path.basename(yml).startswith("miniFE.24x20x16.mx.")
+    true_res = float(yaml_value(yml, "True Final Resid Norm"))
+    r0 = float(yaml_value(yml, "Initial Resid Norm"))
+    assert true_res <= 1e-8 * r0
+
+
+def test_cpp_shim_matches_oracle(tmp_path):
+    exe = os.path.join(tmp_path, "shim_solve")
+    from minife_gb300 import build
+    build.build()
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "shim_solve.cpp"), "-L",
+                    os.path.join(ROOT, "minife_gb300"), "-lminife_gb300",
+                    "-Wl,-rpath," + os.path.join(ROOT, "minife_gb300"), "-o", exe], check=True)
+    out = subprocess.run([exe, "10", "9", "8"], capture_output=True, text=True, check=True).stdout
+    v = {k: float(x) for k, x in (ln.split() for ln in out.splitlines())}
+    ro, cols, vals, b = O.build_system(10, 9, 8)
+    s = 0.0
+    for a in vals:  # same summation order as the shim program
+        s += a
+    assert v["vals_sum"] == s
+    x = 1.0 / (1.0 + np.arange(ro.size - 1))
+    y = O.matvec(ro, cols, vals, x)
+    assert abs(v["matvec_dot"] - O.dot(x, y)) <= 1e-13 * abs(O.dot(np.abs(x), np.abs(y)))
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, b)
+    assert abs(int(v["num_iters"]) - it) <= 2
+    assert abs(v["x_sum"] - xo.sum()) <= 1e-11 * np.abs(xo).sum()
