@@ -200,13 +200,47 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
         ok = false;
         break;
       }
-      if (active) {
+      const bool vxm = ix > 0, vxp = ix < P.Nx - 1;
+      const bool vym = iy > 0, vyp = iy < P.Ny - 1;
+      const bool vzm = iz > 0, vzp = iz < P.Nz - 1;
+      const bool interior = active && vxm && vxp && vym && vyp && vzm && vzp;
+      // warps whose rows all have the full 27 columns (about three in four
+      // at 256^3) take the unmasked code: value k of a row is rowv[k]
+      const bool all_interior = __all_sync(0xffffffffu, interior);
+      if (all_interior) {
         const T* sv = st0 + (size_t)s * stage_elems;
         const T* sx = sv + P.capv;
         const T* rowv = sv + (roff - s_vbase[s]);
-        const bool vxm = ix > 0, vxp = ix < P.Nx - 1;
-        const bool vym = iy > 0, vyp = iy < P.Ny - 1;
-        const bool vzm = iz > 0, vzp = iz < P.Nz - 1;
+        const T* xc = sx + 4 * (size_t)P.capx + (r - s_xbase[s][4]);
+        T s0 = T(0), s1 = T(0);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const int off = (j / 3 - 1) * P.NxNy + (j % 3 - 1) * P.Nx;
+          const T* seg = sx + (size_t)j * P.capx + (r + off - s_xbase[s][j]);
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int k = j * 3 + dx + 1;
+            if (k & 1) s1 = fma(rowv[k], seg[dx], s1);
+            else s0 = fma(rowv[k], seg[dx], s0);
+          }
+        }
+        const T sum = s0 + s1;
+        const T xr = xc[0];
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);  // stage s no longer read by this warp
+        if (MODE == BOX_RESID) {
+          const double res = P.b[r] - widen(sum);
+          if (P.y32 != nullptr) P.y32[r] = (float)res;
+          else P.y[r] = (T)res;
+          dacc = fma(res, res, dacc);
+        } else {
+          P.y[r] = sum;
+          if (MODE == BOX_DOT) dacc = fma(widen(sum), widen(xr), dacc);
+        }
+      } else if (active) {
+        const T* sv = st0 + (size_t)s * stage_elems;
+        const T* sx = sv + P.capv;
+        const T* rowv = sv + (roff - s_vbase[s]);
         const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp;
         const int cxy = cx * cy;
         // x[r] lives in the centre segment (j = 4) of every tile
