@@ -411,8 +411,38 @@ def run_gpu(args):
     return 0
 
 
+def run_probe(args):
+    """Small fixed workloads for profiler captures (ncu): 'spmv' = the box
+    system at --dims^3, three FP64 and three FP32 matvecs; 'cg' = the system
+    and a 4-iteration CG solve."""
+    import torch
+    import minife_gb300 as M
+    torch.cuda.set_device(0)
+    d = args.dims
+    A, b = M.build_system(d, d, d)
+    if args.probe == "spmv":
+        x = torch.randn(A.nrows, dtype=torch.float64, device="cuda")
+        y = torch.empty_like(x)
+        for _ in range(3):
+            M.matvec(A, x, y)
+        A32 = M.to_f32(A)
+        x32 = x.float()
+        y32 = torch.empty_like(x32)
+        for _ in range(3):
+            M.matvec(A32, x32, y32)
+    else:
+        x = torch.zeros_like(b)
+        M.cg_solve(A, b, x, max_iter=4, tol=TOL, tol_mode="relative")
+    torch.cuda.synchronize()
+    print("probe %s %d^3 done" % (args.probe, d))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
+    ap.add_argument("--probe", choices=["spmv", "cg"], default=None,
+                    help="run a small fixed workload for a profiler capture and exit")
+    ap.add_argument("--dims", type=int, default=128)
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
@@ -427,6 +457,8 @@ def main():
     ap.add_argument("--ref-iters", type=int, default=401,
                     help="CG iterations of the 256^3 solve to 1e-8 (the GPU solve's count)")
     args = ap.parse_args()
+    if args.probe:
+        return run_probe(args)
     if args.impl == "reference":
         return run_reference(args)
     return run_gpu(args)
