@@ -32,7 +32,7 @@ __all__ = [
     "MiniFEError", "Context", "CSRMatrix", "CGResult", "default_context", "box_dims",
     "generate_matrix_structure", "assemble_FE_data", "impose_dirichlet", "box_bc_rows",
     "build_system", "matvec", "matvec_and_dot", "dot", "waxpby", "fused_waxpby", "cg_solve",
-    "cg_solve_host", "verify_solution", "element_gradient", "to_f32", "spmm",
+    "cg_solve_host", "cg_solve_multi", "verify_solution", "element_gradient", "to_f32", "spmm",
 ]
 
 DBL_EPSILON = 2.220446049250313e-16
@@ -377,6 +377,30 @@ def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
     if not (st == 0 or (allow_breakdown and st in (_abi.MFE_BREAKDOWN, _abi.MFE_MAXITER))):
         ctx.check(st, "mfe_cg_solve")
     return _result(ctx, r, record_history)
+
+
+def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPSILON,
+                   tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
+                   ctx: Context | None = None) -> list:
+    """nrhs independent CG solves on one box matrix advanced together (one
+    matrix read per iteration for all of them).  B, X: device (n, nrhs) FP64,
+    contiguous; X holds the initial guesses and receives the solutions.
+    nrhs divides 32.  precision "f64" runs the reference's CG per column
+    (ref/src/cg_solve.hpp:69); "mixed" runs FP32 products with FP64 reliable
+    updates.  Returns one CGResult per right-hand side."""
+    ctx = ctx or default_context()
+    if B.dim() != 2 or tuple(X.shape) != tuple(B.shape):
+        raise ValueError("B and X must be (n, nrhs) with the same shape")
+    nrhs = B.shape[1]
+    m = A.c()
+    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k)
+    res = (MfeCgResult * nrhs)()
+    st = ctx.lib.mfe_cg_solve_multi(ctx.h, ctypes.byref(m), nrhs, _ptr(B), _ptr(X),
+                                    ctypes.byref(o), res)
+    if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
+        ctx.check(st, "mfe_cg_solve_multi")
+    return [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status, tuple(r.times),
+                     r.refinements, None) for r in res]
 
 
 def cg_solve_host(row_offsets, cols, vals, b, x, max_iter=200, tol=DBL_EPSILON,

@@ -29,6 +29,7 @@ SOURCES = {
     "mfe_spmv_box.cu": [],
     "mfe_noalloc.cu": [],
     "mfe_mixed.cu": [],
+    "mfe_multi.cu": [],
     "mfe_cg.cu": [],
 }
 

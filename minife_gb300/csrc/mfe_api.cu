@@ -579,8 +579,12 @@ mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X,
 mfe_status mfe_cg_solve_multi(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const double* B,
                               double* X, const mfe_cg_opts* opts, mfe_cg_result* results)
 {
-  (void)A; (void)nrhs; (void)B; (void)X; (void)opts; (void)results;
-  return fail(ctx, MFE_NOT_SUPPORTED, "multi-RHS CG is not built yet");
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, A));
+  if (!opts || !results || (A->nrows > 0 && (!B || !X))) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  if (A->nrows == 0) return fail(ctx, MFE_BAD_ARG, "empty matrix");
+  MFE_TRY(set_device(ctx));
+  return cg_multi(ctx, A, nrhs, B, X, opts, results);
 }
 
 mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims,

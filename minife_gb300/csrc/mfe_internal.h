@@ -96,6 +96,10 @@ mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const doubl
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,
                     const mfe_cg_opts* opts, mfe_cg_result* res);
 
+// ---- multi-RHS CG (mfe_multi.cu) ----
+mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64, int nrhs, const double* B, double* X,
+                    const mfe_cg_opts* opts, mfe_cg_result* results);
+
 // ---- BLAS-1 and CG (mfe_cg.cu) ----
 mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
                       double* dev_out);

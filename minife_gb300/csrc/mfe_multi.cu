@@ -1,0 +1,759 @@
+// Multi-right-hand-side CG on one box matrix: nrhs independent CG solves
+// advanced together so every iteration reads the matrix once.
+//
+// Layout: X, B, and every work vector are row-major n x nrhs (X[i*nrhs + j]),
+// so the rows a tile of the 27-point stencil touches are contiguous blocks of
+// nrhs values.  k_spmm_box stages a tile's values and its nine x-row
+// segments (all right-hand sides) into shared memory with bulk async copies
+// (producer warp, full/empty mbarriers, as k_spmv_box) and runs one warp per
+// row and one lane per right-hand side: the row's 27 values are broadcast to
+// the warp, and lane j reads x[col*nrhs + j], so shared-memory reads are
+// conflict-free.  Each lane accumulates its right-hand side's dot in FP64.
+//
+// The solver is the mixed-precision one of mfe_mixed.cu applied per
+// right-hand side: FP32 matrix copy, FP32 vectors, FP64 dots and scalars
+// (alpha_j, beta_j), FP64 solution; reliable updates (x += x32, R = B - A X in
+// FP64) happen for all right-hand sides together every refine_k iterations or
+// when any unconverged right-hand side's recursive residual drops tenfold or
+// claims convergence.  A converged right-hand side is frozen (alpha_j = 0).
+// nrhs must divide 32 (1, 2, 4, 8, 16, 32).
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <map>
+#include <mutex>
+#include <utility>
+
+#include "mfe_box.cuh"
+#include "mfe_common.cuh"
+#include "mfe_internal.h"
+
+namespace mfe {
+
+constexpr int kMaxRhs = 32;
+constexpr int kTileRowsM = 16;  // rows per tile = consumer warps per CTA
+constexpr int kStagesM = 2;
+constexpr int kVT = 256;
+constexpr int kMaxPartM = 2048;
+
+struct MultiState {
+  double rr[kMaxRhs], rr_new[kMaxRhs], pAp[kMaxRhs], beta[kMaxRhs];
+  double rr_true[kMaxRhs], rr_at_update[kMaxRhs], normr0[kMaxRhs], tol_abs[kMaxRhs];
+  double normr_true[kMaxRhs];
+  int done[kMaxRhs];
+  int iters[kMaxRhs];  // iterations until each right-hand side converged
+  int nrhs, k, max_iter, since, refine_k, gate, cont, first, updates, status, tol_mode;
+  unsigned err;
+  double delta2;
+};
+
+enum MMode { MM_DOT = 1, MM_RESID = 2 };
+
+template <typename T, typename RT>
+struct SpmmParams {
+  int n, Nx, Ny, Nz, NxNy, nrhs;
+  int64_t nnz;
+  const T* __restrict__ vals;
+  const T* __restrict__ x;  // n x nrhs
+  T* __restrict__ y;        // n x nrhs (DOT)
+  const double* __restrict__ b;  // n x nrhs (RESID)
+  RT* __restrict__ yres;         // RESID output: b - A x rounded to RT
+  int capv, capx;                // stage capacities (elements)
+  double* partials;              // [grid][32]
+  unsigned* ticket;
+  double* out;                   // [32] totals
+  const int* gate;               // nullable
+  unsigned* err;
+};
+
+// Per-lane dots of the block summed over its warps, then over blocks in
+// block order by the last block: out[j] = total of lane j.  red: >= 33*32.
+__device__ void multi_dot_reduce(double v, double* red, double* partials, unsigned* ticket,
+                                 double* out, int nlanes)
+{
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  red[warp * 32 + lane] = v;
+  __syncthreads();
+  __shared__ bool am_last;
+  if (threadIdx.x < 32) {
+    double s = 0.0;
+    for (int w = 0; w < nw; ++w) s += red[w * 32 + threadIdx.x];
+    partials[(size_t)blockIdx.x * 32 + threadIdx.x] = s;
+  }
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) am_last = (atomicAdd(ticket, 1u) == gridDim.x - 1);
+  __syncthreads();
+  if (!am_last) return;
+  __threadfence();
+  if (threadIdx.x < nlanes) {
+    double s = 0.0;
+    for (unsigned bl = 0; bl < gridDim.x; ++bl) s += __ldcg(&partials[(size_t)bl * 32 + threadIdx.x]);
+    out[threadIdx.x] = s;
+  }
+  if (threadIdx.x == 0) *ticket = 0u;
+}
+
+template <typename T, int MODE, typename RT>
+__global__ void __launch_bounds__(kTileRowsM * 32 + 32, 2) k_spmm_box(SpmmParams<T, RT> P)
+{
+  constexpr int R = kTileRowsM, S = kStagesM;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full[S], empty[S];
+  __shared__ int64_t s_vbase[S];
+  __shared__ int64_t s_xbase[S][9];
+  __shared__ int s_ok[S];
+  __shared__ double red[(R + 1) * 32];
+  constexpr int VA = 16 / sizeof(T);
+  const size_t stage_elems = (size_t)P.capv + 9 * (size_t)P.capx;
+  T* const st0 = reinterpret_cast<T*>(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = (P.n + R - 1) / R;
+  const int nr = P.nrhs;
+  if (P.gate != nullptr && *P.gate == 0) return;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], R);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  double dacc = 0.0;
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = true;
+      unsigned issued[S] = {};
+      int it = 0;
+      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
+        const int s = it % S;
+        if (it >= S) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / S) - 1) & 1));
+        if (!ok) break;
+        T* sv = st0 + (size_t)s * stage_elems;
+        T* sx = sv + P.capv;
+        const int r0 = tile * R, r1 = min(P.n, r0 + R);
+        const int64_t a = row_offset_of32(r0, P.Nx, P.Ny, P.Nz, P.NxNy);
+        const int64_t e = row_offset_of32(r1, P.Nx, P.Ny, P.Nz, P.NxNy);
+        const int64_t av = a & ~(int64_t)(VA - 1);
+        int64_t bv = min((e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
+        if (bv < av) bv = av;
+        bool fits = max(bv, e) - av <= P.capv;
+        const int64_t ntot = (int64_t)P.n * nr;
+        int64_t xlo[9], xbl[9], xhi[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const int off = (j / 3 - 1) * P.NxNy + (j % 3 - 1) * P.Nx;
+          const int lo = min(max(r0 + off - 1, 0), P.n);
+          int hi = min(r1 + off + 1, P.n);
+          if (hi < lo) hi = lo;
+          const int64_t elo = (int64_t)lo * nr, ehi = (int64_t)hi * nr;
+          const int64_t lal = elo & ~(int64_t)(VA - 1);
+          int64_t bl = min((ehi + VA - 1) & ~(int64_t)(VA - 1), ntot & ~(int64_t)(VA - 1));
+          if (bl < lal) bl = lal;
+          xlo[j] = lal;
+          xbl[j] = bl;
+          xhi[j] = ehi;
+          fits = fits && (max(bl, ehi) - lal <= P.capx);
+        }
+        ++issued[s];
+        if (!fits) {
+          // cannot happen for the stage capacities the host computes
+          atomicOr(P.err, ERR_TILE_OVERFLOW);
+          s_ok[s] = 0;
+          mbar_arrive_expect_tx(&full[s], 0);
+          continue;
+        }
+        s_ok[s] = 1;
+        s_vbase[s] = av;
+        unsigned bytes = (unsigned)((bv - av) * sizeof(T));
+        for (int64_t k = bv; k < e; ++k) sv[k - av] = P.vals[k];
+        for (int j = 0; j < 9; ++j) {
+          s_xbase[s][j] = xlo[j];
+          T* dx = sx + (size_t)j * P.capx;
+          for (int64_t k = xbl[j]; k < xhi[j]; ++k) dx[k - xlo[j]] = P.x[k];
+          bytes += (unsigned)((xbl[j] - xlo[j]) * sizeof(T));
+        }
+        fence_proxy_async_smem();
+        mbar_arrive_expect_tx(&full[s], bytes);
+        if (bv > av) bulk_g2s(sv, P.vals + av, (unsigned)((bv - av) * sizeof(T)), &full[s]);
+        for (int j = 0; j < 9; ++j)
+          if (xbl[j] > xlo[j])
+            bulk_g2s(sx + (size_t)j * P.capx, P.x + xlo[j],
+                     (unsigned)((xbl[j] - xlo[j]) * sizeof(T)), &full[s]);
+      }
+      if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        for (int s = 0; s < S; ++s)
+          if (issued[s]) mbar_wait_bounded(&full[s], (issued[s] - 1) & 1u);
+      }
+    }
+  } else {
+    const int lr = warp - 1;
+    const bool lane_on = lane < nr;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int s = it % S;
+      const int r = tile * R + lr;
+      const bool active = r < P.n;  // warp-uniform
+      const int rr = active ? r : P.n - 1;
+      const int iz = rr / P.NxNy, rem = rr - iz * P.NxNy, iy = rem / P.Nx, ix = rem - iy * P.Nx;
+      const int64_t roff = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
+      if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        break;
+      }
+      T sum = T(0);
+      T xr = T(0);
+      const bool ok = active && s_ok[s] != 0;
+      if (ok) {
+        const T* sv = st0 + (size_t)s * stage_elems;
+        const T* sx = sv + P.capv;
+        const T* rowv = sv + (roff - s_vbase[s]);
+        const bool vxm = ix > 0, vxp = ix < P.Nx - 1, vym = iy > 0, vyp = iy < P.Ny - 1;
+        const bool vzm = iz > 0, vzp = iz < P.Nz - 1;
+        const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp, cxy = cx * cy;
+        const int lj = lane_on ? lane : 0;
+        const T* xc = sx + 4 * (size_t)P.capx + ((int64_t)r * nr + lj - s_xbase[s][4]);
+        xr = xc[0];
+        T s0 = T(0), s1 = T(0);
+        int slot = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz) {
+          const bool vz = dz < 0 ? vzm : (dz > 0 ? vzp : true);
+          const int bz = dz < 0 ? 0 : (dz == 0 ? (int)vzm : (int)vzm + 1);
+#pragma unroll
+          for (int dy = -1; dy <= 1; ++dy) {
+            const bool vy = dy < 0 ? vym : (dy > 0 ? vyp : true);
+            const int by = dy < 0 ? 0 : (dy == 0 ? (int)vym : (int)vym + 1);
+            const int j = (dz + 1) * 3 + (dy + 1);
+            const int off = dz * P.NxNy + dy * P.Nx;
+            const T* seg = sx + (size_t)j * P.capx + ((int64_t)(r + off) * nr + lj - s_xbase[s][j]);
+            const int pbase = bz * cxy + by * cx;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+              const bool vx = dx < 0 ? vxm : (dx > 0 ? vxp : true);
+              const int bx = dx < 0 ? 0 : (dx == 0 ? (int)vxm : (int)vxm + 1);
+              const bool valid = vz && vy && vx;
+              const T v = rowv[valid ? pbase + bx : 0];
+              const T xv = *(valid ? seg + (int64_t)dx * nr : xc);
+              if (slot & 1) {
+                const T t1 = fma(v, xv, s1);
+                s1 = valid ? t1 : s1;
+              } else {
+                const T t0 = fma(v, xv, s0);
+                s0 = valid ? t0 : s0;
+              }
+              ++slot;
+            }
+          }
+        }
+        sum = s0 + s1;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (ok && lane_on) {
+        const int64_t idx = (int64_t)r * nr + lane;
+        if (MODE == MM_RESID) {
+          const double res = P.b[idx] - widen(sum);
+          P.yres[idx] = (RT)res;
+          dacc = fma(res, res, dacc);
+        } else {
+          P.y[idx] = sum;
+          dacc = fma(widen(sum), widen(xr), dacc);
+        }
+      }
+    }
+  }
+  multi_dot_reduce(warp == 0 ? 0.0 : dacc, red, P.partials, P.ticket, P.out, nr);
+}
+
+// lanes j, j+nrhs, j+2nrhs, ... of a warp hold right-hand side j: sum them
+// into lane j (nrhs divides 32)
+__device__ __forceinline__ double lane_group_sum(double v, int nrhs)
+{
+  for (int o = 16; o >= nrhs; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename V>
+__global__ void __launch_bounds__(kVT)
+    k_mr_p(int64_t ntot, int nrhs, const V* __restrict__ r, V* __restrict__ p, const MultiState* st)
+{
+  const int j = threadIdx.x % nrhs;
+  const bool first = st->first != 0;
+  const V beta = st->done[j] ? V(0) : (V)st->beta[j];
+  for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT)
+    p[i] = first ? r[i] : fma(beta, p[i], r[i]);
+}
+
+// x += alpha_j p, r -= alpha_j Ap, rr_new_j = r_j.r_j (FP64); x is the FP32
+// correction x32 in the mixed solver and the FP64 solution otherwise
+template <typename V>
+__global__ void __launch_bounds__(kVT)
+    k_mr_update(int64_t ntot, int nrhs, V* __restrict__ x, V* __restrict__ r,
+                const V* __restrict__ p, const V* __restrict__ Ap, MultiState* st,
+                double* partials, unsigned* ticket)
+{
+  __shared__ double red[(kVT / 32 + 1) * 32];
+  const int j = threadIdx.x % nrhs;
+  const V alpha = st->done[j] ? V(0) : (V)(st->rr[j] / st->pAp[j]);
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT) {
+    x[i] = fma(alpha, p[i], x[i]);
+    const V rv = fma(-alpha, Ap[i], r[i]);
+    r[i] = rv;
+    const double d = widen(rv);
+    acc = fma(d, d, acc);
+  }
+  acc = lane_group_sum(acc, nrhs);
+  if ((threadIdx.x & 31) >= nrhs) acc = 0.0;
+  multi_dot_reduce(acc, red, partials, ticket, st->rr_new, nrhs);
+}
+
+__global__ void __launch_bounds__(kVT)
+    k_mr_xupdate(int64_t ntot, double* __restrict__ x, float* __restrict__ x32, const MultiState* st)
+{
+  if (st->gate == 0) return;
+  for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT) {
+    x[i] += f2d_exact(x32[i]);
+    x32[i] = 0.0f;
+  }
+}
+
+// Mixed solver, one warp, after the update kernel: decide whether this
+// iteration ends with a reliable update (any open right-hand side whose
+// recursive residual fell tenfold since the last one or claims convergence,
+// refine_k iterations since the last one, or the iteration limit).
+__global__ void k_mr_decide(MultiState* st)
+{
+  const int j = threadIdx.x;
+  const int nr = st->nrhs;
+  bool trig = false, brk = false;
+  if (j < nr && !st->done[j]) {
+    brk = !(st->pAp[j] > 0.0);
+    const double t = st->rr_new[j];
+    trig = t < st->delta2 * st->rr_at_update[j] || t <= st->tol_abs[j] * st->tol_abs[j];
+  }
+  const bool any_trig = __any_sync(0xffffffffu, trig);
+  const bool any_brk = __any_sync(0xffffffffu, brk);
+  if (j == 0) {
+    st->k += 1;
+    st->since += 1;
+    st->first = 0;
+    if (any_brk) st->status = MFE_BREAKDOWN;
+    st->gate = st->status == 0 && (any_trig || st->since >= st->refine_k || st->k >= st->max_iter);
+  }
+}
+
+// Mixed solver, one warp, after the gated FP64 residual: per right-hand side
+// beta and rr from the true residual (reliable update) or the recursive one.
+__global__ void k_mr_after(MultiState* st, cudaGraphConditionalHandle h, int in_graph)
+{
+  const int j = threadIdx.x;
+  const int nr = st->nrhs;
+  const int gate = st->gate;
+  if (j < nr && !st->done[j] && st->status == 0) {
+    if (gate) {
+      st->normr_true[j] = sqrt(st->rr_true[j]);
+      if (st->normr_true[j] <= st->tol_abs[j]) {
+        st->done[j] = 1;
+        st->iters[j] = st->k;
+      } else {
+        st->beta[j] = st->rr_true[j] / st->rr[j];
+        st->rr[j] = st->rr_true[j];
+        st->rr_at_update[j] = st->rr_true[j];
+      }
+    } else {
+      st->beta[j] = st->rr_new[j] / st->rr[j];
+      st->rr[j] = st->rr_new[j];
+    }
+  }
+  const bool open = __any_sync(0xffffffffu, j < nr && !st->done[j]);
+  if (j == 0) {
+    if (gate) {
+      st->updates += 1;
+      st->since = 0;
+    }
+    st->gate = 0;
+    st->cont = open && st->status == 0 && st->k < st->max_iter;
+    if (in_graph) cudaGraphSetConditional(h, st->cont ? 1u : 0u);
+  }
+}
+
+// FP64 solver, one warp, after the update kernel of iteration k: the
+// reference's loop test per right-hand side (cg_solve.hpp: the loop runs
+// iteration k+1 while k+1 <= max_iter and normr > tol, normr being |r| at the
+// top of iteration k, i.e. before its update).
+__global__ void k_mr_after64(MultiState* st, cudaGraphConditionalHandle h, int in_graph)
+{
+  const int j = threadIdx.x;
+  const int nr = st->nrhs;
+  const int k = st->k + 1;
+  bool brk = false;
+  if (j < nr && !st->done[j]) {
+    brk = !(st->pAp[j] > 0.0);
+    if (k + 1 <= st->max_iter && st->normr_true[j] > st->tol_abs[j]) {
+      const double rn = st->rr_new[j];
+      st->beta[j] = rn / st->rr[j];
+      st->rr[j] = rn;
+      st->normr_true[j] = sqrt(rn);
+    } else {
+      st->done[j] = 1;
+      st->iters[j] = k;
+    }
+  }
+  const bool any_brk = __any_sync(0xffffffffu, brk);
+  const bool open = __any_sync(0xffffffffu, j < nr && !st->done[j]);
+  if (j == 0) {
+    st->k = k;
+    st->first = 0;
+    if (any_brk) st->status = MFE_BREAKDOWN;
+    st->cont = open && st->status == 0;
+    if (in_graph) cudaGraphSetConditional(h, st->cont ? 1u : 0u);
+  }
+}
+
+__global__ void k_mr_init(MultiState* st)
+{
+  const int j = threadIdx.x;
+  const int nr = st->nrhs;
+  if (j < nr) {
+    const double nrm = sqrt(st->rr_true[j]);
+    st->normr0[j] = nrm;
+    st->normr_true[j] = nrm;
+    if (st->tol_mode) st->tol_abs[j] *= nrm;
+    st->rr[j] = st->rr_true[j];
+    st->rr_at_update[j] = st->rr_true[j];
+    st->done[j] = !(nrm > st->tol_abs[j]);
+    st->iters[j] = 0;
+  }
+  const bool open = __any_sync(0xffffffffu, j < nr && !st->done[j]);
+  if (j == 0) st->cont = open && st->max_iter > 0;
+}
+
+__global__ void k_mr_begin(const MultiState* st, cudaGraphConditionalHandle h)
+{
+  cudaGraphSetConditional(h, st->cont ? 1u : 0u);
+}
+
+// ---------------------------------------------------------------------------
+// host
+// ---------------------------------------------------------------------------
+namespace {
+
+int spmm_capv() { return ((kTileRowsM * 27 + 8) + 3) & ~3; }
+int spmm_capx(int nrhs) { return (int)((((int64_t)(kTileRowsM + 2) * nrhs + 8) + 3) & ~3); }
+template <typename T>
+size_t spmm_smem(int nrhs)
+{
+  return (size_t)kStagesM * ((size_t)spmm_capv() + 9 * (size_t)spmm_capx(nrhs)) * sizeof(T);
+}
+
+// Sets the dynamic shared memory limit of one instantiation for nrhs and
+// returns its resident CTAs per SM; cached per (device, nrhs) so launches
+// recorded into a graph make no further runtime calls.
+template <typename T, int MODE, typename RT>
+mfe_status spmm_setup(mfe_ctx* ctx, int nrhs, int* per_sm)
+{
+  static std::map<std::pair<int, int>, int> cache;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_pair(ctx->device, nrhs);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    const size_t smem = spmm_smem<T>(nrhs);
+    MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_box<T, MODE, RT>,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int n = 1;
+    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                          &n, k_spmm_box<T, MODE, RT>, kTileRowsM * 32 + 32, smem));
+    it = cache.emplace(key, std::max(n, 1)).first;
+  }
+  if (per_sm) *per_sm = it->second;
+  return MFE_OK;
+}
+
+template <typename T, int MODE, typename RT>
+mfe_status launch_spmm_t(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const T* X, T* Y,
+                         const double* Bv, RT* yres, double* partials, unsigned* ticket,
+                         double* out, const int* gate, unsigned* err)
+{
+  SpmmParams<T, RT> P;
+  P.Nx = A->box_nx + 1;
+  P.Ny = A->box_ny + 1;
+  P.Nz = A->box_nz + 1;
+  P.NxNy = P.Nx * P.Ny;
+  P.n = (int)A->nrows;
+  P.nrhs = nrhs;
+  P.nnz = A->nnz;
+  P.vals = static_cast<const T*>(A->vals);
+  P.x = X;
+  P.y = Y;
+  P.b = Bv;
+  P.yres = yres;
+  P.capv = spmm_capv();
+  P.capx = spmm_capx(nrhs);
+  P.partials = partials;
+  P.ticket = ticket;
+  P.out = out;
+  P.gate = gate;
+  P.err = err;
+  const size_t smem = spmm_smem<T>(nrhs);
+  const int threads = kTileRowsM * 32 + 32;
+  int per_sm = 1;
+  MFE_TRY((spmm_setup<T, MODE, RT>(ctx, nrhs, &per_sm)));
+  const int64_t ntiles = ceil_div(A->nrows, (int64_t)kTileRowsM);
+  const int grid = (int)std::max<int64_t>(
+      1, std::min<int64_t>({ntiles, (int64_t)ctx->sm_count * per_sm, (int64_t)kMaxPartM}));
+  k_spmm_box<T, MODE, RT><<<grid, threads, smem, ctx->stream>>>(P);
+  return check_launch(ctx, "k_spmm_box");
+}
+
+template <typename V>
+struct MultiBufs {
+  V *r, *p, *Ap;
+  float* x32;  // mixed only
+  MultiState* st;
+  double* partials;  // [2][kMaxPartM][32]
+  unsigned* tickets;
+  unsigned* err;
+};
+
+int vgrid(mfe_ctx* ctx, int64_t n)
+{
+  return (int)std::max<int64_t>(
+      1, std::min<int64_t>({ceil_div(std::max<int64_t>(n, 1), (int64_t)kVT),
+                            (int64_t)ctx->sm_count * 8, (int64_t)kMaxPartM}));
+}
+
+// one iteration of the mixed solver: FP32 SpMM, FP32 vectors, gated FP64
+// reliable update
+mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, int nrhs,
+                            const double* B, double* X, const MultiBufs<float>& W,
+                            cudaGraphConditionalHandle h, int in_graph)
+{
+  const int64_t ntot = A64.nrows * (int64_t)nrhs;
+  k_mr_p<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
+  MFE_TRY(check_launch(ctx, "k_mr_p"));
+  MFE_TRY((launch_spmm_t<float, MM_DOT, float>(ctx, &A32, nrhs, W.p, W.Ap, nullptr, nullptr,
+                                                W.partials, W.tickets, W.st->pAp, nullptr, W.err)));
+  k_mr_update<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
+      ntot, nrhs, W.x32, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
+  MFE_TRY(check_launch(ctx, "k_mr_update"));
+  k_mr_decide<<<1, 32, 0, ctx->stream>>>(W.st);
+  MFE_TRY(check_launch(ctx, "k_mr_decide"));
+  k_mr_xupdate<<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, X, W.x32, W.st);
+  MFE_TRY(check_launch(ctx, "k_mr_xupdate"));
+  MFE_TRY((launch_spmm_t<double, MM_RESID, float>(ctx, &A64, nrhs, X, nullptr, B, W.r, W.partials,
+                                                   W.tickets, W.st->rr_true, &W.st->gate, W.err)));
+  k_mr_after<<<1, 32, 0, ctx->stream>>>(W.st, h, in_graph);
+  return check_launch(ctx, "k_mr_after");
+}
+
+// one iteration of the FP64 solver (the reference's CG per right-hand side)
+mfe_status multi_iter_f64(mfe_ctx* ctx, const mfe_csr& A64, int nrhs, double* X,
+                          const MultiBufs<double>& W, cudaGraphConditionalHandle h, int in_graph)
+{
+  const int64_t ntot = A64.nrows * (int64_t)nrhs;
+  k_mr_p<double><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
+  MFE_TRY(check_launch(ctx, "k_mr_p"));
+  MFE_TRY((launch_spmm_t<double, MM_DOT, double>(ctx, &A64, nrhs, W.p, W.Ap, nullptr, nullptr,
+                                                  W.partials, W.tickets, W.st->pAp, nullptr, W.err)));
+  k_mr_update<double><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
+      ntot, nrhs, X, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
+  MFE_TRY(check_launch(ctx, "k_mr_update"));
+  k_mr_after64<<<1, 32, 0, ctx->stream>>>(W.st, h, in_graph);
+  return check_launch(ctx, "k_mr_after64");
+}
+
+// Runs `body` (which launches one iteration on ctx->stream) as a CUDA graph
+// with a conditional while node driven by the state's `cont`, or, with
+// MFE_CG_EAGER set, as a host loop reading `cont` back each iteration.
+template <typename Body>
+mfe_status run_loop(mfe_ctx* ctx, MultiState* dev_st, MultiState* host_st, Body body)
+{
+  if (getenv("MFE_CG_EAGER") != nullptr) {
+    for (;;) {
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(host_st, dev_st, sizeof(MultiState),
+                                        cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!host_st->cont) return MFE_OK;
+      MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
+    }
+  }
+  cudaStream_t run_stream = ctx->stream, s = ctx->own_stream;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  mfe_status st = MFE_OK;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    ctx->stream = s;
+    e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+      k_mr_begin<<<1, 1, 0, s>>>(dev_st, h);
+      e = cudaStreamEndCapture(s, &g);
+    }
+    cudaGraphNode_t nodes[4];
+    size_t nn = 4;
+    if (e == cudaSuccess) e = cudaGraphGetNodes(g, nodes, &nn);
+    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+    memset(cp_buf, 0, sizeof(cp_buf));
+    cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+    cp->type = cudaGraphNodeTypeConditional;
+    cp->conditional.handle = h;
+    cp->conditional.type = cudaGraphCondTypeWhile;
+    cp->conditional.size = 1;
+    cudaGraphNode_t cnode;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
+    if (e == cudaSuccess) {
+      cudaGraph_t body_graph = cp->conditional.phGraph_out[0];
+      e = cudaStreamBeginCaptureToGraph(s, body_graph, nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        st = body(h, 1);
+        cudaGraph_t tmp;
+        const cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+        if (e == cudaSuccess) e = e2;
+      }
+    }
+    ctx->stream = run_stream;
+    if (e == cudaSuccess && st == MFE_OK) e = cudaGraphInstantiate(&ex, g, 0);
+    if (e == cudaSuccess && st == MFE_OK) e = cudaGraphLaunch(ex, ctx->stream);
+  }
+  if (ex) cudaGraphExecDestroy(ex);
+  if (g) cudaGraphDestroy(g);
+  if (st != MFE_OK) return st;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "multi-RHS CG graph");
+  return MFE_OK;
+}
+
+}  // namespace
+
+mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double* B, double* X,
+                    const mfe_cg_opts* o, mfe_cg_result* results)
+{
+  if (nrhs < 1 || nrhs > kMaxRhs || (32 % nrhs) != 0)
+    return fail(ctx, MFE_BAD_ARG, "nrhs must divide 32 (1, 2, 4, 8, 16 or 32)");
+  if (o->precision != MFE_PREC_MIXED && o->precision != MFE_PREC_F64)
+    return fail(ctx, MFE_BAD_ARG, "unknown precision");
+  if (A64_in->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "A must be FP64");
+  mfe_csr A64 = *A64_in;
+  if (!csr_is_box(&A64)) {
+    int bx, by, bz;
+    MFE_TRY(detect_box(ctx, &A64, &bx, &by, &bz));
+    A64.box_nx = bx;
+    A64.box_ny = by;
+    A64.box_nz = bz;
+  }
+  if (!csr_is_box(&A64))
+    return fail(ctx, MFE_NOT_SUPPORTED, "multi-RHS CG needs a box-structured matrix");
+  if (((uintptr_t)A64.vals & 15u) || ((uintptr_t)X & 15u) || ((uintptr_t)B & 15u))
+    return fail(ctx, MFE_BAD_ARG, "matrix values, B and X must be 16-byte aligned");
+  const bool mixed = o->precision == MFE_PREC_MIXED;
+  const int64_t ntot = A64.nrows * nrhs;
+
+  mfe_csr A32 = A64;
+  if (mixed) {
+    float* v32 = static_cast<float*>(
+        workspace(ctx, "mixed.vals32", sizeof(float) * (size_t)(A64.nnz + 4)));
+    if (!v32) return fail(ctx, MFE_OOM, "FP32 matrix copy allocation failed");
+    if (ctx->f32_src_vals != A64.vals || ctx->f32_src_nnz != A64.nnz) {
+      MFE_TRY(launch_convert_f32(ctx, static_cast<const double*>(A64.vals), v32, A64.nnz));
+      ctx->f32_src_vals = A64.vals;
+      ctx->f32_src_nnz = A64.nnz;
+    }
+    A32.vals = v32;
+    A32.dtype = MFE_F32;
+  }
+  const size_t vb = (mixed ? sizeof(float) : sizeof(double)) * (size_t)(ntot + 8);
+  void* r = workspace(ctx, "multi.r", vb);
+  void* p = workspace(ctx, "multi.p", vb);
+  void* Ap = workspace(ctx, "multi.Ap", vb);
+  float* x32 = mixed ? static_cast<float*>(workspace(ctx, "multi.x32", vb)) : nullptr;
+  MultiState* dst = static_cast<MultiState*>(workspace(ctx, "multi.state", sizeof(MultiState)));
+  double* partials =
+      static_cast<double*>(workspace(ctx, "multi.partials", sizeof(double) * 2 * kMaxPartM * 32));
+  const bool fresh = ctx->ws.find("multi.tickets") == ctx->ws.end();
+  unsigned* tickets = static_cast<unsigned*>(workspace(ctx, "multi.tickets", sizeof(unsigned) * 4));
+  unsigned* err = static_cast<unsigned*>(workspace(ctx, "multi.err", sizeof(unsigned)));
+  if (!r || !p || !Ap || (mixed && !x32) || !dst || !partials || !tickets || !err)
+    return fail(ctx, MFE_OOM, "multi-RHS workspace allocation failed");
+  if (fresh) MFE_CUDA_TRY(ctx, cudaMemsetAsync(tickets, 0, sizeof(unsigned) * 4, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream));
+
+  MultiState* hs = static_cast<MultiState*>(host_scratch(ctx, sizeof(MultiState) + 64));
+  if (!hs) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
+  memset(hs, 0, sizeof(MultiState));
+  hs->nrhs = nrhs;
+  hs->max_iter = std::max(0, o->max_iter);
+  hs->refine_k = o->refine_k > 0 ? o->refine_k : 50;
+  hs->delta2 = 1e-2;
+  hs->first = 1;
+  hs->tol_mode = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;
+  for (int j = 0; j < nrhs; ++j) hs->tol_abs[j] = o->tol;
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst, hs, sizeof(MultiState), cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(p, 0, vb, ctx->stream));
+  if (mixed) {
+    MFE_CUDA_TRY(ctx, cudaMemsetAsync(x32, 0, vb, ctx->stream));
+    MFE_TRY((launch_spmm_t<double, MM_RESID, float>(ctx, &A64, nrhs, X, nullptr, B,
+                                                     static_cast<float*>(r), partials, tickets,
+                                                     dst->rr_true, nullptr, err)));
+  } else {
+    MFE_TRY((launch_spmm_t<double, MM_RESID, double>(ctx, &A64, nrhs, X, nullptr, B,
+                                                      static_cast<double*>(r), partials, tickets,
+                                                      dst->rr_true, nullptr, err)));
+  }
+  k_mr_init<<<1, 32, 0, ctx->stream>>>(dst);
+  MFE_TRY(check_launch(ctx, "k_mr_init"));
+
+  // kernel attributes and occupancy are set up before the loop is captured
+  if (mixed) {
+    MFE_TRY((spmm_setup<float, MM_DOT, float>(ctx, nrhs, nullptr)));
+  } else {
+    MFE_TRY((spmm_setup<double, MM_DOT, double>(ctx, nrhs, nullptr)));
+  }
+  if (mixed) {
+    MultiBufs<float> W{static_cast<float*>(r), static_cast<float*>(p), static_cast<float*>(Ap),
+                       x32, dst, partials, tickets, err};
+    MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
+      return multi_iter_mixed(ctx, A32, A64, nrhs, B, X, W, h, in_graph);
+    }));
+  } else {
+    MultiBufs<double> W{static_cast<double*>(r), static_cast<double*>(p),
+                        static_cast<double*>(Ap), nullptr, dst, partials, tickets, err};
+    MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
+      return multi_iter_f64(ctx, A64, nrhs, X, W, h, in_graph);
+    }));
+  }
+  unsigned* herr = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned char*>(hs) + sizeof(MultiState));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, dst, sizeof(MultiState), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  if (*herr) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during multi-RHS CG");
+  mfe_status worst = MFE_OK;
+  for (int j = 0; j < nrhs; ++j) {
+    mfe_cg_result& res = results[j];
+    memset(&res, 0, sizeof(res));
+    res.num_iters = hs->done[j] ? hs->iters[j] : hs->k;
+    res.normr = hs->normr_true[j];
+    res.normr0 = hs->normr0[j];
+    res.final_resid = hs->normr_true[j];
+    res.times[4] = ms * 1e-3;
+    res.refinements = hs->updates;
+    res.fp64_spmvs = mixed ? hs->updates + 1 : hs->k + 1;
+    const bool converged = mixed ? hs->done[j] != 0 : !(hs->normr_true[j] > hs->tol_abs[j]);
+    res.status = hs->status ? MFE_BREAKDOWN : (converged ? MFE_OK : MFE_MAXITER);
+    if (res.status != MFE_OK && worst == MFE_OK) worst = (mfe_status)res.status;
+  }
+  return worst;
+}
+
+}  // namespace mfe
