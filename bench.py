@@ -414,7 +414,8 @@ def run_gpu(args):
 def run_probe(args):
     """Small fixed workloads for profiler captures (ncu): 'spmv' = the box
     system at --dims^3, three FP64 and three FP32 matvecs; 'cg' = the system
-    and a 4-iteration CG solve."""
+    and a 4-iteration CG solve; 'multi' = the system and a 6-iteration
+    mixed-precision solve of 32 right-hand sides (reliable update every 3)."""
     import torch
     import minife_gb300 as M
     torch.cuda.set_device(0)
@@ -430,6 +431,12 @@ def run_probe(args):
         y32 = torch.empty_like(x32)
         for _ in range(3):
             M.matvec(A32, x32, y32)
+    elif args.probe == "multi":
+        g = torch.Generator(device="cpu").manual_seed(0)
+        B = torch.randn(A.nrows, 32, generator=g, dtype=torch.float64).cuda().contiguous()
+        X = torch.zeros_like(B)
+        M.cg_solve_multi(A, B, X, max_iter=6, tol=TOL, tol_mode="relative", precision="mixed",
+                         refine_k=3)
     else:
         x = torch.zeros_like(b)
         M.cg_solve(A, b, x, max_iter=4, tol=TOL, tol_mode="relative")
@@ -440,7 +447,7 @@ def run_probe(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["spmv", "cg"], default=None,
+    ap.add_argument("--probe", choices=["spmv", "cg", "multi"], default=None,
                     help="run a small fixed workload for a profiler capture and exit")
     ap.add_argument("--dims", type=int, default=128)
     ap.add_argument("--gpus", type=int, default=1)

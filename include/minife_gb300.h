@@ -81,6 +81,9 @@ mfe_status mfe_ctx_destroy(mfe_ctx* ctx);
 mfe_status mfe_set_stream(mfe_ctx* ctx, void* stream);
 /* Return to the context's own (non-blocking) stream. */
 mfe_status mfe_use_own_stream(mfe_ctx* ctx);
+/* Wait for the context's stream.  Returns MFE_TIMEOUT (and clears the
+ * condition) when a standalone SpMV/SpMM launched since the last call gave
+ * up one of its bounded waits; solver calls report this themselves. */
 mfe_status mfe_synchronize(mfe_ctx* ctx);
 const char* mfe_last_error_string(const mfe_ctx* ctx);
 const char* mfe_status_string(mfe_status s);
@@ -286,7 +289,10 @@ mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const doub
 mfe_status mfe_box_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v);
 
 /* Multi-RHS: Y = A X for nrhs column vectors stored row-major (X[i*nrhs + j]),
- * reading A once per product.  FP64 or FP32 by A->dtype (X, Y same type). */
+ * reading A once per product.  FP64 or FP32 by A->dtype (X, Y same type).
+ * Box matrices with nrhs dividing 32 and 16-byte aligned arrays take the
+ * staged box kernel (one warp per row, one lane per column); others a
+ * thread-per-(row, column) CSR kernel. */
 mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X, void* Y);
 
 /* Multi-RHS CG on one matrix: nrhs independent CG solves (each with its own

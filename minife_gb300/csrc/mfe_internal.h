@@ -97,6 +97,10 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x
                     const mfe_cg_opts* opts, mfe_cg_result* res);
 
 // ---- multi-RHS CG (mfe_multi.cu) ----
+// True when Y = A X can take the box-structured SpMM (box matrix, nrhs
+// dividing 32, 16-byte aligned values and vectors).
+bool spmm_box_eligible(const mfe_csr* A, int nrhs, const void* X, const void* Y);
+mfe_status launch_spmm_box(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y);
 mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64, int nrhs, const double* B, double* X,
                     const mfe_cg_opts* opts, mfe_cg_result* results);
 

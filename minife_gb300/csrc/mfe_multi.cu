@@ -49,7 +49,7 @@ struct MultiState {
   double delta2;
 };
 
-enum MMode { MM_DOT = 1, MM_RESID = 2 };
+enum MMode { MM_PLAIN = 0, MM_DOT = 1, MM_RESID = 2 };
 
 template <typename T, typename RT>
 struct SpmmParams {
@@ -261,12 +261,12 @@ __global__ void __launch_bounds__(kTileRowsM * 32 + 32, 2) k_spmm_box(SpmmParams
           dacc = fma(res, res, dacc);
         } else {
           P.y[idx] = sum;
-          dacc = fma(widen(sum), widen(xr), dacc);
+          if (MODE == MM_DOT) dacc = fma(widen(sum), widen(xr), dacc);
         }
       }
     }
   }
-  multi_dot_reduce(warp == 0 ? 0.0 : dacc, red, P.partials, P.ticket, P.out, nr);
+  if (MODE != MM_PLAIN) multi_dot_reduce(warp == 0 ? 0.0 : dacc, red, P.partials, P.ticket, P.out, nr);
 }
 
 // lanes j, j+nrhs, j+2nrhs, ... of a warp hold right-hand side j: sum them
@@ -451,25 +451,32 @@ size_t spmm_smem(int nrhs)
   return (size_t)kStagesM * ((size_t)spmm_capv() + 9 * (size_t)spmm_capx(nrhs)) * sizeof(T);
 }
 
-// Sets the dynamic shared memory limit of one instantiation for nrhs and
-// returns its resident CTAs per SM; cached per (device, nrhs) so launches
-// recorded into a graph make no further runtime calls.
+// Raises the dynamic shared memory limit of one instantiation to what nrhs
+// needs (the limit is per kernel, so it only grows) and returns its resident
+// CTAs per SM for nrhs; cached per (device, nrhs) so launches recorded into a
+// graph make no further runtime calls.
 template <typename T, int MODE, typename RT>
 mfe_status spmm_setup(mfe_ctx* ctx, int nrhs, int* per_sm)
 {
-  static std::map<std::pair<int, int>, int> cache;
+  static std::map<std::pair<int, int>, int> occ;
+  static std::map<int, size_t> limit;
   static std::mutex mu;
   std::lock_guard<std::mutex> lock(mu);
   const auto key = std::make_pair(ctx->device, nrhs);
-  auto it = cache.find(key);
-  if (it == cache.end()) {
+  auto it = occ.find(key);
+  if (it == occ.end()) {
     const size_t smem = spmm_smem<T>(nrhs);
-    MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_box<T, MODE, RT>,
-                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    size_t& lim = limit[ctx->device];
+    if (smem > lim) {
+      MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_box<T, MODE, RT>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem));
+      lim = smem;
+    }
     int n = 1;
     MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
                           &n, k_spmm_box<T, MODE, RT>, kTileRowsM * 32 + 32, smem));
-    it = cache.emplace(key, std::max(n, 1)).first;
+    it = occ.emplace(key, std::max(n, 1)).first;
   }
   if (per_sm) *per_sm = it->second;
   return MFE_OK;
@@ -632,6 +639,25 @@ mfe_status run_loop(mfe_ctx* ctx, MultiState* dev_st, MultiState* host_st, Body 
 }
 
 }  // namespace
+
+bool spmm_box_eligible(const mfe_csr* A, int nrhs, const void* X, const void* Y)
+{
+  return csr_is_box(A) && nrhs >= 1 && nrhs <= kMaxRhs && (32 % nrhs) == 0 &&
+         !((uintptr_t)A->vals & 15u) && !((uintptr_t)X & 15u) && !((uintptr_t)Y & 15u);
+}
+
+mfe_status launch_spmm_box(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y)
+{
+  unsigned* err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
+  if (!err) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  if (A->dtype == MFE_F64)
+    return launch_spmm_t<double, MM_PLAIN, double>(ctx, A, nrhs, static_cast<const double*>(X),
+                                                   static_cast<double*>(Y), nullptr, nullptr,
+                                                   nullptr, nullptr, nullptr, nullptr, err);
+  return launch_spmm_t<float, MM_PLAIN, float>(ctx, A, nrhs, static_cast<const float*>(X),
+                                               static_cast<float*>(Y), nullptr, nullptr, nullptr,
+                                               nullptr, nullptr, nullptr, err);
+}
 
 mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double* B, double* X,
                     const mfe_cg_opts* o, mfe_cg_result* results)

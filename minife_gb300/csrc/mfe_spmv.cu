@@ -520,6 +520,9 @@ mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
 
 mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y)
 {
+  if (A->nrows == 0) return MFE_OK;
+  if (spmm_box_eligible(A, nrhs, X, Y) && getenv("MFE_SPMV_GENERIC") == nullptr)
+    return launch_spmm_box(ctx, A, nrhs, X, Y);
   const int64_t total = A->nrows * (int64_t)nrhs;
   const int64_t blocks = std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, 256),
                                                                 (int64_t)ctx->sm_count * 16));

@@ -139,3 +139,36 @@ def test_multi_rejects_non_box_matrix():
     with pytest.raises(M.MiniFEError) as ei:
         M.cg_solve_multi(A2, B, torch.zeros_like(B), precision="f64")
     assert ei.value.status == 7  # MFE_NOT_SUPPORTED
+
+
+@pytest.mark.parametrize("dims,nrhs", [((10, 10, 10), 32), ((17, 3, 5), 8), ((7, 9, 4), 1),
+                                       ((12, 11, 10), 3)])
+def test_spmm_matches_oracle_per_column(dims, nrhs):
+    """Y = A X column by column against the oracle's matvec: the box kernel
+    (nrhs dividing 32) and the CSR kernel (nrhs = 3) within the FMA
+    reordering bound of a 27-term row sum."""
+    A, b = M.build_system(*dims)
+    ro, cols, vals, _ = O.build_system(*dims)
+    rng = np.random.default_rng(nrhs)
+    X = rng.standard_normal((A.nrows, nrhs))
+    Y = torch.empty(A.nrows, nrhs, dtype=torch.float64, device=b.device)
+    M.spmm(A, torch.from_numpy(X).to(b.device), Y)
+    M.default_context().synchronize()
+    Yh = host(Y)
+    for j in range(nrhs):
+        yo = O.matvec(ro, cols, vals, X[:, j])
+        bound = 30 * 2.0 ** -53 * O.matvec(ro, cols, np.abs(vals), np.abs(X[:, j])) + 1e-300
+        assert np.all(np.abs(Yh[:, j] - yo) <= bound), j
+
+
+def test_spmm_fp32_box_and_generic_agree():
+    dims = (14, 9, 11)
+    A, b = M.build_system(*dims)
+    A32 = M.to_f32(A)
+    X = torch.randn(A.nrows, 16, dtype=torch.float32, device=b.device)
+    Y = torch.empty_like(X)
+    M.spmm(A32, X, Y)
+    Yref = torch.empty(A.nrows, 16, dtype=torch.float64, device=b.device)
+    M.spmm(A, X.double().contiguous(), Yref)
+    err = (Y.double() - Yref).abs().max().item()
+    assert err <= 1e-5 * Yref.abs().max().item()
