@@ -106,6 +106,15 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned by
                : "memory");
 }
 
+// Adds bytes to the current phase's expected transaction count without
+// arriving (each lane of a producer warp announces its own copy).
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes)
+{
+  asm volatile("mbarrier.expect_tx.relaxed.cta.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
 // Plain arrival (count 1), release semantics: prior shared-memory reads by
 // this thread are ordered before the phase can complete.
 __device__ __forceinline__ void mbar_arrive(uint64_t* bar)
@@ -186,6 +195,30 @@ __device__ __forceinline__ double f2d_exact(float f)
 
 __device__ __forceinline__ double widen(double v) { return v; }
 __device__ __forceinline__ double widen(float v) { return f2d_exact(v); }
+
+// ---------------------------------------------------------------------------
+// Double-float accumulator for sums of FP32 products, FP32 operations only
+// (FP64 arithmetic on GB300 runs at 1/60 of the FP32 rate).  Each product is
+// split exactly into p + pe with an FMA (Dekker's TwoProduct), p is added to
+// hi with Knuth's TwoSum, and both rounding errors go to lo, so hi + lo holds
+// the sum to about 48 significant bits.  The __f*_rn intrinsics keep the
+// compiler from contracting the steps into FMAs, which would lose the error
+// terms.
+// ---------------------------------------------------------------------------
+struct DFAcc {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add_product(float a, float b)
+  {
+    const float p = __fmul_rn(a, b);
+    const float pe = __fmaf_rn(a, b, -p);
+    const float t = __fadd_rn(hi, p);
+    const float bp = __fsub_rn(t, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    hi = t;
+    lo = __fadd_rn(lo, __fadd_rn(err, pe));
+  }
+  __device__ __forceinline__ double value() const { return f2d_exact(hi) + f2d_exact(lo); }
+};
 
 // ---------------------------------------------------------------------------
 // misc

@@ -10,12 +10,12 @@
 // the warp, and lane j reads x[col*nrhs + j], so shared-memory reads are
 // conflict-free.  Each lane accumulates its right-hand side's dot in FP64.
 //
-// The solver is the mixed-precision one of mfe_mixed.cu applied per
-// right-hand side: FP32 matrix copy, FP32 vectors, FP64 dots and scalars
-// (alpha_j, beta_j), FP64 solution; reliable updates (x += x32, R = B - A X in
-// FP64) happen for all right-hand sides together every refine_k iterations or
-// when any unconverged right-hand side's recursive residual drops tenfold or
-// claims convergence.  A converged right-hand side is frozen (alpha_j = 0).
+// The mixed solver is the one of mfe_mixed.cu applied per right-hand side:
+// FP32 matrix copy, FP32 vectors, FP64 dots and scalars (alpha_j, beta_j),
+// FP64 solution; reliable updates (x += x32, R = B - A X in FP64) happen for
+// all right-hand sides together (see k_mr_decide).  The FP64 solver runs the
+// reference's CG per right-hand side.  A finished right-hand side is frozen
+// (alpha_j = 0).
 // nrhs must divide 32 (1, 2, 4, 8, 16, 32).
 #include <algorithm>
 #include <cmath>
@@ -34,9 +34,25 @@ namespace mfe {
 
 constexpr int kMaxRhs = 32;
 constexpr int kTileRowsM = 16;  // rows per tile = consumer warps per CTA
-constexpr int kStagesM = 2;
+constexpr int kProdM = 2;       // producer warps per CTA (tiles alternate between them)
+constexpr int kThreadsM = (kTileRowsM + kProdM) * 32;
 constexpr int kVT = 256;
 constexpr int kMaxPartM = 2048;
+
+// stage capacities (elements): a tile's values, and one x segment of
+// kTileRowsM + 2 rows of nrhs values, each with room for rounding both ends
+// to the 16-byte bulk-copy granule
+__host__ __device__ constexpr int spmm_capv() { return ((kTileRowsM * 27 + 8) + 3) & ~3; }
+__host__ __device__ constexpr int spmm_capx(int nrhs)
+{
+  return (((kTileRowsM + 2) * nrhs + 8) + 3) & ~3;
+}
+// pipeline depth: a FP32 stage of 32 right-hand sides is 22.8 KB, a FP64 one 45.5 KB
+template <typename T>
+__host__ __device__ constexpr int spmm_stages()
+{
+  return sizeof(T) == 4 ? 4 : 2;
+}
 
 struct MultiState {
   double rr[kMaxRhs], rr_new[kMaxRhs], pAp[kMaxRhs], beta[kMaxRhs];
@@ -96,22 +112,31 @@ __device__ void multi_dot_reduce(double v, double* red, double* partials, unsign
   if (threadIdx.x == 0) *ticket = 0u;
 }
 
-template <typename T, int MODE, typename RT>
-__global__ void __launch_bounds__(kTileRowsM * 32 + 32, 2) k_spmm_box(SpmmParams<T, RT> P)
+// NRC: nrhs as a compile-time constant (32), or 0 to read it from P
+template <typename T, int MODE, typename RT, int NRC>
+__global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<T, RT> P)
 {
-  constexpr int R = kTileRowsM, S = kStagesM;
+  constexpr int R = kTileRowsM, S = spmm_stages<T>();
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t full[S], empty[S];
-  __shared__ int64_t s_vbase[S];
+  __shared__ uint32_t s_vbase[S];  // first staged value (low 32 bits of its index)
   __shared__ int64_t s_xbase[S][9];
-  __shared__ int s_ok[S];
-  __shared__ double red[(R + 1) * 32];
+  __shared__ int s_ok[S];    // stage holds the tile (capacities sufficed)
+  __shared__ int s_fast[S];  // every x segment starts at its unclamped row
+  // per row of the staged tile: low 32 bits of its CSR offset, and which of
+  // its -x,+x,-y,+y,-z,+z neighbours exist (bits 0-5)
+  __shared__ uint32_t s_rro[S][R];
+  __shared__ int s_rflags[S][R];
+  __shared__ double red[(R + kProdM) * 32];
+  static_assert(S % kProdM == 0, "each producer warp owns whole stages");
   constexpr int VA = 16 / sizeof(T);
-  const size_t stage_elems = (size_t)P.capv + 9 * (size_t)P.capx;
+  const int nr = NRC ? NRC : P.nrhs;
+  const int capx = NRC ? spmm_capx(NRC) : P.capx;
+  constexpr int capv = spmm_capv();
+  const int stage_elems = capv + 9 * capx;
   T* const st0 = reinterpret_cast<T*>(smem);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = (P.n + R - 1) / R;
-  const int nr = P.nrhs;
   if (P.gate != nullptr && *P.gate == 0) return;
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
@@ -121,101 +146,173 @@ __global__ void __launch_bounds__(kTileRowsM * 32 + 32, 2) k_spmm_box(SpmmParams
     fence_mbar_init();
   }
   __syncthreads();
-  double dacc = 0.0;
-  if (warp == 0) {
-    if (lane == 0) {
-      bool ok = true;
-      unsigned issued[S] = {};
-      int it = 0;
-      for (int tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x, ++it) {
-        const int s = it % S;
-        if (it >= S) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / S) - 1) & 1));
-        if (!ok) break;
-        T* sv = st0 + (size_t)s * stage_elems;
-        T* sx = sv + P.capv;
-        const int r0 = tile * R, r1 = min(P.n, r0 + R);
-        const int64_t a = row_offset_of32(r0, P.Nx, P.Ny, P.Nz, P.NxNy);
-        const int64_t e = row_offset_of32(r1, P.Nx, P.Ny, P.Nz, P.NxNy);
-        const int64_t av = a & ~(int64_t)(VA - 1);
-        int64_t bv = min((e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
-        if (bv < av) bv = av;
-        bool fits = max(bv, e) - av <= P.capv;
-        const int64_t ntot = (int64_t)P.n * nr;
-        int64_t xlo[9], xbl[9], xhi[9];
-#pragma unroll
-        for (int j = 0; j < 9; ++j) {
-          const int off = (j / 3 - 1) * P.NxNy + (j % 3 - 1) * P.Nx;
-          const int lo = min(max(r0 + off - 1, 0), P.n);
-          int hi = min(r1 + off + 1, P.n);
-          if (hi < lo) hi = lo;
-          const int64_t elo = (int64_t)lo * nr, ehi = (int64_t)hi * nr;
-          const int64_t lal = elo & ~(int64_t)(VA - 1);
-          int64_t bl = min((ehi + VA - 1) & ~(int64_t)(VA - 1), ntot & ~(int64_t)(VA - 1));
-          if (bl < lal) bl = lal;
-          xlo[j] = lal;
-          xbl[j] = bl;
-          xhi[j] = ehi;
-          fits = fits && (max(bl, ehi) - lal <= P.capx);
-        }
-        ++issued[s];
-        if (!fits) {
-          // cannot happen for the stage capacities the host computes
+  double dacc = 0.0;  // FP64 products (RESID; DOT of FP64 operands)
+  DFAcc facc;         // FP32 products (DOT of FP32 operands)
+  if (warp < kProdM) {
+    // producer warps: warp p stages the CTA's tiles it = p, p + kProdM, ...
+    // (stages s = it % S).  Lanes 0-8 compute the nine x segments (lane j:
+    // rows r0 + off_j - 1 .. r1 + off_j of offset j = (dz, dy)), lane 9 the
+    // values range, lanes 16-31 the rows' CSR offsets and neighbour flags
+    // (coordinates advanced incrementally, no division per tile); every lane
+    // announces and issues its own copy, lane 0 arrives.
+    const int p = warp;
+    bool ok = true;
+    const int64_t ntot = (int64_t)P.n * nr;
+    const int rl = lane - 16;
+    int ix = 0, iy = 0, iz = 0, sxs = 0, sys = 0, szs = 0;
+    if (lane >= 16) {
+      const int64_t stride = (int64_t)kProdM * gridDim.x * R;
+      szs = (int)(stride / P.NxNy);
+      const int rs = (int)(stride - (int64_t)szs * P.NxNy);
+      sys = rs / P.Nx;
+      sxs = rs - sys * P.Nx;
+      const int64_t rfirst = ((int64_t)blockIdx.x + (int64_t)p * gridDim.x) * R + rl;
+      iz = (int)(rfirst / P.NxNy);
+      const int rem = (int)(rfirst - (int64_t)iz * P.NxNy);
+      iy = rem / P.Nx;
+      ix = rem - iy * P.Nx;
+    }
+    int it = p;
+    for (int tile = blockIdx.x + p * gridDim.x; tile < ntiles; tile += kProdM * gridDim.x, it += kProdM) {
+      const int s = it % S;
+      if (it >= S) {
+        if (lane == 0) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / S) - 1) & 1));
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+      }
+      if (!ok) break;
+      T* sv = st0 + (size_t)s * stage_elems;
+      const int r0 = tile * R, r1 = min(P.n, r0 + R);
+      int64_t ro = 0;
+      int cnt = 0, flags = 0;
+      if (lane >= 16) {
+        ro = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
+        cnt = nbr(ix, P.Nx) * nbr(iy, P.Ny) * nbr(iz, P.Nz);
+        flags = (ix > 0) | (ix < P.Nx - 1) << 1 | (iy > 0) << 2 | (iy < P.Ny - 1) << 3 |
+                (iz > 0) << 4 | (iz < P.Nz - 1) << 5;
+      }
+      const int64_t a = __shfl_sync(0xffffffffu, ro, 16);
+      const int64_t e = __shfl_sync(0xffffffffu, ro + cnt, 16 + (r1 - r0 - 1));
+      // this lane's piece: elements [lo_e, bl_e) by bulk copy, [bl_e, hi_e)
+      // (the unaligned end of the array) by plain loads
+      int64_t lo_e = 0, bl_e = 0, hi_e = 0;
+      const T* src = P.x;
+      T* dst = sv;
+      bool fits = true, fast = true;
+      if (lane < 9) {
+        const int off = (lane / 3 - 1) * P.NxNy + (lane % 3 - 1) * P.Nx;
+        const int lo = min(max(r0 + off - 1, 0), P.n);
+        int hi = min(r1 + off + 1, P.n);
+        if (hi < lo) hi = lo;
+        const int64_t elo = (int64_t)lo * nr;
+        hi_e = (int64_t)hi * nr;
+        lo_e = elo & ~(int64_t)(VA - 1);
+        bl_e = min((hi_e + VA - 1) & ~(int64_t)(VA - 1), ntot & ~(int64_t)(VA - 1));
+        if (bl_e < lo_e) bl_e = lo_e;
+        fits = max(bl_e, hi_e) - lo_e <= capx;
+        fast = lo == r0 + off - 1 && lo_e == elo;
+        dst = sv + capv + lane * capx;
+      } else if (lane == 9) {
+        hi_e = e;
+        lo_e = a & ~(int64_t)(VA - 1);
+        bl_e = min((hi_e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
+        if (bl_e < lo_e) bl_e = lo_e;
+        fits = max(bl_e, hi_e) - lo_e <= capv;
+        src = P.vals;
+      }
+      fits = __all_sync(0xffffffffu, fits);
+      fast = __all_sync(0xffffffffu, fast);
+      if (lane >= 16) {
+        s_rro[s][rl] = (uint32_t)ro;
+        s_rflags[s][rl] = r0 + rl < r1 ? flags : 0;
+        ix += sxs;
+        const int cx = ix >= P.Nx;
+        ix -= cx ? P.Nx : 0;
+        iy += sys + cx;
+        const int cy = iy >= P.Ny;
+        iy -= cy ? P.Ny : 0;
+        iz += szs + cy;
+      }
+      if (!fits) {
+        // cannot happen for the stage capacities the host computes
+        if (lane == 0) {
           atomicOr(P.err, ERR_TILE_OVERFLOW);
           s_ok[s] = 0;
-          mbar_arrive_expect_tx(&full[s], 0);
-          continue;
         }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&full[s]);
+        continue;
+      }
+      if (lane < 9) s_xbase[s][lane] = lo_e;
+      if (lane == 9) s_vbase[s] = (uint32_t)lo_e;
+      if (lane == 0) {
         s_ok[s] = 1;
-        s_vbase[s] = av;
-        unsigned bytes = (unsigned)((bv - av) * sizeof(T));
-        for (int64_t k = bv; k < e; ++k) sv[k - av] = P.vals[k];
-        for (int j = 0; j < 9; ++j) {
-          s_xbase[s][j] = xlo[j];
-          T* dx = sx + (size_t)j * P.capx;
-          for (int64_t k = xbl[j]; k < xhi[j]; ++k) dx[k - xlo[j]] = P.x[k];
-          bytes += (unsigned)((xbl[j] - xlo[j]) * sizeof(T));
-        }
+        s_fast[s] = fast;
+      }
+      if (hi_e > bl_e) {
+        for (int64_t k = bl_e; k < hi_e; ++k) dst[k - lo_e] = src[k];
         fence_proxy_async_smem();
-        mbar_arrive_expect_tx(&full[s], bytes);
-        if (bv > av) bulk_g2s(sv, P.vals + av, (unsigned)((bv - av) * sizeof(T)), &full[s]);
-        for (int j = 0; j < 9; ++j)
-          if (xbl[j] > xlo[j])
-            bulk_g2s(sx + (size_t)j * P.capx, P.x + xlo[j],
-                     (unsigned)((xbl[j] - xlo[j]) * sizeof(T)), &full[s]);
       }
-      if (!ok) {
-        atomicOr(P.err, ERR_WAIT_TIMEOUT);
-        for (int s = 0; s < S; ++s)
-          if (issued[s]) mbar_wait_bounded(&full[s], (issued[s] - 1) & 1u);
+      const unsigned bytes = (unsigned)((bl_e - lo_e) * sizeof(T));
+      if (bytes) {
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(dst, src + lo_e, bytes, &full[s]);
       }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&full[s]);
+    }
+    if (!ok && lane == 0) {
+      // wait (bounded) for the copies this warp issued: its tiles before
+      // `it`, stage st (st = p mod kProdM) holding ceil((it - st) / S) of them
+      atomicOr(P.err, ERR_WAIT_TIMEOUT);
+      for (int st = p; st < S && st < it; st += kProdM)
+        mbar_wait_bounded(&full[st], (unsigned)(((it - st + S - 1) / S - 1) & 1));
     }
   } else {
-    const int lr = warp - 1;
+    const int lr = warp - kProdM;
     const bool lane_on = lane < nr;
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
       const int s = it % S;
       const int r = tile * R + lr;
       const bool active = r < P.n;  // warp-uniform
-      const int rr = active ? r : P.n - 1;
-      const int iz = rr / P.NxNy, rem = rr - iz * P.NxNy, iy = rem / P.Nx, ix = rem - iy * P.Nx;
-      const int64_t roff = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
       if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
         atomicOr(P.err, ERR_WAIT_TIMEOUT);
         break;
       }
       T sum = T(0);
       T xr = T(0);
+      const int flags = s_rflags[s][lr];
       const bool ok = active && s_ok[s] != 0;
-      if (ok) {
-        const T* sv = st0 + (size_t)s * stage_elems;
-        const T* sx = sv + P.capv;
-        const T* rowv = sv + (roff - s_vbase[s]);
-        const bool vxm = ix > 0, vxp = ix < P.Nx - 1, vym = iy > 0, vyp = iy < P.Ny - 1;
-        const bool vzm = iz > 0, vzp = iz < P.Nz - 1;
+      const bool interior = flags == 63;
+      const int lj = lane_on ? lane : 0;
+      const T* sv = st0 + (size_t)s * stage_elems;
+      const T* sx = sv + capv;
+      const T* rowv = sv + (s_rro[s][lr] - s_vbase[s]);
+      if (ok && interior && s_fast[s]) {
+        // every segment of this stage starts at row r0 + off_j - 1, so row r's
+        // x values sit at the same place in all nine: fixed offsets, 27 terms
+        const T* xb = sx + (lr + 1) * nr + lj;
+        xr = xb[4 * capx];
+        T s0 = T(0), s1 = T(0);
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            const int slot = j * 3 + dx + 1;
+            const T v = rowv[slot];
+            const T xv = xb[j * capx + dx * nr];
+            if (slot & 1)
+              s1 = fma(v, xv, s1);
+            else
+              s0 = fma(v, xv, s0);
+          }
+        }
+        sum = s0 + s1;
+      } else if (ok) {
+        const bool vxm = flags & 1, vxp = flags & 2, vym = flags & 4, vyp = flags & 8;
+        const bool vzm = flags & 16, vzp = flags & 32;
         const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp, cxy = cx * cy;
-        const int lj = lane_on ? lane : 0;
-        const T* xc = sx + 4 * (size_t)P.capx + ((int64_t)r * nr + lj - s_xbase[s][4]);
+        const T* xc = sx + 4 * (size_t)capx + ((int64_t)r * nr + lj - s_xbase[s][4]);
         xr = xc[0];
         T s0 = T(0), s1 = T(0);
         int slot = 0;
@@ -229,7 +326,7 @@ __global__ void __launch_bounds__(kTileRowsM * 32 + 32, 2) k_spmm_box(SpmmParams
             const int by = dy < 0 ? 0 : (dy == 0 ? (int)vym : (int)vym + 1);
             const int j = (dz + 1) * 3 + (dy + 1);
             const int off = dz * P.NxNy + dy * P.Nx;
-            const T* seg = sx + (size_t)j * P.capx + ((int64_t)(r + off) * nr + lj - s_xbase[s][j]);
+            const T* seg = sx + (size_t)j * capx + ((int64_t)(r + off) * nr + lj - s_xbase[s][j]);
             const int pbase = bz * cxy + by * cx;
 #pragma unroll
             for (int dx = -1; dx <= 1; ++dx) {
@@ -261,12 +358,18 @@ __global__ void __launch_bounds__(kTileRowsM * 32 + 32, 2) k_spmm_box(SpmmParams
           dacc = fma(res, res, dacc);
         } else {
           P.y[idx] = sum;
-          if (MODE == MM_DOT) dacc = fma(widen(sum), widen(xr), dacc);
+          if (MODE == MM_DOT) {
+            if constexpr (sizeof(T) == 4)
+              facc.add_product(sum, xr);
+            else
+              dacc = fma(sum, xr, dacc);
+          }
         }
       }
     }
   }
-  if (MODE != MM_PLAIN) multi_dot_reduce(warp == 0 ? 0.0 : dacc, red, P.partials, P.ticket, P.out, nr);
+  if (MODE != MM_PLAIN)
+    multi_dot_reduce(warp < kProdM ? 0.0 : dacc + facc.value(), red, P.partials, P.ticket, P.out, nr);
 }
 
 // lanes j, j+nrhs, j+2nrhs, ... of a warp hold right-hand side j: sum them
@@ -300,14 +403,17 @@ __global__ void __launch_bounds__(kVT)
   const int j = threadIdx.x % nrhs;
   const V alpha = st->done[j] ? V(0) : (V)(st->rr[j] / st->pAp[j]);
   double acc = 0.0;
+  DFAcc facc;
   for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT) {
     x[i] = fma(alpha, p[i], x[i]);
     const V rv = fma(-alpha, Ap[i], r[i]);
     r[i] = rv;
-    const double d = widen(rv);
-    acc = fma(d, d, acc);
+    if constexpr (sizeof(V) == 4)
+      facc.add_product(rv, rv);
+    else
+      acc = fma(rv, rv, acc);
   }
-  acc = lane_group_sum(acc, nrhs);
+  acc = lane_group_sum(acc + facc.value(), nrhs);
   if ((threadIdx.x & 31) >= nrhs) acc = 0.0;
   multi_dot_reduce(acc, red, partials, ticket, st->rr_new, nrhs);
 }
@@ -323,27 +429,30 @@ __global__ void __launch_bounds__(kVT)
 }
 
 // Mixed solver, one warp, after the update kernel: decide whether this
-// iteration ends with a reliable update (any open right-hand side whose
-// recursive residual fell tenfold since the last one or claims convergence,
-// refine_k iterations since the last one, or the iteration limit).
+// iteration ends with a reliable update, which all right-hand sides share:
+// when every open one has its recursive residual fallen tenfold since the
+// last update or claims convergence, after refine_k iterations, or at the
+// iteration limit.  (Waiting for the slowest keeps the update count near a
+// single solve's; a right-hand side that claims convergence early keeps
+// iterating on its recursion until the update checks its true residual.)
 __global__ void k_mr_decide(MultiState* st)
 {
   const int j = threadIdx.x;
   const int nr = st->nrhs;
-  bool trig = false, brk = false;
+  bool ready = true, brk = false;
   if (j < nr && !st->done[j]) {
     brk = !(st->pAp[j] > 0.0);
     const double t = st->rr_new[j];
-    trig = t < st->delta2 * st->rr_at_update[j] || t <= st->tol_abs[j] * st->tol_abs[j];
+    ready = t < st->delta2 * st->rr_at_update[j] || t <= st->tol_abs[j] * st->tol_abs[j];
   }
-  const bool any_trig = __any_sync(0xffffffffu, trig);
+  const bool all_ready = __all_sync(0xffffffffu, ready);
   const bool any_brk = __any_sync(0xffffffffu, brk);
   if (j == 0) {
     st->k += 1;
     st->since += 1;
     st->first = 0;
     if (any_brk) st->status = MFE_BREAKDOWN;
-    st->gate = st->status == 0 && (any_trig || st->since >= st->refine_k || st->k >= st->max_iter);
+    st->gate = st->status == 0 && (all_ready || st->since >= st->refine_k || st->k >= st->max_iter);
   }
 }
 
@@ -443,20 +552,18 @@ __global__ void k_mr_begin(const MultiState* st, cudaGraphConditionalHandle h)
 // ---------------------------------------------------------------------------
 namespace {
 
-int spmm_capv() { return ((kTileRowsM * 27 + 8) + 3) & ~3; }
-int spmm_capx(int nrhs) { return (int)((((int64_t)(kTileRowsM + 2) * nrhs + 8) + 3) & ~3); }
 template <typename T>
 size_t spmm_smem(int nrhs)
 {
-  return (size_t)kStagesM * ((size_t)spmm_capv() + 9 * (size_t)spmm_capx(nrhs)) * sizeof(T);
+  return (size_t)spmm_stages<T>() * ((size_t)spmm_capv() + 9 * (size_t)spmm_capx(nrhs)) * sizeof(T);
 }
 
-// Raises the dynamic shared memory limit of one instantiation to what nrhs
-// needs (the limit is per kernel, so it only grows) and returns its resident
-// CTAs per SM for nrhs; cached per (device, nrhs) so launches recorded into a
-// graph make no further runtime calls.
-template <typename T, int MODE, typename RT>
-mfe_status spmm_setup(mfe_ctx* ctx, int nrhs, int* per_sm)
+// Raises the dynamic shared memory limit of one kernel instantiation to what
+// nrhs needs (the limit is per kernel, so it only grows) and returns its
+// resident CTAs per SM for nrhs; cached per (device, nrhs) so launches
+// recorded into a graph make no further runtime calls.
+template <typename T, int MODE, typename RT, int NRC>
+mfe_status spmm_setup_k(mfe_ctx* ctx, int nrhs, int* per_sm)
 {
   static std::map<std::pair<int, int>, int> occ;
   static std::map<int, size_t> limit;
@@ -468,18 +575,25 @@ mfe_status spmm_setup(mfe_ctx* ctx, int nrhs, int* per_sm)
     const size_t smem = spmm_smem<T>(nrhs);
     size_t& lim = limit[ctx->device];
     if (smem > lim) {
-      MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_box<T, MODE, RT>,
+      MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_box<T, MODE, RT, NRC>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem));
       lim = smem;
     }
     int n = 1;
     MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                          &n, k_spmm_box<T, MODE, RT>, kTileRowsM * 32 + 32, smem));
+                          &n, k_spmm_box<T, MODE, RT, NRC>, kThreadsM, smem));
     it = occ.emplace(key, std::max(n, 1)).first;
   }
   if (per_sm) *per_sm = it->second;
   return MFE_OK;
+}
+
+template <typename T, int MODE, typename RT>
+mfe_status spmm_setup(mfe_ctx* ctx, int nrhs, int* per_sm)
+{
+  if (nrhs == 32) return spmm_setup_k<T, MODE, RT, 32>(ctx, nrhs, per_sm);
+  return spmm_setup_k<T, MODE, RT, 0>(ctx, nrhs, per_sm);
 }
 
 template <typename T, int MODE, typename RT>
@@ -508,13 +622,16 @@ mfe_status launch_spmm_t(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const T* X, T
   P.gate = gate;
   P.err = err;
   const size_t smem = spmm_smem<T>(nrhs);
-  const int threads = kTileRowsM * 32 + 32;
+  const int threads = kThreadsM;
   int per_sm = 1;
   MFE_TRY((spmm_setup<T, MODE, RT>(ctx, nrhs, &per_sm)));
   const int64_t ntiles = ceil_div(A->nrows, (int64_t)kTileRowsM);
   const int grid = (int)std::max<int64_t>(
       1, std::min<int64_t>({ntiles, (int64_t)ctx->sm_count * per_sm, (int64_t)kMaxPartM}));
-  k_spmm_box<T, MODE, RT><<<grid, threads, smem, ctx->stream>>>(P);
+  if (nrhs == 32)
+    k_spmm_box<T, MODE, RT, 32><<<grid, threads, smem, ctx->stream>>>(P);
+  else
+    k_spmm_box<T, MODE, RT, 0><<<grid, threads, smem, ctx->stream>>>(P);
   return check_launch(ctx, "k_spmm_box");
 }
 
