@@ -33,9 +33,10 @@
 namespace mfe {
 
 constexpr int kMaxRhs = 32;
-constexpr int kTileRowsM = 16;  // rows per tile = consumer warps per CTA
+constexpr int kTileRowsM = 32;  // rows per tile (two per consumer warp)
+constexpr int kConsM = 16;      // consumer warps per CTA
 constexpr int kProdM = 2;       // producer warps per CTA (tiles alternate between them)
-constexpr int kThreadsM = (kTileRowsM + kProdM) * 32;
+constexpr int kThreadsM = (kConsM + kProdM) * 32;
 constexpr int kVT = 256;
 constexpr int kMaxPartM = 2048;
 
@@ -47,15 +48,28 @@ __host__ __device__ constexpr int spmm_capx(int nrhs)
 {
   return (((kTileRowsM + 2) * nrhs + 8) + 3) & ~3;
 }
-// pipeline depth: a FP32 stage of 32 right-hand sides is 22.8 KB, a FP64 one 45.5 KB
+// pipeline depth (one stage per producer warp): a FP32 stage of 32
+// right-hand sides is 42.6 KB, a FP64 one 85 KB
 template <typename T>
 __host__ __device__ constexpr int spmm_stages()
 {
-  return sizeof(T) == 4 ? 4 : 2;
+  return 2;
 }
+
+template <typename T>
+struct Vec2;
+template <>
+struct Vec2<float> {
+  using type = float2;
+};
+template <>
+struct Vec2<double> {
+  using type = double2;
+};
 
 struct MultiState {
   double rr[kMaxRhs], rr_new[kMaxRhs], pAp[kMaxRhs], beta[kMaxRhs];
+  double alpha[kMaxRhs];  // rr / pAp (0 once finished), set with pAp
   double rr_true[kMaxRhs], rr_at_update[kMaxRhs], normr0[kMaxRhs], tol_abs[kMaxRhs];
   double normr_true[kMaxRhs];
   int done[kMaxRhs];
@@ -82,12 +96,14 @@ struct SpmmParams {
   double* out;                   // [32] totals
   const int* gate;               // nullable
   unsigned* err;
+  MultiState* cg;                // DOT mode in a solve: also set cg->alpha from out
 };
 
 // Per-lane dots of the block summed over its warps, then over blocks in
 // block order by the last block: out[j] = total of lane j.  red: >= 33*32.
+// With cg set (out = cg->pAp) the last block also forms cg->alpha.
 __device__ void multi_dot_reduce(double v, double* red, double* partials, unsigned* ticket,
-                                 double* out, int nlanes)
+                                 double* out, int nlanes, MultiState* cg = nullptr)
 {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   red[warp * 32 + lane] = v;
@@ -108,6 +124,7 @@ __device__ void multi_dot_reduce(double v, double* red, double* partials, unsign
     double s = 0.0;
     for (unsigned bl = 0; bl < gridDim.x; ++bl) s += __ldcg(&partials[(size_t)bl * 32 + threadIdx.x]);
     out[threadIdx.x] = s;
+    if (cg) cg->alpha[threadIdx.x] = cg->done[threadIdx.x] ? 0.0 : cg->rr[threadIdx.x] / s;
   }
   if (threadIdx.x == 0) *ticket = 0u;
 }
@@ -127,7 +144,7 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
   // its -x,+x,-y,+y,-z,+z neighbours exist (bits 0-5)
   __shared__ uint32_t s_rro[S][R];
   __shared__ int s_rflags[S][R];
-  __shared__ double red[(R + kProdM) * 32];
+  __shared__ double red[(kConsM + kProdM) * 32];
   static_assert(S % kProdM == 0, "each producer warp owns whole stages");
   constexpr int VA = 16 / sizeof(T);
   const int nr = NRC ? NRC : P.nrhs;
@@ -141,7 +158,7 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
-      mbar_init(&empty[s], R);
+      mbar_init(&empty[s], kConsM);
     }
     fence_mbar_init();
   }
@@ -150,17 +167,19 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
   DFAcc facc;         // FP32 products (DOT of FP32 operands)
   if (warp < kProdM) {
     // producer warps: warp p stages the CTA's tiles it = p, p + kProdM, ...
-    // (stages s = it % S).  Lanes 0-8 compute the nine x segments (lane j:
-    // rows r0 + off_j - 1 .. r1 + off_j of offset j = (dz, dy)), lane 9 the
-    // values range, lanes 16-31 the rows' CSR offsets and neighbour flags
-    // (coordinates advanced incrementally, no division per tile); every lane
-    // announces and issues its own copy, lane 0 arrives.
+    // (stages s = it % S).  Lane l follows row r0 + l of each tile (CSR
+    // offset and neighbour flags, coordinates advanced incrementally: no
+    // division per tile); lanes 0-8 also compute the nine x segments (lane
+    // j: rows r0 + off_j - 1 .. r1 + off_j of offset j = (dz, dy)) and lane
+    // 9 the values range; every lane announces and issues its own copy, lane
+    // 0 arrives.
     const int p = warp;
     bool ok = true;
     const int64_t ntot = (int64_t)P.n * nr;
-    const int rl = lane - 16;
+    static_assert(R == 32, "one producer lane per tile row");
+    const int rl = lane;
     int ix = 0, iy = 0, iz = 0, sxs = 0, sys = 0, szs = 0;
-    if (lane >= 16) {
+    {
       const int64_t stride = (int64_t)kProdM * gridDim.x * R;
       szs = (int)(stride / P.NxNy);
       const int rs = (int)(stride - (int64_t)szs * P.NxNy);
@@ -182,16 +201,12 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
       if (!ok) break;
       T* sv = st0 + (size_t)s * stage_elems;
       const int r0 = tile * R, r1 = min(P.n, r0 + R);
-      int64_t ro = 0;
-      int cnt = 0, flags = 0;
-      if (lane >= 16) {
-        ro = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
-        cnt = nbr(ix, P.Nx) * nbr(iy, P.Ny) * nbr(iz, P.Nz);
-        flags = (ix > 0) | (ix < P.Nx - 1) << 1 | (iy > 0) << 2 | (iy < P.Ny - 1) << 3 |
-                (iz > 0) << 4 | (iz < P.Nz - 1) << 5;
-      }
-      const int64_t a = __shfl_sync(0xffffffffu, ro, 16);
-      const int64_t e = __shfl_sync(0xffffffffu, ro + cnt, 16 + (r1 - r0 - 1));
+      const int64_t ro = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
+      const int cnt = nbr(ix, P.Nx) * nbr(iy, P.Ny) * nbr(iz, P.Nz);
+      const int flags = (ix > 0) | (ix < P.Nx - 1) << 1 | (iy > 0) << 2 | (iy < P.Ny - 1) << 3 |
+                        (iz > 0) << 4 | (iz < P.Nz - 1) << 5;
+      const int64_t a = __shfl_sync(0xffffffffu, ro, 0);
+      const int64_t e = __shfl_sync(0xffffffffu, ro + cnt, r1 - r0 - 1);
       // this lane's piece: elements [lo_e, bl_e) by bulk copy, [bl_e, hi_e)
       // (the unaligned end of the array) by plain loads
       int64_t lo_e = 0, bl_e = 0, hi_e = 0;
@@ -221,7 +236,7 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
       }
       fits = __all_sync(0xffffffffu, fits);
       fast = __all_sync(0xffffffffu, fast);
-      if (lane >= 16) {
+      {
         s_rro[s][rl] = (uint32_t)ro;
         s_rflags[s][rl] = r0 + rl < r1 ? flags : 0;
         ix += sxs;
@@ -267,53 +282,161 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
       for (int st = p; st < S && st < it; st += kProdM)
         mbar_wait_bounded(&full[st], (unsigned)(((it - st + S - 1) / S - 1) & 1));
     }
-  } else {
-    const int lr = warp - kProdM;
-    const bool lane_on = lane < nr;
+  } else if constexpr (NRC == 32) {
+    // consumer warp w: rows 2w (lanes 0-15) and 2w + 1 (lanes 16-31) of each
+    // tile, lane h of a half holding right-hand sides 2h and 2h + 1 (paired
+    // loads and stores; the row's values are broadcast to its half)
+    using V2 = typename Vec2<T>::type;
+    const int w = warp - kProdM, half = lane >> 4, h = lane & 15;
+    const int lrow = 2 * w + half;
+    double d0 = 0.0, d1 = 0.0;
+    DFAcc f0, f1;
     int it = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
       const int s = it % S;
-      const int r = tile * R + lr;
-      const bool active = r < P.n;  // warp-uniform
+      const int r = tile * R + lrow;
       if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
         atomicOr(P.err, ERR_WAIT_TIMEOUT);
         break;
       }
-      T sum = T(0);
-      T xr = T(0);
-      const int flags = s_rflags[s][lr];
-      const bool ok = active && s_ok[s] != 0;
-      const bool interior = flags == 63;
-      const int lj = lane_on ? lane : 0;
+      const int flags = s_rflags[s][lrow];
+      const bool ok = r < P.n && s_ok[s] != 0;
       const T* sv = st0 + (size_t)s * stage_elems;
       const T* sx = sv + capv;
-      const T* rowv = sv + (s_rro[s][lr] - s_vbase[s]);
-      if (ok && interior && s_fast[s]) {
-        // every segment of this stage starts at row r0 + off_j - 1, so row r's
-        // x values sit at the same place in all nine: fixed offsets, 27 terms
-        const T* xb = sx + (lr + 1) * nr + lj;
-        xr = xb[4 * capx];
-        T s0 = T(0), s1 = T(0);
+      const T* rowv = sv + (s_rro[s][lrow] - s_vbase[s]);
+      V2 sum{T(0), T(0)}, xr{T(0), T(0)};
+      if (__all_sync(0xffffffffu, ok && flags == 63) && s_fast[s]) {
+        // every segment of this stage starts at row r0 + off_j - 1, so the
+        // row's x values sit at the same place in all nine: fixed offsets
+        const T* xb = sx + (lrow + 1) * 32 + 2 * h;
+        xr = *reinterpret_cast<const V2*>(xb + 4 * capx);
+        V2 a0{T(0), T(0)}, a1{T(0), T(0)};
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
 #pragma unroll
           for (int dx = -1; dx <= 1; ++dx) {
             const int slot = j * 3 + dx + 1;
             const T v = rowv[slot];
-            const T xv = xb[j * capx + dx * nr];
-            if (slot & 1)
-              s1 = fma(v, xv, s1);
-            else
-              s0 = fma(v, xv, s0);
+            const V2 xv = *reinterpret_cast<const V2*>(xb + j * capx + dx * 32);
+            if (slot & 1) {
+              a1.x = fma(v, xv.x, a1.x);
+              a1.y = fma(v, xv.y, a1.y);
+            } else {
+              a0.x = fma(v, xv.x, a0.x);
+              a0.y = fma(v, xv.y, a0.y);
+            }
           }
         }
-        sum = s0 + s1;
+        sum.x = a0.x + a1.x;
+        sum.y = a0.y + a1.y;
       } else if (ok) {
         const bool vxm = flags & 1, vxp = flags & 2, vym = flags & 4, vyp = flags & 8;
         const bool vzm = flags & 16, vzp = flags & 32;
         const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp, cxy = cx * cy;
+        const T* xc = sx + 4 * (size_t)capx + ((int64_t)r * 32 + 2 * h - s_xbase[s][4]);
+        xr = *reinterpret_cast<const V2*>(xc);
+        V2 a0{T(0), T(0)}, a1{T(0), T(0)};
+        int slot = 0;
+#pragma unroll
+        for (int dz = -1; dz <= 1; ++dz) {
+          const bool vz = dz < 0 ? vzm : (dz > 0 ? vzp : true);
+          const int bz = dz < 0 ? 0 : (dz == 0 ? (int)vzm : (int)vzm + 1);
+#pragma unroll
+          for (int dy = -1; dy <= 1; ++dy) {
+            const bool vy = dy < 0 ? vym : (dy > 0 ? vyp : true);
+            const int by = dy < 0 ? 0 : (dy == 0 ? (int)vym : (int)vym + 1);
+            const int j = (dz + 1) * 3 + (dy + 1);
+            const int off = dz * P.NxNy + dy * P.Nx;
+            const T* seg = sx + (size_t)j * capx + ((int64_t)(r + off) * 32 + 2 * h - s_xbase[s][j]);
+            const int pbase = bz * cxy + by * cx;
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+              const bool vx = dx < 0 ? vxm : (dx > 0 ? vxp : true);
+              const int bx = dx < 0 ? 0 : (dx == 0 ? (int)vxm : (int)vxm + 1);
+              const bool valid = vz && vy && vx;
+              const T v = valid ? rowv[pbase + bx] : T(0);
+              const V2 xv = *reinterpret_cast<const V2*>(valid ? seg + dx * 32 : xc);
+              if (slot & 1) {
+                a1.x = fma(v, xv.x, a1.x);
+                a1.y = fma(v, xv.y, a1.y);
+              } else {
+                a0.x = fma(v, xv.x, a0.x);
+                a0.y = fma(v, xv.y, a0.y);
+              }
+              ++slot;
+            }
+          }
+        }
+        sum.x = a0.x + a1.x;
+        sum.y = a0.y + a1.y;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (ok) {
+        const int64_t idx = (int64_t)r * 32 + 2 * h;
+        if (MODE == MM_RESID) {
+          const double2 b2 = *reinterpret_cast<const double2*>(P.b + idx);
+          const double e0 = b2.x - widen(sum.x), e1 = b2.y - widen(sum.y);
+          typename Vec2<RT>::type o;
+          o.x = (RT)e0;
+          o.y = (RT)e1;
+          *reinterpret_cast<typename Vec2<RT>::type*>(P.yres + idx) = o;
+          d0 = fma(e0, e0, d0);
+          d1 = fma(e1, e1, d1);
+        } else {
+          *reinterpret_cast<V2*>(P.y + idx) = sum;
+          if (MODE == MM_DOT) {
+            if constexpr (sizeof(T) == 4) {
+              f0.add_product(sum.x, xr.x);
+              f1.add_product(sum.y, xr.y);
+            } else {
+              d0 = fma(sum.x, xr.x, d0);
+              d1 = fma(sum.y, xr.y, d1);
+            }
+          }
+        }
+      }
+    }
+    // to one lane per right-hand side: j = 2h + c is held by lanes h, h + 16
+    double t0 = d0 + f0.value(), t1 = d1 + f1.value();
+    t0 += __shfl_xor_sync(0xffffffffu, t0, 16);
+    t1 += __shfl_xor_sync(0xffffffffu, t1, 16);
+    const double u0 = __shfl_sync(0xffffffffu, t0, lane >> 1);
+    const double u1 = __shfl_sync(0xffffffffu, t1, lane >> 1);
+    dacc = (lane & 1) ? u1 : u0;
+  } else {
+    // any nrhs dividing 32: consumer warp w handles rows w and w + 16 of each
+    // tile, one lane per right-hand side
+    const int w = warp - kProdM;
+    const bool lane_on = lane < nr;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int s = it % S;
+      if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        break;
+      }
+      T sum[R / kConsM], xr[R / kConsM];
+      bool okq[R / kConsM];
+#pragma unroll
+      for (int q = 0; q < R / kConsM; ++q) {
+        const int lr = w + q * kConsM;
+        const int r = tile * R + lr;
+        const int flags = s_rflags[s][lr];
+        const bool ok = r < P.n && s_ok[s] != 0;
+        okq[q] = ok;
+        sum[q] = T(0);
+        xr[q] = T(0);
+        const int lj = lane_on ? lane : 0;
+        const T* sv = st0 + (size_t)s * stage_elems;
+        const T* sx = sv + capv;
+        const T* rowv = sv + (s_rro[s][lr] - s_vbase[s]);
+        if (!ok) continue;
+        const bool vxm = flags & 1, vxp = flags & 2, vym = flags & 4, vyp = flags & 8;
+        const bool vzm = flags & 16, vzp = flags & 32;
+        const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp, cxy = cx * cy;
         const T* xc = sx + 4 * (size_t)capx + ((int64_t)r * nr + lj - s_xbase[s][4]);
-        xr = xc[0];
+        xr[q] = xc[0];
         T s0 = T(0), s1 = T(0);
         int slot = 0;
 #pragma unroll
@@ -333,43 +456,43 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
               const bool vx = dx < 0 ? vxm : (dx > 0 ? vxp : true);
               const int bx = dx < 0 ? 0 : (dx == 0 ? (int)vxm : (int)vxm + 1);
               const bool valid = vz && vy && vx;
-              const T v = rowv[valid ? pbase + bx : 0];
+              const T v = valid ? rowv[pbase + bx] : T(0);
               const T xv = *(valid ? seg + (int64_t)dx * nr : xc);
-              if (slot & 1) {
-                const T t1 = fma(v, xv, s1);
-                s1 = valid ? t1 : s1;
-              } else {
-                const T t0 = fma(v, xv, s0);
-                s0 = valid ? t0 : s0;
-              }
+              if (slot & 1)
+                s1 = fma(v, xv, s1);
+              else
+                s0 = fma(v, xv, s0);
               ++slot;
             }
           }
         }
-        sum = s0 + s1;
+        sum[q] = s0 + s1;
       }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[s]);
-      if (ok && lane_on) {
-        const int64_t idx = (int64_t)r * nr + lane;
+#pragma unroll
+      for (int q = 0; q < R / kConsM; ++q) {
+        if (!okq[q] || !lane_on) continue;
+        const int64_t idx = (int64_t)(tile * R + w + q * kConsM) * nr + lane;
         if (MODE == MM_RESID) {
-          const double res = P.b[idx] - widen(sum);
+          const double res = P.b[idx] - widen(sum[q]);
           P.yres[idx] = (RT)res;
           dacc = fma(res, res, dacc);
         } else {
-          P.y[idx] = sum;
+          P.y[idx] = sum[q];
           if (MODE == MM_DOT) {
             if constexpr (sizeof(T) == 4)
-              facc.add_product(sum, xr);
+              facc.add_product(sum[q], xr[q]);
             else
-              dacc = fma(sum, xr, dacc);
+              dacc = fma(sum[q], xr[q], dacc);
           }
         }
       }
     }
   }
   if (MODE != MM_PLAIN)
-    multi_dot_reduce(warp < kProdM ? 0.0 : dacc + facc.value(), red, P.partials, P.ticket, P.out, nr);
+    multi_dot_reduce(warp < kProdM ? 0.0 : dacc + facc.value(), red, P.partials, P.ticket, P.out, nr,
+                     MODE == MM_DOT ? P.cg : nullptr);
 }
 
 // lanes j, j+nrhs, j+2nrhs, ... of a warp hold right-hand side j: sum them
@@ -380,42 +503,134 @@ __device__ __forceinline__ double lane_group_sum(double v, int nrhs)
   return v;
 }
 
+// 16-byte vectors of the work arrays: element e of the n x nrhs block
+// belongs to right-hand side e % nrhs, so the VW components of a thread's
+// vectors keep the same right-hand sides across its grid-stride loop
+// (the stride is a multiple of 32 elements).
+template <typename V>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int n = 2;
+};
+template <typename V>
+__device__ __forceinline__ V& comp(typename Vec16<V>::type& v, int c)
+{
+  return reinterpret_cast<V*>(&v)[c];
+}
+
 template <typename V>
 __global__ void __launch_bounds__(kVT)
     k_mr_p(int64_t ntot, int nrhs, const V* __restrict__ r, V* __restrict__ p, const MultiState* st)
 {
-  const int j = threadIdx.x % nrhs;
+  using VV = typename Vec16<V>::type;
+  constexpr int VW = Vec16<V>::n;
+  const int64_t g0 = (int64_t)blockIdx.x * kVT + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * kVT;
   const bool first = st->first != 0;
-  const V beta = st->done[j] ? V(0) : (V)st->beta[j];
-  for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT)
-    p[i] = first ? r[i] : fma(beta, p[i], r[i]);
+  V beta[VW];
+#pragma unroll
+  for (int c = 0; c < VW; ++c) {
+    const int j = (VW * threadIdx.x + c) % nrhs;
+    beta[c] = st->done[j] ? V(0) : (V)st->beta[j];
+  }
+  const int64_t nvec = ntot / VW;
+  const VV* r4 = reinterpret_cast<const VV*>(r);
+  VV* p4 = reinterpret_cast<VV*>(p);
+  for (int64_t v = g0; v < nvec; v += stride) {
+    const VV rv = r4[v];
+    VV pv = first ? rv : p4[v];
+    if (!first) {
+#pragma unroll
+      for (int c = 0; c < VW; ++c) comp<V>(pv, c) = fma(beta[c], comp<V>(pv, c), comp<V>(const_cast<VV&>(rv), c));
+    }
+    p4[v] = pv;
+  }
+  if (g0 == nvec % stride) {
+#pragma unroll
+    for (int c = 0; c < VW; ++c) {
+      const int64_t e = nvec * VW + c;
+      if (e < ntot) p[e] = first ? r[e] : fma(beta[c], p[e], r[e]);
+    }
+  }
 }
 
-// x += alpha_j p, r -= alpha_j Ap, rr_new_j = r_j.r_j (FP64); x is the FP32
-// correction x32 in the mixed solver and the FP64 solution otherwise
+// x += alpha_j p, r -= alpha_j Ap, rr_new_j = r_j.r_j; x is the FP32
+// correction x32 in the mixed solver and the FP64 solution otherwise.  The
+// FP32 squares are summed in double-float, the FP64 ones in FP64.
 template <typename V>
 __global__ void __launch_bounds__(kVT)
     k_mr_update(int64_t ntot, int nrhs, V* __restrict__ x, V* __restrict__ r,
                 const V* __restrict__ p, const V* __restrict__ Ap, MultiState* st,
                 double* partials, unsigned* ticket)
 {
+  using VV = typename Vec16<V>::type;
+  constexpr int VW = Vec16<V>::n;
   __shared__ double red[(kVT / 32 + 1) * 32];
-  const int j = threadIdx.x % nrhs;
-  const V alpha = st->done[j] ? V(0) : (V)(st->rr[j] / st->pAp[j]);
-  double acc = 0.0;
-  DFAcc facc;
-  for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT) {
-    x[i] = fma(alpha, p[i], x[i]);
-    const V rv = fma(-alpha, Ap[i], r[i]);
-    r[i] = rv;
-    if constexpr (sizeof(V) == 4)
-      facc.add_product(rv, rv);
-    else
-      acc = fma(rv, rv, acc);
+  __shared__ double ent[kVT * VW];
+  const int64_t g0 = (int64_t)blockIdx.x * kVT + threadIdx.x;
+  const int64_t stride = (int64_t)gridDim.x * kVT;
+  V alpha[VW];
+#pragma unroll
+  for (int c = 0; c < VW; ++c) {
+    alpha[c] = (V)st->alpha[(VW * threadIdx.x + c) % nrhs];
   }
-  acc = lane_group_sum(acc + facc.value(), nrhs);
-  if ((threadIdx.x & 31) >= nrhs) acc = 0.0;
-  multi_dot_reduce(acc, red, partials, ticket, st->rr_new, nrhs);
+  double acc[VW];
+  DFAcc facc[VW];
+#pragma unroll
+  for (int c = 0; c < VW; ++c) acc[c] = 0.0;
+  const int64_t nvec = ntot / VW;
+  VV* x4 = reinterpret_cast<VV*>(x);
+  VV* r4 = reinterpret_cast<VV*>(r);
+  const VV* p4 = reinterpret_cast<const VV*>(p);
+  const VV* a4 = reinterpret_cast<const VV*>(Ap);
+  for (int64_t v = g0; v < nvec; v += stride) {
+    VV xv = x4[v], rv = r4[v];
+    VV pv = p4[v], av = a4[v];
+#pragma unroll
+    for (int c = 0; c < VW; ++c) {
+      comp<V>(xv, c) = fma(alpha[c], comp<V>(pv, c), comp<V>(xv, c));
+      const V rn = fma(-alpha[c], comp<V>(av, c), comp<V>(rv, c));
+      comp<V>(rv, c) = rn;
+      if constexpr (sizeof(V) == 4)
+        facc[c].add_product(rn, rn);
+      else
+        acc[c] = fma(rn, rn, acc[c]);
+    }
+    x4[v] = xv;
+    r4[v] = rv;
+  }
+  if (g0 == nvec % stride) {
+#pragma unroll
+    for (int c = 0; c < VW; ++c) {
+      const int64_t e = nvec * VW + c;
+      if (e >= ntot) continue;
+      x[e] = fma(alpha[c], p[e], x[e]);
+      const V rn = fma(-alpha[c], Ap[e], r[e]);
+      r[e] = rn;
+      if constexpr (sizeof(V) == 4)
+        facc[c].add_product(rn, rn);
+      else
+        acc[c] = fma(rn, rn, acc[c]);
+    }
+  }
+  // entry VW*t + c holds right-hand side (VW*t + c) % nrhs; entries t + k*kVT
+  // share thread t's right-hand side t % nrhs
+#pragma unroll
+  for (int c = 0; c < VW; ++c) ent[VW * threadIdx.x + c] = acc[c] + facc[c].value();
+  __syncthreads();
+  double a = 0.0;
+#pragma unroll
+  for (int k = 0; k < VW; ++k) a += ent[threadIdx.x + k * kVT];
+  a = lane_group_sum(a, nrhs);
+  if ((threadIdx.x & 31) >= nrhs) a = 0.0;
+  multi_dot_reduce(a, red, partials, ticket, st->rr_new, nrhs);
 }
 
 __global__ void __launch_bounds__(kVT)
@@ -599,7 +814,7 @@ mfe_status spmm_setup(mfe_ctx* ctx, int nrhs, int* per_sm)
 template <typename T, int MODE, typename RT>
 mfe_status launch_spmm_t(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const T* X, T* Y,
                          const double* Bv, RT* yres, double* partials, unsigned* ticket,
-                         double* out, const int* gate, unsigned* err)
+                         double* out, const int* gate, unsigned* err, MultiState* cg = nullptr)
 {
   SpmmParams<T, RT> P;
   P.Nx = A->box_nx + 1;
@@ -621,6 +836,7 @@ mfe_status launch_spmm_t(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const T* X, T
   P.out = out;
   P.gate = gate;
   P.err = err;
+  P.cg = cg;
   const size_t smem = spmm_smem<T>(nrhs);
   const int threads = kThreadsM;
   int per_sm = 1;
@@ -662,7 +878,8 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
   k_mr_p<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
   MFE_TRY((launch_spmm_t<float, MM_DOT, float>(ctx, &A32, nrhs, W.p, W.Ap, nullptr, nullptr,
-                                                W.partials, W.tickets, W.st->pAp, nullptr, W.err)));
+                                                W.partials, W.tickets, W.st->pAp, nullptr, W.err,
+                                                W.st)));
   k_mr_update<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
       ntot, nrhs, W.x32, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mr_update"));
@@ -684,7 +901,8 @@ mfe_status multi_iter_f64(mfe_ctx* ctx, const mfe_csr& A64, int nrhs, double* X,
   k_mr_p<double><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
   MFE_TRY((launch_spmm_t<double, MM_DOT, double>(ctx, &A64, nrhs, W.p, W.Ap, nullptr, nullptr,
-                                                  W.partials, W.tickets, W.st->pAp, nullptr, W.err)));
+                                                  W.partials, W.tickets, W.st->pAp, nullptr, W.err,
+                                                  W.st)));
   k_mr_update<double><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
       ntot, nrhs, X, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mr_update"));
