@@ -32,7 +32,8 @@ __all__ = [
     "MiniFEError", "Context", "CSRMatrix", "CGResult", "default_context", "box_dims",
     "generate_matrix_structure", "assemble_FE_data", "impose_dirichlet", "box_bc_rows",
     "build_system", "matvec", "matvec_and_dot", "dot", "waxpby", "fused_waxpby", "cg_solve",
-    "cg_solve_host", "cg_solve_multi", "verify_solution", "element_gradient", "to_f32", "spmm",
+    "cg_solve_host", "cg_solve_multi", "batch_solve_boxes", "verify_solution",
+    "element_gradient", "to_f32", "spmm",
 ]
 
 DBL_EPSILON = 2.220446049250313e-16
@@ -401,6 +402,32 @@ def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPS
         ctx.check(st, "mfe_cg_solve_multi")
     return [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status, tuple(r.times),
                      r.refinements, None) for r in res]
+
+
+def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
+                      tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
+                      ctx: Context | None = None):
+    """Assemble and solve len(dims) independent miniFE boxes (k = 1, the
+    reference's boundary conditions) together on the device.  Returns
+    (x, offsets, results): x concatenates the solutions, box i's rows being
+    x[offsets[i]:offsets[i+1]]; results holds one CGResult per box (times[0]
+    = assembly of the batch, times[4] = the batched solve, in seconds)."""
+    torch = _torch()
+    ctx = ctx or default_context()
+    dims = [tuple(int(v) for v in d) for d in dims]
+    offsets = [0]
+    for d in dims:
+        offsets.append(offsets[-1] + box_dims(*d)[0])
+    x = torch.empty(max(offsets[-1], 1), dtype=torch.float64, device="cuda")
+    flat = (ctypes.c_int32 * (3 * len(dims)))(*[v for d in dims for v in d])
+    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k)
+    res = (MfeCgResult * max(len(dims), 1))()
+    st = ctx.lib.mfe_batch_solve_boxes(ctx.h, len(dims), flat, ctypes.byref(o), _ptr(x), res)
+    if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
+        ctx.check(st, "mfe_batch_solve_boxes")
+    return x, offsets, [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status,
+                                 tuple(r.times), r.refinements, None)
+                        for r in res[:len(dims)]]
 
 
 def cg_solve_host(row_offsets, cols, vals, b, x, max_iter=200, tol=DBL_EPSILON,

@@ -30,6 +30,7 @@ SOURCES = {
     "mfe_noalloc.cu": [],
     "mfe_mixed.cu": [],
     "mfe_multi.cu": [],
+    "mfe_batch.cu": [],
     "mfe_cg.cu": [],
 }
 

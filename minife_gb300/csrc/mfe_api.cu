@@ -620,8 +620,13 @@ mfe_status mfe_cg_solve_multi(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, cons
 mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims,
                                  const mfe_cg_opts* opts, double* x_out, mfe_cg_result* results)
 {
-  (void)nbox; (void)dims; (void)opts; (void)x_out; (void)results;
-  return fail(ctx, MFE_NOT_SUPPORTED, "batched boxes are not built yet");
+  if (!ctx) return MFE_BAD_ARG;
+  if (!dims || !opts || !x_out || !results) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  for (int32_t i = 0; i < nbox; ++i)
+    if (!box_ok(dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]))
+      return fail(ctx, MFE_BAD_ARG, "bad box in the batch");
+  MFE_TRY(set_device(ctx));
+  return batch_solve_boxes(ctx, nbox, dims, opts, x_out, results);
 }
 
 }  // extern "C"

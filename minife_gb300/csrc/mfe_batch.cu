@@ -1,0 +1,1050 @@
+// Batched uneven boxes: nbox independent miniFE problems (each its own
+// nx x ny x nz box, k = 1, the reference's boundary conditions) assembled
+// into one concatenated store and solved with CG, all boxes advancing
+// together: every iteration is one fixed sequence of launches over all
+// boxes that are still iterating, captured once as a CUDA graph with a
+// conditional while node.
+//
+// HBM layout.  Box b owns rows [row_base_b, row_base_b + n_b) of every
+// concatenated vector and values [nnz_base_b, nnz_base_b + nnz_b) of the
+// concatenated CSR values (FP64, plus an FP32 copy for the mixed solver);
+// both bases are multiples of four elements, so every slice starts on a
+// 16-byte boundary and the bulk copies of the box SpMV can round ranges
+// outwards inside the slice.  Column indices are not stored: the box
+// layout gives them in closed form (mfe_box.cuh).
+//
+// Work lists.  Each launch walks a list of boxes (those still iterating, or
+// those taking a reliable update) in box order, with prefix sums of their
+// SpMV tiles and vector chunks; one block rebuilds the lists after each
+// iteration, so finished boxes cost nothing and the grid stays busy until
+// the largest box converges.
+//
+// SpMV.  k_bx_spmv is the box SpMV of mfe_spmv_box.cu (warp-specialised:
+// one producer lane stages a tile's values and nine x segments with bulk
+// copies, consumer warps own one row per thread) over the global tile list
+// of the launch.  Per-box dot products are deterministic: each consumer
+// warp writes one partial per (box, CTA) it worked on; the last warp to
+// finish a box (per-box counter) sums that box's partials in CTA order and
+// forms the box's scalar (alpha or the true residual).
+//
+// Vectors.  k_bx_p / k_bx_update walk the chunk list (kBxChunk rows of one
+// box per block pass); per-box r.r: one partial per chunk, the last block of
+// the box sums them in chunk order.
+//
+// Solvers.  FP64: the reference's CG per box (cg_solve.hpp loop test with
+// normr from the top of the iteration).  Mixed: FP32 values and vectors, FP64
+// dots and scalars, FP64 solution; a box takes a reliable update (x += x32,
+// r = b - A64 x in FP64, FP32 copy of r) when its recursive residual fell
+// tenfold since its last update, claims convergence, or after refine_k
+// iterations, and it finishes only on its true FP64 residual.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <vector>
+
+#include "mfe_box.cuh"
+#include "mfe_common.cuh"
+#include "mfe_internal.h"
+
+namespace mfe {
+
+constexpr int kBxMaxBoxes = 1024;
+constexpr int kBxVT = 256;       // vector-kernel block
+constexpr int kBxChunk = 8192;   // rows per vector chunk
+constexpr int kBxPad = 4;        // slice alignment in elements
+
+struct BoxDesc {
+  int Nx, Ny, Nz, NxNy;
+  int n;
+  int ntiles32, ntiles64;  // SpMV tiles at the FP32 and FP64 shapes
+  int nchunks, chunk_base;
+  int64_t row_base, nnz_base;
+};
+
+struct BoxSt {
+  double rr, rr_new, pAp, alpha, beta, rr_true, rr_upd, normr0, normr, tol_abs;
+  int open, gate, iters, since, brk;
+  unsigned cnt_mv, cnt_vec;
+};
+
+struct BatchCtl {
+  int nbox, k, max_iter, refine_k, first, cont, status, updates, tol_mode;
+  double delta2;
+  unsigned err;
+};
+
+// Boxes taking part in a launch, in box order, with prefix sums of their
+// tiles (FP32 and FP64 shapes) and vector chunks.
+struct BxList {
+  int* ids;
+  int* tpre32;
+  int* tpre64;
+  int* cpre;
+  int* count;
+};
+
+__host__ __device__ constexpr int bx_capv(int rows) { return ((rows * 27 + 8) + 3) & ~3; }
+__host__ __device__ constexpr int bx_capx(int rows) { return ((rows + 2 + 8) + 3) & ~3; }
+template <typename T>
+struct BxShape;
+template <>
+struct BxShape<float> {
+  static constexpr int rows = 256, stages = 2;
+};
+template <>
+struct BxShape<double> {
+  static constexpr int rows = 128, stages = 2;
+};
+template <typename T>
+constexpr size_t bx_smem()
+{
+  return (size_t)BxShape<T>::stages *
+         ((size_t)bx_capv(BxShape<T>::rows) + 9 * (size_t)bx_capx(BxShape<T>::rows)) * sizeof(T);
+}
+
+// position q of global index i in a prefix array pre[0..cnt] (pre[q] <= i <
+// pre[q+1]), searching forward from a previous position
+__device__ __forceinline__ int bx_advance(const int* pre, int cnt, int q, int i)
+{
+  if (q < 0 || __ldg(&pre[q]) > i) {
+    int lo = 0, hi = cnt - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (__ldg(&pre[mid]) <= i) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  }
+  while (q + 1 < cnt && __ldg(&pre[q + 1]) <= i) ++q;
+  return q;
+}
+
+enum BxMode { BX_DOT = 1, BX_RESID = 2 };
+
+template <typename T>
+struct BxSpmvParams {
+  const BoxDesc* boxes;
+  BoxSt* st;
+  const int* ids;
+  const int* tpre;
+  const int* count;
+  const T* __restrict__ vals;
+  const T* __restrict__ x;
+  T* __restrict__ y;              // DOT output; RESID output when y32 is null
+  const double* __restrict__ b;   // RESID
+  float* __restrict__ y32;        // RESID output (FP32) when set
+  double* slots;                  // [nbox][grid][consumer warps]
+  unsigned* err;
+};
+
+// Consumer warp cw of this CTA is done with box b (list position q): its
+// partial goes to the box's slot; the last of the box's warps sums the
+// slots of every CTA that worked on the box, in CTA order, and forms the
+// box's scalar.
+template <typename T, int MODE, int C>
+__device__ void bx_flush(const BxSpmvParams<T>& P, int b, int q, int cw, double dacc)
+{
+  const int lane = threadIdx.x & 31;
+  const double v = warp_sum(dacc);
+  const int G = gridDim.x;
+  const int A = __ldg(&P.tpre[q]);
+  const int nt = __ldg(&P.tpre[q + 1]) - A;
+  const unsigned expected = (unsigned)min(nt, G) * C;
+  double* slot = P.slots + (size_t)b * G * C;
+  unsigned old = 0;
+  if (lane == 0) {
+    slot[(size_t)blockIdx.x * C + cw] = v;
+    __threadfence();
+    old = atomicAdd(&P.st[b].cnt_mv, 1u);
+  }
+  old = __shfl_sync(0xffffffffu, old, 0);
+  if (old != expected - 1) return;
+  __threadfence();
+  double s = 0.0;
+  const int a0 = A % G;
+  for (int c = lane; c < G; c += 32) {
+    const bool visited = nt >= G || ((c - a0 + G) % G) < nt;
+    if (!visited) continue;
+#pragma unroll
+    for (int w = 0; w < C; ++w) s += __ldcg(&slot[(size_t)c * C + w]);
+  }
+  s = warp_sum(s);
+  if (lane == 0) {
+    BoxSt& bs = P.st[b];
+    if (MODE == BX_DOT) {
+      bs.pAp = s;
+      if (s > 0.0) {
+        bs.alpha = bs.rr / s;
+      } else {
+        bs.alpha = 0.0;
+        bs.brk = 1;
+      }
+    } else {
+      bs.rr_true = s;
+    }
+    bs.cnt_mv = 0u;
+  }
+}
+
+template <typename T, int MODE>
+__global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<T> P)
+{
+  constexpr int ROWS = BxShape<T>::rows, S = BxShape<T>::stages, C = ROWS / 32;
+  constexpr int capv = bx_capv(ROWS), capx = bx_capx(ROWS);
+  constexpr int stage_elems = capv + 9 * capx;
+  constexpr int VA = 16 / sizeof(T);
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full[S], empty[S];
+  __shared__ int s_vbase[S];
+  __shared__ int s_xbase[S][9];
+  __shared__ int s_ok[S];
+  T* const st0 = reinterpret_cast<T*>(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cnt = *P.count;
+  if (cnt == 0) return;
+  const int total = __ldg(&P.tpre[cnt]);
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < S; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], C);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = true;
+      int it = 0, q = -1, b = -1;
+      BoxDesc d{};
+      for (int i = blockIdx.x; i < total; i += gridDim.x, ++it) {
+        const int s = it % S;
+        if (it >= S) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / S) - 1) & 1));
+        if (!ok) break;
+        const int nq = bx_advance(P.tpre, cnt, q, i);
+        if (nq != q) {
+          q = nq;
+          b = __ldg(&P.ids[q]);
+          d = P.boxes[b];
+        }
+        const int lt = i - __ldg(&P.tpre[q]);
+        T* sv = st0 + (size_t)s * stage_elems;
+        T* sx = sv + capv;
+        const int r0 = lt * ROWS, r1 = min(d.n, r0 + ROWS);
+        const int a = (int)row_offset_of32(r0, d.Nx, d.Ny, d.Nz, d.NxNy);
+        const int e = (int)row_offset_of32(r1, d.Nx, d.Ny, d.Nz, d.NxNy);
+        // ranges round outwards to the copy granule inside the box's padded slice
+        const int av = a & ~(VA - 1), bv = (e + VA - 1) & ~(VA - 1);
+        bool fits = bv - av <= capv;
+        int xlo[9], xhi[9];
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          const int off = (j / 3 - 1) * d.NxNy + (j % 3 - 1) * d.Nx;
+          const int lo = min(max(r0 + off - 1, 0), d.n);
+          const int hi = max(min(r1 + off + 1, d.n), lo);
+          xlo[j] = lo & ~(VA - 1);
+          xhi[j] = (hi + VA - 1) & ~(VA - 1);
+          fits = fits && xhi[j] - xlo[j] <= capx;
+        }
+        if (!fits) {
+          // cannot happen for the stage capacities above
+          atomicOr(P.err, ERR_TILE_OVERFLOW);
+          s_ok[s] = 0;
+          mbar_arrive_expect_tx(&full[s], 0);
+          continue;
+        }
+        s_ok[s] = 1;
+        s_vbase[s] = av;
+        unsigned bytes = (unsigned)((bv - av) * sizeof(T));
+#pragma unroll
+        for (int j = 0; j < 9; ++j) {
+          s_xbase[s][j] = xlo[j];
+          bytes += (unsigned)((xhi[j] - xlo[j]) * sizeof(T));
+        }
+        mbar_arrive_expect_tx(&full[s], bytes);
+        if (bv > av) bulk_g2s(sv, P.vals + d.nnz_base + av, (unsigned)((bv - av) * sizeof(T)), &full[s]);
+#pragma unroll
+        for (int j = 0; j < 9; ++j)
+          if (xhi[j] > xlo[j])
+            bulk_g2s(sx + (size_t)j * capx, P.x + d.row_base + xlo[j],
+                     (unsigned)((xhi[j] - xlo[j]) * sizeof(T)), &full[s]);
+      }
+      if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        for (int st = 0; st < S && st < it; ++st)
+          mbar_wait_bounded(&full[st], (unsigned)(((it - st + S - 1) / S - 1) & 1));
+      }
+    }
+  } else {
+    const int cw = warp - 1;
+    const int lr = cw * 32 + lane;
+    double dacc = 0.0;
+    int it = 0, q = -1, b = -1;
+    BoxDesc d{};
+    for (int i = blockIdx.x; i < total; i += gridDim.x, ++it) {
+      const int s = it % S;
+      const int nq = bx_advance(P.tpre, cnt, q, i);
+      if (nq != q) {
+        if (q >= 0) bx_flush<T, MODE, C>(P, b, q, cw, dacc);
+        dacc = 0.0;
+        q = nq;
+        b = __ldg(&P.ids[q]);
+        d = P.boxes[b];
+      }
+      const int lt = i - __ldg(&P.tpre[q]);
+      const int r = lt * ROWS + lr;
+      const bool active = r < d.n;
+      const int rr = active ? r : d.n - 1;
+      const int iz = rr / d.NxNy, rem = rr - iz * d.NxNy, iy = rem / d.Nx, ix = rem - iy * d.Nx;
+      const int roff = (int)row_offset(ix, iy, iz, d.Nx, d.Ny, d.Nz);
+      if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        break;
+      }
+      T sum = T(0), xr = T(0);
+      const bool ok = active && s_ok[s] != 0;
+      if (ok) {
+        const T* sv = st0 + (size_t)s * stage_elems;
+        const T* sx = sv + capv;
+        const T* rowv = sv + (roff - s_vbase[s]);
+        const bool vxm = ix > 0, vxp = ix < d.Nx - 1, vym = iy > 0, vyp = iy < d.Ny - 1;
+        const bool vzm = iz > 0, vzp = iz < d.Nz - 1;
+        const T* xc = sx + 4 * capx + (r - s_xbase[s][4]);
+        xr = xc[0];
+        T s0 = T(0), s1 = T(0);
+        if (vxm && vxp && vym && vyp && vzm && vzp) {
+#pragma unroll
+          for (int j = 0; j < 9; ++j) {
+            const int off = (j / 3 - 1) * d.NxNy + (j % 3 - 1) * d.Nx;
+            const T* seg = sx + j * capx + (r + off - s_xbase[s][j]);
+#pragma unroll
+            for (int dx = -1; dx <= 1; ++dx) {
+              const int k = j * 3 + dx + 1;
+              if (k & 1) s1 = fma(rowv[k], seg[dx], s1);
+              else s0 = fma(rowv[k], seg[dx], s0);
+            }
+          }
+        } else {
+          const int cx = 1 + vxm + vxp, cy = 1 + vym + vyp, cxy = cx * cy;
+          int slot = 0;
+#pragma unroll
+          for (int dz = -1; dz <= 1; ++dz) {
+            const bool vz = dz < 0 ? vzm : (dz > 0 ? vzp : true);
+            const int bz = dz < 0 ? 0 : (dz == 0 ? (int)vzm : (int)vzm + 1);
+#pragma unroll
+            for (int dy = -1; dy <= 1; ++dy) {
+              const bool vy = dy < 0 ? vym : (dy > 0 ? vyp : true);
+              const int by = dy < 0 ? 0 : (dy == 0 ? (int)vym : (int)vym + 1);
+              const int j = (dz + 1) * 3 + (dy + 1);
+              const int off = dz * d.NxNy + dy * d.Nx;
+              const T* seg = sx + j * capx + (r + off - s_xbase[s][j]);
+              const int pbase = bz * cxy + by * cx;
+#pragma unroll
+              for (int dx = -1; dx <= 1; ++dx) {
+                const bool vx = dx < 0 ? vxm : (dx > 0 ? vxp : true);
+                const int bx = dx < 0 ? 0 : (dx == 0 ? (int)vxm : (int)vxm + 1);
+                const bool valid = vz && vy && vx;
+                const T v = rowv[valid ? pbase + bx : 0];
+                const T xv = *(valid ? seg + dx : xc);
+                if (slot & 1) {
+                  const T t1 = fma(v, xv, s1);
+                  s1 = valid ? t1 : s1;
+                } else {
+                  const T t0 = fma(v, xv, s0);
+                  s0 = valid ? t0 : s0;
+                }
+                ++slot;
+              }
+            }
+          }
+        }
+        sum = s0 + s1;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+      if (ok) {
+        const int64_t g = d.row_base + r;
+        if (MODE == BX_RESID) {
+          const double res = P.b[g] - widen(sum);
+          if (P.y32) P.y32[g] = (float)res;
+          else P.y[g] = (T)res;
+          dacc = fma(res, res, dacc);
+        } else {
+          P.y[g] = sum;
+          dacc = fma(widen(sum), widen(xr), dacc);
+        }
+      }
+    }
+    if (q >= 0) bx_flush<T, MODE, C>(P, b, q, cw, dacc);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// vector kernels over the chunk list
+// ---------------------------------------------------------------------------
+struct BxVecParams {
+  const BoxDesc* boxes;
+  BoxSt* st;
+  BatchCtl* ctl;
+  const int* ids;
+  const int* cpre;
+  const int* count;
+  double* chunk_part;  // [total chunks], static chunk index
+};
+
+// p = r + beta_b p (p = r on the first iteration)
+template <typename V>
+__global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restrict__ r, V* __restrict__ p)
+{
+  const int cnt = *Q.count;
+  if (cnt == 0) return;
+  const int total = __ldg(&Q.cpre[cnt]);
+  const bool first = Q.ctl->first != 0;
+  int q = -1;
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    q = bx_advance(Q.cpre, cnt, q, c);
+    const int b = __ldg(&Q.ids[q]);
+    const BoxDesc& d = Q.boxes[b];
+    const int lc = c - __ldg(&Q.cpre[q]);
+    const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
+    const int len = min(kBxChunk, d.n - lc * kBxChunk);
+    const V beta = (V)Q.st[b].beta;
+    for (int k = threadIdx.x; k < len; k += kBxVT) {
+      const int64_t g = g0 + k;
+      p[g] = first ? r[g] : fma(beta, p[g], r[g]);
+    }
+  }
+}
+
+// x += alpha_b p, r -= alpha_b Ap, rr_new_b = r.r over the box's chunks (x is
+// x32 in the mixed solver, the FP64 solution otherwise)
+template <typename V>
+__global__ void __launch_bounds__(kBxVT)
+    k_bx_update(BxVecParams Q, V* __restrict__ x, V* __restrict__ r, const V* __restrict__ p,
+                const V* __restrict__ Ap)
+{
+  __shared__ double red[32];
+  __shared__ bool last;
+  const int cnt = *Q.count;
+  if (cnt == 0) return;
+  const int total = __ldg(&Q.cpre[cnt]);
+  int q = -1;
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    q = bx_advance(Q.cpre, cnt, q, c);
+    const int b = __ldg(&Q.ids[q]);
+    const BoxDesc& d = Q.boxes[b];
+    const int lc = c - __ldg(&Q.cpre[q]);
+    const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
+    const int len = min(kBxChunk, d.n - lc * kBxChunk);
+    const V alpha = (V)Q.st[b].alpha;
+    double acc = 0.0;
+    DFAcc facc;
+    for (int k = threadIdx.x; k < len; k += kBxVT) {
+      const int64_t g = g0 + k;
+      x[g] = fma(alpha, p[g], x[g]);
+      const V rn = fma(-alpha, Ap[g], r[g]);
+      r[g] = rn;
+      if constexpr (sizeof(V) == 4)
+        facc.add_product(rn, rn);
+      else
+        acc = fma(rn, rn, acc);
+    }
+    const double bt = block_sum(acc + facc.value(), red);
+    if (threadIdx.x == 0) {
+      Q.chunk_part[d.chunk_base + lc] = bt;
+      __threadfence();
+      last = atomicAdd(&Q.st[b].cnt_vec, 1u) == (unsigned)d.nchunks - 1;
+    }
+    __syncthreads();
+    if (last) {
+      __threadfence();
+      double s = 0.0;
+      for (int k = threadIdx.x; k < d.nchunks; k += kBxVT) s += __ldcg(&Q.chunk_part[d.chunk_base + k]);
+      s = block_sum(s, red);
+      if (threadIdx.x == 0) {
+        Q.st[b].rr_new = s;
+        Q.st[b].cnt_vec = 0u;
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// x += x32, x32 = 0 over the chunks of the listed (gated) boxes
+__global__ void __launch_bounds__(kBxVT)
+    k_bx_xupdate(BxVecParams Q, double* __restrict__ x, float* __restrict__ x32)
+{
+  const int cnt = *Q.count;
+  if (cnt == 0) return;
+  const int total = __ldg(&Q.cpre[cnt]);
+  int q = -1;
+  for (int c = blockIdx.x; c < total; c += gridDim.x) {
+    q = bx_advance(Q.cpre, cnt, q, c);
+    const int b = __ldg(&Q.ids[q]);
+    const BoxDesc& d = Q.boxes[b];
+    const int lc = c - __ldg(&Q.cpre[q]);
+    const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
+    const int len = min(kBxChunk, d.n - lc * kBxChunk);
+    for (int k = threadIdx.x; k < len; k += kBxVT) {
+      x[g0 + k] += f2d_exact(x32[g0 + k]);
+      x32[g0 + k] = 0.0f;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// per-box bookkeeping: one block of 1024 threads, box b on thread b
+// ---------------------------------------------------------------------------
+// Rebuilds `list` from the boxes whose flag is set (block-wide exclusive scan
+// of their tile and chunk counts).
+__device__ void bx_build_list(const BoxDesc* boxes, int nbox, bool flag, BxList L)
+{
+  __shared__ int wsum[4][32];
+  const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+  const bool f = t < nbox && flag;
+  int v[4] = {f ? 1 : 0, f ? boxes[t].ntiles32 : 0, f ? boxes[t].ntiles64 : 0, f ? boxes[t].nchunks : 0};
+  int inc[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    int x = v[k];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    inc[k] = x;
+    if (lane == 31) wsum[k][w] = x;
+  }
+  __syncthreads();
+  if (w == 0) {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) {
+      int x = wsum[k][lane];
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
+      }
+      wsum[k][lane] = x;  // inclusive over warps
+    }
+  }
+  __syncthreads();
+  int ex[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) ex[k] = inc[k] - v[k] + (w > 0 ? wsum[k][w - 1] : 0);
+  if (f) {
+    L.ids[ex[0]] = t;
+    L.tpre32[ex[0]] = ex[1];
+    L.tpre64[ex[0]] = ex[2];
+    L.cpre[ex[0]] = ex[3];
+  }
+  if (t == blockDim.x - 1) {
+    const int n = ex[0] + v[0];
+    *L.count = n;
+    L.tpre32[n] = ex[1] + v[1];
+    L.tpre64[n] = ex[2] + v[2];
+    L.cpre[n] = ex[3] + v[3];
+  }
+  __syncthreads();
+}
+
+// after the initial residual: normr0, tolerances, open boxes
+__global__ void __launch_bounds__(1024) k_bx_init(const BoxDesc* boxes, BoxSt* st, BatchCtl* ctl, BxList open)
+{
+  const int b = threadIdx.x;
+  const int nbox = ctl->nbox;
+  bool f = false;
+  if (b < nbox) {
+    BoxSt& s = st[b];
+    const double nrm = sqrt(s.rr_true);
+    s.normr0 = nrm;
+    s.normr = nrm;
+    if (ctl->tol_mode) s.tol_abs *= nrm;
+    s.rr = s.rr_true;
+    s.rr_upd = s.rr_true;
+    s.iters = 0;
+    s.since = 0;
+    s.gate = 0;
+    s.brk = 0;
+    s.open = nrm > s.tol_abs && ctl->max_iter > 0;
+    f = s.open;
+  }
+  __syncthreads();
+  bx_build_list(boxes, nbox, f, open);
+  if (b == 0) ctl->cont = *open.count > 0;
+}
+
+__global__ void k_bx_begin(const BatchCtl* ctl, cudaGraphConditionalHandle h)
+{
+  cudaGraphSetConditional(h, ctl->cont ? 1u : 0u);
+}
+
+// Mixed solver, after the update: which open boxes take a reliable update
+// this iteration (gate list).
+__global__ void __launch_bounds__(1024) k_bx_decide(const BoxDesc* boxes, BoxSt* st, BatchCtl* ctl, BxList gate)
+{
+  const int b = threadIdx.x;
+  const int nbox = ctl->nbox;
+  const int k = ctl->k + 1;
+  bool f = false;
+  if (b < nbox && st[b].open) {
+    BoxSt& s = st[b];
+    s.since += 1;
+    const double t = s.rr_new;
+    const bool ready = t < ctl->delta2 * s.rr_upd || t <= s.tol_abs * s.tol_abs;
+    s.gate = !s.brk && (ready || s.since >= ctl->refine_k || k >= ctl->max_iter);
+    f = s.gate;
+  }
+  __syncthreads();
+  bx_build_list(boxes, nbox, f, gate);
+}
+
+// Mixed solver, end of iteration: finish boxes whose true residual meets
+// the tolerance, restart the recursion of the others from it, rebuild the
+// open list.
+__global__ void __launch_bounds__(1024)
+    k_bx_after(const BoxDesc* boxes, BoxSt* st, BatchCtl* ctl, BxList open,
+               cudaGraphConditionalHandle h, int in_graph)
+{
+  const int b = threadIdx.x;
+  const int nbox = ctl->nbox;
+  const int k = ctl->k + 1;
+  bool f = false;
+  __shared__ int any_gate, any_brk;
+  if (b == 0) {
+    any_gate = 0;
+    any_brk = 0;
+  }
+  __syncthreads();
+  if (b < nbox && st[b].open) {
+    BoxSt& s = st[b];
+    if (s.brk) {
+      s.open = 0;
+      s.iters = k;
+      atomicOr(&any_brk, 1);
+    } else if (s.gate) {
+      atomicOr(&any_gate, 1);
+      s.normr = sqrt(s.rr_true);
+      s.since = 0;
+      if (s.normr <= s.tol_abs) {
+        s.open = 0;
+        s.iters = k;
+      } else {
+        s.beta = s.rr_true / s.rr;
+        s.rr = s.rr_true;
+        s.rr_upd = s.rr_true;
+      }
+      s.gate = 0;
+    } else {
+      s.beta = s.rr_new / s.rr;
+      s.rr = s.rr_new;
+    }
+    if (s.open && k >= ctl->max_iter) {
+      s.open = 0;
+      s.iters = k;
+    }
+    f = s.open;
+  }
+  __syncthreads();
+  bx_build_list(boxes, nbox, f, open);
+  if (b == 0) {
+    ctl->k = k;
+    ctl->first = 0;
+    if (any_gate) ctl->updates += 1;
+    if (any_brk) ctl->status = MFE_BREAKDOWN;
+    ctl->cont = *open.count > 0;
+    if (in_graph) cudaGraphSetConditional(h, ctl->cont ? 1u : 0u);
+  }
+}
+
+// FP64 solver, end of iteration k: the reference's loop test per box
+// (iteration k+1 runs while k+1 <= max_iter and normr > tol, normr being
+// |r| at the top of iteration k).
+__global__ void __launch_bounds__(1024)
+    k_bx_after64(const BoxDesc* boxes, BoxSt* st, BatchCtl* ctl, BxList open,
+                 cudaGraphConditionalHandle h, int in_graph)
+{
+  const int b = threadIdx.x;
+  const int nbox = ctl->nbox;
+  const int k = ctl->k + 1;
+  bool f = false;
+  __shared__ int any_brk;
+  if (b == 0) any_brk = 0;
+  __syncthreads();
+  if (b < nbox && st[b].open) {
+    BoxSt& s = st[b];
+    if (s.brk) {
+      s.open = 0;
+      s.iters = k;
+      atomicOr(&any_brk, 1);
+    } else if (k + 1 <= ctl->max_iter && s.normr > s.tol_abs) {
+      s.beta = s.rr_new / s.rr;
+      s.rr = s.rr_new;
+      s.normr = sqrt(s.rr_new);
+    } else {
+      s.open = 0;
+      s.iters = k;
+    }
+    f = s.open;
+  }
+  __syncthreads();
+  bx_build_list(boxes, nbox, f, open);
+  if (b == 0) {
+    ctl->k = k;
+    ctl->first = 0;
+    if (any_brk) ctl->status = MFE_BREAKDOWN;
+    ctl->cont = *open.count > 0;
+    if (in_graph) cudaGraphSetConditional(h, ctl->cont ? 1u : 0u);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T, int MODE>
+int bx_grid(mfe_ctx* ctx)
+{
+  static int per_sm[64] = {};
+  const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
+  if (per_sm[dev] == 0) {
+    cudaFuncSetAttribute(k_bx_spmv<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)bx_smem<T>());
+    int n = 1;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bx_spmv<T, MODE>, BxShape<T>::rows + 32,
+                                                  bx_smem<T>());
+    per_sm[dev] = std::max(n, 1);
+  }
+  return ctx->sm_count * per_sm[dev];
+}
+
+struct BatchBufs {
+  BoxDesc* boxes;
+  BoxSt* st;
+  BatchCtl* ctl;
+  BxList open, gate, all;
+  double* slots;
+  double* chunk_part;
+  double *vals64, *b, *x;
+  float* vals32;
+  void *r, *p, *Ap;  // FP32 (mixed) or FP64
+  float* x32;
+  int nbox, grid32, grid64;
+};
+
+template <typename T, int MODE>
+mfe_status bx_spmv(mfe_ctx* ctx, const BatchBufs& W, const BxList& L, const T* vals, const T* x,
+                   T* y, const double* b, float* y32, int grid)
+{
+  BxSpmvParams<T> P;
+  P.boxes = W.boxes;
+  P.st = W.st;
+  P.ids = L.ids;
+  P.tpre = sizeof(T) == 4 ? L.tpre32 : L.tpre64;
+  P.count = L.count;
+  P.vals = vals;
+  P.x = x;
+  P.y = y;
+  P.b = b;
+  P.y32 = y32;
+  P.slots = W.slots;
+  P.err = &W.ctl->err;
+  k_bx_spmv<T, MODE><<<grid, BxShape<T>::rows + 32, bx_smem<T>(), ctx->stream>>>(P);
+  return check_launch(ctx, "k_bx_spmv");
+}
+
+BxVecParams bx_vec(const BatchBufs& W, const BxList& L)
+{
+  return BxVecParams{W.boxes, W.st, W.ctl, L.ids, L.cpre, L.count, W.chunk_part};
+}
+
+int bx_vgrid(mfe_ctx* ctx) { return ctx->sm_count * 8; }
+
+mfe_status bx_iter_mixed(mfe_ctx* ctx, const BatchBufs& W, cudaGraphConditionalHandle h, int in_graph)
+{
+  float* r = static_cast<float*>(W.r);
+  float* p = static_cast<float*>(W.p);
+  float* Ap = static_cast<float*>(W.Ap);
+  const int vg = bx_vgrid(ctx);
+  k_bx_p<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), r, p);
+  MFE_TRY(check_launch(ctx, "k_bx_p"));
+  MFE_TRY((bx_spmv<float, BX_DOT>(ctx, W, W.open, W.vals32, p, Ap, nullptr, nullptr, W.grid32)));
+  k_bx_update<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), W.x32, r, p, Ap);
+  MFE_TRY(check_launch(ctx, "k_bx_update"));
+  k_bx_decide<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.gate);
+  MFE_TRY(check_launch(ctx, "k_bx_decide"));
+  k_bx_xupdate<<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.gate), W.x, W.x32);
+  MFE_TRY(check_launch(ctx, "k_bx_xupdate"));
+  MFE_TRY((bx_spmv<double, BX_RESID>(ctx, W, W.gate, W.vals64, W.x, nullptr, W.b, r, W.grid64)));
+  k_bx_after<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.open, h, in_graph);
+  return check_launch(ctx, "k_bx_after");
+}
+
+mfe_status bx_iter_f64(mfe_ctx* ctx, const BatchBufs& W, cudaGraphConditionalHandle h, int in_graph)
+{
+  double* r = static_cast<double*>(W.r);
+  double* p = static_cast<double*>(W.p);
+  double* Ap = static_cast<double*>(W.Ap);
+  const int vg = bx_vgrid(ctx);
+  k_bx_p<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), r, p);
+  MFE_TRY(check_launch(ctx, "k_bx_p"));
+  MFE_TRY((bx_spmv<double, BX_DOT>(ctx, W, W.open, W.vals64, p, Ap, nullptr, nullptr, W.grid64)));
+  k_bx_update<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), W.x, r, p, Ap);
+  MFE_TRY(check_launch(ctx, "k_bx_update"));
+  k_bx_after64<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.open, h, in_graph);
+  return check_launch(ctx, "k_bx_after64");
+}
+
+int64_t pad4(int64_t v) { return (v + kBxPad - 1) / kBxPad * kBxPad; }
+
+mfe_status bx_list_alloc(mfe_ctx* ctx, const char* name, int nbox, BxList* L)
+{
+  const size_t per = (size_t)nbox + 2;
+  int* a = static_cast<int*>(workspace(ctx, name, sizeof(int) * (4 * per + 1)));
+  if (!a) return fail(ctx, MFE_OOM, "batch list allocation failed");
+  L->ids = a;
+  L->tpre32 = a + per;
+  L->tpre64 = a + 2 * per;
+  L->cpre = a + 3 * per;
+  L->count = a + 4 * per;
+  return MFE_OK;
+}
+
+}  // namespace
+
+mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const mfe_cg_opts* o,
+                             double* x_out, mfe_cg_result* results)
+{
+  if (nbox < 1 || nbox > kBxMaxBoxes) return fail(ctx, MFE_BAD_ARG, "nbox must be 1..1024");
+  if (o->precision != MFE_PREC_MIXED && o->precision != MFE_PREC_F64)
+    return fail(ctx, MFE_BAD_ARG, "unknown precision");
+  const bool mixed = o->precision == MFE_PREC_MIXED;
+  constexpr int R32 = BxShape<float>::rows, R64 = BxShape<double>::rows;
+
+  // ---- plan: slices, tiles, chunks ----
+  std::vector<BoxDesc> hd(nbox);
+  int64_t rows_tot = 0, nnz_tot = 0, max_nnz = 0, max_rows = 0;
+  int chunks_tot = 0;
+  for (int i = 0; i < nbox; ++i) {
+    const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
+    int64_t n = 0, nnz = 0;
+    if (mfe_box_dims(nx, ny, nz, &n, &nnz) != MFE_OK || nnz > INT32_MAX - 64)
+      return fail(ctx, MFE_BAD_ARG, "bad box dimensions in the batch");
+    BoxDesc& d = hd[i];
+    d.Nx = nx + 1;
+    d.Ny = ny + 1;
+    d.Nz = nz + 1;
+    d.NxNy = d.Nx * d.Ny;
+    d.n = (int)n;
+    d.ntiles32 = (int)ceil_div(n, R32);
+    d.ntiles64 = (int)ceil_div(n, R64);
+    d.nchunks = (int)ceil_div(n, kBxChunk);
+    d.chunk_base = chunks_tot;
+    d.row_base = rows_tot;
+    d.nnz_base = nnz_tot;
+    chunks_tot += d.nchunks;
+    rows_tot += pad4(n);
+    nnz_tot += pad4(nnz);
+    max_nnz = std::max(max_nnz, nnz);
+    max_rows = std::max(max_rows, n);
+  }
+
+  // ---- device buffers ----
+  BatchBufs W{};
+  W.nbox = nbox;
+  W.grid32 = bx_grid<float, BX_DOT>(ctx);
+  W.grid64 = std::max(bx_grid<double, BX_DOT>(ctx), bx_grid<double, BX_RESID>(ctx));
+  const int G = std::max(W.grid32, W.grid64);
+  const size_t vb = (mixed ? sizeof(float) : sizeof(double)) * (size_t)(rows_tot + 8);
+  W.boxes = static_cast<BoxDesc*>(workspace(ctx, "batch.boxes", sizeof(BoxDesc) * nbox));
+  W.st = static_cast<BoxSt*>(workspace(ctx, "batch.state", sizeof(BoxSt) * nbox));
+  W.ctl = static_cast<BatchCtl*>(workspace(ctx, "batch.ctl", sizeof(BatchCtl)));
+  W.slots = static_cast<double*>(workspace(ctx, "batch.slots", sizeof(double) * (size_t)nbox * G * 8));
+  W.chunk_part = static_cast<double*>(workspace(ctx, "batch.chunks", sizeof(double) * (size_t)chunks_tot));
+  W.vals64 = static_cast<double*>(workspace(ctx, "batch.vals64", sizeof(double) * (size_t)(nnz_tot + 8)));
+  W.b = static_cast<double*>(workspace(ctx, "batch.b", sizeof(double) * (size_t)(rows_tot + 8)));
+  W.x = static_cast<double*>(workspace(ctx, "batch.x", sizeof(double) * (size_t)(rows_tot + 8)));
+  W.r = workspace(ctx, "batch.r", vb);
+  W.p = workspace(ctx, "batch.p", vb);
+  W.Ap = workspace(ctx, "batch.Ap", vb);
+  W.vals32 = mixed ? static_cast<float*>(workspace(ctx, "batch.vals32", sizeof(float) * (size_t)(nnz_tot + 8)))
+                   : nullptr;
+  W.x32 = mixed ? static_cast<float*>(workspace(ctx, "batch.x32", sizeof(float) * (size_t)(rows_tot + 8)))
+                : nullptr;
+  int32_t* ro = static_cast<int32_t*>(workspace(ctx, "batch.ro", sizeof(int32_t) * (size_t)(max_rows + 1)));
+  int32_t* cols = static_cast<int32_t*>(workspace(ctx, "batch.cols", sizeof(int32_t) * (size_t)(max_nnz + 4)));
+  if (!W.boxes || !W.st || !W.ctl || !W.slots || !W.chunk_part || !W.vals64 || !W.b || !W.x ||
+      !W.r || !W.p || !W.Ap || (mixed && (!W.vals32 || !W.x32)) || !ro || !cols)
+    return fail(ctx, MFE_OOM, "batch workspace allocation failed");
+  MFE_TRY(bx_list_alloc(ctx, "batch.list.open", nbox, &W.open));
+  MFE_TRY(bx_list_alloc(ctx, "batch.list.gate", nbox, &W.gate));
+  MFE_TRY(bx_list_alloc(ctx, "batch.list.all", nbox, &W.all));
+
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.boxes, hd.data(), sizeof(BoxDesc) * nbox, cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.vals64, 0, sizeof(double) * (size_t)(nnz_tot + 8), ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.b, 0, sizeof(double) * (size_t)(rows_tot + 8), ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.x, 0, sizeof(double) * (size_t)(rows_tot + 8), ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.r, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.p, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.Ap, 0, vb, ctx->stream));
+  if (mixed) MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.x32, 0, sizeof(float) * (size_t)(rows_tot + 8), ctx->stream));
+
+  // ---- assembly, box by box (structure into scratch, values into the slice) ----
+  for (int i = 0; i < nbox; ++i) {
+    const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
+    MFE_TRY(launch_structure(ctx, nx, ny, nz, ro, cols));
+    MFE_TRY(launch_assemble(ctx, nx, ny, nz, nullptr, ro, W.vals64 + hd[i].nnz_base,
+                            W.b + hd[i].row_base, 1));
+  }
+  if (mixed) MFE_TRY(launch_convert_f32(ctx, W.vals64, W.vals32, nnz_tot + 8));
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+
+  // ---- initial state, r = b - A x0 over all boxes ----
+  std::vector<BoxSt> hs(nbox);
+  for (int i = 0; i < nbox; ++i) {
+    memset(&hs[i], 0, sizeof(BoxSt));
+    hs[i].tol_abs = o->tol;
+  }
+  BatchCtl hc{};
+  hc.nbox = nbox;
+  hc.max_iter = std::max(0, o->max_iter);
+  hc.refine_k = o->refine_k > 0 ? o->refine_k : 50;
+  hc.first = 1;
+  hc.tol_mode = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;
+  hc.delta2 = 1e-2;
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.st, hs.data(), sizeof(BoxSt) * nbox, cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.ctl, &hc, sizeof(BatchCtl), cudaMemcpyHostToDevice, ctx->stream));
+  // list of all boxes (host-built, then copied)
+  {
+    std::vector<int> h(4 * ((size_t)nbox + 2) + 1, 0);
+    const size_t per = (size_t)nbox + 2;
+    int t32 = 0, t64 = 0, ch = 0;
+    for (int i = 0; i < nbox; ++i) {
+      h[i] = i;
+      h[per + i] = t32;
+      h[2 * per + i] = t64;
+      h[3 * per + i] = ch;
+      t32 += hd[i].ntiles32;
+      t64 += hd[i].ntiles64;
+      ch += hd[i].nchunks;
+    }
+    h[per + nbox] = t32;
+    h[2 * per + nbox] = t64;
+    h[3 * per + nbox] = ch;
+    h[4 * per] = nbox;
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.all.ids, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice,
+                                      ctx->stream));
+    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // h goes out of scope
+  }
+  if (mixed)
+    MFE_TRY((bx_spmv<double, BX_RESID>(ctx, W, W.all, W.vals64, W.x, nullptr, W.b,
+                                        static_cast<float*>(W.r), W.grid64)));
+  else
+    MFE_TRY((bx_spmv<double, BX_RESID>(ctx, W, W.all, W.vals64, W.x, static_cast<double*>(W.r),
+                                        W.b, nullptr, W.grid64)));
+  k_bx_init<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.open);
+  MFE_TRY(check_launch(ctx, "k_bx_init"));
+  cudaEvent_t ev_solve0 = nullptr, ev_solve1 = nullptr;
+  MFE_CUDA_TRY(ctx, cudaEventCreate(&ev_solve0));
+  MFE_CUDA_TRY(ctx, cudaEventCreate(&ev_solve1));
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ev_solve0, ctx->stream));
+
+  // ---- iterations ----
+  auto body = [&](cudaGraphConditionalHandle h, int in_graph) -> mfe_status {
+    return mixed ? bx_iter_mixed(ctx, W, h, in_graph) : bx_iter_f64(ctx, W, h, in_graph);
+  };
+  mfe_status st = MFE_OK;
+  if (getenv("MFE_CG_EAGER") != nullptr) {
+    BatchCtl* hctl = static_cast<BatchCtl*>(host_scratch(ctx, sizeof(BatchCtl)));
+    if (!hctl) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
+    for (;;) {
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hctl, W.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!hctl->cont) break;
+      MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
+    }
+  } else {
+    cudaStream_t run_stream = ctx->stream, s = ctx->own_stream;
+    cudaGraph_t g = nullptr;
+    cudaGraphExec_t ex = nullptr;
+    cudaGraphConditionalHandle h = 0;
+    cudaError_t e = cudaGraphCreate(&g, 0);
+    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+    if (e == cudaSuccess) {
+      ctx->stream = s;
+      e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        k_bx_begin<<<1, 1, 0, s>>>(W.ctl, h);
+        e = cudaStreamEndCapture(s, &g);
+      }
+      cudaGraphNode_t nodes[4];
+      size_t nn = 4;
+      if (e == cudaSuccess) e = cudaGraphGetNodes(g, nodes, &nn);
+      alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+      memset(cp_buf, 0, sizeof(cp_buf));
+      cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+      cp->type = cudaGraphNodeTypeConditional;
+      cp->conditional.handle = h;
+      cp->conditional.type = cudaGraphCondTypeWhile;
+      cp->conditional.size = 1;
+      cudaGraphNode_t cnode;
+      if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
+      if (e == cudaSuccess) {
+        cudaGraph_t bg = cp->conditional.phGraph_out[0];
+        e = cudaStreamBeginCaptureToGraph(s, bg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        if (e == cudaSuccess) {
+          st = body(h, 1);
+          cudaGraph_t tmp;
+          const cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+          if (e == cudaSuccess) e = e2;
+        }
+      }
+      ctx->stream = run_stream;
+      if (e == cudaSuccess && st == MFE_OK) e = cudaGraphInstantiate(&ex, g, 0);
+      if (e == cudaSuccess && st == MFE_OK) e = cudaGraphLaunch(ex, ctx->stream);
+    }
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    if (st != MFE_OK) return st;
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched CG graph");
+  }
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ev_solve1, ctx->stream));
+
+  // ---- results ----
+  int64_t out = 0;
+  for (int i = 0; i < nbox; ++i) {
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(x_out + out, W.x + hd[i].row_base, sizeof(double) * hd[i].n,
+                                      cudaMemcpyDeviceToDevice, ctx->stream));
+    out += hd[i].n;
+  }
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), W.st, sizeof(BoxSt) * nbox, cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&hc, W.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  float ms_asm = 0.f, ms_solve = 0.f;
+  cudaEventElapsedTime(&ms_asm, ctx->ev0, ctx->ev1);
+  cudaEventElapsedTime(&ms_solve, ev_solve0, ev_solve1);
+  cudaEventDestroy(ev_solve0);
+  cudaEventDestroy(ev_solve1);
+  if (hc.err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during the batched solve");
+  mfe_status worst = MFE_OK;
+  for (int i = 0; i < nbox; ++i) {
+    const BoxSt& s = hs[i];
+    mfe_cg_result& r = results[i];
+    memset(&r, 0, sizeof(r));
+    r.num_iters = s.open ? hc.k : s.iters;
+    r.normr = s.normr;
+    r.normr0 = s.normr0;
+    r.final_resid = s.normr;
+    r.times[0] = ms_asm * 1e-3;  // assembly of the whole batch
+    r.times[4] = ms_solve * 1e-3;
+    r.refinements = hc.updates;
+    r.status = s.brk ? MFE_BREAKDOWN : (s.normr <= s.tol_abs ? MFE_OK : MFE_MAXITER);
+    if (r.status != MFE_OK && worst == MFE_OK) worst = (mfe_status)r.status;
+  }
+  return worst;
+}
+
+}  // namespace mfe

@@ -104,6 +104,10 @@ mfe_status launch_spmm_box(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void*
 mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64, int nrhs, const double* B, double* X,
                     const mfe_cg_opts* opts, mfe_cg_result* results);
 
+// ---- batched uneven boxes (mfe_batch.cu) ----
+mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const mfe_cg_opts* opts,
+                             double* x_out, mfe_cg_result* results);
+
 // ---- BLAS-1 and CG (mfe_cg.cu) ----
 mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
                       double* dev_out);
