@@ -60,7 +60,9 @@ struct BoxDesc {
   int n;
   int ntiles32, ntiles64;  // SpMV tiles at the FP32 and FP64 shapes
   int nchunks, chunk_base;
-  int64_t row_base, nnz_base;
+  int64_t row_base;        // first row in the vectors (ghost zones either side)
+  int64_t nnz_base;        // first value in the compressed FP64 values
+  int64_t ell_base;        // first value in the padded FP32 values (27 per row)
 };
 
 struct BoxSt {
@@ -139,56 +141,76 @@ struct BxSpmvParams {
   unsigned* err;
 };
 
-// Consumer warp cw of this CTA is done with box b (list position q): its
-// partial goes to the box's slot; the last of the box's warps sums the
-// slots of every CTA that worked on the box, in CTA order, and forms the
-// box's scalar.
-template <typename T, int MODE, int C>
-__device__ void bx_flush(const BxSpmvParams<T>& P, int b, int q, int cw, double dacc)
+// Tiles are split into contiguous ranges, one per CTA: CTA c takes tiles
+// [bx_start(c), bx_start(c + 1)) of the launch's tile list.
+__device__ __forceinline__ int bx_start(int c, int total, int G)
+{
+  return (int)(((int64_t)c * total) / G);
+}
+
+// Consumer warp cw of this CTA is done with box b (tiles [A, E) of the
+// list): its partial goes to slot (b, CTA, cw); the last of the box's warps
+// sums the slots of the CTAs whose ranges meet [A, E), in CTA order, and
+// forms the box's scalar.
+template <int MODE, int C>
+__device__ void bx_flush(BoxSt* st, double* slots, int b, int A, int E, int total, int cw,
+                         double dacc)
 {
   const int lane = threadIdx.x & 31;
   const double v = warp_sum(dacc);
   const int G = gridDim.x;
-  const int A = __ldg(&P.tpre[q]);
-  const int nt = __ldg(&P.tpre[q + 1]) - A;
-  const unsigned expected = (unsigned)min(nt, G) * C;
-  double* slot = P.slots + (size_t)b * G * C;
+  // first and last CTA whose range meets [A, E): bx_start(c) <= A < bx_start(c+1)
+  const int c0 = (int)min((int64_t)(G - 1), ((int64_t)(A + 1) * G + total - 1) / total - 1);
+  const int c1 = (int)min((int64_t)(G - 1), ((int64_t)E * G + total - 1) / total - 1);
+  unsigned ranges = 0;  // CTAs in c0..c1 with a non-empty range
+  if (total >= G) {
+    ranges = (unsigned)(c1 - c0 + 1);
+  } else {
+    for (int c = c0 + lane; c <= c1; c += 32)
+      ranges += bx_start(c + 1, total, G) > bx_start(c, total, G) ? 1u : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) ranges += __shfl_xor_sync(0xffffffffu, ranges, o);
+  }
+  double* slot = slots + (size_t)b * G * C;
   unsigned old = 0;
   if (lane == 0) {
     slot[(size_t)blockIdx.x * C + cw] = v;
     __threadfence();
-    old = atomicAdd(&P.st[b].cnt_mv, 1u);
+    old = atomicAdd(&st[b].cnt_mv, 1u);
   }
   old = __shfl_sync(0xffffffffu, old, 0);
-  if (old != expected - 1) return;
+  if (old != ranges * C - 1) return;
   __threadfence();
-  double s = 0.0;
-  const int a0 = A % G;
-  for (int c = lane; c < G; c += 32) {
-    const bool visited = nt >= G || ((c - a0 + G) % G) < nt;
-    if (!visited) continue;
+  double sacc = 0.0;
+  for (int c = c0 + lane; c <= c1; c += 32) {
+    if (bx_start(c + 1, total, G) <= bx_start(c, total, G)) continue;
 #pragma unroll
-    for (int w = 0; w < C; ++w) s += __ldcg(&slot[(size_t)c * C + w]);
+    for (int w = 0; w < C; ++w) sacc += __ldcg(&slot[(size_t)c * C + w]);
   }
-  s = warp_sum(s);
+  sacc = warp_sum(sacc);
   if (lane == 0) {
-    BoxSt& bs = P.st[b];
+    BoxSt& bs = st[b];
     if (MODE == BX_DOT) {
-      bs.pAp = s;
-      if (s > 0.0) {
-        bs.alpha = bs.rr / s;
+      bs.pAp = sacc;
+      if (sacc > 0.0) {
+        bs.alpha = bs.rr / sacc;
       } else {
         bs.alpha = 0.0;
         bs.brk = 1;
       }
     } else {
-      bs.rr_true = s;
+      bs.rr_true = sacc;
     }
     bs.cnt_mv = 0u;
   }
 }
 
-template <typename T, int MODE>
+// Box SpMV over the launch's tile list.  ELL: FP32 values in the padded
+// 27-per-row layout (zeros for missing neighbours), so every row runs the
+// unmasked 27-term code; otherwise the compressed CSR values with masked
+// slots for boundary rows.  x has ghost zones of zeros around each box, so
+// the nine segments are never clamped.
+template <typename T, int MODE, bool ELL>
 __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<T> P)
 {
   constexpr int ROWS = BxShape<T>::rows, S = BxShape<T>::stages, C = ROWS / 32;
@@ -205,6 +227,9 @@ __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<
   const int cnt = *P.count;
   if (cnt == 0) return;
   const int total = __ldg(&P.tpre[cnt]);
+  const int t_begin = bx_start(blockIdx.x, total, gridDim.x);
+  const int t_end = bx_start(blockIdx.x + 1, total, gridDim.x);
+  if (t_begin >= t_end) return;
   if (threadIdx.x == 0) {
     for (int s = 0; s < S; ++s) {
       mbar_init(&full[s], 1);
@@ -216,35 +241,44 @@ __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<
   if (warp == 0) {
     if (lane == 0) {
       bool ok = true;
-      int it = 0, q = -1, b = -1;
+      int it = 0, q = -1;
       BoxDesc d{};
-      for (int i = blockIdx.x; i < total; i += gridDim.x, ++it) {
+      int A = 0;
+      for (int i = t_begin; i < t_end; ++i, ++it) {
         const int s = it % S;
         if (it >= S) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / S) - 1) & 1));
         if (!ok) break;
         const int nq = bx_advance(P.tpre, cnt, q, i);
         if (nq != q) {
           q = nq;
-          b = __ldg(&P.ids[q]);
-          d = P.boxes[b];
+          d = P.boxes[__ldg(&P.ids[q])];
+          A = __ldg(&P.tpre[q]);
         }
-        const int lt = i - __ldg(&P.tpre[q]);
+        const int lt = i - A;
         T* sv = st0 + (size_t)s * stage_elems;
         T* sx = sv + capv;
         const int r0 = lt * ROWS, r1 = min(d.n, r0 + ROWS);
-        const int a = (int)row_offset_of32(r0, d.Nx, d.Ny, d.Nz, d.NxNy);
-        const int e = (int)row_offset_of32(r1, d.Nx, d.Ny, d.Nz, d.NxNy);
-        // ranges round outwards to the copy granule inside the box's padded slice
-        const int av = a & ~(VA - 1), bv = (e + VA - 1) & ~(VA - 1);
+        int av, bv;
+        const T* vsrc;
+        if (ELL) {
+          av = 27 * r0;
+          bv = (27 * r1 + VA - 1) & ~(VA - 1);
+          vsrc = P.vals + d.ell_base;
+        } else {
+          const int a = (int)row_offset_of32(r0, d.Nx, d.Ny, d.Nz, d.NxNy);
+          const int e = (int)row_offset_of32(r1, d.Nx, d.Ny, d.Nz, d.NxNy);
+          av = a & ~(VA - 1);
+          bv = (e + VA - 1) & ~(VA - 1);
+          vsrc = P.vals + d.nnz_base;
+        }
         bool fits = bv - av <= capv;
         int xlo[9], xhi[9];
 #pragma unroll
         for (int j = 0; j < 9; ++j) {
           const int off = (j / 3 - 1) * d.NxNy + (j % 3 - 1) * d.Nx;
-          const int lo = min(max(r0 + off - 1, 0), d.n);
-          const int hi = max(min(r1 + off + 1, d.n), lo);
-          xlo[j] = lo & ~(VA - 1);
-          xhi[j] = (hi + VA - 1) & ~(VA - 1);
+          // inside the box's ghost zones: [-ghost, n + ghost)
+          xlo[j] = (r0 + off - 1) & ~(VA - 1);
+          xhi[j] = (r1 + off + 1 + VA - 1) & ~(VA - 1);
           fits = fits && xhi[j] - xlo[j] <= capx;
         }
         if (!fits) {
@@ -263,12 +297,11 @@ __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<
           bytes += (unsigned)((xhi[j] - xlo[j]) * sizeof(T));
         }
         mbar_arrive_expect_tx(&full[s], bytes);
-        if (bv > av) bulk_g2s(sv, P.vals + d.nnz_base + av, (unsigned)((bv - av) * sizeof(T)), &full[s]);
+        bulk_g2s(sv, vsrc + av, (unsigned)((bv - av) * sizeof(T)), &full[s]);
 #pragma unroll
         for (int j = 0; j < 9; ++j)
-          if (xhi[j] > xlo[j])
-            bulk_g2s(sx + (size_t)j * capx, P.x + d.row_base + xlo[j],
-                     (unsigned)((xhi[j] - xlo[j]) * sizeof(T)), &full[s]);
+          bulk_g2s(sx + (size_t)j * capx, P.x + d.row_base + xlo[j],
+                   (unsigned)((xhi[j] - xlo[j]) * sizeof(T)), &full[s]);
       }
       if (!ok) {
         atomicOr(P.err, ERR_WAIT_TIMEOUT);
@@ -279,25 +312,36 @@ __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<
   } else {
     const int cw = warp - 1;
     const int lr = cw * 32 + lane;
-    double dacc = 0.0;
-    int it = 0, q = -1, b = -1;
+    double dacc = 0.0;  // RESID, and DOT of FP64 operands
+    DFAcc facc;         // DOT of FP32 operands
+    int it = 0, q = -1, b = -1, A = 0, E = 0;
     BoxDesc d{};
-    for (int i = blockIdx.x; i < total; i += gridDim.x, ++it) {
+    for (int i = t_begin; i < t_end; ++i, ++it) {
       const int s = it % S;
       const int nq = bx_advance(P.tpre, cnt, q, i);
       if (nq != q) {
-        if (q >= 0) bx_flush<T, MODE, C>(P, b, q, cw, dacc);
+        if (q >= 0) bx_flush<MODE, C>(P.st, P.slots, b, A, E, total, cw, dacc + facc.value());
         dacc = 0.0;
+        facc = DFAcc{};
         q = nq;
         b = __ldg(&P.ids[q]);
         d = P.boxes[b];
+        A = __ldg(&P.tpre[q]);
+        E = __ldg(&P.tpre[q + 1]);
       }
-      const int lt = i - __ldg(&P.tpre[q]);
-      const int r = lt * ROWS + lr;
+      const int r = (i - A) * ROWS + lr;
       const bool active = r < d.n;
-      const int rr = active ? r : d.n - 1;
-      const int iz = rr / d.NxNy, rem = rr - iz * d.NxNy, iy = rem / d.Nx, ix = rem - iy * d.Nx;
-      const int roff = (int)row_offset(ix, iy, iz, d.Nx, d.Ny, d.Nz);
+      int iz = 0, iy = 0, ix = 0, roff = 0;
+      if (!ELL) {
+        const int rr = active ? r : d.n - 1;
+        iz = rr / d.NxNy;
+        const int rem = rr - iz * d.NxNy;
+        iy = rem / d.Nx;
+        ix = rem - iy * d.Nx;
+        roff = (int)row_offset(ix, iy, iz, d.Nx, d.Ny, d.Nz);
+      } else {
+        roff = 27 * r;
+      }
       if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
         atomicOr(P.err, ERR_WAIT_TIMEOUT);
         break;
@@ -308,12 +352,14 @@ __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<
         const T* sv = st0 + (size_t)s * stage_elems;
         const T* sx = sv + capv;
         const T* rowv = sv + (roff - s_vbase[s]);
-        const bool vxm = ix > 0, vxp = ix < d.Nx - 1, vym = iy > 0, vyp = iy < d.Ny - 1;
-        const bool vzm = iz > 0, vzp = iz < d.Nz - 1;
         const T* xc = sx + 4 * capx + (r - s_xbase[s][4]);
         xr = xc[0];
         T s0 = T(0), s1 = T(0);
-        if (vxm && vxp && vym && vyp && vzm && vzp) {
+        const bool vxm = ELL || ix > 0, vxp = ELL || ix < d.Nx - 1;
+        const bool vym = ELL || iy > 0, vyp = ELL || iy < d.Ny - 1;
+        const bool vzm = ELL || iz > 0, vzp = ELL || iz < d.Nz - 1;
+        // warps whose rows all have the full 27 columns take the unmasked code
+        if (ELL || __all_sync(__activemask(), vxm && vxp && vym && vyp && vzm && vzp)) {
 #pragma unroll
           for (int j = 0; j < 9; ++j) {
             const int off = (j / 3 - 1) * d.NxNy + (j % 3 - 1) * d.Nx;
@@ -372,17 +418,58 @@ __global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<
           dacc = fma(res, res, dacc);
         } else {
           P.y[g] = sum;
-          dacc = fma(widen(sum), widen(xr), dacc);
+          if constexpr (sizeof(T) == 4)
+            facc.add_product(sum, xr);
+          else
+            dacc = fma(sum, xr, dacc);
         }
       }
     }
-    if (q >= 0) bx_flush<T, MODE, C>(P, b, q, cw, dacc);
+    if (q >= 0) bx_flush<MODE, C>(P.st, P.slots, b, A, E, total, cw, dacc + facc.value());
+  }
+}
+
+// FP32 values of box b in the padded 27-per-row layout (slot k = (dz, dy, dx)
+// in the CSR column order; zero where the neighbour lies outside the box)
+__global__ void k_bx_ell(BoxDesc d, const double* __restrict__ vals64, float* __restrict__ ell)
+{
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < d.n; r += gridDim.x * blockDim.x) {
+    const int iz = r / d.NxNy, rem = r - iz * d.NxNy, iy = rem / d.Nx, ix = rem - iy * d.Nx;
+    int64_t k = d.nnz_base + row_offset(ix, iy, iz, d.Nx, d.Ny, d.Nz);
+    float* out = ell + d.ell_base + (int64_t)27 * r;
+    int slot = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx, ++slot) {
+          const bool in = ix + dx >= 0 && ix + dx < d.Nx && iy + dy >= 0 && iy + dy < d.Ny &&
+                          iz + dz >= 0 && iz + dz < d.Nz;
+          out[slot] = in ? (float)vals64[k++] : 0.0f;
+        }
   }
 }
 
 // ---------------------------------------------------------------------------
 // vector kernels over the chunk list
 // ---------------------------------------------------------------------------
+// 16-byte vectors of the work arrays (chunks start on 16-byte boundaries)
+template <typename V>
+struct BxVec16;
+template <>
+struct BxVec16<float> {
+  using type = float4;
+  static constexpr int n = 4;
+};
+template <>
+struct BxVec16<double> {
+  using type = double2;
+  static constexpr int n = 2;
+};
+template <typename V>
+__device__ __forceinline__ V& bx_comp(typename BxVec16<V>::type& v, int c)
+{
+  return reinterpret_cast<V*>(&v)[c];
+}
+
 struct BxVecParams {
   const BoxDesc* boxes;
   BoxSt* st;
@@ -410,7 +497,22 @@ __global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restri
     const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
     const int len = min(kBxChunk, d.n - lc * kBxChunk);
     const V beta = (V)Q.st[b].beta;
-    for (int k = threadIdx.x; k < len; k += kBxVT) {
+    using VV = typename BxVec16<V>::type;
+    constexpr int VW = BxVec16<V>::n;
+    const VV* r4 = reinterpret_cast<const VV*>(r + g0);
+    VV* p4 = reinterpret_cast<VV*>(p + g0);
+    for (int k = threadIdx.x; k < len / VW; k += kBxVT) {
+      const VV rv = r4[k];
+      VV pv = rv;
+      if (!first) {
+        pv = p4[k];
+#pragma unroll
+        for (int c = 0; c < VW; ++c)
+          bx_comp<V>(pv, c) = fma(beta, bx_comp<V>(pv, c), bx_comp<V>(const_cast<VV&>(rv), c));
+      }
+      p4[k] = pv;
+    }
+    for (int k = len / VW * VW + threadIdx.x; k < len; k += kBxVT) {
       const int64_t g = g0 + k;
       p[g] = first ? r[g] : fma(beta, p[g], r[g]);
     }
@@ -440,7 +542,29 @@ __global__ void __launch_bounds__(kBxVT)
     const V alpha = (V)Q.st[b].alpha;
     double acc = 0.0;
     DFAcc facc;
-    for (int k = threadIdx.x; k < len; k += kBxVT) {
+    using VV = typename BxVec16<V>::type;
+    constexpr int VW = BxVec16<V>::n;
+    VV* x4 = reinterpret_cast<VV*>(x + g0);
+    VV* r4 = reinterpret_cast<VV*>(r + g0);
+    const VV* p4 = reinterpret_cast<const VV*>(p + g0);
+    const VV* a4 = reinterpret_cast<const VV*>(Ap + g0);
+    for (int k = threadIdx.x; k < len / VW; k += kBxVT) {
+      VV xv = x4[k], rv = r4[k];
+      VV pv = p4[k], av = a4[k];
+#pragma unroll
+      for (int c = 0; c < VW; ++c) {
+        bx_comp<V>(xv, c) = fma(alpha, bx_comp<V>(pv, c), bx_comp<V>(xv, c));
+        const V rn = fma(-alpha, bx_comp<V>(av, c), bx_comp<V>(rv, c));
+        bx_comp<V>(rv, c) = rn;
+        if constexpr (sizeof(V) == 4)
+          facc.add_product(rn, rn);
+        else
+          acc = fma(rn, rn, acc);
+      }
+      x4[k] = xv;
+      r4[k] = rv;
+    }
+    for (int k = len / VW * VW + threadIdx.x; k < len; k += kBxVT) {
       const int64_t g = g0 + k;
       x[g] = fma(alpha, p[g], x[g]);
       const V rn = fma(-alpha, Ap[g], r[g]);
@@ -704,17 +828,24 @@ __global__ void __launch_bounds__(1024)
 // ---------------------------------------------------------------------------
 namespace {
 
+// float SpMVs read the padded 27-per-row values, double ones the compressed CSR
+template <typename T>
+constexpr bool bx_ell()
+{
+  return sizeof(T) == 4;
+}
+
 template <typename T, int MODE>
 int bx_grid(mfe_ctx* ctx)
 {
   static int per_sm[64] = {};
   const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
   if (per_sm[dev] == 0) {
-    cudaFuncSetAttribute(k_bx_spmv<T, MODE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncSetAttribute(k_bx_spmv<T, MODE, bx_ell<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)bx_smem<T>());
     int n = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bx_spmv<T, MODE>, BxShape<T>::rows + 32,
-                                                  bx_smem<T>());
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bx_spmv<T, MODE, bx_ell<T>()>,
+                                                  BxShape<T>::rows + 32, bx_smem<T>());
     per_sm[dev] = std::max(n, 1);
   }
   return ctx->sm_count * per_sm[dev];
@@ -728,7 +859,7 @@ struct BatchBufs {
   double* slots;
   double* chunk_part;
   double *vals64, *b, *x;
-  float* vals32;
+  float* ell32;  // padded 27-per-row FP32 values (mixed solver)
   void *r, *p, *Ap;  // FP32 (mixed) or FP64
   float* x32;
   int nbox, grid32, grid64;
@@ -751,7 +882,7 @@ mfe_status bx_spmv(mfe_ctx* ctx, const BatchBufs& W, const BxList& L, const T* v
   P.y32 = y32;
   P.slots = W.slots;
   P.err = &W.ctl->err;
-  k_bx_spmv<T, MODE><<<grid, BxShape<T>::rows + 32, bx_smem<T>(), ctx->stream>>>(P);
+  k_bx_spmv<T, MODE, bx_ell<T>()><<<grid, BxShape<T>::rows + 32, bx_smem<T>(), ctx->stream>>>(P);
   return check_launch(ctx, "k_bx_spmv");
 }
 
@@ -770,7 +901,7 @@ mfe_status bx_iter_mixed(mfe_ctx* ctx, const BatchBufs& W, cudaGraphConditionalH
   const int vg = bx_vgrid(ctx);
   k_bx_p<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), r, p);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
-  MFE_TRY((bx_spmv<float, BX_DOT>(ctx, W, W.open, W.vals32, p, Ap, nullptr, nullptr, W.grid32)));
+  MFE_TRY((bx_spmv<float, BX_DOT>(ctx, W, W.open, W.ell32, p, Ap, nullptr, nullptr, W.grid32)));
   k_bx_update<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), W.x32, r, p, Ap);
   MFE_TRY(check_launch(ctx, "k_bx_update"));
   k_bx_decide<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.gate);
@@ -825,7 +956,7 @@ mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const 
 
   // ---- plan: slices, tiles, chunks ----
   std::vector<BoxDesc> hd(nbox);
-  int64_t rows_tot = 0, nnz_tot = 0, max_nnz = 0, max_rows = 0;
+  int64_t rows_tot = 0, nnz_tot = 0, ell_tot = 0, max_nnz = 0, max_rows = 0;
   int chunks_tot = 0;
   for (int i = 0; i < nbox; ++i) {
     const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
@@ -842,11 +973,16 @@ mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const 
     d.ntiles64 = (int)ceil_div(n, R64);
     d.nchunks = (int)ceil_div(n, kBxChunk);
     d.chunk_base = chunks_tot;
-    d.row_base = rows_tot;
+    // ghost zone: rows a tile's x segments reach outside the box, rounded to
+    // the copy granule
+    const int64_t ghost = pad4((int64_t)d.NxNy + d.Nx + 1 + kBxPad);
+    d.row_base = rows_tot + ghost;
     d.nnz_base = nnz_tot;
+    d.ell_base = ell_tot;
     chunks_tot += d.nchunks;
-    rows_tot += pad4(n);
+    rows_tot += ghost + pad4(n) + ghost;
     nnz_tot += pad4(nnz);
+    ell_tot += pad4(27 * n);
     max_nnz = std::max(max_nnz, nnz);
     max_rows = std::max(max_rows, n);
   }
@@ -869,14 +1005,14 @@ mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const 
   W.r = workspace(ctx, "batch.r", vb);
   W.p = workspace(ctx, "batch.p", vb);
   W.Ap = workspace(ctx, "batch.Ap", vb);
-  W.vals32 = mixed ? static_cast<float*>(workspace(ctx, "batch.vals32", sizeof(float) * (size_t)(nnz_tot + 8)))
-                   : nullptr;
+  W.ell32 = mixed ? static_cast<float*>(workspace(ctx, "batch.ell32", sizeof(float) * (size_t)(ell_tot + 8)))
+                  : nullptr;
   W.x32 = mixed ? static_cast<float*>(workspace(ctx, "batch.x32", sizeof(float) * (size_t)(rows_tot + 8)))
                 : nullptr;
   int32_t* ro = static_cast<int32_t*>(workspace(ctx, "batch.ro", sizeof(int32_t) * (size_t)(max_rows + 1)));
   int32_t* cols = static_cast<int32_t*>(workspace(ctx, "batch.cols", sizeof(int32_t) * (size_t)(max_nnz + 4)));
   if (!W.boxes || !W.st || !W.ctl || !W.slots || !W.chunk_part || !W.vals64 || !W.b || !W.x ||
-      !W.r || !W.p || !W.Ap || (mixed && (!W.vals32 || !W.x32)) || !ro || !cols)
+      !W.r || !W.p || !W.Ap || (mixed && (!W.ell32 || !W.x32)) || !ro || !cols)
     return fail(ctx, MFE_OOM, "batch workspace allocation failed");
   MFE_TRY(bx_list_alloc(ctx, "batch.list.open", nbox, &W.open));
   MFE_TRY(bx_list_alloc(ctx, "batch.list.gate", nbox, &W.gate));
@@ -899,7 +1035,13 @@ mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const 
     MFE_TRY(launch_assemble(ctx, nx, ny, nz, nullptr, ro, W.vals64 + hd[i].nnz_base,
                             W.b + hd[i].row_base, 1));
   }
-  if (mixed) MFE_TRY(launch_convert_f32(ctx, W.vals64, W.vals32, nnz_tot + 8));
+  if (mixed) {
+    for (int i = 0; i < nbox; ++i) {
+      k_bx_ell<<<(unsigned)std::min<int64_t>(ceil_div(hd[i].n, 256), (int64_t)ctx->sm_count * 8), 256, 0,
+                 ctx->stream>>>(hd[i], W.vals64, W.ell32);
+      MFE_TRY(check_launch(ctx, "k_bx_ell"));
+    }
+  }
   MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
 
   // ---- initial state, r = b - A x0 over all boxes ----
