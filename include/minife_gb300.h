@@ -302,14 +302,40 @@ mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X,
 mfe_status mfe_cg_solve_multi(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const double* B,
                               double* X, const mfe_cg_opts* opts, mfe_cg_result* results);
 
-/* Batched uneven boxes: nbox independent miniFE problems (dims[3*i..3*i+2]),
- * each assembled (k = 1, reference BCs) and solved with CG in one persistent
- * launch per iteration block, all boxes advancing together.  x_out (device)
- * receives the concatenated solutions (offsets: prefix sums of the boxes'
- * rows); results: nbox entries (host). */
+/* Batched uneven boxes: nbox (1..1024) independent miniFE problems
+ * (dims[3*i..3*i+2] = nx, ny, nz), each assembled as the reference does
+ * (k = 1, its Dirichlet faces) into one concatenated device store, then
+ * solved with CG, all boxes advancing together: one CUDA graph whose while
+ * loop runs the iterations, each launch walking only the boxes still
+ * iterating.  opts as for mfe_cg_solve (FP64: the reference's CG per box;
+ * MIXED: FP32 SpMV with FP64 reliable updates, each box stopping on its true
+ * FP64 residual).  x_out (device) receives the concatenated solutions (box i
+ * at the prefix sum of the rows of boxes < i); results: nbox entries (host),
+ * times[0] = assembly of the batch, times[4] = the batched solve (s).
+ * mfe_batch_solve_boxes = create + solve + destroy. */
 mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims,
                                  const mfe_cg_opts* opts, double* x_out,
                                  mfe_cg_result* results);
+
+/* The same in steps: create assembles the batch once (owning its device
+ * memory), solve may run any number of times (other tolerances, precision
+ * or launch shape), destroy frees it. */
+typedef struct mfe_batch mfe_batch;
+/* Launch shape of a batched solve (the autotuner's knobs). */
+typedef struct mfe_batch_tuning {
+  int32_t spmv_rows;    /* rows per FP32 SpMV tile: 128 or 256 (default 256) */
+  int32_t spmv_stages;  /* its shared-memory pipeline stages: 2..4 (default 2) */
+  int32_t chunk_rows;   /* rows per vector-kernel chunk: 1024..2^20, multiple of 4 (8192) */
+} mfe_batch_tuning;
+mfe_status mfe_batch_create(mfe_ctx* ctx, int32_t nbox, const int32_t* dims, mfe_batch** out);
+mfe_status mfe_batch_set_tuning(mfe_ctx* ctx, mfe_batch* batch, const mfe_batch_tuning* t);
+/* rows and nonzeros of all boxes, assembly seconds, current launch shape
+ * (any pointer may be NULL). */
+mfe_status mfe_batch_info(const mfe_batch* batch, int64_t* rows, int64_t* nnz,
+                          double* assembly_seconds, mfe_batch_tuning* tuning);
+mfe_status mfe_batch_solve(mfe_ctx* ctx, mfe_batch* batch, const mfe_cg_opts* opts,
+                           double* x_out, mfe_cg_result* results);
+void mfe_batch_destroy(mfe_batch* batch);
 
 #ifdef __cplusplus
 }

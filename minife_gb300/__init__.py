@@ -32,7 +32,7 @@ __all__ = [
     "MiniFEError", "Context", "CSRMatrix", "CGResult", "default_context", "box_dims",
     "generate_matrix_structure", "assemble_FE_data", "impose_dirichlet", "box_bc_rows",
     "build_system", "matvec", "matvec_and_dot", "dot", "waxpby", "fused_waxpby", "cg_solve",
-    "cg_solve_host", "cg_solve_multi", "batch_solve_boxes", "verify_solution",
+    "cg_solve_host", "cg_solve_multi", "Batch", "batch_solve_boxes", "verify_solution",
     "element_gradient", "to_f32", "spmm",
 ]
 
@@ -404,30 +404,82 @@ def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPS
                      r.refinements, None) for r in res]
 
 
+class Batch:
+    """nbox independent miniFE boxes (k = 1, the reference's boundary
+    conditions) assembled once into one device store (mfe_batch_create) and
+    solved together any number of times.  Box i's solution is
+    x[offsets[i]:offsets[i+1]] of the vector solve() returns."""
+
+    def __init__(self, dims, ctx: Context | None = None):
+        self.ctx = ctx or default_context()
+        self.dims = [tuple(int(v) for v in d) for d in dims]
+        self.offsets = [0]
+        for d in self.dims:
+            self.offsets.append(self.offsets[-1] + box_dims(*d)[0])
+        flat = (ctypes.c_int32 * (3 * len(self.dims)))(*[v for d in self.dims for v in d])
+        h = ctypes.c_void_p()
+        self.ctx.check(self.ctx.lib.mfe_batch_create(self.ctx.h, len(self.dims), flat,
+                                                     ctypes.byref(h)), "mfe_batch_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.mfe_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):  # pragma: no cover - interpreter teardown order varies
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def info(self):
+        """(rows, nonzeros, assembly seconds, tuning dict)."""
+        rows, nnz, t = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_double()
+        tu = _abi.MfeBatchTuning()
+        self.ctx.lib.mfe_batch_info(self.h, ctypes.byref(rows), ctypes.byref(nnz),
+                                    ctypes.byref(t), ctypes.byref(tu))
+        return rows.value, nnz.value, t.value, {"spmv_rows": tu.spmv_rows,
+                                                "spmv_stages": tu.spmv_stages,
+                                                "chunk_rows": tu.chunk_rows}
+
+    def set_tuning(self, spmv_rows: int = 256, spmv_stages: int = 2, chunk_rows: int = 8192):
+        tu = _abi.MfeBatchTuning(int(spmv_rows), int(spmv_stages), int(chunk_rows))
+        self.ctx.check(self.ctx.lib.mfe_batch_set_tuning(self.ctx.h, self.h, ctypes.byref(tu)),
+                       "mfe_batch_set_tuning")
+
+    def solve(self, max_iter: int = 200, tol: float = DBL_EPSILON, tol_mode: str = "absolute",
+              precision: str = "mixed", refine_k: int = 0, x=None):
+        """Returns (x, results): results holds one CGResult per box (times[0] =
+        assembly of the batch, times[4] = the batched solve, in seconds)."""
+        torch = _torch()
+        ctx = self.ctx
+        ctx.bind_torch_stream()
+        if x is None:
+            x = torch.empty(max(self.offsets[-1], 1), dtype=torch.float64, device="cuda")
+        o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k)
+        res = (MfeCgResult * len(self.dims))()
+        st = ctx.lib.mfe_batch_solve(ctx.h, self.h, ctypes.byref(o), _ptr(x), res)
+        if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
+            ctx.check(st, "mfe_batch_solve")
+        return x, [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status,
+                            tuple(r.times), r.refinements, None) for r in res]
+
+
 def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
                       tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
-                      ctx: Context | None = None):
-    """Assemble and solve len(dims) independent miniFE boxes (k = 1, the
-    reference's boundary conditions) together on the device.  Returns
-    (x, offsets, results): x concatenates the solutions, box i's rows being
-    x[offsets[i]:offsets[i+1]]; results holds one CGResult per box (times[0]
-    = assembly of the batch, times[4] = the batched solve, in seconds)."""
-    torch = _torch()
-    ctx = ctx or default_context()
-    dims = [tuple(int(v) for v in d) for d in dims]
-    offsets = [0]
-    for d in dims:
-        offsets.append(offsets[-1] + box_dims(*d)[0])
-    x = torch.empty(max(offsets[-1], 1), dtype=torch.float64, device="cuda")
-    flat = (ctypes.c_int32 * (3 * len(dims)))(*[v for d in dims for v in d])
-    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k)
-    res = (MfeCgResult * max(len(dims), 1))()
-    st = ctx.lib.mfe_batch_solve_boxes(ctx.h, len(dims), flat, ctypes.byref(o), _ptr(x), res)
-    if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
-        ctx.check(st, "mfe_batch_solve_boxes")
-    return x, offsets, [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status,
-                                 tuple(r.times), r.refinements, None)
-                        for r in res[:len(dims)]]
+                      tuning: dict | None = None, ctx: Context | None = None):
+    """Assemble and solve len(dims) independent miniFE boxes together
+    (mfe_batch_solve_boxes).  Returns (x, offsets, results); box i's rows are
+    x[offsets[i]:offsets[i+1]]."""
+    b = Batch(dims, ctx)
+    try:
+        if tuning:
+            b.set_tuning(**tuning)
+        x, res = b.solve(max_iter, tol, tol_mode, precision, refine_k)
+        return x, b.offsets, res
+    finally:
+        b.close()
 
 
 def cg_solve_host(row_offsets, cols, vals, b, x, max_iter=200, tol=DBL_EPSILON,

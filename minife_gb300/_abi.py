@@ -52,6 +52,10 @@ class MfeCgResult(ctypes.Structure):
     ]
 
 
+class MfeBatchTuning(ctypes.Structure):
+    _fields_ = [("spmv_rows", c_int32), ("spmv_stages", c_int32), ("chunk_rows", c_int32)]
+
+
 _P = ctypes.POINTER
 # name -> (restype, argtypes)
 SIGNATURES = {
@@ -106,6 +110,13 @@ SIGNATURES = {
                                           _P(MfeCgOpts), _P(MfeCgResult)]),
     "mfe_batch_solve_boxes": (ctypes.c_int, [c_void_p, c_int32, c_void_p, _P(MfeCgOpts),
                                              c_void_p, _P(MfeCgResult)]),
+    "mfe_batch_create": (ctypes.c_int, [c_void_p, c_int32, c_void_p, _P(c_void_p)]),
+    "mfe_batch_set_tuning": (ctypes.c_int, [c_void_p, c_void_p, _P(MfeBatchTuning)]),
+    "mfe_batch_info": (ctypes.c_int, [c_void_p, _P(c_int64), _P(c_int64), _P(c_double),
+                                      _P(MfeBatchTuning)]),
+    "mfe_batch_solve": (ctypes.c_int, [c_void_p, c_void_p, _P(MfeCgOpts), c_void_p,
+                                       _P(MfeCgResult)]),
+    "mfe_batch_destroy": (None, [c_void_p]),
 }
 
 _LIB = None

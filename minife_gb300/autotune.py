@@ -1,0 +1,133 @@
+"""Autotuner for the batched box solver: picks the FP32 SpMV tile shape (rows
+per tile, pipeline stages), the vector-kernel chunk size and the mixed
+solver's reliable-update interval (refine_k) by timing the batch itself on
+the device, and caches the choice in a JSON file keyed by the device and the
+workload.
+
+Search (coordinate descent, each timing read from the library's own CUDA
+events, results[i].times[4]):
+
+1. SpMV shape: every (rows, stages) the library instantiates, each timed on
+   a solve capped at `probe_iters` iterations, so every shape does the same
+   work;
+2. chunk rows: the same capped solve at the best shape;
+3. refine_k: full solves to the tolerance at the best shape and chunk, only
+   candidates whose every box converges.
+
+The cache lives in $MFE_TUNE_CACHE, else minife_gb300/_tuning_cache.json.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+SHAPES = [(256, 2), (256, 3), (256, 4), (128, 2), (128, 3), (128, 4)]
+CHUNKS = [4096, 8192, 16384, 32768]
+REFINE_K = [25, 50, 100]
+DEFAULT = {"spmv_rows": 256, "spmv_stages": 2, "chunk_rows": 8192, "refine_k": 50}
+
+
+def cache_path() -> str:
+    return os.environ.get("MFE_TUNE_CACHE", os.path.join(HERE, "_tuning_cache.json"))
+
+
+def _device_key() -> str:
+    import torch
+    if not torch.cuda.is_available():
+        return "no-gpu"
+    p = torch.cuda.get_device_properties(torch.cuda.current_device())
+    return "%s/sm%d" % (p.name, p.multi_processor_count)
+
+
+def signature(dims, precision: str) -> str:
+    """Device, precision and the multiset of box dimensions."""
+    h = hashlib.sha1(json.dumps(sorted(tuple(int(v) for v in d) for d in dims)).encode())
+    return "%s|%s|%s" % (_device_key(), precision, h.hexdigest()[:16])
+
+
+def _load() -> dict:
+    try:
+        with open(cache_path()) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {}
+
+
+def _store(key: str, entry: dict) -> None:
+    data = _load()
+    data[key] = entry
+    path = cache_path()
+    tmp = path + ".tmp"
+    with open(tmp, "w") as f:
+        json.dump(data, f, indent=1, sort_keys=True)
+    os.replace(tmp, path)
+
+
+def lookup(dims, precision: str = "mixed") -> dict | None:
+    return _load().get(signature(dims, precision))
+
+
+def _solve_time(batch, precision, tol, tol_mode, max_iter, refine_k, reps):
+    best, res = None, None
+    for _ in range(reps):
+        _, res = batch.solve(max_iter=max_iter, tol=tol, tol_mode=tol_mode, precision=precision,
+                             refine_k=refine_k)
+        t = res[0].times[4]
+        best = t if best is None else min(best, t)
+    return best, res
+
+
+def tune_batch(batch, precision: str = "mixed", tol: float = 1e-8, tol_mode: str = "relative",
+               max_iter: int = 5000, probe_iters: int = 40, reps: int = 2, use_cache: bool = True,
+               log=None) -> dict:
+    """Tune `batch` (a minife_gb300.Batch) and apply the result to it.
+    Returns the chosen configuration with the timings behind it."""
+    key = signature(batch.dims, precision)
+    if use_cache:
+        hit = _load().get(key)
+        if hit is not None:
+            batch.set_tuning(hit["spmv_rows"], hit["spmv_stages"], hit["chunk_rows"])
+            return dict(hit, cached=True)
+    say = log or (lambda *a: None)
+    cur = dict(DEFAULT)
+    trials = []
+
+    def capped(cfg):
+        batch.set_tuning(cfg["spmv_rows"], cfg["spmv_stages"], cfg["chunk_rows"])
+        t, _ = _solve_time(batch, precision, 0.0, tol_mode, probe_iters, cfg["refine_k"], reps)
+        trials.append({"stage": "capped", **cfg, "seconds": t})
+        say("capped %s: %.4f s" % (cfg, t))
+        return t
+
+    best_t = None
+    for rows, stages in SHAPES:
+        cfg = dict(cur, spmv_rows=rows, spmv_stages=stages)
+        t = capped(cfg)
+        if best_t is None or t < best_t:
+            best_t, cur = t, cfg
+    for chunk in CHUNKS:
+        if chunk == cur["chunk_rows"]:
+            continue
+        cfg = dict(cur, chunk_rows=chunk)
+        t = capped(cfg)
+        if t < best_t:
+            best_t, cur = t, cfg
+    batch.set_tuning(cur["spmv_rows"], cur["spmv_stages"], cur["chunk_rows"])
+    best_full = None
+    if precision == "mixed":
+        for k in REFINE_K:
+            t, res = _solve_time(batch, precision, tol, tol_mode, max_iter, k, reps)
+            ok = all(r.status == 0 for r in res)
+            trials.append({"stage": "full", **dict(cur, refine_k=k), "seconds": t, "converged": ok})
+            say("full refine_k=%d: %.4f s%s" % (k, t, "" if ok else " (not converged)"))
+            if ok and (best_full is None or t < best_full):
+                best_full, cur = t, dict(cur, refine_k=k)
+    else:
+        best_full, _ = _solve_time(batch, precision, tol, tol_mode, max_iter, cur["refine_k"], reps)
+    entry = dict(cur, solve_seconds=best_full, trials=trials)
+    if use_cache:
+        _store(key, entry)
+    return dict(entry, cached=False)

@@ -629,4 +629,42 @@ mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims
   return batch_solve_boxes(ctx, nbox, dims, opts, x_out, results);
 }
 
+mfe_status mfe_batch_create(mfe_ctx* ctx, int32_t nbox, const int32_t* dims, mfe_batch** out)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  if (!dims || !out) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  *out = nullptr;
+  for (int32_t i = 0; i < nbox; ++i)
+    if (!box_ok(dims[3 * i], dims[3 * i + 1], dims[3 * i + 2]))
+      return fail(ctx, MFE_BAD_ARG, "bad box in the batch");
+  MFE_TRY(set_device(ctx));
+  return batch_create(ctx, nbox, dims, out);
+}
+
+mfe_status mfe_batch_set_tuning(mfe_ctx* ctx, mfe_batch* batch, const mfe_batch_tuning* t)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  if (!batch || !t) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  return batch_set_tuning(ctx, batch, t);
+}
+
+mfe_status mfe_batch_info(const mfe_batch* batch, int64_t* rows, int64_t* nnz,
+                          double* assembly_seconds, mfe_batch_tuning* tuning)
+{
+  if (!batch) return MFE_BAD_ARG;
+  batch_info(batch, rows, nnz, assembly_seconds, tuning);
+  return MFE_OK;
+}
+
+mfe_status mfe_batch_solve(mfe_ctx* ctx, mfe_batch* batch, const mfe_cg_opts* opts,
+                           double* x_out, mfe_cg_result* results)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  if (!batch || !opts || !results) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  return batch_solve(ctx, batch, opts, x_out, results);
+}
+
+void mfe_batch_destroy(mfe_batch* batch) { batch_destroy(batch); }
+
 }  // extern "C"

@@ -27,8 +27,8 @@
 // finish a box (per-box counter) sums that box's partials in CTA order and
 // forms the box's scalar (alpha or the true residual).
 //
-// Vectors.  k_bx_p / k_bx_update walk the chunk list (kBxChunk rows of one
-// box per block pass); per-box r.r: one partial per chunk, the last block of
+// Vectors.  k_bx_p / k_bx_update walk the chunk list (a tunable number of
+// rows of one box per block pass); per-box r.r: one partial per chunk, the last block of
 // the box sums them in chunk order.
 //
 // Solvers.  FP64: the reference's CG per box (cg_solve.hpp loop test with
@@ -52,7 +52,6 @@ namespace mfe {
 
 constexpr int kBxMaxBoxes = 1024;
 constexpr int kBxVT = 256;       // vector-kernel block
-constexpr int kBxChunk = 8192;   // rows per vector chunk
 constexpr int kBxPad = 4;        // slice alignment in elements
 
 struct BoxDesc {
@@ -89,22 +88,13 @@ struct BxList {
 
 __host__ __device__ constexpr int bx_capv(int rows) { return ((rows * 27 + 8) + 3) & ~3; }
 __host__ __device__ constexpr int bx_capx(int rows) { return ((rows + 2 + 8) + 3) & ~3; }
-template <typename T>
-struct BxShape;
-template <>
-struct BxShape<float> {
-  static constexpr int rows = 256, stages = 2;
-};
-template <>
-struct BxShape<double> {
-  static constexpr int rows = 128, stages = 2;
-};
-template <typename T>
-constexpr size_t bx_smem()
+// dynamic shared memory of a box-SpMV launch shape (rows per tile, stages)
+inline size_t bx_smem(size_t elem, int rows, int stages)
 {
-  return (size_t)BxShape<T>::stages *
-         ((size_t)bx_capv(BxShape<T>::rows) + 9 * (size_t)bx_capx(BxShape<T>::rows)) * sizeof(T);
+  return (size_t)stages * ((size_t)bx_capv(rows) + 9 * (size_t)bx_capx(rows)) * elem;
 }
+// FP64 products run at the one shape (FP64-FMA-bound); the FP32 shape is tunable
+constexpr int kBx64Rows = 128, kBx64Stages = 2;
 
 // position q of global index i in a prefix array pre[0..cnt] (pre[q] <= i <
 // pre[q+1]), searching forward from a previous position
@@ -210,10 +200,10 @@ __device__ void bx_flush(BoxSt* st, double* slots, int b, int A, int E, int tota
 // unmasked 27-term code; otherwise the compressed CSR values with masked
 // slots for boundary rows.  x has ghost zones of zeros around each box, so
 // the nine segments are never clamped.
-template <typename T, int MODE, bool ELL>
-__global__ void __launch_bounds__(BxShape<T>::rows + 32) k_bx_spmv(BxSpmvParams<T> P)
+template <typename T, int MODE, bool ELL, int ROWS, int S>
+__global__ void __launch_bounds__(ROWS + 32) k_bx_spmv(BxSpmvParams<T> P)
 {
-  constexpr int ROWS = BxShape<T>::rows, S = BxShape<T>::stages, C = ROWS / 32;
+  constexpr int C = ROWS / 32;
   constexpr int capv = bx_capv(ROWS), capx = bx_capx(ROWS);
   constexpr int stage_elems = capv + 9 * capx;
   constexpr int VA = 16 / sizeof(T);
@@ -478,6 +468,7 @@ struct BxVecParams {
   const int* cpre;
   const int* count;
   double* chunk_part;  // [total chunks], static chunk index
+  int chunk;           // rows per chunk (multiple of 4)
 };
 
 // p = r + beta_b p (p = r on the first iteration)
@@ -494,8 +485,8 @@ __global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restri
     const int b = __ldg(&Q.ids[q]);
     const BoxDesc& d = Q.boxes[b];
     const int lc = c - __ldg(&Q.cpre[q]);
-    const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
-    const int len = min(kBxChunk, d.n - lc * kBxChunk);
+    const int64_t g0 = d.row_base + (int64_t)lc * Q.chunk;
+    const int len = min(Q.chunk, d.n - lc * Q.chunk);
     const V beta = (V)Q.st[b].beta;
     using VV = typename BxVec16<V>::type;
     constexpr int VW = BxVec16<V>::n;
@@ -537,8 +528,8 @@ __global__ void __launch_bounds__(kBxVT)
     const int b = __ldg(&Q.ids[q]);
     const BoxDesc& d = Q.boxes[b];
     const int lc = c - __ldg(&Q.cpre[q]);
-    const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
-    const int len = min(kBxChunk, d.n - lc * kBxChunk);
+    const int64_t g0 = d.row_base + (int64_t)lc * Q.chunk;
+    const int len = min(Q.chunk, d.n - lc * Q.chunk);
     const V alpha = (V)Q.st[b].alpha;
     double acc = 0.0;
     DFAcc facc;
@@ -608,8 +599,8 @@ __global__ void __launch_bounds__(kBxVT)
     const int b = __ldg(&Q.ids[q]);
     const BoxDesc& d = Q.boxes[b];
     const int lc = c - __ldg(&Q.cpre[q]);
-    const int64_t g0 = d.row_base + (int64_t)lc * kBxChunk;
-    const int len = min(kBxChunk, d.n - lc * kBxChunk);
+    const int64_t g0 = d.row_base + (int64_t)lc * Q.chunk;
+    const int len = min(Q.chunk, d.n - lc * Q.chunk);
     for (int k = threadIdx.x; k < len; k += kBxVT) {
       x[g0 + k] += f2d_exact(x32[g0 + k]);
       x32[g0 + k] = 0.0f;
@@ -826,52 +817,115 @@ __global__ void __launch_bounds__(1024)
 // ---------------------------------------------------------------------------
 // host
 // ---------------------------------------------------------------------------
-namespace {
+}  // namespace mfe
 
-// float SpMVs read the padded 27-per-row values, double ones the compressed CSR
-template <typename T>
-constexpr bool bx_ell()
-{
-  return sizeof(T) == 4;
-}
-
-template <typename T, int MODE>
-int bx_grid(mfe_ctx* ctx)
-{
-  static int per_sm[64] = {};
-  const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
-  if (per_sm[dev] == 0) {
-    cudaFuncSetAttribute(k_bx_spmv<T, MODE, bx_ell<T>()>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)bx_smem<T>());
-    int n = 1;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_bx_spmv<T, MODE, bx_ell<T>()>,
-                                                  BxShape<T>::rows + 32, bx_smem<T>());
-    per_sm[dev] = std::max(n, 1);
-  }
-  return ctx->sm_count * per_sm[dev];
-}
-
-struct BatchBufs {
-  BoxDesc* boxes;
-  BoxSt* st;
-  BatchCtl* ctl;
-  BxList open, gate, all;
-  double* slots;
-  double* chunk_part;
-  double *vals64, *b, *x;
-  float* ell32;  // padded 27-per-row FP32 values (mixed solver)
-  void *r, *p, *Ap;  // FP32 (mixed) or FP64
-  float* x32;
-  int nbox, grid32, grid64;
+// The batch handle: the assembled store of every box, owned device memory,
+// and the launch shape the solves use.
+struct mfe_batch {
+  int device = 0;
+  int nbox = 0;
+  std::vector<int32_t> dims;
+  std::vector<mfe::BoxDesc> hd;  // bases; tile and chunk counts filled per solve
+  int64_t rows_tot = 0, nnz_tot = 0, ell_tot = 0, rows_real = 0, nnz_real = 0;
+  double assembly_s = 0.0;
+  mfe_batch_tuning tune{256, 2, 8192};
+  bool ell_ready = false;
+  // device memory
+  mfe::BoxDesc* boxes = nullptr;
+  mfe::BoxSt* st = nullptr;
+  mfe::BatchCtl* ctl = nullptr;
+  int* lists = nullptr;  // three lists (open, gate, all)
+  double* slots = nullptr;
+  size_t slots_bytes = 0;
+  double* chunk_part = nullptr;
+  size_t chunk_part_bytes = 0;
+  double *vals64 = nullptr, *b = nullptr, *x = nullptr;
+  float* ell32 = nullptr;
+  void *r = nullptr, *p = nullptr, *Ap = nullptr;
+  float* x32 = nullptr;
+  size_t vec_bytes = 0;  // bytes of r, p, Ap as allocated
+  std::vector<void*> owned;
 };
 
+namespace mfe {
+namespace {
+
+int64_t pad4(int64_t v) { return (v + kBxPad - 1) / kBxPad * kBxPad; }
+
+// FP32 products read the padded 27-per-row values, FP64 ones the compressed CSR
+template <int MODE, int R, int S>
+cudaError_t bx_cfg32(int* per_sm)
+{
+  auto k = k_bx_spmv<float, MODE, true, R, S>;
+  const size_t smem = bx_smem(sizeof(float), R, S);
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k, R + 32, smem);
+  return e;
+}
+
+template <typename F>
+auto bx_dispatch32(int rows, int stages, F&& f)
+{
+  if (rows == 128) {
+    if (stages == 3) return f.template operator()<128, 3>();
+    if (stages == 4) return f.template operator()<128, 4>();
+    return f.template operator()<128, 2>();
+  }
+  if (stages == 3) return f.template operator()<256, 3>();
+  if (stages == 4) return f.template operator()<256, 4>();
+  return f.template operator()<256, 2>();
+}
+
+bool bx_shape_ok(const mfe_batch_tuning& t)
+{
+  return (t.spmv_rows == 128 || t.spmv_rows == 256) && t.spmv_stages >= 2 && t.spmv_stages <= 4 &&
+         t.chunk_rows >= 1024 && t.chunk_rows <= (1 << 20) && t.chunk_rows % 4 == 0;
+}
+
+struct Grids {
+  int g32, g64;
+};
+
+// grid sizes (resident CTAs) of the FP32 shape and the FP64 shape; the
+// attributes are set here, before any graph capture
+mfe_status bx_grids(mfe_ctx* ctx, const mfe_batch_tuning& t, Grids* g)
+{
+  int per32 = 1, pd = 1, pr = 1;
+  cudaError_t e = bx_dispatch32(t.spmv_rows, t.spmv_stages,
+                                [&]<int R, int S>() { return bx_cfg32<BX_DOT, R, S>(&per32); });
+  const size_t smem64 = bx_smem(sizeof(double), kBx64Rows, kBx64Stages);
+  auto kd = k_bx_spmv<double, BX_DOT, false, kBx64Rows, kBx64Stages>;
+  auto kr = k_bx_spmv<double, BX_RESID, false, kBx64Rows, kBx64Stages>;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kd, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(kr, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem64);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pd, kd, kBx64Rows + 32, smem64);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pr, kr, kBx64Rows + 32, smem64);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched SpMV configuration");
+  g->g32 = ctx->sm_count * std::max(per32, 1);
+  g->g64 = ctx->sm_count * std::max(std::min(pd, pr), 1);
+  return MFE_OK;
+}
+
+struct Run {
+  mfe_batch* bt;
+  BxList open, gate, all;
+  Grids grid;
+  bool mixed;
+};
+
+BxVecParams bx_vec(const Run& R, const BxList& L)
+{
+  return BxVecParams{R.bt->boxes, R.bt->st, R.bt->ctl, L.ids, L.cpre, L.count, R.bt->chunk_part,
+                     R.bt->tune.chunk_rows};
+}
+
 template <typename T, int MODE>
-mfe_status bx_spmv(mfe_ctx* ctx, const BatchBufs& W, const BxList& L, const T* vals, const T* x,
-                   T* y, const double* b, float* y32, int grid)
+BxSpmvParams<T> bx_params(const Run& R, const BxList& L, const T* vals, const T* x, T* y,
+                          const double* b, float* y32)
 {
   BxSpmvParams<T> P;
-  P.boxes = W.boxes;
-  P.st = W.st;
+  P.boxes = R.bt->boxes;
+  P.st = R.bt->st;
   P.ids = L.ids;
   P.tpre = sizeof(T) == 4 ? L.tpre32 : L.tpre64;
   P.count = L.count;
@@ -880,171 +934,318 @@ mfe_status bx_spmv(mfe_ctx* ctx, const BatchBufs& W, const BxList& L, const T* v
   P.y = y;
   P.b = b;
   P.y32 = y32;
-  P.slots = W.slots;
-  P.err = &W.ctl->err;
-  k_bx_spmv<T, MODE, bx_ell<T>()><<<grid, BxShape<T>::rows + 32, bx_smem<T>(), ctx->stream>>>(P);
+  P.slots = R.bt->slots;
+  P.err = &R.bt->ctl->err;
+  return P;
+}
+
+mfe_status bx_spmv32(mfe_ctx* ctx, const Run& R, const BxList& L, const float* x, float* y)
+{
+  const BxSpmvParams<float> P = bx_params<float, BX_DOT>(R, L, R.bt->ell32, x, y, nullptr, nullptr);
+  bx_dispatch32(R.bt->tune.spmv_rows, R.bt->tune.spmv_stages, [&]<int RW, int S>() {
+    k_bx_spmv<float, BX_DOT, true, RW, S>
+        <<<R.grid.g32, RW + 32, bx_smem(sizeof(float), RW, S), ctx->stream>>>(P);
+    return 0;
+  });
   return check_launch(ctx, "k_bx_spmv");
 }
 
-BxVecParams bx_vec(const BatchBufs& W, const BxList& L)
+template <int MODE>
+mfe_status bx_spmv64(mfe_ctx* ctx, const Run& R, const BxList& L, const double* x, double* y,
+                     const double* b, float* y32)
 {
-  return BxVecParams{W.boxes, W.st, W.ctl, L.ids, L.cpre, L.count, W.chunk_part};
+  const BxSpmvParams<double> P = bx_params<double, MODE>(R, L, R.bt->vals64, x, y, b, y32);
+  k_bx_spmv<double, MODE, false, kBx64Rows, kBx64Stages>
+      <<<R.grid.g64, kBx64Rows + 32, bx_smem(sizeof(double), kBx64Rows, kBx64Stages), ctx->stream>>>(P);
+  return check_launch(ctx, "k_bx_spmv");
 }
 
 int bx_vgrid(mfe_ctx* ctx) { return ctx->sm_count * 8; }
 
-mfe_status bx_iter_mixed(mfe_ctx* ctx, const BatchBufs& W, cudaGraphConditionalHandle h, int in_graph)
+mfe_status bx_iter_mixed(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle h, int in_graph)
 {
-  float* r = static_cast<float*>(W.r);
-  float* p = static_cast<float*>(W.p);
-  float* Ap = static_cast<float*>(W.Ap);
+  mfe_batch* bt = R.bt;
+  float* r = static_cast<float*>(bt->r);
+  float* p = static_cast<float*>(bt->p);
+  float* Ap = static_cast<float*>(bt->Ap);
   const int vg = bx_vgrid(ctx);
-  k_bx_p<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), r, p);
+  k_bx_p<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
-  MFE_TRY((bx_spmv<float, BX_DOT>(ctx, W, W.open, W.ell32, p, Ap, nullptr, nullptr, W.grid32)));
-  k_bx_update<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), W.x32, r, p, Ap);
+  MFE_TRY(bx_spmv32(ctx, R, R.open, p, Ap));
+  k_bx_update<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), bt->x32, r, p, Ap);
   MFE_TRY(check_launch(ctx, "k_bx_update"));
-  k_bx_decide<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.gate);
+  k_bx_decide<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.gate);
   MFE_TRY(check_launch(ctx, "k_bx_decide"));
-  k_bx_xupdate<<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.gate), W.x, W.x32);
+  k_bx_xupdate<<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.gate), bt->x, bt->x32);
   MFE_TRY(check_launch(ctx, "k_bx_xupdate"));
-  MFE_TRY((bx_spmv<double, BX_RESID>(ctx, W, W.gate, W.vals64, W.x, nullptr, W.b, r, W.grid64)));
-  k_bx_after<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.open, h, in_graph);
+  MFE_TRY(bx_spmv64<BX_RESID>(ctx, R, R.gate, bt->x, nullptr, bt->b, r));
+  k_bx_after<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open, h, in_graph);
   return check_launch(ctx, "k_bx_after");
 }
 
-mfe_status bx_iter_f64(mfe_ctx* ctx, const BatchBufs& W, cudaGraphConditionalHandle h, int in_graph)
+mfe_status bx_iter_f64(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle h, int in_graph)
 {
-  double* r = static_cast<double*>(W.r);
-  double* p = static_cast<double*>(W.p);
-  double* Ap = static_cast<double*>(W.Ap);
+  mfe_batch* bt = R.bt;
+  double* r = static_cast<double*>(bt->r);
+  double* p = static_cast<double*>(bt->p);
+  double* Ap = static_cast<double*>(bt->Ap);
   const int vg = bx_vgrid(ctx);
-  k_bx_p<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), r, p);
+  k_bx_p<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
-  MFE_TRY((bx_spmv<double, BX_DOT>(ctx, W, W.open, W.vals64, p, Ap, nullptr, nullptr, W.grid64)));
-  k_bx_update<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(W, W.open), W.x, r, p, Ap);
+  MFE_TRY(bx_spmv64<BX_DOT>(ctx, R, R.open, p, Ap, nullptr, nullptr));
+  k_bx_update<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), bt->x, r, p, Ap);
   MFE_TRY(check_launch(ctx, "k_bx_update"));
-  k_bx_after64<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.open, h, in_graph);
+  k_bx_after64<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open, h, in_graph);
   return check_launch(ctx, "k_bx_after64");
 }
 
-int64_t pad4(int64_t v) { return (v + kBxPad - 1) / kBxPad * kBxPad; }
-
-mfe_status bx_list_alloc(mfe_ctx* ctx, const char* name, int nbox, BxList* L)
+void* bx_alloc(mfe_batch* bt, size_t bytes)
 {
-  const size_t per = (size_t)nbox + 2;
-  int* a = static_cast<int*>(workspace(ctx, name, sizeof(int) * (4 * per + 1)));
-  if (!a) return fail(ctx, MFE_OOM, "batch list allocation failed");
-  L->ids = a;
-  L->tpre32 = a + per;
-  L->tpre64 = a + 2 * per;
-  L->cpre = a + 3 * per;
-  L->count = a + 4 * per;
+  void* ptr = nullptr;
+  if (cudaMalloc(&ptr, bytes) != cudaSuccess) return nullptr;
+  bt->owned.push_back(ptr);
+  return ptr;
+}
+
+BxList bx_list(int* base, int nbox, int which)
+{
+  const size_t per = (size_t)nbox + 2, stride = 4 * per + 4;
+  int* a = base + which * stride;
+  return BxList{a, a + per, a + 2 * per, a + 3 * per, a + 4 * per};
+}
+
+// Runs `body` as a CUDA graph with a conditional while node on ctl->cont (or,
+// with MFE_CG_EAGER set, as a host loop reading cont back each iteration).
+template <typename Body>
+mfe_status bx_loop(mfe_ctx* ctx, BatchCtl* dctl, Body body)
+{
+  if (getenv("MFE_CG_EAGER") != nullptr) {
+    BatchCtl* hctl = static_cast<BatchCtl*>(host_scratch(ctx, sizeof(BatchCtl)));
+    if (!hctl) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
+    for (;;) {
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hctl, dctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!hctl->cont) return MFE_OK;
+      MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
+    }
+  }
+  cudaStream_t run_stream = ctx->stream, s = ctx->own_stream;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  cudaGraphConditionalHandle h = 0;
+  mfe_status st = MFE_OK;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
+  if (e == cudaSuccess) {
+    ctx->stream = s;
+    e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+    if (e == cudaSuccess) {
+      k_bx_begin<<<1, 1, 0, s>>>(dctl, h);
+      e = cudaStreamEndCapture(s, &g);
+    }
+    cudaGraphNode_t nodes[4];
+    size_t nn = 4;
+    if (e == cudaSuccess) e = cudaGraphGetNodes(g, nodes, &nn);
+    alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
+    memset(cp_buf, 0, sizeof(cp_buf));
+    cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
+    cp->type = cudaGraphNodeTypeConditional;
+    cp->conditional.handle = h;
+    cp->conditional.type = cudaGraphCondTypeWhile;
+    cp->conditional.size = 1;
+    cudaGraphNode_t cnode;
+    if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
+    if (e == cudaSuccess) {
+      cudaGraph_t bg = cp->conditional.phGraph_out[0];
+      e = cudaStreamBeginCaptureToGraph(s, bg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+      if (e == cudaSuccess) {
+        st = body(h, 1);
+        cudaGraph_t tmp;
+        const cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+        if (e == cudaSuccess) e = e2;
+      }
+    }
+    ctx->stream = run_stream;
+    if (e == cudaSuccess && st == MFE_OK) e = cudaGraphInstantiate(&ex, g, 0);
+    if (e == cudaSuccess && st == MFE_OK) e = cudaGraphLaunch(ex, ctx->stream);
+  }
+  if (ex) cudaGraphExecDestroy(ex);
+  if (g) cudaGraphDestroy(g);
+  if (st != MFE_OK) return st;
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched CG graph");
   return MFE_OK;
 }
 
 }  // namespace
 
-mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const mfe_cg_opts* o,
-                             double* x_out, mfe_cg_result* results)
+mfe_status batch_create(mfe_ctx* ctx, int nbox, const int32_t* dims, mfe_batch** out)
 {
+  *out = nullptr;
   if (nbox < 1 || nbox > kBxMaxBoxes) return fail(ctx, MFE_BAD_ARG, "nbox must be 1..1024");
-  if (o->precision != MFE_PREC_MIXED && o->precision != MFE_PREC_F64)
-    return fail(ctx, MFE_BAD_ARG, "unknown precision");
-  const bool mixed = o->precision == MFE_PREC_MIXED;
-  constexpr int R32 = BxShape<float>::rows, R64 = BxShape<double>::rows;
-
-  // ---- plan: slices, tiles, chunks ----
-  std::vector<BoxDesc> hd(nbox);
-  int64_t rows_tot = 0, nnz_tot = 0, ell_tot = 0, max_nnz = 0, max_rows = 0;
-  int chunks_tot = 0;
+  mfe_batch* bt = new mfe_batch();
+  bt->device = ctx->device;
+  bt->nbox = nbox;
+  bt->dims.assign(dims, dims + 3 * nbox);
+  bt->hd.resize(nbox);
+  int64_t max_nnz = 0, max_rows = 0;
   for (int i = 0; i < nbox; ++i) {
     const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
     int64_t n = 0, nnz = 0;
-    if (mfe_box_dims(nx, ny, nz, &n, &nnz) != MFE_OK || nnz > INT32_MAX - 64)
+    if (mfe_box_dims(nx, ny, nz, &n, &nnz) != MFE_OK || nnz > INT32_MAX - 64 || 27 * n > INT32_MAX - 64) {
+      delete bt;
       return fail(ctx, MFE_BAD_ARG, "bad box dimensions in the batch");
-    BoxDesc& d = hd[i];
+    }
+    BoxDesc& d = bt->hd[i];
+    memset(&d, 0, sizeof(d));
     d.Nx = nx + 1;
     d.Ny = ny + 1;
     d.Nz = nz + 1;
     d.NxNy = d.Nx * d.Ny;
     d.n = (int)n;
-    d.ntiles32 = (int)ceil_div(n, R32);
-    d.ntiles64 = (int)ceil_div(n, R64);
-    d.nchunks = (int)ceil_div(n, kBxChunk);
-    d.chunk_base = chunks_tot;
     // ghost zone: rows a tile's x segments reach outside the box, rounded to
     // the copy granule
     const int64_t ghost = pad4((int64_t)d.NxNy + d.Nx + 1 + kBxPad);
-    d.row_base = rows_tot + ghost;
-    d.nnz_base = nnz_tot;
-    d.ell_base = ell_tot;
-    chunks_tot += d.nchunks;
-    rows_tot += ghost + pad4(n) + ghost;
-    nnz_tot += pad4(nnz);
-    ell_tot += pad4(27 * n);
+    d.row_base = bt->rows_tot + ghost;
+    d.nnz_base = bt->nnz_tot;
+    d.ell_base = bt->ell_tot;
+    bt->rows_tot += ghost + pad4(n) + ghost;
+    bt->nnz_tot += pad4(nnz);
+    bt->ell_tot += pad4(27 * n);
+    bt->rows_real += n;
+    bt->nnz_real += nnz;
     max_nnz = std::max(max_nnz, nnz);
     max_rows = std::max(max_rows, n);
   }
-
-  // ---- device buffers ----
-  BatchBufs W{};
-  W.nbox = nbox;
-  W.grid32 = bx_grid<float, BX_DOT>(ctx);
-  W.grid64 = std::max(bx_grid<double, BX_DOT>(ctx), bx_grid<double, BX_RESID>(ctx));
-  const int G = std::max(W.grid32, W.grid64);
-  const size_t vb = (mixed ? sizeof(float) : sizeof(double)) * (size_t)(rows_tot + 8);
-  W.boxes = static_cast<BoxDesc*>(workspace(ctx, "batch.boxes", sizeof(BoxDesc) * nbox));
-  W.st = static_cast<BoxSt*>(workspace(ctx, "batch.state", sizeof(BoxSt) * nbox));
-  W.ctl = static_cast<BatchCtl*>(workspace(ctx, "batch.ctl", sizeof(BatchCtl)));
-  W.slots = static_cast<double*>(workspace(ctx, "batch.slots", sizeof(double) * (size_t)nbox * G * 8));
-  W.chunk_part = static_cast<double*>(workspace(ctx, "batch.chunks", sizeof(double) * (size_t)chunks_tot));
-  W.vals64 = static_cast<double*>(workspace(ctx, "batch.vals64", sizeof(double) * (size_t)(nnz_tot + 8)));
-  W.b = static_cast<double*>(workspace(ctx, "batch.b", sizeof(double) * (size_t)(rows_tot + 8)));
-  W.x = static_cast<double*>(workspace(ctx, "batch.x", sizeof(double) * (size_t)(rows_tot + 8)));
-  W.r = workspace(ctx, "batch.r", vb);
-  W.p = workspace(ctx, "batch.p", vb);
-  W.Ap = workspace(ctx, "batch.Ap", vb);
-  W.ell32 = mixed ? static_cast<float*>(workspace(ctx, "batch.ell32", sizeof(float) * (size_t)(ell_tot + 8)))
-                  : nullptr;
-  W.x32 = mixed ? static_cast<float*>(workspace(ctx, "batch.x32", sizeof(float) * (size_t)(rows_tot + 8)))
-                : nullptr;
+  const size_t rows8 = (size_t)(bt->rows_tot + 8);
+  bt->boxes = static_cast<BoxDesc*>(bx_alloc(bt, sizeof(BoxDesc) * nbox));
+  bt->st = static_cast<BoxSt*>(bx_alloc(bt, sizeof(BoxSt) * nbox));
+  bt->ctl = static_cast<BatchCtl*>(bx_alloc(bt, sizeof(BatchCtl)));
+  bt->lists = static_cast<int*>(bx_alloc(bt, sizeof(int) * 3 * (4 * ((size_t)nbox + 2) + 4)));
+  bt->vals64 = static_cast<double*>(bx_alloc(bt, sizeof(double) * (size_t)(bt->nnz_tot + 8)));
+  bt->b = static_cast<double*>(bx_alloc(bt, sizeof(double) * rows8));
+  bt->x = static_cast<double*>(bx_alloc(bt, sizeof(double) * rows8));
   int32_t* ro = static_cast<int32_t*>(workspace(ctx, "batch.ro", sizeof(int32_t) * (size_t)(max_rows + 1)));
   int32_t* cols = static_cast<int32_t*>(workspace(ctx, "batch.cols", sizeof(int32_t) * (size_t)(max_nnz + 4)));
-  if (!W.boxes || !W.st || !W.ctl || !W.slots || !W.chunk_part || !W.vals64 || !W.b || !W.x ||
-      !W.r || !W.p || !W.Ap || (mixed && (!W.ell32 || !W.x32)) || !ro || !cols)
-    return fail(ctx, MFE_OOM, "batch workspace allocation failed");
-  MFE_TRY(bx_list_alloc(ctx, "batch.list.open", nbox, &W.open));
-  MFE_TRY(bx_list_alloc(ctx, "batch.list.gate", nbox, &W.gate));
-  MFE_TRY(bx_list_alloc(ctx, "batch.list.all", nbox, &W.all));
-
-  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.boxes, hd.data(), sizeof(BoxDesc) * nbox, cudaMemcpyHostToDevice, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.vals64, 0, sizeof(double) * (size_t)(nnz_tot + 8), ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.b, 0, sizeof(double) * (size_t)(rows_tot + 8), ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.x, 0, sizeof(double) * (size_t)(rows_tot + 8), ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.r, 0, vb, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.p, 0, vb, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.Ap, 0, vb, ctx->stream));
-  if (mixed) MFE_CUDA_TRY(ctx, cudaMemsetAsync(W.x32, 0, sizeof(float) * (size_t)(rows_tot + 8), ctx->stream));
-
-  // ---- assembly, box by box (structure into scratch, values into the slice) ----
-  for (int i = 0; i < nbox; ++i) {
-    const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
-    MFE_TRY(launch_structure(ctx, nx, ny, nz, ro, cols));
-    MFE_TRY(launch_assemble(ctx, nx, ny, nz, nullptr, ro, W.vals64 + hd[i].nnz_base,
-                            W.b + hd[i].row_base, 1));
+  if (!bt->boxes || !bt->st || !bt->ctl || !bt->lists || !bt->vals64 || !bt->b || !bt->x || !ro || !cols) {
+    batch_destroy(bt);
+    return fail(ctx, MFE_OOM, "batch allocation failed");
   }
-  if (mixed) {
+  mfe_status st = MFE_OK;
+  auto cu = [&](cudaError_t e, const char* w) {
+    if (st == MFE_OK && e != cudaSuccess) st = cuda_fail(ctx, e, w);
+  };
+  cu(cudaEventRecord(ctx->ev0, ctx->stream), "event");
+  cu(cudaMemsetAsync(bt->vals64, 0, sizeof(double) * (size_t)(bt->nnz_tot + 8), ctx->stream), "memset");
+  cu(cudaMemsetAsync(bt->b, 0, sizeof(double) * rows8, ctx->stream), "memset");
+  for (int i = 0; i < nbox && st == MFE_OK; ++i) {
+    const int nx = dims[3 * i], ny = dims[3 * i + 1], nz = dims[3 * i + 2];
+    st = launch_structure(ctx, nx, ny, nz, ro, cols);
+    if (st == MFE_OK)
+      st = launch_assemble(ctx, nx, ny, nz, nullptr, ro, bt->vals64 + bt->hd[i].nnz_base,
+                           bt->b + bt->hd[i].row_base, 1);
+  }
+  cu(cudaEventRecord(ctx->ev1, ctx->stream), "event");
+  cu(cudaEventSynchronize(ctx->ev1), "assembly");
+  if (st != MFE_OK) {
+    batch_destroy(bt);
+    return st;
+  }
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  bt->assembly_s = ms * 1e-3;
+  *out = bt;
+  return MFE_OK;
+}
+
+void batch_destroy(mfe_batch* bt)
+{
+  if (!bt) return;
+  int prev = -1;
+  cudaGetDevice(&prev);
+  cudaSetDevice(bt->device);
+  for (void* p : bt->owned) cudaFree(p);
+  if (prev >= 0) cudaSetDevice(prev);
+  delete bt;
+}
+
+void batch_info(const mfe_batch* bt, int64_t* rows, int64_t* nnz, double* assembly_s,
+                mfe_batch_tuning* tuning)
+{
+  if (rows) *rows = bt->rows_real;
+  if (nnz) *nnz = bt->nnz_real;
+  if (assembly_s) *assembly_s = bt->assembly_s;
+  if (tuning) *tuning = bt->tune;
+}
+
+mfe_status batch_set_tuning(mfe_ctx* ctx, mfe_batch* bt, const mfe_batch_tuning* t)
+{
+  if (!bx_shape_ok(*t)) return fail(ctx, MFE_BAD_ARG, "spmv_rows 128|256, spmv_stages 2..4, chunk_rows 1024..2^20 (multiple of 4)");
+  bt->tune = *t;
+  return MFE_OK;
+}
+
+mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double* x_out,
+                       mfe_cg_result* results)
+{
+  if (o->precision != MFE_PREC_MIXED && o->precision != MFE_PREC_F64)
+    return fail(ctx, MFE_BAD_ARG, "unknown precision");
+  if (bt->device != ctx->device) return fail(ctx, MFE_BAD_ARG, "batch belongs to another device");
+  const int nbox = bt->nbox;
+  Run R;
+  R.bt = bt;
+  R.mixed = o->precision == MFE_PREC_MIXED;
+  R.open = bx_list(bt->lists, nbox, 0);
+  R.gate = bx_list(bt->lists, nbox, 1);
+  R.all = bx_list(bt->lists, nbox, 2);
+  MFE_TRY(bx_grids(ctx, bt->tune, &R.grid));
+  const size_t rows8 = (size_t)(bt->rows_tot + 8);
+
+  // tiles and chunks of each box at this launch shape
+  int chunks_tot = 0;
+  for (auto& d : bt->hd) {
+    d.ntiles32 = (int)ceil_div(d.n, bt->tune.spmv_rows);
+    d.ntiles64 = (int)ceil_div(d.n, kBx64Rows);
+    d.nchunks = (int)ceil_div(d.n, bt->tune.chunk_rows);
+    d.chunk_base = chunks_tot;
+    chunks_tot += d.nchunks;
+  }
+  // buffers that depend on the precision or the shape (grown, never shrunk)
+  const size_t vb = (R.mixed ? sizeof(float) : sizeof(double)) * rows8;
+  if (bt->vec_bytes < vb) {
+    bt->r = bx_alloc(bt, vb);
+    bt->p = bx_alloc(bt, vb);
+    bt->Ap = bx_alloc(bt, vb);
+    if (!bt->r || !bt->p || !bt->Ap) return fail(ctx, MFE_OOM, "batch vector allocation failed");
+    bt->vec_bytes = vb;
+  }
+  if (R.mixed && !bt->x32) {
+    bt->x32 = static_cast<float*>(bx_alloc(bt, sizeof(float) * rows8));
+    bt->ell32 = static_cast<float*>(bx_alloc(bt, sizeof(float) * (size_t)(bt->ell_tot + 8)));
+    if (!bt->x32 || !bt->ell32) return fail(ctx, MFE_OOM, "batch FP32 allocation failed");
+  }
+  const size_t slots_b = sizeof(double) * (size_t)nbox * std::max(R.grid.g32, R.grid.g64) * 8;
+  if (bt->slots_bytes < slots_b) {
+    bt->slots = static_cast<double*>(bx_alloc(bt, slots_b));
+    if (!bt->slots) return fail(ctx, MFE_OOM, "batch slot allocation failed");
+    bt->slots_bytes = slots_b;
+  }
+  const size_t cp_b = sizeof(double) * (size_t)(chunks_tot + 1);
+  if (bt->chunk_part_bytes < cp_b) {
+    bt->chunk_part = static_cast<double*>(bx_alloc(bt, cp_b));
+    if (!bt->chunk_part) return fail(ctx, MFE_OOM, "batch chunk allocation failed");
+    bt->chunk_part_bytes = cp_b;
+  }
+  if (R.mixed && !bt->ell_ready) {
     for (int i = 0; i < nbox; ++i) {
-      k_bx_ell<<<(unsigned)std::min<int64_t>(ceil_div(hd[i].n, 256), (int64_t)ctx->sm_count * 8), 256, 0,
-                 ctx->stream>>>(hd[i], W.vals64, W.ell32);
+      k_bx_ell<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(bt->hd[i].n, 256),
+                                                                  (int64_t)ctx->sm_count * 8)),
+                 256, 0, ctx->stream>>>(bt->hd[i], bt->vals64, bt->ell32);
       MFE_TRY(check_launch(ctx, "k_bx_ell"));
     }
+    bt->ell_ready = true;
   }
-  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
 
-  // ---- initial state, r = b - A x0 over all boxes ----
+  // state: x = 0, ghosts and work vectors zero, per-box tolerances
   std::vector<BoxSt> hs(nbox);
   for (int i = 0; i < nbox; ++i) {
     memset(&hs[i], 0, sizeof(BoxSt));
@@ -1057,119 +1258,61 @@ mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const 
   hc.first = 1;
   hc.tol_mode = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;
   hc.delta2 = 1e-2;
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.st, hs.data(), sizeof(BoxSt) * nbox, cudaMemcpyHostToDevice, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.ctl, &hc, sizeof(BatchCtl), cudaMemcpyHostToDevice, ctx->stream));
-  // list of all boxes (host-built, then copied)
+  std::vector<int> hl(4 * ((size_t)nbox + 2) + 4, 0);
   {
-    std::vector<int> h(4 * ((size_t)nbox + 2) + 1, 0);
     const size_t per = (size_t)nbox + 2;
     int t32 = 0, t64 = 0, ch = 0;
     for (int i = 0; i < nbox; ++i) {
-      h[i] = i;
-      h[per + i] = t32;
-      h[2 * per + i] = t64;
-      h[3 * per + i] = ch;
-      t32 += hd[i].ntiles32;
-      t64 += hd[i].ntiles64;
-      ch += hd[i].nchunks;
+      hl[i] = i;
+      hl[per + i] = t32;
+      hl[2 * per + i] = t64;
+      hl[3 * per + i] = ch;
+      t32 += bt->hd[i].ntiles32;
+      t64 += bt->hd[i].ntiles64;
+      ch += bt->hd[i].nchunks;
     }
-    h[per + nbox] = t32;
-    h[2 * per + nbox] = t64;
-    h[3 * per + nbox] = ch;
-    h[4 * per] = nbox;
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(W.all.ids, h.data(), sizeof(int) * h.size(), cudaMemcpyHostToDevice,
-                                      ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));  // h goes out of scope
+    hl[per + nbox] = t32;
+    hl[2 * per + nbox] = t64;
+    hl[3 * per + nbox] = ch;
+    hl[4 * per] = nbox;
   }
-  if (mixed)
-    MFE_TRY((bx_spmv<double, BX_RESID>(ctx, W, W.all, W.vals64, W.x, nullptr, W.b,
-                                        static_cast<float*>(W.r), W.grid64)));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(bt->boxes, bt->hd.data(), sizeof(BoxDesc) * nbox, cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(bt->st, hs.data(), sizeof(BoxSt) * nbox, cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(bt->ctl, &hc, sizeof(BatchCtl), cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(R.all.ids, hl.data(), sizeof(int) * hl.size(), cudaMemcpyHostToDevice, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(bt->x, 0, sizeof(double) * rows8, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(bt->r, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(bt->p, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(bt->Ap, 0, vb, ctx->stream));
+  if (R.mixed) MFE_CUDA_TRY(ctx, cudaMemsetAsync(bt->x32, 0, sizeof(float) * rows8, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
+
+  // r = b - A x0 over all boxes, then the open list
+  if (R.mixed)
+    MFE_TRY(bx_spmv64<BX_RESID>(ctx, R, R.all, bt->x, nullptr, bt->b, static_cast<float*>(bt->r)));
   else
-    MFE_TRY((bx_spmv<double, BX_RESID>(ctx, W, W.all, W.vals64, W.x, static_cast<double*>(W.r),
-                                        W.b, nullptr, W.grid64)));
-  k_bx_init<<<1, 1024, 0, ctx->stream>>>(W.boxes, W.st, W.ctl, W.open);
+    MFE_TRY(bx_spmv64<BX_RESID>(ctx, R, R.all, bt->x, static_cast<double*>(bt->r), bt->b, nullptr));
+  k_bx_init<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open);
   MFE_TRY(check_launch(ctx, "k_bx_init"));
-  cudaEvent_t ev_solve0 = nullptr, ev_solve1 = nullptr;
-  MFE_CUDA_TRY(ctx, cudaEventCreate(&ev_solve0));
-  MFE_CUDA_TRY(ctx, cudaEventCreate(&ev_solve1));
-  MFE_CUDA_TRY(ctx, cudaEventRecord(ev_solve0, ctx->stream));
+  MFE_TRY(bx_loop(ctx, bt->ctl, [&](cudaGraphConditionalHandle h, int in_graph) -> mfe_status {
+    return R.mixed ? bx_iter_mixed(ctx, R, h, in_graph) : bx_iter_f64(ctx, R, h, in_graph);
+  }));
+  MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
 
-  // ---- iterations ----
-  auto body = [&](cudaGraphConditionalHandle h, int in_graph) -> mfe_status {
-    return mixed ? bx_iter_mixed(ctx, W, h, in_graph) : bx_iter_f64(ctx, W, h, in_graph);
-  };
-  mfe_status st = MFE_OK;
-  if (getenv("MFE_CG_EAGER") != nullptr) {
-    BatchCtl* hctl = static_cast<BatchCtl*>(host_scratch(ctx, sizeof(BatchCtl)));
-    if (!hctl) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
-    for (;;) {
-      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hctl, W.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, ctx->stream));
-      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      if (!hctl->cont) break;
-      MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
+  // results
+  if (x_out) {
+    int64_t out = 0;
+    for (int i = 0; i < nbox; ++i) {
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(x_out + out, bt->x + bt->hd[i].row_base,
+                                        sizeof(double) * bt->hd[i].n, cudaMemcpyDeviceToDevice, ctx->stream));
+      out += bt->hd[i].n;
     }
-  } else {
-    cudaStream_t run_stream = ctx->stream, s = ctx->own_stream;
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t ex = nullptr;
-    cudaGraphConditionalHandle h = 0;
-    cudaError_t e = cudaGraphCreate(&g, 0);
-    if (e == cudaSuccess) e = cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault);
-    if (e == cudaSuccess) {
-      ctx->stream = s;
-      e = cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-      if (e == cudaSuccess) {
-        k_bx_begin<<<1, 1, 0, s>>>(W.ctl, h);
-        e = cudaStreamEndCapture(s, &g);
-      }
-      cudaGraphNode_t nodes[4];
-      size_t nn = 4;
-      if (e == cudaSuccess) e = cudaGraphGetNodes(g, nodes, &nn);
-      alignas(cudaGraphNodeParams) unsigned char cp_buf[sizeof(cudaGraphNodeParams)];
-      memset(cp_buf, 0, sizeof(cp_buf));
-      cudaGraphNodeParams* cp = reinterpret_cast<cudaGraphNodeParams*>(cp_buf);
-      cp->type = cudaGraphNodeTypeConditional;
-      cp->conditional.handle = h;
-      cp->conditional.type = cudaGraphCondTypeWhile;
-      cp->conditional.size = 1;
-      cudaGraphNode_t cnode;
-      if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
-      if (e == cudaSuccess) {
-        cudaGraph_t bg = cp->conditional.phGraph_out[0];
-        e = cudaStreamBeginCaptureToGraph(s, bg, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
-        if (e == cudaSuccess) {
-          st = body(h, 1);
-          cudaGraph_t tmp;
-          const cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
-          if (e == cudaSuccess) e = e2;
-        }
-      }
-      ctx->stream = run_stream;
-      if (e == cudaSuccess && st == MFE_OK) e = cudaGraphInstantiate(&ex, g, 0);
-      if (e == cudaSuccess && st == MFE_OK) e = cudaGraphLaunch(ex, ctx->stream);
-    }
-    if (ex) cudaGraphExecDestroy(ex);
-    if (g) cudaGraphDestroy(g);
-    if (st != MFE_OK) return st;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "batched CG graph");
   }
-  MFE_CUDA_TRY(ctx, cudaEventRecord(ev_solve1, ctx->stream));
-
-  // ---- results ----
-  int64_t out = 0;
-  for (int i = 0; i < nbox; ++i) {
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(x_out + out, W.x + hd[i].row_base, sizeof(double) * hd[i].n,
-                                      cudaMemcpyDeviceToDevice, ctx->stream));
-    out += hd[i].n;
-  }
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), W.st, sizeof(BoxSt) * nbox, cudaMemcpyDeviceToHost, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&hc, W.ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs.data(), bt->st, sizeof(BoxSt) * nbox, cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&hc, bt->ctl, sizeof(BatchCtl), cudaMemcpyDeviceToHost, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  float ms_asm = 0.f, ms_solve = 0.f;
-  cudaEventElapsedTime(&ms_asm, ctx->ev0, ctx->ev1);
-  cudaEventElapsedTime(&ms_solve, ev_solve0, ev_solve1);
-  cudaEventDestroy(ev_solve0);
-  cudaEventDestroy(ev_solve1);
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   if (hc.err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during the batched solve");
   mfe_status worst = MFE_OK;
   for (int i = 0; i < nbox; ++i) {
@@ -1180,13 +1323,23 @@ mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const 
     r.normr = s.normr;
     r.normr0 = s.normr0;
     r.final_resid = s.normr;
-    r.times[0] = ms_asm * 1e-3;  // assembly of the whole batch
-    r.times[4] = ms_solve * 1e-3;
+    r.times[0] = bt->assembly_s;  // assembly of the whole batch
+    r.times[4] = ms * 1e-3;       // the batched solve
     r.refinements = hc.updates;
     r.status = s.brk ? MFE_BREAKDOWN : (s.normr <= s.tol_abs ? MFE_OK : MFE_MAXITER);
     if (r.status != MFE_OK && worst == MFE_OK) worst = (mfe_status)r.status;
   }
   return worst;
+}
+
+mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const mfe_cg_opts* o,
+                             double* x_out, mfe_cg_result* results)
+{
+  mfe_batch* bt = nullptr;
+  MFE_TRY(batch_create(ctx, nbox, dims, &bt));
+  const mfe_status st = batch_solve(ctx, bt, o, x_out, results);
+  batch_destroy(bt);
+  return st;
 }
 
 }  // namespace mfe

@@ -105,6 +105,13 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64, int nrhs, const double* B,
                     const mfe_cg_opts* opts, mfe_cg_result* results);
 
 // ---- batched uneven boxes (mfe_batch.cu) ----
+mfe_status batch_create(mfe_ctx* ctx, int nbox, const int32_t* dims, mfe_batch** out);
+void batch_destroy(mfe_batch* bt);
+void batch_info(const mfe_batch* bt, int64_t* rows, int64_t* nnz, double* assembly_s,
+                mfe_batch_tuning* tuning);
+mfe_status batch_set_tuning(mfe_ctx* ctx, mfe_batch* bt, const mfe_batch_tuning* t);
+mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* opts, double* x_out,
+                       mfe_cg_result* results);
 mfe_status batch_solve_boxes(mfe_ctx* ctx, int nbox, const int32_t* dims, const mfe_cg_opts* opts,
                              double* x_out, mfe_cg_result* results);
 

@@ -1,0 +1,69 @@
+"""The autotuner's search and cache logic, driven by a stand-in batch whose
+solve times come from a table (no GPU)."""
+import pytest
+
+from minife_gb300 import autotune
+
+
+class _Res:
+    def __init__(self, t, status=0):
+        self.times = (0.0, 0.0, 0.0, 0.0, t)
+        self.status = status
+
+
+class FakeBatch:
+    """solve() time: a function of the current shape/chunk (capped runs) or
+    of refine_k (full runs)."""
+
+    def __init__(self):
+        self.dims = [(4, 5, 6), (7, 3, 9)]
+        self.tuning = None
+        self.calls = []
+
+    def set_tuning(self, rows, stages, chunk):
+        self.tuning = (rows, stages, chunk)
+
+    def solve(self, max_iter, tol, tol_mode, precision, refine_k):
+        rows, stages, chunk = self.tuning
+        self.calls.append((self.tuning, max_iter, tol, refine_k))
+        if tol == 0.0:  # capped probe: shape (128, 3) and chunk 16384 are fastest
+            t = 1.0 + 0.1 * abs(rows - 128) / 128 + 0.05 * abs(stages - 3) + \
+                0.01 * abs(chunk - 16384) / 16384
+            return None, [_Res(t, 5)] * 2
+        # full solves: refine_k 100 fastest but does not converge, 50 next
+        t = {25: 3.0, 50: 2.0, 100: 1.0}[refine_k]
+        return None, [_Res(t, 0 if refine_k != 100 else 5)] * 2
+
+
+@pytest.fixture
+def cache(tmp_path, monkeypatch):
+    monkeypatch.setenv("MFE_TUNE_CACHE", str(tmp_path / "tune.json"))
+    monkeypatch.setattr(autotune, "_device_key", lambda: "fake/sm1")
+    return tmp_path / "tune.json"
+
+
+def test_search_picks_fastest_converging(cache):
+    b = FakeBatch()
+    cfg = autotune.tune_batch(b, probe_iters=5, reps=1)
+    assert (cfg["spmv_rows"], cfg["spmv_stages"], cfg["chunk_rows"]) == (128, 3, 16384)
+    assert cfg["refine_k"] == 50           # 100 is faster but did not converge
+    assert b.tuning == (128, 3, 16384)     # applied to the batch
+    assert not cfg["cached"] and cache.exists()
+    assert all(c[1] == 5 for c in b.calls if c[2] == 0.0)  # capped probes
+
+
+def test_cache_hit_skips_search(cache):
+    b = FakeBatch()
+    autotune.tune_batch(b, probe_iters=5, reps=1)
+    b2 = FakeBatch()
+    cfg = autotune.tune_batch(b2, probe_iters=5, reps=1)
+    assert cfg["cached"] and b2.calls == [] and b2.tuning == (128, 3, 16384)
+    assert autotune.lookup(b.dims, "mixed")["refine_k"] == 50
+    # another workload or precision is another entry
+    assert autotune.lookup([(4, 5, 6)], "mixed") is None
+    assert autotune.lookup(b.dims, "f64") is None
+
+
+def test_signature_ignores_box_order(cache):
+    assert autotune.signature([(1, 2, 3), (4, 5, 6)], "mixed") == \
+        autotune.signature([(4, 5, 6), (1, 2, 3)], "mixed")

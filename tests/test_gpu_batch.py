@@ -87,3 +87,48 @@ def test_batch_rejects_bad_dims():
     with pytest.raises(M.MiniFEError) as ei:
         M.batch_solve_boxes([(4, 4, 4), (0, 3, 3)])
     assert ei.value.status == 1
+
+
+def test_batch_handle_shapes_agree():
+    """One assembled batch solved at every launch shape: FP64 results are
+    identical up to dot-product order (iterations within 1), and the C entry
+    point mfe_batch_solve_boxes gives the handle's answer."""
+    import ctypes
+    from minife_gb300 import _abi
+    dims = [(9, 7, 5), (3, 12, 6), (10, 4, 4)]
+    b = M.Batch(dims)
+    x0, r0 = b.solve(max_iter=500, tol=1e-10, tol_mode="relative", precision="f64")
+    x0 = x0.clone()
+    for rows, stages, chunk in [(128, 2, 1024), (128, 4, 4096), (256, 3, 1 << 20)]:
+        b.set_tuning(rows, stages, chunk)
+        for prec in ("f64", "mixed"):
+            x, r = b.solve(max_iter=3000, tol=1e-10, tol_mode="relative", precision=prec)
+            assert all(ri.status == 0 for ri in r)
+            if prec == "f64":
+                assert all(abs(ri.num_iters - rj.num_iters) <= 1 for ri, rj in zip(r, r0))
+                assert torch.allclose(x, x0, rtol=0, atol=1e-9)
+    assert b.info()[3] == {"spmv_rows": 256, "spmv_stages": 3, "chunk_rows": 1 << 20}
+    with pytest.raises(M.MiniFEError):
+        b.set_tuning(96, 2, 8192)
+    b.close()
+    ctx = M.default_context()
+    flat = (ctypes.c_int32 * 9)(*[v for d in dims for v in d])
+    o, _ = M._opts(500, 1e-10, "relative", "f64")
+    res = (_abi.MfeCgResult * 3)()
+    xc = torch.empty_like(x0)
+    assert ctx.lib.mfe_batch_solve_boxes(ctx.h, 3, flat, ctypes.byref(o), M._ptr(xc), res) == 0
+    assert torch.allclose(xc, x0, rtol=0, atol=1e-12)
+
+
+def test_autotune_small_batch(tmp_path, monkeypatch):
+    from minife_gb300 import autotune
+    monkeypatch.setenv("MFE_TUNE_CACHE", str(tmp_path / "tune.json"))
+    b = M.Batch([(12, 10, 8), (6, 6, 6), (16, 5, 7)])
+    cfg = autotune.tune_batch(b, probe_iters=5, reps=1)
+    assert (cfg["spmv_rows"], cfg["spmv_stages"]) in autotune.SHAPES
+    assert cfg["chunk_rows"] in autotune.CHUNKS and cfg["refine_k"] in autotune.REFINE_K
+    x, res = b.solve(max_iter=3000, tol=1e-8, tol_mode="relative", precision="mixed",
+                     refine_k=cfg["refine_k"])
+    assert all(r.status == 0 for r in res)
+    assert autotune.tune_batch(b)["cached"]
+    b.close()
