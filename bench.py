@@ -364,9 +364,27 @@ def run_gpu(args):
                  "dtype": "f32 matrix/vectors, f64 dots/scalars/solution"}
         del A32, xm, x64
 
-    cpu = None
+    # launches of the timed headline region: per CG iteration the SpMV, the
+    # update and the p update, plus the initial residual and setup per solve
+    gpu_launches = args.steps * (3 * res.num_iters + 2)
+
+    # batched uneven boxes and multi-RHS: measured after the headline system
+    # is released, so their stores have the memory
+    batch = multi = None
     if rank == 0 and not args.no_cpu:
         ro, cols, vals, bh = host_system(A, b)
+    else:
+        ro = cols = vals = bh = None
+    if not args.no_batch or not args.no_multi:
+        del A, b, x, p, Ap
+        torch.cuda.empty_cache()
+        if not args.no_batch:
+            batch = bench_batch(args, world, stream)
+        if not args.no_multi:
+            multi = bench_multi(args, world, stream)
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
         dt, threads = cpu_cg_sample(ro, cols, vals, bh, args.cpu_sample)
         per_it = dt / args.cpu_sample
         cpu = {"value": per_it * res.num_iters, "unit": "s", "cores": threads, "kind": "port",
@@ -391,6 +409,8 @@ def run_gpu(args):
             "cg_effective_gbs": iter_bytes * res.num_iters / t_step / 1e9,
             "assembly_s": t_assembly,
             "mixed": mixed,
+            "batch": batch,
+            "multi_rhs": multi,
             "spmv_f64_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -404,11 +424,113 @@ def run_gpu(args):
                                               "peak measured with an FMA-only kernel"}},
             "e2e": e2e,
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps * (3 * res.num_iters + 2),
+            "gpu_launches": gpu_launches,
             "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     return 0
+
+
+def batch_dims(nbox=96, lo=32, hi=160, seed=20261204):
+    """Seeded uneven boxes: nx, ny, nz uniform in {lo..hi}."""
+    import numpy as np
+    rng = np.random.default_rng(seed)
+    return [tuple(int(v) for v in rng.integers(lo, hi + 1, size=3)) for _ in range(nbox)]
+
+
+def bench_batch(args, world, stream):
+    """96 uneven boxes (seeded, each dimension uniform in 32..160), each with
+    the miniFE right-hand side, assembled once and solved together in mixed
+    precision to 1e-8 relative (every box stopping on its true FP64
+    residual), launch shape and refine_k from the autotuner.  Timed: the
+    batched solve (one graph launch) per step; the sequential baseline is
+    the same boxes solved one after another with the single-box mixed
+    solver."""
+    import torch
+    import minife_gb300 as M
+    from minife_gb300 import autotune
+    dims = batch_dims()
+    bt = M.Batch(dims)
+    rows, nnz, t_asm, _ = bt.info()
+    cfg = autotune.tune_batch(bt, precision="mixed", tol=TOL, probe_iters=30, reps=1)
+    x = torch.empty(bt.offsets[-1], dtype=torch.float64, device="cuda")
+    for _ in range(max(1, args.warmup - 1)):
+        bt.solve(max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed",
+                 refine_k=cfg["refine_k"], x=x)
+    torch.cuda.synchronize()
+    barrier(world)
+    ts = []
+    for _ in range(args.steps):
+        _, res = bt.solve(max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed",
+                          refine_k=cfg["refine_k"], x=x)
+        ts.append(res[0].times[4])
+    barrier(world)
+    t = max_over_ranks(world, sum(ts) / len(ts))
+    its = [r.num_iters for r in res]
+    work = sum(r.num_iters * M.box_dims(*d)[1] for r, d in zip(res, dims))
+    _, res64 = bt.solve(max_iter=5000, tol=TOL, tol_mode="relative", precision="f64", x=x)
+    out = {"boxes": len(dims), "dims": "seeded U{32..160}^3 (numpy default_rng(20261204))",
+           "rows": rows, "nnz": nnz, "assembly_s": t_asm, "value": t, "unit": "s",
+           "tuning": {k: cfg[k] for k in ("spmv_rows", "spmv_stages", "chunk_rows", "refine_k")},
+           "tuned_from_cache": cfg.get("cached", False),
+           "iterations": {"min": min(its), "max": max(its)},
+           "all_converged": all(r.status == 0 for r in res),
+           "max_rel_resid": max(r.final_resid / r.normr0 for r in res),
+           "nnz_iterations_per_s": work / t,
+           "fp64_batched_s": res64[0].times[4]}
+    bt.close()
+    del x
+    if not args.no_seq:
+        t_seq = 0.0
+        for d in dims:
+            A, b = M.build_system(*d)
+            xx = torch.zeros_like(b)
+            r = M.cg_solve(A, b, xx, max_iter=5000, tol=TOL, tol_mode="relative",
+                           precision="mixed", refine_k=50)
+            t_seq += r.total_time
+            del A, b, xx
+        out["sequential_mixed_s"] = t_seq
+        out["speedup_vs_sequential"] = t_seq / t
+    return out
+
+
+def bench_multi(args, world, stream):
+    """32 seeded random-normal right-hand sides on the 128^3 system, solved
+    together (one SpMM per iteration) in mixed precision to 1e-8 relative."""
+    import torch
+    import minife_gb300 as M
+    A, b = M.build_system(128, 128, 128)
+    g = torch.Generator(device="cpu").manual_seed(0)
+    B = torch.randn(A.nrows, 32, generator=g, dtype=torch.float64).cuda().contiguous()
+    X = torch.zeros_like(B)
+    for _ in range(max(1, args.warmup - 1)):
+        X.zero_()
+        M.cg_solve_multi(A, B, X, max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed")
+    torch.cuda.synchronize()
+    barrier(world)
+    ts = []
+    for _ in range(args.steps):
+        X.zero_()
+        res = M.cg_solve_multi(A, B, X, max_iter=5000, tol=TOL, tol_mode="relative",
+                               precision="mixed")
+        ts.append(res[0].times[4])
+    t = max_over_ranks(world, sum(ts) / len(ts))
+    out = {"rhs": 32, "system": "128^3", "value": t, "unit": "s",
+           "iterations_max": max(r.num_iters for r in res),
+           "reliable_updates": res[0].refinements,
+           "all_converged": all(r.status == 0 for r in res),
+           "max_rel_resid": max(r.final_resid / r.normr0 for r in res)}
+    if not args.no_seq:
+        t_seq = 0.0
+        for j in range(32):
+            bj = B[:, j].contiguous()
+            xj = torch.zeros_like(bj)
+            r = M.cg_solve(A, bj, xj, max_iter=5000, tol=TOL, tol_mode="relative",
+                           precision="mixed", refine_k=50)
+            t_seq += r.total_time
+        out["sequential_mixed_s"] = t_seq
+        out["speedup_vs_sequential"] = t_seq / t
+    return out
 
 
 def run_probe(args):
@@ -457,6 +579,12 @@ def main():
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-mixed", action="store_true")
+    ap.add_argument("--no-batch", action="store_true",
+                    help="skip the 96-box batched solve")
+    ap.add_argument("--no-multi", action="store_true",
+                    help="skip the 32-right-hand-side solve")
+    ap.add_argument("--no-seq", action="store_true",
+                    help="skip the sequential baselines of the batched and multi-RHS solves")
     ap.add_argument("--refine-k", type=int, default=50,
                     help="mixed solver: reliable update at least every k inner iterations")
     ap.add_argument("--cpu-sample", type=int, default=20)
