@@ -14,7 +14,8 @@
 // multi-rank ones have no effect on one GPU).  GB300 keys: precision (f64 |
 // mixed), max_iters (default 200, driver.hpp:241), abs_tol (default
 // DBL_EPSILON, driver.hpp:245), rel_tol (overrides abs_tol: stop at
-// ||r|| <= rel_tol ||r0||), refine_k (mixed solver).
+// ||r|| <= rel_tol ||r0||), refine_k (mixed solver), kernels (1: the
+// reference's MINIFE_KERNELS timing loops instead of the CG solve).
 #include <sys/utsname.h>
 #include <unistd.h>
 
@@ -85,7 +86,7 @@ void check(mfe_ctx* ctx, mfe_status s, const char* what)
 }
 
 struct Params {
-  int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads;
+  int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads, kernels;
   float load_imbalance;
   std::string name, precision;
   int max_iters, refine_k;
@@ -124,6 +125,7 @@ int main(int argc, char** argv)
   p.abs_tol = parse_parameter<double>(as, "abs_tol", std::numeric_limits<double>::epsilon());
   p.rel_tol = parse_parameter<double>(as, "rel_tol", 0.0);
   p.refine_k = parse_parameter<int>(as, "refine_k", 0);
+  p.kernels = parse_parameter<int>(as, "kernels", 0);
 
   // print_params=1 on the command line: print the parsed parameters and stop
   // (no GPU needed); an input_file replaces the other arguments, as in the
@@ -244,111 +246,173 @@ int main(int argc, char** argv)
     ma->add("NNZ per proc AVG", (double)nnz);
   }
 
-  // x = 0 (Vector is zero-filled, ref/src/Vector.hpp:49-51)
-  check(ctx, mfe_waxpby(ctx, nrows, 0.0, b, 0.0, b, x), "mfe_waxpby");
-
-  mfe_cg_opts o;
-  mfe_cg_opts_default(&o);
-  o.max_iter = p.max_iters;
-  o.tol = p.abs_tol;
-  if (p.rel_tol > 0) {
-    o.tol = p.rel_tol;
-    o.tol_mode = MFE_TOL_RELATIVE;
-  }
-  o.precision = p.precision == "mixed" ? MFE_PREC_MIXED : MFE_PREC_F64;
-  o.refine_k = p.refine_k;
-  std::cout << "Starting CG solver ... " << std::endl;
-  mfe_cg_result r;
-  const mfe_status st = mfe_cg_solve(ctx, &A, b, x, &o, &r);
-  if (st == MFE_BREAKDOWN) std::cerr << "miniFE::cg_solve ERROR, numerical breakdown!" << std::endl;
-  else if (st != MFE_OK && st != MFE_MAXITER) check(ctx, st, "mfe_cg_solve");
-  std::cout << "Initial Residual = " << r.normr0 << std::endl;
-  std::cout << "Final Resid Norm: " << r.normr << std::endl;
-
   int verify_result = 0;
-  if (p.verify_solution > 0) {
-    std::cout << "verifying solution at ~ (0.5, 0.5, 0.5) ..." << std::endl;
-    double max_err = 0;
-    int passed = 0;
-    check(ctx, mfe_verify_solution(ctx, p.nx, p.ny, p.nz, x, 0.06, 0, &max_err, &passed),
-          "mfe_verify_solution");
-    if (passed) std::cout << "solution matches analytic solution to within 0.06 or better." << std::endl;
-    else std::cout << "max absolute error is " << max_err << ":" << std::endl;
-    verify_result = passed ? 0 : 1;
-  }
-
-  // per-operation times: the solve fuses the operations into three kernels
-  // per iteration, so each operation is timed alone on the solved system and
-  // scaled by the reference's operation counts (driver.hpp:331-335)
-  const int it = r.num_iters;
-  double t_mv = 0, t_dot = 0, t_wax = 0;
-  {
-    double* w = nullptr;
-    check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&w), "mfe_device_alloc");
-    double d = 0;
-    const int reps = 5;
-    check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+  if (p.kernels) {
+    // kernel timing mode (ref/src/time_kernels.hpp:42-134, driver.hpp:257-272,
+    // compiled in by MINIFE_KERNELS there, a run-time key here): x = 0 with
+    // x[0] = 0.9, then 500 waxpby(1, x, 0, x, p), 500 matvec(A, p, x) and 500
+    // dot(x, p) accumulated into the reported "Final Resid Norm"
+    std::cout.width(30);
+    std::cout << "Starting kernel timing loops ..." << std::endl;
+    const int iters = 500;
+    double* pv = nullptr;
+    check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&pv), "mfe_device_alloc");
+    check(ctx, mfe_waxpby(ctx, nrows, 0.0, b, 0.0, b, x), "mfe_waxpby");
+    check(ctx, mfe_waxpby(ctx, nrows, 0.0, b, 0.0, b, pv), "mfe_waxpby");
+    const double x0 = 0.9;
+    check(ctx, mfe_memcpy_h2d(ctx, x, &x0, sizeof(double)), "mfe_memcpy_h2d");
     check(ctx, mfe_synchronize(ctx), "sync");
     double s0 = now();
-    for (int i = 0; i < reps; ++i) check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+    for (int i = 0; i < iters; ++i) check(ctx, mfe_waxpby(ctx, nrows, 1.0, x, 0.0, x, pv), "mfe_waxpby");
     check(ctx, mfe_synchronize(ctx), "sync");
-    t_mv = (now() - s0) / reps;
+    const double t_wax = now() - s0;
     s0 = now();
-    for (int i = 0; i < reps; ++i) check(ctx, mfe_dot(ctx, nrows, x, w, &d), "mfe_dot");
-    t_dot = (now() - s0) / reps;
-    s0 = now();
-    for (int i = 0; i < reps; ++i) check(ctx, mfe_waxpby(ctx, nrows, 1.0, x, 0.5, w, w), "mfe_waxpby");
+    for (int i = 0; i < iters; ++i) check(ctx, mfe_spmv(ctx, &A, pv, x), "mfe_spmv");
     check(ctx, mfe_synchronize(ctx), "sync");
-    t_wax = (now() - s0) / reps;
-    mfe_device_free(ctx, w);
-  }
-  const double total = r.times[4];
-  // driver.hpp:314-401, with global_nrows = nx*ny*nz as in the reference
-  grp->add("ScalarType", "double");
-  grp->add("GlobalOrdinalType", "int");
-  grp->add("LocalOrdinalType", "int");
-  auto* cg = doc.add("CG solve", "");
-  cg->add("Iterations", it);
-  cg->add("Final Resid Norm", r.normr);
-  const double global_nrows = (double)p.nx * p.ny * p.nz;
-  double mv_flops = (double)nnz * 2.0 * (it + 1);
-  double dot_flops = global_nrows * 2.0 * (2 * it);
-  double waxpy_flops = global_nrows * 3.0 * (3 * it + 2);
-  const double tw = t_wax * (3 * it + 2), td = t_dot * (2 * it), tm = t_mv * (it + 1);
-  auto mflops = [](double f, double t) { return t > 1e-4 ? 1e-6 * f / t : -1.0; };
-  auto add_rate = [&](const char* key, double f, double t) {
-    const double m = mflops(f, t);
-    if (m >= 0) cg->add(key, m);
-    else cg->add(key, "inf");
-  };
-  cg->add("WAXPY Time", tw);
-  cg->add("WAXPY Flops", waxpy_flops);
-  add_rate("WAXPY Mflops", waxpy_flops, tw);
-  cg->add("DOT Time", td);
-  cg->add("DOT Flops", dot_flops);
-  add_rate("DOT Mflops", dot_flops, td);
-  cg->add("MATVEC Time", tm);
-  cg->add("MATVEC Flops", mv_flops);
-  add_rate("MATVEC Mflops", mv_flops, tm);
-  auto* tot = cg->add("Total", "");
-  const double total_flops = mv_flops + dot_flops + waxpy_flops;
-  tot->add("Total CG Time", total);
-  tot->add("Total CG Flops", total_flops);
-  const double tm_rate = mflops(total_flops, total);
-  if (tm_rate >= 0) tot->add("Total CG Mflops", tm_rate);
-  else tot->add("Total CG Mflops", "inf");
-  cg->add("Time per iteration", it > 0 ? total / it : 0.0);
+    const double t_mv = now() - s0;
+    s0 = now();
+    double xdotp = 0.0;
+    for (int i = 0; i < iters; ++i) {
+      double d = 0.0;
+      check(ctx, mfe_dot(ctx, nrows, x, pv, &d), "mfe_dot");
+      xdotp += d;
+    }
+    const double t_dot = now() - s0;
+    mfe_device_free(ctx, pv);
+    grp->add("ScalarType", "double");
+    grp->add("GlobalOrdinalType", "int");
+    grp->add("LocalOrdinalType", "int");
+    auto* kt = doc.add("Kernel timings", "");
+    kt->add("Iterations", iters);
+    kt->add("Final Resid Norm", xdotp);
+    // one of each operation per iteration (driver.hpp:337-342)
+    const double global_nrows = (double)p.nx * p.ny * p.nz;
+    const double mv_flops = (double)nnz * 2.0 * iters;
+    const double dot_flops = global_nrows * 2.0 * iters;
+    const double waxpy_flops = global_nrows * 3.0 * iters;
+    auto add_rate = [&](const char* key, double f, double t) {
+      if (t > 1e-4) kt->add(key, 1e-6 * f / t);
+      else kt->add(key, "inf");
+    };
+    kt->add("WAXPY Time", t_wax);
+    kt->add("WAXPY Flops", waxpy_flops);
+    add_rate("WAXPY Mflops", waxpy_flops, t_wax);
+    kt->add("DOT Time", t_dot);
+    kt->add("DOT Flops", dot_flops);
+    add_rate("DOT Mflops", dot_flops, t_dot);
+    kt->add("MATVEC Time", t_mv);
+    kt->add("MATVEC Flops", mv_flops);
+    add_rate("MATVEC Mflops", mv_flops, t_mv);
+    auto* gpu = doc.add("GB300", "");
+    gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) * iters / t_mv * 1e-9);
+    gpu->add("DOT GB/s (host-synchronous calls)", 16.0 * nrows * iters / t_dot * 1e-9);
+    gpu->add("WAXPY GB/s", 24.0 * nrows * iters / t_wax * 1e-9);
+  } else {
+    // x = 0 (Vector is zero-filled, ref/src/Vector.hpp:49-51)
+    check(ctx, mfe_waxpby(ctx, nrows, 0.0, b, 0.0, b, x), "mfe_waxpby");
 
-  auto* gpu = doc.add("GB300", "");
-  gpu->add("precision", p.precision);
-  gpu->add("tolerance mode", p.rel_tol > 0 ? "relative" : "absolute");
-  gpu->add("tolerance", o.tol);
-  gpu->add("Initial Resid Norm", r.normr0);
-  gpu->add("True Final Resid Norm", r.final_resid);
-  gpu->add("reliable updates", r.refinements);
-  gpu->add("op times", "standalone kernels scaled by operation counts");
-  gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) / t_mv * 1e-9);
-  if (p.verify_solution > 0) gpu->add("verification", verify_result == 0 ? "passed" : "failed");
+    mfe_cg_opts o;
+    mfe_cg_opts_default(&o);
+    o.max_iter = p.max_iters;
+    o.tol = p.abs_tol;
+    if (p.rel_tol > 0) {
+      o.tol = p.rel_tol;
+      o.tol_mode = MFE_TOL_RELATIVE;
+    }
+    o.precision = p.precision == "mixed" ? MFE_PREC_MIXED : MFE_PREC_F64;
+    o.refine_k = p.refine_k;
+    std::cout << "Starting CG solver ... " << std::endl;
+    mfe_cg_result r;
+    const mfe_status st = mfe_cg_solve(ctx, &A, b, x, &o, &r);
+    if (st == MFE_BREAKDOWN) std::cerr << "miniFE::cg_solve ERROR, numerical breakdown!" << std::endl;
+    else if (st != MFE_OK && st != MFE_MAXITER) check(ctx, st, "mfe_cg_solve");
+    std::cout << "Initial Residual = " << r.normr0 << std::endl;
+    std::cout << "Final Resid Norm: " << r.normr << std::endl;
+
+      if (p.verify_solution > 0) {
+      std::cout << "verifying solution at ~ (0.5, 0.5, 0.5) ..." << std::endl;
+      double max_err = 0;
+      int passed = 0;
+      check(ctx, mfe_verify_solution(ctx, p.nx, p.ny, p.nz, x, 0.06, 0, &max_err, &passed),
+            "mfe_verify_solution");
+      if (passed) std::cout << "solution matches analytic solution to within 0.06 or better." << std::endl;
+      else std::cout << "max absolute error is " << max_err << ":" << std::endl;
+      verify_result = passed ? 0 : 1;
+    }
+
+    // per-operation times: the solve fuses the operations into three kernels
+    // per iteration, so each operation is timed alone on the solved system and
+    // scaled by the reference's operation counts (driver.hpp:331-335)
+    const int it = r.num_iters;
+    double t_mv = 0, t_dot = 0, t_wax = 0;
+    {
+      double* w = nullptr;
+      check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&w), "mfe_device_alloc");
+      double d = 0;
+      const int reps = 5;
+      check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+      check(ctx, mfe_synchronize(ctx), "sync");
+      double s0 = now();
+      for (int i = 0; i < reps; ++i) check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+      check(ctx, mfe_synchronize(ctx), "sync");
+      t_mv = (now() - s0) / reps;
+      s0 = now();
+      for (int i = 0; i < reps; ++i) check(ctx, mfe_dot(ctx, nrows, x, w, &d), "mfe_dot");
+      t_dot = (now() - s0) / reps;
+      s0 = now();
+      for (int i = 0; i < reps; ++i) check(ctx, mfe_waxpby(ctx, nrows, 1.0, x, 0.5, w, w), "mfe_waxpby");
+      check(ctx, mfe_synchronize(ctx), "sync");
+      t_wax = (now() - s0) / reps;
+      mfe_device_free(ctx, w);
+    }
+    const double total = r.times[4];
+    // driver.hpp:314-401, with global_nrows = nx*ny*nz as in the reference
+    grp->add("ScalarType", "double");
+    grp->add("GlobalOrdinalType", "int");
+    grp->add("LocalOrdinalType", "int");
+    auto* cg = doc.add("CG solve", "");
+    cg->add("Iterations", it);
+    cg->add("Final Resid Norm", r.normr);
+    const double global_nrows = (double)p.nx * p.ny * p.nz;
+    double mv_flops = (double)nnz * 2.0 * (it + 1);
+    double dot_flops = global_nrows * 2.0 * (2 * it);
+    double waxpy_flops = global_nrows * 3.0 * (3 * it + 2);
+    const double tw = t_wax * (3 * it + 2), td = t_dot * (2 * it), tm = t_mv * (it + 1);
+    auto mflops = [](double f, double t) { return t > 1e-4 ? 1e-6 * f / t : -1.0; };
+    auto add_rate = [&](const char* key, double f, double t) {
+      const double m = mflops(f, t);
+      if (m >= 0) cg->add(key, m);
+      else cg->add(key, "inf");
+    };
+    cg->add("WAXPY Time", tw);
+    cg->add("WAXPY Flops", waxpy_flops);
+    add_rate("WAXPY Mflops", waxpy_flops, tw);
+    cg->add("DOT Time", td);
+    cg->add("DOT Flops", dot_flops);
+    add_rate("DOT Mflops", dot_flops, td);
+    cg->add("MATVEC Time", tm);
+    cg->add("MATVEC Flops", mv_flops);
+    add_rate("MATVEC Mflops", mv_flops, tm);
+    auto* tot = cg->add("Total", "");
+    const double total_flops = mv_flops + dot_flops + waxpy_flops;
+    tot->add("Total CG Time", total);
+    tot->add("Total CG Flops", total_flops);
+    const double tm_rate = mflops(total_flops, total);
+    if (tm_rate >= 0) tot->add("Total CG Mflops", tm_rate);
+    else tot->add("Total CG Mflops", "inf");
+    cg->add("Time per iteration", it > 0 ? total / it : 0.0);
+
+    auto* gpu = doc.add("GB300", "");
+    gpu->add("precision", p.precision);
+    gpu->add("tolerance mode", p.rel_tol > 0 ? "relative" : "absolute");
+    gpu->add("tolerance", o.tol);
+    gpu->add("Initial Resid Norm", r.normr0);
+    gpu->add("True Final Resid Norm", r.final_resid);
+    gpu->add("reliable updates", r.refinements);
+    gpu->add("op times", "standalone kernels scaled by operation counts");
+    gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) / t_mv * 1e-9);
+    if (p.verify_solution > 0) gpu->add("verification", verify_result == 0 ? "passed" : "failed");
+  }
 
   mfe_device_free(ctx, b);
   mfe_device_free(ctx, x);

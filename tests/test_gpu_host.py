@@ -71,6 +71,24 @@ def test_minife_x_mixed_relative(tmp_path):
     assert true_res <= 1e-8 * r0
 
 
+def test_minife_x_kernel_timing_mode(tmp_path):
+    """kernels=1: the reference's MINIFE_KERNELS loops (time_kernels.hpp):
+    500 of each operation with x = 0.9 e_0, so every dot is p.A p = 0.81 A_00
+    (row 0 is a Dirichlet row: A_00 = 1) and the reported norm is their sum."""
+    r, yml = run_driver(tmp_path, "nx=12", "ny=10", "nz=8", "kernels=1")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert "Starting kernel timing loops" in r.stdout
+    keys = yaml_keys(yml)
+    for k in ("0:Kernel timings", "2:Iterations", "2:WAXPY Time", "2:DOT Time",
+              "2:MATVEC Time", "2:MATVEC Mflops"):
+        assert k in keys, k
+    assert "0:CG solve" not in keys
+    assert int(yaml_value(yml, "Iterations")) == 500
+    assert abs(float(yaml_value(yml, "Final Resid Norm")) - 500 * (0.9 * 0.9)) <= 1e-9
+    nnz = int(yaml_value(yml, "Global NNZ"))
+    assert float(yaml_value(yml, "MATVEC Flops")) == 2.0 * nnz * 500
+
+
 def test_cpp_shim_matches_oracle(tmp_path):
     exe = os.path.join(tmp_path, "shim_solve")
     from minife_gb300 import build
