@@ -337,6 +337,20 @@ mfe_status mfe_batch_solve(mfe_ctx* ctx, mfe_batch* batch, const mfe_cg_opts* op
                            double* x_out, mfe_cg_result* results);
 void mfe_batch_destroy(mfe_batch* batch);
 
+/* ------------------------------------------------------------------ */
+/* the reference's debug dumps                                          */
+/* ------------------------------------------------------------------ */
+
+/* write_matrix / write_vector (ref/src/SparseMatrix_functions.hpp:98-140,
+ * ref/src/Vector_functions.hpp:49-82) on one rank: the file is
+ * "<filename>.1.0"; matrix: "nrows nnz" then one "row col coef" line per
+ * stored entry; vector: "n" then one "index coef" line (index from
+ * start_index); numbers in the default std::ostream format (6 significant
+ * digits).  Arrays on the device; the call synchronises the stream. */
+mfe_status mfe_write_matrix(mfe_ctx* ctx, const mfe_csr* A, const char* filename);
+mfe_status mfe_write_vector(mfe_ctx* ctx, int64_t n, const double* x, int64_t start_index,
+                            const char* filename);
+
 #ifdef __cplusplus
 }
 #endif

@@ -117,6 +117,8 @@ SIGNATURES = {
     "mfe_batch_solve": (ctypes.c_int, [c_void_p, c_void_p, _P(MfeCgOpts), c_void_p,
                                        _P(MfeCgResult)]),
     "mfe_batch_destroy": (None, [c_void_p]),
+    "mfe_write_matrix": (ctypes.c_int, [c_void_p, _P(MfeCsr), ctypes.c_char_p]),
+    "mfe_write_vector": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_int64, ctypes.c_char_p]),
 }
 
 _LIB = None

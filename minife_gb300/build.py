@@ -31,6 +31,7 @@ SOURCES = {
     "mfe_mixed.cu": [],
     "mfe_multi.cu": [],
     "mfe_batch.cu": [],
+    "mfe_dump.cu": [],
     "mfe_cg.cu": [],
 }
 

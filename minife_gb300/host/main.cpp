@@ -15,7 +15,9 @@
 // mixed), max_iters (default 200, driver.hpp:241), abs_tol (default
 // DBL_EPSILON, driver.hpp:245), rel_tol (overrides abs_tol: stop at
 // ||r|| <= rel_tol ||r0||), refine_k (mixed solver), kernels (1: the
-// reference's MINIFE_KERNELS timing loops instead of the CG solve).
+// reference's MINIFE_KERNELS timing loops instead of the CG solve), dump (1:
+// the reference's MINIFE_DEBUG files A_prebc.mtx, b_prebc.vec, A.mtx, b.vec,
+// A_local.mtx, b_local.vec, x.vec, each with the ".1.0" suffix).
 #include <sys/utsname.h>
 #include <unistd.h>
 
@@ -86,7 +88,7 @@ void check(mfe_ctx* ctx, mfe_status s, const char* what)
 }
 
 struct Params {
-  int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads, kernels;
+  int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads, kernels, dump;
   float load_imbalance;
   std::string name, precision;
   int max_iters, refine_k;
@@ -126,6 +128,7 @@ int main(int argc, char** argv)
   p.rel_tol = parse_parameter<double>(as, "rel_tol", 0.0);
   p.refine_k = parse_parameter<int>(as, "refine_k", 0);
   p.kernels = parse_parameter<int>(as, "kernels", 0);
+  p.dump = parse_parameter<int>(as, "dump", 0);
 
   // print_params=1 on the command line: print the parsed parameters and stop
   // (no GPU needed); an input_file replaces the other arguments, as in the
@@ -213,15 +216,43 @@ int main(int argc, char** argv)
   print_timed("generating matrix structure...", gen_structure, t_total);
 
   t0 = now();
-  check(ctx, mfe_assemble(ctx, p.nx, p.ny, p.nz, nullptr, &A, b, 1), "mfe_assemble");
+  // with dump=1 (the reference's MINIFE_DEBUG dumps, driver.hpp:206-234) the
+  // Dirichlet passes run separately so the pre-BC system can be written
+  check(ctx, mfe_assemble(ctx, p.nx, p.ny, p.nz, nullptr, &A, b, p.dump ? 0 : 1), "mfe_assemble");
   check(ctx, mfe_synchronize(ctx), "mfe_synchronize");
   const double fe_assembly = now() - t0;
   t_total += fe_assembly;
   print_timed("assembling FE data...", fe_assembly, t_total);
-  // both impose_dirichlet passes run inside the assembly kernel
-  print_timed("imposing Dirichlet BC...", 0.0, t_total);
-  print_timed("imposing Dirichlet BC...", 0.0, t_total);
+  if (p.dump) {
+    check(ctx, mfe_write_matrix(ctx, &A, "A_prebc.mtx"), "mfe_write_matrix");
+    check(ctx, mfe_write_vector(ctx, nrows, b, 0, "b_prebc.vec"), "mfe_write_vector");
+    int32_t* bc = nullptr;
+    int64_t nbc = 0;
+    check(ctx, mfe_device_alloc(ctx, 4 * (size_t)nrows, (void**)&bc), "mfe_device_alloc");
+    for (int which = 0; which < 2; ++which) {
+      t0 = now();
+      check(ctx, mfe_box_bc_rows(ctx, p.nx, p.ny, p.nz, which, bc, &nbc), "mfe_box_bc_rows");
+      check(ctx, mfe_impose_dirichlet(ctx, &A, b, which == 0 ? 0.0 : 1.0, bc, nbc),
+            "mfe_impose_dirichlet");
+      check(ctx, mfe_synchronize(ctx), "mfe_synchronize");
+      const double t_bc = now() - t0;
+      t_total += t_bc;
+      print_timed("imposing Dirichlet BC...", t_bc, t_total);
+    }
+    mfe_device_free(ctx, bc);
+    check(ctx, mfe_write_matrix(ctx, &A, "A.mtx"), "mfe_write_matrix");
+    check(ctx, mfe_write_vector(ctx, nrows, b, 0, "b.vec"), "mfe_write_vector");
+  } else {
+    // both impose_dirichlet passes run inside the assembly kernel
+    print_timed("imposing Dirichlet BC...", 0.0, t_total);
+    print_timed("imposing Dirichlet BC...", 0.0, t_total);
+  }
   print_timed("making matrix indices local...", 0.0, t_total);
+  if (p.dump) {
+    // make_local_matrix leaves a one-rank matrix as it is
+    check(ctx, mfe_write_matrix(ctx, &A, "A_local.mtx"), "mfe_write_matrix");
+    check(ctx, mfe_write_vector(ctx, nrows, b, 0, "b_local.vec"), "mfe_write_vector");
+  }
 
   doc.add("Matrix structure generation", "")->add("Mat-struc-gen Time", gen_structure);
   doc.add("FE assembly", "")->add("FE assembly Time", fe_assembly);
@@ -414,6 +445,7 @@ int main(int argc, char** argv)
     if (p.verify_solution > 0) gpu->add("verification", verify_result == 0 ? "passed" : "failed");
   }
 
+  if (p.dump && !p.kernels) check(ctx, mfe_write_vector(ctx, nrows, x, 0, "x.vec"), "mfe_write_vector");
   mfe_device_free(ctx, b);
   mfe_device_free(ctx, x);
   mfe_csr_free(ctx, &A);

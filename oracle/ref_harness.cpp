@@ -71,10 +71,13 @@ static int element_case(const std::string& out)
 int main(int argc, char** argv)
 {
   if (argc == 3 && std::string(argv[1]) == "element") return element_case(argv[2]);
-  if (argc != 8) {
-    std::fprintf(stderr, "usage: %s nx ny nz max_iter tol_mode tol outdir\n", argv[0]);
+  if (argc != 8 && argc != 9) {
+    std::fprintf(stderr, "usage: %s nx ny nz max_iter tol_mode tol outdir [dump]\n", argv[0]);
     return 1;
   }
+  // dump: also write the reference's own MINIFE_DEBUG files (write_matrix /
+  // write_vector, driver.hpp:206-234,308-310) into the working directory
+  const bool dump_files = argc == 9 && std::string(argv[8]) == "dump";
   int nx = std::atoi(argv[1]), ny = std::atoi(argv[2]), nz = std::atoi(argv[3]);
   int max_iter = std::atoi(argv[4]);
   int tol_mode = std::atoi(argv[5]);
@@ -97,11 +100,19 @@ int main(int argc, char** argv)
   dump(out + "/cols.i32", &A.packed_cols[0], A.packed_cols.size());
   dump(out + "/vals_prebc.f64", &A.packed_coefs[0], A.packed_coefs.size());
   dump(out + "/b_prebc.f64", &b.coefs[0], b.coefs.size());
+  if (dump_files) {
+    miniFE::write_matrix("A_prebc.mtx", A);
+    miniFE::write_vector("b_prebc.vec", b);
+  }
 
   miniFE::impose_dirichlet(0.0, A, b, nx + 1, ny + 1, nz + 1, mesh.bc_rows_0);
   miniFE::impose_dirichlet(1.0, A, b, nx + 1, ny + 1, nz + 1, mesh.bc_rows_1);
   dump(out + "/vals.f64", &A.packed_coefs[0], A.packed_coefs.size());
   dump(out + "/b.f64", &b.coefs[0], b.coefs.size());
+  if (dump_files) {
+    miniFE::write_matrix("A.mtx", A);
+    miniFE::write_vector("b.vec", b);
+  }
 
   miniFE::make_local_matrix(A);
 
@@ -113,6 +124,7 @@ int main(int argc, char** argv)
   miniFE::cg_solve(A, b, x, miniFE::matvec_std<Mat, Vec>(), max_iter, abs_tol,
                    num_iters, normr, times);
   dump(out + "/x.f64", &x.coefs[0], x.coefs.size());
+  if (dump_files) miniFE::write_vector("x.vec", x);
   int verify = miniFE::verify_solution(mesh, x, 0.06, false);
 
   FILE* f = std::fopen((out + "/meta.txt").c_str(), "w");

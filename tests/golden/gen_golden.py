@@ -18,6 +18,7 @@ import hashlib
 import json
 import os
 import re
+import shutil
 import subprocess
 import sys
 import tempfile
@@ -127,6 +128,15 @@ def main():
             f.write("\n".join(keys) + "\n")
         with open(os.path.join(HERE, "ref_stdout_nx10.txt"), "w") as f:
             f.write(run.stdout)
+    # the reference's own MINIFE_DEBUG dump files (write_matrix /
+    # write_vector) for the 2x3x2 box, reference defaults
+    ddir = os.path.join(HERE, "dumps_2x3x2")
+    os.makedirs(ddir, exist_ok=True)
+    with tempfile.TemporaryDirectory() as tmp:
+        subprocess.run([HARNESS, "2", "3", "2", "200", "0", repr(2.220446049250313e-16), tmp,
+                        "dump"], cwd=tmp, check=True)
+        for name in ("A_prebc.mtx", "b_prebc.vec", "A.mtx", "b.vec", "x.vec"):
+            shutil.copy(os.path.join(tmp, name + ".1.0"), os.path.join(ddir, name + ".1.0"))
     np.savez_compressed(os.path.join(HERE, "minife_golden.npz"), **out)
     with open(os.path.join(HERE, "golden_hashes.json"), "w") as f:
         json.dump(hashes, f, indent=1, sort_keys=True)

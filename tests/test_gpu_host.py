@@ -89,6 +89,23 @@ def test_minife_x_kernel_timing_mode(tmp_path):
     assert float(yaml_value(yml, "MATVEC Flops")) == 2.0 * nnz * 500
 
 
+def test_minife_x_dump_files_match_reference(tmp_path):
+    """dump=1 writes the reference's MINIFE_DEBUG files; for the 2x3x2 box the
+    system files are byte-identical to the ones the reference wrote
+    (tests/golden/dumps_2x3x2) and x agrees to the printed digits."""
+    r, yml = run_driver(tmp_path, "nx=2", "ny=3", "nz=2", "dump=1")
+    assert r.returncode == 0, r.stdout + r.stderr
+    ref = os.path.join(ROOT, "tests", "golden", "dumps_2x3x2")
+    for name in ("A_prebc.mtx", "b_prebc.vec", "A.mtx", "b.vec"):
+        ours = open(os.path.join(tmp_path, name + ".1.0")).read()
+        assert ours == open(os.path.join(ref, name + ".1.0")).read(), name
+    assert open(os.path.join(tmp_path, "A_local.mtx.1.0")).read() == \
+        open(os.path.join(ref, "A.mtx.1.0")).read()
+    xo = [float(l.split()[1]) for l in open(os.path.join(ref, "x.vec.1.0")).read().splitlines()[1:]]
+    xs = [float(l.split()[1]) for l in open(os.path.join(tmp_path, "x.vec.1.0")).read().splitlines()[1:]]
+    assert np.allclose(xs, xo, rtol=1e-5, atol=1e-12)
+
+
 def test_cpp_shim_matches_oracle(tmp_path):
     exe = os.path.join(tmp_path, "shim_solve")
     from minife_gb300 import build
