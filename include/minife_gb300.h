@@ -223,6 +223,8 @@ typedef struct mfe_cg_opts {
                              mfe_cg_history) */
   const mfe_csr* A32;   /* mixed: optional prepared FP32 copy of A (NULL: the
                            library converts and caches one) */
+  int32_t precond;      /* mfe_cg_solve: 0 none (the reference's CG), 1 Jacobi
+                           (M = diag(A), FP64; stops on ||r|| after the update) */
 } mfe_cg_opts;
 
 /* Fill opts with the reference's defaults (max_iter 200, absolute tol

@@ -328,7 +328,7 @@ class CGResult:
 
 
 def _opts(max_iter, tol, tol_mode, precision, refine_k=0, inner_tol=0.0, max_refine=0,
-          record_history=False, A32=None):
+          record_history=False, A32=None, precond="none"):
     o = MfeCgOpts()
     _abi.load().mfe_cg_opts_default(ctypes.byref(o))
     o.max_iter = int(max_iter)
@@ -339,6 +339,7 @@ def _opts(max_iter, tol, tol_mode, precision, refine_k=0, inner_tol=0.0, max_ref
     o.inner_tol = float(inner_tol)
     o.max_refine = int(max_refine)
     o.record_history = 1 if record_history else 0
+    o.precond = {"none": 0, "jacobi": 1}[precond]
     keep = None
     if A32 is not None:
         keep = A32.c()
@@ -362,15 +363,16 @@ def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
              tol_mode: str = "absolute", precision: str = "f64", refine_k: int = 0,
              inner_tol: float = 0.0, max_refine: int = 0, record_history: bool = False,
              A32: CSRMatrix | None = None, allow_breakdown: bool = True,
-             ctx: Context | None = None) -> CGResult:
+             precond: str = "none", ctx: Context | None = None) -> CGResult:
     """cg_solve (ref/src/cg_solve.hpp:69) on device vectors; x holds the
     initial guess and receives the solution.  Breakdown (the reference prints
     an error and returns) is reported in CGResult.status unless
-    allow_breakdown is False."""
+    allow_breakdown is False.  precond="jacobi" runs the Jacobi-preconditioned
+    CG (FP64, stops on ||r|| after the update)."""
     ctx = ctx or default_context()
     m = A.c()
     o, keep = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine,
-                    record_history, A32)
+                    record_history, A32, precond)
     r = MfeCgResult()
     st = ctx.lib.mfe_cg_solve(ctx.h, ctypes.byref(m), _ptr(b), _ptr(x), ctypes.byref(o),
                               ctypes.byref(r))

@@ -40,7 +40,7 @@ class MfeCgOpts(ctypes.Structure):
         ("max_iter", c_int32), ("tol_mode", c_int32), ("tol", c_double),
         ("precision", c_int32), ("refine_k", c_int32), ("inner_tol", c_double),
         ("max_refine", c_int32), ("record_history", c_int32),
-        ("A32", ctypes.POINTER(MfeCsr)),
+        ("A32", ctypes.POINTER(MfeCsr)), ("precond", c_int32),
     ]
 
 

@@ -32,6 +32,7 @@ SOURCES = {
     "mfe_multi.cu": [],
     "mfe_batch.cu": [],
     "mfe_dump.cu": [],
+    "mfe_pcg.cu": [],
     "mfe_cg.cu": [],
 }
 

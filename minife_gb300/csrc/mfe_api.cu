@@ -517,7 +517,8 @@ mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double*
   if (opts) o = *opts;
   else mfe_cg_opts_default(&o);
   if (o.max_iter < 0 || !(o.tol >= 0.0) ||
-      (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED))
+      (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED) ||
+      (o.precond != 0 && o.precond != 1))
     return fail(ctx, MFE_BAD_ARG, "bad CG options");
   MFE_TRY(set_device(ctx));
   if (A->nrows == 0) return MFE_OK;

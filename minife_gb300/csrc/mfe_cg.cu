@@ -513,6 +513,7 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
 mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                          const mfe_cg_opts* opts, mfe_cg_result* res)
 {
+  if (opts->precond == 1) return cg_jacobi(ctx, A, b, x, opts, res);
   if (opts->precision == MFE_PREC_F64) return cg_f64(ctx, A, b, x, opts, res);
   return cg_mixed(ctx, A, b, x, opts, res);
 }

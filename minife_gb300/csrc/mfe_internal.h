@@ -96,6 +96,10 @@ mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const doubl
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,
                     const mfe_cg_opts* opts, mfe_cg_result* res);
 
+// ---- Jacobi-preconditioned CG (mfe_pcg.cu) ----
+mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
+                     const mfe_cg_opts* opts, mfe_cg_result* res);
+
 // ---- multi-RHS CG (mfe_multi.cu) ----
 // True when Y = A X can take the box-structured SpMM (box matrix, nrhs
 // dividing 32, 16-byte aligned values and vectors).

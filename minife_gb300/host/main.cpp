@@ -17,7 +17,8 @@
 // ||r|| <= rel_tol ||r0||), refine_k (mixed solver), kernels (1: the
 // reference's MINIFE_KERNELS timing loops instead of the CG solve), dump (1:
 // the reference's MINIFE_DEBUG files A_prebc.mtx, b_prebc.vec, A.mtx, b.vec,
-// A_local.mtx, b_local.vec, x.vec, each with the ".1.0" suffix).
+// A_local.mtx, b_local.vec, x.vec, each with the ".1.0" suffix), precond
+// (none | jacobi: diagonal-preconditioned CG).
 #include <sys/utsname.h>
 #include <unistd.h>
 
@@ -90,7 +91,7 @@ void check(mfe_ctx* ctx, mfe_status s, const char* what)
 struct Params {
   int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads, kernels, dump;
   float load_imbalance;
-  std::string name, precision;
+  std::string name, precision, precond;
   int max_iters, refine_k;
   double abs_tol, rel_tol;
 };
@@ -129,6 +130,7 @@ int main(int argc, char** argv)
   p.refine_k = parse_parameter<int>(as, "refine_k", 0);
   p.kernels = parse_parameter<int>(as, "kernels", 0);
   p.dump = parse_parameter<int>(as, "dump", 0);
+  p.precond = parse_parameter<std::string>(as, "precond", "none");
 
   // print_params=1 on the command line: print the parsed parameters and stop
   // (no GPU needed); an input_file replaces the other arguments, as in the
@@ -351,6 +353,7 @@ int main(int argc, char** argv)
       o.tol_mode = MFE_TOL_RELATIVE;
     }
     o.precision = p.precision == "mixed" ? MFE_PREC_MIXED : MFE_PREC_F64;
+  o.precond = p.precond == "jacobi" ? 1 : 0;
     o.refine_k = p.refine_k;
     std::cout << "Starting CG solver ... " << std::endl;
     mfe_cg_result r;
@@ -435,6 +438,7 @@ int main(int argc, char** argv)
 
     auto* gpu = doc.add("GB300", "");
     gpu->add("precision", p.precision);
+    gpu->add("preconditioner", p.precond);
     gpu->add("tolerance mode", p.rel_tol > 0 ? "relative" : "absolute");
     gpu->add("tolerance", o.tol);
     gpu->add("Initial Resid Norm", r.normr0);
