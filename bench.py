@@ -146,7 +146,8 @@ def max_over_ranks(world, v):
         return v
     import torch
     import torch.distributed as dist
-    t = torch.tensor([v], dtype=torch.float64, device="cuda")
+    dev = "cuda" if torch.cuda.is_available() else "cpu"
+    t = torch.tensor([v], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -193,9 +194,10 @@ def run_reference(args):
     O.build()
     # the system is built on the host by the oracle (the reference's element
     # loop restated), so no GPU code runs in this arm
+    dims = (args.ref_dims,) * 3
     t0 = time.perf_counter()
-    ro, cols, vals, bh = O.build_system(*DIMS)
-    log("reference arm: host assembly of %dx%dx%d took %.1f s" % (*DIMS, time.perf_counter() - t0))
+    ro, cols, vals, bh = O.build_system(*dims)
+    log("reference arm: host assembly of %dx%dx%d took %.1f s" % (*dims, time.perf_counter() - t0))
     iters_full = args.ref_iters
     per = []
     threads = 1
@@ -210,12 +212,12 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic (miniFE box, generated)",
-        "config": {"workload": "cg_f64_256^3_to_1e-8_rel", "nx": DIMS[0], "ny": DIMS[1],
-                   "nz": DIMS[2], "iterations": iters_full},
+        "config": {"workload": "cg_f64_256^3_to_1e-8_rel", "nx": dims[0], "ny": dims[1],
+                   "nz": dims[2], "iterations": iters_full},
         "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                         "sample": "%d CG iterations per step on the 256^3 system, %d steps, "
-                                   "scaled to %d iterations" % (args.ref_sample, args.steps,
-                                                                iters_full)},
+                         "sample": "%d CG iterations per step on the %d^3 system, %d steps, "
+                                   "scaled to %d iterations" % (args.ref_sample, dims[0],
+                                                                args.steps, iters_full)},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -588,6 +590,8 @@ def main():
     ap.add_argument("--refine-k", type=int, default=50,
                     help="mixed solver: reliable update at least every k inner iterations")
     ap.add_argument("--cpu-sample", type=int, default=20)
+    ap.add_argument("--ref-dims", type=int, default=DIMS[0],
+                    help="reference arm: box edge of the sampled system (the metric's is 256)")
     ap.add_argument("--ref-sample", type=int, default=10)
     ap.add_argument("--ref-iters", type=int, default=401,
                     help="CG iterations of the 256^3 solve to 1e-8 (the GPU solve's count)")
