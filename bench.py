@@ -434,10 +434,12 @@ def run_gpu(args):
 
 
 def batch_dims(nbox=96, lo=32, hi=160, seed=20261204):
-    """Seeded uneven boxes: nx, ny, nz uniform in {lo..hi}."""
+    """Seeded uneven boxes: nx, ny, nz uniform in {lo..hi} (the first nbox
+    of the 96-box sequence)."""
     import numpy as np
     rng = np.random.default_rng(seed)
-    return [tuple(int(v) for v in rng.integers(lo, hi + 1, size=3)) for _ in range(nbox)]
+    dims = [tuple(int(v) for v in rng.integers(lo, hi + 1, size=3)) for _ in range(96)]
+    return dims[:nbox]
 
 
 def bench_batch(args, world, stream):
@@ -539,10 +541,20 @@ def run_probe(args):
     """Small fixed workloads for profiler captures (ncu): 'spmv' = the box
     system at --dims^3, three FP64 and three FP32 matvecs; 'cg' = the system
     and a 4-iteration CG solve; 'multi' = the system and a 6-iteration
-    mixed-precision solve of 32 right-hand sides (reliable update every 3)."""
+    mixed-precision solve of 32 right-hand sides (reliable update every 3);
+    'batch' = the first --nbox of the seeded uneven boxes solved together in
+    mixed precision to 1e-8 (default shape, refine_k 50)."""
     import torch
     import minife_gb300 as M
     torch.cuda.set_device(0)
+    if args.probe == "batch":
+        dims = batch_dims(args.nbox)
+        x, off, res = M.batch_solve_boxes(dims, max_iter=5000, tol=TOL, tol_mode="relative",
+                                          precision="mixed", refine_k=50)
+        torch.cuda.synchronize()
+        print("probe batch %d boxes done: %d iterations, solve %.3f s"
+              % (len(dims), max(r.num_iters for r in res), res[0].times[4]))
+        return 0
     d = args.dims
     A, b = M.build_system(d, d, d)
     if args.probe == "spmv":
@@ -555,6 +567,8 @@ def run_probe(args):
         y32 = torch.empty_like(x32)
         for _ in range(3):
             M.matvec(A32, x32, y32)
+    elif args.probe == "batch":
+        pass
     elif args.probe == "multi":
         g = torch.Generator(device="cpu").manual_seed(0)
         B = torch.randn(A.nrows, 32, generator=g, dtype=torch.float64).cuda().contiguous()
@@ -571,9 +585,10 @@ def run_probe(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["spmv", "cg", "multi"], default=None,
+    ap.add_argument("--probe", choices=["spmv", "cg", "multi", "batch"], default=None,
                     help="run a small fixed workload for a profiler capture and exit")
     ap.add_argument("--dims", type=int, default=128)
+    ap.add_argument("--nbox", type=int, default=96, help="boxes of the batch probe")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
