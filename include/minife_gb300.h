@@ -340,6 +340,33 @@ mfe_status mfe_batch_solve(mfe_ctx* ctx, mfe_batch* batch, const mfe_cg_opts* op
 void mfe_batch_destroy(mfe_batch* batch);
 
 /* ------------------------------------------------------------------ */
+/* the reference's ELL matrix                                           */
+/* ------------------------------------------------------------------ */
+
+/* ELLMatrix (ref/src/ELLMatrix.hpp, MINIFE_ELL_MATRIX) on the device:
+ * ncols_per_row entries per row, row-major (row r at r*ncols_per_row), the
+ * row's columns ascending first, then padding entries with column 0 and
+ * value 0 (MatrixInitOp<ELLMatrix>, ref/src/MatrixInitOp.hpp:160-220). */
+typedef struct mfe_ell {
+  int64_t nrows;
+  int32_t ncols_per_row;   /* 27 for miniFE's matrices */
+  int32_t dtype;           /* mfe_dtype */
+  int32_t* cols;           /* device, nrows*ncols_per_row */
+  void* vals;              /* device, nrows*ncols_per_row */
+} mfe_ell;
+
+/* E->cols/vals (caller-allocated, nrows*ncols_per_row each) and
+ * E->ncols_per_row set by the caller; fills them from A (MFE_BAD_ARG if a row
+ * is longer than ncols_per_row) and sets E->nrows and E->dtype. */
+mfe_status mfe_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E);
+/* matvec_std<ELLMatrix> (ref/src/SparseMatrix_functions.hpp:579-611): y = A x,
+ * every stored entry summed (padding adds 0 * x[0]). */
+mfe_status mfe_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y);
+/* cg_solve with the ELL matvec (FP64; opts as for mfe_cg_solve). */
+mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, double* x,
+                            const mfe_cg_opts* opts, mfe_cg_result* result);
+
+/* ------------------------------------------------------------------ */
 /* the reference's debug dumps                                          */
 /* ------------------------------------------------------------------ */
 

@@ -33,7 +33,7 @@ __all__ = [
     "generate_matrix_structure", "assemble_FE_data", "impose_dirichlet", "box_bc_rows",
     "build_system", "matvec", "matvec_and_dot", "dot", "waxpby", "fused_waxpby", "cg_solve",
     "cg_solve_host", "cg_solve_multi", "Batch", "batch_solve_boxes", "verify_solution",
-    "element_gradient", "to_f32", "spmm",
+    "element_gradient", "to_f32", "spmm", "ELLMatrix", "matvec_ell", "cg_solve_ell",
 ]
 
 DBL_EPSILON = 2.220446049250313e-16
@@ -190,6 +190,72 @@ class CSRMatrix:
         cols = torch.empty(nnz + 4, dtype=torch.int32, device=dev)[:nnz]
         vals = torch.empty(nnz + 4, dtype=dtype or torch.float64, device=dev)[:nnz]
         return CSRMatrix(ro, cols, vals, box=(nx, ny, nz), max_row_len=27)
+
+
+class ELLMatrix:
+    """The reference's ELLMatrix (ref/src/ELLMatrix.hpp) on the device:
+    ncols_per_row entries per row, row-major, the row's columns first and
+    then padding (column 0, value 0)."""
+
+    def __init__(self, cols, coefs, ncols_per_row: int):
+        self.cols = cols
+        self.coefs = coefs
+        self.num_cols_per_row = int(ncols_per_row)
+        self.has_local_indices = True
+
+    @property
+    def nrows(self) -> int:
+        return self.cols.numel() // self.num_cols_per_row
+
+    def num_nonzeros(self) -> int:
+        return self.cols.numel()
+
+    def c(self):
+        torch = _torch()
+        e = _abi.MfeEll()
+        e.nrows = self.nrows
+        e.ncols_per_row = self.num_cols_per_row
+        e.dtype = MFE_F64 if self.coefs.dtype == torch.float64 else MFE_F32
+        e.cols = self.cols.data_ptr()
+        e.vals = self.coefs.data_ptr()
+        return e
+
+    @staticmethod
+    def from_csr(A: "CSRMatrix", ncols_per_row: int = 27, ctx: Context | None = None):
+        torch = _torch()
+        ctx = ctx or default_context()
+        n = A.nrows
+        E = ELLMatrix(torch.empty(n * ncols_per_row + 4, dtype=torch.int32,
+                                  device=A.packed_cols.device)[: n * ncols_per_row],
+                      torch.empty(n * ncols_per_row + 4, dtype=A.packed_coefs.dtype,
+                                  device=A.packed_cols.device)[: n * ncols_per_row],
+                      ncols_per_row)
+        e = E.c()
+        m = A.c()
+        ctx.check(ctx.lib.mfe_csr_to_ell(ctx.h, ctypes.byref(m), ctypes.byref(e)), "mfe_csr_to_ell")
+        return E
+
+
+def matvec_ell(E: ELLMatrix, x, y, ctx: Context | None = None):
+    """matvec_std<ELLMatrix> (ref/src/SparseMatrix_functions.hpp:579-611)."""
+    ctx = ctx or default_context()
+    e = E.c()
+    ctx.check(ctx.lib.mfe_spmv_ell(ctx.h, ctypes.byref(e), _ptr(x), _ptr(y)), "mfe_spmv_ell")
+    return y
+
+
+def cg_solve_ell(E: ELLMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
+                 tol_mode: str = "absolute", ctx: Context | None = None) -> CGResult:
+    """cg_solve with the ELL matvec (FP64)."""
+    ctx = ctx or default_context()
+    e = E.c()
+    o, _ = _opts(max_iter, tol, tol_mode, "f64")
+    r = MfeCgResult()
+    st = ctx.lib.mfe_cg_solve_ell(ctx.h, ctypes.byref(e), _ptr(b), _ptr(x), ctypes.byref(o),
+                                  ctypes.byref(r))
+    if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
+        ctx.check(st, "mfe_cg_solve_ell")
+    return _result(ctx, r, False)
 
 
 def generate_matrix_structure(nx, ny, nz, ctx: Context | None = None) -> CSRMatrix:

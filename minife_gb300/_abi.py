@@ -52,6 +52,11 @@ class MfeCgResult(ctypes.Structure):
     ]
 
 
+class MfeEll(ctypes.Structure):
+    _fields_ = [("nrows", c_int64), ("ncols_per_row", c_int32), ("dtype", c_int32),
+                ("cols", c_void_p), ("vals", c_void_p)]
+
+
 class MfeBatchTuning(ctypes.Structure):
     _fields_ = [("spmv_rows", c_int32), ("spmv_stages", c_int32), ("chunk_rows", c_int32)]
 
@@ -118,6 +123,10 @@ SIGNATURES = {
                                        _P(MfeCgResult)]),
     "mfe_batch_destroy": (None, [c_void_p]),
     "mfe_write_matrix": (ctypes.c_int, [c_void_p, _P(MfeCsr), ctypes.c_char_p]),
+    "mfe_csr_to_ell": (ctypes.c_int, [c_void_p, _P(MfeCsr), _P(MfeEll)]),
+    "mfe_spmv_ell": (ctypes.c_int, [c_void_p, _P(MfeEll), c_void_p, c_void_p]),
+    "mfe_cg_solve_ell": (ctypes.c_int, [c_void_p, _P(MfeEll), c_void_p, c_void_p, _P(MfeCgOpts),
+                                        _P(MfeCgResult)]),
     "mfe_write_vector": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_int64, ctypes.c_char_p]),
 }
 

@@ -33,6 +33,7 @@ SOURCES = {
     "mfe_batch.cu": [],
     "mfe_dump.cu": [],
     "mfe_pcg.cu": [],
+    "mfe_ell.cu": [],
     "mfe_cg.cu": [],
 }
 

@@ -630,6 +630,54 @@ mfe_status mfe_batch_solve_boxes(mfe_ctx* ctx, int32_t nbox, const int32_t* dims
   return batch_solve_boxes(ctx, nbox, dims, opts, x_out, results);
 }
 
+static mfe_status check_ell(mfe_ctx* ctx, const mfe_ell* E, bool need_rows)
+{
+  if (!E) return fail(ctx, MFE_BAD_ARG, "null matrix");
+  if (E->ncols_per_row < 1 || E->ncols_per_row > 1024 || E->nrows < 0 ||
+      E->nrows * (int64_t)E->ncols_per_row >= ((int64_t)1 << 31))
+    return fail(ctx, MFE_BAD_ARG, "ELL sizes out of range for 32-bit indices");
+  if ((need_rows || E->nrows > 0) && (!E->cols || !E->vals)) return fail(ctx, MFE_BAD_ARG, "null ELL array");
+  return MFE_OK;
+}
+
+mfe_status mfe_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_csr(ctx, A));
+  if (!E || E->ncols_per_row < 1 || E->ncols_per_row > 1024 ||
+      A->nrows * (int64_t)E->ncols_per_row >= ((int64_t)1 << 31))
+    return fail(ctx, MFE_BAD_ARG, "bad ELL target");
+  if (A->nrows > 0 && (!E->cols || !E->vals)) return fail(ctx, MFE_BAD_ARG, "null ELL array");
+  MFE_TRY(set_device(ctx));
+  return launch_csr_to_ell(ctx, A, E);
+}
+
+mfe_status mfe_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_ell(ctx, E, false));
+  if (E->dtype != MFE_F64 && E->dtype != MFE_F32) return fail(ctx, MFE_BAD_ARG, "bad dtype");
+  if (E->nrows > 0 && (!x || !y)) return fail(ctx, MFE_BAD_ARG, "null vector");
+  MFE_TRY(set_device(ctx));
+  if (E->nrows == 0) return MFE_OK;
+  mfe_csr V;
+  MFE_TRY(ell_view(ctx, E, &V));
+  return launch_spmv(ctx, &V, x, y, nullptr, nullptr, nullptr);
+}
+
+mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, double* x,
+                            const mfe_cg_opts* opts, mfe_cg_result* result)
+{
+  if (!ctx || !result) return MFE_BAD_ARG;
+  MFE_TRY(check_ell(ctx, E, false));
+  if (E->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "cg_solve needs the FP64 matrix");
+  MFE_TRY(set_device(ctx));
+  if (E->nrows == 0) return MFE_OK;
+  mfe_csr V;
+  MFE_TRY(ell_view(ctx, E, &V));
+  return mfe_cg_solve(ctx, &V, b, x, opts, result);
+}
+
 mfe_status mfe_batch_create(mfe_ctx* ctx, int32_t nbox, const int32_t* dims, mfe_batch** out)
 {
   if (!ctx) return MFE_BAD_ARG;

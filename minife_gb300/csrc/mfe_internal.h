@@ -96,6 +96,11 @@ mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const doubl
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,
                     const mfe_cg_opts* opts, mfe_cg_result* res);
 
+// ---- the reference's ELL matrix (mfe_ell.cu) ----
+mfe_status launch_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E);
+// CSR view of an ELL matrix (row offsets r * ncols_per_row, cached in workspace)
+mfe_status ell_view(mfe_ctx* ctx, const mfe_ell* E, mfe_csr* V);
+
 // ---- Jacobi-preconditioned CG (mfe_pcg.cu) ----
 mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                      const mfe_cg_opts* opts, mfe_cg_result* res);
