@@ -32,6 +32,9 @@ struct mfe_ctx {
   // cached FP32 copy of a matrix for the mixed-precision solver
   const void* f32_src_vals = nullptr;
   int64_t f32_src_nnz = 0;
+  // cached padded 28-per-row FP32 copy (multi-RHS mixed solver)
+  const void* ell28_src = nullptr;
+  int64_t ell28_nnz = 0;
   mfe_csr f32_copy{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };

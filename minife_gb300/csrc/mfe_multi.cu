@@ -495,6 +495,161 @@ __global__ void __launch_bounds__(kThreadsM, NRC ? 2 : 1) k_spmm_box(SpmmParams<
                      MODE == MM_DOT ? P.cg : nullptr);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 A P for exactly 32 right-hand sides in the mixed solver: the matrix in a
+// padded 28-per-row layout (the 27 stencil slots in (dz, dy, dx) order, zeros
+// for missing neighbours, one zero pad so every row starts on 16 bytes) and P
+// with ghost zones of zero rows around it, so no row needs a mask.  Each
+// consumer warp owns four consecutive rows with one lane per right-hand side:
+// the six x values of each of the nine lines serve all four rows (54 loads per
+// 108 FMAs instead of one load per FMA), and each row's values come in seven
+// 16-byte broadcast loads; shared-memory traffic per row is half that of
+// k_spmm_box.
+// ---------------------------------------------------------------------------
+constexpr int kER = 32;                     // rows per tile
+constexpr int kEW = 8;                      // consumer warps, four rows each
+constexpr int kECapX = (kER + 2) * 32;      // floats per x segment
+constexpr int kECapV = kER * 28;            // floats of a tile's values
+constexpr int kEStage = kECapV + 9 * kECapX;
+constexpr int kEThreads = (kEW + 2) * 32;
+
+struct Ell32Params {
+  int n, Nx, NxNy;
+  const float* __restrict__ ell;  // [ceil(n/32)*32][28]
+  const float* __restrict__ p;    // n x 32, ghost zones before and after
+  float* __restrict__ Ap;
+  double* partials;
+  unsigned* ticket;
+  MultiState* st;
+  unsigned* err;
+};
+
+__global__ void __launch_bounds__(kEThreads, 2) k_spmm_ell32(Ell32Params P)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t full[2], empty[2];
+  __shared__ double red[(kEW + 2) * 32];
+  float* const st0 = reinterpret_cast<float*>(smem);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int ntiles = (P.n + kER - 1) / kER;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < 2; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kEW);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  DFAcc facc;
+  if (warp < 2) {
+    // producer warp w stages the CTA's tiles it = w, w + 2, ... into stage w
+    const int s = warp;
+    bool ok = true;
+    int it = warp;
+    for (int tile = blockIdx.x + warp * gridDim.x; tile < ntiles; tile += 2 * gridDim.x, it += 2) {
+      if (it >= 2) {
+        if (lane == 0) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / 2) - 1) & 1));
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+      }
+      if (!ok) break;
+      float* sv = st0 + (size_t)s * kEStage;
+      const int64_t r0 = (int64_t)tile * kER;
+      if (lane < 9) {
+        const int64_t off = (int64_t)(lane / 3 - 1) * P.NxNy + (lane % 3 - 1) * P.Nx;
+        const unsigned bytes = kECapX * sizeof(float);
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(sv + kECapV + lane * kECapX, P.p + (r0 + off - 1) * 32, bytes, &full[s]);
+      } else if (lane == 9) {
+        const unsigned bytes = kECapV * sizeof(float);
+        mbar_expect_tx(&full[s], bytes);
+        bulk_g2s(sv, P.ell + r0 * 28, bytes, &full[s]);
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&full[s]);
+    }
+    if (!ok && lane == 0) {
+      // bounded wait for the copies of this warp's last issued tile
+      atomicOr(P.err, ERR_WAIT_TIMEOUT);
+      mbar_wait_bounded(&full[s], (unsigned)(((it - 2) / 2) & 1));
+    }
+  } else {
+    const int cw = warp - 2;
+    int it = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+      const int s = it & 1;
+      if (!mbar_wait_bounded(&full[s], (unsigned)((it >> 1) & 1))) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        break;
+      }
+      const float* sv = st0 + (size_t)s * kEStage;
+      // segment j holds rows r0 + off_j - 1 .. r0 + off_j + 32: local row
+      // 4cw + k is the neighbour dx = k - i - 1 of row 4cw + i
+      const float* xs = sv + kECapV + (4 * cw) * 32 + lane;
+      float xw[9][6];
+#pragma unroll
+      for (int j = 0; j < 9; ++j)
+#pragma unroll
+        for (int k = 0; k < 6; ++k) xw[j][k] = xs[j * kECapX + k * 32];
+      float acc[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float4* v4 = reinterpret_cast<const float4*>(sv + (4 * cw + i) * 28);
+        float v[28];
+#pragma unroll
+        for (int q = 0; q < 7; ++q) {
+          const float4 t = v4[q];
+          v[4 * q] = t.x;
+          v[4 * q + 1] = t.y;
+          v[4 * q + 2] = t.z;
+          v[4 * q + 3] = t.w;
+        }
+        float a0 = 0.0f, a1 = 0.0f;
+#pragma unroll
+        for (int k = 0; k < 27; ++k) {
+          if (k & 1)
+            a1 = fmaf(v[k], xw[k / 3][i + k % 3], a1);
+          else
+            a0 = fmaf(v[k], xw[k / 3][i + k % 3], a0);
+        }
+        acc[i] = a0 + a1;
+      }
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[s]);
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int64_t r = (int64_t)tile * kER + 4 * cw + i;
+        if (r < P.n) {
+          P.Ap[r * 32 + lane] = acc[i];
+          facc.add_product(acc[i], xw[4][i + 1]);
+        }
+      }
+    }
+  }
+  multi_dot_reduce(warp < 2 ? 0.0 : facc.value(), red, P.partials, P.ticket, P.st->pAp, 32, P.st);
+}
+
+// FP64 box CSR -> FP32 padded 28-per-row values (slot order, zeros outside
+// the box and in the pad); rows n .. are left as the caller zeroed them
+__global__ void k_mr_ell28(int Nx, int Ny, int Nz, const double* __restrict__ vals,
+                           float* __restrict__ ell)
+{
+  const int n = Nx * Ny * Nz, NxNy = Nx * Ny;
+  for (int r = blockIdx.x * blockDim.x + threadIdx.x; r < n; r += gridDim.x * blockDim.x) {
+    const int iz = r / NxNy, rem = r - iz * NxNy, iy = rem / Nx, ix = rem - iy * Nx;
+    int64_t k = row_offset(ix, iy, iz, Nx, Ny, Nz);
+    float* out = ell + (int64_t)r * 28;
+    int slot = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx, ++slot) {
+          const bool in = ix + dx >= 0 && ix + dx < Nx && iy + dy >= 0 && iy + dy < Ny &&
+                          iz + dz >= 0 && iz + dz < Nz;
+          out[slot] = in ? (float)vals[k++] : 0.0f;
+        }
+    out[27] = 0.0f;
+  }
+}
+
 // lanes j, j+nrhs, j+2nrhs, ... of a warp hold right-hand side j: sum them
 // into lane j (nrhs divides 32)
 __device__ __forceinline__ double lane_group_sum(double v, int nrhs)
@@ -859,7 +1014,29 @@ struct MultiBufs {
   double* partials;  // [2][kMaxPartM][32]
   unsigned* tickets;
   unsigned* err;
+  const float* ell = nullptr;  // mixed, 32 right-hand sides: padded values (p has ghost zones)
+  int ell_grid = 0;
 };
+
+size_t ell32_smem() { return (size_t)2 * kEStage * sizeof(float); }
+
+// resident CTAs of k_spmm_ell32 on this device (attribute set once, before
+// any capture)
+mfe_status ell32_grid(mfe_ctx* ctx, int* grid)
+{
+  static int per_sm[64] = {};
+  const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
+  if (per_sm[dev] == 0) {
+    MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_ell32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)ell32_smem()));
+    int n = 1;
+    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_spmm_ell32, kEThreads,
+                                                                    ell32_smem()));
+    per_sm[dev] = std::max(n, 1);
+  }
+  *grid = ctx->sm_count * per_sm[dev];
+  return MFE_OK;
+}
 
 int vgrid(mfe_ctx* ctx, int64_t n)
 {
@@ -877,9 +1054,25 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
   k_mr_p<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
-  MFE_TRY((launch_spmm_t<float, MM_DOT, float>(ctx, &A32, nrhs, W.p, W.Ap, nullptr, nullptr,
-                                                W.partials, W.tickets, W.st->pAp, nullptr, W.err,
-                                                W.st)));
+  if (W.ell) {
+    Ell32Params E;
+    E.n = (int)A64.nrows;
+    E.Nx = A64.box_nx + 1;
+    E.NxNy = E.Nx * (A64.box_ny + 1);
+    E.ell = W.ell;
+    E.p = W.p;
+    E.Ap = W.Ap;
+    E.partials = W.partials;
+    E.ticket = W.tickets;
+    E.st = W.st;
+    E.err = W.err;
+    k_spmm_ell32<<<W.ell_grid, kEThreads, ell32_smem(), ctx->stream>>>(E);
+    MFE_TRY(check_launch(ctx, "k_spmm_ell32"));
+  } else {
+    MFE_TRY((launch_spmm_t<float, MM_DOT, float>(ctx, &A32, nrhs, W.p, W.Ap, nullptr, nullptr,
+                                                  W.partials, W.tickets, W.st->pAp, nullptr, W.err,
+                                                  W.st)));
+  }
   k_mr_update<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
       ntot, nrhs, W.x32, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mr_update"));
@@ -1032,7 +1225,34 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   }
   const size_t vb = (mixed ? sizeof(float) : sizeof(double)) * (size_t)(ntot + 8);
   void* r = workspace(ctx, "multi.r", vb);
-  void* p = workspace(ctx, "multi.p", vb);
+  // mixed with 32 right-hand sides: the padded-values SpMM, which reads p
+  // with ghost zones of zero rows on both sides (the stencil's reach plus a
+  // partial tile)
+  const bool use_ell = mixed && nrhs == 32 && getenv("MFE_MULTI_CSR") == nullptr;
+  const int64_t Nx = A64.box_nx + 1, NxNy = Nx * (A64.box_ny + 1);
+  const int64_t ghost = NxNy + Nx + 1 + kER;
+  const size_t pb = use_ell ? sizeof(float) * (size_t)((A64.nrows + 2 * ghost) * 32 + 8) : vb;
+  void* pbase = workspace(ctx, use_ell ? "multi.pg" : "multi.p", pb);
+  void* p = use_ell && pbase ? static_cast<void*>(static_cast<float*>(pbase) + ghost * 32) : pbase;
+  float* ell = nullptr;
+  int ell_grid = 0;
+  if (use_ell) {
+    const int64_t ntl = (A64.nrows + kER - 1) / kER;
+    const size_t eb = sizeof(float) * (size_t)(ntl * kER * 28 + 8);
+    ell = static_cast<float*>(workspace(ctx, "multi.ell28", eb));
+    if (!ell) return fail(ctx, MFE_OOM, "padded FP32 matrix allocation failed");
+    if (ctx->ell28_src != A64.vals || ctx->ell28_nnz != A64.nnz) {
+      MFE_CUDA_TRY(ctx, cudaMemsetAsync(ell, 0, eb, ctx->stream));
+      k_mr_ell28<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(A64.nrows, (int64_t)256),
+                                                                    (int64_t)ctx->sm_count * 8)),
+                   256, 0, ctx->stream>>>((int)Nx, A64.box_ny + 1, A64.box_nz + 1,
+                                          static_cast<const double*>(A64.vals), ell);
+      MFE_TRY(check_launch(ctx, "k_mr_ell28"));
+      ctx->ell28_src = A64.vals;
+      ctx->ell28_nnz = A64.nnz;
+    }
+    MFE_TRY(ell32_grid(ctx, &ell_grid));
+  }
   void* Ap = workspace(ctx, "multi.Ap", vb);
   float* x32 = mixed ? static_cast<float*>(workspace(ctx, "multi.x32", vb)) : nullptr;
   MultiState* dst = static_cast<MultiState*>(workspace(ctx, "multi.state", sizeof(MultiState)));
@@ -1041,7 +1261,7 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   const bool fresh = ctx->ws.find("multi.tickets") == ctx->ws.end();
   unsigned* tickets = static_cast<unsigned*>(workspace(ctx, "multi.tickets", sizeof(unsigned) * 4));
   unsigned* err = static_cast<unsigned*>(workspace(ctx, "multi.err", sizeof(unsigned)));
-  if (!r || !p || !Ap || (mixed && !x32) || !dst || !partials || !tickets || !err)
+  if (!r || !pbase || !Ap || (mixed && !x32) || !dst || !partials || !tickets || !err)
     return fail(ctx, MFE_OOM, "multi-RHS workspace allocation failed");
   if (fresh) MFE_CUDA_TRY(ctx, cudaMemsetAsync(tickets, 0, sizeof(unsigned) * 4, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaMemsetAsync(err, 0, sizeof(unsigned), ctx->stream));
@@ -1058,7 +1278,7 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   for (int j = 0; j < nrhs; ++j) hs->tol_abs[j] = o->tol;
   MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst, hs, sizeof(MultiState), cudaMemcpyHostToDevice, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(p, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(pbase, 0, pb, ctx->stream));
   if (mixed) {
     MFE_CUDA_TRY(ctx, cudaMemsetAsync(x32, 0, vb, ctx->stream));
     MFE_TRY((launch_spmm_t<double, MM_RESID, float>(ctx, &A64, nrhs, X, nullptr, B,
@@ -1080,7 +1300,7 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   }
   if (mixed) {
     MultiBufs<float> W{static_cast<float*>(r), static_cast<float*>(p), static_cast<float*>(Ap),
-                       x32, dst, partials, tickets, err};
+                       x32, dst, partials, tickets, err, ell, ell_grid};
     MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
       return multi_iter_mixed(ctx, A32, A64, nrhs, B, X, W, h, in_graph);
     }));
