@@ -6,6 +6,9 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <tuple>
+#include <mutex>
+#include <map>
 #include <vector>
 
 #include "mfe_internal.h"
@@ -92,6 +95,21 @@ static mfe_status check_csr(mfe_ctx* ctx, const mfe_csr* A)
     return fail(ctx, MFE_BAD_ARG, "null matrix array");
   if (A->dtype != MFE_F64 && A->dtype != MFE_F32) return fail(ctx, MFE_BAD_ARG, "bad dtype");
   return MFE_OK;
+}
+
+int resident_blocks(mfe_ctx* ctx, const void* kernel, int threads, size_t smem)
+{
+  static std::map<std::tuple<const void*, int, int, size_t>, int> cache;
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  const auto key = std::make_tuple(kernel, ctx->device, threads, smem);
+  auto it = cache.find(key);
+  if (it == cache.end()) {
+    int b = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, threads, smem) != cudaSuccess) b = 4;
+    it = cache.emplace(key, std::max(b, 1)).first;
+  }
+  return it->second * ctx->sm_count;
 }
 
 }  // namespace mfe

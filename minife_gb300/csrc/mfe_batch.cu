@@ -960,7 +960,8 @@ mfe_status bx_spmv64(mfe_ctx* ctx, const Run& R, const BxList& L, const double* 
   return check_launch(ctx, "k_bx_spmv");
 }
 
-int bx_vgrid(mfe_ctx* ctx) { return ctx->sm_count * 8; }
+// one wave of resident blocks of `kernel`
+int bx_vgrid(mfe_ctx* ctx, const void* kernel) { return resident_blocks(ctx, kernel, kBxVT, 0); }
 
 mfe_status bx_iter_mixed(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle h, int in_graph)
 {
@@ -968,15 +969,16 @@ mfe_status bx_iter_mixed(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle 
   float* r = static_cast<float*>(bt->r);
   float* p = static_cast<float*>(bt->p);
   float* Ap = static_cast<float*>(bt->Ap);
-  const int vg = bx_vgrid(ctx);
-  k_bx_p<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
+  k_bx_p<float><<<bx_vgrid(ctx, (const void*)k_bx_p<float>), kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
   MFE_TRY(bx_spmv32(ctx, R, R.open, p, Ap));
-  k_bx_update<float><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), bt->x32, r, p, Ap);
+  k_bx_update<float><<<bx_vgrid(ctx, (const void*)k_bx_update<float>), kBxVT, 0, ctx->stream>>>(
+      bx_vec(R, R.open), bt->x32, r, p, Ap);
   MFE_TRY(check_launch(ctx, "k_bx_update"));
   k_bx_decide<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.gate);
   MFE_TRY(check_launch(ctx, "k_bx_decide"));
-  k_bx_xupdate<<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.gate), bt->x, bt->x32);
+  k_bx_xupdate<<<bx_vgrid(ctx, (const void*)k_bx_xupdate), kBxVT, 0, ctx->stream>>>(
+      bx_vec(R, R.gate), bt->x, bt->x32);
   MFE_TRY(check_launch(ctx, "k_bx_xupdate"));
   MFE_TRY(bx_spmv64<BX_RESID>(ctx, R, R.gate, bt->x, nullptr, bt->b, r));
   k_bx_after<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open, h, in_graph);
@@ -989,11 +991,11 @@ mfe_status bx_iter_f64(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle h,
   double* r = static_cast<double*>(bt->r);
   double* p = static_cast<double*>(bt->p);
   double* Ap = static_cast<double*>(bt->Ap);
-  const int vg = bx_vgrid(ctx);
-  k_bx_p<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
+  k_bx_p<double><<<bx_vgrid(ctx, (const void*)k_bx_p<double>), kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
   MFE_TRY(bx_spmv64<BX_DOT>(ctx, R, R.open, p, Ap, nullptr, nullptr));
-  k_bx_update<double><<<vg, kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), bt->x, r, p, Ap);
+  k_bx_update<double><<<bx_vgrid(ctx, (const void*)k_bx_update<double>), kBxVT, 0, ctx->stream>>>(
+      bx_vec(R, R.open), bt->x, r, p, Ap);
   MFE_TRY(check_launch(ctx, "k_bx_update"));
   k_bx_after64<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open, h, in_graph);
   return check_launch(ctx, "k_bx_after64");
@@ -1294,6 +1296,11 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
     MFE_TRY(bx_spmv64<BX_RESID>(ctx, R, R.all, bt->x, static_cast<double*>(bt->r), bt->b, nullptr));
   k_bx_init<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open);
   MFE_TRY(check_launch(ctx, "k_bx_init"));
+  // occupancy queries before the loop is captured
+  for (const void* k : {(const void*)k_bx_p<float>, (const void*)k_bx_update<float>,
+                        (const void*)k_bx_xupdate, (const void*)k_bx_p<double>,
+                        (const void*)k_bx_update<double>})
+    bx_vgrid(ctx, k);
   MFE_TRY(bx_loop(ctx, bt->ctl, [&](cudaGraphConditionalHandle h, int in_graph) -> mfe_status {
     return R.mixed ? bx_iter_mixed(ctx, R, h, in_graph) : bx_iter_f64(ctx, R, h, in_graph);
   }));

@@ -52,6 +52,12 @@ void* workspace(mfe_ctx* ctx, const char* name, size_t bytes);
 // Pinned host scratch of at least `bytes`.
 void* host_scratch(mfe_ctx* ctx, size_t bytes);
 
+// Blocks of `kernel` (threads per block, dynamic shared memory) resident at
+// once on the context's device: occupancy x SM count, cached per kernel and
+// device.  Grid-stride kernels sized to it run in one wave instead of a full
+// wave plus a partial one.  Call it once before a graph capture.
+int resident_blocks(mfe_ctx* ctx, const void* kernel, int threads, size_t smem);
+
 // ---- assembly (mfe_assemble.cu) ----
 mfe_status launch_structure(mfe_ctx* ctx, int nx, int ny, int nz, int32_t* ro, int32_t* cols);
 mfe_status launch_assemble(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,

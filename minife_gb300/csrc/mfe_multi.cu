@@ -1038,11 +1038,29 @@ mfe_status ell32_grid(mfe_ctx* ctx, int* grid)
   return MFE_OK;
 }
 
-int vgrid(mfe_ctx* ctx, int64_t n)
+// One wave of resident blocks (a second, partial wave of a grid-stride
+// kernel would run at a fraction of the bandwidth): the occupancy of the
+// kernel times the SM count, cached per kernel and device.
+template <typename K>
+int vgrid(mfe_ctx* ctx, int64_t n, K kernel)
 {
+  static std::map<std::pair<const void*, int>, int> cache;
+  static std::mutex mu;
+  int per_sm = 0;
+  {
+    std::lock_guard<std::mutex> lock(mu);
+    const auto key = std::make_pair(reinterpret_cast<const void*>(kernel), ctx->device);
+    auto it = cache.find(key);
+    if (it == cache.end()) {
+      int b = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, kernel, kVT, 0) != cudaSuccess) b = 4;
+      it = cache.emplace(key, std::max(b, 1)).first;
+    }
+    per_sm = it->second;
+  }
   return (int)std::max<int64_t>(
       1, std::min<int64_t>({ceil_div(std::max<int64_t>(n, 1), (int64_t)kVT),
-                            (int64_t)ctx->sm_count * 8, (int64_t)kMaxPartM}));
+                            (int64_t)ctx->sm_count * per_sm, (int64_t)kMaxPartM}));
 }
 
 // one iteration of the mixed solver: FP32 SpMM, FP32 vectors, gated FP64
@@ -1052,7 +1070,7 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
                             cudaGraphConditionalHandle h, int in_graph)
 {
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
-  k_mr_p<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
+  k_mr_p<float><<<vgrid(ctx, ntot, k_mr_p<float>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
   if (W.ell) {
     Ell32Params E;
@@ -1073,12 +1091,12 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
                                                   W.partials, W.tickets, W.st->pAp, nullptr, W.err,
                                                   W.st)));
   }
-  k_mr_update<float><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
+  k_mr_update<float><<<vgrid(ctx, ntot, k_mr_update<float>), kVT, 0, ctx->stream>>>(
       ntot, nrhs, W.x32, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mr_update"));
   k_mr_decide<<<1, 32, 0, ctx->stream>>>(W.st);
   MFE_TRY(check_launch(ctx, "k_mr_decide"));
-  k_mr_xupdate<<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, X, W.x32, W.st);
+  k_mr_xupdate<<<vgrid(ctx, ntot, k_mr_xupdate), kVT, 0, ctx->stream>>>(ntot, X, W.x32, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_xupdate"));
   MFE_TRY((launch_spmm_t<double, MM_RESID, float>(ctx, &A64, nrhs, X, nullptr, B, W.r, W.partials,
                                                    W.tickets, W.st->rr_true, &W.st->gate, W.err)));
@@ -1091,12 +1109,12 @@ mfe_status multi_iter_f64(mfe_ctx* ctx, const mfe_csr& A64, int nrhs, double* X,
                           const MultiBufs<double>& W, cudaGraphConditionalHandle h, int in_graph)
 {
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
-  k_mr_p<double><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
+  k_mr_p<double><<<vgrid(ctx, ntot, k_mr_p<double>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
   MFE_TRY((launch_spmm_t<double, MM_DOT, double>(ctx, &A64, nrhs, W.p, W.Ap, nullptr, nullptr,
                                                   W.partials, W.tickets, W.st->pAp, nullptr, W.err,
                                                   W.st)));
-  k_mr_update<double><<<vgrid(ctx, ntot), kVT, 0, ctx->stream>>>(
+  k_mr_update<double><<<vgrid(ctx, ntot, k_mr_update<double>), kVT, 0, ctx->stream>>>(
       ntot, nrhs, X, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mr_update"));
   k_mr_after64<<<1, 32, 0, ctx->stream>>>(W.st, h, in_graph);
@@ -1293,6 +1311,14 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   MFE_TRY(check_launch(ctx, "k_mr_init"));
 
   // kernel attributes and occupancy are set up before the loop is captured
+  if (mixed) {
+    vgrid(ctx, ntot, k_mr_p<float>);
+    vgrid(ctx, ntot, k_mr_update<float>);
+    vgrid(ctx, ntot, k_mr_xupdate);
+  } else {
+    vgrid(ctx, ntot, k_mr_p<double>);
+    vgrid(ctx, ntot, k_mr_update<double>);
+  }
   if (mixed) {
     MFE_TRY((spmm_setup<float, MM_DOT, float>(ctx, nrhs, nullptr)));
   } else {
