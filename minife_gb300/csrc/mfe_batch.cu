@@ -735,8 +735,10 @@ __global__ void __launch_bounds__(1024)
   if (b < nbox && st[b].open) {
     BoxSt& s = st[b];
     if (s.brk) {
+      // p.Ap <= 0 in iteration k (0 after an exact solve): stop with the k-1
+      // completed updates, as the reference's breakdown exit does
       s.open = 0;
-      s.iters = k;
+      s.iters = k - 1;
       atomicOr(&any_brk, 1);
     } else if (s.gate) {
       atomicOr(&any_gate, 1);
@@ -791,7 +793,7 @@ __global__ void __launch_bounds__(1024)
     BoxSt& s = st[b];
     if (s.brk) {
       s.open = 0;
-      s.iters = k;
+      s.iters = k - 1;
       atomicOr(&any_brk, 1);
     } else if (k + 1 <= ctl->max_iter && s.normr > s.tol_abs) {
       s.beta = s.rr_new / s.rr;

@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(kT)
 {
   __shared__ double red[32];
   __shared__ float s_alpha;
-  if (threadIdx.x == 0) s_alpha = (float)(st->rr / st->pAp);
+  if (threadIdx.x == 0) s_alpha = st->pAp > 0.0 ? (float)(st->rr / st->pAp) : 0.0f;
   __syncthreads();
   const float alpha = s_alpha;
   double acc = 0.0;

@@ -74,6 +74,7 @@ struct MultiState {
   double normr_true[kMaxRhs];
   int done[kMaxRhs];
   int iters[kMaxRhs];  // iterations until each right-hand side converged
+  int brk[kMaxRhs];    // p.Ap <= 0 met (the right-hand side stops alone)
   int nrhs, k, max_iter, since, refine_k, gate, cont, first, updates, status, tol_mode;
   unsigned err;
   double delta2;
@@ -124,7 +125,8 @@ __device__ void multi_dot_reduce(double v, double* red, double* partials, unsign
     double s = 0.0;
     for (unsigned bl = 0; bl < gridDim.x; ++bl) s += __ldcg(&partials[(size_t)bl * 32 + threadIdx.x]);
     out[threadIdx.x] = s;
-    if (cg) cg->alpha[threadIdx.x] = cg->done[threadIdx.x] ? 0.0 : cg->rr[threadIdx.x] / s;
+    if (cg)
+      cg->alpha[threadIdx.x] = cg->done[threadIdx.x] || !(s > 0.0) ? 0.0 : cg->rr[threadIdx.x] / s;
   }
   if (threadIdx.x == 0) *ticket = 0u;
 }
@@ -811,7 +813,10 @@ __global__ void k_mr_decide(MultiState* st)
   const int nr = st->nrhs;
   bool ready = true, brk = false;
   if (j < nr && !st->done[j]) {
+    // p.Ap <= 0 (alpha was 0): this right-hand side stops at the reliable
+    // update taken now, converged if its true residual says so
     brk = !(st->pAp[j] > 0.0);
+    if (brk) st->brk[j] = 1;
     const double t = st->rr_new[j];
     ready = t < st->delta2 * st->rr_at_update[j] || t <= st->tol_abs[j] * st->tol_abs[j];
   }
@@ -821,8 +826,7 @@ __global__ void k_mr_decide(MultiState* st)
     st->k += 1;
     st->since += 1;
     st->first = 0;
-    if (any_brk) st->status = MFE_BREAKDOWN;
-    st->gate = st->status == 0 && (all_ready || st->since >= st->refine_k || st->k >= st->max_iter);
+    st->gate = all_ready || any_brk || st->since >= st->refine_k || st->k >= st->max_iter;
   }
 }
 
@@ -833,12 +837,16 @@ __global__ void k_mr_after(MultiState* st, cudaGraphConditionalHandle h, int in_
   const int j = threadIdx.x;
   const int nr = st->nrhs;
   const int gate = st->gate;
-  if (j < nr && !st->done[j] && st->status == 0) {
+  if (j < nr && !st->done[j]) {
     if (gate) {
       st->normr_true[j] = sqrt(st->rr_true[j]);
       if (st->normr_true[j] <= st->tol_abs[j]) {
         st->done[j] = 1;
         st->iters[j] = st->k;
+        st->brk[j] = 0;
+      } else if (st->brk[j]) {
+        st->done[j] = 1;
+        st->iters[j] = st->k - 1;
       } else {
         st->beta[j] = st->rr_true[j] / st->rr[j];
         st->rr[j] = st->rr_true[j];
@@ -856,7 +864,7 @@ __global__ void k_mr_after(MultiState* st, cudaGraphConditionalHandle h, int in_
       st->since = 0;
     }
     st->gate = 0;
-    st->cont = open && st->status == 0 && st->k < st->max_iter;
+    st->cont = open && st->k < st->max_iter;
     if (in_graph) cudaGraphSetConditional(h, st->cont ? 1u : 0u);
   }
 }
@@ -870,10 +878,14 @@ __global__ void k_mr_after64(MultiState* st, cudaGraphConditionalHandle h, int i
   const int j = threadIdx.x;
   const int nr = st->nrhs;
   const int k = st->k + 1;
-  bool brk = false;
   if (j < nr && !st->done[j]) {
-    brk = !(st->pAp[j] > 0.0);
-    if (k + 1 <= st->max_iter && st->normr_true[j] > st->tol_abs[j]) {
+    if (!(st->pAp[j] > 0.0)) {
+      // the reference reports a breakdown and returns with the k-1
+      // completed iterations (cg_solve.hpp:186-198); the others go on
+      st->brk[j] = 1;
+      st->done[j] = 1;
+      st->iters[j] = k - 1;
+    } else if (k + 1 <= st->max_iter && st->normr_true[j] > st->tol_abs[j]) {
       const double rn = st->rr_new[j];
       st->beta[j] = rn / st->rr[j];
       st->rr[j] = rn;
@@ -883,13 +895,11 @@ __global__ void k_mr_after64(MultiState* st, cudaGraphConditionalHandle h, int i
       st->iters[j] = k;
     }
   }
-  const bool any_brk = __any_sync(0xffffffffu, brk);
   const bool open = __any_sync(0xffffffffu, j < nr && !st->done[j]);
   if (j == 0) {
     st->k = k;
     st->first = 0;
-    if (any_brk) st->status = MFE_BREAKDOWN;
-    st->cont = open && st->status == 0;
+    st->cont = open;
     if (in_graph) cudaGraphSetConditional(h, st->cont ? 1u : 0u);
   }
 }
@@ -1356,8 +1366,9 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
     res.times[4] = ms * 1e-3;
     res.refinements = hs->updates;
     res.fp64_spmvs = mixed ? hs->updates + 1 : hs->k + 1;
-    const bool converged = mixed ? hs->done[j] != 0 : !(hs->normr_true[j] > hs->tol_abs[j]);
-    res.status = hs->status ? MFE_BREAKDOWN : (converged ? MFE_OK : MFE_MAXITER);
+    const bool converged = mixed ? hs->done[j] != 0 && !hs->brk[j]
+                                 : !(hs->normr_true[j] > hs->tol_abs[j]);
+    res.status = hs->brk[j] ? MFE_BREAKDOWN : (converged ? MFE_OK : MFE_MAXITER);
     if (res.status != MFE_OK && worst == MFE_OK) worst = (mfe_status)res.status;
   }
   return worst;

@@ -132,3 +132,30 @@ def test_autotune_small_batch(tmp_path, monkeypatch):
     assert all(r.status == 0 for r in res)
     assert autotune.tune_batch(b)["cached"]
     b.close()
+
+
+def test_batch_tiny_boxes_and_breakdown():
+    """Boxes of one to a few elements next to ordinary ones.  1x1x1, 1x1x2 and
+    5x3x1 have only Dirichlet rows or nearly: CG solves them exactly in one
+    iteration and the next meets p.Ap = 0, where the reference reports a
+    breakdown and returns (cg_solve.hpp:186-198; the oracle does the same,
+    with one completed iteration and normr 0).  The other boxes are not
+    affected."""
+    dims = [(1, 1, 1), (1, 1, 2), (5, 3, 1), (2, 2, 2), (6, 7, 8)]
+    for prec in ("f64", "mixed"):
+        x, off, res = M.batch_solve_boxes(dims, max_iter=500, tol=1e-10, tol_mode="relative",
+                                          precision=prec)
+        xh = host(x)
+        for i, d in enumerate(dims):
+            ro, cols, vals, b = O.build_system(*d)
+            xo, it, nr, st = O.cg_solve(ro, cols, vals, b, max_iter=500, tol=1e-10, tol_mode=1)
+            xi = xh[off[i]:off[i + 1]]
+            assert np.all(np.isfinite(xi)), (prec, d)
+            rel = np.linalg.norm(b - O.matvec(ro, cols, vals, xi)) / np.linalg.norm(b)
+            assert rel <= 1e-9, (prec, d, rel)
+            if st == 1:  # the oracle broke down after an exact solve
+                assert res[i].status in (0, 4), (prec, d, res[i])
+                if prec == "f64":
+                    assert res[i].status == 4 and res[i].num_iters == it and res[i].normr == 0.0
+            else:
+                assert res[i].status == 0, (prec, d, res[i])

@@ -172,3 +172,34 @@ def test_spmm_fp32_box_and_generic_agree():
     M.spmm(A, X.double().contiguous(), Yref)
     err = (Y.double() - Yref).abs().max().item()
     assert err <= 1e-5 * Yref.abs().max().item()
+
+
+def test_multi_column_breakdown_is_local():
+    """A right-hand side that CG solves exactly in one iteration (a unit
+    vector on a Dirichlet row) meets p.Ap = 0 next; FP64 mode stops that
+    column alone with the reference's breakdown (one completed iteration),
+    mixed mode finishes it on its true residual; the other columns converge
+    as usual."""
+    dims = (9, 8, 7)
+    A, b = M.build_system(*dims)
+    B = rhs_block(b, 4, seed=21)
+    B[:, 1] = 0.0
+    B[0, 1] = 1.0  # row 0 (node (0,0,0)) is a Dirichlet row
+    ro, cols, vals, _ = O.build_system(*dims)
+    Bh = host(B)
+    for prec in ("f64", "mixed"):
+        X = torch.zeros_like(B)
+        res = M.cg_solve_multi(A, B, X, max_iter=1000, tol=1e-10, tol_mode="relative",
+                               precision=prec)
+        Xh = host(X)
+        assert np.all(np.isfinite(Xh))
+        assert np.allclose(Xh[:, 1], Bh[:, 1], rtol=0, atol=1e-15)
+        if prec == "f64":
+            assert res[1].status == 4 and res[1].num_iters == 1
+        else:
+            assert res[1].status == 0
+        for j in (0, 2, 3):
+            assert res[j].status == 0, (prec, j, res[j])
+            rel = np.linalg.norm(Bh[:, j] - O.matvec(ro, cols, vals, Xh[:, j])) / \
+                np.linalg.norm(Bh[:, j])
+            assert rel <= 1e-9, (prec, j, rel)
