@@ -285,6 +285,18 @@ mfe_status mfe_verify_solution(mfe_ctx* ctx, int nx, int ny, int nz, const doubl
 mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const double* u,
                                 const double* lambda, double* g);
 
+/* The whole adjoint gradient in one call: L = 1/2 ||u - u_target||^2 over all
+ * nodes, u solving the box problem assembled with per-element conductivity
+ * kappa (device, nx*ny*nz; NULL: k = 1 everywhere); grad (device, nx*ny*nz)
+ * receives dL/dkappa: forward CG, adjoint CG on (u - u_target) with its
+ * Dirichlet rows zeroed, element contraction (mfe_element_gradient).  opts
+ * (relative tolerance recommended) serve both solves; u_out (device, rows),
+ * loss (host), fwd and adj (host results) may be NULL. */
+mfe_status mfe_adjoint_grad(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,
+                            const double* u_target, const mfe_cg_opts* opts, double* u_out,
+                            double* grad, double* loss, mfe_cg_result* fwd,
+                            mfe_cg_result* adj);
+
 /* v[r] = 0 on every Dirichlet row of the box (faces of both boundary sets of
  * simple_mesh_description.hpp:62-224).  Used to form the adjoint right-hand
  * side of a box solve, which must vanish on the prescribed rows. */

@@ -110,6 +110,9 @@ SIGNATURES = {
     "mfe_element_gradient": (ctypes.c_int, [c_void_p] + [ctypes.c_int] * 3 +
                              [c_void_p, c_void_p, c_void_p]),
     "mfe_box_zero_boundary": (ctypes.c_int, [c_void_p] + [ctypes.c_int] * 3 + [c_void_p]),
+    "mfe_adjoint_grad": (ctypes.c_int, [c_void_p] + [ctypes.c_int] * 3 +
+                         [c_void_p, c_void_p, _P(MfeCgOpts), c_void_p, c_void_p, _P(c_double),
+                          _P(MfeCgResult), _P(MfeCgResult)]),
     "mfe_spmm": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_int32, c_void_p, c_void_p]),
     "mfe_cg_solve_multi": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_int32, c_void_p, c_void_p,
                                           _P(MfeCgOpts), _P(MfeCgResult)]),

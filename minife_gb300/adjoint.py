@@ -68,6 +68,27 @@ def solve(kappa, dims, tol=1e-10, max_iter=20000, precision="f64"):
                           precision)
 
 
+def grad_l2(kappa, dims, u_target, tol=1e-10, max_iter=20000, precision="f64", ctx=None):
+    """(loss, grad, u) of L = 1/2 ||u - u_target||^2 in one native call
+    (mfe_adjoint_grad): forward solve, adjoint solve and element contraction
+    without the autograd tape."""
+    import ctypes
+    from . import MfeCgResult, _opts, _ptr, default_context
+    ctx = ctx or default_context()
+    nx, ny, nz = (int(d) for d in dims)
+    kap = kappa.detach().to(torch.float64).contiguous()
+    tgt = u_target.detach().to(torch.float64).contiguous()
+    u = torch.empty_like(tgt)
+    g = torch.empty_like(kap)
+    o, _ = _opts(max_iter, tol, "relative", precision)
+    loss = ctypes.c_double()
+    rf, ra = MfeCgResult(), MfeCgResult()
+    ctx.check(ctx.lib.mfe_adjoint_grad(ctx.h, nx, ny, nz, _ptr(kap), _ptr(tgt), ctypes.byref(o),
+                                       _ptr(u), _ptr(g), ctypes.byref(loss), ctypes.byref(rf),
+                                       ctypes.byref(ra)), "mfe_adjoint_grad")
+    return loss.value, g, u
+
+
 def loss_l2(u, u_target):
     return 0.5 * torch.sum((u - u_target) ** 2)
 

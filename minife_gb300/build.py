@@ -34,6 +34,7 @@ SOURCES = {
     "mfe_dump.cu": [],
     "mfe_pcg.cu": [],
     "mfe_ell.cu": [],
+    "mfe_adjoint.cu": [],
     "mfe_cg.cu": [],
 }
 

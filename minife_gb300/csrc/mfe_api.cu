@@ -608,6 +608,24 @@ mfe_status mfe_element_gradient(mfe_ctx* ctx, int nx, int ny, int nz, const doub
   return launch_element_gradient(ctx, nx, ny, nz, u, lambda, g);
 }
 
+mfe_status mfe_adjoint_grad(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,
+                            const double* u_target, const mfe_cg_opts* opts, double* u_out,
+                            double* grad, double* loss, mfe_cg_result* fwd, mfe_cg_result* adj)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  if (!u_target || !grad) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  if (!box_ok(nx, ny, nz)) return fail(ctx, MFE_BAD_ARG, "bad box");
+  mfe_cg_opts o;
+  if (opts) o = *opts;
+  else mfe_cg_opts_default(&o);
+  if (o.max_iter < 0 || !(o.tol >= 0.0) ||
+      (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED) ||
+      (o.precond != 0 && o.precond != 1))
+    return fail(ctx, MFE_BAD_ARG, "bad CG options");
+  MFE_TRY(set_device(ctx));
+  return adjoint_grad(ctx, nx, ny, nz, kappa, u_target, &o, u_out, grad, loss, fwd, adj);
+}
+
 mfe_status mfe_box_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v)
 {
   if (!ctx || !v) return fail(ctx, MFE_BAD_ARG, "bad arguments");

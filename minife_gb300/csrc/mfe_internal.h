@@ -105,6 +105,11 @@ mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const doubl
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,
                     const mfe_cg_opts* opts, mfe_cg_result* res);
 
+// ---- adjoint gradient (mfe_adjoint.cu) ----
+mfe_status adjoint_grad(mfe_ctx* ctx, int nx, int ny, int nz, const double* kappa,
+                        const double* u_target, const mfe_cg_opts* opts, double* u_out,
+                        double* grad, double* loss, mfe_cg_result* fwd, mfe_cg_result* adj);
+
 // ---- the reference's ELL matrix (mfe_ell.cu) ----
 mfe_status launch_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E);
 // CSR view of an ELL matrix (row offsets r * ncols_per_row, cached in workspace)

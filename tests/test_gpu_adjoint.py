@@ -94,3 +94,22 @@ def test_adjoint_matches_central_differences(dims, nfd):
     scale = np.abs(g).max()
     err = np.abs(fd - g[elems]).max()
     assert err <= 1e-4 * scale, (err, scale, fd[:4], g[elems][:4])
+
+
+@pytest.mark.parametrize("dims", [(8, 7, 6), (12, 10, 9)])
+def test_native_adjoint_grad_matches_oracle_and_autograd(dims):
+    """mfe_adjoint_grad (forward solve, adjoint solve and contraction in one C
+    call) against the oracle's FP64 gradient and the autograd path."""
+    kappa, kappa_t = setup_problem(dims)
+    ut = gpu_target(dims, kappa_t)
+    k = torch.from_numpy(kappa).cuda()
+    loss, g, u = adjoint.grad_l2(k, dims, ut, tol=1e-13)
+    g_ref, u_ref = oracle_gradient(dims, kappa, ut.cpu().numpy())
+    assert np.linalg.norm(u.cpu().numpy() - u_ref) <= 1e-10 * np.linalg.norm(u_ref)
+    assert abs(loss - 0.5 * float(np.sum((u_ref - ut.cpu().numpy()) ** 2))) <= 1e-9 * loss
+    scale = np.abs(g_ref).max()
+    assert np.abs(g.cpu().numpy() - g_ref).max() <= 1e-8 * scale
+    ka = k.clone().requires_grad_(True)
+    la = adjoint.loss_l2(adjoint.solve(ka, dims, tol=1e-13), ut)
+    la.backward()
+    assert np.abs(ka.grad.cpu().numpy() - g.cpu().numpy()).max() <= 1e-9 * scale
