@@ -543,7 +543,8 @@ def run_probe(args):
     and a 4-iteration CG solve; 'multi' = the system and a 6-iteration
     mixed-precision solve of 32 right-hand sides (reliable update every 3);
     'batch' = the first --nbox of the seeded uneven boxes solved together in
-    mixed precision to 1e-8 (default shape, refine_k 50)."""
+    mixed precision to 1e-8 (default shape, refine_k 50); 'mixed' = the
+    system solved in mixed precision to 1e-8 (--refine-k)."""
     import torch
     import minife_gb300 as M
     torch.cuda.set_device(0)
@@ -569,6 +570,11 @@ def run_probe(args):
             M.matvec(A32, x32, y32)
     elif args.probe == "batch":
         pass
+    elif args.probe == "mixed":
+        x = torch.zeros_like(b)
+        r = M.cg_solve(A, b, x, max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed",
+                       refine_k=args.refine_k)
+        print("mixed: %d inner iterations, %d reliable updates" % (r.num_iters, r.refinements))
     elif args.probe == "multi":
         g = torch.Generator(device="cpu").manual_seed(0)
         B = torch.randn(A.nrows, 32, generator=g, dtype=torch.float64).cuda().contiguous()
@@ -585,7 +591,7 @@ def run_probe(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["spmv", "cg", "multi", "batch"], default=None,
+    ap.add_argument("--probe", choices=["spmv", "cg", "mixed", "multi", "batch"], default=None,
                     help="run a small fixed workload for a profiler capture and exit")
     ap.add_argument("--dims", type=int, default=128)
     ap.add_argument("--nbox", type=int, default=96, help="boxes of the batch probe")
