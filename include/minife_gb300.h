@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MFE_ABI_VERSION 1
+#define MFE_ABI_VERSION 2
 
 typedef enum mfe_status {
   MFE_OK = 0,
@@ -225,6 +225,12 @@ typedef struct mfe_cg_opts {
                            library converts and caches one) */
   int32_t precond;      /* mfe_cg_solve: 0 none (the reference's CG), 1 Jacobi
                            (M = diag(A), FP64; stops on ||r|| after the update) */
+  int32_t mixed_operator; /* mixed, single right-hand side: 0 = the FP32
+                           stencil operator when every row of A lies within
+                           2^-22 (relative to the row) of its boundary class's
+                           stencil (checked on the device; a miniFE box with
+                           k = 1), else the FP32 copy of the values;
+                           1 = always the FP32 copy of the values */
 } mfe_cg_opts;
 
 /* Fill opts with the reference's defaults (max_iter 200, absolute tol
@@ -244,7 +250,18 @@ typedef struct mfe_cg_result {
                            accounted to MATVECDOT and WAXPY */
   int32_t refinements;  /* mixed: outer refinement sweeps */
   int32_t fp64_spmvs;   /* number of FP64 matvecs performed */
+  int32_t inner_operator; /* mixed solves: the FP32 operator of the inner
+                             iteration, one of mfe_inner_operator; 0 for
+                             FP64 solves */
 } mfe_cg_result;
+
+/* mfe_cg_result.inner_operator */
+typedef enum mfe_inner_operator {
+  MFE_INNER_NONE = 0,
+  MFE_INNER_STENCIL = 1,  /* verified 27-coefficient stencil (x and y only) */
+  MFE_INNER_VALUES = 2,   /* FP32 copy of the CSR values */
+  MFE_INNER_PADDED = 3    /* FP32 values padded to fixed-length rows */
+} mfe_inner_operator;
 
 /* cg_solve (ref/src/cg_solve.hpp:69-229) with matvec_std: solves A x = b
  * from the initial guess in x (device).  FP64 precision follows the

@@ -387,6 +387,9 @@ class CGResult:
     times: tuple
     refinements: int
     history: list | None = None
+    # mixed solves: the FP32 operator of the inner iteration ("stencil",
+    # "values" or "padded"); "none" for FP64 solves
+    inner_operator: str = "none"
 
     @property
     def total_time(self) -> float:
@@ -394,7 +397,7 @@ class CGResult:
 
 
 def _opts(max_iter, tol, tol_mode, precision, refine_k=0, inner_tol=0.0, max_refine=0,
-          record_history=False, A32=None, precond="none"):
+          record_history=False, A32=None, precond="none", mixed_operator="auto"):
     o = MfeCgOpts()
     _abi.load().mfe_cg_opts_default(ctypes.byref(o))
     o.max_iter = int(max_iter)
@@ -406,6 +409,7 @@ def _opts(max_iter, tol, tol_mode, precision, refine_k=0, inner_tol=0.0, max_ref
     o.max_refine = int(max_refine)
     o.record_history = 1 if record_history else 0
     o.precond = {"none": 0, "jacobi": 1}[precond]
+    o.mixed_operator = {"auto": 0, "values": 1}[mixed_operator]
     keep = None
     if A32 is not None:
         keep = A32.c()
@@ -421,24 +425,34 @@ def _result(ctx, r: MfeCgResult, record_history: bool) -> CGResult:
         buf = (ctypes.c_double * max(cnt.value, 1))()
         ctx.lib.mfe_cg_history(ctx.h, buf, cnt.value, ctypes.byref(cnt))
         hist = list(buf[: cnt.value])
+    return _cg_result(r, hist)
+
+
+_INNER = {0: "none", 1: "stencil", 2: "values", 3: "padded"}
+
+
+def _cg_result(r: MfeCgResult, hist=None) -> CGResult:
     return CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status, tuple(r.times),
-                    r.refinements, hist)
+                    r.refinements, hist, _INNER.get(r.inner_operator, "none"))
 
 
 def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
              tol_mode: str = "absolute", precision: str = "f64", refine_k: int = 0,
              inner_tol: float = 0.0, max_refine: int = 0, record_history: bool = False,
              A32: CSRMatrix | None = None, allow_breakdown: bool = True,
-             precond: str = "none", ctx: Context | None = None) -> CGResult:
+             precond: str = "none", mixed_operator: str = "auto",
+             ctx: Context | None = None) -> CGResult:
     """cg_solve (ref/src/cg_solve.hpp:69) on device vectors; x holds the
     initial guess and receives the solution.  Breakdown (the reference prints
     an error and returns) is reported in CGResult.status unless
     allow_breakdown is False.  precond="jacobi" runs the Jacobi-preconditioned
-    CG (FP64, stops on ||r|| after the update)."""
+    CG (FP64, stops on ||r|| after the update).  mixed_operator="values"
+    makes the mixed solver use the FP32 copy of the values even where the
+    verified FP32 stencil operator applies ("auto")."""
     ctx = ctx or default_context()
     m = A.c()
     o, keep = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine,
-                    record_history, A32, precond)
+                    record_history, A32, precond, mixed_operator)
     r = MfeCgResult()
     st = ctx.lib.mfe_cg_solve(ctx.h, ctypes.byref(m), _ptr(b), _ptr(x), ctypes.byref(o),
                               ctypes.byref(r))
@@ -468,8 +482,7 @@ def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPS
                                     ctypes.byref(o), res)
     if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
         ctx.check(st, "mfe_cg_solve_multi")
-    return [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status, tuple(r.times),
-                     r.refinements, None) for r in res]
+    return [_cg_result(r) for r in res]
 
 
 class Batch:
@@ -530,8 +543,7 @@ class Batch:
         st = ctx.lib.mfe_batch_solve(ctx.h, self.h, ctypes.byref(o), _ptr(x), res)
         if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
             ctx.check(st, "mfe_batch_solve")
-        return x, [CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status,
-                            tuple(r.times), r.refinements, None) for r in res]
+        return x, [_cg_result(r) for r in res]
 
 
 def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,

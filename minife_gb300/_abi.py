@@ -40,7 +40,7 @@ class MfeCgOpts(ctypes.Structure):
         ("max_iter", c_int32), ("tol_mode", c_int32), ("tol", c_double),
         ("precision", c_int32), ("refine_k", c_int32), ("inner_tol", c_double),
         ("max_refine", c_int32), ("record_history", c_int32),
-        ("A32", ctypes.POINTER(MfeCsr)), ("precond", c_int32),
+        ("A32", ctypes.POINTER(MfeCsr)), ("precond", c_int32), ("mixed_operator", c_int32),
     ]
 
 
@@ -48,7 +48,7 @@ class MfeCgResult(ctypes.Structure):
     _fields_ = [
         ("num_iters", c_int32), ("status", c_int32), ("normr", c_double),
         ("normr0", c_double), ("final_resid", c_double), ("times", c_double * 5),
-        ("refinements", c_int32), ("fp64_spmvs", c_int32),
+        ("refinements", c_int32), ("fp64_spmvs", c_int32), ("inner_operator", c_int32),
     ]
 
 

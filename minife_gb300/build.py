@@ -35,6 +35,7 @@ SOURCES = {
     "mfe_pcg.cu": [],
     "mfe_ell.cu": [],
     "mfe_adjoint.cu": [],
+    "mfe_stencil.cu": [],
     "mfe_cg.cu": [],
 }
 

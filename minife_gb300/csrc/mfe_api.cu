@@ -318,7 +318,6 @@ mfe_status mfe_csr_free(mfe_ctx* ctx, mfe_csr* A)
   if (A->row_offsets) cudaFree(A->row_offsets);
   if (A->cols) cudaFree(A->cols);
   if (A->vals) cudaFree(A->vals);
-  if (ctx->f32_src_vals == A->vals) ctx->f32_src_vals = nullptr;
   memset(A, 0, sizeof(*A));
   return MFE_OK;
 }

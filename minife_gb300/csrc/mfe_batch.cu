@@ -1335,6 +1335,7 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
     r.times[0] = bt->assembly_s;  // assembly of the whole batch
     r.times[4] = ms * 1e-3;       // the batched solve
     r.refinements = hc.updates;
+    r.inner_operator = R.mixed ? MFE_INNER_PADDED : MFE_INNER_NONE;
     r.status = s.brk ? MFE_BREAKDOWN : (s.normr <= s.tol_abs ? MFE_OK : MFE_MAXITER);
     if (r.status != MFE_OK && worst == MFE_OK) worst = (mfe_status)r.status;
   }

@@ -29,12 +29,6 @@ struct mfe_ctx {
   size_t host_scratch_bytes = 0;
   mfe_cg_graph* cg_graph = nullptr;
   std::vector<double> history;
-  // cached FP32 copy of a matrix for the mixed-precision solver
-  const void* f32_src_vals = nullptr;
-  int64_t f32_src_nnz = 0;
-  // cached padded 28-per-row FP32 copy (multi-RHS mixed solver)
-  const void* ell28_src = nullptr;
-  int64_t ell28_nnz = 0;
   mfe_csr f32_copy{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 };
@@ -97,9 +91,30 @@ mfe_status launch_spmv_box(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* 
                            const DotSink* sink, const double* resid_b, void* cg_state);
 // r32 = (float)(b - A64 x), ||b - A64 x||^2 (FP64) into sink->out; when gate
 // is set the launch does nothing unless *gate != 0 (read on the device).
+// r32_pad > 0: r32 has rows of Nx + r32_pad entries (x-padded layout).
 mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const double* x,
                                    const double* b, float* r32, const DotSink* sink,
-                                   const int* gate);
+                                   const int* gate, int r32_pad = 0);
+
+// ---- FP32 stencil operator of the mixed solver (mfe_stencil.cu) ----
+// The stencil SpMV works on x-padded vectors: node (ix, iy, iz) at
+// (iz * Ny + iy) * Nxp + ix with Nxp = Nx rounded up to a multiple of 4; the
+// entries ix >= Nx are zero.  stencil_pitch is Nxp, stencil_rows the padded
+// length, stencil_ghost the zero rows needed on both sides of the vector the
+// SpMV reads.
+int stencil_pitch(const mfe_csr* A);
+int64_t stencil_rows(const mfe_csr* A);
+int64_t stencil_ghost(const mfe_csr* A);
+// checks that A64 is a miniFE box operator (Dirichlet rows dd * I, interior
+// rows one 27-point stencil with Dirichlet neighbours zeroed) to FP32
+// accuracy, row by row; on success coef[0..26] is the interior stencil in
+// slot order (dz, dy, dx) and coef[27] = dd
+mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok);
+mfe_status stencil_grid(mfe_ctx* ctx, int* grid);
+// y = S x and x.y into sink->out, both x-padded (y's padding entries are
+// written as zeros); x has stencil_ghost rows of zeros on both sides
+mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef, const float* x,
+                               float* y, const DotSink* sink, int grid, unsigned* err);
 
 // ---- mixed-precision CG (mfe_mixed.cu) ----
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,

@@ -149,13 +149,16 @@ __global__ void __launch_bounds__(kT)
 }
 
 // reliable update, part 1 (gated): x += x32, x32 = 0
+// x32 may be x-padded (rows of Nx + pad entries; row i at i + (i / Nx) * pad)
 __global__ void __launch_bounds__(kT)
-    k_mx_xupdate(int64_t n, double* __restrict__ x, float* __restrict__ x32, const MixState* st)
+    k_mx_xupdate(int64_t n, double* __restrict__ x, float* __restrict__ x32, const MixState* st,
+                 int Nx, int pad)
 {
   if (st->gate == 0) return;
   for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
-    x[i] += f2d_exact(x32[i]);
-    x32[i] = 0.0f;
+    const int64_t j = pad ? i + (i / Nx) * pad : i;
+    x[i] += f2d_exact(x32[j]);
+    x32[j] = 0.0f;
   }
 }
 
@@ -216,6 +219,12 @@ struct MixBufs {
   double* history;
   double* partials;  // 2 * kMaxPart
   unsigned* tickets; // 2
+  bool stencil = false;  // FP32 stencil operator (x-padded vectors, p with ghost zones)
+  float coef[28];        // its interior stencil and Dirichlet diagonal
+  int stencil_grid = 0;
+  int64_t nv = 0;        // length of the FP32 vectors
+  int pad = 0;           // x padding of the FP32 vectors (0: natural layout)
+  unsigned* err = nullptr;
 };
 
 // one wave of resident blocks of `kernel`
@@ -229,24 +238,28 @@ int grid_for(mfe_ctx* ctx, int64_t n, const void* kernel)
 mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, const double* b,
                        double* x, const MixBufs& B, cudaGraphConditionalHandle h, int in_graph)
 {
-  const int64_t n = A64.nrows;
-  k_mx_p<<<grid_for(ctx, n / 4, (const void*)k_mx_p), kT, 0, ctx->stream>>>(n, B.r, B.p, B.st);
+  const int64_t n = A64.nrows, nv = B.nv;
+  k_mx_p<<<grid_for(ctx, nv / 4, (const void*)k_mx_p), kT, 0, ctx->stream>>>(nv, B.r, B.p, B.st);
   MFE_TRY(check_launch(ctx, "k_mx_p"));
   DotSink s1;
   s1.partials = B.partials;
   s1.ticket = B.tickets;
   s1.out = &B.st->pAp;
-  MFE_TRY(launch_spmv(ctx, &A32, B.p, B.Ap, &s1, nullptr, nullptr));
-  k_mx_update<<<grid_for(ctx, n / 4, (const void*)k_mx_update), kT, 0, ctx->stream>>>(n, B.x32, B.r, B.p, B.Ap, B.st,
+  if (B.stencil)
+    MFE_TRY(launch_spmv_stencil(ctx, &A32, B.coef, B.p, B.Ap, &s1, B.stencil_grid, B.err));
+  else
+    MFE_TRY(launch_spmv(ctx, &A32, B.p, B.Ap, &s1, nullptr, nullptr));
+  k_mx_update<<<grid_for(ctx, nv / 4, (const void*)k_mx_update), kT, 0, ctx->stream>>>(nv, B.x32, B.r, B.p, B.Ap, B.st,
                                                              B.partials + kMaxPart, B.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mx_update"));
-  k_mx_xupdate<<<grid_for(ctx, n, (const void*)k_mx_xupdate), kT, 0, ctx->stream>>>(n, x, B.x32, B.st);
+  k_mx_xupdate<<<grid_for(ctx, n, (const void*)k_mx_xupdate), kT, 0, ctx->stream>>>(
+      n, x, B.x32, B.st, A64.box_nx + 1, B.pad);
   MFE_TRY(check_launch(ctx, "k_mx_xupdate"));
   DotSink s2;
   s2.partials = B.partials;
   s2.ticket = B.tickets;
   s2.out = &B.st->rr_true;
-  MFE_TRY(launch_box_resid_f32out(ctx, &A64, x, b, B.r, &s2, &B.st->gate));
+  MFE_TRY(launch_box_resid_f32out(ctx, &A64, x, b, B.r, &s2, &B.st->gate, B.pad));
   k_mx_after<<<1, 1, 0, ctx->stream>>>(B.st, h, in_graph);
   return check_launch(ctx, "k_mx_after");
 }
@@ -272,36 +285,53 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
     return fail(ctx, MFE_BAD_ARG, "mixed solver: matrix values and x must be 16-byte aligned");
   A64.max_row_len = 27;
 
-  // FP32 copy of the values (cached per source matrix on the context)
+  // The inner FP32 operator: the verified stencil when the matrix is a
+  // miniFE box operator (checked on every call), else an FP32 copy of the
+  // values (made on every call: a cache keyed on the values pointer would go
+  // stale when an allocator hands the same address to another matrix).
+  MixBufs B;
+  bool use_stencil = false;
+  if (o->mixed_operator == 0 && o->A32 == nullptr)
+    MFE_TRY(stencil_prepare(ctx, &A64, B.coef, &use_stencil));
   mfe_csr A32;
   if (o->A32 != nullptr) {
     A32 = *o->A32;
     if (A32.dtype != MFE_F32 || A32.nnz != A64.nnz || A32.nrows != n)
       return fail(ctx, MFE_BAD_ARG, "opts->A32 does not match A");
   } else {
-    float* v32 = static_cast<float*>(workspace(ctx, "mixed.vals32", sizeof(float) * (size_t)(A64.nnz + 4)));
-    if (!v32) return fail(ctx, MFE_OOM, "FP32 matrix copy allocation failed");
-    if (ctx->f32_src_vals != A64.vals || ctx->f32_src_nnz != A64.nnz) {
-      MFE_TRY(launch_convert_f32(ctx, static_cast<const double*>(A64.vals), v32, A64.nnz));
-      ctx->f32_src_vals = A64.vals;
-      ctx->f32_src_nnz = A64.nnz;
-    }
     A32 = A64;
-    A32.vals = v32;
     A32.dtype = MFE_F32;
+    A32.vals = nullptr;
+    if (!use_stencil) {
+      float* v32 = static_cast<float*>(workspace(ctx, "mixed.vals32", sizeof(float) * (size_t)(A64.nnz + 4)));
+      if (!v32) return fail(ctx, MFE_OOM, "FP32 matrix copy allocation failed");
+      MFE_TRY(launch_convert_f32(ctx, static_cast<const double*>(A64.vals), v32, A64.nnz));
+      A32.vals = v32;
+    }
   }
   A32.box_nx = A64.box_nx;
   A32.box_ny = A64.box_ny;
   A32.box_nz = A64.box_nz;
   A32.max_row_len = 27;
 
-  MixBufs B;
-  const size_t vb = sizeof(float) * (size_t)std::max<int64_t>(n + 4, 4);
+  // with the stencil the FP32 vectors are x-padded and p has ghost zones of
+  // zero rows around it
+  B.nv = use_stencil ? stencil_rows(&A64) : n;
+  B.pad = use_stencil ? stencil_pitch(&A64) - (A64.box_nx + 1) : 0;
+  const size_t vb = sizeof(float) * (size_t)std::max<int64_t>(B.nv + 4, 4);
   B.r = static_cast<float*>(workspace(ctx, "mixed.r", vb));
-  B.p = static_cast<float*>(workspace(ctx, "mixed.p", vb));
+  const int64_t ghost = use_stencil ? stencil_ghost(&A64) : 0;
+  const size_t pb = sizeof(float) * (size_t)(std::max<int64_t>(B.nv + 4, 4) + 2 * ghost);
+  float* pbase = static_cast<float*>(workspace(ctx, use_stencil ? "mixed.pg" : "mixed.p", pb));
+  B.p = pbase ? pbase + ghost : nullptr;
+  if (use_stencil) {
+    B.stencil = true;
+    MFE_TRY(stencil_grid(ctx, &B.stencil_grid));
+  }
   B.Ap = static_cast<float*>(workspace(ctx, "mixed.Ap", vb));
   B.x32 = static_cast<float*>(workspace(ctx, "mixed.x32", vb));
   B.st = static_cast<MixState*>(workspace(ctx, "mixed.state", sizeof(MixState)));
+  B.err = B.st ? &B.st->err : nullptr;  // the stencil SpMV's bounded waits report here
   const int max_iter = std::max(0, o->max_iter);
   B.history = static_cast<double*>(workspace(ctx, "mixed.history", sizeof(double) * ((size_t)max_iter + 2)));
   B.partials = static_cast<double*>(workspace(ctx, "mixed.partials", sizeof(double) * 2 * kMaxPart));
@@ -328,13 +358,14 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
   MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev0, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(B.st, hs, sizeof(MixState), cudaMemcpyHostToDevice, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaMemsetAsync(B.x32, 0, vb, ctx->stream));
-  MFE_CUDA_TRY(ctx, cudaMemsetAsync(B.p, 0, vb, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(pbase, 0, pb, ctx->stream));
+  if (B.pad) MFE_CUDA_TRY(ctx, cudaMemsetAsync(B.r, 0, vb, ctx->stream));  // padding entries stay 0
   {
     DotSink s;
     s.partials = B.partials;
     s.ticket = B.tickets;
     s.out = &B.st->rr_true;
-    MFE_TRY(launch_box_resid_f32out(ctx, &A64, x, b, B.r, &s, nullptr));
+    MFE_TRY(launch_box_resid_f32out(ctx, &A64, x, b, B.r, &s, nullptr, B.pad));
   }
   k_mx_init<<<1, 1, 0, ctx->stream>>>(B.st);
   MFE_TRY(check_launch(ctx, "k_mx_init"));
@@ -412,6 +443,7 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
   res->times[4] = ms * 1e-3;
   res->refinements = hs->updates;
   res->fp64_spmvs = hs->updates + 1;
+  res->inner_operator = B.stencil ? MFE_INNER_STENCIL : MFE_INNER_VALUES;
   mfe_status status = MFE_OK;
   if (hs->status != 0) status = MFE_BREAKDOWN;
   else if (hs->normr_true > hs->tol_abs) status = MFE_MAXITER;

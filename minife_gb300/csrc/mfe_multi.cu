@@ -1238,25 +1238,26 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   const bool mixed = o->precision == MFE_PREC_MIXED;
   const int64_t ntot = A64.nrows * nrhs;
 
+  // mixed with 32 right-hand sides: the padded-values SpMM, which reads p
+  // with ghost zones of zero rows on both sides (the stencil's reach plus a
+  // partial tile).  The FP32 operator (padded or CSR values) is rebuilt on
+  // every call: a cache keyed on the values pointer would go stale when an
+  // allocator hands the same address to another matrix.
+  const bool use_ell = mixed && nrhs == 32 && getenv("MFE_MULTI_CSR") == nullptr;
   mfe_csr A32 = A64;
-  if (mixed) {
+  if (mixed && !use_ell) {
     float* v32 = static_cast<float*>(
         workspace(ctx, "mixed.vals32", sizeof(float) * (size_t)(A64.nnz + 4)));
     if (!v32) return fail(ctx, MFE_OOM, "FP32 matrix copy allocation failed");
-    if (ctx->f32_src_vals != A64.vals || ctx->f32_src_nnz != A64.nnz) {
-      MFE_TRY(launch_convert_f32(ctx, static_cast<const double*>(A64.vals), v32, A64.nnz));
-      ctx->f32_src_vals = A64.vals;
-      ctx->f32_src_nnz = A64.nnz;
-    }
+    MFE_TRY(launch_convert_f32(ctx, static_cast<const double*>(A64.vals), v32, A64.nnz));
     A32.vals = v32;
+    A32.dtype = MFE_F32;
+  } else if (mixed) {
+    A32.vals = nullptr;
     A32.dtype = MFE_F32;
   }
   const size_t vb = (mixed ? sizeof(float) : sizeof(double)) * (size_t)(ntot + 8);
   void* r = workspace(ctx, "multi.r", vb);
-  // mixed with 32 right-hand sides: the padded-values SpMM, which reads p
-  // with ghost zones of zero rows on both sides (the stencil's reach plus a
-  // partial tile)
-  const bool use_ell = mixed && nrhs == 32 && getenv("MFE_MULTI_CSR") == nullptr;
   const int64_t Nx = A64.box_nx + 1, NxNy = Nx * (A64.box_ny + 1);
   const int64_t ghost = NxNy + Nx + 1 + kER;
   const size_t pb = use_ell ? sizeof(float) * (size_t)((A64.nrows + 2 * ghost) * 32 + 8) : vb;
@@ -1269,16 +1270,12 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
     const size_t eb = sizeof(float) * (size_t)(ntl * kER * 28 + 8);
     ell = static_cast<float*>(workspace(ctx, "multi.ell28", eb));
     if (!ell) return fail(ctx, MFE_OOM, "padded FP32 matrix allocation failed");
-    if (ctx->ell28_src != A64.vals || ctx->ell28_nnz != A64.nnz) {
-      MFE_CUDA_TRY(ctx, cudaMemsetAsync(ell, 0, eb, ctx->stream));
-      k_mr_ell28<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(A64.nrows, (int64_t)256),
-                                                                    (int64_t)ctx->sm_count * 8)),
-                   256, 0, ctx->stream>>>((int)Nx, A64.box_ny + 1, A64.box_nz + 1,
-                                          static_cast<const double*>(A64.vals), ell);
-      MFE_TRY(check_launch(ctx, "k_mr_ell28"));
-      ctx->ell28_src = A64.vals;
-      ctx->ell28_nnz = A64.nnz;
-    }
+    MFE_CUDA_TRY(ctx, cudaMemsetAsync(ell, 0, eb, ctx->stream));
+    k_mr_ell28<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(A64.nrows, (int64_t)256),
+                                                                  (int64_t)ctx->sm_count * 8)),
+                 256, 0, ctx->stream>>>((int)Nx, A64.box_ny + 1, A64.box_nz + 1,
+                                        static_cast<const double*>(A64.vals), ell);
+    MFE_TRY(check_launch(ctx, "k_mr_ell28"));
     MFE_TRY(ell32_grid(ctx, &ell_grid));
   }
   void* Ap = workspace(ctx, "multi.Ap", vb);
@@ -1366,6 +1363,7 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
     res.times[4] = ms * 1e-3;
     res.refinements = hs->updates;
     res.fp64_spmvs = mixed ? hs->updates + 1 : hs->k + 1;
+    res.inner_operator = !mixed ? MFE_INNER_NONE : (ell ? MFE_INNER_PADDED : MFE_INNER_VALUES);
     const bool converged = mixed ? hs->done[j] != 0 && !hs->brk[j]
                                  : !(hs->normr_true[j] > hs->tol_abs[j]);
     res.status = hs->brk[j] ? MFE_BREAKDOWN : (converged ? MFE_OK : MFE_MAXITER);

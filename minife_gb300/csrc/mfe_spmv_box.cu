@@ -47,6 +47,7 @@ struct BoxParams {
   CgState* cg;
   unsigned* err;
   float* y32;          // BOX_RESID: when set, the residual is written as FP32 here
+  int y32_pad;         // y32 rows are (Nx + y32_pad) long: row r goes to r + (r / Nx) * y32_pad
   const int* gate;     // when set and *gate == 0 the launch does nothing
 };
 
@@ -230,7 +231,8 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
         if (lane == 0) mbar_arrive(&empty[s]);  // stage s no longer read by this warp
         if (MODE == BOX_RESID) {
           const double res = P.b[r] - widen(sum);
-          if (P.y32 != nullptr) P.y32[r] = (float)res;
+          if (P.y32 != nullptr)
+            P.y32[P.y32_pad ? (int64_t)r + (int64_t)(r / P.Nx) * P.y32_pad : (int64_t)r] = (float)res;
           else P.y[r] = (T)res;
           dacc = fma(res, res, dacc);
         } else {
@@ -285,7 +287,8 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
         if (lane == 0) mbar_arrive(&empty[s]);  // stage s no longer read by this warp
         if (MODE == BOX_RESID) {
           const double res = P.b[r] - widen(sum);
-          if (P.y32 != nullptr) P.y32[r] = (float)res;
+          if (P.y32 != nullptr)
+            P.y32[P.y32_pad ? (int64_t)r + (int64_t)(r / P.Nx) * P.y32_pad : (int64_t)r] = (float)res;
           else P.y[r] = (T)res;
           dacc = fma(res, res, dacc);
         } else {
@@ -471,10 +474,11 @@ mfe_status detect_box(mfe_ctx* ctx, const mfe_csr* A, int* nx, int* ny, int* nz)
 template <typename T, int MODE>
 static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
                                const DotSink* sink, const double* b, CgState* cg,
-                               float* y32 = nullptr, const int* gate = nullptr)
+                               float* y32 = nullptr, const int* gate = nullptr, int y32_pad = 0)
 {
   BoxParams<T> P;
   P.y32 = y32;
+  P.y32_pad = y32_pad;
   P.gate = gate;
   P.Nx = A->box_nx + 1;
   P.Ny = A->box_ny + 1;
@@ -529,10 +533,10 @@ mfe_status launch_spmv_box(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* 
 
 mfe_status launch_box_resid_f32out(mfe_ctx* ctx, const mfe_csr* A64, const double* x,
                                    const double* b, float* r32, const DotSink* sink,
-                                   const int* gate)
+                                   const int* gate, int r32_pad)
 {
   if (A64->nrows == 0) return MFE_OK;
-  return box_launch_t<double, BOX_RESID>(ctx, A64, x, nullptr, sink, b, nullptr, r32, gate);
+  return box_launch_t<double, BOX_RESID>(ctx, A64, x, nullptr, sink, b, nullptr, r32, gate, r32_pad);
 }
 
 }  // namespace mfe

@@ -1,0 +1,489 @@
+// FP32 inner operator of the mixed-precision solver as a verified stencil.
+//
+// On a miniFE box every node of the six faces is a Dirichlet node
+// (simple_mesh_description.hpp fills bc_rows_0 / bc_rows_1 from all six
+// faces) and impose_dirichlet (Dirichlet_conditions.hpp) turns each such row
+// into the identity scaled by its diagonal and zeroes the Dirichlet columns
+// of the other rows.  Every row of A is then one of two kinds:
+//   * a Dirichlet row: dd * x_r, one diagonal value dd for all of them;
+//   * an interior row: the interior 27-point stencil with the entries of
+//     Dirichlet neighbours zeroed.
+// stencil_prepare checks this on the matrix itself, every call:
+// k_st_table rounds one representative row of each of the 5 x 5 x 5
+// coordinate classes (first node, second node, interior, second-last, last)
+// to FP32, the host checks each class row against the model above (within
+// 2^-22 of the row's largest magnitude), and k_st_verify checks EVERY entry
+// of A against its class row's entry (within 2^-22 relative; exact zeros
+// where the class row has a zero).  Only then does the mixed
+// solver use the stencil; otherwise (per-element conductivity, a matrix that
+// is not a miniFE box, boxes with fewer than five nodes along a dimension)
+// it keeps the FP32 copy of the values.  The inner FP32 iteration then reads
+// only x and y per row (8 bytes instead of 4 per nonzero plus 8), while the
+// reliable updates compute r = b - A x with the exact FP64 values, so the
+// returned solution still meets the FP64-verified tolerance.
+//
+// k_spmv_stencil works on x-padded vectors (x pitch Nxp = Nx rounded up to a
+// multiple of 4, padding entries zero), so every line segment it copies
+// starts on a 16-byte boundary at the same phase and every shared-memory
+// load has a fixed offset.  It marches along z: a CTA owns 256 consecutive
+// positions of the padded xy plane (one per consumer thread) and a run of z
+// steps; a producer lane streams the three line segments (y-1, y, y+1) of
+// each plane the CTA needs into a ring of shared-memory slots (three planes
+// per slot) with bulk copies, from a vector with ghost zones of zero rows
+// around it.  Each consumer keeps the 3 x 9 values of planes z-1, z, z+1 in
+// registers, so a row costs 9 shared-memory loads and 27 FMAs whose
+// coefficients are kernel parameters (constant-bank operands: no
+// registers).  Lanes next to a Dirichlet node zero the masked neighbours as
+// they load them; Dirichlet planes and the planes next to them take
+// warp-uniform branches.  The (plane tile, z) steps are split evenly over
+// one wave of CTAs.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+
+#include "mfe_box.cuh"
+#include "mfe_common.cuh"
+#include "mfe_internal.h"
+
+namespace mfe {
+
+namespace {
+
+constexpr int kSP = 256;                  // plane positions per CTA
+constexpr int kSC = kSP / 32;             // consumer warps
+constexpr int kSS = 4;                    // ring slots
+constexpr int kSKP = 3;                   // planes per slot
+constexpr int kSCap = ((kSP + 2 + 6) + 3) & ~3;  // floats per line segment: 16-byte multiple
+constexpr int kSSlot = kSKP * 3 * kSCap;  // three y lines per plane
+constexpr int kSTable = 125 * 28;         // class rows, 28 floats each
+constexpr size_t kStSmem = sizeof(float) * kSS * kSSlot;  // the ring (dynamic shared memory)
+static_assert((kSCap * sizeof(float)) % 16 == 0 && kSCap >= kSP + 8,
+              "bulk-copy destinations in shared memory must stay 16-byte aligned");
+
+__host__ __device__ __forceinline__ int st_cls(int i, int N)
+{
+  return i == 0 ? 0 : (i == N - 1 ? 4 : (i == 1 ? 1 : (i == N - 2 ? 3 : 2)));
+}
+
+__host__ __device__ __forceinline__ int st_rep(int c, int N)
+{
+  return c == 0 ? 0 : (c == 1 ? 1 : (c == 2 ? 2 : (c == 3 ? N - 2 : N - 1)));
+}
+
+// true if class c has a node along a dimension of N nodes
+__host__ __device__ __forceinline__ bool st_has(int c, int N)
+{
+  const int i = st_rep(c, N);
+  return i >= 0 && i < N && st_cls(i, N) == c;
+}
+
+// one thread per class: the class's representative row rounded to FP32 in
+// slot order (dz, dy, dx), zeros for missing neighbours
+__global__ void k_st_table(int Nx, int Ny, int Nz, const double* __restrict__ vals,
+                           float* __restrict__ table)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c >= 125) return;
+  const int cx = c % 5, cy = (c / 5) % 5, cz = c / 25;
+  float* out = table + c * 28;
+  if (!st_has(cx, Nx) || !st_has(cy, Ny) || !st_has(cz, Nz)) {
+    for (int k = 0; k < 28; ++k) out[k] = 0.0f;  // no row has this class
+    return;
+  }
+  const int ix = st_rep(cx, Nx), iy = st_rep(cy, Ny), iz = st_rep(cz, Nz);
+  int64_t k = row_offset(ix, iy, iz, Nx, Ny, Nz);
+  int slot = 0;
+  for (int dz = -1; dz <= 1; ++dz)
+    for (int dy = -1; dy <= 1; ++dy)
+      for (int dx = -1; dx <= 1; ++dx, ++slot) {
+        const bool in = ix + dx >= 0 && ix + dx < Nx && iy + dy >= 0 && iy + dy < Ny &&
+                        iz + dz >= 0 && iz + dz < Nz;
+        out[slot] = in ? (float)vals[k++] : 0.0f;
+      }
+  out[27] = 0.0f;
+}
+
+// every entry a against its class row's value s (FP32, widened exactly):
+// |a - s| <= tol = 2^-22 max|a_row|, checked on the FP64 bit patterns with
+// integer operations only (GB300's FP64 pipe is far too slow for 27
+// comparisons per row) through two sufficient conditions: both |a| and |s|
+// at most tol / 2 (the cancellation noise of entries that are zero in exact
+// arithmetic), or |s| >= 2 tol, the same sign and the patterns at most
+// 2^(e_tol - e_s + 51) apart (e: unbiased exponents), which bounds
+// |a - s| by 2^e_tol <= tol.  Anything else counts as a mismatch.  A warp
+// takes 32
+// consecutive rows: their values are one contiguous range of at most
+// 32 * 27, loaded coalesced into shared memory, then each lane checks its
+// own row from there.
+constexpr int kVW = 4;  // warps per block (27 KB of static shared memory)
+__global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
+                                                        const double* __restrict__ vals,
+                                                        const float* __restrict__ table, unsigned* bad)
+{
+  __shared__ double sv[kVW][32 * 27];
+  const int n = Nx * Ny * Nz, NxNy = Nx * Ny;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  double* w = sv[warp];
+  unsigned nbad = 0;
+  for (int r0 = (blockIdx.x * kVW + warp) * 32; r0 < n; r0 += gridDim.x * kVW * 32) {
+    const int64_t kw = row_offset_of32(r0, Nx, Ny, Nz, NxNy);
+    const int64_t ke = row_offset_of32(min(n, r0 + 32), Nx, Ny, Nz, NxNy);
+    const int m = (int)(ke - kw);  // <= 32 * 27
+    for (int i = lane; i < m; i += 32) w[i] = __ldg(vals + kw + i);
+    __syncwarp();
+    const int r = r0 + lane;
+    if (r < n) {
+      const int iz = r / NxNy, rem = r - iz * NxNy, iy = rem / Nx, ix = rem - iy * Nx;
+      const float* s = table + (st_cls(ix, Nx) + 5 * st_cls(iy, Ny) + 25 * st_cls(iz, Nz)) * 28;
+      const double* a = w + (row_offset(ix, iy, iz, Nx, Ny, Nz) - kw);
+      constexpr long long kMag = 0x7fffffffffffffffll, kOne = 1ll << 52;  // kOne: one binade
+      const int len = nbr(ix, Nx) * nbr(iy, Ny) * nbr(iz, Nz);
+      long long amax = 0;
+      for (int t = 0; t < len; ++t) amax = max(amax, __double_as_longlong(a[t]) & kMag);
+      const long long tol = amax - 22 * kOne;  // 2^-22 max|a_row| (bit pattern)
+      bool good = tol >= 2 * kOne;             // a normal tol / 2
+      const long long half = tol - kOne, twice = tol + kOne;
+      const int e_tol = (int)(tol >> 52);
+      int q = 0, slot = 0;
+      for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+          for (int dx = -1; dx <= 1; ++dx, ++slot) {
+            const bool in = ix + dx >= 0 && ix + dx < Nx && iy + dy >= 0 && iy + dy < Ny &&
+                            iz + dz >= 0 && iz + dz < Nz;
+            const long long ab = in ? __double_as_longlong(a[q++]) : 0ll;
+            const long long sb = __double_as_longlong(f2d_exact(s[slot]));
+            const long long am = ab & kMag, sm = sb & kMag;
+            const bool small = am <= half && sm <= half;
+            const int sh = e_tol - (int)(sm >> 52) + 51;  // in [28, 50] when sm >= twice
+            const long long d = ab - sb;
+            const bool big = sm >= twice && (ab ^ sb) >= 0 && sh >= 0 &&
+                             d <= (1ll << sh) && d >= -(1ll << sh);
+            good = good && (small || big);
+          }
+      nbad += good ? 0u : 1u;
+    }
+    __syncwarp();
+  }
+  if (nbad) atomicOr(bad, 1u);
+}
+
+struct StParams {
+  int Nx, Ny, Nz, Nxp, NP, ntile;  // NP = Ny * Nxp, the padded plane
+  float coef[27];  // interior stencil, slot order (dz, dy, dx)
+  float dd;        // diagonal of the Dirichlet rows
+  const float* __restrict__ x;  // ghost zones around it
+  float* __restrict__ y;
+  double* partials;
+  unsigned* ticket;
+  double* dot_out;
+  unsigned* err;
+};
+
+// first float of the copy of line (z, dy = j - 1) for plane positions
+// [c0, c1): four before c0 (c0, NP and Nxp are multiples of 4), and the
+// copy holds c1 - c0 + 8 floats
+__device__ __forceinline__ int64_t st_lo(const StParams& P, int z, int j, int c0)
+{
+  return (int64_t)z * P.NP + (int64_t)(j - 1) * P.Nxp + c0 - 4;
+}
+
+// nine values of one plane around a position, q = 3 * (dy + 1) + (dx + 1)
+struct StPlane {
+  float v[9];
+};
+
+// interior-stencil row sum over planes A (dz = -1), B (dz = 0), C (dz = +1);
+// HA / HC false: that plane is a Dirichlet plane and contributes nothing
+template <bool HA, bool HC>
+__device__ __forceinline__ float st_sum(const StParams& P, const StPlane& A, const StPlane& B,
+                                        const StPlane& C)
+{
+  float a[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int k = 0; k < 9; ++k) {
+    if (HA) a[k & 1] = fmaf(P.coef[k], A.v[k], a[k & 1]);
+    a[2 + (k & 1)] = fmaf(P.coef[9 + k], B.v[k], a[2 + (k & 1)]);
+    if (HC) a[4 + (k & 1)] = fmaf(P.coef[18 + k], C.v[k], a[4 + (k & 1)]);
+  }
+  return ((a[0] + a[1]) + (a[2] + a[3])) + (a[4] + a[5]);
+}
+
+__global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_constant__ StParams P)
+{
+  extern __shared__ __align__(128) unsigned char st_smem_raw[];
+  float* const ring = reinterpret_cast<float*>(st_smem_raw);
+  __shared__ uint64_t full[kSS], empty[kSS];
+  __shared__ double red[32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  // this CTA's share of the (plane tile, z) steps, tile-major
+  const int64_t T = (int64_t)P.ntile * P.Nz;
+  const int64_t q0 = T * blockIdx.x / gridDim.x, q1 = T * (blockIdx.x + 1) / gridDim.x;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kSC);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  DFAcc facc;
+  // Slot sequence of a run of rows za .. zb-1 of one plane tile: planes
+  // (za-1, za), then z+1 .. z+min(3, zb-z) for z = za, za+3, ...
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = true;
+      int it = 0;
+      for (int64_t q = q0; ok && q < q1;) {
+        const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
+        const int zb = (int)min((int64_t)P.Nz, za + (q1 - q));
+        const int c0 = tile * kSP, c1 = min(P.NP, c0 + kSP);
+        for (int z = za - 3; z < zb; z += 3, ++it) {
+          const int zf = z < za ? za - 1 : z + 1;
+          const int np = z < za ? 2 : min(3, zb - z);  // planes zf .. zf+np-1
+          const int s = it % kSS;
+          if (it >= kSS) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / kSS) - 1) & 1));
+          if (!ok) break;
+          const unsigned seg = (unsigned)((c1 - c0 + 8) * sizeof(float));
+          mbar_arrive_expect_tx(&full[s], seg * 3u * (unsigned)np);
+          for (int pl = 0; pl < np; ++pl)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              bulk_g2s(ring + s * kSSlot + (pl * 3 + j) * kSCap, P.x + st_lo(P, zf + pl, j, c0), seg,
+                       &full[s]);
+        }
+        q += zb - za;
+      }
+      if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        for (int st = 0; st < kSS && st < it; ++st)
+          mbar_wait_bounded(&full[st], (unsigned)(((it - st + kSS - 1) / kSS - 1) & 1));
+      }
+    }
+  } else {
+    const int lr = (warp - 1) * 32 + lane;
+    bool ok = true;
+    int it = 0;
+    StPlane W0, W1, W2;
+    int c = 0;
+    bool active = false, special = false, mxl = false, mxh = false, myl = false, myh = false, wm = false;
+    float dmul = 0.0f;
+    const float* sx = ring;
+    int lane_off = 0;
+    auto wait_slot = [&]() {
+      const int s = it % kSS;
+      sx = ring + s * kSSlot + lane_off;
+      return mbar_wait_bounded(&full[s], (unsigned)((it / kSS) & 1));
+    };
+    auto release_slot = [&]() {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[it % kSS]);
+      ++it;
+    };
+    // the slot's plane pl around this thread's position into W, masked neighbours zeroed
+    auto load_plane = [&](int pl, StPlane& W) {
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        const float* seg = sx + (pl * 3 + j) * kSCap;
+        W.v[j * 3 + 0] = seg[-1];
+        W.v[j * 3 + 1] = seg[0];
+        W.v[j * 3 + 2] = seg[1];
+      }
+      if (wm) {  // the same for the whole warp
+        if (mxl) W.v[0] = W.v[3] = W.v[6] = 0.0f;
+        if (mxh) W.v[2] = W.v[5] = W.v[8] = 0.0f;
+        if (myl) W.v[0] = W.v[1] = W.v[2] = 0.0f;
+        if (myh) W.v[6] = W.v[7] = W.v[8] = 0.0f;
+      }
+    };
+    // row z's result: Dirichlet rows dd * x, padding and idle lanes 0
+    auto finish = [&](int z, float sum, const StPlane& B) {
+      sum = special ? dmul * B.v[4] : sum;
+      if (active) P.y[(int64_t)z * P.NP + c] = sum;
+      facc.add_product(sum, B.v[4]);
+    };
+    auto row = [&](int z, const StPlane& A, const StPlane& B, const StPlane& C) {
+      float sum;
+      if (z >= 2 && z <= P.Nz - 3) sum = st_sum<true, true>(P, A, B, C);  // z is the same for the warp
+      else if (z == 0 || z == P.Nz - 1) sum = P.dd * B.v[4];
+      else if (z == 1 && z == P.Nz - 2) sum = st_sum<false, false>(P, A, B, C);
+      else if (z == 1) sum = st_sum<false, true>(P, A, B, C);
+      else sum = st_sum<true, false>(P, A, B, C);
+      finish(z, sum, B);
+    };
+    for (int64_t q = q0; ok && q < q1;) {
+      const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
+      const int zb = (int)min((int64_t)P.Nz, za + (q1 - q));
+      const int c0 = tile * kSP;
+      const int c1 = min(P.NP, c0 + kSP);
+      c = c0 + lr;
+      active = c < c1;
+      const int cc = active ? c : c1 - 1;
+      lane_off = cc - c0 + 4;
+      const int iy = cc / P.Nxp, ix = cc - iy * P.Nxp;
+      const bool real = active && ix < P.Nx;
+      const bool dir = ix == 0 || ix == P.Nx - 1 || iy == 0 || iy == P.Ny - 1;
+      special = !real || dir;
+      dmul = real ? P.dd : 0.0f;
+      mxl = ix == 1;
+      mxh = ix == P.Nx - 2;
+      myl = iy == 1;
+      myh = iy == P.Ny - 2;
+      wm = __any_sync(0xffffffffu, mxl || mxh || myl || myh);
+      ok = wait_slot();
+      if (!ok) break;
+      load_plane(0, W0);
+      load_plane(1, W1);
+      release_slot();
+      for (int z = za; z < zb; z += 3) {
+        if (!wait_slot()) {
+          ok = false;
+          break;
+        }
+        if (z >= 2 && z + 2 <= P.Nz - 3 && z + 3 <= zb) {  // three interior rows
+          load_plane(0, W2);
+          finish(z, st_sum<true, true>(P, W0, W1, W2), W1);
+          load_plane(1, W0);
+          finish(z + 1, st_sum<true, true>(P, W1, W2, W0), W2);
+          load_plane(2, W1);
+          finish(z + 2, st_sum<true, true>(P, W2, W0, W1), W0);
+        } else {
+          load_plane(0, W2);
+          row(z, W0, W1, W2);
+          if (z + 1 < zb) {
+            load_plane(1, W0);
+            row(z + 1, W1, W2, W0);
+          }
+          if (z + 2 < zb) {
+            load_plane(2, W1);
+            row(z + 2, W2, W0, W1);
+          }
+        }
+        release_slot();
+      }
+      q += zb - za;
+    }
+    if (!ok) atomicOr(P.err, ERR_WAIT_TIMEOUT);
+  }
+  const double bt = block_sum(warp == 0 ? 0.0 : facc.value(), red);
+  double total;
+  if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0) *P.dot_out = total;
+}
+
+// The model check of the class rows (host): Dirichlet classes hold dd on the
+// diagonal only, the others the interior row with Dirichlet neighbours zeroed.
+bool st_model(int Nx, int Ny, int Nz, const float* tab, float* coef, float* dd)
+{
+  if (!st_has(2, Nx) || !st_has(2, Ny) || !st_has(2, Nz)) return false;
+  const float* sI = tab + (2 + 5 * 2 + 25 * 2) * 28;
+  *dd = tab[13];  // class (0, 0, 0): node (0, 0, 0), a Dirichlet node
+  for (int k = 0; k < 27; ++k) coef[k] = sI[k];
+  for (int c = 0; c < 125; ++c) {
+    const int cx = c % 5, cy = (c / 5) % 5, cz = c / 25;
+    if (!st_has(cx, Nx) || !st_has(cy, Ny) || !st_has(cz, Nz)) continue;
+    const int ix = st_rep(cx, Nx), iy = st_rep(cy, Ny), iz = st_rep(cz, Nz);
+    const bool dir = ix == 0 || ix == Nx - 1 || iy == 0 || iy == Ny - 1 || iz == 0 || iz == Nz - 1;
+    const float* s = tab + c * 28;
+    float amax = 0.0f;
+    for (int k = 0; k < 27; ++k) amax = std::max(amax, std::fabs(s[k]));
+    const double tol = std::ldexp((double)amax, -22);
+    int slot = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx, ++slot) {
+          double want;
+          if (dir) {
+            want = slot == 13 ? (double)*dd : 0.0;
+          } else {
+            const int jx = ix + dx, jy = iy + dy, jz = iz + dz;
+            const bool nd = jx == 0 || jx == Nx - 1 || jy == 0 || jy == Ny - 1 || jz == 0 || jz == Nz - 1;
+            want = nd ? 0.0 : (double)sI[slot];
+          }
+          if (std::fabs((double)s[slot] - want) > tol) return false;
+        }
+  }
+  return true;
+}
+
+}  // namespace
+
+int stencil_pitch(const mfe_csr* A) { return ((A->box_nx + 1) + 3) & ~3; }
+
+int64_t stencil_rows(const mfe_csr* A)
+{
+  return (int64_t)stencil_pitch(A) * (A->box_ny + 1) * (A->box_nz + 1);
+}
+
+int64_t stencil_ghost(const mfe_csr* A)
+{
+  const int64_t Nxp = stencil_pitch(A), NP = Nxp * (A->box_ny + 1);
+  return NP + Nxp + 8;
+}
+
+mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok)
+{
+  *ok = false;
+  if (A64->box_nx <= 0 || A64->box_ny <= 0 || A64->box_nz <= 0) return MFE_OK;
+  const int Nx = A64->box_nx + 1, Ny = A64->box_ny + 1, Nz = A64->box_nz + 1;
+  if (Nx < 5 || Ny < 5 || Nz < 5) return MFE_OK;  // no interior class
+  float* table = static_cast<float*>(workspace(ctx, "stencil.table", sizeof(float) * kSTable + 16));
+  if (!table) return fail(ctx, MFE_OOM, "stencil workspace allocation failed");
+  unsigned* bad = reinterpret_cast<unsigned*>(table + kSTable);
+  const double* vals = static_cast<const double*>(A64->vals);
+  k_st_table<<<1, 128, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table);
+  MFE_TRY(check_launch(ctx, "k_st_table"));
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(bad, 0, sizeof(unsigned), ctx->stream));
+  const int blocks = (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(A64->nrows, (int64_t)kVW * 32),
+                           (int64_t)resident_blocks(ctx, (const void*)k_st_verify, kVW * 32, 0)));
+  k_st_verify<<<blocks, kVW * 32, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table, bad);
+  MFE_TRY(check_launch(ctx, "k_st_verify"));
+  float* host = static_cast<float*>(host_scratch(ctx, sizeof(float) * kSTable + 16));
+  if (!host) return fail(ctx, MFE_OOM, "pinned host scratch allocation failed");
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(host, table, sizeof(float) * kSTable + sizeof(unsigned),
+                                    cudaMemcpyDeviceToHost, ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  unsigned hb;
+  memcpy(&hb, host + kSTable, sizeof(unsigned));
+  *ok = hb == 0 && st_model(Nx, Ny, Nz, host, coef, coef + 27);
+  return MFE_OK;
+}
+
+mfe_status stencil_grid(mfe_ctx* ctx, int* grid)
+{
+  static int per_sm[64] = {};
+  const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
+  if (per_sm[dev] == 0) {
+    MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmv_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)kStSmem));
+    int b = 1;
+    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_stencil, kSP + 32, kStSmem));
+    per_sm[dev] = std::max(b, 1);
+  }
+  *grid = ctx->sm_count * per_sm[dev];
+  return MFE_OK;
+}
+
+mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef, const float* x,
+                               float* y, const DotSink* sink, int grid, unsigned* err)
+{
+  StParams P;
+  P.Nx = A->box_nx + 1;
+  P.Ny = A->box_ny + 1;
+  P.Nz = A->box_nz + 1;
+  P.Nxp = stencil_pitch(A);
+  P.NP = P.Nxp * P.Ny;
+  P.ntile = (int)ceil_div(P.NP, (int64_t)kSP);
+  for (int k = 0; k < 27; ++k) P.coef[k] = coef[k];
+  P.dd = coef[27];
+  P.x = x;
+  P.y = y;
+  P.partials = sink->partials;
+  P.ticket = sink->ticket;
+  P.dot_out = sink->out;
+  P.err = err;
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)grid, (int64_t)P.ntile * P.Nz));
+  k_spmv_stencil<<<g, kSP + 32, kStSmem, ctx->stream>>>(P);
+  return check_launch(ctx, "k_spmv_stencil");
+}
+
+}  // namespace mfe

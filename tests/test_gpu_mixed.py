@@ -73,3 +73,60 @@ def test_mixed_with_prepared_f32_copy_and_history():
     assert res.status == 0 and res.final_resid <= 1e-9 * res.normr0
     assert len(res.history) == res.num_iters + 1
     assert res.refinements >= 1
+
+
+@pytest.mark.parametrize("dims", [(30, 30, 30), (17, 9, 11), (4, 4, 4), (3, 4, 2), (40, 5, 6)])
+def test_mixed_stencil_operator_and_values_copy(dims):
+    """The verified FP32 stencil operator (default on a k = 1 box with an
+    interior node, i.e. at least 4 elements along each dimension) and the
+    FP32 copy of the values both reach the FP64-verified tolerance with about
+    the same number of inner iterations."""
+    A, b = M.build_system(*dims)
+    ro, cols, vals, bo = O.build_system(*dims)
+    its = {}
+    for op in ("auto", "values"):
+        x = torch.zeros_like(b)
+        res = M.cg_solve(A, b, x, max_iter=3000, tol=1e-8, tol_mode="relative", precision="mixed",
+                         mixed_operator=op)
+        assert res.status == 0, (op, res)
+        want = "stencil" if op == "auto" and min(dims) >= 4 else "values"
+        assert res.inner_operator == want, (op, res.inner_operator)
+        rel = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x))) / np.linalg.norm(bo)
+        assert rel <= 1e-8, (op, rel)
+        its[op] = res.num_iters
+    assert abs(its["auto"] - its["values"]) <= max(3, 0.1 * its["values"]), its
+
+
+def test_mixed_stencil_first_iterations_match_values():
+    """Two inner iterations from x = 0 with each FP32 operator: the residual
+    norms agree to FP32 accuracy, so the stencil applies the same operator as
+    the matrix (Dirichlet rows, masked neighbours of rows beside them, z
+    boundaries) and not merely one that converges."""
+    dims = (13, 6, 9)
+    A, b = M.build_system(*dims)
+    out = {}
+    for op in ("auto", "values"):
+        x = torch.zeros_like(b)
+        res = M.cg_solve(A, b, x, max_iter=2, tol=0.0, tol_mode="relative", precision="mixed",
+                         refine_k=1, mixed_operator=op, record_history=True)
+        out[op] = (res, host(x))
+    ra, xa = out["auto"]
+    rv, xv = out["values"]
+    assert ra.inner_operator == "stencil" and rv.inner_operator == "values"
+    assert np.abs(xa - xv).max() <= 1e-5 * np.abs(xv).max()
+    assert abs(ra.final_resid - rv.final_resid) <= 1e-5 * rv.normr0
+
+
+def test_mixed_falls_back_for_per_element_conductivity():
+    """With random per-element conductivity no class stencil fits the rows, so
+    the solver uses the FP32 copy of the values and still converges."""
+    dims = (10, 9, 8)
+    rng = np.random.default_rng(5)
+    kappa = np.exp(rng.normal(0.0, 0.5, size=dims[0] * dims[1] * dims[2]))
+    A, b = M.build_system(*dims, kappa=torch.from_numpy(kappa).cuda())
+    ro, cols, vals, bo = O.build_system(*dims, kappa=kappa)
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=3000, tol=1e-8, tol_mode="relative", precision="mixed")
+    assert res.status == 0 and res.inner_operator == "values"
+    rel = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x))) / np.linalg.norm(bo)
+    assert rel <= 1e-8
