@@ -330,41 +330,54 @@ def run_gpu(args):
                "d2h_bytes_per_step": 8 * n, "iterations": r2.num_iters}
         del ro_h, cols_h, vals_h
 
-    # mixed precision (FP32 matrix/vectors, FP64 dots and reliable updates) to
-    # the same FP64-verified tolerance, same system, same timing rules
+    # mixed precision (FP32 inner operator and vectors, FP64 dots and reliable
+    # updates) to the same FP64-verified tolerance, same system, same timing
+    # rules.  The default inner operator is the verified FP32 stencil (its
+    # per-call verification of every row is inside the timed region); the
+    # FP32 copy of the values (prepared once, outside) is timed beside it.
     mixed = None
     if not args.no_mixed:
         x64 = x.clone()
         xm = torch.zeros_like(b)
+
+        def time_mixed(A32):
+            for _ in range(args.warmup):
+                xm.zero_()
+                M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
+                           precision="mixed", refine_k=args.refine_k, A32=A32)
+            torch.cuda.synchronize()
+            barrier(world)
+            m0 = torch.cuda.Event(enable_timing=True)
+            m1 = torch.cuda.Event(enable_timing=True)
+            m0.record(stream)
+            for _ in range(args.steps):
+                xm.zero_()
+                rm = M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
+                                precision="mixed", refine_k=args.refine_k, A32=A32)
+            m1.record(stream)
+            torch.cuda.synchronize()
+            barrier(world)
+            return max_over_ranks(world, m0.elapsed_time(m1) * 1e-3 / args.steps), rm
+
         A32 = M.to_f32(A)
-        for _ in range(args.warmup):
-            xm.zero_()
-            rm = M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
-                            precision="mixed", refine_k=args.refine_k, A32=A32)
-        torch.cuda.synchronize()
-        barrier(world)
-        m0 = torch.cuda.Event(enable_timing=True)
-        m1 = torch.cuda.Event(enable_timing=True)
-        m0.record(stream)
-        for _ in range(args.steps):
-            xm.zero_()
-            rm = M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
-                            precision="mixed", refine_k=args.refine_k, A32=A32)
-        m1.record(stream)
-        torch.cuda.synchronize()
-        barrier(world)
-        t_mixed = max_over_ranks(world, m0.elapsed_time(m1) * 1e-3 / args.steps)
+        t_values, rv = time_mixed(A32)
+        del A32
+        t_mixed, rm = time_mixed(None)
         rcm, errm = M.verify_solution(*DIMS, xm)
         diff = xm - x64
         mixed = {"value": t_mixed, "unit": "s", "speedup_vs_fp64": t_step / t_mixed,
+                 "inner_operator": rm.inner_operator,
                  "inner_iterations": rm.num_iters, "reliable_updates": rm.refinements,
                  "refine_k": args.refine_k, "status": rm.status,
                  "final_rel_resid_fp64": rm.final_resid / rm.normr0,
                  "err_vs_fp64_solution": {"rel_l2": float(diff.norm() / x64.norm()),
                                           "max_abs": float(diff.abs().max())},
                  "analytic_check": {"max_err": errm, "passed": rcm == 0},
-                 "dtype": "f32 matrix/vectors, f64 dots/scalars/solution"}
-        del A32, xm, x64
+                 "values_copy": {"value": t_values, "unit": "s",
+                                 "speedup_vs_fp64": t_step / t_values,
+                                 "inner_iterations": rv.num_iters, "status": rv.status},
+                 "dtype": "f32 inner operator/vectors, f64 dots/scalars/solution"}
+        del xm, x64
 
     # launches of the timed headline region: per CG iteration the SpMV, the
     # update and the p update, plus the initial residual and setup per solve

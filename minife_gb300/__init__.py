@@ -530,15 +530,18 @@ class Batch:
                        "mfe_batch_set_tuning")
 
     def solve(self, max_iter: int = 200, tol: float = DBL_EPSILON, tol_mode: str = "absolute",
-              precision: str = "mixed", refine_k: int = 0, x=None):
+              precision: str = "mixed", refine_k: int = 0, x=None, mixed_operator: str = "auto"):
         """Returns (x, results): results holds one CGResult per box (times[0] =
-        assembly of the batch, times[4] = the batched solve, in seconds)."""
+        assembly of the batch, times[4] = the batched solve, in seconds).
+        Mixed precision: mixed_operator "auto" uses the verified FP32 stencil
+        when every box passes its check (else the padded FP32 values),
+        "values" always the padded FP32 values."""
         torch = _torch()
         ctx = self.ctx
         ctx.bind_torch_stream()
         if x is None:
             x = torch.empty(max(self.offsets[-1], 1), dtype=torch.float64, device="cuda")
-        o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k)
+        o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k, mixed_operator=mixed_operator)
         res = (MfeCgResult * len(self.dims))()
         st = ctx.lib.mfe_batch_solve(ctx.h, self.h, ctypes.byref(o), _ptr(x), res)
         if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
@@ -548,7 +551,8 @@ class Batch:
 
 def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
                       tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
-                      tuning: dict | None = None, ctx: Context | None = None):
+                      tuning: dict | None = None, ctx: Context | None = None,
+                      mixed_operator: str = "auto"):
     """Assemble and solve len(dims) independent miniFE boxes together
     (mfe_batch_solve_boxes).  Returns (x, offsets, results); box i's rows are
     x[offsets[i]:offsets[i+1]]."""
@@ -556,7 +560,8 @@ def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
     try:
         if tuning:
             b.set_tuning(**tuning)
-        x, res = b.solve(max_iter, tol, tol_mode, precision, refine_k)
+        x, res = b.solve(max_iter, tol, tol_mode, precision, refine_k,
+                         mixed_operator=mixed_operator)
         return x, b.offsets, res
     finally:
         b.close()

@@ -47,6 +47,7 @@
 #include "mfe_box.cuh"
 #include "mfe_common.cuh"
 #include "mfe_internal.h"
+#include "mfe_stencil.cuh"
 
 namespace mfe {
 
@@ -435,6 +436,212 @@ __global__ void k_bx_ell(BoxDesc d, const double* __restrict__ vals64, float* __
                           iz + dz >= 0 && iz + dz < d.Nz;
           out[slot] = in ? (float)vals64[k++] : 0.0f;
         }
+  }
+}
+
+// Batched FP32 stencil SpMV of the mixed solver, used when every box is a
+// verified miniFE box operator (stencil_prepare_box): the z-marching kernel
+// of mfe_stencil.cu over the (box, plane tile, z) steps of the listed boxes
+// (tpre holds their prefix sums, box-major, then tile-major), in each box's
+// natural layout inside its ghost zones (the per-plane copy phase follows the
+// row's address mod 4), with the box's 27 interior coefficients in registers
+// and its p.Ap finished by bx_flush.
+struct BxStParams {
+  const BoxDesc* boxes;
+  BoxSt* st;
+  const int* ids;
+  const int* tpre;
+  const int* count;
+  const float* coef;  // [nbox][28]: interior stencil (slot order), Dirichlet diagonal
+  const float* __restrict__ x;
+  float* __restrict__ y;
+  double* slots;      // [nbox][grid][kSC]
+  unsigned* err;
+};
+
+// first float of the 16-byte aligned copy of line (z, dy = j - 1) of a box for
+// plane positions [c0, c1), and one past its last
+__device__ __forceinline__ int64_t bxs_lo(const BoxDesc& d, int z, int j, int c0)
+{
+  return ((int64_t)z * d.NxNy + (int64_t)(j - 1) * d.Nx + c0 - 1) & ~(int64_t)3;
+}
+__device__ __forceinline__ int64_t bxs_hi(const BoxDesc& d, int z, int j, int c1)
+{
+  return ((int64_t)z * d.NxNy + (int64_t)(j - 1) * d.Nx + c1 + 1 + 3) & ~(int64_t)3;
+}
+
+__global__ void __launch_bounds__(kSP + 32, 2) k_bx_stencil(const __grid_constant__ BxStParams P)
+{
+  extern __shared__ __align__(128) unsigned char bxs_smem[];
+  float* const ring = reinterpret_cast<float*>(bxs_smem);
+  __shared__ uint64_t full[kSS], empty[kSS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cnt = *P.count;
+  if (cnt == 0) return;
+  const int total = __ldg(&P.tpre[cnt]);
+  const int t_begin = bx_start(blockIdx.x, total, gridDim.x);
+  const int t_end = bx_start(blockIdx.x + 1, total, gridDim.x);
+  if (t_begin >= t_end) return;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kSC);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  // Slot sequence of a run of rows za .. zb-1 of one plane tile: planes
+  // (za-1, za), then z+1 .. z+min(3, zb-z) for z = za, za+3, ...
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = true;
+      int it = 0, q = -1, A = 0, E = 0;
+      BoxDesc d{};
+      for (int i = t_begin; ok && i < t_end;) {
+        const int nq = bx_advance(P.tpre, cnt, q, i);
+        if (nq != q) {
+          q = nq;
+          d = P.boxes[__ldg(&P.ids[q])];
+          A = __ldg(&P.tpre[q]);
+          E = __ldg(&P.tpre[q + 1]);
+        }
+        const int tile = (i - A) / d.Nz, za = (i - A) - tile * d.Nz;
+        const int zb = min(d.Nz, za + (min(t_end, E) - i));
+        const int c0 = tile * kSP, c1 = min(d.NxNy, c0 + kSP);
+        const float* xb = P.x + d.row_base;
+        for (int z = za - 3; z < zb; z += 3, ++it) {
+          const int zf = z < za ? za - 1 : z + 1;
+          const int np = z < za ? 2 : min(3, zb - z);  // planes zf .. zf+np-1
+          const int s = it % kSS;
+          if (it >= kSS) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / kSS) - 1) & 1));
+          if (!ok) break;
+          unsigned bytes = 0;
+          for (int pl = 0; pl < np; ++pl)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              bytes += (unsigned)((bxs_hi(d, zf + pl, j, c1) - bxs_lo(d, zf + pl, j, c0)) * sizeof(float));
+          mbar_arrive_expect_tx(&full[s], bytes);
+          for (int pl = 0; pl < np; ++pl)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const int64_t lo = bxs_lo(d, zf + pl, j, c0);
+              bulk_g2s(ring + s * kSSlot + (pl * 3 + j) * kSCap, xb + lo,
+                       (unsigned)((bxs_hi(d, zf + pl, j, c1) - lo) * sizeof(float)), &full[s]);
+            }
+        }
+        i += zb - za;
+      }
+      if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        for (int st = 0; st < kSS && st < it; ++st)
+          mbar_wait_bounded(&full[st], (unsigned)(((it - st + kSS - 1) / kSS - 1) & 1));
+      }
+    }
+  } else {
+    const int cw = warp - 1;
+    const int lr = cw * 32 + lane;
+    bool ok = true;
+    int it = 0, q = -1, b = -1, A = 0, E = 0;
+    BoxDesc d{};
+    DFAcc facc;
+    float sv[27], dd = 0.0f;
+    StPlane W0, W1, W2;
+    int c = 0, cc = 0, c0 = 0;
+    bool active = false, dir = false, mxl = false, mxh = false, myl = false, myh = false, wm = false;
+    const float* sx = ring;
+    auto wait_slot = [&]() {
+      const int s = it % kSS;
+      sx = ring + s * kSSlot + (cc - c0 + 1);
+      return mbar_wait_bounded(&full[s], (unsigned)((it / kSS) & 1));
+    };
+    auto release_slot = [&]() {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[it % kSS]);
+      ++it;
+    };
+    // plane z (the slot's plane pl) around position cc into W, masked neighbours zeroed
+    auto load_plane = [&](int pl, int z, StPlane& W) {
+      const unsigned zb0 = (unsigned)z * (unsigned)d.NxNy + (unsigned)(c0 - 1);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        // the copy starts (base + c0 - 1) mod 4 floats before position c0 - 1
+        const float* seg = sx + (pl * 3 + j) * kSCap + ((zb0 + (unsigned)((j - 1) * d.Nx)) & 3u);
+        W.v[j * 3 + 0] = seg[-1];
+        W.v[j * 3 + 1] = seg[0];
+        W.v[j * 3 + 2] = seg[1];
+      }
+      if (wm) {  // the same for the whole warp
+        if (mxl) W.v[0] = W.v[3] = W.v[6] = 0.0f;
+        if (mxh) W.v[2] = W.v[5] = W.v[8] = 0.0f;
+        if (myl) W.v[0] = W.v[1] = W.v[2] = 0.0f;
+        if (myh) W.v[6] = W.v[7] = W.v[8] = 0.0f;
+      }
+    };
+    const auto cf = [&](int k) { return sv[k]; };
+    auto finish = [&](int z, float sum, const StPlane& B) {
+      sum = dir ? dd * B.v[4] : sum;
+      if (active) {
+        P.y[d.row_base + (int64_t)z * d.NxNy + c] = sum;
+        facc.add_product(sum, B.v[4]);
+      }
+    };
+    auto row = [&](int z, const StPlane& A_, const StPlane& B, const StPlane& C) {
+      finish(z, st_row_sum(cf, dd, z, d.Nz, A_, B, C), B);  // z is the same for the warp
+    };
+    for (int i = t_begin; ok && i < t_end;) {
+      const int nq = bx_advance(P.tpre, cnt, q, i);
+      if (nq != q) {
+        if (q >= 0) bx_flush<BX_DOT, kSC>(P.st, P.slots, b, A, E, total, cw, facc.value());
+        facc = DFAcc{};
+        q = nq;
+        b = __ldg(&P.ids[q]);
+        d = P.boxes[b];
+        A = __ldg(&P.tpre[q]);
+        E = __ldg(&P.tpre[q + 1]);
+#pragma unroll
+        for (int k = 0; k < 27; ++k) sv[k] = __ldg(P.coef + (size_t)b * 28 + k);
+        dd = __ldg(P.coef + (size_t)b * 28 + 27);
+      }
+      const int tile = (i - A) / d.Nz, za = (i - A) - tile * d.Nz;
+      const int zb = min(d.Nz, za + (min(t_end, E) - i));
+      c0 = tile * kSP;
+      const int c1 = min(d.NxNy, c0 + kSP);
+      c = c0 + lr;
+      active = c < c1;
+      cc = active ? c : c1 - 1;
+      const int iy = cc / d.Nx, ix = cc - iy * d.Nx;
+      dir = ix == 0 || ix == d.Nx - 1 || iy == 0 || iy == d.Ny - 1;
+      mxl = ix == 1;
+      mxh = ix == d.Nx - 2;
+      myl = iy == 1;
+      myh = iy == d.Ny - 2;
+      wm = __any_sync(0xffffffffu, mxl || mxh || myl || myh);
+      ok = wait_slot();
+      if (!ok) break;
+      load_plane(0, za - 1, W0);
+      load_plane(1, za, W1);
+      release_slot();
+      for (int z = za; z < zb; z += 3) {
+        if (!wait_slot()) {
+          ok = false;
+          break;
+        }
+        load_plane(0, z + 1, W2);
+        row(z, W0, W1, W2);
+        if (z + 1 < zb) {
+          load_plane(1, z + 2, W0);
+          row(z + 1, W1, W2, W0);
+        }
+        if (z + 2 < zb) {
+          load_plane(2, z + 3, W1);
+          row(z + 2, W2, W0, W1);
+        }
+        release_slot();
+      }
+      i += zb - za;
+    }
+    if (!ok) atomicOr(P.err, ERR_WAIT_TIMEOUT);
+    if (q >= 0) bx_flush<BX_DOT, kSC>(P.st, P.slots, b, A, E, total, cw, facc.value());
   }
 }
 
@@ -832,6 +1039,8 @@ struct mfe_batch {
   double assembly_s = 0.0;
   mfe_batch_tuning tune{256, 2, 8192};
   bool ell_ready = false;
+  int stencil_state = 0;   // 0: not checked, 1: every box verified, 2: not every box
+  float* coef = nullptr;   // [nbox][28] when stencil_state == 1
   // device memory
   mfe::BoxDesc* boxes = nullptr;
   mfe::BoxSt* st = nullptr;
@@ -913,7 +1122,43 @@ struct Run {
   BxList open, gate, all;
   Grids grid;
   bool mixed;
+  bool stencil;  // FP32 products by k_bx_stencil (tpre32 then counts its steps)
 };
+
+void* bx_alloc(mfe_batch* bt, size_t bytes);
+
+// resident CTAs of the batched stencil SpMV (attribute set before any capture)
+mfe_status bx_stencil_grid(mfe_ctx* ctx, int* grid)
+{
+  cudaError_t e = cudaFuncSetAttribute(k_bx_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)kStSmem);
+  int per = 1;
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bx_stencil, kSP + 32, kStSmem);
+  if (e != cudaSuccess) return cuda_fail(ctx, e, "batched stencil SpMV configuration");
+  *grid = ctx->sm_count * std::max(per, 1);
+  return MFE_OK;
+}
+
+// every box checked once per batch (its values never change after assembly)
+mfe_status bx_stencil_prepare(mfe_ctx* ctx, mfe_batch* bt)
+{
+  if (bt->stencil_state != 0) return MFE_OK;
+  std::vector<float> hc((size_t)bt->nbox * 28);
+  bool all = true;
+  for (int i = 0; i < bt->nbox && all; ++i) {
+    const BoxDesc& d = bt->hd[i];
+    bool ok = false;
+    MFE_TRY(stencil_prepare_box(ctx, d.Nx, d.Ny, d.Nz, bt->vals64 + d.nnz_base, &hc[(size_t)i * 28], &ok));
+    all = ok;
+  }
+  if (all) {
+    bt->coef = static_cast<float*>(bx_alloc(bt, sizeof(float) * hc.size()));
+    if (!bt->coef) return fail(ctx, MFE_OOM, "batch stencil allocation failed");
+    MFE_CUDA_TRY(ctx, cudaMemcpy(bt->coef, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice));
+  }
+  bt->stencil_state = all ? 1 : 2;
+  return MFE_OK;
+}
 
 BxVecParams bx_vec(const Run& R, const BxList& L)
 {
@@ -943,6 +1188,21 @@ BxSpmvParams<T> bx_params(const Run& R, const BxList& L, const T* vals, const T*
 
 mfe_status bx_spmv32(mfe_ctx* ctx, const Run& R, const BxList& L, const float* x, float* y)
 {
+  if (R.stencil) {
+    BxStParams S;
+    S.boxes = R.bt->boxes;
+    S.st = R.bt->st;
+    S.ids = L.ids;
+    S.tpre = L.tpre32;
+    S.count = L.count;
+    S.coef = R.bt->coef;
+    S.x = x;
+    S.y = y;
+    S.slots = R.bt->slots;
+    S.err = &R.bt->ctl->err;
+    k_bx_stencil<<<R.grid.g32, kSP + 32, kStSmem, ctx->stream>>>(S);
+    return check_launch(ctx, "k_bx_stencil");
+  }
   const BxSpmvParams<float> P = bx_params<float, BX_DOT>(R, L, R.bt->ell32, x, y, nullptr, nullptr);
   bx_dispatch32(R.bt->tune.spmv_rows, R.bt->tune.spmv_stages, [&]<int RW, int S>() {
     k_bx_spmv<float, BX_DOT, true, RW, S>
@@ -1198,16 +1458,20 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
   Run R;
   R.bt = bt;
   R.mixed = o->precision == MFE_PREC_MIXED;
+  if (R.mixed && o->mixed_operator == 0) MFE_TRY(bx_stencil_prepare(ctx, bt));
+  R.stencil = R.mixed && o->mixed_operator == 0 && bt->stencil_state == 1;
   R.open = bx_list(bt->lists, nbox, 0);
   R.gate = bx_list(bt->lists, nbox, 1);
   R.all = bx_list(bt->lists, nbox, 2);
   MFE_TRY(bx_grids(ctx, bt->tune, &R.grid));
+  if (R.stencil) MFE_TRY(bx_stencil_grid(ctx, &R.grid.g32));
   const size_t rows8 = (size_t)(bt->rows_tot + 8);
 
-  // tiles and chunks of each box at this launch shape
+  // tiles (stencil steps) and chunks of each box at this launch shape
   int chunks_tot = 0;
   for (auto& d : bt->hd) {
-    d.ntiles32 = (int)ceil_div(d.n, bt->tune.spmv_rows);
+    d.ntiles32 = R.stencil ? (int)(ceil_div(d.NxNy, (int64_t)kSP) * d.Nz)
+                           : (int)ceil_div(d.n, bt->tune.spmv_rows);
     d.ntiles64 = (int)ceil_div(d.n, kBx64Rows);
     d.nchunks = (int)ceil_div(d.n, bt->tune.chunk_rows);
     d.chunk_base = chunks_tot;
@@ -1224,8 +1488,11 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
   }
   if (R.mixed && !bt->x32) {
     bt->x32 = static_cast<float*>(bx_alloc(bt, sizeof(float) * rows8));
+    if (!bt->x32) return fail(ctx, MFE_OOM, "batch FP32 allocation failed");
+  }
+  if (R.mixed && !R.stencil && !bt->ell32) {
     bt->ell32 = static_cast<float*>(bx_alloc(bt, sizeof(float) * (size_t)(bt->ell_tot + 8)));
-    if (!bt->x32 || !bt->ell32) return fail(ctx, MFE_OOM, "batch FP32 allocation failed");
+    if (!bt->ell32) return fail(ctx, MFE_OOM, "batch FP32 allocation failed");
   }
   const size_t slots_b = sizeof(double) * (size_t)nbox * std::max(R.grid.g32, R.grid.g64) * 8;
   if (bt->slots_bytes < slots_b) {
@@ -1239,7 +1506,7 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
     if (!bt->chunk_part) return fail(ctx, MFE_OOM, "batch chunk allocation failed");
     bt->chunk_part_bytes = cp_b;
   }
-  if (R.mixed && !bt->ell_ready) {
+  if (R.mixed && !R.stencil && !bt->ell_ready) {
     for (int i = 0; i < nbox; ++i) {
       k_bx_ell<<<(unsigned)std::max<int64_t>(1, std::min<int64_t>(ceil_div(bt->hd[i].n, 256),
                                                                   (int64_t)ctx->sm_count * 8)),
@@ -1335,7 +1602,7 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
     r.times[0] = bt->assembly_s;  // assembly of the whole batch
     r.times[4] = ms * 1e-3;       // the batched solve
     r.refinements = hc.updates;
-    r.inner_operator = R.mixed ? MFE_INNER_PADDED : MFE_INNER_NONE;
+    r.inner_operator = !R.mixed ? MFE_INNER_NONE : (R.stencil ? MFE_INNER_STENCIL : MFE_INNER_PADDED);
     r.status = s.brk ? MFE_BREAKDOWN : (s.normr <= s.tol_abs ? MFE_OK : MFE_MAXITER);
     if (r.status != MFE_OK && worst == MFE_OK) worst = (mfe_status)r.status;
   }

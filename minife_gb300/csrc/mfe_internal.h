@@ -110,6 +110,9 @@ int64_t stencil_ghost(const mfe_csr* A);
 // accuracy, row by row; on success coef[0..26] is the interior stencil in
 // slot order (dz, dy, dx) and coef[27] = dd
 mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok);
+// the same for one box of Nx x Ny x Nz nodes whose CSR values start at vals
+mfe_status stencil_prepare_box(mfe_ctx* ctx, int Nx, int Ny, int Nz, const double* vals, float* coef,
+                               bool* ok);
 mfe_status stencil_grid(mfe_ctx* ctx, int* grid);
 // y = S x and x.y into sink->out, both x-padded (y's padding entries are
 // written as zeros); x has stencil_ghost rows of zeros on both sides

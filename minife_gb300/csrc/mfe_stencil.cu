@@ -44,26 +44,13 @@
 #include "mfe_box.cuh"
 #include "mfe_common.cuh"
 #include "mfe_internal.h"
+#include "mfe_stencil.cuh"
 
 namespace mfe {
 
 namespace {
 
-constexpr int kSP = 256;                  // plane positions per CTA
-constexpr int kSC = kSP / 32;             // consumer warps
-constexpr int kSS = 4;                    // ring slots
-constexpr int kSKP = 3;                   // planes per slot
-constexpr int kSCap = ((kSP + 2 + 6) + 3) & ~3;  // floats per line segment: 16-byte multiple
-constexpr int kSSlot = kSKP * 3 * kSCap;  // three y lines per plane
 constexpr int kSTable = 125 * 28;         // class rows, 28 floats each
-constexpr size_t kStSmem = sizeof(float) * kSS * kSSlot;  // the ring (dynamic shared memory)
-static_assert((kSCap * sizeof(float)) % 16 == 0 && kSCap >= kSP + 8,
-              "bulk-copy destinations in shared memory must stay 16-byte aligned");
-
-__host__ __device__ __forceinline__ int st_cls(int i, int N)
-{
-  return i == 0 ? 0 : (i == N - 1 ? 4 : (i == 1 ? 1 : (i == N - 2 ? 3 : 2)));
-}
 
 __host__ __device__ __forceinline__ int st_rep(int c, int N)
 {
@@ -187,27 +174,6 @@ __device__ __forceinline__ int64_t st_lo(const StParams& P, int z, int j, int c0
   return (int64_t)z * P.NP + (int64_t)(j - 1) * P.Nxp + c0 - 4;
 }
 
-// nine values of one plane around a position, q = 3 * (dy + 1) + (dx + 1)
-struct StPlane {
-  float v[9];
-};
-
-// interior-stencil row sum over planes A (dz = -1), B (dz = 0), C (dz = +1);
-// HA / HC false: that plane is a Dirichlet plane and contributes nothing
-template <bool HA, bool HC>
-__device__ __forceinline__ float st_sum(const StParams& P, const StPlane& A, const StPlane& B,
-                                        const StPlane& C)
-{
-  float a[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-  for (int k = 0; k < 9; ++k) {
-    if (HA) a[k & 1] = fmaf(P.coef[k], A.v[k], a[k & 1]);
-    a[2 + (k & 1)] = fmaf(P.coef[9 + k], B.v[k], a[2 + (k & 1)]);
-    if (HC) a[4 + (k & 1)] = fmaf(P.coef[18 + k], C.v[k], a[4 + (k & 1)]);
-  }
-  return ((a[0] + a[1]) + (a[2] + a[3])) + (a[4] + a[5]);
-}
-
 __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_constant__ StParams P)
 {
   extern __shared__ __align__(128) unsigned char st_smem_raw[];
@@ -301,14 +267,9 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
       if (active) P.y[(int64_t)z * P.NP + c] = sum;
       facc.add_product(sum, B.v[4]);
     };
+    const auto cf = [&](int k) { return P.coef[k]; };  // constant-bank operands
     auto row = [&](int z, const StPlane& A, const StPlane& B, const StPlane& C) {
-      float sum;
-      if (z >= 2 && z <= P.Nz - 3) sum = st_sum<true, true>(P, A, B, C);  // z is the same for the warp
-      else if (z == 0 || z == P.Nz - 1) sum = P.dd * B.v[4];
-      else if (z == 1 && z == P.Nz - 2) sum = st_sum<false, false>(P, A, B, C);
-      else if (z == 1) sum = st_sum<false, true>(P, A, B, C);
-      else sum = st_sum<true, false>(P, A, B, C);
-      finish(z, sum, B);
+      finish(z, st_row_sum(cf, P.dd, z, P.Nz, A, B, C), B);  // z is the same for the warp
     };
     for (int64_t q = q0; ok && q < q1;) {
       const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
@@ -341,11 +302,11 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
         }
         if (z >= 2 && z + 2 <= P.Nz - 3 && z + 3 <= zb) {  // three interior rows
           load_plane(0, W2);
-          finish(z, st_sum<true, true>(P, W0, W1, W2), W1);
+          finish(z, st_sum<true, true>(cf, W0, W1, W2), W1);
           load_plane(1, W0);
-          finish(z + 1, st_sum<true, true>(P, W1, W2, W0), W2);
+          finish(z + 1, st_sum<true, true>(cf, W1, W2, W0), W2);
           load_plane(2, W1);
-          finish(z + 2, st_sum<true, true>(P, W2, W0, W1), W0);
+          finish(z + 2, st_sum<true, true>(cf, W2, W0, W1), W0);
         } else {
           load_plane(0, W2);
           row(z, W0, W1, W2);
@@ -419,21 +380,20 @@ int64_t stencil_ghost(const mfe_csr* A)
   return NP + Nxp + 8;
 }
 
-mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok)
+mfe_status stencil_prepare_box(mfe_ctx* ctx, int Nx, int Ny, int Nz, const double* vals, float* coef,
+                               bool* ok)
 {
   *ok = false;
-  if (A64->box_nx <= 0 || A64->box_ny <= 0 || A64->box_nz <= 0) return MFE_OK;
-  const int Nx = A64->box_nx + 1, Ny = A64->box_ny + 1, Nz = A64->box_nz + 1;
   if (Nx < 5 || Ny < 5 || Nz < 5) return MFE_OK;  // no interior class
   float* table = static_cast<float*>(workspace(ctx, "stencil.table", sizeof(float) * kSTable + 16));
   if (!table) return fail(ctx, MFE_OOM, "stencil workspace allocation failed");
   unsigned* bad = reinterpret_cast<unsigned*>(table + kSTable);
-  const double* vals = static_cast<const double*>(A64->vals);
   k_st_table<<<1, 128, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table);
   MFE_TRY(check_launch(ctx, "k_st_table"));
   MFE_CUDA_TRY(ctx, cudaMemsetAsync(bad, 0, sizeof(unsigned), ctx->stream));
+  const int64_t n = (int64_t)Nx * Ny * Nz;
   const int blocks = (int)std::max<int64_t>(
-      1, std::min<int64_t>(ceil_div(A64->nrows, (int64_t)kVW * 32),
+      1, std::min<int64_t>(ceil_div(n, (int64_t)kVW * 32),
                            (int64_t)resident_blocks(ctx, (const void*)k_st_verify, kVW * 32, 0)));
   k_st_verify<<<blocks, kVW * 32, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table, bad);
   MFE_TRY(check_launch(ctx, "k_st_verify"));
@@ -446,6 +406,14 @@ mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* 
   memcpy(&hb, host + kSTable, sizeof(unsigned));
   *ok = hb == 0 && st_model(Nx, Ny, Nz, host, coef, coef + 27);
   return MFE_OK;
+}
+
+mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok)
+{
+  *ok = false;
+  if (A64->box_nx <= 0 || A64->box_ny <= 0 || A64->box_nz <= 0) return MFE_OK;
+  return stencil_prepare_box(ctx, A64->box_nx + 1, A64->box_ny + 1, A64->box_nz + 1,
+                             static_cast<const double*>(A64->vals), coef, ok);
 }
 
 mfe_status stencil_grid(mfe_ctx* ctx, int* grid)

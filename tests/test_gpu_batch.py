@@ -159,3 +159,33 @@ def test_batch_tiny_boxes_and_breakdown():
                     assert res[i].status == 4 and res[i].num_iters == it and res[i].normr == 0.0
             else:
                 assert res[i].status == 0, (prec, d, res[i])
+
+
+def test_batch_stencil_operator_matches_values():
+    """Every box with an interior node (>= 4 elements per dimension): the
+    batched mixed solver runs the verified FP32 stencil; each box reaches the
+    FP64-verified tolerance with about as many iterations as with the padded
+    FP32 values.  A batch holding a thinner box falls back to the values."""
+    dims = [(4, 5, 6), (10, 10, 10), (12, 7, 5), (9, 11, 6), (16, 4, 4), (20, 13, 17)]
+    b = M.Batch(dims)
+    out = {}
+    for op in ("auto", "values"):
+        x, res = b.solve(max_iter=3000, tol=1e-8, tol_mode="relative", precision="mixed",
+                         mixed_operator=op)
+        out[op] = (host(x).copy(), res)
+    b.close()
+    xa, ra = out["auto"]
+    xv, rv = out["values"]
+    off = np.cumsum([0] + [(d[0] + 1) * (d[1] + 1) * (d[2] + 1) for d in dims])
+    for i, d in enumerate(dims):
+        assert ra[i].inner_operator == "stencil" and rv[i].inner_operator == "padded"
+        assert ra[i].status == 0 and rv[i].status == 0, (d, ra[i], rv[i])
+        ro, cols, vals, bo = O.build_system(*d)
+        for xs in (xa, xv):
+            xi = xs[off[i]:off[i + 1]]
+            rel = np.linalg.norm(bo - O.matvec(ro, cols, vals, xi)) / np.linalg.norm(bo)
+            assert rel <= 1e-8, (d, rel)
+        assert abs(ra[i].num_iters - rv[i].num_iters) <= max(3, 0.1 * rv[i].num_iters)
+    x, off2, res = M.batch_solve_boxes([(10, 10, 10), (3, 8, 8)], max_iter=3000, tol=1e-8,
+                                       tol_mode="relative", precision="mixed")
+    assert all(r.inner_operator == "padded" and r.status == 0 for r in res)
