@@ -75,12 +75,15 @@ def test_mixed_with_prepared_f32_copy_and_history():
     assert res.refinements >= 1
 
 
-@pytest.mark.parametrize("dims", [(30, 30, 30), (17, 9, 11), (4, 4, 4), (3, 4, 2), (40, 5, 6)])
+@pytest.mark.parametrize("dims", [(30, 30, 30), (17, 9, 11), (4, 4, 4), (3, 4, 2), (40, 5, 6),
+                                  (11, 6, 7), (14, 8, 4)])
 def test_mixed_stencil_operator_and_values_copy(dims):
     """The verified FP32 stencil operator (default on a k = 1 box with an
     interior node, i.e. at least 4 elements along each dimension) and the
     FP32 copy of the values both reach the FP64-verified tolerance with about
-    the same number of inner iterations."""
+    the same number of inner iterations.  The x pitch of the stencil's
+    vectors is Nx rounded up to 4: the cases cover padding 0 (11: Nx = 12),
+    1, 2 and 3, and nz = 4 (one interior plane)."""
     A, b = M.build_system(*dims)
     ro, cols, vals, bo = O.build_system(*dims)
     its = {}
