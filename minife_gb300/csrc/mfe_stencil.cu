@@ -25,14 +25,15 @@
 // k_spmv_stencil works on x-padded vectors (x pitch Nxp = Nx rounded up to a
 // multiple of 4, padding entries zero), so every line segment it copies
 // starts on a 16-byte boundary at the same phase and every shared-memory
-// load has a fixed offset.  It marches along z: a CTA owns 256 consecutive
-// positions of the padded xy plane (one per consumer thread) and a run of z
-// steps; a producer lane streams the three line segments (y-1, y, y+1) of
-// each plane the CTA needs into a ring of shared-memory slots (three planes
-// per slot) with bulk copies, from a vector with ghost zones of zero rows
-// around it.  Each consumer keeps the 3 x 9 values of planes z-1, z, z+1 in
-// registers, so a row costs 9 shared-memory loads and 27 FMAs whose
-// coefficients are kernel parameters (constant-bank operands: no
+// load has a fixed offset.  It marches along z: a CTA owns 512 consecutive
+// positions of the padded xy plane (two adjacent ones per consumer thread)
+// and a run of z steps; a producer lane streams the three line segments
+// (y-1, y, y+1) of each plane the CTA needs into a ring of shared-memory
+// slots (three planes per slot) with bulk copies, from a vector with ghost
+// zones of zero rows around it.  Each consumer keeps planes z-1, z, z+1 of
+// its two rows (x[c-1 .. c+2] of three lines, from three 8-byte loads per
+// line) in registers, so a row costs 4.5 shared-memory loads and 27 FMAs
+// whose coefficients are kernel parameters (constant-bank operands: no
 // registers).  Lanes next to a Dirichlet node zero the masked neighbours as
 // they load them; Dirichlet planes and the planes next to them take
 // warp-uniform branches.  The (plane tile, z) steps are split evenly over
@@ -174,14 +175,58 @@ __device__ __forceinline__ int64_t st_lo(const StParams& P, int z, int j, int c0
   return (int64_t)z * P.NP + (int64_t)(j - 1) * P.Nxp + c0 - 4;
 }
 
-__global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_constant__ StParams P)
+// Two adjacent positions per consumer thread (c even, c + 1): 512-position
+// tiles, so a CTA's bulk copies are half as many and twice as long, and a
+// line's four values x[c-1 .. c+2] come from three 8-byte shared loads for
+// both rows.  A neighbour value is zeroed in the shared window only where
+// the other position is a Dirichlet row (whose sum is replaced by dd * x),
+// and the centres are kept unmasked for that and for the dot.
+constexpr int kS2P = 512;                                 // plane positions per CTA
+constexpr int kS2Cap = kS2P + 8;                          // floats per line segment
+constexpr int kS2Slot = kSKP * 3 * kS2Cap;
+constexpr size_t kS2Smem = sizeof(float) * kSS * kS2Slot;
+static_assert((kS2Cap * sizeof(float)) % 16 == 0, "bulk-copy destinations stay 16-byte aligned");
+
+// line j of a plane: v[4j .. 4j+3] = x[c-1], x[c], x[c+1], x[c+2]; c0, c1:
+// the unmasked centres x[c], x[c+1] of line j = 1
+struct StPlane2 {
+  float v[12];
+  float c0, c1;
+};
+
+template <bool HA, bool HC, typename CF>
+__device__ __forceinline__ void st_sum2(CF cf, const StPlane2& A, const StPlane2& B, const StPlane2& C,
+                                        float& s0, float& s1)
 {
-  extern __shared__ __align__(128) unsigned char st_smem_raw[];
-  float* const ring = reinterpret_cast<float*>(st_smem_raw);
+  float a[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+  float b[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int j = 0; j < 3; ++j)
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      const int k = j * 3 + d, w = 4 * j + d;
+      if (HA) {
+        a[k & 1] = fmaf(cf(k), A.v[w], a[k & 1]);
+        b[k & 1] = fmaf(cf(k), A.v[w + 1], b[k & 1]);
+      }
+      a[2 + (k & 1)] = fmaf(cf(9 + k), B.v[w], a[2 + (k & 1)]);
+      b[2 + (k & 1)] = fmaf(cf(9 + k), B.v[w + 1], b[2 + (k & 1)]);
+      if (HC) {
+        a[4 + (k & 1)] = fmaf(cf(18 + k), C.v[w], a[4 + (k & 1)]);
+        b[4 + (k & 1)] = fmaf(cf(18 + k), C.v[w + 1], b[4 + (k & 1)]);
+      }
+    }
+  s0 = ((a[0] + a[1]) + (a[2] + a[3])) + (a[4] + a[5]);
+  s1 = ((b[0] + b[1]) + (b[2] + b[3])) + (b[4] + b[5]);
+}
+
+__global__ void __launch_bounds__(kS2P / 2 + 32, 2) k_spmv_stencil(const __grid_constant__ StParams P)
+{
+  extern __shared__ __align__(128) unsigned char st2_smem_raw[];
+  float* const ring = reinterpret_cast<float*>(st2_smem_raw);
   __shared__ uint64_t full[kSS], empty[kSS];
   __shared__ double red[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  // this CTA's share of the (plane tile, z) steps, tile-major
   const int64_t T = (int64_t)P.ntile * P.Nz;
   const int64_t q0 = T * blockIdx.x / gridDim.x, q1 = T * (blockIdx.x + 1) / gridDim.x;
   if (threadIdx.x == 0) {
@@ -193,8 +238,6 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
   }
   __syncthreads();
   DFAcc facc;
-  // Slot sequence of a run of rows za .. zb-1 of one plane tile: planes
-  // (za-1, za), then z+1 .. z+min(3, zb-z) for z = za, za+3, ...
   if (warp == 0) {
     if (lane == 0) {
       bool ok = true;
@@ -202,7 +245,7 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
       for (int64_t q = q0; ok && q < q1;) {
         const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
         const int zb = (int)min((int64_t)P.Nz, za + (q1 - q));
-        const int c0 = tile * kSP, c1 = min(P.NP, c0 + kSP);
+        const int c0 = tile * kS2P, c1 = min(P.NP, c0 + kS2P);
         for (int z = za - 3; z < zb; z += 3, ++it) {
           const int zf = z < za ? za - 1 : z + 1;
           const int np = z < za ? 2 : min(3, zb - z);  // planes zf .. zf+np-1
@@ -214,7 +257,7 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
           for (int pl = 0; pl < np; ++pl)
 #pragma unroll
             for (int j = 0; j < 3; ++j)
-              bulk_g2s(ring + s * kSSlot + (pl * 3 + j) * kSCap, P.x + st_lo(P, zf + pl, j, c0), seg,
+              bulk_g2s(ring + s * kS2Slot + (pl * 3 + j) * kS2Cap, P.x + st_lo(P, zf + pl, j, c0), seg,
                        &full[s]);
         }
         q += zb - za;
@@ -229,15 +272,15 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
     const int lr = (warp - 1) * 32 + lane;
     bool ok = true;
     int it = 0;
-    StPlane W0, W1, W2;
-    int c = 0;
-    bool active = false, special = false, mxl = false, mxh = false, myl = false, myh = false, wm = false;
-    float dmul = 0.0f;
+    StPlane2 W0, W1, W2;
+    int c = 0, lane_off = 0;
+    bool active = false, sp0 = false, sp1 = false, m1 = false, m2 = false, m3 = false, myl = false,
+         myh = false, wm = false;
+    float dm0 = 0.0f, dm1 = 0.0f;
     const float* sx = ring;
-    int lane_off = 0;
     auto wait_slot = [&]() {
       const int s = it % kSS;
-      sx = ring + s * kSSlot + lane_off;
+      sx = ring + s * kS2Slot + lane_off;
       return mbar_wait_bounded(&full[s], (unsigned)((it / kSS) & 1));
     };
     auto release_slot = [&]() {
@@ -245,51 +288,77 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
       if (lane == 0) mbar_arrive(&empty[it % kSS]);
       ++it;
     };
-    // the slot's plane pl around this thread's position into W, masked neighbours zeroed
-    auto load_plane = [&](int pl, StPlane& W) {
+    // the slot's plane pl around positions c, c + 1 into W (sx points at x[c-2])
+    auto load_plane = [&](int pl, StPlane2& W) {
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
-        const float* seg = sx + (pl * 3 + j) * kSCap;
-        W.v[j * 3 + 0] = seg[-1];
-        W.v[j * 3 + 1] = seg[0];
-        W.v[j * 3 + 2] = seg[1];
+        const float* seg = sx + (pl * 3 + j) * kS2Cap;
+        const float2 a = *reinterpret_cast<const float2*>(seg);
+        const float2 b = *reinterpret_cast<const float2*>(seg + 2);
+        const float2 e = *reinterpret_cast<const float2*>(seg + 4);
+        W.v[4 * j] = a.y;
+        W.v[4 * j + 1] = b.x;
+        W.v[4 * j + 2] = b.y;
+        W.v[4 * j + 3] = e.x;
+        if (j == 1) {
+          W.c0 = b.x;
+          W.c1 = b.y;
+        }
       }
       if (wm) {  // the same for the whole warp
-        if (mxl) W.v[0] = W.v[3] = W.v[6] = 0.0f;
-        if (mxh) W.v[2] = W.v[5] = W.v[8] = 0.0f;
-        if (myl) W.v[0] = W.v[1] = W.v[2] = 0.0f;
-        if (myh) W.v[6] = W.v[7] = W.v[8] = 0.0f;
+        if (m1) W.v[1] = W.v[5] = W.v[9] = 0.0f;    // x[c]: c is Dirichlet (ix = 0)
+        if (m2) W.v[2] = W.v[6] = W.v[10] = 0.0f;   // x[c+1]: c + 1 is Dirichlet (Nx - 1)
+        if (m3) W.v[3] = W.v[7] = W.v[11] = 0.0f;   // x[c+2]: Dirichlet, used by c + 1 only
+        if (myl) W.v[0] = W.v[1] = W.v[2] = W.v[3] = 0.0f;
+        if (myh) W.v[8] = W.v[9] = W.v[10] = W.v[11] = 0.0f;
       }
     };
-    // row z's result: Dirichlet rows dd * x, padding and idle lanes 0
-    auto finish = [&](int z, float sum, const StPlane& B) {
-      sum = special ? dmul * B.v[4] : sum;
-      if (active) P.y[(int64_t)z * P.NP + c] = sum;
-      facc.add_product(sum, B.v[4]);
+    auto finish = [&](int z, float s0, float s1, const StPlane2& B) {
+      s0 = sp0 ? dm0 * B.c0 : s0;
+      s1 = sp1 ? dm1 * B.c1 : s1;
+      if (active) *reinterpret_cast<float2*>(P.y + (int64_t)z * P.NP + c) = make_float2(s0, s1);
+      facc.add_product(s0, B.c0);
+      facc.add_product(s1, B.c1);
     };
     const auto cf = [&](int k) { return P.coef[k]; };  // constant-bank operands
-    auto row = [&](int z, const StPlane& A, const StPlane& B, const StPlane& C) {
-      finish(z, st_row_sum(cf, P.dd, z, P.Nz, A, B, C), B);  // z is the same for the warp
+    auto row = [&](int z, const StPlane2& A, const StPlane2& B, const StPlane2& C) {
+      float s0, s1;
+      if (z >= 2 && z <= P.Nz - 3) {
+        st_sum2<true, true>(cf, A, B, C, s0, s1);
+      } else if (z == 0 || z == P.Nz - 1) {
+        s0 = P.dd * B.c0;
+        s1 = P.dd * B.c1;
+      } else if (z == 1 && z == P.Nz - 2) {
+        st_sum2<false, false>(cf, A, B, C, s0, s1);
+      } else if (z == 1) {
+        st_sum2<false, true>(cf, A, B, C, s0, s1);
+      } else {
+        st_sum2<true, false>(cf, A, B, C, s0, s1);
+      }
+      finish(z, s0, s1, B);
     };
     for (int64_t q = q0; ok && q < q1;) {
       const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
       const int zb = (int)min((int64_t)P.Nz, za + (q1 - q));
-      const int c0 = tile * kSP;
-      const int c1 = min(P.NP, c0 + kSP);
-      c = c0 + lr;
-      active = c < c1;
-      const int cc = active ? c : c1 - 1;
-      lane_off = cc - c0 + 4;
-      const int iy = cc / P.Nxp, ix = cc - iy * P.Nxp;
-      const bool real = active && ix < P.Nx;
-      const bool dir = ix == 0 || ix == P.Nx - 1 || iy == 0 || iy == P.Ny - 1;
-      special = !real || dir;
-      dmul = real ? P.dd : 0.0f;
-      mxl = ix == 1;
-      mxh = ix == P.Nx - 2;
+      const int c0 = tile * kS2P;
+      const int c1 = min(P.NP, c0 + kS2P);
+      c = c0 + 2 * lr;
+      active = c < c1;  // then c + 1 < c1 too (both even)
+      const int cc = active ? c : c1 - 2;
+      lane_off = cc - c0 + 2;  // x[cc - 2]: even, so the 8-byte loads are aligned
+      const int iy = cc / P.Nxp, ix0 = cc - iy * P.Nxp, ix1 = ix0 + 1;
+      const bool dy = iy == 0 || iy == P.Ny - 1;
+      const bool real0 = active && ix0 < P.Nx, real1 = active && ix1 < P.Nx;
+      sp0 = !real0 || dy || ix0 == 0 || ix0 == P.Nx - 1;
+      sp1 = !real1 || dy || ix1 == P.Nx - 1;
+      dm0 = real0 ? P.dd : 0.0f;
+      dm1 = real1 ? P.dd : 0.0f;
+      m1 = ix1 == 1;
+      m2 = ix0 == P.Nx - 2;
+      m3 = ix1 == P.Nx - 2;
       myl = iy == 1;
       myh = iy == P.Ny - 2;
-      wm = __any_sync(0xffffffffu, mxl || mxh || myl || myh);
+      wm = __any_sync(0xffffffffu, m1 || m2 || m3 || myl || myh);
       ok = wait_slot();
       if (!ok) break;
       load_plane(0, W0);
@@ -301,12 +370,16 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_spmv_stencil(const __grid_const
           break;
         }
         if (z >= 2 && z + 2 <= P.Nz - 3 && z + 3 <= zb) {  // three interior rows
+          float s0, s1;
           load_plane(0, W2);
-          finish(z, st_sum<true, true>(cf, W0, W1, W2), W1);
+          st_sum2<true, true>(cf, W0, W1, W2, s0, s1);
+          finish(z, s0, s1, W1);
           load_plane(1, W0);
-          finish(z + 1, st_sum<true, true>(cf, W1, W2, W0), W2);
+          st_sum2<true, true>(cf, W1, W2, W0, s0, s1);
+          finish(z + 1, s0, s1, W2);
           load_plane(2, W1);
-          finish(z + 2, st_sum<true, true>(cf, W2, W0, W1), W0);
+          st_sum2<true, true>(cf, W2, W0, W1, s0, s1);
+          finish(z + 2, s0, s1, W0);
         } else {
           load_plane(0, W2);
           row(z, W0, W1, W2);
@@ -422,9 +495,9 @@ mfe_status stencil_grid(mfe_ctx* ctx, int* grid)
   const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
   if (per_sm[dev] == 0) {
     MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmv_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)kStSmem));
+                                           (int)kS2Smem));
     int b = 1;
-    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_stencil, kSP + 32, kStSmem));
+    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_stencil, kS2P / 2 + 32, kS2Smem));
     per_sm[dev] = std::max(b, 1);
   }
   *grid = ctx->sm_count * per_sm[dev];
@@ -440,7 +513,7 @@ mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef
   P.Nz = A->box_nz + 1;
   P.Nxp = stencil_pitch(A);
   P.NP = P.Nxp * P.Ny;
-  P.ntile = (int)ceil_div(P.NP, (int64_t)kSP);
+  P.ntile = (int)ceil_div(P.NP, (int64_t)kS2P);
   for (int k = 0; k < 27; ++k) P.coef[k] = coef[k];
   P.dd = coef[27];
   P.x = x;
@@ -450,7 +523,7 @@ mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef
   P.dot_out = sink->out;
   P.err = err;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)grid, (int64_t)P.ntile * P.Nz));
-  k_spmv_stencil<<<g, kSP + 32, kStSmem, ctx->stream>>>(P);
+  k_spmv_stencil<<<g, kS2P / 2 + 32, kS2Smem, ctx->stream>>>(P);
   return check_launch(ctx, "k_spmv_stencil");
 }
 
