@@ -222,15 +222,22 @@ typedef struct mfe_cg_opts {
   int32_t record_history; /* 1: keep normr of every iteration (see
                              mfe_cg_history) */
   const mfe_csr* A32;   /* mixed: optional prepared FP32 copy of A (NULL: the
-                           library converts and caches one) */
+                           library uses its stencil operator or converts a
+                           copy on every call, see mixed_operator) */
   int32_t precond;      /* mfe_cg_solve: 0 none (the reference's CG), 1 Jacobi
                            (M = diag(A), FP64; stops on ||r|| after the update) */
-  int32_t mixed_operator; /* mixed, single right-hand side: 0 = the FP32
-                           stencil operator when every row of A lies within
-                           2^-22 (relative to the row) of its boundary class's
-                           stencil (checked on the device; a miniFE box with
-                           k = 1), else the FP32 copy of the values;
-                           1 = always the FP32 copy of the values */
+  int32_t mixed_operator; /* mixed solves (mfe_cg_solve, mfe_batch_solve):
+                           0 = the FP32 stencil operator (28 numbers: the
+                           interior 27-point stencil and the Dirichlet
+                           diagonal) when A is a miniFE box operator: every
+                           row is dd * x_r (Dirichlet node) or the interior
+                           stencil with the Dirichlet neighbours zeroed, every
+                           entry within 2^-22 of its row's largest magnitude
+                           (checked on the device on every call; once per
+                           batch handle), else the FP32 copy of the values
+                           (padded values for batches); 1 = always the FP32
+                           values.  mfe_cg_result.inner_operator reports
+                           which ran. */
 } mfe_cg_opts;
 
 /* Fill opts with the reference's defaults (max_iter 200, absolute tol
