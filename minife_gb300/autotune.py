@@ -9,7 +9,8 @@ events, results[i].times[4]):
 
 1. SpMV shape: every (rows, stages) the library instantiates, each timed on
    a solve capped at `probe_iters` iterations, so every shape does the same
-   work;
+   work (skipped when the batch runs the FP32 stencil operator, which has
+   one shape: the first trial reports it);
 2. chunk rows: the same capped solve at the best shape;
 3. refine_k: full solves to the tolerance at the best shape and chunk, only
    candidates whose every box converges.
@@ -95,9 +96,12 @@ def tune_batch(batch, precision: str = "mixed", tol: float = 1e-8, tol_mode: str
     cur = dict(DEFAULT)
     trials = []
 
+    op = ["none"]
+
     def capped(cfg):
         batch.set_tuning(cfg["spmv_rows"], cfg["spmv_stages"], cfg["chunk_rows"])
-        t, _ = _solve_time(batch, precision, 0.0, tol_mode, probe_iters, cfg["refine_k"], reps)
+        t, res = _solve_time(batch, precision, 0.0, tol_mode, probe_iters, cfg["refine_k"], reps)
+        op[0] = getattr(res[0], "inner_operator", "none")
         trials.append({"stage": "capped", **cfg, "seconds": t})
         say("capped %s: %.4f s" % (cfg, t))
         return t
@@ -108,6 +112,8 @@ def tune_batch(batch, precision: str = "mixed", tol: float = 1e-8, tol_mode: str
         t = capped(cfg)
         if best_t is None or t < best_t:
             best_t, cur = t, cfg
+        if op[0] == "stencil":
+            break  # the SpMV shape does not apply to the stencil operator
     for chunk in CHUNKS:
         if chunk == cur["chunk_rows"]:
             continue
@@ -127,7 +133,7 @@ def tune_batch(batch, precision: str = "mixed", tol: float = 1e-8, tol_mode: str
                 best_full, cur = t, dict(cur, refine_k=k)
     else:
         best_full, _ = _solve_time(batch, precision, tol, tol_mode, max_iter, cur["refine_k"], reps)
-    entry = dict(cur, solve_seconds=best_full, trials=trials)
+    entry = dict(cur, solve_seconds=best_full, inner_operator=op[0], trials=trials)
     if use_cache:
         _store(key, entry)
     return dict(entry, cached=False)

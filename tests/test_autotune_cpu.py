@@ -6,9 +6,10 @@ from minife_gb300 import autotune
 
 
 class _Res:
-    def __init__(self, t, status=0):
+    def __init__(self, t, status=0, op="padded"):
         self.times = (0.0, 0.0, 0.0, 0.0, t)
         self.status = status
+        self.inner_operator = op
 
 
 class FakeBatch:
@@ -67,3 +68,19 @@ def test_cache_hit_skips_search(cache):
 def test_signature_ignores_box_order(cache):
     assert autotune.signature([(1, 2, 3), (4, 5, 6)], "mixed") == \
         autotune.signature([(4, 5, 6), (1, 2, 3)], "mixed")
+
+
+class StencilBatch(FakeBatch):
+    """Every box passes the stencil check: the SpMV shape has no effect."""
+
+    def solve(self, max_iter, tol, tol_mode, precision, refine_k):
+        t, res = super().solve(max_iter, tol, tol_mode, precision, refine_k)
+        return t, [_Res(r.times[4], r.status, "stencil") for r in res]
+
+
+def test_stencil_batch_skips_shape_search(cache):
+    b = StencilBatch()
+    cfg = autotune.tune_batch(b, probe_iters=5, reps=1)
+    shapes = {c[0][:2] for c in b.calls if c[2] == 0.0}
+    assert shapes == {autotune.SHAPES[0]}   # one capped trial, then chunks only
+    assert cfg["inner_operator"] == "stencil" and cfg["refine_k"] == 50
