@@ -514,7 +514,7 @@ def bench_batch(args, world, stream):
     residual), launch shape and refine_k from the autotuner.  Timed: the
     batched solve (one graph launch) per step; the sequential baseline is
     the same boxes solved one after another with the single-box mixed
-    solver."""
+    solver at the same refine_k."""
     import torch
     import minife_gb300 as M
     from minife_gb300 import autotune
@@ -555,10 +555,11 @@ def bench_batch(args, world, stream):
             A, b = M.build_system(*d)
             xx = torch.zeros_like(b)
             r = M.cg_solve(A, b, xx, max_iter=5000, tol=TOL, tol_mode="relative",
-                           precision="mixed", refine_k=50)
+                           precision="mixed", refine_k=cfg["refine_k"])
             t_seq += r.total_time
             del A, b, xx
         out["sequential_mixed_s"] = t_seq
+        out["sequential_refine_k"] = cfg["refine_k"]
         out["speedup_vs_sequential"] = t_seq / t
     return out
 

@@ -27,7 +27,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 
 SHAPES = [(256, 2), (256, 3), (256, 4), (128, 2), (128, 3), (128, 4)]
 CHUNKS = [4096, 8192, 16384, 32768]
-REFINE_K = [25, 50, 100]
+REFINE_K = [25, 50, 100, 200]
 DEFAULT = {"spmv_rows": 256, "spmv_stages": 2, "chunk_rows": 8192, "refine_k": 50}
 
 

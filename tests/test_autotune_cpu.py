@@ -31,9 +31,9 @@ class FakeBatch:
             t = 1.0 + 0.1 * abs(rows - 128) / 128 + 0.05 * abs(stages - 3) + \
                 0.01 * abs(chunk - 16384) / 16384
             return None, [_Res(t, 5)] * 2
-        # full solves: refine_k 100 fastest but does not converge, 50 next
-        t = {25: 3.0, 50: 2.0, 100: 1.0}[refine_k]
-        return None, [_Res(t, 0 if refine_k != 100 else 5)] * 2
+        # full solves: refine_k 100 and 200 fastest but do not converge, 50 next
+        t = {25: 3.0, 50: 2.0, 100: 1.0, 200: 0.5}[refine_k]
+        return None, [_Res(t, 0 if refine_k < 100 else 5)] * 2
 
 
 @pytest.fixture
@@ -47,7 +47,7 @@ def test_search_picks_fastest_converging(cache):
     b = FakeBatch()
     cfg = autotune.tune_batch(b, probe_iters=5, reps=1)
     assert (cfg["spmv_rows"], cfg["spmv_stages"], cfg["chunk_rows"]) == (128, 3, 16384)
-    assert cfg["refine_k"] == 50           # 100 is faster but did not converge
+    assert cfg["refine_k"] == 50           # 100 and 200 are faster but did not converge
     assert b.tuning == (128, 3, 16384)     # applied to the batch
     assert not cfg["cached"] and cache.exists()
     assert all(c[1] == 5 for c in b.calls if c[2] == 0.0)  # capped probes
