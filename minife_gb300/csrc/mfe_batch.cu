@@ -645,6 +645,254 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_bx_stencil(const __grid_constan
   }
 }
 
+// Two adjacent plane positions per consumer thread (c - c0 even, c + 1) over
+// 512-position tiles, for batches whose boxes all have mirror-symmetric
+// stencils: a coefficient then depends only on (|dz|, |dy|, |dx|), so a box
+// needs 8 weights in registers (w[4|dz| + 2|dy| + |dx|]) and a line of the
+// window x[c-1 .. c+2] gives row c  w0 x[c] + w1 (x[c-1] + x[c+1]) and row
+// c + 1  w0 x[c+1] + w1 (x[c] + x[c+2]).  Both y neighbours of a position are
+// at -Nx / +Nx in the flattened plane, so a pair needs the same three lines;
+// a pair that straddles two x lines is two Dirichlet rows (ix = Nx-1 and 0),
+// whose results are replaced by dd * x.  Natural layout: four scalar loads
+// per line (the copy phase follows the row's address mod 4).
+constexpr int kB2P = 512;
+constexpr int kB2Cap = ((kB2P + 9) + 3) & ~3;  // copies hold x[c0-1-phase .. c1+1]
+constexpr int kB2Slot = kSKP * 3 * kB2Cap;
+constexpr size_t kB2Smem = sizeof(float) * kSS * kB2Slot;
+static_assert((kB2Cap * sizeof(float)) % 16 == 0, "bulk-copy destinations stay 16-byte aligned");
+
+// one past the last float of the copy of line (z, dy = j - 1) for the pair
+// kernel: its last row c1 - 1 reads x[c1 + 1]
+__device__ __forceinline__ int64_t bxs_hi2(const BoxDesc& d, int z, int j, int c1)
+{
+  return ((int64_t)z * d.NxNy + (int64_t)(j - 1) * d.Nx + c1 + 2 + 3) & ~(int64_t)3;
+}
+
+struct BxPlane2 {
+  float v[12];  // line j: x[c-1], x[c], x[c+1], x[c+2]
+  float c0, c1;  // unmasked centres
+};
+
+__device__ __forceinline__ void bx_sum2(const float* w, const BxPlane2& A, const BxPlane2& B,
+                                        const BxPlane2& C, bool HA, bool HC, float& s0, float& s1)
+{
+  float a[4] = {0.0f, 0.0f, 0.0f, 0.0f}, b[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+  for (int pz = 0; pz < 3; ++pz) {
+    const BxPlane2& P = pz == 0 ? A : (pz == 1 ? B : C);
+    if ((pz == 0 && !HA) || (pz == 2 && !HC)) continue;
+#pragma unroll
+    for (int j = 0; j < 3; ++j) {
+      const int cls = 4 * (pz != 1) + 2 * (j != 1);
+      const float w0 = w[cls], w1 = w[cls + 1];
+      const float* v = P.v + 4 * j;
+      a[2 * (j & 1)] = fmaf(w0, v[1], a[2 * (j & 1)]);
+      a[2 * (j & 1) + 1] = fmaf(w1, v[0] + v[2], a[2 * (j & 1) + 1]);
+      b[2 * (j & 1)] = fmaf(w0, v[2], b[2 * (j & 1)]);
+      b[2 * (j & 1) + 1] = fmaf(w1, v[1] + v[3], b[2 * (j & 1) + 1]);
+    }
+  }
+  s0 = (a[0] + a[1]) + (a[2] + a[3]);
+  s1 = (b[0] + b[1]) + (b[2] + b[3]);
+}
+
+__global__ void __launch_bounds__(kB2P / 2 + 32, 2) k_bx_stencil2(const __grid_constant__ BxStParams P)
+{
+  extern __shared__ __align__(128) unsigned char bx2_smem[];
+  float* const ring = reinterpret_cast<float*>(bx2_smem);
+  __shared__ uint64_t full[kSS], empty[kSS];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int cnt = *P.count;
+  if (cnt == 0) return;
+  const int total = __ldg(&P.tpre[cnt]);
+  const int t_begin = bx_start(blockIdx.x, total, gridDim.x);
+  const int t_end = bx_start(blockIdx.x + 1, total, gridDim.x);
+  if (t_begin >= t_end) return;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kSS; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kSC);
+    }
+    fence_mbar_init();
+  }
+  __syncthreads();
+  if (warp == 0) {
+    if (lane == 0) {
+      bool ok = true;
+      int it = 0, q = -1, A = 0, E = 0;
+      BoxDesc d{};
+      for (int i = t_begin; ok && i < t_end;) {
+        const int nq = bx_advance(P.tpre, cnt, q, i);
+        if (nq != q) {
+          q = nq;
+          d = P.boxes[__ldg(&P.ids[q])];
+          A = __ldg(&P.tpre[q]);
+          E = __ldg(&P.tpre[q + 1]);
+        }
+        const int tile = (i - A) / d.Nz, za = (i - A) - tile * d.Nz;
+        const int zb = min(d.Nz, za + (min(t_end, E) - i));
+        const int c0 = tile * kB2P, c1 = min(d.NxNy, c0 + kB2P);
+        const float* xb = P.x + d.row_base;
+        for (int z = za - 3; z < zb; z += 3, ++it) {
+          const int zf = z < za ? za - 1 : z + 1;
+          const int np = z < za ? 2 : min(3, zb - z);  // planes zf .. zf+np-1
+          const int s = it % kSS;
+          if (it >= kSS) ok = mbar_wait_bounded(&empty[s], (unsigned)(((it / kSS) - 1) & 1));
+          if (!ok) break;
+          unsigned bytes = 0;
+          for (int pl = 0; pl < np; ++pl)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+              bytes += (unsigned)((bxs_hi2(d, zf + pl, j, c1) - bxs_lo(d, zf + pl, j, c0)) * sizeof(float));
+          mbar_arrive_expect_tx(&full[s], bytes);
+          for (int pl = 0; pl < np; ++pl)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+              const int64_t lo = bxs_lo(d, zf + pl, j, c0);
+              bulk_g2s(ring + s * kB2Slot + (pl * 3 + j) * kB2Cap, xb + lo,
+                       (unsigned)((bxs_hi2(d, zf + pl, j, c1) - lo) * sizeof(float)), &full[s]);
+            }
+        }
+        i += zb - za;
+      }
+      if (!ok) {
+        atomicOr(P.err, ERR_WAIT_TIMEOUT);
+        for (int st = 0; st < kSS && st < it; ++st)
+          mbar_wait_bounded(&full[st], (unsigned)(((it - st + kSS - 1) / kSS - 1) & 1));
+      }
+    }
+  } else {
+    const int cw = warp - 1;
+    const int lr = cw * 32 + lane;
+    bool ok = true;
+    int it = 0, q = -1, b = -1, A = 0, E = 0;
+    BoxDesc d{};
+    DFAcc facc;
+    float w[8], dd = 0.0f;
+    BxPlane2 W0, W1, W2;
+    int c = 0, c0 = 0, cc = 0;
+    bool act0 = false, act1 = false, sp0 = false, sp1 = false;
+    bool m1 = false, m2 = false, m3 = false, myl = false, myh = false, wm = false;
+    const float* sx = ring;
+    auto wait_slot = [&]() {
+      const int s = it % kSS;
+      sx = ring + s * kB2Slot + (cc - c0 + 1);
+      return mbar_wait_bounded(&full[s], (unsigned)((it / kSS) & 1));
+    };
+    auto release_slot = [&]() {
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[it % kSS]);
+      ++it;
+    };
+    // plane z (the slot's plane pl) around positions cc, cc + 1 into W
+    auto load_plane = [&](int pl, int z, BxPlane2& W) {
+      const unsigned zb0 = (unsigned)z * (unsigned)d.NxNy + (unsigned)(c0 - 1);
+#pragma unroll
+      for (int j = 0; j < 3; ++j) {
+        // sx points at x[cc] of a copy starting at position c0 - 1 (phase 0)
+        const float* seg = sx + (pl * 3 + j) * kB2Cap + ((zb0 + (unsigned)((j - 1) * d.Nx)) & 3u);
+        W.v[4 * j] = seg[-1];
+        W.v[4 * j + 1] = seg[0];
+        W.v[4 * j + 2] = seg[1];
+        W.v[4 * j + 3] = seg[2];
+        if (j == 1) {
+          W.c0 = seg[0];
+          W.c1 = seg[1];
+        }
+      }
+      if (wm) {  // the same for the whole warp
+        if (m1) W.v[1] = W.v[5] = W.v[9] = 0.0f;   // x[c]: c is Dirichlet (ix = 0)
+        if (m2) W.v[2] = W.v[6] = W.v[10] = 0.0f;  // x[c+1]: c + 1 is Dirichlet
+        if (m3) W.v[3] = W.v[7] = W.v[11] = 0.0f;  // x[c+2]: Dirichlet, used by c + 1 only
+        if (myl) W.v[0] = W.v[1] = W.v[2] = W.v[3] = 0.0f;
+        if (myh) W.v[8] = W.v[9] = W.v[10] = W.v[11] = 0.0f;
+      }
+    };
+    auto finish = [&](int z, float s0, float s1, const BxPlane2& B) {
+      s0 = sp0 ? dd * B.c0 : s0;
+      s1 = sp1 ? dd * B.c1 : s1;
+      const int64_t g = d.row_base + (int64_t)z * d.NxNy + c;
+      if (act0) {
+        P.y[g] = s0;
+        facc.add_product(s0, B.c0);
+      }
+      if (act1) {
+        P.y[g + 1] = s1;
+        facc.add_product(s1, B.c1);
+      }
+    };
+    auto row = [&](int z, const BxPlane2& A_, const BxPlane2& B, const BxPlane2& C) {
+      float s0, s1;
+      if (z == 0 || z == d.Nz - 1) {  // the same for the whole warp
+        s0 = dd * B.c0;
+        s1 = dd * B.c1;
+      } else {
+        bx_sum2(w, A_, B, C, z != 1, z != d.Nz - 2, s0, s1);
+      }
+      finish(z, s0, s1, B);
+    };
+    for (int i = t_begin; ok && i < t_end;) {
+      const int nq = bx_advance(P.tpre, cnt, q, i);
+      if (nq != q) {
+        if (q >= 0) bx_flush<BX_DOT, kSC>(P.st, P.slots, b, A, E, total, cw, facc.value());
+        facc = DFAcc{};
+        q = nq;
+        b = __ldg(&P.ids[q]);
+        d = P.boxes[b];
+        A = __ldg(&P.tpre[q]);
+        E = __ldg(&P.tpre[q + 1]);
+#pragma unroll
+        for (int k = 0; k < 8; ++k) w[k] = __ldg(P.coef + (size_t)b * 28 + k);
+        dd = __ldg(P.coef + (size_t)b * 28 + 27);
+      }
+      const int tile = (i - A) / d.Nz, za = (i - A) - tile * d.Nz;
+      const int zb = min(d.Nz, za + (min(t_end, E) - i));
+      c0 = tile * kB2P;
+      const int c1 = min(d.NxNy, c0 + kB2P);
+      c = c0 + 2 * lr;
+      act0 = c < c1;
+      act1 = c + 1 < c1;
+      cc = act0 ? c : c1 - 1;  // c1 - 1 >= c0, and cc + 2 stays inside the copy
+      const int iy = cc / d.Nx, ix0 = cc - iy * d.Nx, ix1 = ix0 + 1;
+      const bool dy = iy == 0 || iy == d.Ny - 1;
+      sp0 = dy || ix0 == 0 || ix0 == d.Nx - 1;
+      // ix1 == Nx: c + 1 starts the next x line (ix 0, a Dirichlet node)
+      sp1 = dy || ix1 >= d.Nx - 1;
+      m1 = ix1 == 1;
+      m2 = ix0 == d.Nx - 2;
+      m3 = ix1 == d.Nx - 2;
+      myl = iy == 1;
+      myh = iy == d.Ny - 2;
+      wm = __any_sync(0xffffffffu, m1 || m2 || m3 || myl || myh);
+      ok = wait_slot();
+      if (!ok) break;
+      load_plane(0, za - 1, W0);
+      load_plane(1, za, W1);
+      release_slot();
+      for (int z = za; z < zb; z += 3) {
+        if (!wait_slot()) {
+          ok = false;
+          break;
+        }
+        load_plane(0, z + 1, W2);
+        row(z, W0, W1, W2);
+        if (z + 1 < zb) {
+          load_plane(1, z + 2, W0);
+          row(z + 1, W1, W2, W0);
+        }
+        if (z + 2 < zb) {
+          load_plane(2, z + 3, W1);
+          row(z + 2, W2, W0, W1);
+        }
+        release_slot();
+      }
+      i += zb - za;
+    }
+    if (!ok) atomicOr(P.err, ERR_WAIT_TIMEOUT);
+    if (q >= 0) bx_flush<BX_DOT, kSC>(P.st, P.slots, b, A, E, total, cw, facc.value());
+  }
+}
+
 // ---------------------------------------------------------------------------
 // vector kernels over the chunk list
 // ---------------------------------------------------------------------------
@@ -1041,6 +1289,8 @@ struct mfe_batch {
   bool ell_ready = false;
   int stencil_state = 0;   // 0: not checked, 1: every box verified, 2: not every box
   float* coef = nullptr;   // [nbox][28] when stencil_state == 1
+  float* coef8 = nullptr;  // [nbox][28]: 8 mirror-class weights and dd (index 27) when
+                           // every box's stencil is mirror-symmetric, else null
   // device memory
   mfe::BoxDesc* boxes = nullptr;
   mfe::BoxSt* st = nullptr;
@@ -1123,20 +1373,44 @@ struct Run {
   Grids grid;
   bool mixed;
   bool stencil;  // FP32 products by k_bx_stencil (tpre32 then counts its steps)
+  bool stencil2; // ... by k_bx_stencil2 (mirror-symmetric stencils, two rows per thread)
 };
 
 void* bx_alloc(mfe_batch* bt, size_t bytes);
 
 // resident CTAs of the batched stencil SpMV (attribute set before any capture)
-mfe_status bx_stencil_grid(mfe_ctx* ctx, int* grid)
+mfe_status bx_stencil_grid(mfe_ctx* ctx, bool pair, int* grid)
 {
-  cudaError_t e = cudaFuncSetAttribute(k_bx_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       (int)kStSmem);
+  const void* k = pair ? (const void*)k_bx_stencil2 : (const void*)k_bx_stencil;
+  const size_t smem = pair ? kB2Smem : kStSmem;
+  const int threads = pair ? kB2P / 2 + 32 : kSP + 32;
+  cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   int per = 1;
-  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_bx_stencil, kSP + 32, kStSmem);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, threads, smem);
   if (e != cudaSuccess) return cuda_fail(ctx, e, "batched stencil SpMV configuration");
   *grid = ctx->sm_count * std::max(per, 1);
   return MFE_OK;
+}
+
+// the 8 mirror-class weights of a verified stencil (coef[0..26] slot order
+// (dz, dy, dx), coef[27] = dd): weight 4|dz| + 2|dy| + |dx| is the entry at
+// (|dz|, |dy|, |dx|); every entry must lie within 2^-22 max|coef| of its
+// class weight (so the operator stays within 2^-21 of every row of A)
+bool bx_mirror_classes(const float* coef, float* w8)
+{
+  float amax = 0.0f;
+  for (int k = 0; k < 27; ++k) amax = std::max(amax, std::fabs(coef[k]));
+  const double tol = std::ldexp((double)amax, -22);
+  for (int c = 0; c < 8; ++c) {
+    const int az = c >> 2, ay = (c >> 1) & 1, ax = c & 1;
+    w8[c] = coef[(az + 1) * 9 + (ay + 1) * 3 + (ax + 1)];
+  }
+  for (int k = 0; k < 27; ++k) {
+    const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+    const int c = 4 * (dz != 0) + 2 * (dy != 0) + (dx != 0);
+    if (std::fabs((double)coef[k] - (double)w8[c]) > tol) return false;
+  }
+  return true;
 }
 
 // every box checked once per batch (its values never change after assembly)
@@ -1155,6 +1429,17 @@ mfe_status bx_stencil_prepare(mfe_ctx* ctx, mfe_batch* bt)
     bt->coef = static_cast<float*>(bx_alloc(bt, sizeof(float) * hc.size()));
     if (!bt->coef) return fail(ctx, MFE_OOM, "batch stencil allocation failed");
     MFE_CUDA_TRY(ctx, cudaMemcpy(bt->coef, hc.data(), sizeof(float) * hc.size(), cudaMemcpyHostToDevice));
+    std::vector<float> h8(hc.size(), 0.0f);
+    bool sym = true;
+    for (int i = 0; i < bt->nbox && sym; ++i) {
+      sym = bx_mirror_classes(&hc[(size_t)i * 28], &h8[(size_t)i * 28]);
+      h8[(size_t)i * 28 + 27] = hc[(size_t)i * 28 + 27];
+    }
+    if (sym) {
+      bt->coef8 = static_cast<float*>(bx_alloc(bt, sizeof(float) * h8.size()));
+      if (!bt->coef8) return fail(ctx, MFE_OOM, "batch stencil allocation failed");
+      MFE_CUDA_TRY(ctx, cudaMemcpy(bt->coef8, h8.data(), sizeof(float) * h8.size(), cudaMemcpyHostToDevice));
+    }
   }
   bt->stencil_state = all ? 1 : 2;
   return MFE_OK;
@@ -1195,11 +1480,15 @@ mfe_status bx_spmv32(mfe_ctx* ctx, const Run& R, const BxList& L, const float* x
     S.ids = L.ids;
     S.tpre = L.tpre32;
     S.count = L.count;
-    S.coef = R.bt->coef;
+    S.coef = R.stencil2 ? R.bt->coef8 : R.bt->coef;
     S.x = x;
     S.y = y;
     S.slots = R.bt->slots;
     S.err = &R.bt->ctl->err;
+    if (R.stencil2) {
+      k_bx_stencil2<<<R.grid.g32, kB2P / 2 + 32, kB2Smem, ctx->stream>>>(S);
+      return check_launch(ctx, "k_bx_stencil2");
+    }
     k_bx_stencil<<<R.grid.g32, kSP + 32, kStSmem, ctx->stream>>>(S);
     return check_launch(ctx, "k_bx_stencil");
   }
@@ -1460,17 +1749,18 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
   R.mixed = o->precision == MFE_PREC_MIXED;
   if (R.mixed && o->mixed_operator == 0) MFE_TRY(bx_stencil_prepare(ctx, bt));
   R.stencil = R.mixed && o->mixed_operator == 0 && bt->stencil_state == 1;
+  R.stencil2 = R.stencil && bt->coef8 != nullptr;
   R.open = bx_list(bt->lists, nbox, 0);
   R.gate = bx_list(bt->lists, nbox, 1);
   R.all = bx_list(bt->lists, nbox, 2);
   MFE_TRY(bx_grids(ctx, bt->tune, &R.grid));
-  if (R.stencil) MFE_TRY(bx_stencil_grid(ctx, &R.grid.g32));
+  if (R.stencil) MFE_TRY(bx_stencil_grid(ctx, R.stencil2, &R.grid.g32));
   const size_t rows8 = (size_t)(bt->rows_tot + 8);
 
   // tiles (stencil steps) and chunks of each box at this launch shape
   int chunks_tot = 0;
   for (auto& d : bt->hd) {
-    d.ntiles32 = R.stencil ? (int)(ceil_div(d.NxNy, (int64_t)kSP) * d.Nz)
+    d.ntiles32 = R.stencil ? (int)(ceil_div(d.NxNy, (int64_t)(R.stencil2 ? kB2P : kSP)) * d.Nz)
                            : (int)ceil_div(d.n, bt->tune.spmv_rows);
     d.ntiles64 = (int)ceil_div(d.n, kBx64Rows);
     d.nchunks = (int)ceil_div(d.n, bt->tune.chunk_rows);
