@@ -444,6 +444,10 @@ int main(int argc, char** argv)
     gpu->add("Initial Resid Norm", r.normr0);
     gpu->add("True Final Resid Norm", r.final_resid);
     gpu->add("reliable updates", r.refinements);
+    if (p.precision == "mixed")
+      gpu->add("inner operator", r.inner_operator == MFE_INNER_STENCIL
+                                     ? "FP32 stencil (verified)"
+                                     : (r.inner_operator == MFE_INNER_VALUES ? "FP32 values" : "other"));
     gpu->add("op times", "standalone kernels scaled by operation counts");
     gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) / t_mv * 1e-9);
     if (p.verify_solution > 0) gpu->add("verification", verify_result == 0 ? "passed" : "failed");

@@ -69,6 +69,7 @@ def test_minife_x_mixed_relative(tmp_path):
     true_res = float(yaml_value(yml, "True Final Resid Norm"))
     r0 = float(yaml_value(yml, "Initial Resid Norm"))
     assert true_res <= 1e-8 * r0
+    assert yaml_value(yml, "inner operator") == "FP32 stencil (verified)"
 
 
 def test_minife_x_kernel_timing_mode(tmp_path):
