@@ -1408,7 +1408,7 @@ bool bx_mirror_classes(const float* coef, float* w8)
   for (int k = 0; k < 27; ++k) {
     const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
     const int c = 4 * (dz != 0) + 2 * (dy != 0) + (dx != 0);
-    if (std::fabs((double)coef[k] - (double)w8[c]) > tol) return false;
+    if (!(std::fabs((double)coef[k] - (double)w8[c]) <= tol)) return false;
   }
   return true;
 }

@@ -129,7 +129,8 @@ __global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
       long long amax = 0;
       for (int t = 0; t < len; ++t) amax = max(amax, __double_as_longlong(a[t]) & kMag);
       const long long tol = amax - 22 * kOne;  // 2^-22 max|a_row| (bit pattern)
-      bool good = tol >= 2 * kOne;             // a normal tol / 2
+      // a normal tol / 2, and no infinite or NaN entry in the row
+      bool good = tol >= 2 * kOne && amax < 0x7ff0000000000000ll;
       const long long half = tol - kOne, twice = tol + kOne;
       const int e_tol = (int)(tol >> 52);
       int q = 0, slot = 0;
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
                             iz + dz >= 0 && iz + dz < Nz;
             const long long ab = in ? __double_as_longlong(a[q++]) : 0ll;
             const long long sb = __double_as_longlong(f2d_exact(s[slot]));
-            const long long am = ab & kMag, sm = sb & kMag;
+            const long long am = ab & kMag, sm = sb & kMag;  // sm finite: class rows are checked on the host
             const bool small = am <= half && sm <= half;
             const int sh = e_tol - (int)(sm >> 52) + 51;  // in [28, 50] when sm >= twice
             const long long d = ab - sb;
@@ -418,7 +419,10 @@ bool st_model(int Nx, int Ny, int Nz, const float* tab, float* coef, float* dd)
     const bool dir = ix == 0 || ix == Nx - 1 || iy == 0 || iy == Ny - 1 || iz == 0 || iz == Nz - 1;
     const float* s = tab + c * 28;
     float amax = 0.0f;
-    for (int k = 0; k < 27; ++k) amax = std::max(amax, std::fabs(s[k]));
+    for (int k = 0; k < 27; ++k) {
+      if (!std::isfinite(s[k])) return false;
+      amax = std::max(amax, std::fabs(s[k]));
+    }
     const double tol = std::ldexp((double)amax, -22);
     int slot = 0;
     for (int dz = -1; dz <= 1; ++dz)
@@ -432,7 +436,7 @@ bool st_model(int Nx, int Ny, int Nz, const float* tab, float* coef, float* dd)
             const bool nd = jx == 0 || jx == Nx - 1 || jy == 0 || jy == Ny - 1 || jz == 0 || jz == Nz - 1;
             want = nd ? 0.0 : (double)sI[slot];
           }
-          if (std::fabs((double)s[slot] - want) > tol) return false;
+          if (!(std::fabs((double)s[slot] - want) <= tol)) return false;
         }
   }
   return true;

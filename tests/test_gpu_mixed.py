@@ -133,3 +133,16 @@ def test_mixed_falls_back_for_per_element_conductivity():
     assert res.status == 0 and res.inner_operator == "values"
     rel = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x))) / np.linalg.norm(bo)
     assert rel <= 1e-8
+
+
+def test_mixed_stencil_check_rejects_non_finite_values():
+    """A NaN in one interior entry fails the stencil check (the row's largest
+    magnitude is not finite), so the solver keeps the FP32 values copy."""
+    dims = (9, 8, 7)
+    A, b = M.build_system(*dims)
+    ro, cols, vals, bo = O.build_system(*dims)
+    r = ((4 * 9) + 4) * 10 + 5  # an interior node
+    A.packed_coefs[int(ro[r]) + 13] = float("nan")
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=3, tol=1e-8, tol_mode="relative", precision="mixed")
+    assert res.inner_operator == "values"
