@@ -385,7 +385,7 @@ def run_gpu(args):
 
     # batched uneven boxes and multi-RHS: measured after the headline system
     # is released, so their stores have the memory
-    batch = multi = adjoint = None
+    batch = multi = adjoint = small = None
     if rank == 0 and not args.no_cpu:
         ro, cols, vals, bh = host_system(A, b)
     else:
@@ -399,6 +399,8 @@ def run_gpu(args):
             multi = bench_multi(args, world, stream)
         if not args.no_adjoint:
             adjoint = bench_adjoint(args, world, stream)
+    if not args.no_small:
+        small = bench_small(args, world, stream)
 
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -429,6 +431,7 @@ def run_gpu(args):
             "batch": batch,
             "multi_rhs": multi,
             "adjoint": adjoint,
+            "small_30cubed": small,
             "spmv_f64_gbs": achieved,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                          "frac": achieved / peak, "traffic": traffic,
@@ -450,6 +453,50 @@ def run_gpu(args):
 
 
 SEED = 20261201  # S: adjoint conductivity S, target S + 1, FD elements S + 2, batch S + 3
+
+
+def bench_small(args, world, stream):
+    """The reference's CPU-sized case, 30^3 (29,791 rows): FP64 CG to 1e-8
+    relative (max 200 iterations) and to the reference's own stop (absolute
+    DBL_EPSILON, max 200), GPU time per solve by CUDA events, beside the
+    OpenMP CPU baseline on the same host arrays (rank 0)."""
+    import torch
+    import minife_gb300 as M
+    A, b = M.build_system(30, 30, 30)
+    out = {"system": "30^3", "rows": A.nrows, "nnz": A.nnz}
+    for name, tol, mode in (("rel_1e-8", TOL, "relative"), ("abs_eps", 2.220446049250313e-16, "absolute")):
+        x = torch.zeros_like(b)
+        for _ in range(args.warmup):
+            x.zero_()
+            r = M.cg_solve(A, b, x, max_iter=200, tol=tol, tol_mode=mode)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(args.steps):
+            x.zero_()
+            r = M.cg_solve(A, b, x, max_iter=200, tol=tol, tol_mode=mode)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        out[name] = {"gpu_s": max_over_ranks(world, e0.elapsed_time(e1) * 1e-3 / args.steps),
+                     "iterations": r.num_iters, "normr": r.normr}
+    if not args.no_cpu and (world == 1 or int(os.environ.get("RANK", "0")) == 0):
+        import ctypes
+        import numpy as np
+        from oracle import oracle as O
+        ro, cols, vals, bh = host_system(A, b)
+        L = O.cpubase()
+        nr = ctypes.c_double()
+        best = None
+        for _ in range(3):
+            xh = np.zeros(bh.size)
+            t0 = time.perf_counter()
+            L.cpub_cg_solve(bh.size, ro, cols, vals, bh, xh, 200, TOL, 1, ctypes.byref(nr))
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        out["cpu_port_rel_1e-8_s"] = best
+        out["cpu_cores"] = int(L.cpub_num_threads())
+    return out
 
 
 def bench_adjoint(args, world, stream):
@@ -670,6 +717,7 @@ def main():
     ap.add_argument("--no-mixed", action="store_true")
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 96-box batched solve")
+    ap.add_argument("--no-small", action="store_true", help="skip the 30^3 case")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint-gradient leg (128^3 gradient + FD spot check)")
     ap.add_argument("--adjoint-dims", type=int, default=128)
