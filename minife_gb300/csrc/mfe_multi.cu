@@ -1034,17 +1034,9 @@ size_t ell32_smem() { return (size_t)2 * kEStage * sizeof(float); }
 // any capture)
 mfe_status ell32_grid(mfe_ctx* ctx, int* grid)
 {
-  static int per_sm[64] = {};
-  const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
-  if (per_sm[dev] == 0) {
-    MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_ell32, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)ell32_smem()));
-    int n = 1;
-    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k_spmm_ell32, kEThreads,
-                                                                    ell32_smem()));
-    per_sm[dev] = std::max(n, 1);
-  }
-  *grid = ctx->sm_count * per_sm[dev];
+  MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmm_ell32, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)ell32_smem()));
+  *grid = resident_blocks(ctx, (const void*)k_spmm_ell32, kEThreads, ell32_smem());
   return MFE_OK;
 }
 

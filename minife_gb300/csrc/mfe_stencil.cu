@@ -493,18 +493,12 @@ mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* 
                              static_cast<const double*>(A64->vals), coef, ok);
 }
 
+// one wave of resident CTAs (the attribute is set before any graph capture)
 mfe_status stencil_grid(mfe_ctx* ctx, int* grid)
 {
-  static int per_sm[64] = {};
-  const int dev = ctx->device >= 0 && ctx->device < 64 ? ctx->device : 0;
-  if (per_sm[dev] == 0) {
-    MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmv_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)kS2Smem));
-    int b = 1;
-    MFE_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_spmv_stencil, kS2P / 2 + 32, kS2Smem));
-    per_sm[dev] = std::max(b, 1);
-  }
-  *grid = ctx->sm_count * per_sm[dev];
+  MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmv_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)kS2Smem));
+  *grid = resident_blocks(ctx, (const void*)k_spmv_stencil, kS2P / 2 + 32, kS2Smem);
   return MFE_OK;
 }
 
