@@ -42,6 +42,7 @@ struct MixState {
   double rr_at_update;  // rr right after the last reliable update
   double normr0, tol_abs, normr_true;
   double delta2;        // update when rr_new < delta2 * rr_at_update
+  double alpha_prev;    // alpha of the last update, whose x32 += alpha p is still pending
   int k;                // inner iterations done
   int max_iter;
   int since;            // iterations since the last reliable update
@@ -53,29 +54,45 @@ struct MixState {
   int status;           // 0 ok, MFE_BREAKDOWN
   int record;
   unsigned err;
-  int pad;
+  int x_pending;        // 1: x32 += alpha_prev p is due (done by the next p update or
+                        // the gated x update, whichever comes first)
   double* history;      // recursive normr per iteration (record)
 };
 
 constexpr int kT = 256;
 constexpr int kMaxPart = 8192;
 
-// p = r (first) or p = r + beta p, FP32 (cg_solve.hpp:153-161)
+// p = r (first) or p = r + beta p, FP32 (cg_solve.hpp:153-161).  The previous
+// iteration's x32 += alpha p (cg_solve.hpp:201-205) is done here, where the
+// old p is read anyway, unless the reliable update already folded it in:
+// the update kernel then reads only r and Ap.
 __global__ void __launch_bounds__(kT)
-    k_mx_p(int64_t n, const float* __restrict__ r, float* __restrict__ p, const MixState* st)
+    k_mx_p(int64_t n, const float* __restrict__ r, float* __restrict__ p, float* __restrict__ x32,
+           const MixState* st)
 {
   const bool first = st->first != 0;
+  const bool addx = !first && st->x_pending != 0;
   const float beta = (float)st->beta;
+  const float alpha = (float)st->alpha_prev;
   const int64_t stride = (int64_t)gridDim.x * kT;
   const int64_t n4 = n >> 2;
   const float4* r4 = reinterpret_cast<const float4*>(r);
   float4* p4 = reinterpret_cast<float4*>(p);
+  float4* x4 = reinterpret_cast<float4*>(x32);
   for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n4; i += stride) {
     const float4 rv = r4[i];
     float4 pv;
     if (first) pv = rv;
     else {
       pv = p4[i];
+      if (addx) {
+        float4 xv = x4[i];
+        xv.x = fmaf(alpha, pv.x, xv.x);
+        xv.y = fmaf(alpha, pv.y, xv.y);
+        xv.z = fmaf(alpha, pv.z, xv.z);
+        xv.w = fmaf(alpha, pv.w, xv.w);
+        x4[i] = xv;
+      }
       pv.x = fmaf(beta, pv.x, rv.x);
       pv.y = fmaf(beta, pv.y, rv.y);
       pv.z = fmaf(beta, pv.z, rv.z);
@@ -84,14 +101,17 @@ __global__ void __launch_bounds__(kT)
     p4[i] = pv;
   }
   const int64_t t = (n4 << 2) + (int64_t)blockIdx.x * kT + threadIdx.x;
-  if (blockIdx.x == 0 && t < n) p[t] = first ? r[t] : fmaf(beta, p[t], r[t]);
+  if (blockIdx.x == 0 && t < n) {
+    if (addx) x32[t] = fmaf(alpha, p[t], x32[t]);
+    p[t] = first ? r[t] : fmaf(beta, p[t], r[t]);
+  }
 }
 
-// x32 += alpha p, r -= alpha Ap, r.r in FP64 (cg_solve.hpp:201-213, :158);
-// the last block decides whether a reliable update is due.
+// r -= alpha Ap, r.r in FP64 (cg_solve.hpp:206-213, :158); x32 += alpha p is
+// left pending (k_mx_p / k_mx_xupdate).  The last block decides whether a
+// reliable update is due.
 __global__ void __launch_bounds__(kT)
-    k_mx_update(int64_t n, float* __restrict__ x32, float* __restrict__ r,
-                const float* __restrict__ p, const float* __restrict__ Ap, MixState* st,
+    k_mx_update(int64_t n, float* __restrict__ r, const float* __restrict__ Ap, MixState* st,
                 double* partials, unsigned* ticket)
 {
   __shared__ double red[32];
@@ -102,22 +122,15 @@ __global__ void __launch_bounds__(kT)
   double acc = 0.0;
   const int64_t stride = (int64_t)gridDim.x * kT;
   const int64_t n4 = n >> 2;
-  float4* x4 = reinterpret_cast<float4*>(x32);
   float4* r4 = reinterpret_cast<float4*>(r);
-  const float4* p4 = reinterpret_cast<const float4*>(p);
   const float4* a4 = reinterpret_cast<const float4*>(Ap);
   for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n4; i += stride) {
-    float4 xv = x4[i], rv = r4[i];
-    const float4 pv = p4[i], av = a4[i];
-    xv.x = fmaf(alpha, pv.x, xv.x);
-    xv.y = fmaf(alpha, pv.y, xv.y);
-    xv.z = fmaf(alpha, pv.z, xv.z);
-    xv.w = fmaf(alpha, pv.w, xv.w);
+    float4 rv = r4[i];
+    const float4 av = a4[i];
     rv.x = fmaf(-alpha, av.x, rv.x);
     rv.y = fmaf(-alpha, av.y, rv.y);
     rv.z = fmaf(-alpha, av.z, rv.z);
     rv.w = fmaf(-alpha, av.w, rv.w);
-    x4[i] = xv;
     r4[i] = rv;
     double d;
     d = f2d_exact(rv.x); acc = fma(d, d, acc);
@@ -127,7 +140,6 @@ __global__ void __launch_bounds__(kT)
   }
   const int64_t t = (n4 << 2) + (int64_t)blockIdx.x * kT + threadIdx.x;
   if (blockIdx.x == 0 && t < n) {
-    x32[t] = fmaf(alpha, p[t], x32[t]);
     const float rv = fmaf(-alpha, Ap[t], r[t]);
     r[t] = rv;
     const double d = f2d_exact(rv);
@@ -137,6 +149,8 @@ __global__ void __launch_bounds__(kT)
   double total;
   if (grid_reduce_last(bt, partials, ticket, red, &total) && threadIdx.x == 0) {
     st->rr_new = total;
+    st->alpha_prev = alpha;
+    st->x_pending = 1;
     st->k += 1;
     st->since += 1;
     st->first = 0;
@@ -151,15 +165,18 @@ __global__ void __launch_bounds__(kT)
 // reliable update, part 1 (gated): x += x32, x32 = 0
 // x32 may be x-padded (rows of Nx + pad entries; row i at i + (i / Nx) * pad)
 __global__ void __launch_bounds__(kT)
-    k_mx_xupdate(int64_t n, double* __restrict__ x, float* __restrict__ x32, const MixState* st,
-                 int Nx, int pad)
+    k_mx_xupdate(int64_t n, double* __restrict__ x, float* __restrict__ x32,
+                 const float* __restrict__ p, MixState* st, int Nx, int pad)
 {
   if (st->gate == 0) return;
+  // the pending x32 += alpha p folded in (the same FP32 FMA k_mx_p would do)
+  const float alpha = (float)st->alpha_prev;
   for (int64_t i = (int64_t)blockIdx.x * kT + threadIdx.x; i < n; i += (int64_t)gridDim.x * kT) {
     const int64_t j = pad ? i + (i / Nx) * pad : i;
-    x[i] += f2d_exact(x32[j]);
+    x[i] += f2d_exact(fmaf(alpha, p[j], x32[j]));
     x32[j] = 0.0f;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->x_pending = 0;  // read next by k_mx_p only
 }
 
 // bookkeeping (one thread): finish a reliable update, set the loop condition
@@ -239,7 +256,7 @@ mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, con
                        double* x, const MixBufs& B, cudaGraphConditionalHandle h, int in_graph)
 {
   const int64_t n = A64.nrows, nv = B.nv;
-  k_mx_p<<<grid_for(ctx, nv / 4, (const void*)k_mx_p), kT, 0, ctx->stream>>>(nv, B.r, B.p, B.st);
+  k_mx_p<<<grid_for(ctx, nv / 4, (const void*)k_mx_p), kT, 0, ctx->stream>>>(nv, B.r, B.p, B.x32, B.st);
   MFE_TRY(check_launch(ctx, "k_mx_p"));
   DotSink s1;
   s1.partials = B.partials;
@@ -249,11 +266,11 @@ mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, con
     MFE_TRY(launch_spmv_stencil(ctx, &A32, B.coef, B.p, B.Ap, &s1, B.stencil_grid, B.err));
   else
     MFE_TRY(launch_spmv(ctx, &A32, B.p, B.Ap, &s1, nullptr, nullptr));
-  k_mx_update<<<grid_for(ctx, nv / 4, (const void*)k_mx_update), kT, 0, ctx->stream>>>(nv, B.x32, B.r, B.p, B.Ap, B.st,
-                                                             B.partials + kMaxPart, B.tickets + 1);
+  k_mx_update<<<grid_for(ctx, nv / 4, (const void*)k_mx_update), kT, 0, ctx->stream>>>(
+      nv, B.r, B.Ap, B.st, B.partials + kMaxPart, B.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mx_update"));
   k_mx_xupdate<<<grid_for(ctx, n, (const void*)k_mx_xupdate), kT, 0, ctx->stream>>>(
-      n, x, B.x32, B.st, A64.box_nx + 1, B.pad);
+      n, x, B.x32, B.p, B.st, A64.box_nx + 1, B.pad);
   MFE_TRY(check_launch(ctx, "k_mx_xupdate"));
   DotSink s2;
   s2.partials = B.partials;
