@@ -67,7 +67,9 @@ struct BoxDesc {
 
 struct BoxSt {
   double rr, rr_new, pAp, alpha, beta, rr_true, rr_upd, normr0, normr, tol_abs;
+  double alpha_prev;  // mixed: alpha whose x32 += alpha p is still pending
   int open, gate, iters, since, brk;
+  int x_pending;      // mixed: 1 while x32 += alpha_prev p is due
   unsigned cnt_mv, cnt_vec;
 };
 
@@ -926,9 +928,12 @@ struct BxVecParams {
   int chunk;           // rows per chunk (multiple of 4)
 };
 
-// p = r + beta_b p (p = r on the first iteration)
+// p = r + beta_b p (p = r on the first iteration).  Mixed (V = float): the
+// box's previous x32 += alpha p is done here, where the old p is read anyway,
+// unless its reliable update already folded it in (k_bx_xupdate).
 template <typename V>
-__global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restrict__ r, V* __restrict__ p)
+__global__ void __launch_bounds__(kBxVT)
+    k_bx_p(BxVecParams Q, const V* __restrict__ r, V* __restrict__ p, float* __restrict__ x32)
 {
   const int cnt = *Q.count;
   if (cnt == 0) return;
@@ -943,6 +948,8 @@ __global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restri
     const int64_t g0 = d.row_base + (int64_t)lc * Q.chunk;
     const int len = min(Q.chunk, d.n - lc * Q.chunk);
     const V beta = (V)Q.st[b].beta;
+    const bool addx = sizeof(V) == 4 && !first && Q.st[b].x_pending != 0;
+    const float alpha = (float)Q.st[b].alpha_prev;
     using VV = typename BxVec16<V>::type;
     constexpr int VW = BxVec16<V>::n;
     const VV* r4 = reinterpret_cast<const VV*>(r + g0);
@@ -952,6 +959,18 @@ __global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restri
       VV pv = rv;
       if (!first) {
         pv = p4[k];
+        if constexpr (sizeof(V) == 4) {
+          if (addx) {
+            float4* x4 = reinterpret_cast<float4*>(x32 + g0);
+            float4 xv = x4[k];
+            const float4 po = reinterpret_cast<const float4&>(pv);
+            xv.x = fmaf(alpha, po.x, xv.x);
+            xv.y = fmaf(alpha, po.y, xv.y);
+            xv.z = fmaf(alpha, po.z, xv.z);
+            xv.w = fmaf(alpha, po.w, xv.w);
+            x4[k] = xv;
+          }
+        }
 #pragma unroll
         for (int c = 0; c < VW; ++c)
           bx_comp<V>(pv, c) = fma(beta, bx_comp<V>(pv, c), bx_comp<V>(const_cast<VV&>(rv), c));
@@ -960,6 +979,9 @@ __global__ void __launch_bounds__(kBxVT) k_bx_p(BxVecParams Q, const V* __restri
     }
     for (int k = len / VW * VW + threadIdx.x; k < len; k += kBxVT) {
       const int64_t g = g0 + k;
+      if constexpr (sizeof(V) == 4) {
+        if (addx) x32[g] = fmaf(alpha, (float)p[g], x32[g]);
+      }
       p[g] = first ? r[g] : fma(beta, p[g], r[g]);
     }
   }
@@ -994,12 +1016,17 @@ __global__ void __launch_bounds__(kBxVT)
     VV* r4 = reinterpret_cast<VV*>(r + g0);
     const VV* p4 = reinterpret_cast<const VV*>(p + g0);
     const VV* a4 = reinterpret_cast<const VV*>(Ap + g0);
+    // mixed (V = float): x32 += alpha p is left pending (k_bx_p / k_bx_xupdate)
+    constexpr bool kX = sizeof(V) == 8;
     for (int k = threadIdx.x; k < len / VW; k += kBxVT) {
-      VV xv = x4[k], rv = r4[k];
-      VV pv = p4[k], av = a4[k];
+      VV xv, rv = r4[k], pv, av = a4[k];
+      if constexpr (kX) {
+        xv = x4[k];
+        pv = p4[k];
+      }
 #pragma unroll
       for (int c = 0; c < VW; ++c) {
-        bx_comp<V>(xv, c) = fma(alpha, bx_comp<V>(pv, c), bx_comp<V>(xv, c));
+        if constexpr (kX) bx_comp<V>(xv, c) = fma(alpha, bx_comp<V>(pv, c), bx_comp<V>(xv, c));
         const V rn = fma(-alpha, bx_comp<V>(av, c), bx_comp<V>(rv, c));
         bx_comp<V>(rv, c) = rn;
         if constexpr (sizeof(V) == 4)
@@ -1007,12 +1034,12 @@ __global__ void __launch_bounds__(kBxVT)
         else
           acc = fma(rn, rn, acc);
       }
-      x4[k] = xv;
+      if constexpr (kX) x4[k] = xv;
       r4[k] = rv;
     }
     for (int k = len / VW * VW + threadIdx.x; k < len; k += kBxVT) {
       const int64_t g = g0 + k;
-      x[g] = fma(alpha, p[g], x[g]);
+      if constexpr (kX) x[g] = fma(alpha, p[g], x[g]);
       const V rn = fma(-alpha, Ap[g], r[g]);
       r[g] = rn;
       if constexpr (sizeof(V) == 4)
@@ -1035,15 +1062,21 @@ __global__ void __launch_bounds__(kBxVT)
       if (threadIdx.x == 0) {
         Q.st[b].rr_new = s;
         Q.st[b].cnt_vec = 0u;
+        if constexpr (!kX) {
+          Q.st[b].alpha_prev = Q.st[b].alpha;
+          Q.st[b].x_pending = 1;
+        }
       }
     }
     __syncthreads();
   }
 }
 
-// x += x32, x32 = 0 over the chunks of the listed (gated) boxes
+// x += x32 + alpha p (the pending update, the same FP32 FMA k_bx_p would do),
+// x32 = 0 over the chunks of the listed (gated) boxes
 __global__ void __launch_bounds__(kBxVT)
-    k_bx_xupdate(BxVecParams Q, double* __restrict__ x, float* __restrict__ x32)
+    k_bx_xupdate(BxVecParams Q, double* __restrict__ x, float* __restrict__ x32,
+                 const float* __restrict__ p)
 {
   const int cnt = *Q.count;
   if (cnt == 0) return;
@@ -1056,10 +1089,12 @@ __global__ void __launch_bounds__(kBxVT)
     const int lc = c - __ldg(&Q.cpre[q]);
     const int64_t g0 = d.row_base + (int64_t)lc * Q.chunk;
     const int len = min(Q.chunk, d.n - lc * Q.chunk);
+    const float alpha = (float)Q.st[b].alpha_prev;
     for (int k = threadIdx.x; k < len; k += kBxVT) {
-      x[g0 + k] += f2d_exact(x32[g0 + k]);
+      x[g0 + k] += f2d_exact(fmaf(alpha, p[g0 + k], x32[g0 + k]));
       x32[g0 + k] = 0.0f;
     }
+    if (lc == 0 && threadIdx.x == 0) Q.st[b].x_pending = 0;  // read next by k_bx_p only
   }
 }
 
@@ -1520,7 +1555,8 @@ mfe_status bx_iter_mixed(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle 
   float* r = static_cast<float*>(bt->r);
   float* p = static_cast<float*>(bt->p);
   float* Ap = static_cast<float*>(bt->Ap);
-  k_bx_p<float><<<bx_vgrid(ctx, (const void*)k_bx_p<float>), kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
+  k_bx_p<float><<<bx_vgrid(ctx, (const void*)k_bx_p<float>), kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p,
+                                                                                          bt->x32);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
   MFE_TRY(bx_spmv32(ctx, R, R.open, p, Ap));
   k_bx_update<float><<<bx_vgrid(ctx, (const void*)k_bx_update<float>), kBxVT, 0, ctx->stream>>>(
@@ -1529,7 +1565,7 @@ mfe_status bx_iter_mixed(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle 
   k_bx_decide<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.gate);
   MFE_TRY(check_launch(ctx, "k_bx_decide"));
   k_bx_xupdate<<<bx_vgrid(ctx, (const void*)k_bx_xupdate), kBxVT, 0, ctx->stream>>>(
-      bx_vec(R, R.gate), bt->x, bt->x32);
+      bx_vec(R, R.gate), bt->x, bt->x32, p);
   MFE_TRY(check_launch(ctx, "k_bx_xupdate"));
   MFE_TRY(bx_spmv64<BX_RESID>(ctx, R, R.gate, bt->x, nullptr, bt->b, r));
   k_bx_after<<<1, 1024, 0, ctx->stream>>>(bt->boxes, bt->st, bt->ctl, R.open, h, in_graph);
@@ -1542,7 +1578,8 @@ mfe_status bx_iter_f64(mfe_ctx* ctx, const Run& R, cudaGraphConditionalHandle h,
   double* r = static_cast<double*>(bt->r);
   double* p = static_cast<double*>(bt->p);
   double* Ap = static_cast<double*>(bt->Ap);
-  k_bx_p<double><<<bx_vgrid(ctx, (const void*)k_bx_p<double>), kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p);
+  k_bx_p<double><<<bx_vgrid(ctx, (const void*)k_bx_p<double>), kBxVT, 0, ctx->stream>>>(bx_vec(R, R.open), r, p,
+                                                                                            nullptr);
   MFE_TRY(check_launch(ctx, "k_bx_p"));
   MFE_TRY(bx_spmv64<BX_DOT>(ctx, R, R.open, p, Ap, nullptr, nullptr));
   k_bx_update<double><<<bx_vgrid(ctx, (const void*)k_bx_update<double>), kBxVT, 0, ctx->stream>>>(
