@@ -77,6 +77,7 @@ struct MultiState {
   int brk[kMaxRhs];    // p.Ap <= 0 met (the right-hand side stops alone)
   int nrhs, k, max_iter, since, refine_k, gate, cont, first, updates, status, tol_mode;
   unsigned err;
+  int x_pending;  // mixed: x32 += alpha p of the last update not yet done
   double delta2;
 };
 
@@ -684,18 +685,25 @@ __device__ __forceinline__ V& comp(typename Vec16<V>::type& v, int c)
 
 template <typename V>
 __global__ void __launch_bounds__(kVT)
-    k_mr_p(int64_t ntot, int nrhs, const V* __restrict__ r, V* __restrict__ p, const MultiState* st)
+    k_mr_p(int64_t ntot, int nrhs, const V* __restrict__ r, V* __restrict__ p, float* __restrict__ x32,
+           const MultiState* st)
 {
   using VV = typename Vec16<V>::type;
   constexpr int VW = Vec16<V>::n;
   const int64_t g0 = (int64_t)blockIdx.x * kVT + threadIdx.x;
   const int64_t stride = (int64_t)gridDim.x * kVT;
   const bool first = st->first != 0;
-  V beta[VW];
+  // mixed (V = float): the last update's x32 += alpha p, done here where the
+  // old p is read anyway (st->alpha still holds that update's alphas), unless
+  // the reliable update already folded it in
+  constexpr bool kX = sizeof(V) == 4;
+  const bool addx = kX && !first && st->x_pending != 0;
+  V beta[VW], alpha[VW];
 #pragma unroll
   for (int c = 0; c < VW; ++c) {
     const int j = (VW * threadIdx.x + c) % nrhs;
     beta[c] = st->done[j] ? V(0) : (V)st->beta[j];
+    alpha[c] = (V)st->alpha[j];
   }
   const int64_t nvec = ntot / VW;
   const VV* r4 = reinterpret_cast<const VV*>(r);
@@ -704,6 +712,15 @@ __global__ void __launch_bounds__(kVT)
     const VV rv = r4[v];
     VV pv = first ? rv : p4[v];
     if (!first) {
+      if constexpr (kX) {
+        if (addx) {
+          VV* x4 = reinterpret_cast<VV*>(x32);
+          VV xv = x4[v];
+#pragma unroll
+          for (int c = 0; c < VW; ++c) comp<V>(xv, c) = fma(alpha[c], comp<V>(pv, c), comp<V>(xv, c));
+          x4[v] = xv;
+        }
+      }
 #pragma unroll
       for (int c = 0; c < VW; ++c) comp<V>(pv, c) = fma(beta[c], comp<V>(pv, c), comp<V>(const_cast<VV&>(rv), c));
     }
@@ -713,7 +730,11 @@ __global__ void __launch_bounds__(kVT)
 #pragma unroll
     for (int c = 0; c < VW; ++c) {
       const int64_t e = nvec * VW + c;
-      if (e < ntot) p[e] = first ? r[e] : fma(beta[c], p[e], r[e]);
+      if (e >= ntot) continue;
+      if constexpr (kX) {
+        if (addx) x32[e] = fma(alpha[c], p[e], x32[e]);
+      }
+      p[e] = first ? r[e] : fma(beta[c], p[e], r[e]);
     }
   }
 }
@@ -747,12 +768,17 @@ __global__ void __launch_bounds__(kVT)
   VV* r4 = reinterpret_cast<VV*>(r);
   const VV* p4 = reinterpret_cast<const VV*>(p);
   const VV* a4 = reinterpret_cast<const VV*>(Ap);
+  // mixed (V = float): x32 += alpha p is left pending (k_mr_p / k_mr_xupdate)
+  constexpr bool kX = sizeof(V) == 8;
   for (int64_t v = g0; v < nvec; v += stride) {
-    VV xv = x4[v], rv = r4[v];
-    VV pv = p4[v], av = a4[v];
+    VV xv, rv = r4[v], pv, av = a4[v];
+    if constexpr (kX) {
+      xv = x4[v];
+      pv = p4[v];
+    }
 #pragma unroll
     for (int c = 0; c < VW; ++c) {
-      comp<V>(xv, c) = fma(alpha[c], comp<V>(pv, c), comp<V>(xv, c));
+      if constexpr (kX) comp<V>(xv, c) = fma(alpha[c], comp<V>(pv, c), comp<V>(xv, c));
       const V rn = fma(-alpha[c], comp<V>(av, c), comp<V>(rv, c));
       comp<V>(rv, c) = rn;
       if constexpr (sizeof(V) == 4)
@@ -760,7 +786,7 @@ __global__ void __launch_bounds__(kVT)
       else
         acc[c] = fma(rn, rn, acc[c]);
     }
-    x4[v] = xv;
+    if constexpr (kX) x4[v] = xv;
     r4[v] = rv;
   }
   if (g0 == nvec % stride) {
@@ -768,7 +794,7 @@ __global__ void __launch_bounds__(kVT)
     for (int c = 0; c < VW; ++c) {
       const int64_t e = nvec * VW + c;
       if (e >= ntot) continue;
-      x[e] = fma(alpha[c], p[e], x[e]);
+      if constexpr (kX) x[e] = fma(alpha[c], p[e], x[e]);
       const V rn = fma(-alpha[c], Ap[e], r[e]);
       r[e] = rn;
       if constexpr (sizeof(V) == 4)
@@ -791,13 +817,17 @@ __global__ void __launch_bounds__(kVT)
 }
 
 __global__ void __launch_bounds__(kVT)
-    k_mr_xupdate(int64_t ntot, double* __restrict__ x, float* __restrict__ x32, const MultiState* st)
+    k_mr_xupdate(int64_t ntot, int nrhs, double* __restrict__ x, float* __restrict__ x32,
+                 const float* __restrict__ p, MultiState* st)
 {
   if (st->gate == 0) return;
+  // the pending x32 += alpha p folded in (the same FP32 FMA k_mr_p would do)
   for (int64_t i = (int64_t)blockIdx.x * kVT + threadIdx.x; i < ntot; i += (int64_t)gridDim.x * kVT) {
-    x[i] += f2d_exact(x32[i]);
+    const float alpha = (float)st->alpha[i % nrhs];
+    x[i] += f2d_exact(fmaf(alpha, p[i], x32[i]));
     x32[i] = 0.0f;
   }
+  if (blockIdx.x == 0 && threadIdx.x == 0) st->x_pending = 0;  // read next by k_mr_p only
 }
 
 // Mixed solver, one warp, after the update kernel: decide whether this
@@ -826,6 +856,7 @@ __global__ void k_mr_decide(MultiState* st)
     st->k += 1;
     st->since += 1;
     st->first = 0;
+    st->x_pending = 1;  // this iteration's x32 += alpha p (k_mr_p next, or k_mr_xupdate)
     st->gate = all_ready || any_brk || st->since >= st->refine_k || st->k >= st->max_iter;
   }
 }
@@ -1072,7 +1103,7 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
                             cudaGraphConditionalHandle h, int in_graph)
 {
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
-  k_mr_p<float><<<vgrid(ctx, ntot, k_mr_p<float>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
+  k_mr_p<float><<<vgrid(ctx, ntot, k_mr_p<float>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.x32, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
   if (W.ell) {
     Ell32Params E;
@@ -1098,7 +1129,7 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
   MFE_TRY(check_launch(ctx, "k_mr_update"));
   k_mr_decide<<<1, 32, 0, ctx->stream>>>(W.st);
   MFE_TRY(check_launch(ctx, "k_mr_decide"));
-  k_mr_xupdate<<<vgrid(ctx, ntot, k_mr_xupdate), kVT, 0, ctx->stream>>>(ntot, X, W.x32, W.st);
+  k_mr_xupdate<<<vgrid(ctx, ntot, k_mr_xupdate), kVT, 0, ctx->stream>>>(ntot, nrhs, X, W.x32, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_xupdate"));
   MFE_TRY((launch_spmm_t<double, MM_RESID, float>(ctx, &A64, nrhs, X, nullptr, B, W.r, W.partials,
                                                    W.tickets, W.st->rr_true, &W.st->gate, W.err)));
@@ -1111,7 +1142,8 @@ mfe_status multi_iter_f64(mfe_ctx* ctx, const mfe_csr& A64, int nrhs, double* X,
                           const MultiBufs<double>& W, cudaGraphConditionalHandle h, int in_graph)
 {
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
-  k_mr_p<double><<<vgrid(ctx, ntot, k_mr_p<double>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.st);
+  k_mr_p<double><<<vgrid(ctx, ntot, k_mr_p<double>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, nullptr,
+                                                                             W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
   MFE_TRY((launch_spmm_t<double, MM_DOT, double>(ctx, &A64, nrhs, W.p, W.Ap, nullptr, nullptr,
                                                   W.partials, W.tickets, W.st->pAp, nullptr, W.err,
