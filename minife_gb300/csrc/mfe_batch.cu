@@ -650,9 +650,9 @@ __global__ void __launch_bounds__(kSP + 32, 2) k_bx_stencil(const __grid_constan
 // Two adjacent plane positions per consumer thread (c - c0 even, c + 1) over
 // 512-position tiles, for batches whose boxes all have mirror-symmetric
 // stencils: a coefficient then depends only on (|dz|, |dy|, |dx|), so a box
-// needs 8 weights in registers (w[4|dz| + 2|dy| + |dx|]) and a line of the
-// window x[c-1 .. c+2] gives row c  w0 x[c] + w1 (x[c-1] + x[c+1]) and row
-// c + 1  w0 x[c+1] + w1 (x[c] + x[c+2]).  Both y neighbours of a position are
+// needs 8 weights in registers (w[4|dz| + 2|dy| + |dx|]); each plane of the
+// window x[c-1 .. c+2] is reduced once to its per-class sums for the two
+// rows (st_sep_reduce) and a row takes 8 FMAs (st_sep_rows).  Both y neighbours of a position are
 // at -Nx / +Nx in the flattened plane, so a pair needs the same three lines;
 // a pair that straddles two x lines is two Dirichlet rows (ix = Nx-1 and 0),
 // whose results are replaced by dd * x.  Natural layout: four scalar loads
@@ -674,29 +674,6 @@ struct BxPlane2 {
   float v[12];  // line j: x[c-1], x[c], x[c+1], x[c+2]
   float c0, c1;  // unmasked centres
 };
-
-__device__ __forceinline__ void bx_sum2(const float* w, const BxPlane2& A, const BxPlane2& B,
-                                        const BxPlane2& C, bool HA, bool HC, float& s0, float& s1)
-{
-  float a[4] = {0.0f, 0.0f, 0.0f, 0.0f}, b[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
-  for (int pz = 0; pz < 3; ++pz) {
-    const BxPlane2& P = pz == 0 ? A : (pz == 1 ? B : C);
-    if ((pz == 0 && !HA) || (pz == 2 && !HC)) continue;
-#pragma unroll
-    for (int j = 0; j < 3; ++j) {
-      const int cls = 4 * (pz != 1) + 2 * (j != 1);
-      const float w0 = w[cls], w1 = w[cls + 1];
-      const float* v = P.v + 4 * j;
-      a[2 * (j & 1)] = fmaf(w0, v[1], a[2 * (j & 1)]);
-      a[2 * (j & 1) + 1] = fmaf(w1, v[0] + v[2], a[2 * (j & 1) + 1]);
-      b[2 * (j & 1)] = fmaf(w0, v[2], b[2 * (j & 1)]);
-      b[2 * (j & 1) + 1] = fmaf(w1, v[1] + v[3], b[2 * (j & 1) + 1]);
-    }
-  }
-  s0 = (a[0] + a[1]) + (a[2] + a[3]);
-  s1 = (b[0] + b[1]) + (b[2] + b[3]);
-}
 
 __global__ void __launch_bounds__(kB2P / 2 + 32, 2) k_bx_stencil2(const __grid_constant__ BxStParams P)
 {
@@ -770,8 +747,8 @@ __global__ void __launch_bounds__(kB2P / 2 + 32, 2) k_bx_stencil2(const __grid_c
     int it = 0, q = -1, b = -1, A = 0, E = 0;
     BoxDesc d{};
     DFAcc facc;
-    float w[8], dd = 0.0f;
-    BxPlane2 W0, W1, W2;
+    float w[8] = {}, dd = 0.0f;
+    StSep2 W0, W1, W2;
     int c = 0, c0 = 0, cc = 0;
     bool act0 = false, act1 = false, sp0 = false, sp1 = false;
     bool m1 = false, m2 = false, m3 = false, myl = false, myh = false, wm = false;
@@ -787,7 +764,8 @@ __global__ void __launch_bounds__(kB2P / 2 + 32, 2) k_bx_stencil2(const __grid_c
       ++it;
     };
     // plane z (the slot's plane pl) around positions cc, cc + 1 into W
-    auto load_plane = [&](int pl, int z, BxPlane2& W) {
+    auto load_plane = [&](int pl, int z, StSep2& Wo) {
+      BxPlane2 W;
       const unsigned zb0 = (unsigned)z * (unsigned)d.NxNy + (unsigned)(c0 - 1);
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
@@ -809,27 +787,39 @@ __global__ void __launch_bounds__(kB2P / 2 + 32, 2) k_bx_stencil2(const __grid_c
         if (myl) W.v[0] = W.v[1] = W.v[2] = W.v[3] = 0.0f;
         if (myh) W.v[8] = W.v[9] = W.v[10] = W.v[11] = 0.0f;
       }
+      st_sep_reduce(W.v, W.c0, W.c1, Wo);
     };
-    auto finish = [&](int z, float s0, float s1, const BxPlane2& B) {
+    // p.Ap: the pair's two products summed in FP32, the running sum in
+    // double-float (act1 implies act0)
+    auto finish = [&](int z, float s0, float s1, const StSep2& B) {
       s0 = sp0 ? dd * B.c0 : s0;
       s1 = sp1 ? dd * B.c1 : s1;
       const int64_t g = d.row_base + (int64_t)z * d.NxNy + c;
       if (act0) {
         P.y[g] = s0;
-        facc.add_product(s0, B.c0);
-      }
-      if (act1) {
-        P.y[g + 1] = s1;
-        facc.add_product(s1, B.c1);
+        float pr = s0 * B.c0;
+        if (act1) {
+          P.y[g + 1] = s1;
+          pr = fmaf(s1, B.c1, pr);
+        }
+        facc.add(pr);
       }
     };
-    auto row = [&](int z, const BxPlane2& A_, const BxPlane2& B, const BxPlane2& C) {
+    const auto wf = [&](int k) { return w[k]; };
+    auto row = [&](int z, const StSep2& A_, const StSep2& B, const StSep2& C) {
       float s0, s1;
-      if (z == 0 || z == d.Nz - 1) {  // the same for the whole warp
+      // z cases are the same for the whole warp
+      if (z >= 2 && z <= d.Nz - 3) {
+        st_sep_rows<true, true>(wf, A_, B, C, s0, s1);
+      } else if (z == 0 || z == d.Nz - 1) {
         s0 = dd * B.c0;
         s1 = dd * B.c1;
+      } else if (z == 1 && z == d.Nz - 2) {
+        st_sep_rows<false, false>(wf, A_, B, C, s0, s1);
+      } else if (z == 1) {
+        st_sep_rows<false, true>(wf, A_, B, C, s0, s1);
       } else {
-        bx_sum2(w, A_, B, C, z != 1, z != d.Nz - 2, s0, s1);
+        st_sep_rows<true, false>(wf, A_, B, C, s0, s1);
       }
       finish(z, s0, s1, B);
     };
@@ -1427,27 +1417,6 @@ mfe_status bx_stencil_grid(mfe_ctx* ctx, bool pair, int* grid)
   return MFE_OK;
 }
 
-// the 8 mirror-class weights of a verified stencil (coef[0..26] slot order
-// (dz, dy, dx), coef[27] = dd): weight 4|dz| + 2|dy| + |dx| is the entry at
-// (|dz|, |dy|, |dx|); every entry must lie within 2^-22 max|coef| of its
-// class weight (so the operator stays within 2^-21 of every row of A)
-bool bx_mirror_classes(const float* coef, float* w8)
-{
-  float amax = 0.0f;
-  for (int k = 0; k < 27; ++k) amax = std::max(amax, std::fabs(coef[k]));
-  const double tol = std::ldexp((double)amax, -22);
-  for (int c = 0; c < 8; ++c) {
-    const int az = c >> 2, ay = (c >> 1) & 1, ax = c & 1;
-    w8[c] = coef[(az + 1) * 9 + (ay + 1) * 3 + (ax + 1)];
-  }
-  for (int k = 0; k < 27; ++k) {
-    const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
-    const int c = 4 * (dz != 0) + 2 * (dy != 0) + (dx != 0);
-    if (!(std::fabs((double)coef[k] - (double)w8[c]) <= tol)) return false;
-  }
-  return true;
-}
-
 // every box checked once per batch (its values never change after assembly)
 mfe_status bx_stencil_prepare(mfe_ctx* ctx, mfe_batch* bt)
 {
@@ -1467,7 +1436,7 @@ mfe_status bx_stencil_prepare(mfe_ctx* ctx, mfe_batch* bt)
     std::vector<float> h8(hc.size(), 0.0f);
     bool sym = true;
     for (int i = 0; i < bt->nbox && sym; ++i) {
-      sym = bx_mirror_classes(&hc[(size_t)i * 28], &h8[(size_t)i * 28]);
+      sym = stencil_mirror_classes(&hc[(size_t)i * 28], &h8[(size_t)i * 28]);
       h8[(size_t)i * 28 + 27] = hc[(size_t)i * 28 + 27];
     }
     if (sym) {

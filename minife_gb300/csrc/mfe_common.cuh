@@ -217,6 +217,15 @@ struct DFAcc {
     hi = t;
     lo = __fadd_rn(lo, __fadd_rn(err, pe));
   }
+  // an FP32 term (already rounded) added with TwoSum
+  __device__ __forceinline__ void add(float v)
+  {
+    const float t = __fadd_rn(hi, v);
+    const float bp = __fsub_rn(t, hi);
+    const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(v, bp));
+    hi = t;
+    lo = __fadd_rn(lo, err);
+  }
   __device__ __forceinline__ double value() const { return f2d_exact(hi) + f2d_exact(lo); }
 };
 

@@ -113,8 +113,15 @@ mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* 
 // the same for one box of Nx x Ny x Nz nodes whose CSR values start at vals
 mfe_status stencil_prepare_box(mfe_ctx* ctx, int Nx, int Ny, int Nz, const double* vals, float* coef,
                                bool* ok);
-mfe_status stencil_grid(mfe_ctx* ctx, int* grid);
-// y = S x and x.y into sink->out, both x-padded (y's padding entries are
+// the 8 mirror-class weights of a verified stencil (coef[0..26] slot order
+// (dz, dy, dx)): weight 4|dz| + 2|dy| + |dx| is the entry at (|dz|, |dy|,
+// |dx|); true when every entry lies within 2^-22 max|coef| of its class
+// weight (the operator then stays within 2^-21 of every row of A)
+bool stencil_mirror_classes(const float* coef, float* w8);
+// resident CTAs (one wave) of the stencil SpMV variant coef selects
+mfe_status stencil_grid(mfe_ctx* ctx, const float* coef, int* grid);
+// y = S x and x.y into sink->out (the eight class weights when the stencil
+// is mirror-symmetric, else the 27 coefficients), both x-padded (y's padding entries are
 // written as zeros); x has stencil_ghost rows of zeros on both sides
 mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef, const float* x,
                                float* y, const DotSink* sink, int grid, unsigned* err);

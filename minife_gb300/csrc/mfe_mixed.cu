@@ -107,9 +107,11 @@ __global__ void __launch_bounds__(kT)
   }
 }
 
-// r -= alpha Ap, r.r in FP64 (cg_solve.hpp:206-213, :158); x32 += alpha p is
-// left pending (k_mx_p / k_mx_xupdate).  The last block decides whether a
-// reliable update is due.
+// r -= alpha Ap, r.r (cg_solve.hpp:206-213, :158) accumulated in double-float
+// per thread (FP32 operations: one FP64 FMA per row would make the kernel
+// FP64-bound on GB300) and summed in FP64 across threads and blocks; x32 +=
+// alpha p is left pending (k_mx_p / k_mx_xupdate).  The last block decides
+// whether a reliable update is due.
 __global__ void __launch_bounds__(kT)
     k_mx_update(int64_t n, float* __restrict__ r, const float* __restrict__ Ap, MixState* st,
                 double* partials, unsigned* ticket)
@@ -119,7 +121,7 @@ __global__ void __launch_bounds__(kT)
   if (threadIdx.x == 0) s_alpha = st->pAp > 0.0 ? (float)(st->rr / st->pAp) : 0.0f;
   __syncthreads();
   const float alpha = s_alpha;
-  double acc = 0.0;
+  DFAcc acc;
   const int64_t stride = (int64_t)gridDim.x * kT;
   const int64_t n4 = n >> 2;
   float4* r4 = reinterpret_cast<float4*>(r);
@@ -132,20 +134,18 @@ __global__ void __launch_bounds__(kT)
     rv.z = fmaf(-alpha, av.z, rv.z);
     rv.w = fmaf(-alpha, av.w, rv.w);
     r4[i] = rv;
-    double d;
-    d = f2d_exact(rv.x); acc = fma(d, d, acc);
-    d = f2d_exact(rv.y); acc = fma(d, d, acc);
-    d = f2d_exact(rv.z); acc = fma(d, d, acc);
-    d = f2d_exact(rv.w); acc = fma(d, d, acc);
+    acc.add_product(rv.x, rv.x);
+    acc.add_product(rv.y, rv.y);
+    acc.add_product(rv.z, rv.z);
+    acc.add_product(rv.w, rv.w);
   }
   const int64_t t = (n4 << 2) + (int64_t)blockIdx.x * kT + threadIdx.x;
   if (blockIdx.x == 0 && t < n) {
     const float rv = fmaf(-alpha, Ap[t], r[t]);
     r[t] = rv;
-    const double d = f2d_exact(rv);
-    acc = fma(d, d, acc);
+    acc.add_product(rv, rv);
   }
-  const double bt = block_sum(acc, red);
+  const double bt = block_sum(acc.value(), red);
   double total;
   if (grid_reduce_last(bt, partials, ticket, red, &total) && threadIdx.x == 0) {
     st->rr_new = total;
@@ -343,7 +343,7 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
   B.p = pbase ? pbase + ghost : nullptr;
   if (use_stencil) {
     B.stencil = true;
-    MFE_TRY(stencil_grid(ctx, &B.stencil_grid));
+    MFE_TRY(stencil_grid(ctx, B.coef, &B.stencil_grid));
   }
   B.Ap = static_cast<float*>(workspace(ctx, "mixed.Ap", vb));
   B.x32 = static_cast<float*>(workspace(ctx, "mixed.x32", vb));

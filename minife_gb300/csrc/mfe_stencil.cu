@@ -32,15 +32,20 @@
 // slots (three planes per slot) with bulk copies, from a vector with ghost
 // zones of zero rows around it.  Each consumer keeps planes z-1, z, z+1 of
 // its two rows (x[c-1 .. c+2] of three lines, from three 8-byte loads per
-// line) in registers, so a row costs 4.5 shared-memory loads and 27 FMAs
-// whose coefficients are kernel parameters (constant-bank operands: no
-// registers).  Lanes next to a Dirichlet node zero the masked neighbours as
+// line) in registers, so a row costs 4.5 shared-memory loads.  A
+// mirror-symmetric stencil (every miniFE box's, checked to 2^-22) is applied
+// with its eight class weights: each plane is reduced once to the sums the
+// two rows need per class and a row takes 8 FMAs (st_sep_rows); any other
+// verified stencil takes its 27 coefficients.  Weights and coefficients are
+// kernel parameters (constant-bank operands: no registers).  Lanes next to a
+// Dirichlet node zero the masked neighbours as
 // they load them; Dirichlet planes and the planes next to them take
 // warp-uniform branches.  The (plane tile, z) steps are split evenly over
 // one wave of CTAs.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 
 #include "mfe_box.cuh"
 #include "mfe_common.cuh"
@@ -159,6 +164,7 @@ __global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
 struct StParams {
   int Nx, Ny, Nz, Nxp, NP, ntile;  // NP = Ny * Nxp, the padded plane
   float coef[27];  // interior stencil, slot order (dz, dy, dx)
+  float w8[8];     // its mirror-class weights, class 4|dz| + 2|dy| + |dx|
   float dd;        // diagonal of the Dirichlet rows
   const float* __restrict__ x;  // ghost zones around it
   float* __restrict__ y;
@@ -221,8 +227,14 @@ __device__ __forceinline__ void st_sum2(CF cf, const StPlane2& A, const StPlane2
   s1 = ((b[0] + b[1]) + (b[2] + b[3])) + (b[4] + b[5]);
 }
 
-__global__ void __launch_bounds__(kS2P / 2 + 32, 2) k_spmv_stencil(const __grid_constant__ StParams P)
+// kSep: the stencil is mirror-symmetric and the rows use the eight class
+// weights over reduced planes (st_sep_rows), at 3 CTAs per SM; otherwise
+// the 27 coefficients at 2 CTAs per SM.
+template <bool kSep>
+__global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
+    k_spmv_stencil(const __grid_constant__ StParams P)
 {
+  using Pl = typename std::conditional<kSep, StSep2, StPlane2>::type;
   extern __shared__ __align__(128) unsigned char st2_smem_raw[];
   float* const ring = reinterpret_cast<float*>(st2_smem_raw);
   __shared__ uint64_t full[kSS], empty[kSS];
@@ -273,7 +285,7 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, 2) k_spmv_stencil(const __grid_
     const int lr = (warp - 1) * 32 + lane;
     bool ok = true;
     int it = 0;
-    StPlane2 W0, W1, W2;
+    Pl W0, W1, W2;
     int c = 0, lane_off = 0;
     bool active = false, sp0 = false, sp1 = false, m1 = false, m2 = false, m3 = false, myl = false,
          myh = false, wm = false;
@@ -290,7 +302,8 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, 2) k_spmv_stencil(const __grid_
       ++it;
     };
     // the slot's plane pl around positions c, c + 1 into W (sx points at x[c-2])
-    auto load_plane = [&](int pl, StPlane2& W) {
+    auto load_plane = [&](int pl, Pl& Wo) {
+      StPlane2 W;
 #pragma unroll
       for (int j = 0; j < 3; ++j) {
         const float* seg = sx + (pl * 3 + j) * kS2Cap;
@@ -313,28 +326,43 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, 2) k_spmv_stencil(const __grid_
         if (myl) W.v[0] = W.v[1] = W.v[2] = W.v[3] = 0.0f;
         if (myh) W.v[8] = W.v[9] = W.v[10] = W.v[11] = 0.0f;
       }
+      if constexpr (kSep)
+        st_sep_reduce(W.v, W.c0, W.c1, Wo);
+      else
+        Wo = W;
     };
-    auto finish = [&](int z, float s0, float s1, const StPlane2& B) {
+    // p.Ap: the pair's two products summed in FP32, the running sum in
+    // double-float
+    auto finish = [&](int z, float s0, float s1, const Pl& B) {
       s0 = sp0 ? dm0 * B.c0 : s0;
       s1 = sp1 ? dm1 * B.c1 : s1;
       if (active) *reinterpret_cast<float2*>(P.y + (int64_t)z * P.NP + c) = make_float2(s0, s1);
-      facc.add_product(s0, B.c0);
-      facc.add_product(s1, B.c1);
+      facc.add(fmaf(s1, B.c1, s0 * B.c0));
     };
     const auto cf = [&](int k) { return P.coef[k]; };  // constant-bank operands
-    auto row = [&](int z, const StPlane2& A, const StPlane2& B, const StPlane2& C) {
+    const auto wf = [&](int k) { return P.w8[k]; };
+    auto sum = [&](auto ha, auto hc, const Pl& A, const Pl& B, const Pl& C, float& s0, float& s1) {
+      constexpr bool HA = decltype(ha)::value, HC = decltype(hc)::value;
+      if constexpr (kSep)
+        st_sep_rows<HA, HC>(wf, A, B, C, s0, s1);
+      else
+        st_sum2<HA, HC>(cf, A, B, C, s0, s1);
+    };
+    using T_ = std::true_type;
+    using F_ = std::false_type;
+    auto row = [&](int z, const Pl& A, const Pl& B, const Pl& C) {
       float s0, s1;
       if (z >= 2 && z <= P.Nz - 3) {
-        st_sum2<true, true>(cf, A, B, C, s0, s1);
+        sum(T_{}, T_{}, A, B, C, s0, s1);
       } else if (z == 0 || z == P.Nz - 1) {
         s0 = P.dd * B.c0;
         s1 = P.dd * B.c1;
       } else if (z == 1 && z == P.Nz - 2) {
-        st_sum2<false, false>(cf, A, B, C, s0, s1);
+        sum(F_{}, F_{}, A, B, C, s0, s1);
       } else if (z == 1) {
-        st_sum2<false, true>(cf, A, B, C, s0, s1);
+        sum(F_{}, T_{}, A, B, C, s0, s1);
       } else {
-        st_sum2<true, false>(cf, A, B, C, s0, s1);
+        sum(T_{}, F_{}, A, B, C, s0, s1);
       }
       finish(z, s0, s1, B);
     };
@@ -373,13 +401,13 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, 2) k_spmv_stencil(const __grid_
         if (z >= 2 && z + 2 <= P.Nz - 3 && z + 3 <= zb) {  // three interior rows
           float s0, s1;
           load_plane(0, W2);
-          st_sum2<true, true>(cf, W0, W1, W2, s0, s1);
+          sum(T_{}, T_{}, W0, W1, W2, s0, s1);
           finish(z, s0, s1, W1);
           load_plane(1, W0);
-          st_sum2<true, true>(cf, W1, W2, W0, s0, s1);
+          sum(T_{}, T_{}, W1, W2, W0, s0, s1);
           finish(z + 1, s0, s1, W2);
           load_plane(2, W1);
-          st_sum2<true, true>(cf, W2, W0, W1, s0, s1);
+          sum(T_{}, T_{}, W2, W0, W1, s0, s1);
           finish(z + 2, s0, s1, W0);
         } else {
           load_plane(0, W2);
@@ -493,12 +521,35 @@ mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* 
                              static_cast<const double*>(A64->vals), coef, ok);
 }
 
-// one wave of resident CTAs (the attribute is set before any graph capture)
-mfe_status stencil_grid(mfe_ctx* ctx, int* grid)
+bool stencil_mirror_classes(const float* coef, float* w8)
 {
-  MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k_spmv_stencil, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)kS2Smem));
-  *grid = resident_blocks(ctx, (const void*)k_spmv_stencil, kS2P / 2 + 32, kS2Smem);
+  float amax = 0.0f;
+  for (int k = 0; k < 27; ++k) amax = std::max(amax, std::fabs(coef[k]));
+  const double tol = std::ldexp((double)amax, -22);
+  for (int c = 0; c < 8; ++c) {
+    const int az = c >> 2, ay = (c >> 1) & 1, ax = c & 1;
+    w8[c] = coef[(az + 1) * 9 + (ay + 1) * 3 + (ax + 1)];
+  }
+  for (int k = 0; k < 27; ++k) {
+    const int dz = k / 9 - 1, dy = (k / 3) % 3 - 1, dx = k % 3 - 1;
+    const int c = 4 * (dz != 0) + 2 * (dy != 0) + (dx != 0);
+    if (!(std::fabs((double)coef[k] - (double)w8[c]) <= tol)) return false;
+  }
+  return true;
+}
+
+// one wave of resident CTAs of the variant coef selects (the attributes are
+// set before any graph capture; the largest shared-memory carveout lets
+// three rings share an SM)
+mfe_status stencil_grid(mfe_ctx* ctx, const float* coef, int* grid)
+{
+  float w8[8];
+  const void* k = stencil_mirror_classes(coef, w8) ? (const void*)k_spmv_stencil<true>
+                                                   : (const void*)k_spmv_stencil<false>;
+  MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kS2Smem));
+  MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(k, cudaFuncAttributePreferredSharedMemoryCarveout,
+                                         (int)cudaSharedmemCarveoutMaxShared));
+  *grid = resident_blocks(ctx, k, kS2P / 2 + 32, kS2Smem);
   return MFE_OK;
 }
 
@@ -513,6 +564,7 @@ mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef
   P.NP = P.Nxp * P.Ny;
   P.ntile = (int)ceil_div(P.NP, (int64_t)kS2P);
   for (int k = 0; k < 27; ++k) P.coef[k] = coef[k];
+  const bool sep = stencil_mirror_classes(coef, P.w8);
   P.dd = coef[27];
   P.x = x;
   P.y = y;
@@ -521,7 +573,10 @@ mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef
   P.dot_out = sink->out;
   P.err = err;
   const int g = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)grid, (int64_t)P.ntile * P.Nz));
-  k_spmv_stencil<<<g, kS2P / 2 + 32, kS2Smem, ctx->stream>>>(P);
+  if (sep)
+    k_spmv_stencil<true><<<g, kS2P / 2 + 32, kS2Smem, ctx->stream>>>(P);
+  else
+    k_spmv_stencil<false><<<g, kS2P / 2 + 32, kS2Smem, ctx->stream>>>(P);
   return check_launch(ctx, "k_spmv_stencil");
 }
 
