@@ -726,7 +726,7 @@ def main():
                     help="skip the 32-right-hand-side solve")
     ap.add_argument("--no-seq", action="store_true",
                     help="skip the sequential baselines of the batched and multi-RHS solves")
-    ap.add_argument("--refine-k", type=int, default=50,
+    ap.add_argument("--refine-k", type=int, default=100,
                     help="mixed solver: reliable update at least every k inner iterations")
     ap.add_argument("--cpu-sample", type=int, default=20)
     ap.add_argument("--ref-dims", type=int, default=DIMS[0],

@@ -216,9 +216,14 @@ typedef struct mfe_cg_opts {
   double tol;           /* reference: DBL_EPSILON absolute (driver.hpp:245) */
   int32_t precision;    /* mfe_precision */
   int32_t refine_k;     /* mixed: max inner iterations per refinement sweep
-                           (0 = library default) */
-  double inner_tol;     /* mixed: inner relative reduction per sweep (0 = default) */
-  int32_t max_refine;   /* mixed: max refinement sweeps (0 = default) */
+                           (0 = library default: 100 for one box, 50 for
+                           batched boxes and multiple right-hand sides) */
+  double inner_tol;     /* mixed: a reliable update is due once the recursive
+                           residual fell by this factor since the last one;
+                           [0, 1), 0 = 0.01 */
+  int32_t max_refine;   /* mixed: max reliable updates; the solve stops with
+                           MFE_MAXITER after that many unless converged
+                           (0 = no cap) */
   int32_t record_history; /* 1: keep normr of every iteration (see
                              mfe_cg_history) */
   const mfe_csr* A32;   /* mixed: optional prepared FP32 copy of A (NULL: the

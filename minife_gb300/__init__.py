@@ -464,7 +464,8 @@ def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
 
 def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPSILON,
                    tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
-                   ctx: Context | None = None) -> list:
+                   ctx: Context | None = None, inner_tol: float = 0.0,
+                   max_refine: int = 0) -> list:
     """nrhs independent CG solves on one box matrix advanced together (one
     matrix read per iteration for all of them).  B, X: device (n, nrhs) FP64,
     contiguous; X holds the initial guesses and receives the solutions.
@@ -476,7 +477,7 @@ def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPS
         raise ValueError("B and X must be (n, nrhs) with the same shape")
     nrhs = B.shape[1]
     m = A.c()
-    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k)
+    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine)
     res = (MfeCgResult * nrhs)()
     st = ctx.lib.mfe_cg_solve_multi(ctx.h, ctypes.byref(m), nrhs, _ptr(B), _ptr(X),
                                     ctypes.byref(o), res)
@@ -530,7 +531,8 @@ class Batch:
                        "mfe_batch_set_tuning")
 
     def solve(self, max_iter: int = 200, tol: float = DBL_EPSILON, tol_mode: str = "absolute",
-              precision: str = "mixed", refine_k: int = 0, x=None, mixed_operator: str = "auto"):
+              precision: str = "mixed", refine_k: int = 0, x=None, mixed_operator: str = "auto",
+              inner_tol: float = 0.0, max_refine: int = 0):
         """Returns (x, results): results holds one CGResult per box (times[0] =
         assembly of the batch, times[4] = the batched solve, in seconds).
         Mixed precision: mixed_operator "auto" uses the verified FP32 stencil
@@ -541,7 +543,8 @@ class Batch:
         ctx.bind_torch_stream()
         if x is None:
             x = torch.empty(max(self.offsets[-1], 1), dtype=torch.float64, device="cuda")
-        o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k, mixed_operator=mixed_operator)
+        o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine,
+                     mixed_operator=mixed_operator)
         res = (MfeCgResult * len(self.dims))()
         st = ctx.lib.mfe_batch_solve(ctx.h, self.h, ctypes.byref(o), _ptr(x), res)
         if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
@@ -552,7 +555,7 @@ class Batch:
 def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
                       tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
                       tuning: dict | None = None, ctx: Context | None = None,
-                      mixed_operator: str = "auto"):
+                      mixed_operator: str = "auto", inner_tol: float = 0.0, max_refine: int = 0):
     """Assemble and solve len(dims) independent miniFE boxes together
     (mfe_batch_solve_boxes).  Returns (x, offsets, results); box i's rows are
     x[offsets[i]:offsets[i+1]]."""
@@ -561,7 +564,8 @@ def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
         if tuning:
             b.set_tuning(**tuning)
         x, res = b.solve(max_iter, tol, tol_mode, precision, refine_k,
-                         mixed_operator=mixed_operator)
+                         mixed_operator=mixed_operator, inner_tol=inner_tol,
+                         max_refine=max_refine)
         return x, b.offsets, res
     finally:
         b.close()

@@ -34,9 +34,10 @@
 // Solvers.  FP64: the reference's CG per box (cg_solve.hpp loop test with
 // normr from the top of the iteration).  Mixed: FP32 values and vectors, FP64
 // dots and scalars, FP64 solution; a box takes a reliable update (x += x32,
-// r = b - A64 x in FP64, FP32 copy of r) when its recursive residual fell
-// tenfold since its last update, claims convergence, or after refine_k
-// iterations, and it finishes only on its true FP64 residual.
+// r = b - A64 x in FP64, FP32 copy of r) when its recursive residual fell by
+// inner_tol (default a hundredfold) since its last update, claims
+// convergence, or after refine_k iterations, and it finishes only on its true
+// FP64 residual (or after max_refine updates, when that cap is set).
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -70,11 +71,13 @@ struct BoxSt {
   double alpha_prev;  // mixed: alpha whose x32 += alpha p is still pending
   int open, gate, iters, since, brk;
   int x_pending;      // mixed: 1 while x32 += alpha_prev p is due
+  int upd;            // mixed: reliable updates of this box
   unsigned cnt_mv, cnt_vec;
 };
 
 struct BatchCtl {
   int nbox, k, max_iter, refine_k, first, cont, status, updates, tol_mode;
+  int max_refine;  // mixed: a box stops after this many updates (0: no cap)
   double delta2;
   unsigned err;
 };
@@ -1224,7 +1227,8 @@ __global__ void __launch_bounds__(1024)
       atomicOr(&any_gate, 1);
       s.normr = sqrt(s.rr_true);
       s.since = 0;
-      if (s.normr <= s.tol_abs) {
+      s.upd += 1;
+      if (s.normr <= s.tol_abs || (ctl->max_refine > 0 && s.upd >= ctl->max_refine)) {
         s.open = 0;
         s.iters = k;
       } else {
@@ -1749,6 +1753,7 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
   if (o->precision != MFE_PREC_MIXED && o->precision != MFE_PREC_F64)
     return fail(ctx, MFE_BAD_ARG, "unknown precision");
   if (bt->device != ctx->device) return fail(ctx, MFE_BAD_ARG, "batch belongs to another device");
+  if (o->precision == MFE_PREC_MIXED && !mixed_opts_valid(o)) return fail(ctx, MFE_BAD_ARG, "inner_tol must lie in [0, 1) and max_refine must be >= 0");
   const int nbox = bt->nbox;
   Run R;
   R.bt = bt;
@@ -1824,7 +1829,8 @@ mfe_status batch_solve(mfe_ctx* ctx, mfe_batch* bt, const mfe_cg_opts* o, double
   hc.refine_k = o->refine_k > 0 ? o->refine_k : 50;
   hc.first = 1;
   hc.tol_mode = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;
-  hc.delta2 = 1e-2;
+  hc.delta2 = mixed_delta2(o);
+  hc.max_refine = o->max_refine;
   std::vector<int> hl(4 * ((size_t)nbox + 2) + 4, 0);
   {
     const size_t per = (size_t)nbox + 2;

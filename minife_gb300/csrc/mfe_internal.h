@@ -127,6 +127,22 @@ mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef
                                float* y, const DotSink* sink, int grid, unsigned* err);
 
 // ---- mixed-precision CG (mfe_mixed.cu) ----
+// Reliable-update policy options of the mixed solvers: an update is due once
+// the recursive residual has fallen by inner_tol since the last one (0: 0.01,
+// a drop FP32 recursions follow closely; tenfold updates cost more FP64
+// residual SpMVs for the same iteration count),
+// and max_refine caps the number of updates (0: no cap; the solve then stops
+// with MFE_MAXITER unless it converged).
+inline bool mixed_opts_valid(const mfe_cg_opts* o)
+{
+  return o->inner_tol >= 0.0 && o->inner_tol < 1.0 && o->max_refine >= 0;
+}
+inline double mixed_delta2(const mfe_cg_opts* o)
+{
+  const double t = o->inner_tol > 0.0 ? o->inner_tol : 0.01;
+  return t * t;
+}
+
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64, const double* b, double* x,
                     const mfe_cg_opts* opts, mfe_cg_result* res);
 

@@ -12,9 +12,10 @@
 // recursive residual with the true one; the search direction p is kept, so
 // the recurrence continues instead of restarting and the iteration count stays
 // close to the FP64 solver's.  Updates happen every refine_k iterations, when
-// the recursive residual has dropped tenfold since the last update, and
-// whenever the recursive residual claims convergence; the solve stops only
-// when the true FP64 residual meets the tolerance.
+// the recursive residual has dropped by inner_tol (default a hundredfold)
+// since the last update, and whenever the recursive residual claims
+// convergence; the solve stops only when the true FP64 residual meets the
+// tolerance (or after max_refine updates, when that cap is set).
 //
 // One iteration is three kernels (k_mx_p, the FP32 box SpMV with p.Ap,
 // k_mx_update) plus three that only work when an update is due (the graph
@@ -47,6 +48,7 @@ struct MixState {
   int max_iter;
   int since;            // iterations since the last reliable update
   int refine_k;         // update at least every refine_k iterations
+  int max_refine;       // stop after this many updates (0: no cap)
   int gate;             // 1: a reliable update runs in this iteration
   int cont;             // loop condition
   int first;            // next p update is p = r
@@ -188,7 +190,8 @@ __global__ void k_mx_after(MixState* st, cudaGraphConditionalHandle h, int in_gr
     st->updates += 1;
     st->since = 0;
     st->normr_true = sqrt(st->rr_true);
-    if (st->normr_true <= st->tol_abs || st->k >= st->max_iter) {
+    if (st->normr_true <= st->tol_abs || st->k >= st->max_iter ||
+        (st->max_refine > 0 && st->updates >= st->max_refine)) {
       st->cont = 0;
     } else {
       // continue the recurrence from the true residual, keeping p
@@ -286,6 +289,7 @@ mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, con
 mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double* x,
                     const mfe_cg_opts* o, mfe_cg_result* res)
 {
+  if (!mixed_opts_valid(o)) return fail(ctx, MFE_BAD_ARG, "inner_tol must lie in [0, 1) and max_refine must be >= 0");
   const int64_t n = A64_in->nrows;
   mfe_csr A64 = *A64_in;
   if (!csr_is_box(&A64)) {
@@ -366,8 +370,9 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
   hs->max_iter = max_iter;
   hs->tol_abs = o->tol;
   hs->gate = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;  // consumed by k_mx_init
-  hs->refine_k = o->refine_k > 0 ? o->refine_k : 25;
-  hs->delta2 = 1e-2;
+  hs->refine_k = o->refine_k > 0 ? o->refine_k : 100;
+  hs->delta2 = mixed_delta2(o);
+  hs->max_refine = o->max_refine;
   hs->record = o->record_history ? 1 : 0;
   hs->history = B.history;
   hs->first = 1;

@@ -76,6 +76,7 @@ struct MultiState {
   int iters[kMaxRhs];  // iterations until each right-hand side converged
   int brk[kMaxRhs];    // p.Ap <= 0 met (the right-hand side stops alone)
   int nrhs, k, max_iter, since, refine_k, gate, cont, first, updates, status, tol_mode;
+  int max_refine;  // mixed: stop after this many shared updates (0: no cap)
   unsigned err;
   int x_pending;  // mixed: x32 += alpha p of the last update not yet done
   double delta2;
@@ -832,8 +833,8 @@ __global__ void __launch_bounds__(kVT)
 
 // Mixed solver, one warp, after the update kernel: decide whether this
 // iteration ends with a reliable update, which all right-hand sides share:
-// when every open one has its recursive residual fallen tenfold since the
-// last update or claims convergence, after refine_k iterations, or at the
+// when every open one has its recursive residual fallen by inner_tol since
+// the last update or claims convergence, after refine_k iterations, or at the
 // iteration limit.  (Waiting for the slowest keeps the update count near a
 // single solve's; a right-hand side that claims convergence early keeps
 // iterating on its recursion until the update checks its true residual.)
@@ -895,7 +896,8 @@ __global__ void k_mr_after(MultiState* st, cudaGraphConditionalHandle h, int in_
       st->since = 0;
     }
     st->gate = 0;
-    st->cont = open && st->k < st->max_iter;
+    st->cont = open && st->k < st->max_iter &&
+               !(gate && st->max_refine > 0 && st->updates >= st->max_refine);
     if (in_graph) cudaGraphSetConditional(h, st->cont ? 1u : 0u);
   }
 }
@@ -1246,6 +1248,7 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
     return fail(ctx, MFE_BAD_ARG, "nrhs must divide 32 (1, 2, 4, 8, 16 or 32)");
   if (o->precision != MFE_PREC_MIXED && o->precision != MFE_PREC_F64)
     return fail(ctx, MFE_BAD_ARG, "unknown precision");
+  if (o->precision == MFE_PREC_MIXED && !mixed_opts_valid(o)) return fail(ctx, MFE_BAD_ARG, "inner_tol must lie in [0, 1) and max_refine must be >= 0");
   if (A64_in->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "A must be FP64");
   mfe_csr A64 = *A64_in;
   if (!csr_is_box(&A64)) {
@@ -1321,7 +1324,8 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   hs->nrhs = nrhs;
   hs->max_iter = std::max(0, o->max_iter);
   hs->refine_k = o->refine_k > 0 ? o->refine_k : 50;
-  hs->delta2 = 1e-2;
+  hs->delta2 = mixed_delta2(o);
+  hs->max_refine = o->max_refine;
   hs->first = 1;
   hs->tol_mode = o->tol_mode == MFE_TOL_RELATIVE ? 1 : 0;
   for (int j = 0; j < nrhs; ++j) hs->tol_abs[j] = o->tol;

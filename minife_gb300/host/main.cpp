@@ -14,7 +14,9 @@
 // multi-rank ones have no effect on one GPU).  GB300 keys: precision (f64 |
 // mixed), max_iters (default 200, driver.hpp:241), abs_tol (default
 // DBL_EPSILON, driver.hpp:245), rel_tol (overrides abs_tol: stop at
-// ||r|| <= rel_tol ||r0||), refine_k (mixed solver), kernels (1: the
+// ||r|| <= rel_tol ||r0||), refine_k, inner_tol, max_refine (mixed solver:
+// update at least every refine_k iterations, and once the recursive residual
+// fell by inner_tol; at most max_refine updates), kernels (1: the
 // reference's MINIFE_KERNELS timing loops instead of the CG solve), dump (1:
 // the reference's MINIFE_DEBUG files A_prebc.mtx, b_prebc.vec, A.mtx, b.vec,
 // A_local.mtx, b_local.vec, x.vec, each with the ".1.0" suffix), precond
@@ -92,8 +94,8 @@ struct Params {
   int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads, kernels, dump;
   float load_imbalance;
   std::string name, precision, precond;
-  int max_iters, refine_k;
-  double abs_tol, rel_tol;
+  int max_iters, refine_k, max_refine;
+  double abs_tol, rel_tol, inner_tol;
 };
 
 void print_timed(const char* msg, double t, double total)
@@ -128,6 +130,8 @@ int main(int argc, char** argv)
   p.abs_tol = parse_parameter<double>(as, "abs_tol", std::numeric_limits<double>::epsilon());
   p.rel_tol = parse_parameter<double>(as, "rel_tol", 0.0);
   p.refine_k = parse_parameter<int>(as, "refine_k", 0);
+  p.inner_tol = parse_parameter<double>(as, "inner_tol", 0.0);
+  p.max_refine = parse_parameter<int>(as, "max_refine", 0);
   p.kernels = parse_parameter<int>(as, "kernels", 0);
   p.dump = parse_parameter<int>(as, "dump", 0);
   p.precond = parse_parameter<std::string>(as, "precond", "none");
@@ -140,7 +144,8 @@ int main(int argc, char** argv)
               << p.verify_solution << "\nname " << p.name << "\nload_imbalance "
               << p.load_imbalance << "\nprecision " << p.precision << "\nmax_iters "
               << p.max_iters << "\nabs_tol " << p.abs_tol << "\nrel_tol " << p.rel_tol
-              << "\nrefine_k " << p.refine_k << std::endl;
+              << "\nrefine_k " << p.refine_k << "\ninner_tol " << p.inner_tol << "\nmax_refine "
+              << p.max_refine << std::endl;
     return 0;
   }
 
@@ -355,6 +360,8 @@ int main(int argc, char** argv)
     o.precision = p.precision == "mixed" ? MFE_PREC_MIXED : MFE_PREC_F64;
   o.precond = p.precond == "jacobi" ? 1 : 0;
     o.refine_k = p.refine_k;
+    o.inner_tol = p.inner_tol;
+    o.max_refine = p.max_refine;
     std::cout << "Starting CG solver ... " << std::endl;
     mfe_cg_result r;
     const mfe_status st = mfe_cg_solve(ctx, &A, b, x, &o, &r);

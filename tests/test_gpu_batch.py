@@ -83,6 +83,31 @@ def test_batch_single_box_and_max_iter():
     assert all(r.num_iters == 4 and r.status == 5 for r in res)
 
 
+def test_batch_inner_tol_and_max_refine():
+    dims = [(10, 10, 10), (12, 7, 5), (9, 11, 6)]
+    x, off, res = M.batch_solve_boxes(dims, max_iter=3000, tol=1e-8, tol_mode="relative",
+                                      precision="mixed", refine_k=1000, inner_tol=1e-3)
+    xh = host(x)
+    for i, d in enumerate(dims):
+        ro, cols, vals, b = O.build_system(*d)
+        rel = np.linalg.norm(b - O.matvec(ro, cols, vals, xh[off[i]:off[i + 1]])) / \
+            np.linalg.norm(b)
+        assert res[i].status == 0 and rel <= 1e-8, (d, res[i].status, rel)
+    # one update each (at a tenfold drop): none has converged
+    x, off, res = M.batch_solve_boxes(dims, max_iter=3000, tol=1e-8, tol_mode="relative",
+                                      precision="mixed", max_refine=1)
+    xh = host(x)
+    for i, d in enumerate(dims):
+        ro, cols, vals, b = O.build_system(*d)
+        r = np.linalg.norm(b - O.matvec(ro, cols, vals, xh[off[i]:off[i + 1]]))
+        assert res[i].status == 5, (d, res[i].status)
+        assert abs(r - res[i].final_resid) <= 1e-9 * r
+    with pytest.raises(M.MiniFEError) as ei:
+        M.batch_solve_boxes(dims, tol=1e-8, tol_mode="relative", precision="mixed",
+                            inner_tol=2.0)
+    assert ei.value.status == 1
+
+
 def test_batch_rejects_bad_dims():
     with pytest.raises(M.MiniFEError) as ei:
         M.batch_solve_boxes([(4, 4, 4), (0, 3, 3)])

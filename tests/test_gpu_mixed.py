@@ -64,6 +64,40 @@ def test_mixed_max_iter_reports_maxiter():
     assert abs(r - res.final_resid) <= 1e-9 * r
 
 
+def test_mixed_inner_tol_and_max_refine():
+    """inner_tol is the residual drop that makes a reliable update due (0:
+    a hundredfold); max_refine caps the updates, after which an unconverged
+    solve reports MFE_MAXITER with the reliably updated iterate."""
+    A, b = M.build_system(30, 30, 30)
+    ro, cols, vals, bo = O.build_system(30, 30, 30)
+    updates, iters = {}, {}
+    for t in (0.0, 1e-1, 1e-2, 1e-3):
+        x = torch.zeros_like(b)
+        res = M.cg_solve(A, b, x, max_iter=3000, tol=1e-8, tol_mode="relative",
+                         precision="mixed", refine_k=1000, inner_tol=t)
+        assert res.status == 0, (t, res.status)
+        rel = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x))) / np.linalg.norm(bo)
+        assert rel <= 1e-8, (t, rel)
+        updates[t], iters[t] = res.refinements, res.num_iters
+    assert updates[1e-3] <= updates[1e-2] <= updates[1e-1], updates
+    assert updates[1e-3] < updates[1e-1], updates
+    # the default is 1e-2: the same run
+    assert (updates[0.0], iters[0.0]) == (updates[1e-2], iters[1e-2])
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=3000, tol=1e-8, tol_mode="relative",
+                     precision="mixed", max_refine=2)
+    assert res.status == 5 and res.refinements == 2, (res.status, res.refinements)
+    r = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x)))
+    assert abs(r - res.final_resid) <= 1e-9 * r
+    assert r > 1e-8 * np.linalg.norm(bo)
+    for bad in ({"inner_tol": 1.0}, {"inner_tol": -0.5}, {"inner_tol": float("nan")},
+                {"max_refine": -1}):
+        with pytest.raises(M.MiniFEError) as ei:
+            M.cg_solve(A, b, torch.zeros_like(b), tol=1e-8, tol_mode="relative",
+                       precision="mixed", **bad)
+        assert ei.value.status == 1, bad  # MFE_BAD_ARG
+
+
 def test_mixed_with_prepared_f32_copy_and_history():
     A, b = M.build_system(16, 16, 16)
     A32 = M.to_f32(A)

@@ -92,6 +92,27 @@ def test_multi_mixed_reaches_fp64_tolerance(dims, nrhs, refine_k):
         assert rel_err <= 1e-6, (j, rel_err)
 
 
+def test_multi_inner_tol_and_max_refine():
+    A, b = M.build_system(12, 12, 12)
+    B = rhs_block(b, 4, seed=2)
+    ro, cols, vals, _ = O.build_system(12, 12, 12)
+    X = torch.zeros_like(B)
+    res = M.cg_solve_multi(A, B, X, max_iter=3000, tol=1e-8, tol_mode="relative",
+                           precision="mixed", refine_k=1000, inner_tol=1e-3)
+    Bh, Xh = host(B), host(X)
+    for j in range(4):
+        rel = np.linalg.norm(Bh[:, j] - O.matvec(ro, cols, vals, Xh[:, j])) / \
+            np.linalg.norm(Bh[:, j])
+        assert res[j].status == 0 and rel <= 1e-8, (j, res[j].status, rel)
+    res = M.cg_solve_multi(A, B, torch.zeros_like(B), max_iter=3000, tol=1e-8,
+                           tol_mode="relative", precision="mixed", max_refine=1)
+    assert all(r.status == 5 and r.refinements == 1 for r in res)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.cg_solve_multi(A, B, torch.zeros_like(B), tol=1e-8, tol_mode="relative",
+                         precision="mixed", max_refine=-2)
+    assert ei.value.status == 1
+
+
 def test_multi_zero_column_and_nonzero_guess():
     """A zero right-hand side with a zero guess is converged at entry (0
     iterations, untouched); a nonzero initial guess is honoured."""
