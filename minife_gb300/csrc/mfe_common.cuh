@@ -229,6 +229,81 @@ struct DFAcc {
   __device__ __forceinline__ double value() const { return f2d_exact(hi) + f2d_exact(lo); }
 };
 
+// Double-float reductions with FP32 operations only, so the tail of a kernel
+// whose rows are summed in DFAcc does not queue on the FP64 pipe (1/64 of the
+// FP32 rate on GB300): (hi, lo) += (h2, l2), TwoSum on the high parts.
+__device__ __forceinline__ void df_add(float& hi, float& lo, float h2, float l2)
+{
+  const float t = __fadd_rn(hi, h2);
+  const float bp = __fsub_rn(t, hi);
+  const float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(t, bp)), __fsub_rn(h2, bp));
+  hi = t;
+  lo = __fadd_rn(lo, __fadd_rn(l2, err));
+}
+
+__device__ __forceinline__ void warp_sum_df(float& hi, float& lo)
+{
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+    df_add(hi, lo, h2, l2);
+  }
+}
+
+// block sum of double-float pairs, valid in thread 0; scratch >= 32 pairs
+__device__ __forceinline__ void block_sum_df(float& hi, float& lo, float2* scratch)
+{
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  warp_sum_df(hi, lo);
+  __syncthreads();  // scratch may be reused across calls
+  if (lane == 0) scratch[wid] = make_float2(hi, lo);
+  __syncthreads();
+  const int nw = (blockDim.x + 31) >> 5;
+  hi = 0.0f;
+  lo = 0.0f;
+  if (wid == 0) {
+    if (lane < nw) {
+      hi = scratch[lane].x;
+      lo = scratch[lane].y;
+    }
+    warp_sum_df(hi, lo);
+  }
+}
+
+// grid_reduce_last on double-float pairs: each block's pair goes to its
+// 8-byte slot of partials, the last block sums them in block order and thread
+// 0 gets hi + lo in FP64 (the one FP64 operation).
+__device__ __forceinline__ bool grid_reduce_last_df(const DFAcc& a, double* partials, unsigned* ticket,
+                                                    float2* scratch, double* total)
+{
+  float hi = a.hi, lo = a.lo;
+  block_sum_df(hi, lo, scratch);
+  float2* slots = reinterpret_cast<float2*>(partials);
+  __shared__ bool am_last;
+  if (threadIdx.x == 0) {
+    slots[blockIdx.x] = make_float2(hi, lo);
+    __threadfence();
+    const unsigned t = atomicAdd(ticket, 1u);
+    am_last = (t == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (!am_last) return false;
+  __threadfence();
+  hi = 0.0f;
+  lo = 0.0f;
+  for (unsigned i = threadIdx.x; i < gridDim.x; i += blockDim.x) {
+    const float2 v = __ldcg(&slots[i]);
+    df_add(hi, lo, v.x, v.y);
+  }
+  block_sum_df(hi, lo, scratch);
+  if (threadIdx.x == 0) {
+    *total = f2d_exact(hi) + f2d_exact(lo);
+    *ticket = 0u;
+  }
+  return true;
+}
+
 // ---------------------------------------------------------------------------
 // misc
 // ---------------------------------------------------------------------------

@@ -118,7 +118,7 @@ __global__ void __launch_bounds__(kT)
     k_mx_update(int64_t n, float* __restrict__ r, const float* __restrict__ Ap, MixState* st,
                 double* partials, unsigned* ticket)
 {
-  __shared__ double red[32];
+  __shared__ float2 red[32];
   __shared__ float s_alpha;
   if (threadIdx.x == 0) s_alpha = st->pAp > 0.0 ? (float)(st->rr / st->pAp) : 0.0f;
   __syncthreads();
@@ -147,9 +147,8 @@ __global__ void __launch_bounds__(kT)
     r[t] = rv;
     acc.add_product(rv, rv);
   }
-  const double bt = block_sum(acc.value(), red);
   double total;
-  if (grid_reduce_last(bt, partials, ticket, red, &total) && threadIdx.x == 0) {
+  if (grid_reduce_last_df(acc, partials, ticket, red, &total) && threadIdx.x == 0) {
     st->rr_new = total;
     st->alpha_prev = alpha;
     st->x_pending = 1;

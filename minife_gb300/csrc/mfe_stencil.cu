@@ -238,7 +238,7 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
   extern __shared__ __align__(128) unsigned char st2_smem_raw[];
   float* const ring = reinterpret_cast<float*>(st2_smem_raw);
   __shared__ uint64_t full[kSS], empty[kSS];
-  __shared__ double red[32];
+  __shared__ float2 red[32];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t T = (int64_t)P.ntile * P.Nz;
   const int64_t q0 = T * blockIdx.x / gridDim.x, q1 = T * (blockIdx.x + 1) / gridDim.x;
@@ -427,9 +427,9 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
     }
     if (!ok) atomicOr(P.err, ERR_WAIT_TIMEOUT);
   }
-  const double bt = block_sum(warp == 0 ? 0.0 : facc.value(), red);
+  if (warp == 0) facc = DFAcc{};  // the producer warp holds no rows
   double total;
-  if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0) *P.dot_out = total;
+  if (grid_reduce_last_df(facc, P.partials, P.ticket, red, &total) && threadIdx.x == 0) *P.dot_out = total;
 }
 
 // The model check of the class rows (host): Dirichlet classes hold dd on the
