@@ -57,6 +57,9 @@ def test_gb300_keys(driver):
     p = params(driver, "precision=mixed", "rel_tol=1e-8", "max_iters=5000", "refine_k=30")
     assert p["precision"] == "mixed" and float(p["rel_tol"]) == 1e-8
     assert p["max_iters"] == "5000" and p["refine_k"] == "30"
+    assert float(p["inner_tol"]) == 0.0 and p["max_refine"] == "0"  # library defaults
+    p = params(driver, "precision=mixed", "inner_tol=1e-3", "max_refine=4")
+    assert float(p["inner_tol"]) == 1e-3 and p["max_refine"] == "4"
 
 
 def test_zero_equations_exit(driver):
