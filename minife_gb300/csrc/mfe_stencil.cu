@@ -288,8 +288,9 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
     Pl W0, W1, W2;
     int c = 0, lane_off = 0;
     bool active = false, sp0 = false, sp1 = false, m1 = false, m2 = false, m3 = false, myl = false,
-         myh = false, wm = false;
+         myh = false, wm = false, wsp = false;
     float dm0 = 0.0f, dm1 = 0.0f;
+    float* yp = P.y;  // y at (z, c) of the next row pair
     const float* sx = ring;
     auto wait_slot = [&]() {
       const int s = it % kSS;
@@ -333,10 +334,14 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
     };
     // p.Ap: the pair's two products summed in FP32, the running sum in
     // double-float
-    auto finish = [&](int z, float s0, float s1, const Pl& B) {
-      s0 = sp0 ? dm0 * B.c0 : s0;
-      s1 = sp1 ? dm1 * B.c1 : s1;
-      if (active) *reinterpret_cast<float2*>(P.y + (int64_t)z * P.NP + c) = make_float2(s0, s1);
+    // called for z = za, za + 1, ... of the tile run in order
+    auto finish = [&](float s0, float s1, const Pl& B) {
+      if (wsp) {  // the warp holds a Dirichlet or padding row (the same for the warp)
+        s0 = sp0 ? dm0 * B.c0 : s0;
+        s1 = sp1 ? dm1 * B.c1 : s1;
+      }
+      if (active) *reinterpret_cast<float2*>(yp) = make_float2(s0, s1);
+      yp += P.NP;
       facc.add(fmaf(s1, B.c1, s0 * B.c0));
     };
     const auto cf = [&](int k) { return P.coef[k]; };  // constant-bank operands
@@ -364,7 +369,7 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
       } else {
         sum(T_{}, F_{}, A, B, C, s0, s1);
       }
-      finish(z, s0, s1, B);
+      finish(s0, s1, B);
     };
     for (int64_t q = q0; ok && q < q1;) {
       const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
@@ -388,6 +393,8 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
       myl = iy == 1;
       myh = iy == P.Ny - 2;
       wm = __any_sync(0xffffffffu, m1 || m2 || m3 || myl || myh);
+      wsp = __any_sync(0xffffffffu, sp0 || sp1);
+      yp = P.y + (int64_t)za * P.NP + cc;
       ok = wait_slot();
       if (!ok) break;
       load_plane(0, W0);
@@ -402,13 +409,13 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
           float s0, s1;
           load_plane(0, W2);
           sum(T_{}, T_{}, W0, W1, W2, s0, s1);
-          finish(z, s0, s1, W1);
+          finish(s0, s1, W1);
           load_plane(1, W0);
           sum(T_{}, T_{}, W1, W2, W0, s0, s1);
-          finish(z + 1, s0, s1, W2);
+          finish(s0, s1, W2);
           load_plane(2, W1);
           sum(T_{}, T_{}, W2, W0, W1, s0, s1);
-          finish(z + 2, s0, s1, W0);
+          finish(s0, s1, W0);
         } else {
           load_plane(0, W2);
           row(z, W0, W1, W2);
