@@ -134,6 +134,37 @@ def test_mixed_stencil_operator_and_values_copy(dims):
     assert abs(its["auto"] - its["values"]) <= max(3, 0.1 * its["values"]), its
 
 
+def test_mixed_stencil_without_mirror_symmetry():
+    """A verified stencil that is not mirror-symmetric per axis takes the
+    27-coefficient stencil kernel: the (+-1, +-1, 0) entries scaled by 1.001
+    keep A symmetric positive definite and every interior row one stencil,
+    but coef(1, 1, 0) != coef(1, -1, 0)."""
+    dims = (20, 18, 16)
+    A, b = M.build_system(*dims)
+    N = [d + 1 for d in dims]
+    off = N[0] * N[1] + N[0]  # (dz, dy, dx) = (1, 1, 0)
+    n = A.nrows
+    lens = (A.row_offsets[1:] - A.row_offsets[:-1]).long()
+    rows = torch.repeat_interleave(torch.arange(n, device=lens.device), lens)
+    d = A.packed_cols.long() - rows
+    scale = torch.ones_like(A.packed_coefs)
+    scale[(d == off) | (d == -off)] = 1.001
+    A.packed_coefs.mul_(scale)
+    torch.cuda.synchronize()
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=3000, tol=1e-8, tol_mode="relative", precision="mixed")
+    assert res.status == 0 and res.inner_operator == "stencil", (res.status, res.inner_operator)
+    ro, cols, vals = host(A.row_offsets), host(A.packed_cols), host(A.packed_coefs)
+    bo = host(b)
+    rel = np.linalg.norm(bo - O.matvec(ro, cols, vals, host(x))) / np.linalg.norm(bo)
+    assert rel <= 1e-8, rel
+    xv = torch.zeros_like(b)
+    rv = M.cg_solve(A, b, xv, max_iter=3000, tol=1e-8, tol_mode="relative", precision="mixed",
+                    mixed_operator="values")
+    assert rv.inner_operator == "values"
+    assert abs(res.num_iters - rv.num_iters) <= max(3, rv.num_iters // 10)
+
+
 def test_mixed_stencil_first_iterations_match_values():
     """Two inner iterations from x = 0 with each FP32 operator: the residual
     norms agree to FP32 accuracy, so the stencil applies the same operator as
