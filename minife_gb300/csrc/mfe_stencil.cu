@@ -38,10 +38,12 @@
 // two rows need per class and a row takes 8 FMAs (st_sep_rows); any other
 // verified stencil takes its 27 coefficients.  Weights and coefficients are
 // kernel parameters (constant-bank operands: no registers).  Lanes next to a
-// Dirichlet node zero the masked neighbours as
-// they load them; Dirichlet planes and the planes next to them take
-// warp-uniform branches.  The (plane tile, z) steps are split evenly over
-// one wave of CTAs.
+// Dirichlet node zero the masked neighbours as they load them; Dirichlet
+// planes and the planes next to them take warp-uniform branches, and only
+// warps that hold a Dirichlet (or padding) row replace its sum by dd * x.
+// p.Ap is summed in double-float, across the grid too, so the kernel's one
+// FP64 operation is the final addition.  The (plane tile, z) steps are split
+// evenly over one wave of CTAs.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
