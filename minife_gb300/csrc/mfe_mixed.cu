@@ -4,8 +4,9 @@
 // The reference solves in FP64 only (ref/src/cg_solve.hpp).  Here the inner
 // recurrence runs the reference's CG steps (p update, A p, p.Ap, alpha, x and
 // r updates, r.r, beta) on an FP32 copy of the matrix with FP32 vectors --
-// half the bytes of every pass -- while every reduction accumulates in FP64
-// (widened with integer operations, mfe_common.cuh) and alpha / beta stay
+// half the bytes of every pass -- while every reduction is carried to FP64
+// accuracy (double-float sums on the FP32 pipe, or FP64 sums of values
+// widened with integer operations, mfe_common.cuh) and alpha / beta stay
 // FP64.  The FP32 iterate is a correction x32 to the FP64 solution x.  A
 // reliable update -- x += x32, x32 = 0, r = b - A x in FP64 (the box SpMV
 // writing the residual straight into the FP32 r) -- replaces the drifting
@@ -17,12 +18,13 @@
 // convergence; the solve stops only when the true FP64 residual meets the
 // tolerance (or after max_refine updates, when that cap is set).
 //
-// One iteration is three kernels (k_mx_p, the FP32 box SpMV with p.Ap,
-// k_mx_update) plus three that only work when an update is due (the graph
-// cannot branch cheaply per iteration, so k_mx_xupdate and the FP64 residual
-// SpMV check a device-side gate and return at once when it is closed) and a
-// one-thread bookkeeping kernel that sets the loop condition.  The whole
-// solve is one CUDA graph launch with a conditional while node.
+// One iteration is three kernels (k_mx_p, the FP32 operator with p.Ap -- the
+// verified stencil of mfe_stencil.cu or the box SpMV over an FP32 copy of
+// the values -- and k_mx_update) plus two that only work when an update is
+// due (the graph cannot branch cheaply per iteration, so k_mx_xupdate and the
+// FP64 residual SpMV check a device-side gate and return at once when it is
+// closed) and a one-thread bookkeeping kernel that sets the loop condition.
+// The whole solve is one CUDA graph launch with a conditional while node.
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
