@@ -14,9 +14,10 @@ Keys beyond the base contract:
   roofline     the dominant kernel (the CSR SpMV with fused p.Ap) timed with
                CUDA events on its stream against MEASURED_PEAKS.json's HBM copy
                bandwidth; traffic from the committed ncu summary
-  cpu_baseline the OpenMP CG port (oracle/cpu_baseline.c) on the host cores,
-               a bounded sample of iterations scaled to the solve's count
-  --impl reference  times that CPU baseline as the reference arm.
+  cpu_baseline the OpenMP CG port (oracle/cpu_baseline.c) on the host cores:
+               one whole solve of the same system to the same tolerance
+  --impl reference  times that CPU baseline as the reference arm, one whole
+               solve per timed step.
 """
 from __future__ import annotations
 
@@ -155,19 +156,27 @@ def max_over_ranks(world, v):
 # --------------------------------------------------------------------------
 # CPU baseline (oracle/cpu_baseline.c, OpenMP port of the openmp/ variant)
 # --------------------------------------------------------------------------
-def cpu_cg_sample(ro, cols, vals, b, iters):
-    """Run `iters` CG iterations with the OpenMP baseline; returns (seconds,
-    threads)."""
+def workload_config(world, n, nnz, dims=DIMS):
+    """The `config` both arms print: the 256^3 FP64 CG to 1e-8 relative."""
+    return {"workload": "cg_f64_%d^3_to_1e-8_rel" % dims[0], "nx": dims[0], "ny": dims[1],
+            "nz": dims[2], "rows": n, "nnz": nnz, "tol_rel": TOL,
+            "l2": "inputs larger than L2", "parallelism": "replicas" if world > 1 else "single"}
+
+
+def cpu_cg_solve(ro, cols, vals, b, max_iter=5000, tol=TOL, tol_mode=1):
+    """One OpenMP CG solve from x0 = 0 (relative tolerance by default);
+    returns (seconds, iterations, threads, x)."""
+    import ctypes
     import numpy as np
     from oracle import oracle as O
     L = O.cpubase()
     x = np.zeros(b.size)
-    import ctypes
     nr = ctypes.c_double()
     t0 = time.perf_counter()
-    L.cpub_cg_solve(b.size, ro, cols, vals, b, x, int(iters), 0.0, 0, ctypes.byref(nr))
+    it = L.cpub_cg_solve(b.size, ro, cols, vals, b, x, int(max_iter), float(tol), int(tol_mode),
+                         ctypes.byref(nr))
     t1 = time.perf_counter()
-    return t1 - t0, int(L.cpub_num_threads())
+    return t1 - t0, int(it), int(L.cpub_num_threads()), x
 
 
 def host_system(A, b):
@@ -183,10 +192,11 @@ def host_system(A, b):
 
 
 def run_reference(args):
-    """Reference arm: the CPU CG on the host cores, bounded samples scaled to
-    the full solve's iteration count."""
-    import numpy as np
-    import torch
+    """Reference arm: the OpenMP CG port on all host cores.  Every timed step
+    is one whole solve of the 256^3 system from x0 = 0 to the 1e-8 relative
+    residual (its own iteration count, measured, not scaled).  Warm-up steps
+    are bounded: a short solve (--ref-warmup-iters iterations) each, which
+    pages the arrays in and starts the thread pool."""
     world, rank, local = dist_setup(args.gpus)
     if rank != 0:
         return 0
@@ -198,26 +208,28 @@ def run_reference(args):
     t0 = time.perf_counter()
     ro, cols, vals, bh = O.build_system(*dims)
     log("reference arm: host assembly of %dx%dx%d took %.1f s" % (*dims, time.perf_counter() - t0))
-    iters_full = args.ref_iters
-    per = []
+    for _ in range(args.warmup):
+        cpu_cg_solve(ro, cols, vals, bh, max_iter=args.ref_warmup_iters)
+    ts, its = [], []
     threads = 1
-    for i in range(args.warmup + args.steps):
-        dt, threads = cpu_cg_sample(ro, cols, vals, bh, args.ref_sample)
-        if i >= args.warmup:
-            per.append(dt / args.ref_sample)
-    per_it = sum(per) / len(per)
-    value = per_it * iters_full
+    for _ in range(args.steps):
+        dt, it, threads, _ = cpu_cg_solve(ro, cols, vals, bh)
+        ts.append(dt)
+        its.append(it)
+        log("reference arm: solve %.2f s, %d iterations" % (dt, it))
+    value = sum(ts) / len(ts)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": value * 1e3, "higher_is_better": False, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f64", "data": "synthetic (miniFE box, generated)",
-        "config": {"workload": "cg_f64_256^3_to_1e-8_rel", "nx": dims[0], "ny": dims[1],
-                   "nz": dims[2], "iterations": iters_full},
+        "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (miniFE %d^3 box generated on the host by the oracle)" % dims[0],
+        "config": workload_config(1, ro.size - 1, cols.size, dims),
+        "iterations": {"min": min(its), "max": max(its)},
         "cpu_baseline": {"value": value, "unit": "s", "cores": threads, "kind": "port",
-                         "sample": "%d CG iterations per step on the %d^3 system, %d steps, "
-                                   "scaled to %d iterations" % (args.ref_sample, dims[0],
-                                                                args.steps, iters_full)},
+                         "sample": "whole OpenMP CG solves of the %d^3 system to 1e-8 relative "
+                                   "(%d-%d iterations), one per step, averaged over %d steps"
+                                   % (dims[0], min(its), max(its), args.steps)},
         "e2e": {"value": value, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -404,11 +416,10 @@ def run_gpu(args):
 
     cpu = None
     if rank == 0 and not args.no_cpu:
-        dt, threads = cpu_cg_sample(ro, cols, vals, bh, args.cpu_sample)
-        per_it = dt / args.cpu_sample
-        cpu = {"value": per_it * res.num_iters, "unit": "s", "cores": threads, "kind": "port",
-               "sample": "%d OpenMP CG iterations on the 256^3 system, scaled to %d iterations"
-                         % (args.cpu_sample, res.num_iters)}
+        dt, it_cpu, threads, _ = cpu_cg_solve(ro, cols, vals, bh)
+        cpu = {"value": dt, "unit": "s", "cores": threads, "kind": "port",
+               "sample": "one whole OpenMP CG solve of the 256^3 system to 1e-8 relative "
+                         "(%d iterations)" % it_cpu}
 
     if rank == 0:
         line = {
@@ -417,10 +428,7 @@ def run_gpu(args):
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic (miniFE 256^3 box generated on the device; matrix 5.5 GB > L2, "
                     "no flush needed)",
-            "config": {"workload": "cg_f64_256^3_to_1e-8_rel", "nx": DIMS[0], "ny": DIMS[1],
-                       "nz": DIMS[2], "rows": n, "nnz": nnz, "tol_rel": TOL,
-                       "l2": "inputs larger than L2", "parallelism": "replicas" if world > 1
-                       else "single"},
+            "config": workload_config(world, n, nnz),
             "iterations": res.num_iters,
             "final_rel_resid": final_rel, "reported_rel_normr": rel,
             "analytic_check": {"max_err": err, "passed": rc == 0},
@@ -728,12 +736,10 @@ def main():
                     help="skip the sequential baselines of the batched and multi-RHS solves")
     ap.add_argument("--refine-k", type=int, default=100,
                     help="mixed solver: reliable update at least every k inner iterations")
-    ap.add_argument("--cpu-sample", type=int, default=20)
     ap.add_argument("--ref-dims", type=int, default=DIMS[0],
-                    help="reference arm: box edge of the sampled system (the metric's is 256)")
-    ap.add_argument("--ref-sample", type=int, default=10)
-    ap.add_argument("--ref-iters", type=int, default=401,
-                    help="CG iterations of the 256^3 solve to 1e-8 (the GPU solve's count)")
+                    help="reference arm: box edge of the system (the metric's is 256)")
+    ap.add_argument("--ref-warmup-iters", type=int, default=20,
+                    help="reference arm: CG iterations of each (untimed) warm-up solve")
     args = ap.parse_args()
     if args.probe:
         return run_probe(args)

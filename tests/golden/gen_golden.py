@@ -1,9 +1,9 @@
 """Generate the golden fixtures that pin the oracle to the reference.
 
-Run in a checkout that has the reference mounted (REF, default
-/root/reference) after `make -C oracle ref`, which compiles the unmodified
-reference sources (ref/ variant) with oracle/ref_harness.cpp into
-oracle/_ref/ref_harness.  Writes:
+Run with REF set to a miniFE checkout (the directory holding ref/src), after
+`make -C oracle ref REF=...`, which compiles the unmodified reference sources
+(ref/ variant) with oracle/ref_harness.cpp into oracle/_ref/ref_harness.
+Writes:
 
   tests/golden/minife_golden.npz   full arrays for small boxes
   tests/golden/golden_hashes.json  sha256 of every array for larger boxes
@@ -27,7 +27,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(os.path.dirname(HERE))
-REF = os.environ.get("REF", "/root/reference")
+REF = os.environ.get("REF", "")
 HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
 EPS = 2.220446049250313e-16
 
@@ -83,8 +83,10 @@ def utest_known_answer():
 
 
 def main():
+    if not REF or not os.path.isdir(os.path.join(REF, "ref", "src")):
+        sys.exit("set REF to the miniFE checkout (the directory holding ref/src)")
     if not os.path.exists(HARNESS):
-        sys.exit("build the reference harness first: make -C oracle ref")
+        sys.exit("build the reference harness first: make -C oracle ref REF=$REF")
     out = {}
     hashes = {}
     with tempfile.TemporaryDirectory() as tmp:
