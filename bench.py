@@ -264,56 +264,77 @@ def run_gpu(args):
         ta.append(e0.elapsed_time(e1) * 1e-3)
     t_assembly = min(ta)
 
-    x = torch.zeros_like(b)
-    for _ in range(args.warmup):
-        x.zero_()
-        res = M.cg_solve(A, b, x, max_iter=5000, tol=TOL, tol_mode="relative")
-    torch.cuda.synchronize()
+    def time_solves(op):
+        """CUDA-event time per whole FP64 solve with the given operator."""
+        xx = torch.zeros_like(b)
+        for _ in range(args.warmup):
+            xx.zero_()
+            M.cg_solve(A, b, xx, max_iter=5000, tol=TOL, tol_mode="relative", f64_operator=op)
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        its = []
+        for _ in range(args.steps):
+            xx.zero_()
+            r = M.cg_solve(A, b, xx, max_iter=5000, tol=TOL, tol_mode="relative", f64_operator=op)
+            its.append(r.num_iters)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return max_over_ranks(world, e0.elapsed_time(e1) * 1e-3 / args.steps), r, xx
 
     sampler = ClockSampler(dev) if rank == 0 else None
     if sampler:
         sampler.start()
-    barrier(world)
-    torch.cuda.synchronize()
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    iters = []
-    for _ in range(args.steps):
-        x.zero_()
-        res = M.cg_solve(A, b, x, max_iter=5000, tol=TOL, tol_mode="relative")
-        iters.append(res.num_iters)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    barrier(world)
-    t_total = e0.elapsed_time(e1) * 1e-3
-    t_step = max_over_ranks(world, t_total / args.steps)
+    # headline: the FP64 solve as mfe_cg_solve runs it by default (the
+    # verified FP64 stencil operator; its per-call check of every entry of A
+    # and the final residual with the CSR values are inside the timed region)
+    t_step, res, x = time_solves("auto")
     rel = res.normr / res.normr0
     final_rel = res.final_resid / res.normr0
     rc, err = M.verify_solution(*DIMS, x)
+    # the same solve with the CSR values (matvec_std) for every product
+    t_csr, res_csr, x_csr = time_solves("csr")
+    d_ops = float((x - x_csr).norm() / x_csr.norm())
+    del x_csr
 
-    # dominant kernel: the CG's SpMV (with fused p.Ap), timed alone on the
-    # same stream with CUDA events
+    # dominant kernels timed alone on the same stream with CUDA events: the
+    # FP64 stencil SpMV of the headline solve and the CSR SpMV (with its
+    # fused p.Ap in the CSR solve)
     p = torch.randn(n, dtype=torch.float64, device="cuda")
     Ap = torch.empty_like(p)
-    for _ in range(3):
-        M.matvec_and_dot(A, p, Ap)
-    torch.cuda.synchronize()
-    R = 20
-    k0 = torch.cuda.Event(enable_timing=True)
-    k1 = torch.cuda.Event(enable_timing=True)
-    k0.record(stream)
-    for _ in range(R):
-        M.matvec(A, p, Ap)
-    k1.record(stream)
-    torch.cuda.synchronize()
-    t_spmv = k0.elapsed_time(k1) * 1e-3 / R
+    S = M.Stencil64(A)
+
+    def time_kernel(fn, R=20):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        k0 = torch.cuda.Event(enable_timing=True)
+        k1 = torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        for _ in range(R):
+            fn()
+        k1.record(stream)
+        torch.cuda.synchronize()
+        return k0.elapsed_time(k1) * 1e-3 / R
+
+    t_st = time_kernel(lambda: M.matvec_stencil64(S, p, Ap))
+    t_spmv = time_kernel(lambda: M.matvec(A, p, Ap))
     clocks = sampler.stop() if sampler else None
-    # the box-structured kernel reads the values only (columns and row
+    # stencil SpMV: x read once and y written once (16 B/row); 14 FP64
+    # operations per row (class sums 4, two plane partials 8, final add 1,
+    # p.Ap 1; the timed standalone launch skips the dot: 13)
+    st_bytes = 16 * n
+    st_ops = 13 * n
+    # the box-structured CSR kernel reads the values only (columns and row
     # offsets follow from the box): 8 bytes per nonzero + x and y once
     spmv_bytes = nnz * 8 + 2 * n * 8
-    iter_bytes = nnz * 8 + 11 * n * 8
     csr_equiv_bytes = nnz * (8 + 4) + (n + 1) * 4 + 2 * n * 8
+    # CG iteration bytes: stencil SpMV 16 B/row, update 48, p update 24
+    iter_bytes_st = 88 * n
+    iter_bytes_csr = nnz * 8 + 11 * n * 8
     peak, peak_kind = peaks()
     achieved = spmv_bytes / t_spmv / 1e9
     traffic = traffic_from_profile()
@@ -378,6 +399,7 @@ def run_gpu(args):
         rcm, errm = M.verify_solution(*DIMS, xm)
         diff = xm - x64
         mixed = {"value": t_mixed, "unit": "s", "speedup_vs_fp64": t_step / t_mixed,
+                 "speedup_vs_fp64_csr_values": t_csr / t_mixed,
                  "inner_operator": rm.inner_operator,
                  "inner_iterations": rm.num_iters, "reliable_updates": rm.refinements,
                  "refine_k": args.refine_k, "status": rm.status,
@@ -392,8 +414,10 @@ def run_gpu(args):
         del xm, x64
 
     # launches of the timed headline region: per CG iteration the SpMV, the
-    # update and the p update, plus the initial residual and setup per solve
-    gpu_launches = args.steps * (3 * res.num_iters + 2)
+    # update and the p update; per solve the stencil check (table, its reset
+    # and the row-by-row check), the initial residual, the graph's begin
+    # node and the final residual with the CSR values
+    gpu_launches = args.steps * (3 * res.num_iters + 6)
 
     # batched uneven boxes and multi-RHS: measured after the headline system
     # is released, so their stores have the memory
@@ -430,27 +454,45 @@ def run_gpu(args):
                     "no flush needed)",
             "config": workload_config(world, n, nnz),
             "iterations": res.num_iters,
+            "operator": res.inner_operator,
             "final_rel_resid": final_rel, "reported_rel_normr": rel,
             "analytic_check": {"max_err": err, "passed": rc == 0},
             "ms_per_iter": t_step / res.num_iters * 1e3,
-            "cg_effective_gbs": iter_bytes * res.num_iters / t_step / 1e9,
+            "cg_hbm_gbs": iter_bytes_st * res.num_iters / t_step / 1e9,
             "assembly_s": t_assembly,
+            "fp64_csr_values": {
+                "value": t_csr, "unit": "s", "iterations": res_csr.num_iters,
+                "speedup_of_headline": t_csr / t_step,
+                "final_rel_resid": res_csr.final_resid / res_csr.normr0,
+                "rel_l2_diff_vs_headline_x": d_ops,
+                "ms_per_iter": t_csr / res_csr.num_iters * 1e3,
+                "cg_hbm_gbs": iter_bytes_csr * res_csr.num_iters / t_csr / 1e9,
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": traffic,
+                             "kernel": "k_spmv_box<double> (FP64 box-structured CSR SpMV)",
+                             "algorithmic_bytes": spmv_bytes,
+                             "peak_kind": peak_kind + " (HBM copy)",
+                             "csr_equivalent_gbs": csr_equiv_bytes / t_spmv / 1e9,
+                             "fp64_pipe": {"achieved_gops": nnz / t_spmv / 1e9,
+                                           "peak_gops": FP64_PEAK_TFLOPS / 2 * 1e3,
+                                           "frac": nnz / t_spmv / 1e9 / (FP64_PEAK_TFLOPS / 2 * 1e3)}},
+            },
             "mixed": mixed,
             "batch": batch,
             "multi_rhs": multi,
             "adjoint": adjoint,
             "small_30cubed": small,
-            "spmv_f64_gbs": achieved,
-            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": traffic,
-                         "kernel": "k_spmv_box<double> (FP64 box-structured CSR SpMV)",
-                         "algorithmic_bytes": spmv_bytes, "peak_kind": peak_kind + " (HBM copy)",
-                         "csr_equivalent_gbs": csr_equiv_bytes / t_spmv / 1e9,
-                         "fp64_fma": {"achieved_tflops": 2 * nnz / t_spmv / 1e12,
-                                      "peak_tflops": FP64_PEAK_TFLOPS,
-                                      "frac": 2 * nnz / t_spmv / 1e12 / FP64_PEAK_TFLOPS,
-                                      "note": "FP64 FMA pipe, the binding limit on GB300; "
-                                              "peak measured with an FMA-only kernel"}},
+            "roofline": {"bound": "fp64", "achieved": st_ops / t_st / 1e9,
+                         "peak": FP64_PEAK_TFLOPS / 2 * 1e3, "unit": "G FP64 op/s",
+                         "frac": st_ops / t_st / 1e9 / (FP64_PEAK_TFLOPS / 2 * 1e3),
+                         "traffic": None,
+                         "kernel": "k_spmv_st64 (verified FP64 stencil SpMV, 13 FP64 operations "
+                                   "per row without the fused dot)",
+                         "kernel_ms": t_st * 1e3, "algorithmic_ops": st_ops,
+                         "peak_kind": "measured (FP64 FMA-only kernel, one operation per FMA)",
+                         "hbm": {"achieved_gbs": st_bytes / t_st / 1e9, "peak_gbs": peak,
+                                 "frac": st_bytes / t_st / 1e9 / peak,
+                                 "algorithmic_bytes": st_bytes}},
             "e2e": e2e,
             "cpu_baseline": cpu,
             "gpu_launches": gpu_launches,

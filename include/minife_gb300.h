@@ -33,7 +33,7 @@
 extern "C" {
 #endif
 
-#define MFE_ABI_VERSION 2
+#define MFE_ABI_VERSION 3
 
 typedef enum mfe_status {
   MFE_OK = 0,
@@ -156,6 +156,30 @@ mfe_status mfe_csr_convert_f32(mfe_ctx* ctx, const mfe_csr* src, mfe_csr* dst);
  * y = A x.  x and y have A->dtype. */
 mfe_status mfe_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y);
 
+/* The verified FP64 stencil operator of a miniFE box matrix (no counterpart
+ * in the reference; it stands in for matvec_std, SparseMatrix_functions.hpp:
+ * 545-578, on the matrices assemble_FE_data builds): eight mirror-class
+ * weights w[4|dz| + 2|dy| + |dx|] of the interior 27-point stencil and the
+ * Dirichlet diagonal dd, valid for the box's natural-layout vectors. */
+typedef struct mfe_stencil64 {
+  int32_t box_nx, box_ny, box_nz;  /* elements per dimension */
+  int32_t reserved;
+  double w[8];
+  double dd;
+} mfe_stencil64;
+
+/* Check A (FP64, box dimensions set or detectable) on the device, every
+ * entry within 2^-40 of its row's largest magnitude from its class value
+ * (see mfe_cg_opts.f64_operator), and fill *S.  MFE_NOT_SUPPORTED when A is
+ * not such an operator (per-element conductivity, fewer than 4 elements
+ * along a dimension, not a box matrix). */
+mfe_status mfe_stencil64_from_csr(mfe_ctx* ctx, const mfe_csr* A, mfe_stencil64* S);
+
+/* y = S x (device vectors of the box's rows): 14 FP64 operations per row
+ * instead of the CSR kernel's 27 FMAs; within 2^-39 sum_j |a_ij x_j| (plus
+ * rounding) of A x for the A that S was made from. */
+mfe_status mfe_spmv_stencil64(mfe_ctx* ctx, const mfe_stencil64* S, const double* x, double* y);
+
 /* matvec_and_dot (ref/src/SparseMatrix_functions.hpp:491-536): y = A x and
  * *result = x . y (double, host), accumulated in FP64. */
 mfe_status mfe_matvec_and_dot(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
@@ -170,7 +194,7 @@ mfe_status mfe_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
  * program or framework that reserves the device in its own pool and lets no
  * plugin allocate beside it) and latency-critical loops that cannot take the
  * implicit synchronisation of cudaMalloc/cudaFree.  No counterpart in the
- * reference (its dot, Vector_functions.hpp:194-226, runs on the host).
+ * reference.
  *
  * *result (DEVICE pointer, one double) = x . y, accumulated in FP64 in fixed
  * 8192-element chunks (deterministic for a given n), computed on the calling
@@ -180,9 +204,11 @@ mfe_status mfe_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
  * array inside the library (held by every GPU that loads the library until
  * the process exits).  The first call on each device resolves that array's
  * device address (cudaGetSymbolAddress) and should come before any stream
- * capture.  n > MFE_DOT_NOALLOC_MAX_N returns MFE_BAD_ARG and launches
- * nothing.  All calls share the array, so calls that overlap on the GPU race:
- * order them on one stream. */
+ * capture; calls outside a capture resolve it again, so the entry point
+ * stays valid after a device reset, while calls during a capture use the
+ * address resolved before it.  n > MFE_DOT_NOALLOC_MAX_N returns MFE_BAD_ARG
+ * and launches nothing.  All calls share the array, so calls that overlap on
+ * the GPU race: order them on one stream. */
 #define MFE_DOT_NOALLOC_MAX_N ((int64_t)536870912) /* 2^29 elements */
 mfe_status mfe_dot_noalloc(int64_t n, const double* x, const double* y, double* result,
                            void* stream);
@@ -191,10 +217,28 @@ mfe_status mfe_dot_noalloc(int64_t n, const double* x, const double* y, double* 
 mfe_status mfe_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x,
                       double beta, const double* y, double* w);
 
-/* fused_waxpby (ref/src/Vector_functions.hpp:154-185). */
+/* fused_waxpby (ref/src/Vector_functions.hpp:154-185): w = alpha x + beta y
+ * and w2 = alpha2 x2 + beta2 y2 in one pass over the vectors. */
 mfe_status mfe_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x,
                             double beta, const double* y, double* w, double alpha2,
                             const double* x2, double beta2, const double* y2, double* w2);
+
+/* Dot product of FP32 vectors (device) as the mixed-precision solvers form
+ * their alpha/beta and residual reductions: every product and sum in
+ * double-float on the FP32 pipe (TwoProduct + TwoSum, about 48 significant
+ * bits), *result (host) the FP64 sum of the final pair.  No counterpart in
+ * the reference (its dot over Vector<float> returns float,
+ * Vector_functions.hpp:194-226). */
+mfe_status mfe_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y,
+                       double* result);
+
+/* Fault injection for tests of the bounded-wait error path; no counterpart
+ * in the reference.  The next box-structured SpMV launched on ctx outside a
+ * graph capture issues none of its shared-memory copies, so its consumers'
+ * bounded waits run out after wait_ns nanoseconds (1 ms .. 2 s) with no copy
+ * in flight; the call that launched it returns MFE_TIMEOUT (a solve) or
+ * mfe_synchronize does (mfe_spmv).  The context stays usable. */
+mfe_status mfe_inject_wait_timeout(mfe_ctx* ctx, int64_t wait_ns);
 
 /* ------------------------------------------------------------------ */
 /* CG                                                                  */
@@ -243,6 +287,21 @@ typedef struct mfe_cg_opts {
                            (padded values for batches); 1 = always the FP32
                            values.  mfe_cg_result.inner_operator reports
                            which ran. */
+  int32_t f64_operator; /* FP64 solves (mfe_cg_solve without preconditioner):
+                           0 = the verified FP64 stencil operator when A is a
+                           miniFE box operator whose interior stencil is
+                           mirror-symmetric (every box miniFE assembles with
+                           k = 1): every row is dd * x_r (Dirichlet node) or
+                           the interior stencil with the Dirichlet neighbours
+                           zeroed, every entry within 2^-40 of its row's
+                           largest magnitude from its class value (checked on
+                           the device on every call), so the operator is
+                           within 2^-39 of every entry of A; the solve then
+                           stops only once ||b - A x|| computed with the CSR
+                           values meets the tolerance (restarting CG from x
+                           with that residual otherwise).  Else, and with
+                           1, the CSR values (matvec_std).
+                           mfe_cg_result.inner_operator reports which ran. */
 } mfe_cg_opts;
 
 /* Fill opts with the reference's defaults (max_iter 200, absolute tol
@@ -261,10 +320,11 @@ typedef struct mfe_cg_result {
                            (mytimer.hpp:37-43 order); fused kernels are
                            accounted to MATVECDOT and WAXPY */
   int32_t refinements;  /* mixed: outer refinement sweeps */
-  int32_t fp64_spmvs;   /* number of FP64 matvecs performed */
-  int32_t inner_operator; /* mixed solves: the FP32 operator of the inner
-                             iteration, one of mfe_inner_operator; 0 for
-                             FP64 solves */
+  int32_t fp64_spmvs;   /* number of matvecs with the FP64 CSR values */
+  int32_t inner_operator; /* the operator of the CG iteration, one of
+                             mfe_inner_operator: for mixed solves the FP32
+                             one; for FP64 solves MFE_INNER_STENCIL64 or 0
+                             (the CSR values) */
 } mfe_cg_result;
 
 /* mfe_cg_result.inner_operator */
@@ -272,15 +332,19 @@ typedef enum mfe_inner_operator {
   MFE_INNER_NONE = 0,
   MFE_INNER_STENCIL = 1,  /* verified 27-coefficient stencil (x and y only) */
   MFE_INNER_VALUES = 2,   /* FP32 copy of the CSR values */
-  MFE_INNER_PADDED = 3    /* FP32 values padded to fixed-length rows */
+  MFE_INNER_PADDED = 3,   /* FP32 values padded to fixed-length rows */
+  MFE_INNER_STENCIL64 = 4 /* FP64 solves: the verified FP64 stencil operator
+                             (eight mirror-class weights and the Dirichlet
+                             diagonal; see mfe_cg_opts.f64_operator) */
 } mfe_inner_operator;
 
-/* cg_solve (ref/src/cg_solve.hpp:69-229) with matvec_std: solves A x = b
- * from the initial guess in x (device).  FP64 precision follows the
- * reference's loop exactly (x0 copied to p, r = b - A p, then per iteration
- * p update, A p, p.Ap, breakdown test, x and r updates); the loop runs on the
- * device inside one CUDA graph (a conditional while node), with no host
- * round trip per iteration. */
+/* cg_solve (ref/src/cg_solve.hpp:69-229): solves A x = b from the initial
+ * guess in x (device).  FP64 precision follows the reference's loop exactly
+ * (x0 copied to p, r = b - A p, then per iteration p update, A p, p.Ap,
+ * breakdown test, x and r updates), with matvec_std on the CSR values or,
+ * for verified miniFE box operators, the FP64 stencil operator
+ * (opts->f64_operator); the loop runs on the device inside one CUDA graph (a
+ * conditional while node), with no host round trip per iteration. */
 mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                         const mfe_cg_opts* opts, mfe_cg_result* result);
 

@@ -31,7 +31,8 @@ from ._abi import (MFE_F32, MFE_F64, MFE_PREC_F64, MFE_PREC_MIXED, MFE_TOL_ABSOL
 __all__ = [
     "MiniFEError", "Context", "CSRMatrix", "CGResult", "default_context", "box_dims",
     "generate_matrix_structure", "assemble_FE_data", "impose_dirichlet", "box_bc_rows",
-    "build_system", "matvec", "matvec_and_dot", "dot", "waxpby", "fused_waxpby", "cg_solve",
+    "build_system", "matvec", "matvec_and_dot", "dot", "dot_f32", "waxpby", "fused_waxpby",
+    "inject_wait_timeout", "Stencil64", "matvec_stencil64", "cg_solve",
     "cg_solve_host", "cg_solve_multi", "Batch", "batch_solve_boxes", "verify_solution",
     "element_gradient", "to_f32", "spmm", "ELLMatrix", "matvec_ell", "cg_solve_ell",
 ]
@@ -370,6 +371,48 @@ def waxpby(alpha, x, beta, y, w, ctx: Context | None = None):
     return w
 
 
+class Stencil64:
+    """The verified FP64 stencil operator of a miniFE box matrix
+    (mfe_stencil64_from_csr): checked once against every entry of A, then
+    applied by matvec_stencil64 with 14 FP64 operations per row."""
+
+    def __init__(self, A: "CSRMatrix", ctx: Context | None = None):
+        ctx = ctx or default_context()
+        self.s = _abi.MfeStencil64()
+        m = A.c()
+        ctx.check(ctx.lib.mfe_stencil64_from_csr(ctx.h, ctypes.byref(m), ctypes.byref(self.s)),
+                  "mfe_stencil64_from_csr")
+
+    @property
+    def weights(self):
+        return list(self.s.w), self.s.dd
+
+
+def matvec_stencil64(S: Stencil64, x, y, ctx: Context | None = None):
+    """y = S x through the verified FP64 stencil operator."""
+    ctx = ctx or default_context()
+    ctx.check(ctx.lib.mfe_spmv_stencil64(ctx.h, ctypes.byref(S.s), _ptr(x), _ptr(y)),
+              "mfe_spmv_stencil64")
+    return y
+
+
+def dot_f32(x, y, ctx: Context | None = None) -> float:
+    """x.y of FP32 device vectors, accumulated in double-float as the mixed
+    solvers' reductions are (mfe_dot_f32)."""
+    ctx = ctx or default_context()
+    out = ctypes.c_double()
+    ctx.check(ctx.lib.mfe_dot_f32(ctx.h, x.numel(), _ptr(x), _ptr(y), ctypes.byref(out)),
+              "mfe_dot_f32")
+    return out.value
+
+
+def inject_wait_timeout(wait_ns: int = 20_000_000, ctx: Context | None = None):
+    """Test hook: the next box-structured SpMV on the context withholds its
+    copies, so its bounded waits run out after wait_ns (mfe_inject_wait_timeout)."""
+    ctx = ctx or default_context()
+    ctx.check(ctx.lib.mfe_inject_wait_timeout(ctx.h, int(wait_ns)), "mfe_inject_wait_timeout")
+
+
 def fused_waxpby(alpha, x, beta, y, w, alpha2, x2, beta2, y2, w2, ctx: Context | None = None):
     ctx = ctx or default_context()
     ctx.check(ctx.lib.mfe_fused_waxpby(ctx.h, x.numel(), float(alpha), _ptr(x), float(beta),
@@ -387,8 +430,9 @@ class CGResult:
     times: tuple
     refinements: int
     history: list | None = None
-    # mixed solves: the FP32 operator of the inner iteration ("stencil",
-    # "values" or "padded"); "none" for FP64 solves
+    # the operator of the CG iteration: for mixed solves the FP32 one
+    # ("stencil", "values" or "padded"); for FP64 solves "stencil64" (the
+    # verified FP64 stencil operator) or "none" (the CSR values)
     inner_operator: str = "none"
 
     @property
@@ -397,7 +441,8 @@ class CGResult:
 
 
 def _opts(max_iter, tol, tol_mode, precision, refine_k=0, inner_tol=0.0, max_refine=0,
-          record_history=False, A32=None, precond="none", mixed_operator="auto"):
+          record_history=False, A32=None, precond="none", mixed_operator="auto",
+          f64_operator="auto"):
     o = MfeCgOpts()
     _abi.load().mfe_cg_opts_default(ctypes.byref(o))
     o.max_iter = int(max_iter)
@@ -410,6 +455,7 @@ def _opts(max_iter, tol, tol_mode, precision, refine_k=0, inner_tol=0.0, max_ref
     o.record_history = 1 if record_history else 0
     o.precond = {"none": 0, "jacobi": 1}[precond]
     o.mixed_operator = {"auto": 0, "values": 1}[mixed_operator]
+    o.f64_operator = {"auto": 0, "csr": 1}[f64_operator]
     keep = None
     if A32 is not None:
         keep = A32.c()
@@ -428,7 +474,7 @@ def _result(ctx, r: MfeCgResult, record_history: bool) -> CGResult:
     return _cg_result(r, hist)
 
 
-_INNER = {0: "none", 1: "stencil", 2: "values", 3: "padded"}
+_INNER = {0: "none", 1: "stencil", 2: "values", 3: "padded", 4: "stencil64"}
 
 
 def _cg_result(r: MfeCgResult, hist=None) -> CGResult:
@@ -441,18 +487,20 @@ def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
              inner_tol: float = 0.0, max_refine: int = 0, record_history: bool = False,
              A32: CSRMatrix | None = None, allow_breakdown: bool = True,
              precond: str = "none", mixed_operator: str = "auto",
-             ctx: Context | None = None) -> CGResult:
+             f64_operator: str = "auto", ctx: Context | None = None) -> CGResult:
     """cg_solve (ref/src/cg_solve.hpp:69) on device vectors; x holds the
     initial guess and receives the solution.  Breakdown (the reference prints
     an error and returns) is reported in CGResult.status unless
     allow_breakdown is False.  precond="jacobi" runs the Jacobi-preconditioned
     CG (FP64, stops on ||r|| after the update).  mixed_operator="values"
     makes the mixed solver use the FP32 copy of the values even where the
-    verified FP32 stencil operator applies ("auto")."""
+    verified FP32 stencil operator applies ("auto").  f64_operator="csr"
+    makes the FP64 solver use the CSR values (matvec_std) even where the
+    verified FP64 stencil operator applies ("auto")."""
     ctx = ctx or default_context()
     m = A.c()
     o, keep = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine,
-                    record_history, A32, precond, mixed_operator)
+                    record_history, A32, precond, mixed_operator, f64_operator)
     r = MfeCgResult()
     st = ctx.lib.mfe_cg_solve(ctx.h, ctypes.byref(m), _ptr(b), _ptr(x), ctypes.byref(o),
                               ctypes.byref(r))
@@ -572,7 +620,8 @@ def batch_solve_boxes(dims, max_iter: int = 200, tol: float = DBL_EPSILON,
 
 
 def cg_solve_host(row_offsets, cols, vals, b, x, max_iter=200, tol=DBL_EPSILON,
-                  tol_mode="absolute", precision="f64", ctx: Context | None = None) -> CGResult:
+                  tol_mode="absolute", precision="f64", f64_operator="auto",
+                  ctx: Context | None = None) -> CGResult:
     """Drop-in host call: CSR and vectors in host memory (numpy arrays or CPU
     tensors, int32 / float64); x is updated in place."""
     import numpy as np
@@ -585,7 +634,7 @@ def cg_solve_host(row_offsets, cols, vals, b, x, max_iter=200, tol=DBL_EPSILON,
 
     n = (row_offsets.shape[0] if hasattr(row_offsets, "shape") else len(row_offsets)) - 1
     nnz = cols.shape[0]
-    o, _ = _opts(max_iter, tol, tol_mode, precision)
+    o, _ = _opts(max_iter, tol, tol_mode, precision, f64_operator=f64_operator)
     r = MfeCgResult()
     st = ctx.lib.mfe_cg_solve_host(ctx.h, n, nnz, hp(row_offsets), hp(cols), hp(vals), hp(b),
                                    hp(x), ctypes.byref(o), ctypes.byref(r))

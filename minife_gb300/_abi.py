@@ -41,6 +41,7 @@ class MfeCgOpts(ctypes.Structure):
         ("precision", c_int32), ("refine_k", c_int32), ("inner_tol", c_double),
         ("max_refine", c_int32), ("record_history", c_int32),
         ("A32", ctypes.POINTER(MfeCsr)), ("precond", c_int32), ("mixed_operator", c_int32),
+        ("f64_operator", c_int32),
     ]
 
 
@@ -50,6 +51,11 @@ class MfeCgResult(ctypes.Structure):
         ("normr0", c_double), ("final_resid", c_double), ("times", c_double * 5),
         ("refinements", c_int32), ("fp64_spmvs", c_int32), ("inner_operator", c_int32),
     ]
+
+
+class MfeStencil64(ctypes.Structure):
+    _fields_ = [("box_nx", c_int32), ("box_ny", c_int32), ("box_nz", c_int32),
+                ("reserved", c_int32), ("w", c_double * 8), ("dd", c_double)]
 
 
 class MfeEll(ctypes.Structure):
@@ -92,6 +98,10 @@ SIGNATURES = {
                                           _P(c_double)]),
     "mfe_dot": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p, _P(c_double)]),
     "mfe_dot_noalloc": (ctypes.c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
+    "mfe_stencil64_from_csr": (ctypes.c_int, [c_void_p, _P(MfeCsr), _P(MfeStencil64)]),
+    "mfe_spmv_stencil64": (ctypes.c_int, [c_void_p, _P(MfeStencil64), c_void_p, c_void_p]),
+    "mfe_dot_f32": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p, _P(c_double)]),
+    "mfe_inject_wait_timeout": (ctypes.c_int, [c_void_p, c_int64]),
     "mfe_waxpby": (ctypes.c_int, [c_void_p, c_int64, c_double, c_void_p, c_double, c_void_p,
                                   c_void_p]),
     "mfe_fused_waxpby": (ctypes.c_int, [c_void_p, c_int64, c_double, c_void_p, c_double,

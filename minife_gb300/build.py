@@ -36,6 +36,7 @@ SOURCES = {
     "mfe_ell.cu": [],
     "mfe_adjoint.cu": [],
     "mfe_stencil.cu": [],
+    "mfe_stencil64.cu": [],
     "mfe_cg.cu": [],
 }
 

@@ -508,8 +508,75 @@ mfe_status mfe_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double*
                             const double* y, double* w, double alpha2, const double* x2,
                             double beta2, const double* y2, double* w2)
 {
-  MFE_TRY(mfe_waxpby(ctx, n, alpha, x, beta, y, w));
-  return mfe_waxpby(ctx, n, alpha2, x2, beta2, y2, w2);
+  if (!ctx || n < 0 || (n > 0 && (!x || !y || !w || !x2 || !y2 || !w2)))
+    return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  return launch_fused_waxpby(ctx, n, alpha, x, beta, y, w, alpha2, x2, beta2, y2, w2);
+}
+
+mfe_status mfe_stencil64_from_csr(mfe_ctx* ctx, const mfe_csr* A_in, mfe_stencil64* S)
+{
+  if (!ctx || !S) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(check_csr(ctx, A_in));
+  if (A_in->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "the FP64 stencil needs the FP64 matrix");
+  MFE_TRY(set_device(ctx));
+  mfe_csr A = *A_in;
+  if (!csr_is_box(&A)) {
+    int bx, by, bz;
+    MFE_TRY(detect_box(ctx, &A, &bx, &by, &bz));
+    A.box_nx = bx;
+    A.box_ny = by;
+    A.box_nz = bz;
+  }
+  bool ok = false;
+  memset(S, 0, sizeof(*S));
+  if (csr_is_box(&A)) MFE_TRY(stencil64_prepare(ctx, &A, S->w, &S->dd, &ok));
+  if (!ok) {
+    memset(S, 0, sizeof(*S));
+    return fail(ctx, MFE_NOT_SUPPORTED, "A is not a verified miniFE box operator");
+  }
+  S->box_nx = A.box_nx;
+  S->box_ny = A.box_ny;
+  S->box_nz = A.box_nz;
+  return MFE_OK;
+}
+
+mfe_status mfe_spmv_stencil64(mfe_ctx* ctx, const mfe_stencil64* S, const double* x, double* y)
+{
+  if (!ctx || !S || !x || !y || !box_ok(S->box_nx, S->box_ny, S->box_nz) || S->box_nx < 4 ||
+      S->box_ny < 4 || S->box_nz < 4)
+    return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  mfe_csr A;
+  memset(&A, 0, sizeof(A));
+  A.box_nx = S->box_nx;
+  A.box_ny = S->box_ny;
+  A.box_nz = S->box_nz;
+  A.dtype = MFE_F64;
+  return launch_spmv_st64(ctx, &A, S->w, S->dd, x, y, nullptr, nullptr);
+}
+
+mfe_status mfe_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, double* result)
+{
+  if (!ctx || !result || n < 0 || (n > 0 && (!x || !y))) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  if (n == 0) {
+    *result = 0.0;
+    return MFE_OK;
+  }
+  double* d = dev_scalar(ctx);
+  if (!d) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  MFE_TRY(launch_dot_f32(ctx, n, x, y, d));
+  return read_scalar(ctx, d, result);
+}
+
+mfe_status mfe_inject_wait_timeout(mfe_ctx* ctx, int64_t wait_ns)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  if (wait_ns < 1000000 || wait_ns > 2000000000)
+    return fail(ctx, MFE_BAD_ARG, "wait_ns must lie in [1 ms, 2 s]");
+  ctx->inject_wait_ns = (uint64_t)wait_ns;
+  return MFE_OK;
 }
 
 void mfe_cg_opts_default(mfe_cg_opts* o)
@@ -535,7 +602,7 @@ mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double*
   else mfe_cg_opts_default(&o);
   if (o.max_iter < 0 || !(o.tol >= 0.0) ||
       (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED) ||
-      (o.precond != 0 && o.precond != 1))
+      (o.precond != 0 && o.precond != 1) || (o.f64_operator != 0 && o.f64_operator != 1))
     return fail(ctx, MFE_BAD_ARG, "bad CG options");
   MFE_TRY(set_device(ctx));
   if (A->nrows == 0) return MFE_OK;
@@ -619,7 +686,7 @@ mfe_status mfe_adjoint_grad(mfe_ctx* ctx, int nx, int ny, int nz, const double* 
   else mfe_cg_opts_default(&o);
   if (o.max_iter < 0 || !(o.tol >= 0.0) ||
       (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED) ||
-      (o.precond != 0 && o.precond != 1))
+      (o.precond != 0 && o.precond != 1) || (o.f64_operator != 0 && o.f64_operator != 1))
     return fail(ctx, MFE_BAD_ARG, "bad CG options");
   MFE_TRY(set_device(ctx));
   return adjoint_grad(ctx, nx, ny, nz, kappa, u_target, &o, u_out, grad, loss, fwd, adj);

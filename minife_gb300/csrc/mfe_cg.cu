@@ -46,6 +46,23 @@ __global__ void __launch_bounds__(kVecThreads)
   if (grid_reduce_last(bt, partials, ticket, red, &total) && threadIdx.x == 0) *out = total;
 }
 
+// x.y of FP32 vectors with the mixed solvers' reduction: products and sums
+// in double-float (DFAcc: TwoProduct + TwoSum on the FP32 pipe, about 48
+// significant bits), block and grid sums in double-float too, one FP64
+// addition at the end
+__global__ void __launch_bounds__(kVecThreads)
+    k_dot_df(int64_t n, const float* __restrict__ x, const float* __restrict__ y,
+             double* partials, unsigned* ticket, double* out)
+{
+  __shared__ float2 red[32];
+  DFAcc acc;
+  for (int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kVecThreads)
+    acc.add_product(x[i], y[i]);
+  double total;
+  if (grid_reduce_last_df(acc, partials, ticket, red, &total) && threadIdx.x == 0) *out = total;
+}
+
 __global__ void __launch_bounds__(kVecThreads)
     k_waxpby(int64_t n, double alpha, const double* __restrict__ x, double beta,
              const double* __restrict__ y, double* __restrict__ w)
@@ -53,6 +70,22 @@ __global__ void __launch_bounds__(kVecThreads)
   for (int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n;
        i += (int64_t)gridDim.x * kVecThreads)
     w[i] = fma(alpha, x[i], beta * y[i]);
+}
+
+// fused_waxpby (Vector_functions.hpp:154-185): both updates in one pass
+__global__ void __launch_bounds__(kVecThreads)
+    k_fused_waxpby(int64_t n, double alpha, const double* __restrict__ x, double beta,
+                   const double* __restrict__ y, double* w, double alpha2,
+                   const double* __restrict__ x2, double beta2, const double* __restrict__ y2,
+                   double* w2)
+{
+  for (int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kVecThreads) {
+    const double a = fma(alpha, x[i], beta * y[i]);
+    const double c = fma(alpha2, x2[i], beta2 * y2[i]);
+    w[i] = a;
+    w2[i] = c;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -63,13 +96,13 @@ __global__ void k_cg_begin(const CgState* st, cudaGraphConditionalHandle h)
   cudaGraphSetConditional(h, st->cont ? 1u : 0u);
 }
 
-// p = r (k == 1, cg_solve.hpp:153-155) or p = r + beta p (:156-161).
-// Vectorised as double2 when every array is 16-byte aligned (VEC).
+// p = r (k == 1, cg_solve.hpp:153-155, or a restart) or p = r + beta p
+// (:156-161).  Vectorised as double2 when every array is 16-byte aligned (VEC).
 template <bool VEC>
 __global__ void __launch_bounds__(kVecThreads)
     k_cg_p(int64_t n, const double* __restrict__ r, double* __restrict__ p, const CgState* st)
 {
-  const bool first = (st->k == 1);
+  const bool first = (st->k == 1) || st->p_reset;
   const double beta = st->beta;
   const int64_t stride = (int64_t)gridDim.x * kVecThreads;
   int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x;
@@ -103,6 +136,7 @@ __device__ __forceinline__ void cg_after_update(CgState* st, double rr_new)
   const int k = st->k;
   st->rr_new = rr_new;
   st->num_iters = k;
+  st->p_reset = 0;
   const int cont = (k + 1 <= st->max_iter) && (st->normr > st->tol_abs);
   st->cont = cont;
   if (cont) {
@@ -216,6 +250,25 @@ mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
   return check_launch(ctx, "k_dot");
 }
 
+mfe_status launch_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, double* dev_out)
+{
+  RedBufs rb;
+  MFE_TRY(red_bufs(ctx, &rb));
+  k_dot_df<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, x, y, rb.partials, rb.tickets,
+                                                              dev_out);
+  return check_launch(ctx, "k_dot_df");
+}
+
+mfe_status launch_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
+                               const double* y, double* w, double alpha2, const double* x2,
+                               double beta2, const double* y2, double* w2)
+{
+  if (n <= 0) return MFE_OK;
+  k_fused_waxpby<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, alpha, x, beta, y, w, alpha2,
+                                                                    x2, beta2, y2, w2);
+  return check_launch(ctx, "k_fused_waxpby");
+}
+
 mfe_status launch_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
                          const double* y, double* w)
 {
@@ -233,6 +286,11 @@ struct CgBufs {
   double* Ap;
   CgState* st;
   double* history;
+  // the verified FP64 stencil operator (mfe_stencil64.cu) instead of the CSR
+  // values: its eight mirror-class weights and the Dirichlet diagonal
+  bool st64 = false;
+  double w8[8] = {};
+  double dd = 0.0;
 };
 
 }  // namespace mfe
@@ -241,8 +299,10 @@ struct mfe_cg_graph {
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
   cudaGraphConditionalHandle handle = 0;
-  // what the graph was built for
+  // what the graph was built for: operands, and the stencil operator's
+  // weights (kernel parameters baked into the graph) when it runs
   const void* key[10] = {};
+  double op[10] = {};
   int64_t n = 0;
   cudaStream_t stream = nullptr;
 };
@@ -289,6 +349,7 @@ static mfe_status launch_cg_spmv(mfe_ctx* ctx, const mfe_csr* A, const CgBufs& B
   sink.partials = rb.partials;
   sink.ticket = rb.tickets;
   sink.out = rb.scalars;
+  if (B.st64) return launch_spmv_st64(ctx, A, B.w8, B.dd, B.p, B.Ap, &sink, B.st);
   return launch_spmv(ctx, A, B.p, B.Ap, &sink, nullptr, B.st);
 }
 
@@ -384,6 +445,10 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   }
 
   CgBufs B;
+  // the verified FP64 stencil operator: on every call, before anything else
+  // uses the pinned host scratch (its check reads the class table through it)
+  if (o->f64_operator == 0 && csr_is_box(&A))
+    MFE_TRY(stencil64_prepare(ctx, &A, B.w8, &B.dd, &B.st64));
   B.r = static_cast<double*>(workspace(ctx, "cg.r", sizeof(double) * std::max<int64_t>(n, 1)));
   B.p = static_cast<double*>(workspace(ctx, "cg.p", sizeof(double) * std::max<int64_t>(n, 1)));
   B.Ap = static_cast<double*>(workspace(ctx, "cg.Ap", sizeof(double) * std::max<int64_t>(n, 1)));
@@ -428,62 +493,104 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   const void* key[10] = {A.row_offsets, A.cols, A.vals, x, b, B.r, B.p, B.Ap, B.st,
                          (const void*)(uintptr_t)(((int64_t)A.box_nx << 42) ^
                                                   ((int64_t)A.box_ny << 21) ^ A.box_nz)};
+  double op[10] = {B.st64 ? 1.0 : 0.0, B.dd};
+  for (int c = 0; c < 8; ++c) op[2 + c] = B.w8[c];
   mfe_cg_graph* g = ctx->cg_graph;
-  if (!g || g->n != n || g->stream != ctx->stream || memcmp(g->key, key, sizeof(key)) != 0) {
+  if (!g || g->n != n || g->stream != ctx->stream || memcmp(g->key, key, sizeof(key)) != 0 ||
+      memcmp(g->op, op, sizeof(op)) != 0) {
     cg_graph_destroy(g);
     ctx->cg_graph = nullptr;
     MFE_TRY(build_graph(ctx, &A, x, B, rb, &g));
     memcpy(g->key, key, sizeof(key));
+    memcpy(g->op, op, sizeof(op));
     g->n = n;
     g->stream = ctx->stream;
     ctx->cg_graph = g;
   }
 
   int status = MFE_OK;
+  int csr_products = 1;        // the initial residual
+  double true_resid = -1.0;    // ||b - A x|| with the CSR values (stencil solves)
   // MFE_CG_EAGER=1 issues the same three kernels per iteration as ordinary
   // launches from the host (one small state read per iteration) instead of
   // the graph's device-side loop: identical work, visible to per-kernel
   // profilers that do not descend into conditional graph nodes
   const bool eager = getenv("MFE_CG_EAGER") != nullptr;
-  for (int round = 0;; ++round) {
-    if (eager) {
-      for (;;) {
-        MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
-        MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-        if (!hs->cont || hs->check_pending || hs->err) break;
-        MFE_TRY(launch_cg_p(ctx, n, B));
-        MFE_TRY(launch_cg_spmv(ctx, &A, B, rb));
-        MFE_TRY(launch_cg_update(ctx, n, x, B, rb, 0, 0));
+  for (int restarts = 0;; ++restarts) {
+    for (int round = 0;; ++round) {
+      if (eager) {
+        for (;;) {
+          MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+          MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+          if (!hs->cont || hs->check_pending || hs->err) break;
+          MFE_TRY(launch_cg_p(ctx, n, B));
+          MFE_TRY(launch_cg_spmv(ctx, &A, B, rb));
+          MFE_TRY(launch_cg_update(ctx, n, x, B, rb, 0, 0));
+        }
+      } else {
+        MFE_CUDA_TRY(ctx, cudaGraphLaunch(g->exec, ctx->stream));
       }
-    } else {
-      MFE_CUDA_TRY(ctx, cudaGraphLaunch(g->exec, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (hs->err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during CG");
+      if (!hs->check_pending) break;
+      // breakdown() (cg_solve.hpp:49-67): |p.Ap| <= 100 ||Ap|| ||p|| eps
+      double* d = rb.scalars + 2;
+      MFE_TRY(launch_dot(ctx, n, B.Ap, B.Ap, d));
+      MFE_TRY(launch_dot(ctx, n, B.p, B.p, d + 1));
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hn, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      const double norms[2] = {hn[0], hn[1]};
+      const double pAp = hs->pAp;
+      const bool brk = pAp < 0 ||
+                       std::fabs(pAp) <= 100 * std::sqrt(norms[0]) * std::sqrt(norms[1]) *
+                                             2.220446049250313e-16;
+      if (brk) {
+        status = MFE_BREAKDOWN;
+        break;
+      }
+      hs->brkdown_tol = 0.1 * pAp;
+      hs->check_pending = 0;
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(B.st, hs, sizeof(CgState), cudaMemcpyHostToDevice, ctx->stream));
+      MFE_TRY(launch_cg_update(ctx, n, x, B, rb, 0, 0));
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      if (!hs->cont) break;
     }
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (hs->err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during CG");
-    if (!hs->check_pending) break;
-    // breakdown() (cg_solve.hpp:49-67): |p.Ap| <= 100 ||Ap|| ||p|| eps
-    double* d = rb.scalars + 2;
-    MFE_TRY(launch_dot(ctx, n, B.Ap, B.Ap, d));
-    MFE_TRY(launch_dot(ctx, n, B.p, B.p, d + 1));
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hn, d, 2 * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    const double norms[2] = {hn[0], hn[1]};
-    const double pAp = hs->pAp;
-    const bool brk = pAp < 0 ||
-                     std::fabs(pAp) <= 100 * std::sqrt(norms[0]) * std::sqrt(norms[1]) *
-                                           2.220446049250313e-16;
-    if (brk) {
-      status = MFE_BREAKDOWN;
+    // A stencil solve that met the loop's test is checked with the CSR
+    // values: r = b - A x (written to r, the restart residual if it is
+    // needed) and ||r|| against the same tolerance.  Should the operator's
+    // rounding-level difference from A ever matter, CG restarts from x with
+    // the true residual (at most kMaxRestarts times, within max_iter).
+    if (!B.st64 || status != MFE_OK || !(hs->normr <= hs->tol_abs)) break;
+    {
+      DotSink sink;
+      sink.partials = rb.partials;
+      sink.ticket = rb.tickets;
+      sink.out = rb.scalars + 4;
+      MFE_TRY(launch_spmv(ctx, &A, x, B.r, &sink, b, nullptr));
+      ++csr_products;
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hn, rb.scalars + 4, sizeof(double), cudaMemcpyDeviceToHost,
+                                        ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    const double rr = hn[0];
+    true_resid = std::sqrt(std::max(rr, 0.0));
+    constexpr int kMaxRestarts = 3;
+    if (true_resid <= hs->tol_abs) break;
+    if (restarts >= kMaxRestarts || hs->num_iters + 1 > max_iter) {
+      status = MFE_MAXITER;
+      fail(ctx, MFE_MAXITER, "FP64 stencil CG: the CSR residual stayed above the tolerance");
       break;
     }
-    hs->brkdown_tol = 0.1 * pAp;
+    hs->rtrans = rr;
+    hs->rr_new = rr;
+    hs->normr = true_resid;
+    hs->k = hs->num_iters + 1;
+    hs->p_reset = 1;
     hs->check_pending = 0;
+    hs->cont = hs->normr > hs->tol_abs ? 1 : 0;
     MFE_CUDA_TRY(ctx, cudaMemcpyAsync(B.st, hs, sizeof(CgState), cudaMemcpyHostToDevice, ctx->stream));
-    MFE_TRY(launch_cg_update(ctx, n, x, B, rb, 0, 0));
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (!hs->cont) break;
   }
   MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
@@ -494,11 +601,12 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   res->status = status;
   res->normr = hs->normr;
   res->normr0 = hs->normr0;
-  res->final_resid = std::sqrt(std::max(hs->rr_new, 0.0));
+  res->final_resid = true_resid >= 0.0 ? true_resid : std::sqrt(std::max(hs->rr_new, 0.0));
   for (double& t : res->times) t = 0.0;
   res->times[4] = ms * 1e-3;
   res->refinements = 0;
-  res->fp64_spmvs = hs->num_iters + 1;
+  res->fp64_spmvs = B.st64 ? csr_products : hs->num_iters + 1;
+  res->inner_operator = B.st64 ? MFE_INNER_STENCIL64 : MFE_INNER_NONE;
   if (o->record_history) {
     const int cnt = hs->num_iters + 1;
     ctx->history.resize(cnt);

@@ -27,6 +27,7 @@ struct CgState {
   int record;          // write normr of each iteration to history
   unsigned err;        // kernel error flags (mfe_common.cuh)
   int tol_mode;        // 0 absolute, 1 relative to normr0 (tol kept in tol_abs until init)
+  int p_reset;         // the next p update is p = r (a restart from the true residual)
   double* history;     // device, max_iter + 1 entries (when record)
 };
 

@@ -147,14 +147,15 @@ __device__ __forceinline__ uint64_t global_ns()
 constexpr uint64_t kWaitLimitNs = 2000000000ull;
 
 // Bounded wait; returns false (and the caller records ERR_WAIT_TIMEOUT) if
-// the phase did not complete within kWaitLimitNs (or kMaxPolls polls).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity)
+// the phase did not complete within limit_ns (or kMaxPolls polls).
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity,
+                                                  uint64_t limit_ns = kWaitLimitNs)
 {
   if (mbar_try_wait(bar, parity)) return true;
   const uint64_t t0 = global_ns();
   for (unsigned i = 1; i < kMaxPolls; ++i) {
     if (mbar_try_wait(bar, parity)) return true;
-    if ((i & 63u) == 0 && global_ns() - t0 > kWaitLimitNs) return false;
+    if ((i & 63u) == 0 && global_ns() - t0 > limit_ns) return false;
   }
   return false;
 }
@@ -177,19 +178,31 @@ __device__ __forceinline__ void bulk_g2s(void* smem_dst, const void* gmem_src, u
 // FP64-accumulated dots of FP32 vectors spend their one FP64 operation per
 // element on the FMA.  Built from the IEEE-754 binary32/binary64 layouts:
 // the exponent is rebiased by 1023 - 127 = 896 and the 23-bit fraction moves
-// to the top of the 52-bit one.  Subnormal floats (magnitude < 2^-126)
-// contribute a signed zero.
+// to the top of the 52-bit one.  A subnormal float f * 2^-149 (0 < f < 2^23)
+// is normal in binary64: with h the position of f's leading bit it is
+// 2^(h - 149) * (f / 2^h), exponent field h - 149 + 1023, and f's bits below
+// h become the top of the fraction.
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ double f2d_exact(float f)
 {
   const uint32_t u = __float_as_uint(f);
   const uint32_t e = (u >> 23) & 0xffu;
+  const uint32_t f23 = u & 0x7fffffu;
   const uint64_t sign = (uint64_t)(u & 0x80000000u) << 32;
-  const uint64_t frac = (uint64_t)(u & 0x7fffffu) << 29;
+  const uint64_t frac = (uint64_t)f23 << 29;
   uint64_t bits;
-  if (e == 0u) bits = sign;
-  else if (e == 0xffu) bits = sign | 0x7ff0000000000000ull | frac;
-  else bits = sign | ((uint64_t)(e + 896u) << 52) | frac;
+  if (e == 0u) {
+    if (f23 == 0u) {
+      bits = sign;
+    } else {
+      const int h = 31 - __clz((int)f23);
+      bits = sign | ((uint64_t)(h + 874) << 52) | (((uint64_t)f23 << (52 - h)) & 0xfffffffffffffull);
+    }
+  } else if (e == 0xffu) {
+    bits = sign | 0x7ff0000000000000ull | frac;
+  } else {
+    bits = sign | ((uint64_t)(e + 896u) << 52) | frac;
+  }
   return __longlong_as_double((long long)bits);
 }
 

@@ -31,6 +31,9 @@ struct mfe_ctx {
   std::vector<double> history;
   mfe_csr f32_copy{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  // mfe_inject_wait_timeout: the next box-structured SpMV launched outside a
+  // graph capture withholds its copies; its waits give up after this long
+  uint64_t inject_wait_ns = 0;
 };
 
 namespace mfe {
@@ -126,6 +129,24 @@ mfe_status stencil_grid(mfe_ctx* ctx, const float* coef, int* grid);
 mfe_status launch_spmv_stencil(mfe_ctx* ctx, const mfe_csr* A, const float* coef, const float* x,
                                float* y, const DotSink* sink, int grid, unsigned* err);
 
+// ---- FP64 stencil operator of the FP64 CG (mfe_stencil64.cu; its check in
+// mfe_stencil.cu) ----
+// Tolerance of the FP64 operator: every entry of A within 2^-kSt64TolExp of
+// its row's largest magnitude from its class row, every class-row entry
+// within the same bound of its mirror-class weight, so the operator stays
+// within 2^-(kSt64TolExp - 1) of every entry of A.
+constexpr int kSt64TolExp = 40;
+// checks that A64 is a miniFE box operator whose interior stencil is
+// mirror-symmetric, to the FP64 bound above, row by row on the device; on
+// success w8[c] is the weight of class c = 4|dz| + 2|dy| + |dx| and dd the
+// Dirichlet diagonal
+mfe_status stencil64_prepare(mfe_ctx* ctx, const mfe_csr* A64, double* w8, double* dd, bool* ok);
+// y = S x in FP64 on natural-layout vectors (A's box dimensions), with x.y
+// into the CG state (pAp and the breakdown pre-test) when cg_state is set,
+// else into sink->out (when sink is set)
+mfe_status launch_spmv_st64(mfe_ctx* ctx, const mfe_csr* A, const double* w8, double dd,
+                            const double* x, double* y, const DotSink* sink, void* cg_state);
+
 // ---- mixed-precision CG (mfe_mixed.cu) ----
 // Reliable-update policy options of the mixed solvers: an update is due once
 // the recursive residual has fallen by inner_tol since the last one (0: 0.01,
@@ -184,6 +205,11 @@ mfe_status launch_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y,
                       double* dev_out);
 mfe_status launch_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
                          const double* y, double* w);
+mfe_status launch_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
+                               const double* y, double* w, double alpha2, const double* x2,
+                               double beta2, const double* y2, double* w2);
+// x.y of FP32 vectors accumulated in double-float (the mixed solvers' dots)
+mfe_status launch_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, double* dev_out);
 mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                          const mfe_cg_opts* opts, mfe_cg_result* res);
 void cg_graph_destroy(mfe_cg_graph* g);

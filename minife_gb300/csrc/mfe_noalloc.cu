@@ -60,7 +60,12 @@ __global__ void __launch_bounds__(kThreads)
   if (grid_reduce_last(bt, scratch, ticket, red, &total) && threadIdx.x == 0) *result = total;
 }
 
-// Device address of g_noalloc_scratch per device, resolved once.
+// Device address of g_noalloc_scratch per device.  Resolved at set-up (the
+// first call on the device), and again on every call that is not being
+// captured into a graph: the lookup allocates nothing, and a device reset
+// (cudaDeviceReset, a new primary context) loads the module again at another
+// address, which a cached pointer would miss.  Calls during a capture use
+// the address resolved before it.
 struct DeviceScratch {
   bool ready = false;
   double* ptr = nullptr;
@@ -82,12 +87,18 @@ extern "C" mfe_status mfe_dot_noalloc(int64_t n, const double* x, const double* 
     cudaGetLastError();
     return MFE_CUDA_ERR;
   }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cs) != cudaSuccess) {
+    cudaGetLastError();
+    return MFE_CUDA_ERR;
+  }
   double* scratch = nullptr;
   {
-    // set-up, once per device, with that device current: the host-side name
-    // g_noalloc_scratch is only a stand-in, the kernel needs the device address
+    // set-up with that device current: the host-side name g_noalloc_scratch
+    // is only a stand-in, the kernel needs the device address
     std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (!g_scratch[dev].ready) {
+    if (!g_scratch[dev].ready || cs == cudaStreamCaptureStatusNone) {
       void* p = nullptr;
       if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || p == nullptr) {
         cudaGetLastError();
@@ -98,7 +109,6 @@ extern "C" mfe_status mfe_dot_noalloc(int64_t n, const double* x, const double* 
     }
     scratch = g_scratch[dev].ptr;
   }
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
   // the ticket must start at zero; it may hold a stale count if an earlier
   // launch on this device did not complete
   if (cudaMemsetAsync(scratch + kMaxBlocks, 0, sizeof(double), s) != cudaSuccess) {

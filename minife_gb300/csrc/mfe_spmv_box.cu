@@ -49,6 +49,10 @@ struct BoxParams {
   float* y32;          // BOX_RESID: when set, the residual is written as FP32 here
   int y32_pad;         // y32 rows are (Nx + y32_pad) long: row r goes to r + (r / Nx) * y32_pad
   const int* gate;     // when set and *gate == 0 the launch does nothing
+  // fault injection (mfe_inject_wait_timeout): nonzero = the producer
+  // issues no copy and arrives nowhere, and the consumers' bounded waits on
+  // the first stage give up after this many nanoseconds
+  uint64_t withhold_ns;
 };
 
 template <int MODE>
@@ -112,7 +116,7 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
   bool ok = true;
   if (warp == 0) {
     // ---------------- producer ----------------
-    if (lane == 0) {
+    if (lane == 0 && P.withhold_ns == 0) {
       int it = 0;
       unsigned issued[S];
       for (int s = 0; s < S; ++s) issued[s] = 0;
@@ -196,7 +200,8 @@ __global__ void __launch_bounds__(ROWS + 32) k_spmv_box(BoxParams<T> P)
       const int iy = rem / P.Nx;
       const int ix = rem - iy * P.Nx;
       const int64_t roff = row_offset(ix, iy, iz, P.Nx, P.Ny, P.Nz);
-      if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1))) {
+      if (!mbar_wait_bounded(&full[s], (unsigned)((it / S) & 1),
+                             P.withhold_ns ? P.withhold_ns : kWaitLimitNs)) {
         atomicOr(P.err, ERR_WAIT_TIMEOUT);
         ok = false;
         break;
@@ -500,6 +505,17 @@ static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
   P.err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
+  P.withhold_ns = 0;
+  if (ctx->inject_wait_ns) {
+    // one-shot, and only for a launch that runs now (not one being captured
+    // into a graph, which would replay it)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    MFE_CUDA_TRY(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+      P.withhold_ns = ctx->inject_wait_ns;
+      ctx->inject_wait_ns = 0;
+    }
+  }
   MFE_CUDA_TRY(ctx, box_configure(ctx->device));
   const size_t smem = box_smem<T>(sh.rows, sh.stages);
   const int64_t ntiles = ceil_div(A->nrows, sh.rows);

@@ -72,17 +72,19 @@ __host__ __device__ __forceinline__ bool st_has(int c, int N)
   return i >= 0 && i < N && st_cls(i, N) == c;
 }
 
-// one thread per class: the class's representative row rounded to FP32 in
-// slot order (dz, dy, dx), zeros for missing neighbours
+// one thread per class: the class's representative row in the table's type
+// (rounded to FP32, or exact in FP64) in slot order (dz, dy, dx), zeros for
+// missing neighbours
+template <typename TT>
 __global__ void k_st_table(int Nx, int Ny, int Nz, const double* __restrict__ vals,
-                           float* __restrict__ table)
+                           TT* __restrict__ table)
 {
   const int c = blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= 125) return;
   const int cx = c % 5, cy = (c / 5) % 5, cz = c / 25;
-  float* out = table + c * 28;
+  TT* out = table + c * 28;
   if (!st_has(cx, Nx) || !st_has(cy, Ny) || !st_has(cz, Nz)) {
-    for (int k = 0; k < 28; ++k) out[k] = 0.0f;  // no row has this class
+    for (int k = 0; k < 28; ++k) out[k] = TT(0);  // no row has this class
     return;
   }
   const int ix = st_rep(cx, Nx), iy = st_rep(cy, Ny), iz = st_rep(cz, Nz);
@@ -93,27 +95,33 @@ __global__ void k_st_table(int Nx, int Ny, int Nz, const double* __restrict__ va
       for (int dx = -1; dx <= 1; ++dx, ++slot) {
         const bool in = ix + dx >= 0 && ix + dx < Nx && iy + dy >= 0 && iy + dy < Ny &&
                         iz + dz >= 0 && iz + dz < Nz;
-        out[slot] = in ? (float)vals[k++] : 0.0f;
+        out[slot] = in ? (TT)vals[k++] : TT(0);
       }
-  out[27] = 0.0f;
+  out[27] = TT(0);
 }
 
-// every entry a against its class row's value s (FP32, widened exactly):
-// |a - s| <= tol = 2^-22 max|a_row|, checked on the FP64 bit patterns with
+__device__ __forceinline__ double tab_widen(float v) { return f2d_exact(v); }
+__device__ __forceinline__ double tab_widen(double v) { return v; }
+
+// every entry a against its class row's value s (FP32 widened exactly, or
+// FP64): |a - s| <= tol = 2^-TE max|a_row| (TE = 22 for the FP32 operator,
+// 40 for the FP64 one), checked on the FP64 bit patterns with
 // integer operations only (GB300's FP64 pipe is far too slow for 27
 // comparisons per row) through two sufficient conditions: both |a| and |s|
 // at most tol / 2 (the cancellation noise of entries that are zero in exact
 // arithmetic), or |s| >= 2 tol, the same sign and the patterns at most
-// 2^(e_tol - e_s + 51) apart (e: unbiased exponents), which bounds
-// |a - s| by 2^e_tol <= tol.  Anything else counts as a mismatch.  A warp
+// 2^(e_tol - e_s + 51) apart (e: unbiased exponents; the shift lies in
+// [51 - TE, 50]), which bounds |a - s| by 2^e_tol <= tol.  Anything else
+// counts as a mismatch.  A warp
 // takes 32
 // consecutive rows: their values are one contiguous range of at most
 // 32 * 27, loaded coalesced into shared memory, then each lane checks its
 // own row from there.
 constexpr int kVW = 4;  // warps per block (27 KB of static shared memory)
+template <typename TT, int TE>
 __global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
                                                         const double* __restrict__ vals,
-                                                        const float* __restrict__ table, unsigned* bad)
+                                                        const TT* __restrict__ table, unsigned* bad)
 {
   __shared__ double sv[kVW][32 * 27];
   const int n = Nx * Ny * Nz, NxNy = Nx * Ny;
@@ -129,13 +137,13 @@ __global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
     const int r = r0 + lane;
     if (r < n) {
       const int iz = r / NxNy, rem = r - iz * NxNy, iy = rem / Nx, ix = rem - iy * Nx;
-      const float* s = table + (st_cls(ix, Nx) + 5 * st_cls(iy, Ny) + 25 * st_cls(iz, Nz)) * 28;
+      const TT* s = table + (st_cls(ix, Nx) + 5 * st_cls(iy, Ny) + 25 * st_cls(iz, Nz)) * 28;
       const double* a = w + (row_offset(ix, iy, iz, Nx, Ny, Nz) - kw);
       constexpr long long kMag = 0x7fffffffffffffffll, kOne = 1ll << 52;  // kOne: one binade
       const int len = nbr(ix, Nx) * nbr(iy, Ny) * nbr(iz, Nz);
       long long amax = 0;
       for (int t = 0; t < len; ++t) amax = max(amax, __double_as_longlong(a[t]) & kMag);
-      const long long tol = amax - 22 * kOne;  // 2^-22 max|a_row| (bit pattern)
+      const long long tol = amax - TE * kOne;  // 2^-TE max|a_row| (bit pattern)
       // a normal tol / 2, and no infinite or NaN entry in the row
       bool good = tol >= 2 * kOne && amax < 0x7ff0000000000000ll;
       const long long half = tol - kOne, twice = tol + kOne;
@@ -147,10 +155,10 @@ __global__ void __launch_bounds__(kVW * 32) k_st_verify(int Nx, int Ny, int Nz,
             const bool in = ix + dx >= 0 && ix + dx < Nx && iy + dy >= 0 && iy + dy < Ny &&
                             iz + dz >= 0 && iz + dz < Nz;
             const long long ab = in ? __double_as_longlong(a[q++]) : 0ll;
-            const long long sb = __double_as_longlong(f2d_exact(s[slot]));
+            const long long sb = __double_as_longlong(tab_widen(s[slot]));
             const long long am = ab & kMag, sm = sb & kMag;  // sm finite: class rows are checked on the host
             const bool small = am <= half && sm <= half;
-            const int sh = e_tol - (int)(sm >> 52) + 51;  // in [28, 50] when sm >= twice
+            const int sh = e_tol - (int)(sm >> 52) + 51;  // in [51 - TE, 50] when sm >= twice
             const long long d = ab - sb;
             const bool big = sm >= twice && (ab ^ sb) >= 0 && sh >= 0 &&
                              d <= (1ll << sh) && d >= -(1ll << sh);
@@ -442,11 +450,13 @@ __global__ void __launch_bounds__(kS2P / 2 + 32, kSep ? 3 : 2)
 }
 
 // The model check of the class rows (host): Dirichlet classes hold dd on the
-// diagonal only, the others the interior row with Dirichlet neighbours zeroed.
-bool st_model(int Nx, int Ny, int Nz, const float* tab, float* coef, float* dd)
+// diagonal only, the others the interior row with Dirichlet neighbours
+// zeroed, each entry within 2^-TE of the class row's largest magnitude.
+template <typename TT, int TE>
+bool st_model(int Nx, int Ny, int Nz, const TT* tab, TT* coef, TT* dd)
 {
   if (!st_has(2, Nx) || !st_has(2, Ny) || !st_has(2, Nz)) return false;
-  const float* sI = tab + (2 + 5 * 2 + 25 * 2) * 28;
+  const TT* sI = tab + (2 + 5 * 2 + 25 * 2) * 28;
   *dd = tab[13];  // class (0, 0, 0): node (0, 0, 0), a Dirichlet node
   for (int k = 0; k < 27; ++k) coef[k] = sI[k];
   for (int c = 0; c < 125; ++c) {
@@ -454,13 +464,13 @@ bool st_model(int Nx, int Ny, int Nz, const float* tab, float* coef, float* dd)
     if (!st_has(cx, Nx) || !st_has(cy, Ny) || !st_has(cz, Nz)) continue;
     const int ix = st_rep(cx, Nx), iy = st_rep(cy, Ny), iz = st_rep(cz, Nz);
     const bool dir = ix == 0 || ix == Nx - 1 || iy == 0 || iy == Ny - 1 || iz == 0 || iz == Nz - 1;
-    const float* s = tab + c * 28;
-    float amax = 0.0f;
+    const TT* s = tab + c * 28;
+    TT amax = TT(0);
     for (int k = 0; k < 27; ++k) {
       if (!std::isfinite(s[k])) return false;
       amax = std::max(amax, std::fabs(s[k]));
     }
-    const double tol = std::ldexp((double)amax, -22);
+    const double tol = std::ldexp((double)amax, -TE);
     int slot = 0;
     for (int dz = -1; dz <= 1; ++dz)
       for (int dy = -1; dy <= 1; ++dy)
@@ -494,47 +504,45 @@ int64_t stencil_ghost(const mfe_csr* A)
   return NP + Nxp + 8;
 }
 
-mfe_status stencil_prepare_box(mfe_ctx* ctx, int Nx, int Ny, int Nz, const double* vals, float* coef,
-                               bool* ok)
+namespace {
+
+// the class table (device, TT), the row-by-row check against it and the
+// host model check; coef receives the interior stencil and dd
+template <typename TT, int TE>
+mfe_status prepare_tab(mfe_ctx* ctx, const char* ws_name, int Nx, int Ny, int Nz, const double* vals,
+                       TT* coef, bool* ok)
 {
   *ok = false;
   if (Nx < 5 || Ny < 5 || Nz < 5) return MFE_OK;  // no interior class
-  float* table = static_cast<float*>(workspace(ctx, "stencil.table", sizeof(float) * kSTable + 16));
+  TT* table = static_cast<TT*>(workspace(ctx, ws_name, sizeof(TT) * kSTable + 16));
   if (!table) return fail(ctx, MFE_OOM, "stencil workspace allocation failed");
   unsigned* bad = reinterpret_cast<unsigned*>(table + kSTable);
-  k_st_table<<<1, 128, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table);
+  k_st_table<TT><<<1, 128, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table);
   MFE_TRY(check_launch(ctx, "k_st_table"));
   MFE_CUDA_TRY(ctx, cudaMemsetAsync(bad, 0, sizeof(unsigned), ctx->stream));
   const int64_t n = (int64_t)Nx * Ny * Nz;
   const int blocks = (int)std::max<int64_t>(
       1, std::min<int64_t>(ceil_div(n, (int64_t)kVW * 32),
-                           (int64_t)resident_blocks(ctx, (const void*)k_st_verify, kVW * 32, 0)));
-  k_st_verify<<<blocks, kVW * 32, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table, bad);
+                           (int64_t)resident_blocks(ctx, (const void*)k_st_verify<TT, TE>, kVW * 32, 0)));
+  k_st_verify<TT, TE><<<blocks, kVW * 32, 0, ctx->stream>>>(Nx, Ny, Nz, vals, table, bad);
   MFE_TRY(check_launch(ctx, "k_st_verify"));
-  float* host = static_cast<float*>(host_scratch(ctx, sizeof(float) * kSTable + 16));
+  TT* host = static_cast<TT*>(host_scratch(ctx, sizeof(TT) * kSTable + 16));
   if (!host) return fail(ctx, MFE_OOM, "pinned host scratch allocation failed");
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(host, table, sizeof(float) * kSTable + sizeof(unsigned),
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(host, table, sizeof(TT) * kSTable + sizeof(unsigned),
                                     cudaMemcpyDeviceToHost, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   unsigned hb;
   memcpy(&hb, host + kSTable, sizeof(unsigned));
-  *ok = hb == 0 && st_model(Nx, Ny, Nz, host, coef, coef + 27);
+  *ok = hb == 0 && st_model<TT, TE>(Nx, Ny, Nz, host, coef, coef + 27);
   return MFE_OK;
 }
 
-mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok)
+template <typename TT, int TE>
+bool mirror_classes(const TT* coef, TT* w8)
 {
-  *ok = false;
-  if (A64->box_nx <= 0 || A64->box_ny <= 0 || A64->box_nz <= 0) return MFE_OK;
-  return stencil_prepare_box(ctx, A64->box_nx + 1, A64->box_ny + 1, A64->box_nz + 1,
-                             static_cast<const double*>(A64->vals), coef, ok);
-}
-
-bool stencil_mirror_classes(const float* coef, float* w8)
-{
-  float amax = 0.0f;
+  TT amax = TT(0);
   for (int k = 0; k < 27; ++k) amax = std::max(amax, std::fabs(coef[k]));
-  const double tol = std::ldexp((double)amax, -22);
+  const double tol = std::ldexp((double)amax, -TE);
   for (int c = 0; c < 8; ++c) {
     const int az = c >> 2, ay = (c >> 1) & 1, ax = c & 1;
     w8[c] = coef[(az + 1) * 9 + (ay + 1) * 3 + (ax + 1)];
@@ -545,6 +553,39 @@ bool stencil_mirror_classes(const float* coef, float* w8)
     if (!(std::fabs((double)coef[k] - (double)w8[c]) <= tol)) return false;
   }
   return true;
+}
+
+}  // namespace
+
+mfe_status stencil_prepare_box(mfe_ctx* ctx, int Nx, int Ny, int Nz, const double* vals, float* coef,
+                               bool* ok)
+{
+  return prepare_tab<float, 22>(ctx, "stencil.table", Nx, Ny, Nz, vals, coef, ok);
+}
+
+mfe_status stencil_prepare(mfe_ctx* ctx, const mfe_csr* A64, float* coef, bool* ok)
+{
+  *ok = false;
+  if (A64->box_nx <= 0 || A64->box_ny <= 0 || A64->box_nz <= 0) return MFE_OK;
+  return stencil_prepare_box(ctx, A64->box_nx + 1, A64->box_ny + 1, A64->box_nz + 1,
+                             static_cast<const double*>(A64->vals), coef, ok);
+}
+
+bool stencil_mirror_classes(const float* coef, float* w8) { return mirror_classes<float, 22>(coef, w8); }
+
+mfe_status stencil64_prepare(mfe_ctx* ctx, const mfe_csr* A64, double* w8, double* dd, bool* ok)
+{
+  *ok = false;
+  if (A64->box_nx <= 0 || A64->box_ny <= 0 || A64->box_nz <= 0 || A64->dtype != MFE_F64) return MFE_OK;
+  double coef[28];
+  bool tab_ok = false;
+  const mfe_status st = prepare_tab<double, kSt64TolExp>(
+      ctx, "stencil64.table", A64->box_nx + 1, A64->box_ny + 1, A64->box_nz + 1,
+      static_cast<const double*>(A64->vals), coef, &tab_ok);
+  if (st != MFE_OK) return st;
+  *dd = coef[27];
+  *ok = tab_ok && mirror_classes<double, kSt64TolExp>(coef, w8);
+  return MFE_OK;
 }
 
 // one wave of resident CTAs of the variant coef selects (the attributes are

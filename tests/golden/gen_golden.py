@@ -8,6 +8,14 @@ Writes:
   tests/golden/minife_golden.npz   full arrays for small boxes
   tests/golden/golden_hashes.json  sha256 of every array for larger boxes
 
+With --big N (run separately: the serial reference takes about 7 minutes at
+N = 256) it instead runs the N^3 box to a 1e-8 relative residual and writes
+  tests/golden/golden_<N>.json     sha256 of every array, iteration count,
+                                   final residual, analytic check, ||x||
+  tests/golden/x<N>_strided.npy    x[::997] (the solution, sampled)
+--workdir DIR keeps the harness's raw outputs there and reuses them when a
+run with the same arguments already left them (DIR/args.txt).
+
 The legacy unit test's known-answer element matrix (ref/basic/utest_cases.hpp,
 get_test_elem_mat) is read from the reference source as text and stored too.
 The GPU machine never runs this script; tests only read its outputs.
@@ -82,7 +90,52 @@ def utest_known_answer():
     return vals
 
 
+X_STRIDE = 997
+
+
+def big_case(n, workdir=None):
+    """The N^3 box to 1e-8 relative (max 2000 iterations): hashes and a
+    strided sample of the solution."""
+    case = (n, n, n, 2000, 1, 1e-8)
+    args = [str(v) for v in case[:5]] + [repr(case[5])]
+    own = workdir is None
+    d = workdir or tempfile.mkdtemp()
+    os.makedirs(d, exist_ok=True)
+    stamp = os.path.join(d, "args.txt")
+    if not (os.path.exists(stamp) and open(stamp).read().split() == args and
+            os.path.exists(os.path.join(d, "meta.txt"))):
+        subprocess.run([HARNESS, *args, d], check=True)
+        with open(stamp, "w") as f:
+            f.write(" ".join(args) + "\n")
+    meta = {}
+    for line in open(os.path.join(d, "meta.txt")):
+        k, v = line.split()
+        meta[k] = float(v) if "." in v or "e" in v else int(v)
+    out = {"dims": [n, n, n], "max_iter": case[3], "tol_mode": 1, "tol": case[5],
+           "num_iters": meta["num_iters"], "normr": meta["normr"], "abs_tol": meta["abs_tol"],
+           "verify": meta["verify"], "nrows": meta["nrows"], "nnz": meta["nnz"],
+           "x_stride": X_STRIDE, "sha256": {}}
+    for name, ext, dt in ARRAYS:
+        a = np.fromfile(os.path.join(d, "%s.%s" % (name, ext)), dt)
+        out["sha256"][name] = hashlib.sha256(a.tobytes()).hexdigest()
+        if name == "x":
+            out["x_l2"] = float(np.linalg.norm(a))
+            np.save(os.path.join(HERE, "x%d_strided.npy" % n), a[::X_STRIDE].copy())
+        del a
+    with open(os.path.join(HERE, "golden_%d.json" % n), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    if own:
+        shutil.rmtree(d)
+    print("wrote golden_%d.json and x%d_strided.npy (%d iterations)" % (n, n, meta["num_iters"]))
+
+
 def main():
+    if "--big" in sys.argv:
+        if not os.path.exists(HARNESS):
+            sys.exit("build the reference harness first: make -C oracle ref REF=$REF")
+        n = int(sys.argv[sys.argv.index("--big") + 1])
+        wd = sys.argv[sys.argv.index("--workdir") + 1] if "--workdir" in sys.argv else None
+        return big_case(n, wd)
     if not REF or not os.path.isdir(os.path.join(REF, "ref", "src")):
         sys.exit("set REF to the miniFE checkout (the directory holding ref/src)")
     if not os.path.exists(HARNESS):

@@ -45,7 +45,7 @@ def test_bad_box_rejected():
 def test_status_strings_and_version():
     from minife_gb300 import _abi
     lib = _abi.load()
-    assert lib.mfe_abi_version() == 2
+    assert lib.mfe_abi_version() == 3
     assert lib.mfe_status_string(0) == b"ok"
     assert lib.mfe_status_string(4) == b"numerical breakdown"
 

@@ -214,3 +214,41 @@ def test_batch_stencil_operator_matches_values():
     x, off2, res = M.batch_solve_boxes([(10, 10, 10), (3, 8, 8)], max_iter=3000, tol=1e-8,
                                        tol_mode="relative", precision="mixed")
     assert all(r.inner_operator == "padded" and r.status == 0 for r in res)
+
+
+def test_batch_96_seeded_boxes_true_residuals():
+    """The benchmark's batch (96 boxes, nx, ny, nz ~ U{32..160} seeded as in
+    bench.batch_dims) solved together in mixed precision to 1e-8: every box
+    converges, and for 12 boxes -- the smallest, the largest and ten drawn
+    with a fixed seed -- the true FP64 residual ||b - A x|| / ||b|| computed
+    with the oracle's assembly and CSR matvec meets 1e-8 and the reference's
+    analytic check passes."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+    from bench import batch_dims
+    dims = batch_dims()
+    assert len(dims) == 96
+    bt = M.Batch(dims)
+    try:
+        x, res = bt.solve(max_iter=5000, tol=1e-8, tol_mode="relative", precision="mixed",
+                          refine_k=200)
+        assert all(r.status == 0 for r in res)
+        off = bt.offsets
+        xh = host(x)
+    finally:
+        bt.close()
+    del x
+    sizes = [d[0] * d[1] * d[2] for d in dims]
+    order = np.argsort(sizes)
+    pick = {int(order[0]), int(order[-1])}
+    pick |= {int(i) for i in np.random.default_rng(96).choice(96, 10, replace=False)}
+    assert len(pick) == 12
+    for i in sorted(pick):
+        d = dims[i]
+        ro, cols, vals, b = O.build_system(*d)
+        xi = xh[off[i]:off[i + 1]]
+        rel = np.linalg.norm(b - O.matvec(ro, cols, vals, xi)) / np.linalg.norm(b)
+        assert rel <= 1e-8, (d, rel)
+        rc, err = O.verify_solution(*d, xi)
+        assert rc == 0, (d, err)

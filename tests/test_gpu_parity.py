@@ -166,12 +166,21 @@ def test_dot_waxpby():
         assert np.allclose(host(w), O.waxpby(0.5, x, -1.25, y), rtol=1e-15, atol=1e-15)
 
 
+def expected_operator(dims, op):
+    """The FP64 operator a solve of a miniFE box uses: the verified stencil
+    needs an interior class along every dimension (>= 4 elements)."""
+    return "stencil64" if op == "auto" and min(dims) >= 4 else "none"
+
+
+@pytest.mark.parametrize("op", ["csr", "auto"])
 @pytest.mark.parametrize("dims", [(10, 10, 10), (17, 3, 5), (30, 30, 30)])
-def test_cg_reference_defaults(dims):
-    """max_iter 200, absolute tol DBL_EPSILON (driver.hpp:241-245)."""
+def test_cg_reference_defaults(dims, op):
+    """max_iter 200, absolute tol DBL_EPSILON (driver.hpp:241-245), with the
+    CSR values and with the verified FP64 stencil operator."""
     A, b = M.build_system(*dims)
     x = torch.zeros_like(b)
-    res = M.cg_solve(A, b, x, record_history=True)
+    res = M.cg_solve(A, b, x, record_history=True, f64_operator=op)
+    assert res.inner_operator == expected_operator(dims, op)
     ro, cols, vals, bo = O.build_system(*dims)
     xo, it, nr, st, hist = O.cg_solve(ro, cols, vals, bo, history=True)
     assert abs(res.num_iters - it) <= 2
@@ -189,11 +198,16 @@ def test_cg_reference_defaults(dims):
     assert abs(err - erro) <= 1e-12
 
 
-@pytest.mark.parametrize("dims", [(10, 10, 10), (30, 30, 30), (24, 16, 8)])
-def test_cg_relative_1e8(dims):
+@pytest.mark.parametrize("op", ["csr", "auto"])
+@pytest.mark.parametrize("dims", [(10, 10, 10), (30, 30, 30), (24, 16, 8), (40, 5, 33)])
+def test_cg_relative_1e8(dims, op):
     A, b = M.build_system(*dims)
     x = torch.zeros_like(b)
-    res = M.cg_solve(A, b, x, max_iter=1000, tol=1e-8, tol_mode="relative")
+    res = M.cg_solve(A, b, x, max_iter=1000, tol=1e-8, tol_mode="relative", f64_operator=op)
+    assert res.inner_operator == expected_operator(dims, op)
+    # the stencil solve stops on the residual computed with the CSR values
+    if op == "auto":
+        assert res.final_resid <= 1e-8 * res.normr0
     ro, cols, vals, bo = O.build_system(*dims)
     xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=1000, tol=1e-8, tol_mode=1)
     assert abs(res.num_iters - it) <= 1
@@ -226,13 +240,15 @@ def test_cg_host_dropin():
     assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)
 
 
-def test_cg_nonzero_initial_guess_and_max_iter():
+@pytest.mark.parametrize("op", ["csr", "auto"])
+def test_cg_nonzero_initial_guess_and_max_iter(op):
     dims = (10, 10, 10)
     A, b = M.build_system(*dims)
     ro, cols, vals, bo = O.build_system(*dims)
     x0 = np.random.default_rng(2).standard_normal(ro.size - 1)
     x = cuda(x0)
-    res = M.cg_solve(A, b, x, max_iter=7)
+    res = M.cg_solve(A, b, x, max_iter=7, f64_operator=op)
+    assert res.inner_operator == expected_operator(dims, op)
     xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, x0=x0, max_iter=7)
     assert res.num_iters == it == 7
     # an unconverged CG iterate amplifies rounding differences (FMA vs
@@ -326,3 +342,156 @@ def test_box_detection_through_host_call():
     res2 = M.cg_solve_host(ro, cols2, vals2, bo, x2, max_iter=500, tol=1e-10, tol_mode="relative")
     assert abs(res2.num_iters - it) <= 1
     assert np.linalg.norm(x2 - xo) <= 1e-9 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 4), (5, 9, 6), (33, 17, 12)])
+def test_cg_stencil64_first_iterations(dims):
+    """One and two CG iterations from a random x0 through the verified FP64
+    stencil operator against the oracle's CSR CG: the operator enters r0,
+    p.Ap and the updates, so agreement to rounding level checks it row by
+    row (Dirichlet rows, rows next to the faces, interior)."""
+    A, b = M.build_system(*dims)
+    ro, cols, vals, bo = O.build_system(*dims)
+    x0 = np.random.default_rng(11).standard_normal(ro.size - 1)
+    for k in (1, 2):
+        x = cuda(x0)
+        res = M.cg_solve(A, b, x, max_iter=k)
+        assert res.inner_operator == "stencil64"
+        xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, x0=x0, max_iter=k)
+        assert res.num_iters == it == k
+        assert np.allclose(host(x), xo, rtol=1e-12, atol=1e-12 * np.abs(xo).max())
+
+
+def test_cg_stencil64_not_used_for_per_element_kappa():
+    """Per-element conductivity breaks the constant stencil: the check fails
+    and the CSR values are used, with the same solution as the oracle."""
+    dims = (8, 7, 6)
+    kappa = np.exp(np.random.default_rng(5).normal(0.0, 0.5, size=8 * 7 * 6))
+    A, b = M.build_system(*dims, kappa=cuda(kappa))
+    x = torch.zeros_like(b)
+    res = M.cg_solve(A, b, x, max_iter=1000, tol=1e-10, tol_mode="relative")
+    assert res.inner_operator == "none"
+    ro, cols, vals, bo = O.build_system(*dims, kappa=kappa)
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=1000, tol=1e-10, tol_mode=1)
+    assert abs(res.num_iters - it) <= 1
+    assert np.linalg.norm(host(x) - xo) <= 1e-9 * np.linalg.norm(xo)
+
+
+def test_fused_waxpby():
+    """fused_waxpby (Vector_functions.hpp:154-185): both updates of one call
+    against the oracle's waxpby, twice in a row (outputs reused as inputs)."""
+    rng = np.random.default_rng(12)
+    for n in (1, 5, 4099, 300001):
+        x, y, x2, y2 = (rng.standard_normal(n) for _ in range(4))
+        w = torch.empty(n, dtype=torch.float64, device=DEV)
+        w2 = torch.empty_like(w)
+        M.fused_waxpby(1.5, cuda(x), -0.25, cuda(y), w, -2.0, cuda(x2), 0.75, cuda(y2), w2)
+        wo = O.waxpby(1.5, x, -0.25, y)
+        w2o = O.waxpby(-2.0, x2, 0.75, y2)
+        # one FMA per entry against a multiply and an add: within 1 ulp
+        assert np.allclose(host(w), wo, rtol=2.3e-16, atol=1e-300)
+        assert np.allclose(host(w2), w2o, rtol=2.3e-16, atol=1e-300)
+        v = torch.empty_like(w)
+        v2 = torch.empty_like(w)
+        M.fused_waxpby(0.5, w, 1.0, w2, v, 1.0, w2, -3.0, w, v2)
+        assert np.allclose(host(v), O.waxpby(0.5, host(w), 1.0, host(w2)), rtol=2.3e-16, atol=1e-300)
+        assert np.allclose(host(v2), O.waxpby(1.0, host(w2), -3.0, host(w)), rtol=2.3e-16,
+                           atol=1e-300)
+
+
+def exact_dot(x32, y32):
+    """The exact dot of FP32 vectors rounded once: every product is exact in
+    FP64 (24 + 24 significant bits), math.fsum sums them exactly."""
+    import math
+    return math.fsum((x32.astype(np.float64) * y32.astype(np.float64)).tolist())
+
+
+def test_dot_f32_double_float_bound():
+    """The double-float reduction of the mixed solvers (DFAcc,
+    grid_reduce_last_df) against the exact dot at n = 17 M (the 256^3 row
+    count) with mixed signs and magnitudes over 2^-20 .. 2^20: the error stays
+    within 2^-40 of sum |x_i y_i| (about 48-bit accumulation over ~50 terms
+    per thread plus the block and grid sums), where an FP32 accumulation
+    would be off by ~2^-12."""
+    rng = np.random.default_rng(13)
+    n = 16974593
+    x = (rng.standard_normal(n) * np.exp2(rng.integers(-20, 21, n))).astype(np.float32)
+    y = (rng.standard_normal(n) * np.exp2(rng.integers(-20, 21, n))).astype(np.float32)
+    d = M.dot_f32(cuda(x), cuda(y))
+    ex = exact_dot(x, y)
+    scale = float(np.abs(x.astype(np.float64)) @ np.abs(y.astype(np.float64)))
+    assert abs(d - ex) <= 2.0 ** -40 * scale, (d, ex, scale)
+    # cancellation: the same terms with their negatives appended sum to 0
+    x2 = np.concatenate([x[:4000000], x[:4000000]])
+    y2 = np.concatenate([y[:4000000], -y[:4000000]])
+    d2 = M.dot_f32(cuda(x2), cuda(y2))
+    s2 = float(np.abs(x2.astype(np.float64)) @ np.abs(y2.astype(np.float64)))
+    assert abs(d2) <= 2.0 ** -40 * s2
+
+
+def test_dot_f32_subnormal_terms():
+    """FP32 subnormals widen exactly (f2d_exact): ten products of 2^-140
+    and 1 sum to 10 * 2^-140, a subnormal float, not to zero."""
+    x = np.full(10, 2.0 ** -140, np.float32)
+    y = np.ones(10, np.float32)
+    assert M.dot_f32(cuda(x), cuda(y)) == 10 * 2.0 ** -140
+    x[3] = np.float32(2.0 ** -149)  # the smallest subnormal
+    assert M.dot_f32(cuda(x), cuda(y)) == 9 * 2.0 ** -140 + 2.0 ** -149
+
+
+def test_bounded_wait_timeout_reports_and_recovers():
+    """The bounded-wait error path: the injected fault makes the next box
+    SpMV's producer withhold its copies (nothing in flight), its consumers'
+    waits give up after 20 ms, the solve returns MFE_TIMEOUT; then the same
+    context solves normally.  The same for a standalone matvec, whose
+    timeout mfe_synchronize reports."""
+    dims = (8, 8, 8)
+    A, b = M.build_system(*dims)
+    ro, cols, vals, bo = O.build_system(*dims)
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=500, tol=1e-10, tol_mode=1)
+    ctx = M.default_context()
+    for op in ("csr", "auto"):
+        x = torch.zeros_like(b)
+        M.inject_wait_timeout(20_000_000)
+        with pytest.raises(M.MiniFEError) as ei:
+            M.cg_solve(A, b, x, max_iter=5, tol=1e-10, tol_mode="relative", f64_operator=op)
+        assert ei.value.status == 6  # MFE_TIMEOUT
+        x.zero_()
+        res = M.cg_solve(A, b, x, max_iter=500, tol=1e-10, tol_mode="relative", f64_operator=op)
+        assert res.status == 0 and abs(res.num_iters - it) <= 1
+        assert np.linalg.norm(host(x) - xo) <= 1e-9 * np.linalg.norm(xo)
+    xr = torch.randn(A.nrows, dtype=torch.float64, device=DEV)
+    y = torch.empty_like(xr)
+    M.inject_wait_timeout(20_000_000)
+    M.matvec(A, xr, y)
+    with pytest.raises(M.MiniFEError) as ei:
+        ctx.synchronize()
+    assert ei.value.status == 6
+    M.matvec(A, xr, y)
+    ctx.synchronize()
+    yo = O.matvec(ro, cols, vals, host(xr))
+    assert np.allclose(host(y), yo, rtol=1e-13, atol=1e-13 * np.abs(yo).max())
+
+
+@pytest.mark.parametrize("dims", [(4, 4, 4), (9, 5, 7), (30, 30, 30), (64, 33, 17)])
+def test_matvec_stencil64(dims):
+    """The verified FP64 stencil operator row by row against the oracle's
+    CSR matvec: every row within 2^-39 sum_j |a_ij x_j| (the operator's bound
+    against A) plus FMA rounding, Dirichlet rows included."""
+    A, b = M.build_system(*dims)
+    S = M.Stencil64(A)
+    ro, cols, vals, bo = O.build_system(*dims)
+    x = np.random.default_rng(21).standard_normal(ro.size - 1)
+    y = torch.empty_like(b)
+    M.matvec_stencil64(S, cuda(x), y)
+    yo = O.matvec(ro, cols, vals, x)
+    scale = O.matvec(ro, cols, np.abs(vals), np.abs(x)) + 1e-300
+    assert np.all(np.abs(host(y) - yo) <= (2.0 ** -39 + 30 * 2.0 ** -53) * scale)
+
+
+def test_stencil64_refused_where_it_does_not_apply():
+    for dims, kappa in (((3, 8, 8), None), ((6, 6, 6), np.linspace(0.5, 2.0, 216))):
+        A, b = M.build_system(*dims, kappa=None if kappa is None else cuda(kappa))
+        with pytest.raises(M.MiniFEError) as ei:
+            M.Stencil64(A)
+        assert ei.value.status == 7  # MFE_NOT_SUPPORTED
