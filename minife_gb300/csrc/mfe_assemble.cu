@@ -17,6 +17,7 @@
 //      the CSR row (staged through shared memory for coalescing).
 // No atomics: every coefficient is summed in the reference's element order.
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <vector>
@@ -248,50 +249,129 @@ __global__ void k_to_f32(const double* __restrict__ src, float* __restrict__ dst
 
 // ---------------------------------------------------------------------------
 // verify_solution (ref/fem/verify_solution.hpp:55-174) with the series of
-// ref/fem/analytic_soln.hpp:66-112
+// ref/fem/analytic_soln.hpp:66-112:
+//   soln(x, y, z) = 16/pi^2 sum_p sum_q sinh(l x) sin_py / sinh(l) sin_qz,
+//   l = pi sqrt((2p+1)^2 + (2q+1)^2), p, q = 0..300,
+// where the q loop of a p stops at the first term that is NaN.  A term is
+// NaN exactly when sinh(l x) overflows (then sinh(l) has overflowed too and
+// sin_qz / sinh(l) is a signed zero), so where the q loop stops depends on
+// (x, p) only, and the checked nodes form a product set X x Y x Z of
+// coordinates.  The sum is therefore evaluated through tables instead of
+// 90,601 sinh calls per node:
+//   T[x][p,q] = sinh(l x), D[z][p,q] = sin_qz / sinh(l), S[y][p] = sin_py,
+//   U[x][z][p] = sum over the q the reference sums of T * D,
+//   soln = 16/pi^2 sum_p S[y][p] U[x][z][p];
+// each quantity is the reference's expression, only the order of the
+// products and additions differs (the result agrees to ~1e-15).
 // ---------------------------------------------------------------------------
-__device__ double analytic_soln(double x, double y, double z, int max_p, int max_q)
+constexpr int kSerP = 301;             // p, q = 0..300 (verify_solution.hpp:111)
+constexpr int kSerPQ = kSerP * kSerP;
+constexpr double kPI = 3.141592653589793238462;
+
+// node coordinate along a dimension of N nodes (get_coords, box_utils.hpp:64-82)
+__host__ __device__ __forceinline__ double verify_coord(int i, int N)
 {
-  const double PI = 3.141592653589793238462;
-  const double PI_SQR = PI * PI;
-  const double term0 = 16.0 / (PI_SQR);
-  double sum = 0;
-  for (int p = 0; p <= max_p; ++p) {
-    const double p21y = (2 * p + 1) * PI * y;
-    const double sin_py = sin(p21y) / (2 * p + 1);
-    for (int q = 0; q <= max_q; ++q) {
-      const double q21z = (2 * q + 1) * PI * z;
-      const double sin_qz = sin(q21z) / (2 * q + 1);
-      const double l = sqrt((2 * p + 1) * (2 * p + 1) * PI_SQR + (2 * q + 1) * (2 * q + 1) * PI_SQR);
-      const double sinh1 = sinh(l * x);
-      const double sinh2 = sinh(l);
-      const double tmp = (sinh1 * sin_py) * (sin_qz / sinh2);
-      if (tmp == tmp) sum += tmp;
-      else break;
-    }
-  }
-  return term0 * sum;
+  const int div = N > 1 ? N - 1 : 1;
+  return (1.0 * (double)i) / div;
 }
 
-__global__ void k_verify(int Nx, int Ny, int Nz, const double* __restrict__ xv, int whole,
-                         unsigned long long* __restrict__ max_bits)
+struct VerifyAxes {
+  int x0, nxs, y0, nys, z0, nzs;  // checked index ranges [a0, a0 + n)
+  int Nx, Ny, Nz;
+};
+
+// l and sinh(l) per (p, q) (analytic_soln.hpp fcn_l)
+__global__ void k_ver_l(double* __restrict__ L, double* __restrict__ S2)
 {
-  const int64_t N = (int64_t)Nx * Ny * Nz;
-  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (r >= N) return;
-  const int64_t NxNy = (int64_t)Nx * Ny;
-  const int xdiv = Nx > 1 ? Nx - 1 : 1, ydiv = Ny > 1 ? Ny - 1 : 1, zdiv = Nz > 1 ? Nz - 1 : 1;
-  const double z = (1.0 * (double)(r / NxNy)) / zdiv;
-  const double y = 1.0 * (double)((r % NxNy) / Nx) / ydiv;
-  const double x = 1.0 * (double)(r % Nx) / xdiv;
-  const bool check =
-      whole || (fabs(x - 0.5) < 0.05 && fabs(y - 0.5) < 0.05 && fabs(z - 0.5) < 0.05);
-  if (!check) return;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= kSerPQ) return;
+  const int p = i / kSerP, q = i - p * kSerP;
+  const double PI_SQR = kPI * kPI;
+  const double l = sqrt((2 * p + 1) * (2 * p + 1) * PI_SQR + (2 * q + 1) * (2 * q + 1) * PI_SQR);
+  L[i] = l;
+  S2[i] = sinh(l);
+}
+
+// T[xi][pq] = sinh(l x), D[zi][pq] = sin_qz(z) / sinh(l)
+__global__ void k_ver_td(VerifyAxes A, const double* __restrict__ L, const double* __restrict__ S2,
+                         double* __restrict__ T, double* __restrict__ D)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t nt = (int64_t)A.nxs * kSerPQ, nd = (int64_t)A.nzs * kSerPQ;
+  if (i < nt) {
+    const int xi = (int)(i / kSerPQ), pq = (int)(i - (int64_t)xi * kSerPQ);
+    const double x = verify_coord(A.x0 + xi, A.Nx);
+    T[i] = sinh(L[pq] * x);
+  } else if (i < nt + nd) {
+    const int64_t k = i - nt;
+    const int zi = (int)(k / kSerPQ), pq = (int)(k - (int64_t)zi * kSerPQ);
+    const int q = pq % kSerP;
+    const double z = verify_coord(A.z0 + zi, A.Nz);
+    const double q21z = (2 * q + 1) * kPI * z;
+    const double sin_qz = sin(q21z) / (2 * q + 1);
+    D[k] = sin_qz / S2[pq];
+  }
+}
+
+// U[xi][zi][p] = sum over q < (first q with sinh(l x) = inf) of T * D, in
+// q order; one warp per (xi, zi, p), lanes over q, fixed-order warp sum
+__global__ void k_ver_u(VerifyAxes A, const double* __restrict__ T, const double* __restrict__ D,
+                        double* __restrict__ U)
+{
+  const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int64_t nw = (int64_t)A.nxs * A.nzs * kSerP;
+  if (w >= nw) return;
+  const int p = (int)(w % kSerP);
+  const int64_t xz = w / kSerP;
+  const int zi = (int)(xz % A.nzs), xi = (int)(xz / A.nzs);
+  const double* t = T + (int64_t)xi * kSerPQ + p * kSerP;
+  const double* d = D + (int64_t)zi * kSerPQ + p * kSerP;
+  // the first overflowing q (sinh(l x) grows with q)
+  int qb = kSerP;
+  for (int q0 = 0; q0 < kSerP; q0 += 32) {
+    const int q = q0 + lane;
+    const bool inf = q < kSerP && isinf(t[q]);
+    const unsigned m = __ballot_sync(0xffffffffu, inf);
+    if (m) {
+      qb = q0 + __ffs(m) - 1;
+      break;
+    }
+  }
+  double s = 0.0;
+  for (int q = lane; q < qb; q += 32) s += t[q] * d[q];
+  s = warp_sum(s);
+  if (lane == 0) U[w] = s;
+}
+
+// one thread per checked node: soln from S (formed here) and U, the
+// reference's boundary values, |soln - x| folded into a bitwise maximum
+__global__ void k_ver_node(VerifyAxes A, const double* __restrict__ U, const double* __restrict__ xv,
+                           unsigned long long* __restrict__ max_bits)
+{
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t n = (int64_t)A.nxs * A.nys * A.nzs;
+  if (i >= n) return;
+  const int xi = (int)(i % A.nxs);
+  const int yi = (int)((i / A.nxs) % A.nys);
+  const int zi = (int)(i / ((int64_t)A.nxs * A.nys));
+  const int ix = A.x0 + xi, iy = A.y0 + yi, iz = A.z0 + zi;
+  const double x = verify_coord(ix, A.Nx), y = verify_coord(iy, A.Ny), z = verify_coord(iz, A.Nz);
   double a;
   if (x == 1.0) a = 1;
   else if (x == 0.0 || y == 0.0 || z == 0.0) a = 0;
   else if (y == 1.0 || z == 1.0) a = 0;
-  else a = analytic_soln(x, y, z, 300, 300);
+  else {
+    const double* u = U + ((int64_t)xi * A.nzs + zi) * kSerP;
+    double sum = 0.0;
+    for (int p = 0; p < kSerP; ++p) {
+      const double p21y = (2 * p + 1) * kPI * y;
+      const double sin_py = sin(p21y) / (2 * p + 1);
+      sum += sin_py * u[p];
+    }
+    a = 16.0 / (kPI * kPI) * sum;
+  }
+  const int64_t r = ((int64_t)iz * A.Ny + iy) * A.Nx + ix;
   const double err = fabs(a - xv[r]);
   // non-negative doubles order like their bit patterns
   atomicMax(max_bits, (unsigned long long)__double_as_longlong(err));
@@ -444,16 +524,57 @@ mfe_status launch_convert_f32(mfe_ctx* ctx, const double* src, float* dst, int64
   return check_launch(ctx, "k_to_f32");
 }
 
+// checked index range along a dimension of N nodes: all, or the nodes with
+// |coord - 0.5| < 0.05 (verify_solution.hpp:97-105), a contiguous range
+static void verify_range(int N, int whole, int* a0, int* n)
+{
+  if (whole) {
+    *a0 = 0;
+    *n = N;
+    return;
+  }
+  int lo = -1, hi = -1;
+  for (int i = 0; i < N; ++i)
+    if (std::fabs(verify_coord(i, N) - 0.5) < 0.05) {
+      if (lo < 0) lo = i;
+      hi = i;
+    }
+  *a0 = lo < 0 ? 0 : lo;
+  *n = lo < 0 ? 0 : hi - lo + 1;
+}
+
 mfe_status launch_verify(mfe_ctx* ctx, int nx, int ny, int nz, const double* x, int whole,
                          double* max_err_host)
 {
-  const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
-  const int64_t N = (int64_t)Nx * Ny * Nz;
+  VerifyAxes A;
+  A.Nx = nx + 1;
+  A.Ny = ny + 1;
+  A.Nz = nz + 1;
+  verify_range(A.Nx, whole, &A.x0, &A.nxs);
+  verify_range(A.Ny, whole, &A.y0, &A.nys);
+  verify_range(A.Nz, whole, &A.z0, &A.nzs);
   unsigned long long* d = static_cast<unsigned long long*>(workspace(ctx, "verify.max", 8));
   if (!d) return fail(ctx, MFE_OOM, "verify scratch allocation failed");
   MFE_CUDA_TRY(ctx, cudaMemsetAsync(d, 0, 8, ctx->stream));
-  k_verify<<<(unsigned)ceil_div(N, 128), 128, 0, ctx->stream>>>(Nx, Ny, Nz, x, whole, d);
-  MFE_TRY(check_launch(ctx, "k_verify"));
+  const int64_t nodes = (int64_t)A.nxs * A.nys * A.nzs;
+  if (nodes > 0) {
+    const int64_t nt = (int64_t)A.nxs * kSerPQ, nd = (int64_t)A.nzs * kSerPQ;
+    const int64_t nu = (int64_t)A.nxs * A.nzs * kSerP;
+    double* L = static_cast<double*>(workspace(ctx, "verify.l", sizeof(double) * 2 * kSerPQ));
+    double* T = static_cast<double*>(workspace(ctx, "verify.td", sizeof(double) * (nt + nd)));
+    double* U = static_cast<double*>(workspace(ctx, "verify.u", sizeof(double) * nu));
+    if (!L || !T || !U) return fail(ctx, MFE_OOM, "verify table allocation failed");
+    double* S2 = L + kSerPQ;
+    double* D = T + nt;
+    k_ver_l<<<(unsigned)ceil_div(kSerPQ, 256), 256, 0, ctx->stream>>>(L, S2);
+    MFE_TRY(check_launch(ctx, "k_ver_l"));
+    k_ver_td<<<(unsigned)ceil_div(nt + nd, 256), 256, 0, ctx->stream>>>(A, L, S2, T, D);
+    MFE_TRY(check_launch(ctx, "k_ver_td"));
+    k_ver_u<<<(unsigned)ceil_div(nu * 32, 256), 256, 0, ctx->stream>>>(A, T, D, U);
+    MFE_TRY(check_launch(ctx, "k_ver_u"));
+    k_ver_node<<<(unsigned)ceil_div(nodes, 128), 128, 0, ctx->stream>>>(A, U, x, d);
+    MFE_TRY(check_launch(ctx, "k_ver_node"));
+  }
   unsigned long long* h = static_cast<unsigned long long*>(host_scratch(ctx, 8));
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(h, d, 8, cudaMemcpyDeviceToHost, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));

@@ -20,15 +20,16 @@
 //   P1(z) = w4 a + w5 sx + w6 sy + w7 sxy                (the |dz| = 1 part)
 //   Q(z)  = P1(z-1) + w0 a + w1 sx + w2 sy + w3 sxy      (FMA chain from P1(z-1))
 //   y(z)  = Q(z) + P1(z+1)
-// Marching along z, each plane's class sums and P1 are formed once: with two
-// adjacent positions per thread a plane costs 8 additions (class sums), 8
-// operations for P1, 8 FMAs for Q, and a row 1 final addition and 1 FMA for
-// p.Ap: 14 FP64 operations per row instead of 28.
+// Marching along z, each plane's class sums and P1 are formed once: with four
+// adjacent positions per thread a plane costs 14 additions for the class sums
+// (6 sums of lines y - 1 and y + 1, then 4 sx and 4 sxy), 16 operations for
+// P1 and 16 FMAs for Q, and a row 1 final addition and 1 FMA for p.Ap: 13.5
+// FP64 operations per row instead of the CSR kernel's 28.
 //
-// k_spmv_st64 works on the CG's natural-layout vectors.  A CTA owns 512
-// consecutive positions of the xy plane (two per thread) and a run of z
+// k_spmv_st64 works on the CG's natural-layout vectors.  A CTA owns 1024
+// consecutive positions of the xy plane (four per thread) and a run of z
 // steps; the (plane tile, z) steps are split evenly over the grid.  Each
-// thread reads its 3 x 4 window x[p-1 .. p+2] of lines y-1, y, y+1 of each
+// thread reads its 3 x 6 window x[p-1 .. p+4] of lines y-1, y, y+1 of each
 // plane with 8-byte loads (lines of odd length defeat wider ones), the
 // neighbouring lines and planes coming from L1/L2: the kernel is bound by
 // the FP64 pipe, not by memory.  Window entries that are not interior nodes
@@ -38,6 +39,7 @@
 // over the grid in block order (deterministic for a fixed grid).
 #include <algorithm>
 #include <cmath>
+#include <type_traits>
 
 #include "mfe_cgstate.cuh"
 #include "mfe_common.cuh"
@@ -47,8 +49,7 @@ namespace mfe {
 
 namespace {
 
-constexpr int kT64 = 256;       // threads per CTA
-constexpr int kT64P = 2 * kT64;  // plane positions per CTA
+constexpr int kT64 = 256;  // threads per CTA
 
 struct St64Params {
   int Nx, Ny, Nz, NxNy, ntile;
@@ -62,28 +63,14 @@ struct St64Params {
   CgState* cg;
 };
 
-// class sums and P1 of one interior plane for positions p, p + 1 from the
-// window v[4j + t] = x~[p - 1 + t] of line y + j - 1
-struct St64Sums {
-  double a[2], sx[2], sy[2], sxy[2];
-};
-
-__device__ __forceinline__ void st64_sums(const double* v, St64Sums& S)
-{
-  double e[4];
-#pragma unroll
-  for (int t = 0; t < 4; ++t) e[t] = v[t] + v[8 + t];
-#pragma unroll
-  for (int r = 0; r < 2; ++r) {
-    S.a[r] = v[5 + r];
-    S.sx[r] = v[4 + r] + v[6 + r];
-    S.sy[r] = e[1 + r];
-    S.sxy[r] = e[r] + e[2 + r];
-  }
-}
-
+// KP adjacent positions per thread (2 or 4): the window of a line is
+// x~[p0 - 1 .. p0 + KP], KP + 2 values; a plane's class sums cost KP + 2
+// additions (lines y - 1 and y + 1) plus 2 KP (sx, sxy), i.e. 3 + 2 / KP per
+// row.  DOT: accumulate p.Ap (the CG's SpMV) or not (a plain product).
+template <int KP, bool DOT>
 __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64Params P)
 {
+  constexpr int W = KP + 2;  // window length per line
   __shared__ double red[32];
   const int64_t T = (int64_t)P.ntile * P.Nz;
   const int64_t q0 = T * blockIdx.x / gridDim.x, q1 = T * (blockIdx.x + 1) / gridDim.x;
@@ -91,13 +78,12 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
   for (int64_t q = q0; q < q1;) {
     const int tile = (int)(q / P.Nz), za = (int)(q - (int64_t)tile * P.Nz);
     const int zb = (int)min((int64_t)P.Nz, za + (q1 - q));
-    const int p0 = tile * kT64P + 2 * threadIdx.x;
-    const bool v0 = p0 < P.NxNy, v1 = p0 + 1 < P.NxNy;
-    // mask bit 4j + t: window entry (line y + j - 1, position p0 - 1 + t) is
+    const int p0 = tile * (KP * kT64) + KP * threadIdx.x;
+    // mask bit W j + t: window entry (line y + j - 1, position p0 - 1 + t) is
     // an interior node of the plane (then its address lies inside the plane)
     unsigned mask = 0;
 #pragma unroll
-    for (int t = 0; t < 4; ++t) {
+    for (int t = 0; t < W; ++t) {
       const int pp = p0 - 1 + t;
       if (pp >= 0 && pp < P.NxNy) {
         const int iy = pp / P.Nx, ix = pp - iy * P.Nx;
@@ -105,95 +91,121 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
           const int jy = iy + j - 1;
-          if (inx && jy >= 1 && jy <= P.Ny - 2) mask |= 1u << (4 * j + t);
+          if (inx && jy >= 1 && jy <= P.Ny - 2) mask |= 1u << (W * j + t);
         }
       }
     }
-    const bool bnd0 = !((mask >> 5) & 1u), bnd1 = !((mask >> 6) & 1u);  // Dirichlet rows
-    const bool wb = __any_sync(0xffffffffu, (v0 && bnd0) || (v1 && bnd1));
+    bool valid[KP], bnd[KP];
+    bool any_bnd = false;
+#pragma unroll
+    for (int r = 0; r < KP; ++r) {
+      valid[r] = p0 + r < P.NxNy;
+      bnd[r] = !((mask >> (W + 1 + r)) & 1u);  // a Dirichlet row (or past the plane)
+      any_bnd = any_bnd || (valid[r] && bnd[r]);
+    }
+    const bool wb = __any_sync(0xffffffffu, any_bnd);
     const double* xp = P.x + p0 - 1;  // window origin of plane 0
+    auto ld = [](const double* a) { return __ldg(a); };
 
-    // plane z: centres (unmasked), P1 and Q (chain from P1 of plane z - 1)
-    auto plane = [&](int z, const double* P1in, double* P1, double* Qo, double* cen) {
+    // plane z: centres (unmasked, cen), P1 and, when WITHQ, Q (the FMA chain
+    // from P1 of plane z - 1); nothing else is loaded for Dirichlet planes
+    auto plane = [&](auto withq, int z, const double* P1in, double* P1, double* Qo, double* cen) {
+      constexpr bool WQ = decltype(withq)::value;
       const double* b = xp + (int64_t)z * P.NxNy;
-      cen[0] = v0 ? __ldg(b + 1) : 0.0;
-      cen[1] = v1 ? __ldg(b + 2) : 0.0;
+#pragma unroll
+      for (int r = 0; r < KP; ++r) cen[r] = valid[r] ? ld(b + 1 + r) : 0.0;
       if (z <= 0 || z >= P.Nz - 1) {  // Dirichlet plane (uniform): x~ = 0
-        P1[0] = P1[1] = 0.0;
-        Qo[0] = Qo[1] = 0.0;
+#pragma unroll
+        for (int r = 0; r < KP; ++r) {
+          P1[r] = 0.0;
+          if (WQ) Qo[r] = 0.0;
+        }
         return;
       }
-      double v[12];
+      double v[3 * W];
 #pragma unroll
       for (int j = 0; j < 3; ++j)
 #pragma unroll
-        for (int t = 0; t < 4; ++t) {
-          const int s = 4 * j + t;
-          if (s == 5) v[s] = (mask >> 5) & 1u ? cen[0] : 0.0;
-          else if (s == 6) v[s] = (mask >> 6) & 1u ? cen[1] : 0.0;
-          else v[s] = (mask >> s) & 1u ? __ldg(b + (j - 1) * P.Nx + t) : 0.0;
+        for (int t = 0; t < W; ++t) {
+          const int s = W * j + t;
+          const bool m = (mask >> s) & 1u;
+          if (j == 1 && t >= 1 && t <= KP) v[s] = m ? cen[t - 1] : 0.0;
+          else v[s] = m ? ld(b + (j - 1) * P.Nx + t) : 0.0;
         }
-      St64Sums S;
-      st64_sums(v, S);
+      double e[W];
 #pragma unroll
-      for (int r = 0; r < 2; ++r) {
-        double p1 = P.w[4] * S.a[r];
-        p1 = fma(P.w[5], S.sx[r], p1);
-        p1 = fma(P.w[6], S.sy[r], p1);
-        P1[r] = fma(P.w[7], S.sxy[r], p1);
-        double qv = fma(P.w[0], S.a[r], P1in[r]);
-        qv = fma(P.w[1], S.sx[r], qv);
-        qv = fma(P.w[2], S.sy[r], qv);
-        Qo[r] = fma(P.w[3], S.sxy[r], qv);
+      for (int t = 0; t < W; ++t) e[t] = v[t] + v[2 * W + t];
+#pragma unroll
+      for (int r = 0; r < KP; ++r) {
+        const double a = v[W + 1 + r];
+        const double sx = v[W + r] + v[W + r + 2];
+        const double sy = e[1 + r];
+        const double sxy = e[r] + e[r + 2];
+        double p1 = P.w[4] * a;
+        p1 = fma(P.w[5], sx, p1);
+        p1 = fma(P.w[6], sy, p1);
+        P1[r] = fma(P.w[7], sxy, p1);
+        if (WQ) {
+          double qv = fma(P.w[0], a, P1in[r]);
+          qv = fma(P.w[1], sx, qv);
+          qv = fma(P.w[2], sy, qv);
+          Qo[r] = fma(P.w[3], sxy, qv);
+        }
       }
     };
+    using WithQ = std::true_type;
+    using NoQ = std::false_type;
 
-    double P1c[2] = {0.0, 0.0}, Qc[2], cc[2];
+    double P1c[KP], Qc[KP], cc[KP];
+#pragma unroll
+    for (int r = 0; r < KP; ++r) P1c[r] = 0.0;
     if (za >= 1) {  // P1 of plane za - 1 (its Q is not needed)
-      double zq[2] = {0.0, 0.0}, qd[2], cd[2];
-      plane(za - 1, zq, P1c, qd, cd);
+      double cd[KP];
+      plane(NoQ{}, za - 1, P1c, P1c, nullptr, cd);
     }
     {
-      double P1n[2];
-      plane(za, P1c, P1n, Qc, cc);
-      P1c[0] = P1n[0];
-      P1c[1] = P1n[1];
+      double P1n[KP];
+      plane(WithQ{}, za, P1c, P1n, Qc, cc);
+#pragma unroll
+      for (int r = 0; r < KP; ++r) P1c[r] = P1n[r];
     }
     double* yp = P.y + (int64_t)za * P.NxNy + p0;
     for (int z = za; z < zb; ++z) {
-      double P1n[2] = {0.0, 0.0}, Qn[2] = {0.0, 0.0}, cn[2] = {0.0, 0.0};
-      if (z + 1 < P.Nz) plane(z + 1, P1c, P1n, Qn, cn);
-      double y0, y1;
+      double P1n[KP], Qn[KP], cn[KP];
+#pragma unroll
+      for (int r = 0; r < KP; ++r) P1n[r] = Qn[r] = cn[r] = 0.0;
+      // (the last step's Q, of the run's halo plane, goes unused: one code
+      // path in the loop keeps the kernel at 3 CTAs per SM)
+      if (z + 1 < P.Nz) plane(WithQ{}, z + 1, P1c, P1n, Qn, cn);
+      double yv[KP];
       if (z == 0 || z == P.Nz - 1) {
-        y0 = P.dd * cc[0];
-        y1 = P.dd * cc[1];
+#pragma unroll
+        for (int r = 0; r < KP; ++r) yv[r] = P.dd * cc[r];
       } else {
-        y0 = Qc[0] + P1n[0];
-        y1 = Qc[1] + P1n[1];
+#pragma unroll
+        for (int r = 0; r < KP; ++r) yv[r] = Qc[r] + P1n[r];
         if (wb) {
-          if (bnd0) y0 = P.dd * cc[0];
-          if (bnd1) y1 = P.dd * cc[1];
+#pragma unroll
+          for (int r = 0; r < KP; ++r)
+            if (bnd[r]) yv[r] = P.dd * cc[r];
         }
       }
-      if (v1) {
-        yp[0] = y0;
-        yp[1] = y1;
-      } else if (v0) {
-        yp[0] = y0;
+#pragma unroll
+      for (int r = 0; r < KP; ++r) {
+        if (valid[r]) yp[r] = yv[r];
+        if (DOT) dacc = fma(yv[r], cc[r], dacc);
       }
-      dacc = fma(y0, cc[0], dacc);
-      dacc = fma(y1, cc[1], dacc);
       yp += P.NxNy;
-      P1c[0] = P1n[0];
-      P1c[1] = P1n[1];
-      Qc[0] = Qn[0];
-      Qc[1] = Qn[1];
-      cc[0] = cn[0];
-      cc[1] = cn[1];
+#pragma unroll
+      for (int r = 0; r < KP; ++r) {
+        P1c[r] = P1n[r];
+        Qc[r] = Qn[r];
+        cc[r] = cn[r];
+      }
     }
     q += zb - za;
   }
-  if (P.dot_out == nullptr && P.cg == nullptr) return;
+  if (!DOT) return;
   const double bt = block_sum(dacc, red);
   double total;
   if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0) {
@@ -206,6 +218,23 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
   }
 }
 
+// four positions per thread: measured at 256^3, 0.484 ms per product
+// against 0.493 ms with two (and no difference between the read-only and the
+// L1-cached load paths)
+constexpr int kKP = 4;
+
+template <bool DOT>
+mfe_status st64_launch(mfe_ctx* ctx, St64Params& P)
+{
+  P.ntile = (int)ceil_div(P.NxNy, (int64_t)kKP * kT64);
+  const int64_t T = (int64_t)P.ntile * P.Nz;
+  const int g = (int)std::max<int64_t>(
+      1, std::min<int64_t>(T, (int64_t)resident_blocks(ctx, (const void*)k_spmv_st64<kKP, DOT>,
+                                                       kT64, 0)));
+  k_spmv_st64<kKP, DOT><<<g, kT64, 0, ctx->stream>>>(P);
+  return check_launch(ctx, "k_spmv_st64");
+}
+
 }  // namespace
 
 mfe_status launch_spmv_st64(mfe_ctx* ctx, const mfe_csr* A, const double* w8, double dd,
@@ -216,7 +245,6 @@ mfe_status launch_spmv_st64(mfe_ctx* ctx, const mfe_csr* A, const double* w8, do
   P.Ny = A->box_ny + 1;
   P.Nz = A->box_nz + 1;
   P.NxNy = P.Nx * P.Ny;
-  P.ntile = (int)ceil_div(P.NxNy, (int64_t)kT64P);
   for (int c = 0; c < 8; ++c) P.w[c] = w8[c];
   P.dd = dd;
   P.x = x;
@@ -225,13 +253,10 @@ mfe_status launch_spmv_st64(mfe_ctx* ctx, const mfe_csr* A, const double* w8, do
   P.partials = sink ? sink->partials : nullptr;
   P.ticket = sink ? sink->ticket : nullptr;
   P.dot_out = sink && !cg_state ? sink->out : nullptr;
-  if ((P.cg || P.dot_out) && (!P.partials || !P.ticket))
+  const bool dot = P.cg || P.dot_out;
+  if (dot && (!P.partials || !P.ticket))
     return fail(ctx, MFE_BAD_ARG, "stencil SpMV: a dot needs reduction buffers");
-  const int64_t T = (int64_t)P.ntile * P.Nz;
-  const int g = (int)std::max<int64_t>(
-      1, std::min<int64_t>(T, (int64_t)resident_blocks(ctx, (const void*)k_spmv_st64, kT64, 0)));
-  k_spmv_st64<<<g, kT64, 0, ctx->stream>>>(P);
-  return check_launch(ctx, "k_spmv_st64");
+  return dot ? st64_launch<true>(ctx, P) : st64_launch<false>(ctx, P);
 }
 
 }  // namespace mfe

@@ -166,10 +166,12 @@ def test_dot_waxpby():
         assert np.allclose(host(w), O.waxpby(0.5, x, -1.25, y), rtol=1e-15, atol=1e-15)
 
 
-def expected_operator(dims, op):
+def expected_operator(dims, op, tight=False):
     """The FP64 operator a solve of a miniFE box uses: the verified stencil
-    needs an interior class along every dimension (>= 4 elements)."""
-    return "stencil64" if op == "auto" and min(dims) >= 4 else "none"
+    needs an interior class along every dimension (>= 4 elements) and a
+    tolerance of at least 2^-33 of the initial residual (tight: the
+    reference's absolute DBL_EPSILON stop is far below it)."""
+    return "stencil64" if op == "auto" and min(dims) >= 4 and not tight else "none"
 
 
 @pytest.mark.parametrize("op", ["csr", "auto"])
@@ -180,7 +182,7 @@ def test_cg_reference_defaults(dims, op):
     A, b = M.build_system(*dims)
     x = torch.zeros_like(b)
     res = M.cg_solve(A, b, x, record_history=True, f64_operator=op)
-    assert res.inner_operator == expected_operator(dims, op)
+    assert res.inner_operator == expected_operator(dims, op, tight=True)
     ro, cols, vals, bo = O.build_system(*dims)
     xo, it, nr, st, hist = O.cg_solve(ro, cols, vals, bo, history=True)
     assert abs(res.num_iters - it) <= 2
@@ -248,7 +250,7 @@ def test_cg_nonzero_initial_guess_and_max_iter(op):
     x0 = np.random.default_rng(2).standard_normal(ro.size - 1)
     x = cuda(x0)
     res = M.cg_solve(A, b, x, max_iter=7, f64_operator=op)
-    assert res.inner_operator == expected_operator(dims, op)
+    assert res.inner_operator == expected_operator(dims, op, tight=True)
     xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, x0=x0, max_iter=7)
     assert res.num_iters == it == 7
     # an unconverged CG iterate amplifies rounding differences (FMA vs
@@ -355,7 +357,7 @@ def test_cg_stencil64_first_iterations(dims):
     x0 = np.random.default_rng(11).standard_normal(ro.size - 1)
     for k in (1, 2):
         x = cuda(x0)
-        res = M.cg_solve(A, b, x, max_iter=k)
+        res = M.cg_solve(A, b, x, max_iter=k, tol=1e-8, tol_mode="relative")
         assert res.inner_operator == "stencil64"
         xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, x0=x0, max_iter=k)
         assert res.num_iters == it == k
@@ -386,17 +388,19 @@ def test_fused_waxpby():
         w = torch.empty(n, dtype=torch.float64, device=DEV)
         w2 = torch.empty_like(w)
         M.fused_waxpby(1.5, cuda(x), -0.25, cuda(y), w, -2.0, cuda(x2), 0.75, cuda(y2), w2)
-        wo = O.waxpby(1.5, x, -0.25, y)
-        w2o = O.waxpby(-2.0, x2, 0.75, y2)
-        # one FMA per entry against a multiply and an add: within 1 ulp
-        assert np.allclose(host(w), wo, rtol=2.3e-16, atol=1e-300)
-        assert np.allclose(host(w2), w2o, rtol=2.3e-16, atol=1e-300)
+        # one FMA per entry against a multiply and an add: the two differ by
+        # at most one rounding of alpha x and one of the sum
+        def close(got, a, u, bb, v):
+            ref = O.waxpby(a, u, bb, v)
+            bound = 2.0 ** -52 * (np.abs(a * u) + np.abs(bb * v)) + 1e-300
+            return np.all(np.abs(got - ref) <= bound)
+        assert close(host(w), 1.5, x, -0.25, y)
+        assert close(host(w2), -2.0, x2, 0.75, y2)
         v = torch.empty_like(w)
         v2 = torch.empty_like(w)
         M.fused_waxpby(0.5, w, 1.0, w2, v, 1.0, w2, -3.0, w, v2)
-        assert np.allclose(host(v), O.waxpby(0.5, host(w), 1.0, host(w2)), rtol=2.3e-16, atol=1e-300)
-        assert np.allclose(host(v2), O.waxpby(1.0, host(w2), -3.0, host(w)), rtol=2.3e-16,
-                           atol=1e-300)
+        assert close(host(v), 0.5, host(w), 1.0, host(w2))
+        assert close(host(v2), 1.0, host(w2), -3.0, host(w))
 
 
 def exact_dot(x32, y32):
@@ -495,3 +499,21 @@ def test_stencil64_refused_where_it_does_not_apply():
         with pytest.raises(M.MiniFEError) as ei:
             M.Stencil64(A)
         assert ei.value.status == 7  # MFE_NOT_SUPPORTED
+
+
+@pytest.mark.parametrize("dims,whole", [((12, 10, 8), False), ((30, 30, 30), False),
+                                        ((9, 7, 5), True), ((64, 64, 64), False)])
+def test_verify_solution_matches_oracle(dims, whole):
+    """verify_solution (verify_solution.hpp:55-174) on a solved box and on a
+    perturbed solution: the maximum error against the 300 x 300-term series
+    agrees with the oracle's within 1e-12 (the series is summed in another
+    order), and so does the pass/fail outcome."""
+    A, b = M.build_system(*dims)
+    x = torch.zeros_like(b)
+    M.cg_solve(A, b, x, max_iter=2000, tol=1e-10, tol_mode="relative")
+    rng = np.random.default_rng(31)
+    for xs in (host(x), host(x) + 0.07 * rng.standard_normal(A.nrows)):
+        rc, err = M.verify_solution(*dims, cuda(xs), whole_domain=whole)
+        rco, erro = O.verify_solution(*dims, xs, whole=whole)
+        assert rc == rco
+        assert abs(err - erro) <= 1e-12, (err, erro)
