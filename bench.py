@@ -339,7 +339,12 @@ def run_gpu(args):
     achieved = spmv_bytes / t_spmv / 1e9
     traffic = traffic_from_profile()
 
-    # e2e through the host drop-in call (pinned host CSR, copies inside)
+    # e2e through the host drop-in call (pinned host CSR, copies inside).
+    # Each call is timed on its own; the host x is zeroed between calls,
+    # outside the timed region, as the reference arm allocates its x outside.
+    # The call copies the values, b and x in and x out; it checks the row
+    # offsets and columns against the box layout on the host threads while
+    # the values move, and a verified box layout is not copied.
     e2e = None
     if not args.no_e2e:
         ro_h = A.row_offsets.cpu().pin_memory()
@@ -350,17 +355,21 @@ def run_gpu(args):
         M.cg_solve_host(ro_h, cols_h, vals_h, b_h, x_h, max_iter=5000, tol=TOL,
                         tol_mode="relative")
         barrier(world)
-        t0 = time.perf_counter()
+        t_calls = 0.0
         for _ in range(args.steps):
             x_h.zero_()
+            t0 = time.perf_counter()
             r2 = M.cg_solve_host(ro_h, cols_h, vals_h, b_h, x_h, max_iter=5000, tol=TOL,
                                  tol_mode="relative")
-        t1 = time.perf_counter()
+            t_calls += time.perf_counter() - t0
         barrier(world)
-        t_e2e = max_over_ranks(world, (t1 - t0) / args.steps)
-        h2d = 4 * (n + 1) + 4 * nnz + 8 * nnz + 8 * n + 8 * n
+        t_e2e = max_over_ranks(world, t_calls / args.steps)
+        h2d = 8 * nnz + 8 * n + 8 * n
         e2e = {"value": t_e2e, "unit": "s", "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": 8 * n, "iterations": r2.num_iters}
+               "d2h_bytes_per_step": 8 * n, "iterations": r2.num_iters,
+               "ratio_to_device_solve": t_e2e / t_step,
+               "structure": "row offsets and columns checked on the host against the box "
+                            "layout, not copied"}
         del ro_h, cols_h, vals_h
 
     # mixed precision (FP32 inner operator and vectors, FP64 dots and reliable

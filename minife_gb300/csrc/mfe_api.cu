@@ -7,10 +7,15 @@
 #include <cstdlib>
 #include <cstring>
 #include <tuple>
+#include <atomic>
 #include <mutex>
 #include <map>
+#include <thread>
 #include <vector>
 
+#include <sched.h>
+
+#include "mfe_box.cuh"
 #include "mfe_internal.h"
 
 namespace mfe {
@@ -611,6 +616,79 @@ mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double*
   return st;
 }
 
+namespace {
+
+// Host threads the layout check may use: the CPUs this process may run on.
+int host_threads()
+{
+  cpu_set_t set;
+  CPU_ZERO(&set);
+  int n = 0;
+  if (sched_getaffinity(0, sizeof(set), &set) == 0) n = CPU_COUNT(&set);
+  if (n <= 0) n = (int)std::thread::hardware_concurrency();
+  return std::max(1, std::min(n, 64));
+}
+
+// Whether a host CSR is the closed-form 27-point box layout that
+// generate_matrix_structure gives every miniFE matrix (rows in node order,
+// ascending in-box neighbour columns): dimensions from row 0 (node (0,0,0):
+// columns 0, 1, Nx, Nx + 1, NxNy, ...), then every row offset and column
+// compared with the closed form, rows split over the host threads.
+bool host_box_layout(int64_t n, int64_t nnz, const int32_t* ro, const int32_t* cols, int* bx,
+                     int* by, int* bz)
+{
+  if (n < 8 || nnz < 8 || ro[0] != 0 || ro[1] != 8 || cols[0] != 0 || cols[1] != 1) return false;
+  const int64_t Nx = cols[2], NxNy = cols[4];
+  if (Nx < 2 || NxNy < 2 * Nx || NxNy % Nx != 0 || n % NxNy != 0) return false;
+  const int64_t Ny = NxNy / Nx, Nz = n / NxNy;
+  if (Nz < 2 || box_nnz((int)Nx - 1, (int)Ny - 1, (int)Nz - 1) != nnz) return false;
+  if ((int64_t)ro[n] != nnz) return false;
+  std::atomic<bool> ok{true};
+  const int nt = (int)std::min<int64_t>(host_threads(), std::max<int64_t>(1, n / 65536));
+  auto work = [&](int t) {
+    const int64_t r0 = n * t / nt, r1 = n * (t + 1) / nt;
+    int ix = (int)(r0 % Nx), iy = (int)((r0 / Nx) % Ny), iz = (int)(r0 / NxNy);
+    for (int64_t r = r0; r < r1; ++r) {
+      if (((r - r0) & 4095) == 0 && !ok.load(std::memory_order_relaxed)) return;
+      int64_t k = row_offset(ix, iy, iz, (int)Nx, (int)Ny, (int)Nz);
+      bool good = ro[r] == k;
+      for (int dz = -1; dz <= 1; ++dz) {
+        if (iz + dz < 0 || iz + dz >= Nz) continue;
+        for (int dy = -1; dy <= 1; ++dy) {
+          if (iy + dy < 0 || iy + dy >= Ny) continue;
+          const int64_t base = r + dz * NxNy + dy * Nx;
+          for (int dx = -1; dx <= 1; ++dx) {
+            if (ix + dx < 0 || ix + dx >= Nx) continue;
+            good &= cols[k++] == base + dx;
+          }
+        }
+      }
+      if (!good) {
+        ok.store(false, std::memory_order_relaxed);
+        return;
+      }
+      if (++ix == Nx) {
+        ix = 0;
+        if (++iy == Ny) {
+          iy = 0;
+          ++iz;
+        }
+      }
+    }
+  };
+  std::vector<std::thread> pool;
+  for (int t = 1; t < nt; ++t) pool.emplace_back(work, t);
+  work(0);
+  for (auto& th : pool) th.join();
+  if (!ok.load()) return false;
+  *bx = (int)Nx - 1;
+  *by = (int)Ny - 1;
+  *bz = (int)Nz - 1;
+  return true;
+}
+
+}  // namespace
+
 mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz, const int32_t* ro,
                              const int32_t* cols, const double* vals, const double* b, double* x,
                              const mfe_cg_opts* opts, mfe_cg_result* result)
@@ -625,20 +703,44 @@ mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz, const int
   A.ncols = nrows;
   A.nnz = nnz;
   A.dtype = MFE_F64;
-  A.row_offsets = static_cast<int32_t*>(workspace(ctx, "host.ro", sizeof(int32_t) * (size_t)(nrows + 1)));
-  A.cols = static_cast<int32_t*>(workspace(ctx, "host.cols", sizeof(int32_t) * (size_t)(nnz + 4)));
   A.vals = workspace(ctx, "host.vals", sizeof(double) * (size_t)(nnz + 4));
   double* db = static_cast<double*>(workspace(ctx, "host.b", sizeof(double) * (size_t)std::max<int64_t>(nrows, 1)));
   double* dx = static_cast<double*>(workspace(ctx, "host.x", sizeof(double) * (size_t)std::max<int64_t>(nrows, 1)));
-  if (!A.row_offsets || !A.cols || !A.vals || !db || !dx)
-    return fail(ctx, MFE_OOM, "device allocation for host operands failed");
+  if (!A.vals || !db || !dx) return fail(ctx, MFE_OOM, "device allocation for host operands failed");
   cudaStream_t s = ctx->stream;
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.row_offsets, ro, sizeof(int32_t) * (size_t)(nrows + 1), cudaMemcpyHostToDevice, s));
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.cols, cols, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, s));
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  // the values and vectors go first; while the copy engine moves them the
+  // host threads check the row offsets and columns against the box layout
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
-  mfe_status st = mfe_cg_solve(ctx, &A, db, dx, opts, result);
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  mfe_cg_opts o;
+  if (opts) o = *opts;
+  else mfe_cg_opts_default(&o);
+  // The FP64 solver without preconditioner reads a box matrix's structure in
+  // closed form only (box SpMV, stencil check and stencil SpMV), so a CSR
+  // whose layout the host has verified is solved without copying its
+  // 4 B-per-nonzero column indices and row offsets.
+  int bx = 0, by = 0, bz = 0;
+  const bool box = o.precision == MFE_PREC_F64 && o.precond == 0 &&
+                   getenv("MFE_SPMV_GENERIC") == nullptr &&
+                   host_box_layout(nrows, nnz, ro, cols, &bx, &by, &bz);
+  // device arrays for the structure: filled only when the layout is not the box's
+  A.row_offsets = static_cast<int32_t*>(workspace(ctx, "host.ro", sizeof(int32_t) * (size_t)(nrows + 1)));
+  A.cols = static_cast<int32_t*>(workspace(ctx, box ? "host.ro" : "host.cols",
+                                           box ? sizeof(int32_t) * (size_t)(nrows + 1)
+                                               : sizeof(int32_t) * (size_t)(nnz + 4)));
+  if (!A.row_offsets || !A.cols) return fail(ctx, MFE_OOM, "device allocation for host operands failed");
+  if (box) {
+    A.box_nx = bx;
+    A.box_ny = by;
+    A.box_nz = bz;
+    A.max_row_len = 27;
+  } else {
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.row_offsets, ro, sizeof(int32_t) * (size_t)(nrows + 1),
+                                      cudaMemcpyHostToDevice, s));
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.cols, cols, sizeof(int32_t) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  }
+  mfe_status st = mfe_cg_solve(ctx, &A, db, dx, &o, result);
   if (st != MFE_OK && st != MFE_BREAKDOWN && st != MFE_MAXITER) return st;
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)nrows, cudaMemcpyDeviceToHost, s));
   MFE_CUDA_TRY(ctx, cudaStreamSynchronize(s));

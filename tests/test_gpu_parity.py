@@ -517,3 +517,29 @@ def test_verify_solution_matches_oracle(dims, whole):
         rco, erro = O.verify_solution(*dims, xs, whole=whole)
         assert rc == rco
         assert abs(err - erro) <= 1e-12, (err, erro)
+
+
+@pytest.mark.parametrize("op", ["auto", "csr"])
+def test_cg_host_dropin_box_and_perturbed(op):
+    """The host drop-in call on a box CSR (its layout checked on the host,
+    the structure not copied) and on the same CSR with the last row's
+    columns rotated (values rotated with them: the same operator, another
+    layout, so the structure is copied and the generic path solves it): both
+    agree with the oracle."""
+    dims = (11, 6, 9)
+    ro, cols, vals, bo = O.build_system(*dims)
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=500, tol=1e-10, tol_mode=1)
+    for perturb in (False, True):
+        c2, v2 = cols.copy(), vals.copy()
+        if perturb:
+            a, e = ro[-2], ro[-1]
+            c2[a:e] = np.roll(c2[a:e], 1)
+            v2[a:e] = np.roll(v2[a:e], 1)
+        x = np.zeros(ro.size - 1)
+        res = M.cg_solve_host(ro, c2, v2, bo, x, max_iter=500, tol=1e-10, tol_mode="relative",
+                              f64_operator=op)
+        assert res.status == 0
+        assert abs(res.num_iters - it) <= 1
+        assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)
+        expect = "stencil64" if op == "auto" and not perturb else "none"
+        assert res.inner_operator == expect
