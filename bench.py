@@ -692,6 +692,7 @@ def bench_multi(args, world, stream):
         ts.append(res[0].times[4])
     t = max_over_ranks(world, sum(ts) / len(ts))
     out = {"rhs": 32, "system": "128^3", "value": t, "unit": "s",
+           "inner_operator": res[0].inner_operator,
            "iterations_max": max(r.num_iters for r in res),
            "reliable_updates": res[0].refinements,
            "all_converged": all(r.status == 0 for r in res),

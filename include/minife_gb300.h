@@ -291,7 +291,7 @@ typedef struct mfe_cg_opts {
                            0 = the verified FP64 stencil operator when A is a
                            miniFE box operator whose interior stencil is
                            mirror-symmetric (every box miniFE assembles with
-                           k = 1) and the tolerance is at least 2^-33 of the
+                           k = 1) and the tolerance is at least 2^-36 of the
                            initial residual: every row is dd * x_r (Dirichlet node) or
                            the interior stencil with the Dirichlet neighbours
                            zeroed, every entry within 2^-40 of its row's

@@ -513,19 +513,22 @@ def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,
 def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPSILON,
                    tol_mode: str = "absolute", precision: str = "mixed", refine_k: int = 0,
                    ctx: Context | None = None, inner_tol: float = 0.0,
-                   max_refine: int = 0) -> list:
+                   max_refine: int = 0, mixed_operator: str = "auto") -> list:
     """nrhs independent CG solves on one box matrix advanced together (one
     matrix read per iteration for all of them).  B, X: device (n, nrhs) FP64,
     contiguous; X holds the initial guesses and receives the solutions.
     nrhs divides 32.  precision "f64" runs the reference's CG per column
     (ref/src/cg_solve.hpp:69); "mixed" runs FP32 products with FP64 reliable
-    updates.  Returns one CGResult per right-hand side."""
+    updates: with 32 columns on the verified FP32 stencil operator where it
+    applies (mixed_operator "auto"), else on the FP32 values ("values").
+    Returns one CGResult per right-hand side."""
     ctx = ctx or default_context()
     if B.dim() != 2 or tuple(X.shape) != tuple(B.shape):
         raise ValueError("B and X must be (n, nrhs) with the same shape")
     nrhs = B.shape[1]
     m = A.c()
-    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine)
+    o, _ = _opts(max_iter, tol, tol_mode, precision, refine_k, inner_tol, max_refine,
+                 mixed_operator=mixed_operator)
     res = (MfeCgResult * nrhs)()
     st = ctx.lib.mfe_cg_solve_multi(ctx.h, ctypes.byref(m), nrhs, _ptr(B), _ptr(X),
                                     ctypes.byref(o), res)

@@ -486,14 +486,14 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
     MFE_TRY(launch_spmv(ctx, &A, x, B.r, &sink, b, B.st));
   }
   // The verified FP64 stencil operator (checked on every call) when the
-  // tolerance is at least 2^-33 of the initial residual: the operator lies
+  // tolerance is at least 2^-36 of the initial residual: the operator lies
   // within 2^-39 of every entry of A, so tighter stops (the reference's
   // absolute DBL_EPSILON) would meet its rounding-level difference from A
   // and use the CSR values.
   if (o->f64_operator == 0 && csr_is_box(&A)) {
     MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(CgState), cudaMemcpyDeviceToHost, ctx->stream));
     MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (!hs->err && hs->tol_abs >= std::ldexp(hs->normr0, -33))
+    if (!hs->err && hs->tol_abs >= std::ldexp(hs->normr0, -36))
       MFE_TRY(stencil64_prepare(ctx, &A, B.w8, &B.dd, &B.st64));  // overwrites hs
   }
 

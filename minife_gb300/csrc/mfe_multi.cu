@@ -123,9 +123,26 @@ __device__ void multi_dot_reduce(double v, double* red, double* partials, unsign
   __syncthreads();
   if (!am_last) return;
   __threadfence();
+  // every warp of the last block sums the partials of blocks warp,
+  // warp + nw, ... (four accumulators keep four L2 loads in flight), then
+  // the warps' sums are added in warp order: a fixed order for a fixed grid
+  {
+    const unsigned g = gridDim.x, uw = (unsigned)warp, unw = (unsigned)nw;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0;
+    unsigned bl = uw;
+    for (; bl + 3 * unw < g; bl += 4 * unw) {
+      s0 += __ldcg(&partials[(size_t)bl * 32 + lane]);
+      s1 += __ldcg(&partials[(size_t)(bl + unw) * 32 + lane]);
+      s2 += __ldcg(&partials[(size_t)(bl + 2 * unw) * 32 + lane]);
+      s3 += __ldcg(&partials[(size_t)(bl + 3 * unw) * 32 + lane]);
+    }
+    for (; bl < g; bl += unw) s0 += __ldcg(&partials[(size_t)bl * 32 + lane]);
+    red[warp * 32 + lane] = (s0 + s1) + (s2 + s3);
+  }
+  __syncthreads();
   if (threadIdx.x < nlanes) {
     double s = 0.0;
-    for (unsigned bl = 0; bl < gridDim.x; ++bl) s += __ldcg(&partials[(size_t)bl * 32 + threadIdx.x]);
+    for (int w = 0; w < nw; ++w) s += red[w * 32 + threadIdx.x];
     out[threadIdx.x] = s;
     if (cg)
       cg->alpha[threadIdx.x] = cg->done[threadIdx.x] || !(s > 0.0) ? 0.0 : cg->rr[threadIdx.x] / s;
@@ -632,6 +649,148 @@ __global__ void __launch_bounds__(kEThreads, 2) k_spmm_ell32(Ell32Params P)
   multi_dot_reduce(warp < 2 ? 0.0 : facc.value(), red, P.partials, P.ticket, P.st->pAp, 32, P.st);
 }
 
+// ---------------------------------------------------------------------------
+// FP32 A P for exactly 32 right-hand sides on the verified FP32 stencil
+// operator of the mixed solver (mfe_stencil.cu: every row dd * x_r or the
+// interior stencil with Dirichlet neighbours zeroed, checked on the matrix
+// on every call) with mirror-symmetric weights: P and AP are the only
+// traffic, 256 bytes per row, instead of 368 with the padded values.  A
+// warp owns four adjacent positions of the xy plane, one lane per
+// right-hand side, and marches a chunk of z steps: each plane's window
+// (lines y - 1, y, y + 1 at positions p - 1 .. p + 4) is six 128-byte rows
+// per line, read coalesced, reduced once to the class sums a, sx, sy, sxy of
+// its four rows, and combined as in the FP64 stencil kernel
+// (mfe_stencil64.cu): P1(z) = w4 a + w5 sx + w6 sy + w7 sxy, Q(z) = P1(z-1)
+// + w0 a + w1 sx + w2 sy + w3 sxy, AP(z) = Q(z) + P1(z+1).  The masks of
+// Dirichlet neighbours are the same for the whole warp (one set of
+// positions), so no lane diverges.  Work items are (z chunk, position
+// tile), z-chunk major, so the warps resident together share lines through
+// L2.  p.Ap per right-hand side in double-float, then multi_dot_reduce.
+// ---------------------------------------------------------------------------
+constexpr int kSMW = 8;    // warps per CTA
+constexpr int kSMKP = 4;   // positions per warp
+constexpr int kSMZC = 32;  // z steps per work item
+
+struct MSt32Params {
+  int Nx, Ny, Nz, NxNy, ntile, nzc;
+  float w[8];  // mirror-class weights, class 4|dz| + 2|dy| + |dx|
+  float dd;    // Dirichlet diagonal
+  const float* __restrict__ p;  // n x 32
+  float* __restrict__ Ap;       // n x 32
+  double* partials;
+  unsigned* ticket;
+  MultiState* st;
+};
+
+__global__ void __launch_bounds__(kSMW * 32) k_spmm_st32(const __grid_constant__ MSt32Params P)
+{
+  constexpr int KP = kSMKP, W = KP + 2;
+  __shared__ double red[kSMW * 32];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t items = (int64_t)P.nzc * P.ntile;
+  DFAcc facc;
+  for (int64_t it = (int64_t)blockIdx.x * kSMW + warp; it < items; it += (int64_t)gridDim.x * kSMW) {
+    const int zc = (int)(it / P.ntile), tile = (int)(it - (int64_t)zc * P.ntile);
+    const int za = zc * kSMZC, zb = min(P.Nz, za + kSMZC);
+    const int p0 = tile * KP;
+    // bit W j + t: window entry (line y + j - 1, position p0 - 1 + t) is an
+    // interior node (its row lies inside the plane), the same for all lanes
+    unsigned mask = 0;
+#pragma unroll
+    for (int t = 0; t < W; ++t) {
+      const int pp = p0 - 1 + t;
+      if (pp >= 0 && pp < P.NxNy) {
+        const int iy = pp / P.Nx, ix = pp - iy * P.Nx;
+        const bool inx = ix >= 1 && ix <= P.Nx - 2;
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+          const int jy = iy + j - 1;
+          if (inx && jy >= 1 && jy <= P.Ny - 2) mask |= 1u << (W * j + t);
+        }
+      }
+    }
+    bool valid[KP], bnd[KP];
+#pragma unroll
+    for (int r = 0; r < KP; ++r) {
+      valid[r] = p0 + r < P.NxNy;
+      bnd[r] = !((mask >> (W + 1 + r)) & 1u);
+    }
+    auto row_of = [&](int z, int off) { return ((int64_t)z * P.NxNy + p0 + off) * 32 + lane; };
+    auto plane = [&](int z, const float* P1in, float* P1, float* Qo, float* cen) {
+#pragma unroll
+      for (int r = 0; r < KP; ++r) cen[r] = valid[r] ? __ldg(P.p + row_of(z, r)) : 0.0f;
+      if (z <= 0 || z >= P.Nz - 1) {
+#pragma unroll
+        for (int r = 0; r < KP; ++r) P1[r] = Qo[r] = 0.0f;
+        return;
+      }
+      float v[3 * W];
+#pragma unroll
+      for (int j = 0; j < 3; ++j)
+#pragma unroll
+        for (int t = 0; t < W; ++t) {
+          const int sl = W * j + t;
+          const bool m = (mask >> sl) & 1u;
+          if (j == 1 && t >= 1 && t <= KP) v[sl] = m ? cen[t - 1] : 0.0f;
+          else v[sl] = m ? __ldg(P.p + row_of(z, (j - 1) * P.Nx + t - 1)) : 0.0f;
+        }
+      float e[W];
+#pragma unroll
+      for (int t = 0; t < W; ++t) e[t] = v[t] + v[2 * W + t];
+#pragma unroll
+      for (int r = 0; r < KP; ++r) {
+        const float a = v[W + 1 + r];
+        const float sx = v[W + r] + v[W + r + 2];
+        const float sy = e[1 + r];
+        const float sxy = e[r] + e[r + 2];
+        float p1 = P.w[4] * a;
+        p1 = fmaf(P.w[5], sx, p1);
+        p1 = fmaf(P.w[6], sy, p1);
+        P1[r] = fmaf(P.w[7], sxy, p1);
+        float qv = fmaf(P.w[0], a, P1in[r]);
+        qv = fmaf(P.w[1], sx, qv);
+        qv = fmaf(P.w[2], sy, qv);
+        Qo[r] = fmaf(P.w[3], sxy, qv);
+      }
+    };
+    float P1c[KP], Qc[KP], cc[KP];
+#pragma unroll
+    for (int r = 0; r < KP; ++r) P1c[r] = 0.0f;
+    if (za >= 1) {
+      float zq[KP], qd[KP], cd[KP];
+#pragma unroll
+      for (int r = 0; r < KP; ++r) zq[r] = 0.0f;
+      plane(za - 1, zq, P1c, qd, cd);
+    }
+    {
+      float P1n[KP];
+      plane(za, P1c, P1n, Qc, cc);
+#pragma unroll
+      for (int r = 0; r < KP; ++r) P1c[r] = P1n[r];
+    }
+    for (int z = za; z < zb; ++z) {
+      float P1n[KP], Qn[KP], cn[KP];
+#pragma unroll
+      for (int r = 0; r < KP; ++r) P1n[r] = Qn[r] = cn[r] = 0.0f;
+      if (z + 1 < P.Nz) plane(z + 1, P1c, P1n, Qn, cn);
+#pragma unroll
+      for (int r = 0; r < KP; ++r) {
+        float yv;
+        if (z == 0 || z == P.Nz - 1 || bnd[r]) yv = P.dd * cc[r];
+        else yv = Qc[r] + P1n[r];
+        if (valid[r]) {
+          P.Ap[row_of(z, r)] = yv;
+          facc.add_product(yv, cc[r]);
+        }
+        P1c[r] = P1n[r];
+        Qc[r] = Qn[r];
+        cc[r] = cn[r];
+      }
+    }
+  }
+  multi_dot_reduce(facc.value(), red, P.partials, P.ticket, P.st->pAp, 32, P.st);
+}
+
 // FP64 box CSR -> FP32 padded 28-per-row values (slot order, zeros outside
 // the box and in the pad); rows n .. are left as the caller zeroed them
 __global__ void k_mr_ell28(int Nx, int Ny, int Nz, const double* __restrict__ vals,
@@ -1059,6 +1218,12 @@ struct MultiBufs {
   unsigned* err;
   const float* ell = nullptr;  // mixed, 32 right-hand sides: padded values (p has ghost zones)
   int ell_grid = 0;
+  // mixed, 32 right-hand sides, verified mirror-symmetric FP32 stencil:
+  // k_spmm_st32 with these weights (takes precedence over ell)
+  bool st32 = false;
+  float w8[8] = {};
+  float dd = 0.0f;
+  int st32_grid = 0;
 };
 
 size_t ell32_smem() { return (size_t)2 * kEStage * sizeof(float); }
@@ -1107,7 +1272,24 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
   k_mr_p<float><<<vgrid(ctx, ntot, k_mr_p<float>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.x32, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_p"));
-  if (W.ell) {
+  if (W.st32) {
+    MSt32Params S;
+    S.Nx = A64.box_nx + 1;
+    S.Ny = A64.box_ny + 1;
+    S.Nz = A64.box_nz + 1;
+    S.NxNy = S.Nx * S.Ny;
+    S.ntile = (int)ceil_div(S.NxNy, (int64_t)kSMKP);
+    S.nzc = (int)ceil_div(S.Nz, (int64_t)kSMZC);
+    for (int c = 0; c < 8; ++c) S.w[c] = W.w8[c];
+    S.dd = W.dd;
+    S.p = W.p;
+    S.Ap = W.Ap;
+    S.partials = W.partials;
+    S.ticket = W.tickets;
+    S.st = W.st;
+    k_spmm_st32<<<W.st32_grid, kSMW * 32, 0, ctx->stream>>>(S);
+    MFE_TRY(check_launch(ctx, "k_spmm_st32"));
+  } else if (W.ell) {
     Ell32Params E;
     E.n = (int)A64.nrows;
     E.Nx = A64.box_nx + 1;
@@ -1270,7 +1452,15 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   // partial tile).  The FP32 operator (padded or CSR values) is rebuilt on
   // every call: a cache keyed on the values pointer would go stale when an
   // allocator hands the same address to another matrix.
-  const bool use_ell = mixed && nrhs == 32 && getenv("MFE_MULTI_CSR") == nullptr;
+  // mixed with 32 right-hand sides on a verified mirror-symmetric FP32
+  // stencil (every miniFE box with k = 1): the stencil SpMM, no FP32 matrix
+  bool use_st32 = false;
+  float coef32[28] = {}, w8[8] = {};
+  if (mixed && nrhs == 32 && o->mixed_operator == 0 && getenv("MFE_MULTI_CSR") == nullptr) {
+    MFE_TRY(stencil_prepare(ctx, &A64, coef32, &use_st32));
+    use_st32 = use_st32 && stencil_mirror_classes(coef32, w8);
+  }
+  const bool use_ell = mixed && nrhs == 32 && !use_st32 && getenv("MFE_MULTI_CSR") == nullptr;
   mfe_csr A32 = A64;
   if (mixed && !use_ell) {
     float* v32 = static_cast<float*>(
@@ -1282,6 +1472,15 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   } else if (mixed) {
     A32.vals = nullptr;
     A32.dtype = MFE_F32;
+  }
+  int st32_grid = 0;
+  if (use_st32) {
+    const int64_t items = ceil_div((int64_t)(A64.box_nx + 1) * (A64.box_ny + 1), (int64_t)kSMKP) *
+                          ceil_div((int64_t)(A64.box_nz + 1), (int64_t)kSMZC);
+    st32_grid = (int)std::max<int64_t>(
+        1, std::min<int64_t>({ceil_div(items, (int64_t)kSMW),
+                              (int64_t)resident_blocks(ctx, (const void*)k_spmm_st32, kSMW * 32, 0),
+                              (int64_t)kMaxPartM}));
   }
   const size_t vb = (mixed ? sizeof(float) : sizeof(double)) * (size_t)(ntot + 8);
   void* r = workspace(ctx, "multi.r", vb);
@@ -1362,6 +1561,12 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
   if (mixed) {
     MultiBufs<float> W{static_cast<float*>(r), static_cast<float*>(p), static_cast<float*>(Ap),
                        x32, dst, partials, tickets, err, ell, ell_grid};
+    if (use_st32) {
+      W.st32 = true;
+      for (int c = 0; c < 8; ++c) W.w8[c] = w8[c];
+      W.dd = coef32[27];
+      W.st32_grid = st32_grid;
+    }
     MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
       return multi_iter_mixed(ctx, A32, A64, nrhs, B, X, W, h, in_graph);
     }));
@@ -1391,7 +1596,8 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
     res.times[4] = ms * 1e-3;
     res.refinements = hs->updates;
     res.fp64_spmvs = mixed ? hs->updates + 1 : hs->k + 1;
-    res.inner_operator = !mixed ? MFE_INNER_NONE : (ell ? MFE_INNER_PADDED : MFE_INNER_VALUES);
+    res.inner_operator = !mixed ? MFE_INNER_NONE
+                                : (use_st32 ? MFE_INNER_STENCIL : (ell ? MFE_INNER_PADDED : MFE_INNER_VALUES));
     const bool converged = mixed ? hs->done[j] != 0 && !hs->brk[j]
                                  : !(hs->normr_true[j] > hs->tol_abs[j]);
     res.status = hs->brk[j] ? MFE_BREAKDOWN : (converged ? MFE_OK : MFE_MAXITER);

@@ -224,3 +224,36 @@ def test_multi_column_breakdown_is_local():
             rel = np.linalg.norm(Bh[:, j] - O.matvec(ro, cols, vals, Xh[:, j])) / \
                 np.linalg.norm(Bh[:, j])
             assert rel <= 1e-9, (prec, j, rel)
+
+
+@pytest.mark.parametrize("dims", [(16, 16, 16), (23, 9, 14), (4, 6, 5)])
+def test_multi_mixed_stencil_and_padded_values_agree(dims):
+    """32 right-hand sides in mixed precision with the stencil SpMM (the
+    verified FP32 stencil) and with the padded FP32 values: both reach the
+    1e-8 relative residual checked in FP64 with the oracle's matvec, their
+    iteration counts agree within 10 %, and one product of each (two inner
+    iterations from x = 0 differ only by the operator's FP32 rounding)
+    gives the same solutions to FP32 accuracy."""
+    A, b = M.build_system(*dims)
+    B = rhs_block(b, 32, seed=41)
+    ro, cols, vals, _ = O.build_system(*dims)
+    Bh = host(B)
+    its = {}
+    for op, name in (("auto", "stencil"), ("values", "padded")):
+        X = torch.zeros_like(B)
+        res = M.cg_solve_multi(A, B, X, max_iter=3000, tol=1e-8, tol_mode="relative",
+                               precision="mixed", mixed_operator=op)
+        assert all(r.status == 0 for r in res)
+        assert res[0].inner_operator == name
+        Xh = host(X)
+        for j in range(32):
+            rel = np.linalg.norm(Bh[:, j] - O.matvec(ro, cols, vals, Xh[:, j])) / np.linalg.norm(Bh[:, j])
+            assert rel <= 1e-8, (op, j, rel)
+        its[op] = max(r.num_iters for r in res)
+        X2 = torch.zeros_like(B)
+        M.cg_solve_multi(A, B, X2, max_iter=2, tol=1e-8, tol_mode="relative", precision="mixed",
+                         mixed_operator=op, refine_k=1000)
+        its[op + "_x2"] = host(X2)
+    assert abs(its["auto"] - its["values"]) <= 0.1 * its["values"] + 2
+    d = np.abs(its["auto_x2"] - its["values_x2"]).max()
+    assert d <= 1e-5 * np.abs(its["values_x2"]).max()

@@ -169,7 +169,7 @@ def test_dot_waxpby():
 def expected_operator(dims, op, tight=False):
     """The FP64 operator a solve of a miniFE box uses: the verified stencil
     needs an interior class along every dimension (>= 4 elements) and a
-    tolerance of at least 2^-33 of the initial residual (tight: the
+    tolerance of at least 2^-36 of the initial residual (tight: the
     reference's absolute DBL_EPSILON stop is far below it)."""
     return "stencil64" if op == "auto" and min(dims) >= 4 and not tight else "none"
 
