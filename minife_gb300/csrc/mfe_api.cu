@@ -644,35 +644,56 @@ bool host_box_layout(int64_t n, int64_t nnz, const int32_t* ro, const int32_t* c
   if (Nz < 2 || box_nnz((int)Nx - 1, (int)Ny - 1, (int)Nz - 1) != nnz) return false;
   if ((int64_t)ro[n] != nnz) return false;
   std::atomic<bool> ok{true};
+  // rows are checked line by line (fixed iy, iz); on a line with 1 <= iy <=
+  // Ny - 2 and 1 <= iz <= Nz - 2 the rows 1 .. Nx - 2 hold all 27 columns,
+  // r + off[k] for fixed offsets, and their offsets step by 27
+  int64_t off[27];
+  {
+    int k = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx) off[k++] = dz * NxNy + dy * Nx + dx;
+  }
+  auto general_row = [&](int64_t r, int ix, int iy, int iz) {
+    int64_t k = row_offset(ix, iy, iz, (int)Nx, (int)Ny, (int)Nz);
+    bool good = ro[r] == k;
+    for (int dz = -1; dz <= 1; ++dz) {
+      if (iz + dz < 0 || iz + dz >= Nz) continue;
+      for (int dy = -1; dy <= 1; ++dy) {
+        if (iy + dy < 0 || iy + dy >= Ny) continue;
+        const int64_t base = r + dz * NxNy + dy * Nx;
+        for (int dx = -1; dx <= 1; ++dx) {
+          if (ix + dx < 0 || ix + dx >= Nx) continue;
+          good &= cols[k++] == base + dx;
+        }
+      }
+    }
+    return good;
+  };
+  const int64_t nlines = Ny * Nz;
   const int nt = (int)std::min<int64_t>(host_threads(), std::max<int64_t>(1, n / 65536));
   auto work = [&](int t) {
-    const int64_t r0 = n * t / nt, r1 = n * (t + 1) / nt;
-    int ix = (int)(r0 % Nx), iy = (int)((r0 / Nx) % Ny), iz = (int)(r0 / NxNy);
-    for (int64_t r = r0; r < r1; ++r) {
-      if (((r - r0) & 4095) == 0 && !ok.load(std::memory_order_relaxed)) return;
-      int64_t k = row_offset(ix, iy, iz, (int)Nx, (int)Ny, (int)Nz);
-      bool good = ro[r] == k;
-      for (int dz = -1; dz <= 1; ++dz) {
-        if (iz + dz < 0 || iz + dz >= Nz) continue;
-        for (int dy = -1; dy <= 1; ++dy) {
-          if (iy + dy < 0 || iy + dy >= Ny) continue;
-          const int64_t base = r + dz * NxNy + dy * Nx;
-          for (int dx = -1; dx <= 1; ++dx) {
-            if (ix + dx < 0 || ix + dx >= Nx) continue;
-            good &= cols[k++] == base + dx;
-          }
+    const int64_t l0 = nlines * t / nt, l1 = nlines * (t + 1) / nt;
+    for (int64_t l = l0; l < l1; ++l) {
+      if (!ok.load(std::memory_order_relaxed)) return;
+      const int iy = (int)(l % Ny), iz = (int)(l / Ny);
+      const int64_t r0 = l * Nx;
+      bool good = general_row(r0, 0, iy, iz) && general_row(r0 + Nx - 1, (int)Nx - 1, iy, iz);
+      if (iy >= 1 && iy <= Ny - 2 && iz >= 1 && iz <= Nz - 2) {
+        const int64_t k0 = row_offset(1, iy, iz, (int)Nx, (int)Ny, (int)Nz);
+        for (int ix = 1; ix <= Nx - 2 && good; ++ix) {
+          const int64_t r = r0 + ix, k = k0 + 27 * (int64_t)(ix - 1);
+          bool g = ro[r] == k;
+          const int32_t* c = cols + k;
+          for (int q = 0; q < 27; ++q) g &= (int64_t)c[q] == r + off[q];
+          good = g;
         }
+      } else {
+        for (int ix = 1; ix <= Nx - 2 && good; ++ix) good = general_row(r0 + ix, ix, iy, iz);
       }
       if (!good) {
         ok.store(false, std::memory_order_relaxed);
         return;
-      }
-      if (++ix == Nx) {
-        ix = 0;
-        if (++iy == Ny) {
-          iy = 0;
-          ++iz;
-        }
       }
     }
   };

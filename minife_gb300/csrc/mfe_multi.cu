@@ -682,11 +682,111 @@ struct MSt32Params {
   MultiState* st;
 };
 
+// One work item (positions p0 .. p0 + 3, planes za .. zb - 1) of
+// k_spmm_st32.  MASKED: some window entry is not an interior node (masks and
+// Dirichlet rows apply); otherwise every window entry of every plane is
+// interior and the loads need neither predicates nor selects.  Rows of the
+// item are row (z, r) = z NxNy + p0 + r, lane = right-hand side.
+template <bool MASKED>
+__device__ __forceinline__ void st32_item(const MSt32Params& P, int p0, int za, int zb, unsigned mask,
+                                          DFAcc& facc)
+{
+  constexpr int KP = kSMKP, W = KP + 2;
+  const int lane = threadIdx.x & 31;
+  const int64_t line = (int64_t)P.Nx * 32, plane_stride = (int64_t)P.NxNy * 32;
+  // element (plane z, line y + j - 1, position p0 - 1 + t) of lane's column:
+  // pz + (j - 1) * line + 32 t, pz = the plane's window origin
+  const float* const p_org = P.p + ((int64_t)p0 - 1) * 32 + lane;
+  bool valid[KP], bnd[KP];
+#pragma unroll
+  for (int r = 0; r < KP; ++r) {
+    valid[r] = !MASKED || p0 + r < P.NxNy;
+    bnd[r] = MASKED && !((mask >> (W + 1 + r)) & 1u);
+  }
+  auto plane = [&](int z, const float* P1in, float* P1, float* Qo, float* cen) {
+    const float* pz = p_org + (int64_t)z * plane_stride;
+#pragma unroll
+    for (int r = 0; r < KP; ++r) cen[r] = valid[r] ? __ldg(pz + 32 * (r + 1)) : 0.0f;
+    if (z <= 0 || z >= P.Nz - 1) {  // a Dirichlet plane (uniform)
+#pragma unroll
+      for (int r = 0; r < KP; ++r) P1[r] = Qo[r] = 0.0f;
+      return;
+    }
+    float v[3 * W];
+#pragma unroll
+    for (int j = 0; j < 3; ++j)
+#pragma unroll
+      for (int t = 0; t < W; ++t) {
+        const int sl = W * j + t;
+        if (j == 1 && t >= 1 && t <= KP) {
+          v[sl] = MASKED && !((mask >> sl) & 1u) ? 0.0f : cen[t - 1];
+        } else {
+          const float* a = pz + (j - 1) * line + 32 * t;
+          v[sl] = MASKED ? (((mask >> sl) & 1u) ? __ldg(a) : 0.0f) : __ldg(a);
+        }
+      }
+    float e[W];
+#pragma unroll
+    for (int t = 0; t < W; ++t) e[t] = v[t] + v[2 * W + t];
+#pragma unroll
+    for (int r = 0; r < KP; ++r) {
+      const float a = v[W + 1 + r];
+      const float sx = v[W + r] + v[W + r + 2];
+      const float sy = e[1 + r];
+      const float sxy = e[r] + e[r + 2];
+      float p1 = P.w[4] * a;
+      p1 = fmaf(P.w[5], sx, p1);
+      p1 = fmaf(P.w[6], sy, p1);
+      P1[r] = fmaf(P.w[7], sxy, p1);
+      float qv = fmaf(P.w[0], a, P1in[r]);
+      qv = fmaf(P.w[1], sx, qv);
+      qv = fmaf(P.w[2], sy, qv);
+      Qo[r] = fmaf(P.w[3], sxy, qv);
+    }
+  };
+  float P1c[KP], Qc[KP], cc[KP];
+#pragma unroll
+  for (int r = 0; r < KP; ++r) P1c[r] = 0.0f;
+  if (za >= 1) {
+    float zq[KP], qd[KP], cd[KP];
+#pragma unroll
+    for (int r = 0; r < KP; ++r) zq[r] = 0.0f;
+    plane(za - 1, zq, P1c, qd, cd);
+  }
+  {
+    float P1n[KP];
+    plane(za, P1c, P1n, Qc, cc);
+#pragma unroll
+    for (int r = 0; r < KP; ++r) P1c[r] = P1n[r];
+  }
+  float* yz = P.Ap + ((int64_t)za * P.NxNy + p0) * 32 + lane;
+  for (int z = za; z < zb; ++z) {
+    float P1n[KP], Qn[KP], cn[KP];
+#pragma unroll
+    for (int r = 0; r < KP; ++r) P1n[r] = Qn[r] = cn[r] = 0.0f;
+    if (z + 1 < P.Nz) plane(z + 1, P1c, P1n, Qn, cn);
+    const bool dplane = z == 0 || z == P.Nz - 1;
+#pragma unroll
+    for (int r = 0; r < KP; ++r) {
+      const float yv = (dplane || bnd[r]) ? P.dd * cc[r] : Qc[r] + P1n[r];
+      if (valid[r]) {
+        yz[32 * r] = yv;
+        facc.add_product(yv, cc[r]);
+      }
+      P1c[r] = P1n[r];
+      Qc[r] = Qn[r];
+      cc[r] = cn[r];
+    }
+    yz += plane_stride;
+  }
+}
+
 __global__ void __launch_bounds__(kSMW * 32) k_spmm_st32(const __grid_constant__ MSt32Params P)
 {
   constexpr int KP = kSMKP, W = KP + 2;
+  constexpr unsigned kAll = (1u << (3 * W)) - 1u;
   __shared__ double red[kSMW * 32];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int warp = threadIdx.x >> 5;
   const int64_t items = (int64_t)P.nzc * P.ntile;
   DFAcc facc;
   for (int64_t it = (int64_t)blockIdx.x * kSMW + warp; it < items; it += (int64_t)gridDim.x * kSMW) {
@@ -709,84 +809,10 @@ __global__ void __launch_bounds__(kSMW * 32) k_spmm_st32(const __grid_constant__
         }
       }
     }
-    bool valid[KP], bnd[KP];
-#pragma unroll
-    for (int r = 0; r < KP; ++r) {
-      valid[r] = p0 + r < P.NxNy;
-      bnd[r] = !((mask >> (W + 1 + r)) & 1u);
-    }
-    auto row_of = [&](int z, int off) { return ((int64_t)z * P.NxNy + p0 + off) * 32 + lane; };
-    auto plane = [&](int z, const float* P1in, float* P1, float* Qo, float* cen) {
-#pragma unroll
-      for (int r = 0; r < KP; ++r) cen[r] = valid[r] ? __ldg(P.p + row_of(z, r)) : 0.0f;
-      if (z <= 0 || z >= P.Nz - 1) {
-#pragma unroll
-        for (int r = 0; r < KP; ++r) P1[r] = Qo[r] = 0.0f;
-        return;
-      }
-      float v[3 * W];
-#pragma unroll
-      for (int j = 0; j < 3; ++j)
-#pragma unroll
-        for (int t = 0; t < W; ++t) {
-          const int sl = W * j + t;
-          const bool m = (mask >> sl) & 1u;
-          if (j == 1 && t >= 1 && t <= KP) v[sl] = m ? cen[t - 1] : 0.0f;
-          else v[sl] = m ? __ldg(P.p + row_of(z, (j - 1) * P.Nx + t - 1)) : 0.0f;
-        }
-      float e[W];
-#pragma unroll
-      for (int t = 0; t < W; ++t) e[t] = v[t] + v[2 * W + t];
-#pragma unroll
-      for (int r = 0; r < KP; ++r) {
-        const float a = v[W + 1 + r];
-        const float sx = v[W + r] + v[W + r + 2];
-        const float sy = e[1 + r];
-        const float sxy = e[r] + e[r + 2];
-        float p1 = P.w[4] * a;
-        p1 = fmaf(P.w[5], sx, p1);
-        p1 = fmaf(P.w[6], sy, p1);
-        P1[r] = fmaf(P.w[7], sxy, p1);
-        float qv = fmaf(P.w[0], a, P1in[r]);
-        qv = fmaf(P.w[1], sx, qv);
-        qv = fmaf(P.w[2], sy, qv);
-        Qo[r] = fmaf(P.w[3], sxy, qv);
-      }
-    };
-    float P1c[KP], Qc[KP], cc[KP];
-#pragma unroll
-    for (int r = 0; r < KP; ++r) P1c[r] = 0.0f;
-    if (za >= 1) {
-      float zq[KP], qd[KP], cd[KP];
-#pragma unroll
-      for (int r = 0; r < KP; ++r) zq[r] = 0.0f;
-      plane(za - 1, zq, P1c, qd, cd);
-    }
-    {
-      float P1n[KP];
-      plane(za, P1c, P1n, Qc, cc);
-#pragma unroll
-      for (int r = 0; r < KP; ++r) P1c[r] = P1n[r];
-    }
-    for (int z = za; z < zb; ++z) {
-      float P1n[KP], Qn[KP], cn[KP];
-#pragma unroll
-      for (int r = 0; r < KP; ++r) P1n[r] = Qn[r] = cn[r] = 0.0f;
-      if (z + 1 < P.Nz) plane(z + 1, P1c, P1n, Qn, cn);
-#pragma unroll
-      for (int r = 0; r < KP; ++r) {
-        float yv;
-        if (z == 0 || z == P.Nz - 1 || bnd[r]) yv = P.dd * cc[r];
-        else yv = Qc[r] + P1n[r];
-        if (valid[r]) {
-          P.Ap[row_of(z, r)] = yv;
-          facc.add_product(yv, cc[r]);
-        }
-        P1c[r] = P1n[r];
-        Qc[r] = Qn[r];
-        cc[r] = cn[r];
-      }
-    }
+    if (mask == kAll)
+      st32_item<false>(P, p0, za, zb, mask, facc);
+    else
+      st32_item<true>(P, p0, za, zb, mask, facc);
   }
   multi_dot_reduce(facc.value(), red, P.partials, P.ticket, P.st->pAp, 32, P.st);
 }

@@ -522,17 +522,20 @@ def test_verify_solution_matches_oracle(dims, whole):
 @pytest.mark.parametrize("op", ["auto", "csr"])
 def test_cg_host_dropin_box_and_perturbed(op):
     """The host drop-in call on a box CSR (its layout checked on the host,
-    the structure not copied) and on the same CSR with the last row's
-    columns rotated (values rotated with them: the same operator, another
-    layout, so the structure is copied and the generic path solves it): both
+    the structure not copied) and on the same CSR with one row's columns
+    rotated (values rotated with them: the same operator, another layout, so
+    the structure is copied and the generic path solves it) -- the last row
+    (a boundary line) and an interior row (the check's 27-column path): all
     agree with the oracle."""
     dims = (11, 6, 9)
     ro, cols, vals, bo = O.build_system(*dims)
     xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=500, tol=1e-10, tol_mode=1)
-    for perturb in (False, True):
+    Nx, Ny = dims[0] + 1, dims[1] + 1
+    interior = 5 + Nx * (3 + Ny * 4)
+    for perturb in (None, ro.size - 2, interior):
         c2, v2 = cols.copy(), vals.copy()
-        if perturb:
-            a, e = ro[-2], ro[-1]
+        if perturb is not None:
+            a, e = ro[perturb], ro[perturb + 1]
             c2[a:e] = np.roll(c2[a:e], 1)
             v2[a:e] = np.roll(v2[a:e], 1)
         x = np.zeros(ro.size - 1)
@@ -541,5 +544,5 @@ def test_cg_host_dropin_box_and_perturbed(op):
         assert res.status == 0
         assert abs(res.num_iters - it) <= 1
         assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)
-        expect = "stencil64" if op == "auto" and not perturb else "none"
+        expect = "stencil64" if op == "auto" and perturb is None else "none"
         assert res.inner_operator == expect
