@@ -381,12 +381,18 @@ def run_gpu(args):
     if not args.no_mixed:
         x64 = x.clone()
         xm = torch.zeros_like(b)
+        from minife_gb300 import autotune
+        if args.refine_k > 0:
+            mcfg = {"refine_k": args.refine_k, "inner_tol": 0.01, "cached": None}
+        else:
+            mcfg = autotune.tune_mixed(A, b, tol=TOL, reps=1)
 
         def time_mixed(A32):
+            kw = dict(max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed",
+                      refine_k=mcfg["refine_k"], inner_tol=mcfg["inner_tol"], A32=A32)
             for _ in range(args.warmup):
                 xm.zero_()
-                M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
-                           precision="mixed", refine_k=args.refine_k, A32=A32)
+                M.cg_solve(A, b, xm, **kw)
             torch.cuda.synchronize()
             barrier(world)
             m0 = torch.cuda.Event(enable_timing=True)
@@ -394,8 +400,7 @@ def run_gpu(args):
             m0.record(stream)
             for _ in range(args.steps):
                 xm.zero_()
-                rm = M.cg_solve(A, b, xm, max_iter=5000, tol=TOL, tol_mode="relative",
-                                precision="mixed", refine_k=args.refine_k, A32=A32)
+                rm = M.cg_solve(A, b, xm, **kw)
             m1.record(stream)
             torch.cuda.synchronize()
             barrier(world)
@@ -411,7 +416,8 @@ def run_gpu(args):
                  "speedup_vs_fp64_csr_values": t_csr / t_mixed,
                  "inner_operator": rm.inner_operator,
                  "inner_iterations": rm.num_iters, "reliable_updates": rm.refinements,
-                 "refine_k": args.refine_k, "status": rm.status,
+                 "tuning": {"refine_k": mcfg["refine_k"], "inner_tol": mcfg["inner_tol"]},
+                 "tuned_from_cache": mcfg.get("cached"), "status": rm.status,
                  "final_rel_resid_fp64": rm.final_resid / rm.normr0,
                  "err_vs_fp64_solution": {"rel_l2": float(diff.norm() / x64.norm()),
                                           "max_abs": float(diff.abs().max())},
@@ -672,40 +678,51 @@ def bench_batch(args, world, stream):
 
 def bench_multi(args, world, stream):
     """32 seeded random-normal right-hand sides on the 128^3 system, solved
-    together (one SpMM per iteration) in mixed precision to 1e-8 relative."""
+    together (one SpMM per iteration) in mixed precision to 1e-8 relative,
+    launch shape and reliable-update policy from the autotuner; beside it the
+    same 32 solves one after another with the single-box mixed solver
+    (its own tuned policy for this box)."""
     import torch
     import minife_gb300 as M
+    from minife_gb300 import autotune
     A, b = M.build_system(128, 128, 128)
     g = torch.Generator(device="cpu").manual_seed(0)
     B = torch.randn(A.nrows, 32, generator=g, dtype=torch.float64).cuda().contiguous()
     X = torch.zeros_like(B)
+    cfg = autotune.tune_multi(A, B, X, tol=TOL, reps=1)
+    kw = dict(max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed",
+              refine_k=cfg["refine_k"], inner_tol=cfg["inner_tol"])
     for _ in range(max(1, args.warmup - 1)):
         X.zero_()
-        M.cg_solve_multi(A, B, X, max_iter=5000, tol=TOL, tol_mode="relative", precision="mixed")
+        M.cg_solve_multi(A, B, X, **kw)
     torch.cuda.synchronize()
     barrier(world)
     ts = []
     for _ in range(args.steps):
         X.zero_()
-        res = M.cg_solve_multi(A, B, X, max_iter=5000, tol=TOL, tol_mode="relative",
-                               precision="mixed")
+        res = M.cg_solve_multi(A, B, X, **kw)
         ts.append(res[0].times[4])
     t = max_over_ranks(world, sum(ts) / len(ts))
     out = {"rhs": 32, "system": "128^3", "value": t, "unit": "s",
            "inner_operator": res[0].inner_operator,
+           "tuning": {k: cfg[k] for k in ("z_chunk", "refine_k", "inner_tol")},
+           "tuned_from_cache": cfg.get("cached", False),
            "iterations_max": max(r.num_iters for r in res),
            "reliable_updates": res[0].refinements,
            "all_converged": all(r.status == 0 for r in res),
            "max_rel_resid": max(r.final_resid / r.normr0 for r in res)}
     if not args.no_seq:
+        scfg = autotune.tune_mixed(A, b, tol=TOL, reps=1)
         t_seq = 0.0
         for j in range(32):
             bj = B[:, j].contiguous()
             xj = torch.zeros_like(bj)
             r = M.cg_solve(A, bj, xj, max_iter=5000, tol=TOL, tol_mode="relative",
-                           precision="mixed", refine_k=50)
+                           precision="mixed", refine_k=scfg["refine_k"],
+                           inner_tol=scfg["inner_tol"])
             t_seq += r.total_time
         out["sequential_mixed_s"] = t_seq
+        out["sequential_tuning"] = {"refine_k": scfg["refine_k"], "inner_tol": scfg["inner_tol"]}
         out["speedup_vs_sequential"] = t_seq / t
     return out
 
@@ -794,8 +811,9 @@ def main():
                     help="skip the 32-right-hand-side solve")
     ap.add_argument("--no-seq", action="store_true",
                     help="skip the sequential baselines of the batched and multi-RHS solves")
-    ap.add_argument("--refine-k", type=int, default=100,
-                    help="mixed solver: reliable update at least every k inner iterations")
+    ap.add_argument("--refine-k", type=int, default=0,
+                    help="mixed solver: reliable update at least every k inner iterations "
+                         "(0: the autotuner's choice)")
     ap.add_argument("--ref-dims", type=int, default=DIMS[0],
                     help="reference arm: box edge of the system (the metric's is 256)")
     ap.add_argument("--ref-warmup-iters", type=int, default=20,

@@ -403,6 +403,14 @@ mfe_status mfe_box_zero_boundary(mfe_ctx* ctx, int nx, int ny, int nz, double* v
  * thread-per-(row, column) CSR kernel. */
 mfe_status mfe_spmm(mfe_ctx* ctx, const mfe_csr* A, int32_t nrhs, const void* X, void* Y);
 
+/* Launch shape of the multi-RHS solver on ctx (the autotuner's knob; no
+ * counterpart in the reference): z_chunk = z steps per work item of the
+ * 32-column stencil SpMM, 4..1024 (0 = the default, 32). */
+typedef struct mfe_multi_tuning {
+  int32_t z_chunk;
+} mfe_multi_tuning;
+mfe_status mfe_multi_set_tuning(mfe_ctx* ctx, const mfe_multi_tuning* t);
+
 /* Multi-RHS CG on one matrix: nrhs independent CG solves (each with its own
  * alpha/beta and stopping test) advanced together so every iteration reads A
  * once.  B, X row-major (i*nrhs + j), device, FP64; opts as for mfe_cg_solve

@@ -32,7 +32,7 @@ __all__ = [
     "MiniFEError", "Context", "CSRMatrix", "CGResult", "default_context", "box_dims",
     "generate_matrix_structure", "assemble_FE_data", "impose_dirichlet", "box_bc_rows",
     "build_system", "matvec", "matvec_and_dot", "dot", "dot_f32", "waxpby", "fused_waxpby",
-    "inject_wait_timeout", "Stencil64", "matvec_stencil64", "cg_solve",
+    "inject_wait_timeout", "Stencil64", "matvec_stencil64", "set_multi_tuning", "cg_solve",
     "cg_solve_host", "cg_solve_multi", "Batch", "batch_solve_boxes", "verify_solution",
     "element_gradient", "to_f32", "spmm", "ELLMatrix", "matvec_ell", "cg_solve_ell",
 ]
@@ -535,6 +535,15 @@ def cg_solve_multi(A: CSRMatrix, B, X, max_iter: int = 200, tol: float = DBL_EPS
     if st not in (0, _abi.MFE_BREAKDOWN, _abi.MFE_MAXITER):
         ctx.check(st, "mfe_cg_solve_multi")
     return [_cg_result(r) for r in res]
+
+
+def set_multi_tuning(z_chunk: int = 0, ctx: Context | None = None):
+    """Launch shape of the multi-RHS solver on the context
+    (mfe_multi_set_tuning): z steps per work item of the 32-column stencil
+    SpMM (0: the default)."""
+    ctx = ctx or default_context()
+    t = _abi.MfeMultiTuning(int(z_chunk))
+    ctx.check(ctx.lib.mfe_multi_set_tuning(ctx.h, ctypes.byref(t)), "mfe_multi_set_tuning")
 
 
 class Batch:

@@ -58,6 +58,10 @@ class MfeStencil64(ctypes.Structure):
                 ("reserved", c_int32), ("w", c_double * 8), ("dd", c_double)]
 
 
+class MfeMultiTuning(ctypes.Structure):
+    _fields_ = [("z_chunk", c_int32)]
+
+
 class MfeEll(ctypes.Structure):
     _fields_ = [("nrows", c_int64), ("ncols_per_row", c_int32), ("dtype", c_int32),
                 ("cols", c_void_p), ("vals", c_void_p)]
@@ -124,6 +128,7 @@ SIGNATURES = {
                          [c_void_p, c_void_p, _P(MfeCgOpts), c_void_p, c_void_p, _P(c_double),
                           _P(MfeCgResult), _P(MfeCgResult)]),
     "mfe_spmm": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_int32, c_void_p, c_void_p]),
+    "mfe_multi_set_tuning": (ctypes.c_int, [c_void_p, _P(MfeMultiTuning)]),
     "mfe_cg_solve_multi": (ctypes.c_int, [c_void_p, _P(MfeCsr), c_int32, c_void_p, c_void_p,
                                           _P(MfeCgOpts), _P(MfeCgResult)]),
     "mfe_batch_solve_boxes": (ctypes.c_int, [c_void_p, c_int32, c_void_p, _P(MfeCgOpts),

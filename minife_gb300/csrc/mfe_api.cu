@@ -575,6 +575,15 @@ mfe_status mfe_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, 
   return read_scalar(ctx, d, result);
 }
 
+mfe_status mfe_multi_set_tuning(mfe_ctx* ctx, const mfe_multi_tuning* t)
+{
+  if (!ctx || !t) return MFE_BAD_ARG;
+  if (t->z_chunk != 0 && (t->z_chunk < 4 || t->z_chunk > 1024))
+    return fail(ctx, MFE_BAD_ARG, "z_chunk must be 0 or lie in [4, 1024]");
+  ctx->multi_zchunk = t->z_chunk;
+  return MFE_OK;
+}
+
 mfe_status mfe_inject_wait_timeout(mfe_ctx* ctx, int64_t wait_ns)
 {
   if (!ctx) return MFE_BAD_ARG;

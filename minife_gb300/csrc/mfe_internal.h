@@ -34,6 +34,9 @@ struct mfe_ctx {
   // mfe_inject_wait_timeout: the next box-structured SpMV launched outside a
   // graph capture withholds its copies; its waits give up after this long
   uint64_t inject_wait_ns = 0;
+  // launch shape of the multi-RHS stencil SpMM (mfe_multi_set_tuning): z
+  // steps per work item, 0 = the default
+  int multi_zchunk = 0;
 };
 
 namespace mfe {

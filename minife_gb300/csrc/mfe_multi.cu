@@ -669,10 +669,10 @@ __global__ void __launch_bounds__(kEThreads, 2) k_spmm_ell32(Ell32Params P)
 // ---------------------------------------------------------------------------
 constexpr int kSMW = 8;    // warps per CTA
 constexpr int kSMKP = 4;   // positions per warp
-constexpr int kSMZC = 32;  // z steps per work item
+constexpr int kSMZC = 32;  // default z steps per work item (mfe_multi_set_tuning)
 
 struct MSt32Params {
-  int Nx, Ny, Nz, NxNy, ntile, nzc;
+  int Nx, Ny, Nz, NxNy, ntile, nzc, zc;  // zc: z steps per work item
   float w[8];  // mirror-class weights, class 4|dz| + 2|dy| + |dx|
   float dd;    // Dirichlet diagonal
   const float* __restrict__ p;  // n x 32
@@ -791,7 +791,7 @@ __global__ void __launch_bounds__(kSMW * 32) k_spmm_st32(const __grid_constant__
   DFAcc facc;
   for (int64_t it = (int64_t)blockIdx.x * kSMW + warp; it < items; it += (int64_t)gridDim.x * kSMW) {
     const int zc = (int)(it / P.ntile), tile = (int)(it - (int64_t)zc * P.ntile);
-    const int za = zc * kSMZC, zb = min(P.Nz, za + kSMZC);
+    const int za = zc * P.zc, zb = min(P.Nz, za + P.zc);
     const int p0 = tile * KP;
     // bit W j + t: window entry (line y + j - 1, position p0 - 1 + t) is an
     // interior node (its row lies inside the plane), the same for all lanes
@@ -1250,6 +1250,7 @@ struct MultiBufs {
   float w8[8] = {};
   float dd = 0.0f;
   int st32_grid = 0;
+  int st32_zc = kSMZC;
 };
 
 size_t ell32_smem() { return (size_t)2 * kEStage * sizeof(float); }
@@ -1305,7 +1306,8 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
     S.Nz = A64.box_nz + 1;
     S.NxNy = S.Nx * S.Ny;
     S.ntile = (int)ceil_div(S.NxNy, (int64_t)kSMKP);
-    S.nzc = (int)ceil_div(S.Nz, (int64_t)kSMZC);
+    S.zc = W.st32_zc;
+    S.nzc = (int)ceil_div(S.Nz, (int64_t)S.zc);
     for (int c = 0; c < 8; ++c) S.w[c] = W.w8[c];
     S.dd = W.dd;
     S.p = W.p;
@@ -1500,9 +1502,10 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
     A32.dtype = MFE_F32;
   }
   int st32_grid = 0;
+  const int st32_zc = ctx->multi_zchunk > 0 ? ctx->multi_zchunk : kSMZC;
   if (use_st32) {
     const int64_t items = ceil_div((int64_t)(A64.box_nx + 1) * (A64.box_ny + 1), (int64_t)kSMKP) *
-                          ceil_div((int64_t)(A64.box_nz + 1), (int64_t)kSMZC);
+                          ceil_div((int64_t)(A64.box_nz + 1), (int64_t)st32_zc);
     st32_grid = (int)std::max<int64_t>(
         1, std::min<int64_t>({ceil_div(items, (int64_t)kSMW),
                               (int64_t)resident_blocks(ctx, (const void*)k_spmm_st32, kSMW * 32, 0),
@@ -1592,6 +1595,7 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
       for (int c = 0; c < 8; ++c) W.w8[c] = w8[c];
       W.dd = coef32[27];
       W.st32_grid = st32_grid;
+      W.st32_zc = st32_zc;
     }
     MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
       return multi_iter_mixed(ctx, A32, A64, nrhs, B, X, W, h, in_graph);

@@ -84,3 +84,73 @@ def test_stencil_batch_skips_shape_search(cache):
     shapes = {c[0][:2] for c in b.calls if c[2] == 0.0}
     assert shapes == {autotune.SHAPES[0]}   # one capped trial, then chunks only
     assert cfg["inner_operator"] == "stencil" and cfg["refine_k"] == 50
+
+
+class _Vec:
+    """Stand-in for a device vector: shape, new_zeros and zero_."""
+
+    shape = (8, 32)
+
+    def new_zeros(self, shape):
+        return _Vec()
+
+    def zero_(self):
+        return self
+
+
+class _Box:
+    box = (16, 16, 16)
+
+
+class _CG:
+    def __init__(self, t, status):
+        self.total_time = t
+        self.status = status
+        self.times = (0.0, 0.0, 0.0, 0.0, t)
+
+
+def test_tune_mixed_searches_refine_k_10_to_50(cache, monkeypatch):
+    """refine_k over 10..50 x inner_tol: the fastest converging pair wins,
+    is cached, and a second call is a cache hit with no solves."""
+    import minife_gb300 as M
+    seen = []
+
+    def fake_cg(A, b, x, max_iter, tol, tol_mode, precision, refine_k, inner_tol):
+        seen.append((refine_k, inner_tol))
+        t = 1.0 + abs(refine_k - 30) / 100 + (0.05 if inner_tol == 0.1 else 0.0)
+        return _CG(t, 5 if refine_k == 10 else 0)  # k = 10 fails to converge
+
+    monkeypatch.setattr(M, "cg_solve", fake_cg)
+    cfg = autotune.tune_mixed(_Box(), _Vec(), reps=1)
+    assert (cfg["refine_k"], cfg["inner_tol"]) == (30, 0.01) and not cfg["cached"]
+    assert {k for k, _ in seen} == set(autotune.SINGLE_REFINE_K)
+    assert min(autotune.SINGLE_REFINE_K) == 10 and max(autotune.SINGLE_REFINE_K) == 50
+    seen.clear()
+    cfg2 = autotune.tune_mixed(_Box(), _Vec(), reps=1)
+    assert cfg2["cached"] and seen == [] and cfg2["refine_k"] == 30
+
+
+def test_tune_multi_picks_z_chunk_then_refine(cache, monkeypatch):
+    import minife_gb300 as M
+    state = {"zc": 0}
+    applied = []
+
+    def fake_set(z):
+        state["zc"] = z
+        applied.append(z)
+
+    def fake_multi(A, B, X, max_iter, tol, tol_mode, precision, refine_k, inner_tol):
+        if tol == 0.0:  # capped probe: z chunk 64 fastest
+            t = {16: 1.3, 32: 1.1, 64: 1.0}[state["zc"]]
+            return [_CG(t, 5)] * 2
+        t = {25: 2.0, 50: 1.5, 100: 1.2}[refine_k] + (0.1 if inner_tol == 0.01 else 0.0)
+        return [_CG(t, 0)] * 2
+
+    monkeypatch.setattr(M, "set_multi_tuning", fake_set)
+    monkeypatch.setattr(M, "cg_solve_multi", fake_multi)
+    cfg = autotune.tune_multi(_Box(), _Vec(), _Vec(), reps=1)
+    assert (cfg["z_chunk"], cfg["refine_k"], cfg["inner_tol"]) == (64, 100, 0.1)
+    assert applied[-1] == 64
+    applied.clear()
+    cfg2 = autotune.tune_multi(_Box(), _Vec(), _Vec(), reps=1)
+    assert cfg2["cached"] and applied == [64]
