@@ -40,7 +40,7 @@ SHAPES = [(256, 2), (256, 3), (256, 4), (128, 2), (128, 3), (128, 4)]
 SINGLE_REFINE_K = [10, 20, 30, 40, 50]
 SINGLE_INNER_TOL = [0.1, 0.01]
 # multi-RHS: stencil SpMM z steps per item, then refine_k x inner_tol
-MULTI_ZCHUNK = [16, 32, 64]
+MULTI_ZCHUNK = [8, 16, 32, 64]
 MULTI_REFINE_K = [25, 50, 100]
 MULTI_INNER_TOL = [0.1, 0.01]
 CHUNKS = [4096, 8192, 16384, 32768]

@@ -10,11 +10,17 @@
 // :80-100, SparseMatrix_functions.hpp:183-255):
 //   1. element pass: one thread per element computes its 36-entry symmetric
 //      diffusion matrix and 8-entry source vector into a structure-of-arrays
-//      scratch (coalesced writes);
+//      scratch (coalesced writes); the Jacobian's three columns come from
+//      per-axis tables (an element's x column depends on its x pair only),
+//      computed once per box with the reference's operations in its order;
 //   2. node gather: one thread per node row reads the rows of its (up to) 8
 //      adjacent element matrices, in ascending element order, into 27 stencil
 //      accumulators, applies both Dirichlet passes in registers, and writes
 //      the CSR row (staged through shared memory for coalescing).
+// The passes alternate over slabs of kSlab element planes: the scratch is a
+// ring of kSlab + 1 element planes (element plane z in slot z mod (kSlab +
+// 1)), so a slab's gather still finds the previous slab's last plane, and
+// the scratch is (kSlab + 1) nx ny elements instead of nx ny nz.
 // No atomics: every coefficient is summed in the reference's element order.
 #include <algorithm>
 #include <cmath>
@@ -85,26 +91,83 @@ __global__ void __launch_bounds__(kStructRows)
 // element pass
 // ---------------------------------------------------------------------------
 constexpr int kElemThreads = 128;
+constexpr int kSlab = 16;  // element planes per slab; the ring holds kSlab + 1
 
-// Element e = (ex, ey, ez) in BoxIterator order (x fastest).  Writes
-// ke[k * E + e] (k < 36, upper triangle) and fe[k * E + e] (k < 8).
-__global__ void __launch_bounds__(kElemThreads)
-    k_element(int nx, int ny, int nz, int64_t E, const double* __restrict__ kappa,
-              double* __restrict__ ke, double* __restrict__ fe)
+// Per-axis Jacobian columns: jc[(base_axis + i) * 24 + gp * 3 + a] for
+// element index i along the axis (base: 0 for x, nx for y, nx + ny for z),
+// with the coordinate pair of elem_corner().
+__global__ void k_jcols(int nx, int ny, int nz, double* __restrict__ jc)
 {
-  const int64_t e = (int64_t)blockIdx.x * kElemThreads + threadIdx.x;
-  if (e >= E) return;
-  const int ex = (int)(e % nx);
-  const int ey = (int)((e / nx) % ny);
-  const int ez = (int)(e / ((int64_t)nx * ny));
-  const ElemCorner c = elem_corner(ex, ey, ez, nx, ny, nz);
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int n = (nx + ny + nz) * 8;
+  if (t >= n) return;
+  const int gp = t % 8, row = t / 8;
+  int axis, i;
+  double c0, c1;
+  if (row < nx) {
+    axis = 0;
+    i = row;
+    c0 = (1.0 * (double)i) / (double)nx;
+    c1 = c0 + 1.0 / nx;
+  } else if (row < nx + ny) {
+    axis = 1;
+    i = row - nx;
+    c0 = 1.0 * (double)i / (double)ny;
+    c1 = c0 + 1.0 / ny;
+  } else {
+    axis = 2;
+    i = row - nx - ny;
+    c0 = (1.0 * (double)i) / (double)nz;
+    c1 = c0 + 1.0 / nz;
+  }
+  double col[3];
+  jacobian_column(c_hex8, axis, c0, c1, gp, col);
+  double* o = jc + (int64_t)row * 24 + gp * 3;
+  o[0] = col[0];
+  o[1] = col[1];
+  o[2] = col[2];
+}
+
+// Elements of planes ez0 .. ez0 + nplanes - 1 in BoxIterator order (x
+// fastest).  Element (ex, ey, ez) goes to ring index ri = ((ez mod R) ny + ey)
+// nx + ex: ke[k * RS + ri] (k < 36, upper triangle), fe[k * RS + ri] (k < 8),
+// RS = R nx ny.  kappa (nullable) is indexed by the global element id.
+__global__ void __launch_bounds__(kElemThreads)
+    k_element(int nx, int ny, int nz, int ez0, int nplanes, int R, const double* __restrict__ kappa,
+              const double* __restrict__ jc, double* __restrict__ ke, double* __restrict__ fe)
+{
+  const int64_t nxny = (int64_t)nx * ny;
+  const int64_t el = (int64_t)blockIdx.x * kElemThreads + threadIdx.x;
+  if (el >= nxny * nplanes) return;
+  const int ex = (int)(el % nx);
+  const int ey = (int)((el / nx) % ny);
+  const int ez = ez0 + (int)(el / nxny);
+  const int64_t e = ex + (int64_t)nx * (ey + (int64_t)ny * ez);
+  const int64_t RS = (int64_t)R * nxny;
+  const int64_t ri = ((int64_t)(ez % R) * ny + ey) * nx + ex;
   const double k = kappa ? kappa[e] : 1.0;
+  const double* cx = jc + (int64_t)ex * 24;
+  const double* cy = jc + ((int64_t)nx + ey) * 24;
+  const double* cz = jc + ((int64_t)nx + ny + ez) * 24;
   double em[36], ev[8];
-  element_matrix_vector(c_hex8, c, k, em, ev);
+  element_matrix_vector_j(
+      c_hex8,
+      [&](int gp, double J[9]) {
+        J[0] = __ldg(cx + gp * 3);
+        J[3] = __ldg(cx + gp * 3 + 1);
+        J[6] = __ldg(cx + gp * 3 + 2);
+        J[1] = __ldg(cy + gp * 3);
+        J[4] = __ldg(cy + gp * 3 + 1);
+        J[7] = __ldg(cy + gp * 3 + 2);
+        J[2] = __ldg(cz + gp * 3);
+        J[5] = __ldg(cz + gp * 3 + 1);
+        J[8] = __ldg(cz + gp * 3 + 2);
+      },
+      k, em, ev);
 #pragma unroll
-  for (int i = 0; i < 36; ++i) ke[i * E + e] = em[i];
+  for (int i = 0; i < 36; ++i) ke[i * RS + ri] = em[i];
 #pragma unroll
-  for (int i = 0; i < 8; ++i) fe[i * E + e] = ev[i];
+  for (int i = 0; i < 8; ++i) fe[i * RS + ri] = ev[i];
 }
 
 // ---------------------------------------------------------------------------
@@ -112,20 +175,23 @@ __global__ void __launch_bounds__(kElemThreads)
 // ---------------------------------------------------------------------------
 constexpr int kGatherRows = 128;
 
+// Rows of node planes iz0 .. iz1 - 1; their adjacent elements are in the
+// ring (ke, fe as k_element writes them).
 __global__ void __launch_bounds__(kGatherRows)
-    k_gather(int nx, int ny, int nz, int64_t E, const double* __restrict__ ke,
+    k_gather(int nx, int ny, int nz, int iz0, int iz1, int R, const double* __restrict__ ke,
              const double* __restrict__ fe, const int32_t* __restrict__ ro,
              double* __restrict__ vals, double* __restrict__ b, int impose_bc)
 {
   __shared__ double s_vals[kGatherRows * 27];
   const int Nx = nx + 1, Ny = ny + 1, Nz = nz + 1;
   const int64_t NxNy = (int64_t)Nx * Ny;
-  const int64_t N = NxNy * Nz;
-  const int64_t r0 = (int64_t)blockIdx.x * kGatherRows;
+  const int64_t RS = (int64_t)R * nx * ny;
+  const int64_t R1 = NxNy * iz1;
+  const int64_t r0 = NxNy * iz0 + (int64_t)blockIdx.x * kGatherRows;
   const int64_t r = r0 + threadIdx.x;
-  const int64_t rend = min(r0 + (int64_t)kGatherRows, N);
+  const int64_t rend = min(r0 + (int64_t)kGatherRows, R1);
   const int64_t base = ro[r0];
-  if (r < N) {
+  if (r < R1) {
     const int ix = (int)(r % Nx), iy = (int)((r / Nx) % Ny), iz = (int)(r / NxNy);
     const bool bc1 = (ix == Nx - 1);
     const bool bc0 = (ix == 0 || iy == 0 || iz == 0 || iy == Ny - 1 || iz == Nz - 1);
@@ -157,7 +223,7 @@ __global__ void __launch_bounds__(kGatherRows)
           for (int a = 0; a < 2; ++a) {
             const int ex = ix - 1 + a;
             if (ex < 0 || ex >= nx || ey < 0 || ey >= ny || ez < 0 || ez >= nz) continue;
-            const int64_t e = ex + (int64_t)nx * (ey + (int64_t)ny * ez);
+            const int64_t e = ((int64_t)(ez % R) * ny + ey) * nx + ex;
             const int lr = local_node(1 - a, 1 - bb, 1 - c);
 #pragma unroll
             for (int m = 0; m < 8; ++m) {
@@ -165,9 +231,9 @@ __global__ void __launch_bounds__(kGatherRows)
               const int my = (m == 2 || m == 3 || m == 6 || m == 7);
               const int mz = (m >= 4);
               const int slot = (c + mz) * 9 + (bb + my) * 3 + (a + mx);
-              acc[slot] += __ldg(&ke[(int64_t)sym_index(lr, m) * E + e]);
+              acc[slot] += __ldg(&ke[(int64_t)sym_index(lr, m) * RS + e]);
             }
-            bsum += __ldg(&fe[(int64_t)lr * E + e]);
+            bsum += __ldg(&fe[(int64_t)lr * RS + e]);
           }
         }
       }
@@ -487,17 +553,29 @@ mfe_status launch_assemble(mfe_ctx* ctx, int nx, int ny, int nz, const double* k
                            const int32_t* ro, double* vals, double* b, int impose_bc)
 {
   MFE_TRY(ensure_tables(ctx));
-  const int64_t E = (int64_t)nx * ny * nz;
-  const int64_t N = (int64_t)(nx + 1) * (ny + 1) * (nz + 1);
-  double* ke = static_cast<double*>(workspace(ctx, "assembly.ke", sizeof(double) * 44 * E));
-  if (!ke) return fail(ctx, MFE_OOM, "assembly scratch allocation failed");
-  double* fe = ke + 36 * E;
-  k_element<<<(unsigned)ceil_div(E, kElemThreads), kElemThreads, 0, ctx->stream>>>(
-      nx, ny, nz, E, kappa, ke, fe);
-  MFE_TRY(check_launch(ctx, "k_element"));
-  k_gather<<<(unsigned)ceil_div(N, kGatherRows), kGatherRows, 0, ctx->stream>>>(
-      nx, ny, nz, E, ke, fe, ro, vals, b, impose_bc);
-  return check_launch(ctx, "k_gather");
+  const int64_t nxny = (int64_t)nx * ny;
+  const int64_t NxNy = (int64_t)(nx + 1) * (ny + 1);
+  const int R = std::min(kSlab, nz) + 1;
+  double* jc = static_cast<double*>(workspace(ctx, "assembly.jcols",
+                                              sizeof(double) * 24 * (size_t)(nx + ny + nz)));
+  double* ke = static_cast<double*>(workspace(ctx, "assembly.ring", sizeof(double) * 44 * R * nxny));
+  if (!jc || !ke) return fail(ctx, MFE_OOM, "assembly scratch allocation failed");
+  double* fe = ke + 36 * R * nxny;
+  k_jcols<<<(unsigned)ceil_div((int64_t)(nx + ny + nz) * 8, 128), 128, 0, ctx->stream>>>(nx, ny, nz, jc);
+  MFE_TRY(check_launch(ctx, "k_jcols"));
+  for (int ez0 = 0; ez0 < nz; ez0 += kSlab) {
+    const int np = std::min(kSlab, nz - ez0);
+    k_element<<<(unsigned)ceil_div(nxny * np, kElemThreads), kElemThreads, 0, ctx->stream>>>(
+        nx, ny, nz, ez0, np, R, kappa, jc, ke, fe);
+    MFE_TRY(check_launch(ctx, "k_element"));
+    // node planes whose elements are all in the ring: ez0 .. ez0 + np - 1,
+    // and the last node plane with the last slab
+    const int iz0 = ez0, iz1 = ez0 + np == nz ? nz + 1 : ez0 + np;
+    k_gather<<<(unsigned)ceil_div(NxNy * (iz1 - iz0), kGatherRows), kGatherRows, 0, ctx->stream>>>(
+        nx, ny, nz, iz0, iz1, R, ke, fe, ro, vals, b, impose_bc);
+    MFE_TRY(check_launch(ctx, "k_gather"));
+  }
+  return MFE_OK;
 }
 
 mfe_status launch_impose_dirichlet(mfe_ctx* ctx, const mfe_csr* A, double* b, double value,

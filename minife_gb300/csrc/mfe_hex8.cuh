@@ -78,9 +78,12 @@ __device__ __forceinline__ void jacobian(const ElemCorner& c, const double (*g)[
 // diffusionMatrix_symm (Hex8.hpp:260-361) with conductivity k, and
 // sourceVector (Hex8.hpp:364-410).  em: 36 upper-triangle entries, row-major;
 // ev: 8 entries.  Both loops walk the Gauss points in the same order and
-// compute the same Jacobian, so they share it.
-__device__ __forceinline__ void element_matrix_vector(const Hex8Tables& T, const ElemCorner& c,
-                                                      double k, double em[36], double ev[8])
+// compute the same Jacobian, so they share it.  jf(gp, J) provides the
+// Jacobian at Gauss point gp (jacobian() from the corner coordinates, or the
+// same values from per-axis tables, jacobian_column()).
+template <typename JF>
+__device__ __forceinline__ void element_matrix_vector_j(const Hex8Tables& T, JF jf, double k,
+                                                        double em[36], double ev[8])
 {
 #pragma unroll
   for (int i = 0; i < 36; ++i) em[i] = 0.0;
@@ -91,7 +94,7 @@ __device__ __forceinline__ void element_matrix_vector(const Hex8Tables& T, const
   for (int gp = 0; gp < 8; ++gp) {
     const double (*g)[3] = T.grad[gp];
     double J[9];
-    jacobian(c, g, J);
+    jf(gp, J);
     const double J00 = J[0], J01 = J[1], J02 = J[2], J10 = J[3], J11 = J[4], J12 = J[5],
                  J20 = J[6], J21 = J[7], J22 = J[8];
     const double term0 = J22 * J11 - J21 * J12;
@@ -136,6 +139,36 @@ __device__ __forceinline__ void element_matrix_vector(const Hex8Tables& T, const
 #pragma unroll
     for (int i = 0; i < 8; ++i) ev[i] += T.psi[gp][i] * term;
   }
+}
+
+__device__ __forceinline__ void element_matrix_vector(const Hex8Tables& T, const ElemCorner& c,
+                                                      double k, double em[36], double ev[8])
+{
+  element_matrix_vector_j(T, [&](int gp, double J[9]) { jacobian(c, T.grad[gp], J); }, k, em, ev);
+}
+
+// The Jacobian's column for physical axis x (entries J[a][0], a = 0..2) sums
+// grad[gp][i][a] * x_i over the element's 8 nodes, whose x is x0 or x1: it
+// depends on the element's x pair only, and likewise for y and z.  Computed
+// with jacobian()'s operations in its order (node order, from 0), the column
+// of an element index along an axis is therefore exact for every element of
+// that index.  axis: 0 x, 1 y, 2 z; (c0, c1) the index's coordinate pair.
+__device__ __forceinline__ void jacobian_column(const Hex8Tables& T, int axis, double c0, double c1,
+                                                int gp, double col[3])
+{
+  double s0 = 0, s1 = 0, s2 = 0;
+#pragma unroll
+  for (int i = 0; i < 8; ++i) {
+    const bool hi = axis == 0 ? (i == 1 || i == 2 || i == 5 || i == 6)
+                              : (axis == 1 ? (i == 2 || i == 3 || i == 6 || i == 7) : (i >= 4));
+    const double v = hi ? c1 : c0;
+    s0 += T.grad[gp][i][0] * v;
+    s1 += T.grad[gp][i][1] * v;
+    s2 += T.grad[gp][i][2] * v;
+  }
+  col[0] = s0;
+  col[1] = s1;
+  col[2] = s2;
 }
 
 // Index of (a, b) in the 36-entry upper triangle (a, b in 0..7).

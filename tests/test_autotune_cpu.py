@@ -141,7 +141,7 @@ def test_tune_multi_picks_z_chunk_then_refine(cache, monkeypatch):
 
     def fake_multi(A, B, X, max_iter, tol, tol_mode, precision, refine_k, inner_tol):
         if tol == 0.0:  # capped probe: z chunk 64 fastest
-            t = {16: 1.3, 32: 1.1, 64: 1.0}[state["zc"]]
+            t = {8: 1.4, 16: 1.3, 32: 1.1, 64: 1.0}[state["zc"]]
             return [_CG(t, 5)] * 2
         t = {25: 2.0, 50: 1.5, 100: 1.2}[refine_k] + (0.1 if inner_tol == 0.01 else 0.0)
         return [_CG(t, 0)] * 2
