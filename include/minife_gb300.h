@@ -223,6 +223,11 @@ mfe_status mfe_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double*
                             double beta, const double* y, double* w, double alpha2,
                             const double* x2, double beta2, const double* y2, double* w2);
 
+/* Packing of a halo exchange (exchange_externals.hpp:122-124, send_buffer[i]
+ * = x[elements_to_send[i]]): out[i] = x[idx[i]] for i < n, all device
+ * arrays; idx entries must index x. */
+mfe_status mfe_gather(mfe_ctx* ctx, int64_t n, const int32_t* idx, const double* x, double* out);
+
 /* Dot product of FP32 vectors (device) as the mixed-precision solvers form
  * their alpha/beta and residual reductions: every product and sum in
  * double-float on the FP32 pipe (TwoProduct + TwoSum, about 48 significant

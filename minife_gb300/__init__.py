@@ -134,9 +134,12 @@ def box_dims(nx: int, ny: int, nz: int):
 
 class CSRMatrix:
     """Device CSR with the reference CSRMatrix's fields (one rank:
-    rows[i] == i, has_local_indices true, num_cols == nrows)."""
+    rows[i] == i, has_local_indices true, num_cols == nrows; a rank's local
+    matrix of a multi-rank decomposition has num_cols = owned rows plus
+    externals, minife_gb300.halo)."""
 
-    def __init__(self, row_offsets, packed_cols, packed_coefs, box=(0, 0, 0), max_row_len=0):
+    def __init__(self, row_offsets, packed_cols, packed_coefs, box=(0, 0, 0), max_row_len=0,
+                 num_cols=None):
         torch = _torch()
         assert row_offsets.dtype == torch.int32 and packed_cols.dtype == torch.int32
         assert packed_coefs.dtype in (torch.float64, torch.float32)
@@ -146,6 +149,7 @@ class CSRMatrix:
         self.box = tuple(box)
         self.max_row_len = int(max_row_len)
         self.has_local_indices = True
+        self._num_cols = None if num_cols is None else int(num_cols)
 
     @property
     def nrows(self) -> int:
@@ -153,7 +157,7 @@ class CSRMatrix:
 
     @property
     def num_cols(self) -> int:
-        return self.nrows
+        return self.nrows if self._num_cols is None else self._num_cols
 
     @property
     def nnz(self) -> int:
@@ -170,7 +174,7 @@ class CSRMatrix:
         torch = _torch()
         m = MfeCsr()
         m.nrows = self.nrows
-        m.ncols = self.nrows
+        m.ncols = self.num_cols
         m.nnz = self.nnz
         m.row_offsets = self.row_offsets.data_ptr()
         m.cols = self.packed_cols.data_ptr()
@@ -394,6 +398,16 @@ def matvec_stencil64(S: Stencil64, x, y, ctx: Context | None = None):
     ctx.check(ctx.lib.mfe_spmv_stencil64(ctx.h, ctypes.byref(S.s), _ptr(x), _ptr(y)),
               "mfe_spmv_stencil64")
     return y
+
+
+def gather(x, idx, out=None, ctx: Context | None = None):
+    """out[i] = x[idx[i]] on the device (mfe_gather; idx int32)."""
+    torch = _torch()
+    ctx = ctx or default_context()
+    if out is None:
+        out = torch.empty(idx.numel(), dtype=torch.float64, device=x.device)
+    ctx.check(ctx.lib.mfe_gather(ctx.h, idx.numel(), _ptr(idx), _ptr(x), _ptr(out)), "mfe_gather")
+    return out
 
 
 def dot_f32(x, y, ctx: Context | None = None) -> float:

@@ -104,6 +104,7 @@ SIGNATURES = {
     "mfe_dot_noalloc": (ctypes.c_int, [c_int64, c_void_p, c_void_p, c_void_p, c_void_p]),
     "mfe_stencil64_from_csr": (ctypes.c_int, [c_void_p, _P(MfeCsr), _P(MfeStencil64)]),
     "mfe_spmv_stencil64": (ctypes.c_int, [c_void_p, _P(MfeStencil64), c_void_p, c_void_p]),
+    "mfe_gather": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p, c_void_p]),
     "mfe_dot_f32": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_void_p, _P(c_double)]),
     "mfe_inject_wait_timeout": (ctypes.c_int, [c_void_p, c_int64]),
     "mfe_waxpby": (ctypes.c_int, [c_void_p, c_int64, c_double, c_void_p, c_double, c_void_p,

@@ -561,6 +561,13 @@ mfe_status mfe_spmv_stencil64(mfe_ctx* ctx, const mfe_stencil64* S, const double
   return launch_spmv_st64(ctx, &A, S->w, S->dd, x, y, nullptr, nullptr);
 }
 
+mfe_status mfe_gather(mfe_ctx* ctx, int64_t n, const int32_t* idx, const double* x, double* out)
+{
+  if (!ctx || n < 0 || (n > 0 && (!idx || !x || !out))) return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  MFE_TRY(set_device(ctx));
+  return launch_gather(ctx, n, idx, x, out);
+}
+
 mfe_status mfe_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, double* result)
 {
   if (!ctx || !result || n < 0 || (n > 0 && (!x || !y))) return fail(ctx, MFE_BAD_ARG, "bad arguments");

@@ -72,6 +72,17 @@ __global__ void __launch_bounds__(kVecThreads)
     w[i] = fma(alpha, x[i], beta * y[i]);
 }
 
+// out[i] = x[idx[i]] (the send buffer of a halo exchange,
+// exchange_externals.hpp: send_buffer[i] = x[elements_to_send[i]])
+__global__ void __launch_bounds__(kVecThreads)
+    k_gather_idx(int64_t n, const int32_t* __restrict__ idx, const double* __restrict__ x,
+                 double* __restrict__ out)
+{
+  for (int64_t i = (int64_t)blockIdx.x * kVecThreads + threadIdx.x; i < n;
+       i += (int64_t)gridDim.x * kVecThreads)
+    out[i] = x[idx[i]];
+}
+
 // fused_waxpby (Vector_functions.hpp:154-185): both updates in one pass
 __global__ void __launch_bounds__(kVecThreads)
     k_fused_waxpby(int64_t n, double alpha, const double* __restrict__ x, double beta,
@@ -267,6 +278,13 @@ mfe_status launch_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const doub
   k_fused_waxpby<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, alpha, x, beta, y, w, alpha2,
                                                                     x2, beta2, y2, w2);
   return check_launch(ctx, "k_fused_waxpby");
+}
+
+mfe_status launch_gather(mfe_ctx* ctx, int64_t n, const int32_t* idx, const double* x, double* out)
+{
+  if (n <= 0) return MFE_OK;
+  k_gather_idx<<<vec_grid(ctx, n), kVecThreads, 0, ctx->stream>>>(n, idx, x, out);
+  return check_launch(ctx, "k_gather_idx");
 }
 
 mfe_status launch_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,

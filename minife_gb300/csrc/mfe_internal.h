@@ -211,6 +211,8 @@ mfe_status launch_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x,
 mfe_status launch_fused_waxpby(mfe_ctx* ctx, int64_t n, double alpha, const double* x, double beta,
                                const double* y, double* w, double alpha2, const double* x2,
                                double beta2, const double* y2, double* w2);
+// out[i] = x[idx[i]], i < n (halo exchange send buffers)
+mfe_status launch_gather(mfe_ctx* ctx, int64_t n, const int32_t* idx, const double* x, double* out);
 // x.y of FP32 vectors accumulated in double-float (the mixed solvers' dots)
 mfe_status launch_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, double* dev_out);
 mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
