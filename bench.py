@@ -53,13 +53,14 @@ def peaks():
         return 6800.0, "fallback"
 
 
-def traffic_from_profile():
-    """Per-launch DRAM bytes of the SpMV kernel from the committed ncu summary."""
+def traffic_from_profile(key="bytes_per_launch_256"):
+    """Per-launch DRAM bytes of an SpMV kernel at 256^3 from the committed
+    ncu summary (captured on a smaller box, scaled by the units processed)."""
     path = os.path.join(ROOT, "profiles", "spmv_traffic.json")
     try:
         with open(path) as f:
             d = json.load(f)
-        return float(d["bytes_per_launch_256"])
+        return float(d[key])
     except Exception:
         return None
 
@@ -500,7 +501,7 @@ def run_gpu(args):
             "roofline": {"bound": "fp64", "achieved": st_ops / t_st / 1e9,
                          "peak": FP64_PEAK_TFLOPS / 2 * 1e3, "unit": "G FP64 op/s",
                          "frac": st_ops / t_st / 1e9 / (FP64_PEAK_TFLOPS / 2 * 1e3),
-                         "traffic": None,
+                         "traffic": traffic_from_profile("st64_bytes_per_launch_256"),
                          "kernel": "k_spmv_st64 (verified FP64 stencil SpMV, 12.5 FP64 operations "
                                    "per row without the fused dot)",
                          "kernel_ms": t_st * 1e3, "algorithmic_ops": st_ops,
@@ -730,7 +731,8 @@ def bench_multi(args, world, stream):
 def run_probe(args):
     """Small fixed workloads for profiler captures (ncu): 'spmv' = the box
     system at --dims^3, three FP64 and three FP32 matvecs; 'st64' = the
-    system and three products with its verified FP64 stencil; 'cg' = the system
+    system and three products with its verified FP64 stencil; 'cgfull' = the
+    system, one whole FP64 solve to 1e-8 (--op) and the analytic check; 'cg' = the system
     and a 4-iteration CG solve; 'multi' = the system and a 6-iteration
     mixed-precision solve of 32 right-hand sides (reliable update every 3);
     'batch' = the first --nbox of the seeded uneven boxes solved together in
@@ -749,7 +751,22 @@ def run_probe(args):
         return 0
     d = args.dims
     A, b = M.build_system(d, d, d)
-    if args.probe == "st64":
+    if args.probe == "cgfull":
+        # one whole FP64 solve to 1e-8 (--op: the operator) and the analytic
+        # check, each timed with CUDA events
+        x = torch.zeros_like(b)
+        st = torch.cuda.current_stream()
+        e = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+        e[0].record(st)
+        r = M.cg_solve(A, b, x, max_iter=5000, tol=TOL, tol_mode="relative", f64_operator=args.op)
+        e[1].record(st)
+        rc, err = M.verify_solution(d, d, d, x)
+        e[2].record(st)
+        torch.cuda.synchronize()
+        print("cgfull %s: %d iterations, operator %s, solve %.4f s, verify_solution %.3f ms "
+              "(max err %.4f)" % (args.op, r.num_iters, r.inner_operator,
+                                  e[0].elapsed_time(e[1]) * 1e-3, e[1].elapsed_time(e[2]), err))
+    elif args.probe == "st64":
         x = torch.randn(A.nrows, dtype=torch.float64, device="cuda")
         y = torch.empty_like(x)
         S = M.Stencil64(A)
@@ -788,10 +805,12 @@ def run_probe(args):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--probe", choices=["spmv", "st64", "cg", "mixed", "multi", "batch"],
+    ap.add_argument("--probe", choices=["spmv", "st64", "cg", "cgfull", "mixed", "multi", "batch"],
                     default=None,
                     help="run a small fixed workload for a profiler capture and exit")
     ap.add_argument("--dims", type=int, default=128)
+    ap.add_argument("--op", choices=["auto", "csr"], default="auto",
+                    help="probe cgfull: the FP64 operator")
     ap.add_argument("--nbox", type=int, default=96, help="boxes of the batch probe")
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
