@@ -101,3 +101,20 @@ def test_row_lengths_and_counts():
         ro, cols = O.structure(*dims)
         lens = np.diff(ro)
         assert set(np.unique(lens)) <= {8, 12, 18, 27}
+
+
+def test_oracle_256_assembly_matches_reference_hashes():
+    """At the benchmark's size (256^3: 16,974,593 rows, 454,756,609
+    nonzeros) the oracle's structure, assembled values and right-hand side
+    hash to the arrays the unmodified reference produced
+    (tests/golden/golden_256.json, gen_golden.py --big 256)."""
+    import hashlib
+    import json
+    import os
+    from oracle import oracle as O
+    with open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden",
+                           "golden_256.json")) as f:
+        g = json.load(f)
+    ro, cols, vals, b = O.build_system(256, 256, 256)
+    for name, a in (("row_offsets", ro), ("cols", cols), ("vals", vals), ("b", b)):
+        assert hashlib.sha256(a.tobytes()).hexdigest() == g["sha256"][name], name
