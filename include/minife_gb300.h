@@ -175,9 +175,9 @@ typedef struct mfe_stencil64 {
  * along a dimension, not a box matrix). */
 mfe_status mfe_stencil64_from_csr(mfe_ctx* ctx, const mfe_csr* A, mfe_stencil64* S);
 
-/* y = S x (device vectors of the box's rows): 14 FP64 operations per row
- * instead of the CSR kernel's 27 FMAs; within 2^-39 sum_j |a_ij x_j| (plus
- * rounding) of A x for the A that S was made from. */
+/* y = S x (device vectors of the box's rows): 12.5 FP64 operations per row
+ * on average instead of the CSR kernel's 27 FMAs; within 2^-39 sum_j
+ * |a_ij x_j| (plus rounding) of A x for the A that S was made from. */
 mfe_status mfe_spmv_stencil64(mfe_ctx* ctx, const mfe_stencil64* S, const double* x, double* y);
 
 /* matvec_and_dot (ref/src/SparseMatrix_functions.hpp:491-536): y = A x and
@@ -356,7 +356,11 @@ mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double*
 
 /* Drop-in for the reference's host-side call: CSR and vectors in HOST
  * memory (CSRMatrix/Vector storage), copied to the device, solved with
- * mfe_cg_solve, and x copied back. */
+ * mfe_cg_solve, and x copied back.  For an FP64 solve without preconditioner
+ * the host threads check, while the values are being copied, whether the
+ * row offsets and columns are the 27-point box layout of some nx x ny x nz
+ * box; if they are, only the values and vectors are copied (the solver
+ * reads a box's structure in closed form), otherwise the structure too. */
 mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz,
                              const int32_t* row_offsets, const int32_t* cols,
                              const double* vals, const double* b, double* x,

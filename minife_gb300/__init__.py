@@ -378,7 +378,7 @@ def waxpby(alpha, x, beta, y, w, ctx: Context | None = None):
 class Stencil64:
     """The verified FP64 stencil operator of a miniFE box matrix
     (mfe_stencil64_from_csr): checked once against every entry of A, then
-    applied by matvec_stencil64 with 14 FP64 operations per row."""
+    applied by matvec_stencil64 with 12.5 FP64 operations per row on average."""
 
     def __init__(self, A: "CSRMatrix", ctx: Context | None = None):
         ctx = ctx or default_context()
