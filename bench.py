@@ -11,9 +11,11 @@ Keys beyond the base contract:
   e2e          the same solve through the host drop-in call
                (mfe_cg_solve_host: host CSR and b in pinned memory copied to the
                device inside the timed region, x copied back)
-  roofline     the dominant kernel (the CSR SpMV with fused p.Ap) timed with
-               CUDA events on its stream against MEASURED_PEAKS.json's HBM copy
-               bandwidth; traffic from the committed ncu summary
+  roofline     the dominant kernel (the verified FP64 stencil SpMV) timed with
+               CUDA events on its stream against the measured FP64 pipe rate,
+               its HBM fraction beside it; traffic from the committed ncu
+               summary.  fp64_csr_values carries the same solve with the CSR
+               values and the box CSR SpMV's roofline against HBM.
   cpu_baseline the OpenMP CG port (oracle/cpu_baseline.c) on the host cores:
                one whole solve of the same system to the same tolerance
   --impl reference  times that CPU baseline as the reference arm, one whole
@@ -343,9 +345,11 @@ def run_gpu(args):
     # e2e through the host drop-in call (pinned host CSR, copies inside).
     # Each call is timed on its own; the host x is zeroed between calls,
     # outside the timed region, as the reference arm allocates its x outside.
-    # The call copies the values, b and x in and x out; it checks the row
-    # offsets and columns against the box layout on the host threads while
-    # the values move, and a verified box layout is not copied.
+    # The call copies the values, b and x in and x out.  With x0 = 0 it
+    # starts the stencil solve at once, while the values are copied and
+    # checked on a second stream and the host threads check the layout; the
+    # result counts once all have passed (a verified box layout is not
+    # copied).
     e2e = None
     if not args.no_e2e:
         ro_h = A.row_offsets.cpu().pin_memory()
@@ -370,7 +374,11 @@ def run_gpu(args):
                "d2h_bytes_per_step": 8 * n, "iterations": r2.num_iters,
                "ratio_to_device_solve": t_e2e / t_step,
                "structure": "row offsets and columns checked on the host against the box "
-                            "layout, not copied"}
+                            "layout, not copied",
+               "start": ("speculative: the solve ran beside the values copy and checks"
+                         if r2.inner_operator == "stencil64" and r2.fp64_spmvs == 1
+                         else "after the values copy"),
+               "csr_products": r2.fp64_spmvs}
         del ro_h, cols_h, vals_h
 
     # mixed precision (FP32 inner operator and vectors, FP64 dots and reliable

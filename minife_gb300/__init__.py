@@ -448,6 +448,9 @@ class CGResult:
     # ("stencil", "values" or "padded"); for FP64 solves "stencil64" (the
     # verified FP64 stencil operator) or "none" (the CSR values)
     inner_operator: str = "none"
+    # products with the FP64 CSR values (initial and true residuals of a
+    # stencil solve; every iteration's product otherwise)
+    fp64_spmvs: int = 0
 
     @property
     def total_time(self) -> float:
@@ -493,7 +496,7 @@ _INNER = {0: "none", 1: "stencil", 2: "values", 3: "padded", 4: "stencil64"}
 
 def _cg_result(r: MfeCgResult, hist=None) -> CGResult:
     return CGResult(r.num_iters, r.normr, r.normr0, r.final_resid, r.status, tuple(r.times),
-                    r.refinements, hist, _INNER.get(r.inner_operator, "none"))
+                    r.refinements, hist, _INNER.get(r.inner_operator, "none"), r.fp64_spmvs)
 
 
 def cg_solve(A: CSRMatrix, b, x, max_iter: int = 200, tol: float = DBL_EPSILON,

@@ -5,6 +5,7 @@
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
+#include <cstdint>
 #include <cstring>
 #include <tuple>
 #include <atomic>
@@ -178,6 +179,12 @@ mfe_status mfe_ctx_destroy(mfe_ctx* ctx)
     cudaFree(ctx->f32_copy.vals);
   }
   if (ctx->host_scratch) cudaFreeHost(ctx->host_scratch);
+  if (ctx->side_stream) {
+    cudaStreamSynchronize(ctx->side_stream);
+    cudaStreamDestroy(ctx->side_stream);
+  }
+  if (ctx->ev_side) cudaEventDestroy(ctx->ev_side);
+  if (ctx->side_pinned) cudaFreeHost(ctx->side_pinned);
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->own_stream) cudaStreamDestroy(ctx->own_stream);
@@ -610,6 +617,13 @@ void mfe_cg_opts_default(mfe_cg_opts* o)
   o->precision = MFE_PREC_F64;
 }
 
+static bool cg_opts_valid(const mfe_cg_opts& o)
+{
+  return o.max_iter >= 0 && o.tol >= 0.0 &&
+         (o.precision == MFE_PREC_F64 || o.precision == MFE_PREC_MIXED) &&
+         (o.precond == 0 || o.precond == 1) && (o.f64_operator == 0 || o.f64_operator == 1);
+}
+
 mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                         const mfe_cg_opts* opts, mfe_cg_result* result)
 {
@@ -621,10 +635,7 @@ mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double*
   mfe_cg_opts o;
   if (opts) o = *opts;
   else mfe_cg_opts_default(&o);
-  if (o.max_iter < 0 || !(o.tol >= 0.0) ||
-      (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED) ||
-      (o.precond != 0 && o.precond != 1) || (o.f64_operator != 0 && o.f64_operator != 1))
-    return fail(ctx, MFE_BAD_ARG, "bad CG options");
+  if (!cg_opts_valid(o)) return fail(ctx, MFE_BAD_ARG, "bad CG options");
   MFE_TRY(set_device(ctx));
   if (A->nrows == 0) return MFE_OK;
   mfe_status st = cg_solve_impl(ctx, A, b, x, &o, result);
@@ -726,6 +737,67 @@ bool host_box_layout(int64_t n, int64_t nnz, const int32_t* ro, const int32_t* c
 
 }  // namespace
 
+namespace {
+
+// Row 0 of a box CSR (node (0,0,0): columns 0, 1, Nx, Nx + 1, NxNy, ...)
+// gives the box's dimensions; the sizes must agree with them.  The rest of
+// the layout is checked by host_box_layout.
+bool host_box_dims(int64_t n, int64_t nnz, const int32_t* ro, const int32_t* cols, int* bx, int* by,
+                   int* bz)
+{
+  if (n < 8 || nnz < 8 || ro[0] != 0 || ro[1] != 8 || cols[0] != 0 || cols[1] != 1) return false;
+  const int64_t Nx = cols[2], NxNy = cols[4];
+  if (Nx < 2 || NxNy < 2 * Nx || NxNy % Nx != 0 || n % NxNy != 0) return false;
+  const int64_t Ny = NxNy / Nx, Nz = n / NxNy;
+  if (Nz < 2 || Nx > INT32_MAX || Ny > INT32_MAX || Nz > INT32_MAX) return false;
+  if (box_nnz((int)Nx - 1, (int)Ny - 1, (int)Nz - 1) != nnz || (int64_t)ro[n] != nnz) return false;
+  *bx = (int)Nx - 1;
+  *by = (int)Ny - 1;
+  *bz = (int)Nz - 1;
+  return true;
+}
+
+mfe_status cuda_try(mfe_ctx* ctx, cudaError_t e, const char* where)
+{
+  return e == cudaSuccess ? MFE_OK : cuda_fail(ctx, e, where);
+}
+
+mfe_status side_stream(mfe_ctx* ctx)
+{
+  if (!ctx->side_stream)
+    MFE_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&ctx->side_stream, cudaStreamNonBlocking));
+  if (!ctx->ev_side) MFE_CUDA_TRY(ctx, cudaEventCreateWithFlags(&ctx->ev_side, cudaEventDisableTiming));
+  if (!ctx->side_pinned)
+    MFE_CUDA_TRY(ctx, cudaMallocHost(&ctx->side_pinned, sizeof(double) * kSt64TableLen + 64));
+  return MFE_OK;
+}
+
+// What the speculative start waits for before a result counts: the host
+// layout check (its own thread) and, on the side stream, the values copy and
+// the device check of every entry.
+struct SpecWait {
+  mfe_ctx* ctx;
+  std::thread layout;
+  std::atomic<int> box{-1};  // 1: the box layout of the expected dimensions
+  const unsigned* bad;       // pinned: the device check's result
+  bool done = false, ok = false;
+};
+
+bool spec_settle(SpecWait* w)
+{
+  if (w->done) return w->ok;
+  w->done = true;
+  if (w->layout.joinable()) w->layout.join();
+  bool good = cudaEventSynchronize(w->ctx->ev_side) == cudaSuccess &&
+              cudaStreamWaitEvent(w->ctx->stream, w->ctx->ev_side, 0) == cudaSuccess;
+  w->ok = good && w->box.load() == 1 && *w->bad == 0;
+  return w->ok;
+}
+
+bool spec_confirm(void* arg) { return spec_settle(static_cast<SpecWait*>(arg)); }
+
+}  // namespace
+
 mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz, const int32_t* ro,
                              const int32_t* cols, const double* vals, const double* b, double* x,
                              const mfe_cg_opts* opts, mfe_cg_result* result)
@@ -733,6 +805,10 @@ mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz, const int
   if (!ctx || !result || nrows < 0 || nnz < 0 || nnz >= ((int64_t)1 << 31) ||
       (nrows > 0 && (!ro || !b || !x || (nnz > 0 && (!cols || !vals)))))
     return fail(ctx, MFE_BAD_ARG, "bad arguments");
+  mfe_cg_opts o;
+  if (opts) o = *opts;
+  else mfe_cg_opts_default(&o);
+  if (!cg_opts_valid(o)) return fail(ctx, MFE_BAD_ARG, "bad CG options");
   MFE_TRY(set_device(ctx));
   mfe_csr A;
   memset(&A, 0, sizeof(A));
@@ -745,28 +821,106 @@ mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz, const int
   double* dx = static_cast<double*>(workspace(ctx, "host.x", sizeof(double) * (size_t)std::max<int64_t>(nrows, 1)));
   if (!A.vals || !db || !dx) return fail(ctx, MFE_OOM, "device allocation for host operands failed");
   cudaStream_t s = ctx->stream;
-  // the values and vectors go first; while the copy engine moves them the
-  // host threads check the row offsets and columns against the box layout
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
-  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s));
-  mfe_cg_opts o;
-  if (opts) o = *opts;
-  else mfe_cg_opts_default(&o);
   // The FP64 solver without preconditioner reads a box matrix's structure in
   // closed form only (box SpMV, stencil check and stencil SpMV), so a CSR
   // whose layout the host has verified is solved without copying its
   // 4 B-per-nonzero column indices and row offsets.
-  int bx = 0, by = 0, bz = 0;
-  const bool box = o.precision == MFE_PREC_F64 && o.precond == 0 &&
-                   getenv("MFE_SPMV_GENERIC") == nullptr &&
-                   host_box_layout(nrows, nnz, ro, cols, &bx, &by, &bz);
+  const bool f64_plain = o.precision == MFE_PREC_F64 && o.precond == 0 &&
+                         getenv("MFE_SPMV_GENERIC") == nullptr;
+  int qx = 0, qy = 0, qz = 0;
+  const bool dims = f64_plain && host_box_dims(nrows, nnz, ro, cols, &qx, &qy, &qz);
   // device arrays for the structure: filled only when the layout is not the box's
-  A.row_offsets = static_cast<int32_t*>(workspace(ctx, "host.ro", sizeof(int32_t) * (size_t)(nrows + 1)));
-  A.cols = static_cast<int32_t*>(workspace(ctx, box ? "host.ro" : "host.cols",
-                                           box ? sizeof(int32_t) * (size_t)(nrows + 1)
-                                               : sizeof(int32_t) * (size_t)(nnz + 4)));
-  if (!A.row_offsets || !A.cols) return fail(ctx, MFE_OOM, "device allocation for host operands failed");
+  auto structure_bufs = [&](bool box) {
+    A.row_offsets = static_cast<int32_t*>(workspace(ctx, "host.ro", sizeof(int32_t) * (size_t)(nrows + 1)));
+    A.cols = static_cast<int32_t*>(workspace(ctx, box ? "host.ro" : "host.cols",
+                                             box ? sizeof(int32_t) * (size_t)(nrows + 1)
+                                                 : sizeof(int32_t) * (size_t)(nnz + 4)));
+    return A.row_offsets && A.cols;
+  };
+  int layout = -1;           // host layout check: 1 box, 0 not, -1 not run
+  bool vals_copied = false;  // the values are on their way (ctx->stream waits for them)
+
+  // Speculative start (FP64 stencil operator, x0 = 0): the CG runs while the
+  // values are copied and checked on the side stream and the host threads
+  // check the layout; the solve's result counts only once all have passed.
+  double* htab = nullptr;
+  double w8[8], dd = 0.0;
+  if (dims && o.f64_operator == 0 && side_stream(ctx) == MFE_OK &&
+      (htab = static_cast<double*>(ctx->side_pinned)) != nullptr &&
+      stencil64_host_classes(qx + 1, qy + 1, qz + 1, vals, htab, w8, &dd)) {
+    cudaStream_t s2 = ctx->side_stream;
+    double* dtab = static_cast<double*>(workspace(ctx, "host.st64table", sizeof(double) * kSt64TableLen + 16));
+    if (!dtab || !structure_bufs(true)) return fail(ctx, MFE_OOM, "device allocation for host operands failed");
+    unsigned* dbad = reinterpret_cast<unsigned*>(dtab + kSt64TableLen);
+    unsigned* hbad = reinterpret_cast<unsigned*>(htab + kSt64TableLen);
+    *hbad = 1u;
+    SpecWait w;
+    w.ctx = ctx;
+    w.bad = hbad;
+    // the side stream starts after the work already queued on ctx->stream
+    MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev_side, s));
+    MFE_CUDA_TRY(ctx, cudaStreamWaitEvent(s2, ctx->ev_side, 0));
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s2));
+    vals_copied = true;
+    mfe_status st = MFE_OK;
+    do {
+      if ((st = cuda_try(ctx, cudaMemcpyAsync(dtab, htab, sizeof(double) * kSt64TableLen,
+                                              cudaMemcpyHostToDevice, s2), "table copy")) != MFE_OK) break;
+      if ((st = stencil64_verify_on(ctx, s2, qx + 1, qy + 1, qz + 1, static_cast<const double*>(A.vals),
+                                    dtab, dbad)) != MFE_OK) break;
+      if ((st = cuda_try(ctx, cudaMemcpyAsync(hbad, dbad, sizeof(unsigned), cudaMemcpyDeviceToHost, s2),
+                         "check result copy")) != MFE_OK) break;
+      if ((st = cuda_try(ctx, cudaEventRecord(ctx->ev_side, s2), "event")) != MFE_OK) break;
+      auto check_layout = [&w, nrows, nnz, ro, cols, qx, qy, qz]() {
+        int bx = 0, by = 0, bz = 0;
+        const bool ok = host_box_layout(nrows, nnz, ro, cols, &bx, &by, &bz);
+        w.box.store(ok && bx == qx && by == qy && bz == qz ? 1 : 0);
+      };
+      try {
+        w.layout = std::thread(check_layout);
+      } catch (...) {
+        check_layout();  // no thread to spare: check before the solve
+      }
+      A.box_nx = qx;
+      A.box_ny = qy;
+      A.box_nz = qz;
+      A.max_row_len = 27;
+      CgSpec spec;
+      for (int c = 0; c < 8; ++c) spec.w8[c] = w8[c];
+      spec.dd = dd;
+      spec.confirm = spec_confirm;
+      spec.arg = &w;
+      memset(result, 0, sizeof(*result));
+      st = cg_solve_spec(ctx, &A, db, dx, &o, result, &spec);
+    } while (false);
+    // nothing of this call stays in flight: the host thread ends and the
+    // side stream has read the caller's values before anything returns
+    spec_settle(&w);
+    cudaStreamSynchronize(s2);
+    layout = w.box.load();
+    if (st != kSpecFailed) {
+      if (st != MFE_OK && st != MFE_BREAKDOWN && st != MFE_MAXITER) return st;
+      result->status = st;
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(x, dx, sizeof(double) * (size_t)nrows, cudaMemcpyDeviceToHost, s));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(s));
+      return st;
+    }
+    // the speculation did not hold: the ordinary solve from the caller's x0
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dx, x, sizeof(double) * (size_t)nrows, cudaMemcpyHostToDevice, s));
+  }
+
+  if (!vals_copied)
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(A.vals, vals, sizeof(double) * (size_t)nnz, cudaMemcpyHostToDevice, s));
+  // while the copy engine moves the values the host threads check the layout
+  int bx = 0, by = 0, bz = 0;
+  if (layout < 0) layout = dims && host_box_layout(nrows, nnz, ro, cols, &bx, &by, &bz) ? 1 : 0;
+  else bx = qx, by = qy, bz = qz;
+  const bool box = dims && layout == 1;
+  if (!structure_bufs(box)) return fail(ctx, MFE_OOM, "device allocation for host operands failed");
+  A.box_nx = A.box_ny = A.box_nz = 0;
+  A.max_row_len = 0;
   if (box) {
     A.box_nx = bx;
     A.box_ny = by;
@@ -823,10 +977,7 @@ mfe_status mfe_adjoint_grad(mfe_ctx* ctx, int nx, int ny, int nz, const double* 
   mfe_cg_opts o;
   if (opts) o = *opts;
   else mfe_cg_opts_default(&o);
-  if (o.max_iter < 0 || !(o.tol >= 0.0) ||
-      (o.precision != MFE_PREC_F64 && o.precision != MFE_PREC_MIXED) ||
-      (o.precond != 0 && o.precond != 1) || (o.f64_operator != 0 && o.f64_operator != 1))
-    return fail(ctx, MFE_BAD_ARG, "bad CG options");
+  if (!cg_opts_valid(o)) return fail(ctx, MFE_BAD_ARG, "bad CG options");
   MFE_TRY(set_device(ctx));
   return adjoint_grad(ctx, nx, ny, nz, kappa, u_target, &o, u_out, grad, loss, fwd, adj);
 }

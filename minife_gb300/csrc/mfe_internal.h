@@ -37,6 +37,11 @@ struct mfe_ctx {
   // launch shape of the multi-RHS stencil SpMM (mfe_multi_set_tuning): z
   // steps per work item, 0 = the default
   int multi_zchunk = 0;
+  // the host drop-in call's second stream (the values copy and the operator
+  // check beside a solve already running), its event and a pinned buffer
+  cudaStream_t side_stream = nullptr;
+  cudaEvent_t ev_side = nullptr;
+  void* side_pinned = nullptr;
 };
 
 namespace mfe {
@@ -144,6 +149,19 @@ constexpr int kSt64TolExp = 40;
 // success w8[c] is the weight of class c = 4|dz| + 2|dy| + |dx| and dd the
 // Dirichlet diagonal
 mfe_status stencil64_prepare(mfe_ctx* ctx, const mfe_csr* A64, double* w8, double* dd, bool* ok);
+// The same check split for a matrix still on its way from host memory (the
+// host drop-in call): stencil64_host_classes reads the 125 class rows of the
+// HOST values of a CSR laid out as the box's (Nx x Ny x Nz nodes) into table
+// (kSt64TableLen doubles), checks them against the model and the mirror
+// classes and spot-checks rows spread over the box against them (a predictor
+// only); stencil64_verify_on then checks every entry on the device against
+// the table (already on the device), on stream s, setting *bad (device)
+// nonzero on any mismatch.
+constexpr int kSt64TableLen = 125 * 28;
+bool stencil64_host_classes(int Nx, int Ny, int Nz, const double* vals, double* table, double* w8,
+                            double* dd);
+mfe_status stencil64_verify_on(mfe_ctx* ctx, cudaStream_t s, int Nx, int Ny, int Nz,
+                               const double* vals, const double* table, unsigned* bad);
 // y = S x in FP64 on natural-layout vectors (A's box dimensions), with x.y
 // into the CG state (pAp and the breakdown pre-test) when cg_state is set,
 // else into sink->out (when sink is set)
@@ -217,6 +235,23 @@ mfe_status launch_gather(mfe_ctx* ctx, int64_t n, const int32_t* idx, const doub
 mfe_status launch_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y, double* dev_out);
 mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                          const mfe_cg_opts* opts, mfe_cg_result* res);
+// An FP64 stencil solve started before the matrix values are on the device
+// (the host drop-in call): x0 must be zero (checked on the device), the
+// operator's weights come from the host copy of the matrix, and confirm()
+// runs once before anything reads the CSR values or the solve returns a
+// result.  It must make ctx->stream wait for the values and return whether
+// the layout and every entry passed their checks.  cg_solve_spec returns
+// kSpecFailed when x0 is not zero, the tolerance is below the operator's
+// gate or confirm() returns false; x on the device is then undefined.
+struct CgSpec {
+  double w8[8];
+  double dd;
+  bool (*confirm)(void* arg);
+  void* arg;
+};
+constexpr mfe_status kSpecFailed = (mfe_status)1000;
+mfe_status cg_solve_spec(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
+                         const mfe_cg_opts* opts, mfe_cg_result* res, const CgSpec* spec);
 void cg_graph_destroy(mfe_cg_graph* g);
 
 }  // namespace mfe

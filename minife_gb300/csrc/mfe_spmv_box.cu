@@ -66,17 +66,7 @@ __device__ __forceinline__ void box_epilogue(double total, CgState* cg, double* 
     cg->pAp = total;
     if (total < cg->brkdown_tol) cg->check_pending = 1;
   } else if (MODE == BOX_RESID) {
-    const double normr = sqrt(total);
-    cg->rtrans = total;
-    cg->rr_new = total;
-    cg->normr = normr;
-    cg->normr0 = normr;
-    const double tol_abs = cg->tol_mode ? cg->tol_abs * normr : cg->tol_abs;
-    cg->tol_abs = tol_abs;
-    cg->k = 1;
-    cg->num_iters = 0;
-    cg->cont = (1 <= cg->max_iter) && (normr > tol_abs);
-    if (cg->record) cg->history[0] = cg->history[1] = normr;
+    cg_resid_init(cg, total);
   }
 }
 

@@ -72,19 +72,15 @@ __host__ __device__ __forceinline__ bool st_has(int c, int N)
   return i >= 0 && i < N && st_cls(i, N) == c;
 }
 
-// one thread per class: the class's representative row in the table's type
-// (rounded to FP32, or exact in FP64) in slot order (dz, dy, dx), zeros for
-// missing neighbours
+// class c's representative row in the table's type (rounded to FP32, or
+// exact in FP64) in slot order (dz, dy, dx), zeros for missing neighbours
+// and for classes no row has
 template <typename TT>
-__global__ void k_st_table(int Nx, int Ny, int Nz, const double* __restrict__ vals,
-                           TT* __restrict__ table)
+__host__ __device__ void st_class_row(int c, int Nx, int Ny, int Nz, const double* vals, TT* out)
 {
-  const int c = blockIdx.x * blockDim.x + threadIdx.x;
-  if (c >= 125) return;
   const int cx = c % 5, cy = (c / 5) % 5, cz = c / 25;
-  TT* out = table + c * 28;
   if (!st_has(cx, Nx) || !st_has(cy, Ny) || !st_has(cz, Nz)) {
-    for (int k = 0; k < 28; ++k) out[k] = TT(0);  // no row has this class
+    for (int k = 0; k < 28; ++k) out[k] = TT(0);
     return;
   }
   const int ix = st_rep(cx, Nx), iy = st_rep(cy, Ny), iz = st_rep(cz, Nz);
@@ -98,6 +94,15 @@ __global__ void k_st_table(int Nx, int Ny, int Nz, const double* __restrict__ va
         out[slot] = in ? (TT)vals[k++] : TT(0);
       }
   out[27] = TT(0);
+}
+
+// one thread per class
+template <typename TT>
+__global__ void k_st_table(int Nx, int Ny, int Nz, const double* __restrict__ vals,
+                           TT* __restrict__ table)
+{
+  const int c = blockIdx.x * blockDim.x + threadIdx.x;
+  if (c < 125) st_class_row<TT>(c, Nx, Ny, Nz, vals, table + c * 28);
 }
 
 __device__ __forceinline__ double tab_widen(float v) { return f2d_exact(v); }
@@ -586,6 +591,53 @@ mfe_status stencil64_prepare(mfe_ctx* ctx, const mfe_csr* A64, double* w8, doubl
   *dd = coef[27];
   *ok = tab_ok && mirror_classes<double, kSt64TolExp>(coef, w8);
   return MFE_OK;
+}
+
+bool stencil64_host_classes(int Nx, int Ny, int Nz, const double* vals, double* table, double* w8,
+                            double* dd)
+{
+  if (Nx < 5 || Ny < 5 || Nz < 5) return false;
+  for (int c = 0; c < 125; ++c) st_class_row<double>(c, Nx, Ny, Nz, vals, table + c * 28);
+  double coef[28];
+  if (!st_model<double, kSt64TolExp>(Nx, Ny, Nz, table, coef, coef + 27)) return false;
+  if (!mirror_classes<double, kSt64TolExp>(coef, w8)) return false;
+  *dd = coef[27];
+  // rows spread over the box against their class rows (the device checks
+  // every row; this catches most matrices that are not such an operator --
+  // per-element conductivity, say -- before a solve is started on it)
+  const int64_t n = (int64_t)Nx * Ny * Nz, step = std::max<int64_t>(1, n / 4093);
+  for (int64_t r = 0; r < n; r += step) {
+    const int ix = (int)(r % Nx), iy = (int)((r / Nx) % Ny), iz = (int)(r / ((int64_t)Nx * Ny));
+    const double* sc = table + (st_cls(ix, Nx) + 5 * st_cls(iy, Ny) + 25 * st_cls(iz, Nz)) * 28;
+    double row[28];
+    int64_t k = row_offset(ix, iy, iz, Nx, Ny, Nz);
+    double amax = 0.0;
+    int slot = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+      for (int dy = -1; dy <= 1; ++dy)
+        for (int dx = -1; dx <= 1; ++dx, ++slot) {
+          const bool in = ix + dx >= 0 && ix + dx < Nx && iy + dy >= 0 && iy + dy < Ny &&
+                          iz + dz >= 0 && iz + dz < Nz;
+          row[slot] = in ? vals[k++] : 0.0;
+          amax = std::max(amax, std::fabs(row[slot]));
+        }
+    const double tol = std::ldexp(amax, -kSt64TolExp);
+    for (int q = 0; q < 27; ++q)
+      if (!(std::fabs(row[q] - sc[q]) <= tol)) return false;
+  }
+  return true;
+}
+
+mfe_status stencil64_verify_on(mfe_ctx* ctx, cudaStream_t s, int Nx, int Ny, int Nz,
+                               const double* vals, const double* table, unsigned* bad)
+{
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(bad, 0, sizeof(unsigned), s));
+  const int64_t n = (int64_t)Nx * Ny * Nz;
+  const void* k = (const void*)k_st_verify<double, kSt64TolExp>;
+  const int blocks = (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(n, (int64_t)kVW * 32), (int64_t)resident_blocks(ctx, k, kVW * 32, 0)));
+  k_st_verify<double, kSt64TolExp><<<blocks, kVW * 32, 0, s>>>(Nx, Ny, Nz, vals, table, bad);
+  return check_launch(ctx, "k_st_verify");
 }
 
 // one wave of resident CTAs of the variant coef selects (the attributes are

@@ -546,3 +546,62 @@ def test_cg_host_dropin_box_and_perturbed(op):
         assert np.linalg.norm(x - xo) <= 1e-9 * np.linalg.norm(xo)
         expect = "stencil64" if op == "auto" and perturb is None else "none"
         assert res.inner_operator == expect
+
+
+def test_cg_host_dropin_speculative_start():
+    """The host drop-in call starts an FP64 stencil solve before the values
+    are on the device (x0 = 0): the values copy and the device check of every
+    entry run beside it, and the host threads check the layout.  Every branch
+    against the oracle: the start holds (one product with the CSR values: the
+    final residual); x0 != 0 (the ordinary solve, two CSR products); one
+    entry off its class value by 2^-30 in a row the host's spot check skips
+    (the device check rejects it after the solve: the CSR values solve it);
+    one row's columns rotated (the host layout check rejects it: the generic
+    kernels solve it); the reference's absolute DBL_EPSILON stop (below the
+    operator's gate: the CSR values)."""
+    dims = (24, 20, 22)  # 12,075 rows: the host spot check takes every second row
+    ro, cols, vals, bo = O.build_system(*dims)
+    n = ro.size - 1
+    Nx, Ny = dims[0] + 1, dims[1] + 1
+    row = 5 + Nx * (5 + Ny * 5)  # an interior row of odd index, not a class representative
+    assert row % 2 == 1 and ro[row + 1] - ro[row] == 27
+
+    def run(c, v, x0, **kw):
+        x = x0.copy()
+        kw.setdefault("tol", 1e-10)
+        kw.setdefault("tol_mode", "relative")
+        res = M.cg_solve_host(ro, c, v, bo, x, max_iter=1000, **kw)
+        mode = 1 if kw["tol_mode"] == "relative" else 0
+        xo, it, nr, st = O.cg_solve(ro, c, v, bo, x0=x0, max_iter=1000, tol=kw["tol"],
+                                    tol_mode=mode)
+        assert res.status == 0 and st == 0
+        # iteration counts to 1e-10 differ by rounding (FMA, reduction order)
+        # by a few on some systems; the residual and solution do not
+        assert abs(res.num_iters - it) <= max(2, it // 10), (res.num_iters, it)
+        if mode == 1:
+            r0 = np.linalg.norm(bo - O.matvec(ro, c, v, x0))
+            rel = np.linalg.norm(bo - O.matvec(ro, c, v, x)) / r0
+            assert rel <= 1.001 * kw["tol"], rel
+        # two iterates at a 1e-10 residual differ by its image under A^-1
+        # (condition number ~ 250 here)
+        assert np.linalg.norm(x - xo) <= 1e-7 * np.linalg.norm(xo)
+        return res
+
+    zero = np.zeros(n)
+    res = run(cols, vals, zero)
+    assert res.inner_operator == "stencil64" and res.fp64_spmvs == 1
+    x0 = np.random.default_rng(5).standard_normal(n)
+    res = run(cols, vals, x0)
+    assert res.inner_operator == "stencil64" and res.fp64_spmvs == 2
+    v2 = vals.copy()
+    v2[ro[row] + 13] *= 1.0 + 2.0 ** -30  # the diagonal entry
+    res = run(cols, v2, zero)
+    assert res.inner_operator == "none"
+    c3, v3 = cols.copy(), vals.copy()
+    a, e = ro[row], ro[row + 1]
+    c3[a:e] = np.roll(c3[a:e], 1)
+    v3[a:e] = np.roll(v3[a:e], 1)
+    res = run(c3, v3, zero)
+    assert res.inner_operator == "none"
+    res = run(cols, vals, zero, tol=2.220446049250313e-16, tol_mode="absolute")
+    assert res.inner_operator == "none"
