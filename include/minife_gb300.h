@@ -360,7 +360,13 @@ mfe_status mfe_cg_solve(mfe_ctx* ctx, const mfe_csr* A, const double* b, double*
  * the host threads check, while the values are being copied, whether the
  * row offsets and columns are the 27-point box layout of some nx x ny x nz
  * box; if they are, only the values and vectors are copied (the solver
- * reads a box's structure in closed form), otherwise the structure too. */
+ * reads a box's structure in closed form), otherwise the structure too.
+ * With x0 = 0 and the default FP64 operator the solve does not wait for the
+ * copy: the verified FP64 stencil's weights are read from the host arrays
+ * and the CG starts at once, while a second stream of ctx copies the values
+ * and checks every entry on the device and a host thread checks the layout;
+ * the result counts only after all three have passed (else the ordinary
+ * solve runs from x0).  Nothing of the call is in flight when it returns. */
 mfe_status mfe_cg_solve_host(mfe_ctx* ctx, int64_t nrows, int64_t nnz,
                              const int32_t* row_offsets, const int32_t* cols,
                              const double* vals, const double* b, double* x,

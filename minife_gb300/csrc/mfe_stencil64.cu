@@ -222,15 +222,23 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
 // against 0.493 ms with two (and no difference between the read-only and the
 // L1-cached load paths)
 constexpr int kKP = 4;
+// CTAs per SM of the grid (3 fit: 74 registers): two give z runs half as
+// long again, i.e. fewer halo planes recomputed, and still enough warps to
+// keep the FP64 pipe fed -- measured at 256^3: 0.4842 ms per product against
+// 0.4893 with three and 0.4853 with one.  (Runs of 16-byte loads of the
+// window, masked afterwards, measured 0.517-0.66 ms: the load path is not
+// what bounds the kernel.)
+constexpr int kSt64CtasPerSm = 2;
 
 template <bool DOT>
 mfe_status st64_launch(mfe_ctx* ctx, St64Params& P)
 {
   P.ntile = (int)ceil_div(P.NxNy, (int64_t)kKP * kT64);
   const int64_t T = (int64_t)P.ntile * P.Nz;
-  const int g = (int)std::max<int64_t>(
-      1, std::min<int64_t>(T, (int64_t)resident_blocks(ctx, (const void*)k_spmv_st64<kKP, DOT>,
-                                                       kT64, 0)));
+  const int64_t res = std::min<int64_t>(
+      resident_blocks(ctx, (const void*)k_spmv_st64<kKP, DOT>, kT64, 0),
+      (int64_t)kSt64CtasPerSm * ctx->sm_count);
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(T, res));
   k_spmv_st64<kKP, DOT><<<g, kT64, 0, ctx->stream>>>(P);
   return check_launch(ctx, "k_spmv_st64");
 }
