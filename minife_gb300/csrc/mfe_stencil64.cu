@@ -34,8 +34,10 @@
 // neighbouring lines and planes coming from L1/L2: the kernel is bound by
 // the FP64 pipe, not by memory.  Window entries that are not interior nodes
 // are zeroed by per-thread masks fixed for the whole z run, Dirichlet planes
-// take warp-uniform branches, and only warps holding a Dirichlet row replace
-// its value by dd * x.  p.Ap is summed in FP64 per thread, then per block and
+// take warp-uniform branches, only warps holding a Dirichlet row replace
+// its value by dd * x, and warps holding nothing but Dirichlet rows (the
+// lines y = 0 and Ny - 1) or positions past the plane form dd * x alone.
+// The last step of a run skips the halo plane's unused Q.  p.Ap is summed in FP64 per thread, then per block and
 // over the grid in block order (deterministic for a fixed grid).
 #include <algorithm>
 #include <cmath>
@@ -104,6 +106,30 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
       any_bnd = any_bnd || (valid[r] && bnd[r]);
     }
     const bool wb = __any_sync(0xffffffffu, any_bnd);
+    bool any_row = false;  // an interior row among the thread's positions
+#pragma unroll
+    for (int r = 0; r < KP; ++r) any_row = any_row || (valid[r] && !bnd[r]);
+    if (!__any_sync(0xffffffffu, any_row)) {
+      // every row of the warp is a Dirichlet row (lines y = 0 and Ny - 1)
+      // or past the plane: dd * x, with no stencil work
+      const double* cp = P.x + (int64_t)za * P.NxNy + p0;
+      double* yq = P.y + (int64_t)za * P.NxNy + p0;
+      for (int z = za; z < zb; ++z) {
+#pragma unroll
+        for (int r = 0; r < KP; ++r) {
+          if (valid[r]) {
+            const double c = __ldg(cp + r);
+            const double yv = P.dd * c;
+            yq[r] = yv;
+            if (DOT) dacc = fma(yv, c, dacc);
+          }
+        }
+        cp += P.NxNy;
+        yq += P.NxNy;
+      }
+      q += zb - za;
+      continue;
+    }
     const double* xp = P.x + p0 - 1;  // window origin of plane 0
     auto ld = [](const double* a) { return __ldg(a); };
 
@@ -170,13 +196,12 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
       for (int r = 0; r < KP; ++r) P1c[r] = P1n[r];
     }
     double* yp = P.y + (int64_t)za * P.NxNy + p0;
-    for (int z = za; z < zb; ++z) {
+    // step z: plane z + 1 (its Q only when a later step needs it), then row z
+    auto step = [&](auto withq, int z) {
       double P1n[KP], Qn[KP], cn[KP];
 #pragma unroll
       for (int r = 0; r < KP; ++r) P1n[r] = Qn[r] = cn[r] = 0.0;
-      // (the last step's Q, of the run's halo plane, goes unused: one code
-      // path in the loop keeps the kernel at 3 CTAs per SM)
-      if (z + 1 < P.Nz) plane(WithQ{}, z + 1, P1c, P1n, Qn, cn);
+      if (z + 1 < P.Nz) plane(withq, z + 1, P1c, P1n, Qn, cn);
       double yv[KP];
       if (z == 0 || z == P.Nz - 1) {
 #pragma unroll
@@ -202,7 +227,9 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
         Qc[r] = Qn[r];
         cc[r] = cn[r];
       }
-    }
+    };
+    for (int z = za; z < zb - 1; ++z) step(WithQ{}, z);
+    step(NoQ{}, zb - 1);  // the run's last row: the halo plane's Q goes unused
     q += zb - za;
   }
   if (!DOT) return;
