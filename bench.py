@@ -443,6 +443,10 @@ def run_gpu(args):
     # node and the final residual with the CSR values
     gpu_launches = args.steps * (3 * res.num_iters + 6)
 
+    # the rows after the hot path on the same system: ELL storage and the
+    # Jacobi-preconditioned CG
+    next_rows = None if args.no_next else bench_next_rows(args, world, stream, A, b)
+
     # batched uneven boxes and multi-RHS: measured after the headline system
     # is released, so their stores have the memory
     batch = multi = adjoint = small = None
@@ -502,6 +506,7 @@ def run_gpu(args):
                                            "frac": nnz / t_spmv / 1e9 / (FP64_PEAK_TFLOPS / 2 * 1e3)}},
             },
             "mixed": mixed,
+            "next_rows": next_rows,
             "batch": batch,
             "multi_rhs": multi,
             "adjoint": adjoint,
@@ -527,6 +532,80 @@ def run_gpu(args):
 
 
 SEED = 20261201  # S: adjoint conductivity S, target S + 1, FD elements S + 2, batch S + 3
+
+
+def bench_next_rows(args, world, stream, A, b):
+    """The rows after the hot path, measured on the 256^3 system: ELL storage
+    (ELLMatrix: 27 entries per row, the reference's padded layout) -- its
+    conversion from the CSR, its matvec against the bytes it moves (every
+    padded entry's value and column, x and y once) and the FP64 CG with it to
+    1e-8 relative -- and the Jacobi-preconditioned CG to 1e-8 relative on the
+    CSR.  CUDA events, warm-up first."""
+    import torch
+    import minife_gb300 as M
+    n = A.nrows
+    peak, _ = peaks()
+
+    def ev_time(fn, reps):
+        fn()
+        torch.cuda.synchronize()
+        barrier(world)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        out = None
+        for _ in range(reps):
+            out = fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        barrier(world)
+        return max_over_ranks(world, e0.elapsed_time(e1) * 1e-3 / reps), out
+
+    t_conv, E = ev_time(lambda: M.ELLMatrix.from_csr(A), 1)
+    K = E.num_cols_per_row
+    x = torch.randn(n, dtype=torch.float64, device="cuda")
+    y = torch.empty_like(x)
+    t_mv, _ = ev_time(lambda: M.matvec_ell(E, x, y), 10)
+    ell_bytes = n * K * (8 + 4) + 2 * n * 8
+    # the sliced copy the ELL CG iterates on (the same entries, 32-row
+    # slices column-major)
+    t_sconv, S = ev_time(lambda: M.SELLMatrix.from_ell(E), 1)
+    t_smv, _ = ev_time(lambda: M.matvec_sell(S, x, y), 10)
+    sell_bytes = M.SELLMatrix.entries(n, K) * (8 + 4) + 2 * n * 8
+    del S
+    torch.cuda.empty_cache()
+    xs = torch.zeros_like(b)
+
+    def ell_solve():
+        xs.zero_()
+        return M.cg_solve_ell(E, b, xs, max_iter=5000, tol=TOL, tol_mode="relative")
+
+    t_ell, r_ell = ev_time(ell_solve, 1)
+    ell_rel = r_ell.final_resid / r_ell.normr0
+    del E, x, y
+    torch.cuda.empty_cache()
+
+    def pcg_solve():
+        xs.zero_()
+        return M.cg_solve(A, b, xs, max_iter=5000, tol=TOL, tol_mode="relative", precond="jacobi")
+
+    t_pcg, r_pcg = ev_time(pcg_solve, 1)
+    del xs
+    return {
+        "ell": {"conversion_s": t_conv, "cg_s": t_ell, "iterations": r_ell.num_iters,
+                "final_rel_resid": ell_rel, "ncols_per_row": K,
+                "cg_operator": "sliced ELL copy (32-row slices), made inside the call",
+                "spmv": {"ms": t_mv * 1e3, "bytes": ell_bytes,
+                         "achieved_gbs": ell_bytes / t_mv / 1e9, "peak_gbs": peak,
+                         "frac": ell_bytes / t_mv / 1e9 / peak},
+                "sell_conversion_s": t_sconv,
+                "sell_spmv": {"ms": t_smv * 1e3, "bytes": sell_bytes,
+                              "achieved_gbs": sell_bytes / t_smv / 1e9, "peak_gbs": peak,
+                              "frac": sell_bytes / t_smv / 1e9 / peak,
+                              "fp64_fma_frac": n * K / t_smv / (FP64_PEAK_TFLOPS * 0.5e12)}},
+        "pcg_jacobi": {"value": t_pcg, "unit": "s", "iterations": r_pcg.num_iters,
+                       "final_rel_resid": r_pcg.final_resid / r_pcg.normr0},
+    }
 
 
 def bench_small(args, world, stream):
@@ -830,6 +909,8 @@ def main():
     ap.add_argument("--no-batch", action="store_true",
                     help="skip the 96-box batched solve")
     ap.add_argument("--no-small", action="store_true", help="skip the 30^3 case")
+    ap.add_argument("--no-next", action="store_true",
+                    help="skip the ELL and Jacobi-PCG legs (the rows after the hot path)")
     ap.add_argument("--no-adjoint", action="store_true",
                     help="skip the adjoint-gradient leg (128^3 gradient + FD spot check)")
     ap.add_argument("--adjoint-dims", type=int, default=128)

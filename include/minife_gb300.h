@@ -491,9 +491,34 @@ mfe_status mfe_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E);
 /* matvec_std<ELLMatrix> (ref/src/SparseMatrix_functions.hpp:579-611): y = A x,
  * every stored entry summed (padding adds 0 * x[0]). */
 mfe_status mfe_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y);
-/* cg_solve with the ELL matvec (FP64; opts as for mfe_cg_solve). */
+/* cg_solve with the ELL matvec (FP64; opts as for mfe_cg_solve).  Without
+ * preconditioner the iterations' products run on a sliced copy of E
+ * (mfe_sell, made once per call in context workspace); the initial and
+ * final residuals use E itself. */
 mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, double* x,
                             const mfe_cg_opts* opts, mfe_cg_result* result);
+
+/* Sliced ELL: the ELLMatrix layout transposed for the GPU (no counterpart in
+ * the reference).  Rows come in slices of 32 and a slice is column-major:
+ * entry k of row r sits at ((r / 32) * ncols_per_row + k) * 32 + r % 32, so
+ * entry k of 32 consecutive rows is one 256-byte line of values and one
+ * 128-byte line of columns.  The arrays hold ceil(nrows / 32) * 32 *
+ * ncols_per_row entries; rows past nrows hold column 0, value 0.  FP64. */
+typedef struct mfe_sell {
+  int64_t nrows;
+  int32_t ncols_per_row;
+  int32_t reserved;
+  int32_t* cols;  /* device */
+  double* vals;   /* device */
+} mfe_sell;
+
+/* S->cols / S->vals (caller-allocated, ceil(nrows / 32) * 32 * ncols_per_row
+ * entries each) filled from the FP64 ELL matrix E; sets S->nrows and
+ * S->ncols_per_row. */
+mfe_status mfe_ell_to_sell(mfe_ctx* ctx, const mfe_ell* E, mfe_sell* S);
+/* y = A x with the sliced copy (every stored entry summed, as the ELL
+ * matvec: one FP64 FMA per entry, two partial sums per row). */
+mfe_status mfe_spmv_sell(mfe_ctx* ctx, const mfe_sell* S, const double* x, double* y);
 
 /* ------------------------------------------------------------------ */
 /* the reference's debug dumps                                          */

@@ -241,6 +241,56 @@ class ELLMatrix:
         return E
 
 
+class SELLMatrix:
+    """A sliced copy of an FP64 ELLMatrix (mfe_sell): rows in slices of 32,
+    column-major inside a slice -- entry k of row r at ((r // 32) *
+    ncols_per_row + k) * 32 + r % 32 -- so the entries k of 32 consecutive
+    rows are one coalesced line.  The ELL CG runs its iterations on such a
+    copy."""
+
+    SLICE = 32
+
+    def __init__(self, cols, coefs, nrows: int, ncols_per_row: int):
+        self.cols = cols
+        self.coefs = coefs
+        self.nrows = int(nrows)
+        self.num_cols_per_row = int(ncols_per_row)
+
+    @staticmethod
+    def entries(nrows: int, ncols_per_row: int) -> int:
+        s = SELLMatrix.SLICE
+        return (nrows + s - 1) // s * s * ncols_per_row
+
+    def c(self):
+        e = _abi.MfeSell()
+        e.nrows = self.nrows
+        e.ncols_per_row = self.num_cols_per_row
+        e.cols = self.cols.data_ptr()
+        e.vals = self.coefs.data_ptr()
+        return e
+
+    @staticmethod
+    def from_ell(E: "ELLMatrix", ctx: Context | None = None):
+        torch = _torch()
+        ctx = ctx or default_context()
+        m = SELLMatrix.entries(E.nrows, E.num_cols_per_row)
+        S = SELLMatrix(torch.empty(m, dtype=torch.int32, device=E.cols.device),
+                       torch.empty(m, dtype=torch.float64, device=E.cols.device),
+                       E.nrows, E.num_cols_per_row)
+        s = S.c()
+        e = E.c()
+        ctx.check(ctx.lib.mfe_ell_to_sell(ctx.h, ctypes.byref(e), ctypes.byref(s)), "mfe_ell_to_sell")
+        return S
+
+
+def matvec_sell(S: SELLMatrix, x, y, ctx: Context | None = None):
+    """y = A x with the sliced ELL copy (every stored entry summed)."""
+    ctx = ctx or default_context()
+    s = S.c()
+    ctx.check(ctx.lib.mfe_spmv_sell(ctx.h, ctypes.byref(s), _ptr(x), _ptr(y)), "mfe_spmv_sell")
+    return y
+
+
 def matvec_ell(E: ELLMatrix, x, y, ctx: Context | None = None):
     """matvec_std<ELLMatrix> (ref/src/SparseMatrix_functions.hpp:579-611)."""
     ctx = ctx or default_context()

@@ -67,6 +67,11 @@ class MfeEll(ctypes.Structure):
                 ("cols", c_void_p), ("vals", c_void_p)]
 
 
+class MfeSell(ctypes.Structure):
+    _fields_ = [("nrows", c_int64), ("ncols_per_row", c_int32), ("reserved", c_int32),
+                ("cols", c_void_p), ("vals", c_void_p)]
+
+
 class MfeBatchTuning(ctypes.Structure):
     _fields_ = [("spmv_rows", c_int32), ("spmv_stages", c_int32), ("chunk_rows", c_int32)]
 
@@ -144,6 +149,8 @@ SIGNATURES = {
     "mfe_write_matrix": (ctypes.c_int, [c_void_p, _P(MfeCsr), ctypes.c_char_p]),
     "mfe_csr_to_ell": (ctypes.c_int, [c_void_p, _P(MfeCsr), _P(MfeEll)]),
     "mfe_spmv_ell": (ctypes.c_int, [c_void_p, _P(MfeEll), c_void_p, c_void_p]),
+    "mfe_ell_to_sell": (ctypes.c_int, [c_void_p, _P(MfeEll), _P(MfeSell)]),
+    "mfe_spmv_sell": (ctypes.c_int, [c_void_p, _P(MfeSell), c_void_p, c_void_p]),
     "mfe_cg_solve_ell": (ctypes.c_int, [c_void_p, _P(MfeEll), c_void_p, c_void_p, _P(MfeCgOpts),
                                         _P(MfeCgResult)]),
     "mfe_write_vector": (ctypes.c_int, [c_void_p, c_int64, c_void_p, c_int64, ctypes.c_char_p]),

@@ -1067,7 +1067,59 @@ mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, dou
   if (E->nrows == 0) return MFE_OK;
   mfe_csr V;
   MFE_TRY(ell_view(ctx, E, &V));
-  return mfe_cg_solve(ctx, &V, b, x, opts, result);
+  mfe_cg_opts o;
+  if (opts) o = *opts;
+  else mfe_cg_opts_default(&o);
+  if (!cg_opts_valid(o) || o.precision != MFE_PREC_F64 || o.precond != 0)
+    return mfe_cg_solve(ctx, &V, b, x, opts, result);  // validates, or the other solvers
+  if (!b || !x) return fail(ctx, MFE_BAD_ARG, "null vector");
+  // the iterations run on a sliced copy (one coalesced line per entry of 32 rows)
+  const int64_t ne = sell_entries(E->nrows, E->ncols_per_row);
+  mfe_sell S;
+  memset(&S, 0, sizeof(S));
+  S.cols = static_cast<int32_t*>(workspace(ctx, "ell.sell.cols", sizeof(int32_t) * (size_t)ne));
+  S.vals = static_cast<double*>(workspace(ctx, "ell.sell.vals", sizeof(double) * (size_t)ne));
+  if (!S.cols || !S.vals) return fail(ctx, MFE_OOM, "sliced ELL workspace allocation failed");
+  MFE_TRY(launch_ell_to_sell(ctx, E, &S));
+  memset(result, 0, sizeof(*result));
+  const mfe_status st = cg_solve_sell(ctx, &V, &S, b, x, &o, result);
+  result->status = st;
+  return st;
+}
+
+static mfe_status check_sell(mfe_ctx* ctx, const mfe_sell* S)
+{
+  if (!S) return fail(ctx, MFE_BAD_ARG, "null matrix");
+  if (S->ncols_per_row < 1 || S->ncols_per_row > 1024 || S->nrows < 0 ||
+      sell_entries(S->nrows, S->ncols_per_row) >= ((int64_t)1 << 31))
+    return fail(ctx, MFE_BAD_ARG, "sliced ELL sizes out of range for 32-bit indices");
+  if (S->nrows > 0 && (!S->cols || !S->vals)) return fail(ctx, MFE_BAD_ARG, "null sliced ELL array");
+  return MFE_OK;
+}
+
+mfe_status mfe_ell_to_sell(mfe_ctx* ctx, const mfe_ell* E, mfe_sell* S)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_ell(ctx, E, false));
+  if (E->dtype != MFE_F64) return fail(ctx, MFE_BAD_ARG, "the sliced ELL copy is FP64");
+  if (!S || (E->nrows > 0 && (!S->cols || !S->vals))) return fail(ctx, MFE_BAD_ARG, "null sliced ELL array");
+  MFE_TRY(set_device(ctx));
+  if (E->nrows == 0) {
+    S->nrows = 0;
+    S->ncols_per_row = E->ncols_per_row;
+    return MFE_OK;
+  }
+  return launch_ell_to_sell(ctx, E, S);
+}
+
+mfe_status mfe_spmv_sell(mfe_ctx* ctx, const mfe_sell* S, const double* x, double* y)
+{
+  if (!ctx) return MFE_BAD_ARG;
+  MFE_TRY(check_sell(ctx, S));
+  if (S->nrows > 0 && (!x || !y)) return fail(ctx, MFE_BAD_ARG, "null vector");
+  MFE_TRY(set_device(ctx));
+  if (S->nrows == 0) return MFE_OK;
+  return launch_spmv_sell(ctx, S, x, y, nullptr, nullptr);
 }
 
 mfe_status mfe_batch_create(mfe_ctx* ctx, int32_t nbox, const int32_t* dims, mfe_batch** out)

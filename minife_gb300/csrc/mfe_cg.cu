@@ -334,6 +334,9 @@ struct CgBufs {
   bool st64 = false;
   double w8[8] = {};
   double dd = 0.0;
+  // the sliced ELL copy of an ELL matrix (mfe_ell.cu) for the iterations'
+  // products
+  const mfe_sell* sell = nullptr;
 };
 
 }  // namespace mfe
@@ -344,7 +347,7 @@ struct mfe_cg_graph {
   cudaGraphConditionalHandle handle = 0;
   // what the graph was built for: operands, and the stencil operator's
   // weights (kernel parameters baked into the graph) when it runs
-  const void* key[10] = {};
+  const void* key[12] = {};
   double op[10] = {};
   int64_t n = 0;
   cudaStream_t stream = nullptr;
@@ -393,6 +396,7 @@ static mfe_status launch_cg_spmv(mfe_ctx* ctx, const mfe_csr* A, const CgBufs& B
   sink.ticket = rb.tickets;
   sink.out = rb.scalars;
   if (B.st64) return launch_spmv_st64(ctx, A, B.w8, B.dd, B.p, B.Ap, &sink, B.st);
+  if (B.sell) return launch_spmv_sell(ctx, B.sell, B.p, B.Ap, &sink, B.st);
   return launch_spmv(ctx, A, B.p, B.Ap, &sink, nullptr, B.st);
 }
 
@@ -470,14 +474,15 @@ static mfe_status build_graph(mfe_ctx* ctx, const mfe_csr* A, double* x, const C
 // FP64 CG
 // ---------------------------------------------------------------------------
 static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, double* x,
-                         const mfe_cg_opts* o, mfe_cg_result* res, const CgSpec* spec)
+                         const mfe_cg_opts* o, mfe_cg_result* res, const CgSpec* spec,
+                         const mfe_sell* sell = nullptr)
 {
   const int64_t n = A_in->nrows;
   mfe_csr A = *A_in;
   int max_len = 0;
   MFE_TRY(ensure_max_row_len(ctx, &A, &max_len));
   A.max_row_len = max_len;
-  if (!csr_is_box(&A)) {
+  if (!csr_is_box(&A) && !sell) {
     // a CSR without box dimensions may still be a miniFE box matrix (e.g. one
     // handed over through the host drop-in call): recognise it once per solve
     int bx, by, bz;
@@ -488,6 +493,7 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   }
 
   CgBufs B;
+  B.sell = sell;
   B.r = static_cast<double*>(workspace(ctx, "cg.r", sizeof(double) * std::max<int64_t>(n, 1)));
   B.p = static_cast<double*>(workspace(ctx, "cg.p", sizeof(double) * std::max<int64_t>(n, 1)));
   B.Ap = static_cast<double*>(workspace(ctx, "cg.Ap", sizeof(double) * std::max<int64_t>(n, 1)));
@@ -555,9 +561,11 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
   }
 
   // (re)build the graph when the operands changed
-  const void* key[10] = {A.row_offsets, A.cols, A.vals, x, b, B.r, B.p, B.Ap, B.st,
+  const void* key[12] = {A.row_offsets, A.cols, A.vals, x, b, B.r, B.p, B.Ap, B.st,
                          (const void*)(uintptr_t)(((int64_t)A.box_nx << 42) ^
-                                                  ((int64_t)A.box_ny << 21) ^ A.box_nz)};
+                                                  ((int64_t)A.box_ny << 21) ^ A.box_nz),
+                         sell ? (const void*)sell->vals : nullptr,
+                         sell ? (const void*)sell->cols : nullptr};
   double op[10] = {B.st64 ? 1.0 : 0.0, B.dd};
   for (int c = 0; c < 8; ++c) op[2 + c] = B.w8[c];
   mfe_cg_graph* g = ctx->cg_graph;
@@ -695,6 +703,14 @@ mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double
   if (opts->precond == 1) return cg_jacobi(ctx, A, b, x, opts, res);
   if (opts->precision == MFE_PREC_F64) return cg_f64(ctx, A, b, x, opts, res, nullptr);
   return cg_mixed(ctx, A, b, x, opts, res);
+}
+
+mfe_status cg_solve_sell(mfe_ctx* ctx, const mfe_csr* V, const mfe_sell* S, const double* b,
+                         double* x, const mfe_cg_opts* opts, mfe_cg_result* res)
+{
+  if (opts->precond != 0 || opts->precision != MFE_PREC_F64)
+    return fail(ctx, MFE_BAD_ARG, "the sliced ELL CG is FP64 without preconditioner");
+  return cg_f64(ctx, V, b, x, opts, res, nullptr, S);
 }
 
 mfe_status cg_solve_spec(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,

@@ -7,11 +7,21 @@
 // included, which adds 0 * x[0].
 //
 // On the device an ELL matrix is a CSR whose row offsets are r *
-// num_cols_per_row, so the CSR kernels (and the CG) run on it unchanged: this
-// file converts a CSR into the reference's ELL layout and builds that view.
+// num_cols_per_row, so the CSR kernels run on it unchanged: this file
+// converts a CSR into the reference's ELL layout and builds that view.
+//
+// Row-major ELL suits a CPU walking one row at a time; on the GPU a warp of
+// consecutive rows then reads its entries 8 * num_cols_per_row bytes apart.
+// The ELL CG therefore runs on a sliced copy (mfe_sell): rows in slices of
+// 32, column-major inside a slice, so entry k of 32 consecutive rows is one
+// 256-byte line of values and one 128-byte line of columns, and a lane per
+// row sums its row with no staging and no reduction -- one FP64 FMA per
+// stored entry, as the ELL matvec.  The copy is made once per solve by a
+// shared-memory transpose of each slice (k_ell_to_sell).
 #include <algorithm>
 #include <cstring>
 
+#include "mfe_cgstate.cuh"
 #include "mfe_common.cuh"
 #include "mfe_internal.h"
 
@@ -56,7 +66,130 @@ int grid_for(mfe_ctx* ctx, int64_t n)
   return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(n + 1, 256), (int64_t)ctx->sm_count * 8));
 }
 
+constexpr int kSellRows = 32;   // rows per slice
+constexpr int kSellKC = 64;     // columns of a slice transposed at a time
+constexpr int kSellT = 256;     // threads per block
+
+// one block per slice at a time: the slice's rows [r0, r0 + 32) are one
+// contiguous row-major range of the ELL arrays; kSellKC of its columns at a
+// time go through shared memory, read coalesced along the rows and written
+// coalesced along the slice's column-major order
+__global__ void __launch_bounds__(kSellT)
+    k_ell_to_sell(int64_t n, int K, const int32_t* __restrict__ ec, const double* __restrict__ ev,
+                  int32_t* __restrict__ sc, double* __restrict__ sv)
+{
+  __shared__ double tv[kSellRows * kSellKC];
+  __shared__ int32_t tc[kSellRows * kSellKC];
+  const int64_t nslices = (n + kSellRows - 1) / kSellRows;
+  for (int64_t sl = blockIdx.x; sl < nslices; sl += gridDim.x) {
+    const int64_t r0 = sl * kSellRows;
+    const int rows = (int)min((int64_t)kSellRows, n - r0);
+    for (int k0 = 0; k0 < K; k0 += kSellKC) {
+      const int kc = min(kSellKC, K - k0);
+      for (int i = threadIdx.x; i < kSellRows * kc; i += kSellT) {
+        const int lr = i / kc, k = i - lr * kc;
+        const bool in = lr < rows;
+        const int64_t e = (r0 + lr) * K + k0 + k;
+        tv[lr * kSellKC + k] = in ? ev[e] : 0.0;
+        tc[lr * kSellKC + k] = in ? ec[e] : 0;
+      }
+      __syncthreads();
+      for (int i = threadIdx.x; i < kSellRows * kc; i += kSellT) {
+        const int k = i / kSellRows, lr = i - k * kSellRows;
+        const int64_t o = (sl * K + k0 + k) * kSellRows + lr;
+        sv[o] = tv[lr * kSellKC + k];
+        sc[o] = tc[lr * kSellKC + k];
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// y = A x over a sliced ELL matrix, a warp per slice and a lane per row; DOT:
+// x.y into the CG state (p.Ap and the breakdown pre-test) or into dot_out
+template <bool DOT>
+__global__ void __launch_bounds__(kSellT)
+    k_spmv_sell(int64_t n, int K, const int32_t* __restrict__ sc, const double* __restrict__ sv,
+                const double* __restrict__ x, double* __restrict__ y, double* partials,
+                unsigned* ticket, CgState* cg, double* dot_out)
+{
+  __shared__ double red[32];
+  const int lane = threadIdx.x & 31;
+  const int64_t nslices = (n + kSellRows - 1) / kSellRows;
+  const int64_t wstride = (int64_t)gridDim.x * (kSellT / 32);
+  double dacc = 0.0;
+  for (int64_t sl = (int64_t)blockIdx.x * (kSellT / 32) + (threadIdx.x >> 5); sl < nslices;
+       sl += wstride) {
+    const int64_t base = sl * K * kSellRows + lane;
+    const double* v = sv + base;
+    const int32_t* c = sc + base;
+    double s0 = 0.0, s1 = 0.0;
+    int k = 0;
+#pragma unroll 4
+    for (; k + 1 < K; k += 2) {
+      s0 = fma(__ldg(v + (int64_t)k * kSellRows), __ldg(x + __ldg(c + (int64_t)k * kSellRows)), s0);
+      s1 = fma(__ldg(v + (int64_t)(k + 1) * kSellRows),
+               __ldg(x + __ldg(c + (int64_t)(k + 1) * kSellRows)), s1);
+    }
+    if (k < K) s0 = fma(__ldg(v + (int64_t)k * kSellRows), __ldg(x + __ldg(c + (int64_t)k * kSellRows)), s0);
+    const double sum = s0 + s1;
+    const int64_t r = sl * kSellRows + lane;
+    if (r < n) {
+      y[r] = sum;
+      if (DOT) dacc = fma(sum, __ldg(x + r), dacc);
+    }
+  }
+  if (!DOT) return;
+  const double bt = block_sum(dacc, red);
+  double total;
+  if (grid_reduce_last(bt, partials, ticket, red, &total) && threadIdx.x == 0) {
+    if (cg != nullptr) {
+      cg->pAp = total;
+      if (total < cg->brkdown_tol) cg->check_pending = 1;
+    } else {
+      *dot_out = total;
+    }
+  }
+}
+
 }  // namespace
+
+int64_t sell_entries(int64_t nrows, int K) { return ceil_div(nrows, (int64_t)kSellRows) * kSellRows * K; }
+
+mfe_status launch_ell_to_sell(mfe_ctx* ctx, const mfe_ell* E, mfe_sell* S)
+{
+  const int64_t nslices = ceil_div(E->nrows, (int64_t)kSellRows);
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(nslices, (int64_t)ctx->sm_count * 8));
+  k_ell_to_sell<<<g, kSellT, 0, ctx->stream>>>(E->nrows, E->ncols_per_row, E->cols,
+                                               static_cast<const double*>(E->vals), S->cols, S->vals);
+  MFE_TRY(check_launch(ctx, "k_ell_to_sell"));
+  S->nrows = E->nrows;
+  S->ncols_per_row = E->ncols_per_row;
+  return MFE_OK;
+}
+
+mfe_status launch_spmv_sell(mfe_ctx* ctx, const mfe_sell* S, const double* x, double* y,
+                            const DotSink* sink, void* cg_state)
+{
+  const int64_t nslices = ceil_div(S->nrows, (int64_t)kSellRows);
+  CgState* cg = static_cast<CgState*>(cg_state);
+  const bool dot = cg != nullptr || (sink != nullptr && sink->out != nullptr);
+  const void* k = dot ? (const void*)k_spmv_sell<true> : (const void*)k_spmv_sell<false>;
+  const int g = (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(nslices, (int64_t)(kSellT / 32)),
+                           (int64_t)resident_blocks(ctx, k, kSellT, 0)));
+  if (dot) {
+    if (!sink || !sink->partials || !sink->ticket)
+      return fail(ctx, MFE_BAD_ARG, "sliced ELL SpMV: a dot needs reduction buffers");
+    k_spmv_sell<true><<<g, kSellT, 0, ctx->stream>>>(S->nrows, S->ncols_per_row, S->cols, S->vals, x, y,
+                                                     sink->partials, sink->ticket, cg,
+                                                     cg ? nullptr : sink->out);
+  } else {
+    k_spmv_sell<false><<<g, kSellT, 0, ctx->stream>>>(S->nrows, S->ncols_per_row, S->cols, S->vals, x, y,
+                                                      nullptr, nullptr, nullptr, nullptr);
+  }
+  return check_launch(ctx, "k_spmv_sell");
+}
 
 mfe_status launch_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E)
 {

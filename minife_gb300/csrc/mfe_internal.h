@@ -197,6 +197,13 @@ mfe_status adjoint_grad(mfe_ctx* ctx, int nx, int ny, int nz, const double* kapp
 mfe_status launch_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E);
 // CSR view of an ELL matrix (row offsets r * ncols_per_row, cached in workspace)
 mfe_status ell_view(mfe_ctx* ctx, const mfe_ell* E, mfe_csr* V);
+// sliced ELL (mfe_sell): entries of a copy of nrows rows of K entries
+int64_t sell_entries(int64_t nrows, int K);
+// S->cols / S->vals allocated by the caller; E FP64
+mfe_status launch_ell_to_sell(mfe_ctx* ctx, const mfe_ell* E, mfe_sell* S);
+// y = S x; x.y into the CG state (cg_state set) or sink->out (sink set)
+mfe_status launch_spmv_sell(mfe_ctx* ctx, const mfe_sell* S, const double* x, double* y,
+                            const DotSink* sink, void* cg_state);
 
 // ---- Jacobi-preconditioned CG (mfe_pcg.cu) ----
 mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
@@ -252,6 +259,10 @@ struct CgSpec {
 constexpr mfe_status kSpecFailed = (mfe_status)1000;
 mfe_status cg_solve_spec(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                          const mfe_cg_opts* opts, mfe_cg_result* res, const CgSpec* spec);
+// FP64 CG (no preconditioner) whose iterations' products run on the sliced
+// ELL copy S of the matrix V (an ELL view); the residuals use V
+mfe_status cg_solve_sell(mfe_ctx* ctx, const mfe_csr* V, const mfe_sell* S, const double* b,
+                         double* x, const mfe_cg_opts* opts, mfe_cg_result* res);
 void cg_graph_destroy(mfe_cg_graph* g);
 
 }  // namespace mfe

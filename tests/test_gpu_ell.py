@@ -54,3 +54,64 @@ def test_ell_rejects_short_rows():
     with pytest.raises(M.MiniFEError) as ei:
         M.ELLMatrix.from_csr(A, 20)
     assert ei.value.status == 1
+
+
+def np_sell(ec, ev, n, K):
+    """The sliced layout in numpy: entry k of row r at ((r // 32) * K + k) * 32
+    + r % 32, rows past n padded with column 0, value 0."""
+    ns = (n + 31) // 32
+    sc = np.zeros(ns * 32 * K, np.int32)
+    sv = np.zeros(ns * 32 * K, np.float64)
+    for r in range(n):
+        s, l = divmod(r, 32)
+        idx = (s * K + np.arange(K)) * 32 + l
+        sc[idx] = ec[r * K:(r + 1) * K]
+        sv[idx] = ev[r * K:(r + 1) * K]
+    return sc, sv
+
+
+@pytest.mark.parametrize("dims,K", [((4, 5, 6), 27), ((6, 3, 4), 100)])
+def test_sell_layout_and_matvec(dims, K):
+    """The sliced copy against its layout built in numpy (a partial last
+    slice; K = 100 takes the transpose's column chunks), and its matvec
+    within the FMA-reordering bound of the oracle's."""
+    A, b = M.build_system(*dims)
+    E = M.ELLMatrix.from_csr(A, K)
+    S = M.SELLMatrix.from_ell(E)
+    ro, cols, vals, bo = O.build_system(*dims)
+    n = ro.size - 1
+    assert n % 32 != 0
+    ec, ev = np_ell(ro, cols, vals, K)
+    sc, sv = np_sell(ec, ev, n, K)
+    assert np.array_equal(S.cols.cpu().numpy(), sc)
+    assert np.array_equal(S.coefs.cpu().numpy(), sv)
+    x = np.random.default_rng(4).standard_normal(n)
+    y = torch.empty_like(b)
+    M.matvec_sell(S, torch.from_numpy(x).to(b.device), y)
+    yo = O.matvec(ro, cols, vals, x)
+    bound = 30 * 2.0 ** -53 * O.matvec(ro, cols, np.abs(vals), np.abs(x)) + 1e-300
+    assert np.all(np.abs(y.cpu().numpy() - yo) <= bound)
+
+
+def test_ell_cg_relative_and_jacobi():
+    """The ELL CG to 1e-10 relative (its iterations on the sliced copy) and
+    with the Jacobi preconditioner (the ELL matrix's own products), both
+    against the oracle's solution."""
+    dims = (12, 9, 10)
+    A, b = M.build_system(*dims)
+    E = M.ELLMatrix.from_csr(A, 27)
+    ro, cols, vals, bo = O.build_system(*dims)
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=1000, tol=1e-10, tol_mode=1)
+    xg = torch.zeros_like(b)
+    res = M.cg_solve_ell(E, b, xg, max_iter=1000, tol=1e-10, tol_mode="relative")
+    assert res.status == 0 and abs(res.num_iters - it) <= 1
+    assert np.linalg.norm(xg.cpu().numpy() - xo) <= 1e-9 * np.linalg.norm(xo)
+    xj = torch.zeros_like(b)
+    ctx = M.default_context()
+    o, _ = M._opts(1000, 1e-10, "relative", "f64", precond="jacobi")
+    r = M._abi.MfeCgResult()
+    e = E.c()
+    st = ctx.lib.mfe_cg_solve_ell(ctx.h, M.ctypes.byref(e), M._ptr(b), M._ptr(xj),
+                                  M.ctypes.byref(o), M.ctypes.byref(r))
+    assert st == 0
+    assert np.linalg.norm(xj.cpu().numpy() - xo) <= 1e-8 * np.linalg.norm(xo)

@@ -605,3 +605,25 @@ def test_cg_host_dropin_speculative_start():
     assert res.inner_operator == "none"
     res = run(cols, vals, zero, tol=2.220446049250313e-16, tol_mode="absolute")
     assert res.inner_operator == "none"
+
+
+def test_cg_host_dropin_speculative_edges():
+    """Edge cases of the speculative start against the oracle's CG: a zero
+    right-hand side (nothing to do: x stays 0), max_iter = 0 (x0 returned),
+    and a tolerance the initial residual already meets."""
+    dims = (9, 8, 7)
+    ro, cols, vals, bo = O.build_system(*dims)
+    n = ro.size - 1
+    zero_b = np.zeros(n)
+    x = np.zeros(n)
+    res = M.cg_solve_host(ro, cols, vals, zero_b, x, max_iter=100, tol=1e-8, tol_mode="relative")
+    assert res.status == 0 and res.num_iters == 0 and not x.any()
+    for kw in ({"max_iter": 0, "tol": 1e-8, "tol_mode": "relative"},
+               {"max_iter": 100, "tol": 1e6, "tol_mode": "absolute"}):
+        x = np.zeros(n)
+        res = M.cg_solve_host(ro, cols, vals, bo, x, **kw)
+        xo, it, nr, st = O.cg_solve(ro, cols, vals, bo, max_iter=kw["max_iter"], tol=kw["tol"],
+                                    tol_mode=1 if kw["tol_mode"] == "relative" else 0)
+        assert res.status == 0 and res.num_iters == it == 0, (res.num_iters, it)
+        assert not x.any() and not xo.any()
+        assert abs(res.normr - nr) <= 1e-12 * nr
