@@ -541,6 +541,25 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
     MFE_TRY(launch_spmv(ctx, &A, x, B.r, &sink, b, B.st));
     csr_products = 1;
   }
+  // A CSR that is not a box matrix: the iterations' products run on a
+  // sliced copy (32-row slices, column-major inside a slice, rows padded to
+  // the longest) when its rows are short and even enough for the padding to
+  // stay within a quarter of the nonzeros and the solve may run long enough
+  // to repay the copy; the residuals keep the CSR
+  mfe_sell gen_sell;
+  if (!sell && !csr_is_box(&A) && A.dtype == MFE_F64 && max_iter >= 4 && max_len >= 1 &&
+      max_len <= 64) {
+    const int64_t ne = sell_entries(n, max_len);
+    if (ne < ((int64_t)1 << 31) && (double)ne <= 1.25 * (double)A.nnz + 32.0 * max_len) {
+      memset(&gen_sell, 0, sizeof(gen_sell));
+      gen_sell.cols = static_cast<int32_t*>(workspace(ctx, "cg.sell.cols", sizeof(int32_t) * (size_t)ne));
+      gen_sell.vals = static_cast<double*>(workspace(ctx, "cg.sell.vals", sizeof(double) * (size_t)ne));
+      if (!gen_sell.cols || !gen_sell.vals) return fail(ctx, MFE_OOM, "sliced copy allocation failed");
+      MFE_TRY(launch_csr_to_sell(ctx, &A, max_len, &gen_sell));
+      sell = &gen_sell;
+      B.sell = sell;
+    }
+  }
   // The verified FP64 stencil operator (checked on every call) when the
   // tolerance is at least 2^-36 of the initial residual: the operator lies
   // within 2^-39 of every entry of A, so tighter stops (the reference's

@@ -17,7 +17,9 @@
 // 256-byte line of values and one 128-byte line of columns, and a lane per
 // row sums its row with no staging and no reduction -- one FP64 FMA per
 // stored entry, as the ELL matvec.  The copy is made once per solve by a
-// shared-memory transpose of each slice (k_ell_to_sell).
+// shared-memory transpose of each slice (k_ell_to_sell); the FP64 CG makes
+// the same copy of any CSR that is not a box matrix (k_csr_to_sell, rows
+// padded to the longest).
 #include <algorithm>
 #include <cstring>
 
@@ -152,9 +154,52 @@ __global__ void __launch_bounds__(kSellT)
   }
 }
 
+// a CSR with rows of at most K entries into the sliced layout, one thread
+// per output entry (writes coalesced; each row's entries padded with column
+// 0, value 0)
+__global__ void __launch_bounds__(kSellT)
+    k_csr_to_sell(int64_t n, int K, const int32_t* __restrict__ ro, const int32_t* __restrict__ cols,
+                  const double* __restrict__ vals, int32_t* __restrict__ sc, double* __restrict__ sv,
+                  int64_t total)
+{
+  for (int64_t o = (int64_t)blockIdx.x * kSellT + threadIdx.x; o < total;
+       o += (int64_t)gridDim.x * kSellT) {
+    const int64_t sk = o / kSellRows;  // slice * K + k
+    const int lane = (int)(o - sk * kSellRows);
+    const int64_t sl = sk / K;
+    const int k = (int)(sk - sl * K);
+    const int64_t r = sl * kSellRows + lane;
+    int32_t c = 0;
+    double v = 0.0;
+    if (r < n) {
+      const int32_t a = __ldg(ro + r), e = __ldg(ro + r + 1);
+      if (k < e - a) {
+        c = __ldg(cols + a + k);
+        v = __ldg(vals + a + k);
+      }
+    }
+    sc[o] = c;
+    sv[o] = v;
+  }
+}
+
 }  // namespace
 
 int64_t sell_entries(int64_t nrows, int K) { return ceil_div(nrows, (int64_t)kSellRows) * kSellRows * K; }
+
+mfe_status launch_csr_to_sell(mfe_ctx* ctx, const mfe_csr* A, int K, mfe_sell* S)
+{
+  const int64_t total = sell_entries(A->nrows, K);
+  const int g = (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(total, (int64_t)kSellT),
+                                                            (int64_t)ctx->sm_count * 16));
+  k_csr_to_sell<<<g, kSellT, 0, ctx->stream>>>(A->nrows, K, A->row_offsets, A->cols,
+                                               static_cast<const double*>(A->vals), S->cols, S->vals,
+                                               total);
+  MFE_TRY(check_launch(ctx, "k_csr_to_sell"));
+  S->nrows = A->nrows;
+  S->ncols_per_row = K;
+  return MFE_OK;
+}
 
 mfe_status launch_ell_to_sell(mfe_ctx* ctx, const mfe_ell* E, mfe_sell* S)
 {

@@ -201,6 +201,8 @@ mfe_status ell_view(mfe_ctx* ctx, const mfe_ell* E, mfe_csr* V);
 int64_t sell_entries(int64_t nrows, int K);
 // S->cols / S->vals allocated by the caller; E FP64
 mfe_status launch_ell_to_sell(mfe_ctx* ctx, const mfe_ell* E, mfe_sell* S);
+// the same from an FP64 CSR whose rows hold at most K entries
+mfe_status launch_csr_to_sell(mfe_ctx* ctx, const mfe_csr* A, int K, mfe_sell* S);
 // y = S x; x.y into the CG state (cg_state set) or sink->out (sink set)
 mfe_status launch_spmv_sell(mfe_ctx* ctx, const mfe_sell* S, const double* x, double* y,
                             const DotSink* sink, void* cg_state);

@@ -154,6 +154,33 @@ def test_ragged_generic_csr_tiled():
     assert np.allclose(host(y), O.matvec(ro, cols, vals, x), rtol=1e-13, atol=1e-13)
 
 
+def test_cg_generic_csr_sliced_copy():
+    """A CSR that is not a box matrix (symmetric banded, diagonally dominant,
+    rows of 9 to 17 entries, 4,099 rows: a partial last slice): the FP64 CG
+    iterates on its sliced copy; against the oracle's CG on the same arrays."""
+    n, h = 4099, 8
+    ro = [0]
+    cols, vals = [], []
+    for i in range(n):
+        for j in range(max(0, i - h), min(n, i + h + 1)):
+            cols.append(j)
+            vals.append(20.0 if i == j else -1.0 - 0.01 * ((i + j) % 7))
+        ro.append(len(cols))
+    ro = np.array(ro, np.int32)
+    cols = np.array(cols, np.int32)
+    vals = np.array(vals, np.float64)
+    b = np.random.default_rng(8).standard_normal(n)
+    A = M.CSRMatrix(cuda(ro), cuda(cols), cuda(vals))
+    for tol, mode in ((1e-12, "relative"), (2.220446049250313e-16, "absolute")):
+        x = torch.zeros(n, dtype=torch.float64, device=DEV)
+        res = M.cg_solve(A, cuda(b), x, max_iter=500, tol=tol, tol_mode=mode)
+        xo, it, nr, st = O.cg_solve(ro, cols, vals, b, max_iter=500, tol=tol,
+                                    tol_mode=1 if mode == "relative" else 0)
+        assert res.status == 0 and res.inner_operator == "none"
+        assert abs(res.num_iters - it) <= 1, (res.num_iters, it)
+        assert np.linalg.norm(host(x) - xo) <= 1e-11 * np.linalg.norm(xo)
+
+
 def test_dot_waxpby():
     rng = np.random.default_rng(5)
     for n in (1, 7, 1000, 123457):
@@ -579,9 +606,12 @@ def test_cg_host_dropin_speculative_start():
         # by a few on some systems; the residual and solution do not
         assert abs(res.num_iters - it) <= max(2, it // 10), (res.num_iters, it)
         if mode == 1:
+            # the stencil solve stops on the true residual; the CSR solve, as
+            # the reference, on its recursive one (the true one within drift)
             r0 = np.linalg.norm(bo - O.matvec(ro, c, v, x0))
             rel = np.linalg.norm(bo - O.matvec(ro, c, v, x)) / r0
-            assert rel <= 1.001 * kw["tol"], rel
+            slack = 1.001 if res.inner_operator == "stencil64" else 2.0
+            assert rel <= slack * kw["tol"], rel
         # two iterates at a 1e-10 residual differ by its image under A^-1
         # (condition number ~ 250 here)
         assert np.linalg.norm(x - xo) <= 1e-7 * np.linalg.norm(xo)
