@@ -623,7 +623,8 @@ def bench_next_rows(args, world, stream, A, b):
                               "frac": sell_bytes / t_smv / 1e9 / peak,
                               "fp64_fma_frac": n * K / t_smv / (FP64_PEAK_TFLOPS * 0.5e12)}},
         "pcg_jacobi": {"value": t_pcg, "unit": "s", "iterations": r_pcg.num_iters,
-                       "final_rel_resid": r_pcg.final_resid / r_pcg.normr0},
+                       "final_rel_resid": r_pcg.final_resid / r_pcg.normr0,
+                       "operator": r_pcg.inner_operator},
         "generic_csr_cg": {"value": t_gen, "unit": "s", "iterations": r_gen.num_iters,
                            "final_rel_resid": r_gen.final_resid / r_gen.normr0,
                            "what": "FP64 CG on a CSR that is not a box matrix (one row's "

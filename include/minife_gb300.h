@@ -279,7 +279,10 @@ typedef struct mfe_cg_opts {
                            library uses its stencil operator or converts a
                            copy on every call, see mixed_operator) */
   int32_t precond;      /* mfe_cg_solve: 0 none (the reference's CG), 1 Jacobi
-                           (M = diag(A), FP64; stops on ||r|| after the update) */
+                           (M = diag(A), FP64; stops on ||r|| after the update;
+                           its products follow f64_operator as well, a
+                           stencil solve stopping on ||b - A x|| with the CSR
+                           values) */
   int32_t mixed_operator; /* mixed solves (mfe_cg_solve, mfe_batch_solve):
                            0 = the FP32 stencil operator (28 numbers: the
                            interior 27-point stencil and the Dirichlet
@@ -292,7 +295,7 @@ typedef struct mfe_cg_opts {
                            (padded values for batches); 1 = always the FP32
                            values.  mfe_cg_result.inner_operator reports
                            which ran. */
-  int32_t f64_operator; /* FP64 solves (mfe_cg_solve without preconditioner):
+  int32_t f64_operator; /* FP64 solves (mfe_cg_solve, with or without Jacobi):
                            0 = the verified FP64 stencil operator when A is a
                            miniFE box operator whose interior stencil is
                            mirror-symmetric (every box miniFE assembles with

@@ -7,7 +7,11 @@
 //
 // stopping on ||r|| (absolute, or relative to ||r0||) after the update, at
 // most max_iter iterations.  Kernels: the SpMV of the unpreconditioned solver
-// (box-structured or generic, with p.Ap fused), one update kernel that also
+// (box-structured or generic, with p.Ap fused -- or, for a verified miniFE box
+// operator and a tolerance of at least 2^-36 of the initial residual, the
+// FP64 stencil operator, the solve then stopping only once ||b - A x|| with
+// the CSR values meets the tolerance, restarting from that residual
+// otherwise, as the unpreconditioned solver), one update kernel that also
 // applies M^-1 and reduces r.z and r.r, one p update; the loop is a CUDA graph
 // with a conditional while node, as for the other solvers.
 #include <algorithm>
@@ -77,11 +81,12 @@ __device__ bool two_dot_last(double a, double b, double* partials, unsigned* tic
   return threadIdx.x == 0;
 }
 
-// z = M^-1 r, p = z, rz = r.z, rr = r.r (after the initial residual)
+// z = M^-1 r, p = z, rz = r.z, rr = r.r (after the initial residual, or
+// after a true residual to restart from: restart keeps k and normr0)
 __global__ void __launch_bounds__(kPT)
     k_pcg_init(int64_t n, const double* __restrict__ r, const double* __restrict__ dinv,
                double* __restrict__ z, double* __restrict__ p, PcgState* st, double* partials,
-               unsigned* ticket)
+               unsigned* ticket, int restart)
 {
   __shared__ double red[64];
   double a = 0.0, c = 0.0;
@@ -96,10 +101,12 @@ __global__ void __launch_bounds__(kPT)
   if (two_dot_last(a, c, partials, ticket, red, &rz, &rr)) {
     st->rz = rz;
     st->rr = rr;
-    st->normr0 = sqrt(rr);
-    st->normr = st->normr0;
-    st->k = 0;
-    st->cont = st->max_iter > 0 && st->normr0 > st->tol_abs;
+    st->normr = sqrt(rr);
+    if (!restart) {
+      st->normr0 = st->normr;
+      st->k = 0;
+    }
+    st->cont = st->k < st->max_iter && st->normr > st->tol_abs;
   }
 }
 
@@ -172,9 +179,13 @@ mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
   if (!r || !z || !p || !Ap || !dinv || !st || !partials || !spart || !tickets)
     return fail(ctx, MFE_OOM, "PCG workspace allocation failed");
   if (spmv_grid(ctx, A) > kPMaxSpmvPartials) return fail(ctx, MFE_NOT_SUPPORTED, "matrix too large");
+  bool st64 = false;
+  double w8[8] = {}, dd = 0.0;
   if (fresh) MFE_CUDA_TRY(ctx, cudaMemsetAsync(tickets, 0, sizeof(unsigned) * 4, ctx->stream));
 
-  PcgState* hs = static_cast<PcgState*>(host_scratch(ctx, sizeof(PcgState)));
+  // pinned scratch sized once for the stencil check's class table too, so
+  // it is not reallocated under hs
+  PcgState* hs = static_cast<PcgState*>(host_scratch(ctx, 32768));
   if (!hs) return fail(ctx, MFE_OOM, "pinned scratch allocation failed");
   memset(hs, 0, sizeof(PcgState));
   hs->max_iter = o->max_iter;
@@ -189,39 +200,53 @@ mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
   // r = b - A x0
   DotSink rs{spart, tickets + 2, &st->rr};
   MFE_TRY(launch_spmv(ctx, A, x, r, &rs, b, nullptr));
-  if (o->tol_mode == MFE_TOL_RELATIVE) {
-    // tol_abs = tol * ||r0|| (the initial kernel reads rr written just above)
+  int csr_products = 1;
+  double tol_abs = o->tol;
+  const bool try_st64 = o->f64_operator == 0 && csr_is_box(A) && A->dtype == MFE_F64;
+  if (o->tol_mode == MFE_TOL_RELATIVE || try_st64) {
     MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
     double rr0 = 0.0;
     MFE_CUDA_TRY(ctx, cudaMemcpy(&rr0, &st->rr, sizeof(double), cudaMemcpyDeviceToHost));
-    const double tol_abs = o->tol * sqrt(rr0);
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&st->tol_abs, &tol_abs, sizeof(double), cudaMemcpyHostToDevice,
-                                      ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (o->tol_mode == MFE_TOL_RELATIVE) {
+      // tol_abs = tol * ||r0|| (the initial kernel reads rr written just above)
+      tol_abs = o->tol * sqrt(rr0);
+      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&st->tol_abs, &tol_abs, sizeof(double), cudaMemcpyHostToDevice,
+                                        ctx->stream));
+      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    }
+    // the verified FP64 stencil operator: tolerances below 2^-36 of the
+    // initial residual would meet its rounding-level difference from A
+    bool ok = false;
+    if (try_st64 && tol_abs >= std::ldexp(sqrt(rr0), -36))
+      MFE_TRY(stencil64_prepare(ctx, A, w8, &dd, &ok));  // overwrites hs
+    st64 = ok;
   }
-  k_pcg_init<<<vg, kPT, 0, ctx->stream>>>(n, r, dinv, z, p, st, partials, tickets);
+  k_pcg_init<<<vg, kPT, 0, ctx->stream>>>(n, r, dinv, z, p, st, partials, tickets, 0);
   MFE_TRY(check_launch(ctx, "k_pcg_init"));
   DotSink ps{spart, tickets + 2, &st->pAp};
 
   auto body = [&](cudaGraphConditionalHandle h, int in_graph) -> mfe_status {
-    MFE_TRY(launch_spmv(ctx, A, p, Ap, &ps, nullptr, nullptr));
+    if (st64)
+      MFE_TRY(launch_spmv_st64(ctx, A, w8, dd, p, Ap, &ps, nullptr));
+    else
+      MFE_TRY(launch_spmv(ctx, A, p, Ap, &ps, nullptr, nullptr));
     k_pcg_update<<<vg, kPT, 0, ctx->stream>>>(n, x, r, z, p, Ap, dinv, st, partials, tickets, h,
                                              in_graph);
     MFE_TRY(check_launch(ctx, "k_pcg_update"));
     k_pcg_p<<<vg, kPT, 0, ctx->stream>>>(n, z, p, st);
     return check_launch(ctx, "k_pcg_p");
   };
-  if (getenv("MFE_CG_EAGER") != nullptr) {
-    for (;;) {
-      MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
-      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      if (!hs->cont) break;
-      MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
-    }
-  } else {
+  const bool eager = getenv("MFE_CG_EAGER") != nullptr;
+  cudaGraph_t g = nullptr;
+  cudaGraphExec_t ex = nullptr;
+  auto release = [&]() {
+    if (ex) cudaGraphExecDestroy(ex);
+    if (g) cudaGraphDestroy(g);
+    ex = nullptr;
+    g = nullptr;
+  };
+  if (!eager) {
     cudaStream_t run_stream = ctx->stream, s = ctx->own_stream;
-    cudaGraph_t g = nullptr;
-    cudaGraphExec_t ex = nullptr;
     cudaGraphConditionalHandle h = 0;
     mfe_status bst = MFE_OK;
     cudaError_t e = cudaGraphCreate(&g, 0);
@@ -257,13 +282,56 @@ mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
       }
       ctx->stream = run_stream;
       if (e == cudaSuccess && bst == MFE_OK) e = cudaGraphInstantiate(&ex, g, 0);
-      if (e == cudaSuccess && bst == MFE_OK) e = cudaGraphLaunch(ex, ctx->stream);
     }
-    if (ex) cudaGraphExecDestroy(ex);
-    if (g) cudaGraphDestroy(g);
-    if (bst != MFE_OK) return bst;
-    if (e != cudaSuccess) return cuda_fail(ctx, e, "PCG graph");
+    if (bst != MFE_OK) {
+      release();
+      return bst;
+    }
+    if (e != cudaSuccess) {
+      release();
+      return cuda_fail(ctx, e, "PCG graph");
+    }
   }
+  // the loop; a stencil solve that met its test is checked with the CSR
+  // values and, should the operator's rounding-level difference from A ever
+  // matter, restarted from the true residual (at most three times)
+  double true_resid = -1.0;
+  bool maxed = false;
+  for (int restarts = 0;; ++restarts) {
+    if (eager) {
+      for (;;) {
+        MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
+        MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+        if (!hs->cont) break;
+        MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
+      }
+    } else {
+      const cudaError_t e = cudaGraphLaunch(ex, ctx->stream);
+      if (e != cudaSuccess) {
+        release();
+        return cuda_fail(ctx, e, "PCG graph launch");
+      }
+    }
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
+    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    if (!st64 || hs->status != 0 || !(hs->normr <= hs->tol_abs)) break;
+    DotSink ts{spart, tickets + 2, &st->rr};
+    MFE_TRY(launch_spmv(ctx, A, x, r, &ts, b, nullptr));
+    ++csr_products;
+    double rr = 0.0;
+    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&hs->rr, &st->rr, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    rr = hs->rr;
+    true_resid = sqrt(std::max(rr, 0.0));
+    if (true_resid <= hs->tol_abs) break;
+    if (restarts >= 3 || hs->k >= hs->max_iter) {
+      maxed = true;
+      break;
+    }
+    k_pcg_init<<<vg, kPT, 0, ctx->stream>>>(n, r, dinv, z, p, st, partials, tickets, 1);
+    MFE_TRY(check_launch(ctx, "k_pcg_init"));
+  }
+  release();
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
@@ -273,12 +341,14 @@ mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
   res->num_iters = hs->k;
   res->normr = hs->normr;
   res->normr0 = hs->normr0;
-  res->final_resid = hs->normr;
+  res->final_resid = true_resid >= 0.0 ? true_resid : hs->normr;
   res->times[4] = ms * 1e-3;
-  res->fp64_spmvs = hs->k + 1;
+  res->fp64_spmvs = st64 ? csr_products : hs->k + 1;
+  res->inner_operator = st64 ? MFE_INNER_STENCIL64 : MFE_INNER_NONE;
   ctx->history.clear();
   if (hs->status) return MFE_BREAKDOWN;
-  return hs->normr <= hs->tol_abs ? MFE_OK : MFE_MAXITER;
+  if (maxed) return fail(ctx, MFE_MAXITER, "Jacobi PCG: the CSR residual stayed above the tolerance");
+  return res->final_resid <= hs->tol_abs ? MFE_OK : MFE_MAXITER;
 }
 
 }  // namespace mfe
