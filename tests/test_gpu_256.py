@@ -138,3 +138,51 @@ def test_256_mixed(golden, system):
     assert rc == 0, err
     print("256^3 mixed: %d inner iterations, %d reliable updates, true rel residual %.3e, "
           "sampled x diff %.2e" % (res.num_iters, res.refinements, rel, dx))
+
+
+def test_256_pcg_ell_generic(golden, system):
+    """The solvers beside the hot path at 256^3, each checked by its true
+    residual (the oracle's matvec) and against the reference's sampled
+    solution: the Jacobi PCG (verified stencil operator: it stops on the
+    true residual), the ELL CG iterating on its sliced copy, and the CG of a
+    CSR that is not a box matrix (one interior row's columns rotated, the
+    same operator; both of these stop on the recursive residual, as the
+    reference, so the true one may drift past the tolerance a little)."""
+    A, b, host = system
+    ro, cols, vals, bh = host
+    xs = golden["x_samples"]
+
+    def check(x, slack):
+        xh = x.cpu().numpy()
+        rel = np.linalg.norm(bh - O.matvec(ro, cols, vals, xh)) / np.linalg.norm(bh)
+        assert rel <= slack * 1e-8, rel
+        dx = np.abs(xh[::golden["x_stride"]] - xs).max() / np.abs(xs).max()
+        assert dx <= X_TOL, dx
+
+    x = torch.zeros_like(b)
+    r = M.cg_solve(A, b, x, max_iter=2000, tol=1e-8, tol_mode="relative", precond="jacobi")
+    assert r.status == 0 and r.inner_operator == "stencil64"
+    check(x, 1.001)
+
+    E = M.ELLMatrix.from_csr(A)
+    x = torch.zeros_like(b)
+    r = M.cg_solve_ell(E, b, x, max_iter=2000, tol=1e-8, tol_mode="relative")
+    assert r.status == 0
+    check(x, 2.0)
+    del E
+    torch.cuda.empty_cache()
+
+    Nx = DIMS[0] + 1
+    row = Nx * Nx * (DIMS[2] // 2) + Nx * (DIMS[1] // 2) + DIMS[0] // 2
+    a, e = int(ro[row]), int(ro[row + 1])
+    gcols = A.packed_cols.clone()
+    gvals = A.packed_coefs.clone()
+    gcols[a:e] = torch.roll(gcols[a:e], 1)
+    gvals[a:e] = torch.roll(gvals[a:e], 1)
+    G = M.CSRMatrix(A.row_offsets, gcols, gvals)
+    x = torch.zeros_like(b)
+    r = M.cg_solve(G, b, x, max_iter=2000, tol=1e-8, tol_mode="relative")
+    assert r.status == 0 and r.inner_operator == "none"
+    check(x, 2.0)
+    del G, gcols, gvals
+    torch.cuda.empty_cache()
