@@ -115,10 +115,13 @@ __global__ void __launch_bounds__(kT)
 // per thread (FP32 operations: one FP64 FMA per row would make the kernel
 // FP64-bound on GB300) and summed in FP64 across threads and blocks; x32 +=
 // alpha p is left pending (k_mx_p / k_mx_xupdate).  The last block decides
-// whether a reliable update is due.
+// whether a reliable update is due; inside the graph it also does the
+// bookkeeping of an iteration without one (k_mx_after's, which then runs only
+// in the conditional node of the update) and sets both graph conditions.
 __global__ void __launch_bounds__(kT)
     k_mx_update(int64_t n, float* __restrict__ r, const float* __restrict__ Ap, MixState* st,
-                double* partials, unsigned* ticket)
+                double* partials, unsigned* ticket, cudaGraphConditionalHandle h_loop,
+                cudaGraphConditionalHandle h_upd, int in_graph)
 {
   __shared__ float2 red[32];
   __shared__ float s_alpha;
@@ -162,6 +165,19 @@ __global__ void __launch_bounds__(kT)
     st->gate = st->status == 0 &&
                (st->since >= st->refine_k || total < st->delta2 * st->rr_at_update ||
                 total <= st->tol_abs * st->tol_abs || st->k >= st->max_iter);
+    if (in_graph) {
+      if (!st->gate) {
+        if (st->status != 0) {
+          st->cont = 0;
+        } else {
+          st->beta = total / st->rr;
+          st->rr = total;
+          st->cont = st->k < st->max_iter;
+        }
+        cudaGraphSetConditional(h_loop, st->cont ? 1u : 0u);
+      }
+      cudaGraphSetConditional(h_upd, st->gate ? 1u : 0u);
+    }
   }
 }
 
@@ -256,10 +272,13 @@ int grid_for(mfe_ctx* ctx, int64_t n, const void* kernel)
                            (int64_t)resident_blocks(ctx, kernel, kT, 0)));
 }
 
+// one iteration up to the update decision: p update, FP32 operator with
+// p.Ap, r update (h_upd: the graph condition of the reliable update)
 mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, const double* b,
-                       double* x, const MixBufs& B, cudaGraphConditionalHandle h, int in_graph)
+                       double* x, const MixBufs& B, cudaGraphConditionalHandle h,
+                       cudaGraphConditionalHandle h_upd, int in_graph)
 {
-  const int64_t n = A64.nrows, nv = B.nv;
+  const int64_t nv = B.nv;
   k_mx_p<<<grid_for(ctx, nv / 4, (const void*)k_mx_p), kT, 0, ctx->stream>>>(nv, B.r, B.p, B.x32, B.st);
   MFE_TRY(check_launch(ctx, "k_mx_p"));
   DotSink s1;
@@ -271,8 +290,16 @@ mfe_status launch_iter(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, con
   else
     MFE_TRY(launch_spmv(ctx, &A32, B.p, B.Ap, &s1, nullptr, nullptr));
   k_mx_update<<<grid_for(ctx, nv / 4, (const void*)k_mx_update), kT, 0, ctx->stream>>>(
-      nv, B.r, B.Ap, B.st, B.partials + kMaxPart, B.tickets + 1);
-  MFE_TRY(check_launch(ctx, "k_mx_update"));
+      nv, B.r, B.Ap, B.st, B.partials + kMaxPart, B.tickets + 1, h, h_upd, in_graph);
+  return check_launch(ctx, "k_mx_update");
+}
+
+// the reliable update (gated: its kernels return at once unless it is due;
+// inside the graph they run in a conditional node) and the bookkeeping
+mfe_status launch_update(mfe_ctx* ctx, const mfe_csr& A64, const double* b, double* x,
+                         const MixBufs& B, cudaGraphConditionalHandle h, int in_graph)
+{
+  const int64_t n = A64.nrows;
   k_mx_xupdate<<<grid_for(ctx, n, (const void*)k_mx_xupdate), kT, 0, ctx->stream>>>(
       n, x, B.x32, B.p, B.st, A64.box_nx + 1, B.pad);
   MFE_TRY(check_launch(ctx, "k_mx_xupdate"));
@@ -402,7 +429,8 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
       MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, B.st, sizeof(MixState), cudaMemcpyDeviceToHost, ctx->stream));
       MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
       if (!hs->cont || hs->err) break;
-      MFE_TRY(launch_iter(ctx, A32, A64, b, x, B, 0, 0));
+      MFE_TRY(launch_iter(ctx, A32, A64, b, x, B, 0, 0, 0));
+      MFE_TRY(launch_update(ctx, A64, b, x, B, 0, 0));
     }
   } else {
     // graph: begin kernel, then while(cont) { one iteration }
@@ -434,13 +462,50 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
       cudaGraphNode_t cnode;
       if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
       if (e == cudaSuccess) {
+        // body: the iteration up to the update decision, then a conditional
+        // node holding the reliable update, entered only when it is due
         cudaGraph_t body = cp->conditional.phGraph_out[0];
-        e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        cudaGraphConditionalHandle hu = 0;
+        e = cudaGraphConditionalHandleCreate(&hu, body, 0, 0);
+        if (e == cudaSuccess)
+          e = cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+        cudaGraphNode_t leaf[4];
+        size_t nleaf = 0;
         if (e == cudaSuccess) {
-          st = launch_iter(ctx, A32, A64, b, x, B, h, 1);
+          st = launch_iter(ctx, A32, A64, b, x, B, h, hu, 1);
+          cudaStreamCaptureStatus cs;
+          const cudaGraphNode_t* deps = nullptr;
+          size_t nd = 0;
+          cudaError_t e1 = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+          if (e1 == cudaSuccess && nd >= 1 && nd <= 4) {
+            for (size_t i = 0; i < nd; ++i) leaf[i] = deps[i];
+            nleaf = nd;
+          } else if (e1 == cudaSuccess) {
+            e1 = cudaErrorUnknown;
+          }
           cudaGraph_t tmp;
           cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+          if (e == cudaSuccess) e = e1;
           if (e == cudaSuccess) e = e2;
+        }
+        alignas(cudaGraphNodeParams) unsigned char up_buf[sizeof(cudaGraphNodeParams)];
+        memset(up_buf, 0, sizeof(up_buf));
+        cudaGraphNodeParams* up = reinterpret_cast<cudaGraphNodeParams*>(up_buf);
+        up->type = cudaGraphNodeTypeConditional;
+        up->conditional.handle = hu;
+        up->conditional.type = cudaGraphCondTypeIf;
+        up->conditional.size = 1;
+        cudaGraphNode_t unode;
+        if (e == cudaSuccess && st == MFE_OK) e = cudaGraphAddNode(&unode, body, leaf, nullptr, nleaf, up);
+        if (e == cudaSuccess && st == MFE_OK) {
+          cudaGraph_t ubody = up->conditional.phGraph_out[0];
+          e = cudaStreamBeginCaptureToGraph(s, ubody, nullptr, nullptr, 0, cudaStreamCaptureModeRelaxed);
+          if (e == cudaSuccess) {
+            st = launch_update(ctx, A64, b, x, B, h, 1);
+            cudaGraph_t tmp;
+            cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+            if (e == cudaSuccess) e = e2;
+          }
         }
       }
       ctx->stream = run_stream;
