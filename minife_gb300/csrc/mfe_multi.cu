@@ -1023,7 +1023,11 @@ __global__ void __launch_bounds__(kVT)
 // iteration limit.  (Waiting for the slowest keeps the update count near a
 // single solve's; a right-hand side that claims convergence early keeps
 // iterating on its recursion until the update checks its true residual.)
-__global__ void k_mr_decide(MultiState* st)
+// Inside the graph (in_graph) the reliable update runs in a conditional node:
+// this kernel sets its condition (h_upd) and, for an iteration without one,
+// does k_mr_after's bookkeeping and sets the loop condition (h_loop).
+__global__ void k_mr_decide(MultiState* st, cudaGraphConditionalHandle h_loop,
+                            cudaGraphConditionalHandle h_upd, int in_graph)
 {
   const int j = threadIdx.x;
   const int nr = st->nrhs;
@@ -1038,13 +1042,29 @@ __global__ void k_mr_decide(MultiState* st)
   }
   const bool all_ready = __all_sync(0xffffffffu, ready);
   const bool any_brk = __any_sync(0xffffffffu, brk);
+  const int k = st->k + 1, since = st->since + 1;
+  const bool gate = all_ready || any_brk || since >= st->refine_k || k >= st->max_iter;
+  __syncwarp();
   if (j == 0) {
-    st->k += 1;
-    st->since += 1;
+    st->k = k;
+    st->since = since;
     st->first = 0;
     st->x_pending = 1;  // this iteration's x32 += alpha p (k_mr_p next, or k_mr_xupdate)
-    st->gate = all_ready || any_brk || st->since >= st->refine_k || st->k >= st->max_iter;
+    st->gate = gate;
   }
+  if (!in_graph) return;
+  if (!gate) {
+    if (j < nr && !st->done[j]) {
+      st->beta[j] = st->rr_new[j] / st->rr[j];
+      st->rr[j] = st->rr_new[j];
+    }
+    const bool open = __any_sync(0xffffffffu, j < nr && !st->done[j]);
+    if (j == 0) {
+      st->cont = open && k < st->max_iter;
+      cudaGraphSetConditional(h_loop, st->cont ? 1u : 0u);
+    }
+  }
+  if (j == 0) cudaGraphSetConditional(h_upd, gate ? 1u : 0u);
 }
 
 // Mixed solver, one warp, after the gated FP64 residual: per right-hand side
@@ -1290,11 +1310,11 @@ int vgrid(mfe_ctx* ctx, int64_t n, K kernel)
                             (int64_t)ctx->sm_count * per_sm, (int64_t)kMaxPartM}));
 }
 
-// one iteration of the mixed solver: FP32 SpMM, FP32 vectors, gated FP64
-// reliable update
+// one iteration of the mixed solver up to the update decision: FP32 SpMM,
+// FP32 vectors (h_upd: the graph condition of the reliable update)
 mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64, int nrhs,
-                            const double* B, double* X, const MultiBufs<float>& W,
-                            cudaGraphConditionalHandle h, int in_graph)
+                            const MultiBufs<float>& W, cudaGraphConditionalHandle h,
+                            cudaGraphConditionalHandle h_upd, int in_graph)
 {
   const int64_t ntot = A64.nrows * (int64_t)nrhs;
   k_mr_p<float><<<vgrid(ctx, ntot, k_mr_p<float>), kVT, 0, ctx->stream>>>(ntot, nrhs, W.r, W.p, W.x32, W.st);
@@ -1339,8 +1359,17 @@ mfe_status multi_iter_mixed(mfe_ctx* ctx, const mfe_csr& A32, const mfe_csr& A64
   k_mr_update<float><<<vgrid(ctx, ntot, k_mr_update<float>), kVT, 0, ctx->stream>>>(
       ntot, nrhs, W.x32, W.r, W.p, W.Ap, W.st, W.partials + (size_t)kMaxPartM * 32, W.tickets + 1);
   MFE_TRY(check_launch(ctx, "k_mr_update"));
-  k_mr_decide<<<1, 32, 0, ctx->stream>>>(W.st);
-  MFE_TRY(check_launch(ctx, "k_mr_decide"));
+  k_mr_decide<<<1, 32, 0, ctx->stream>>>(W.st, h, h_upd, in_graph);
+  return check_launch(ctx, "k_mr_decide");
+}
+
+// the gated FP64 reliable update (inside the graph: in a conditional node)
+// and the bookkeeping
+mfe_status multi_update_mixed(mfe_ctx* ctx, const mfe_csr& A64, int nrhs, const double* B,
+                              double* X, const MultiBufs<float>& W, cudaGraphConditionalHandle h,
+                              int in_graph)
+{
+  const int64_t ntot = A64.nrows * (int64_t)nrhs;
   k_mr_xupdate<<<vgrid(ctx, ntot, k_mr_xupdate), kVT, 0, ctx->stream>>>(ntot, nrhs, X, W.x32, W.p, W.st);
   MFE_TRY(check_launch(ctx, "k_mr_xupdate"));
   MFE_TRY((launch_spmm_t<double, MM_RESID, float>(ctx, &A64, nrhs, X, nullptr, B, W.r, W.partials,
@@ -1369,9 +1398,12 @@ mfe_status multi_iter_f64(mfe_ctx* ctx, const mfe_csr& A64, int nrhs, double* X,
 
 // Runs `body` (which launches one iteration on ctx->stream) as a CUDA graph
 // with a conditional while node driven by the state's `cont`, or, with
-// MFE_CG_EAGER set, as a host loop reading `cont` back each iteration.
-template <typename Body>
-mfe_status run_loop(mfe_ctx* ctx, MultiState* dev_st, MultiState* host_st, Body body)
+// MFE_CG_EAGER set, as a host loop reading `cont` back each iteration.  With
+// `update`, the body ends with a conditional IF node holding `update`, its
+// condition set by the body (the handle passed as body's second argument).
+template <typename Body, typename Update>
+mfe_status run_loop(mfe_ctx* ctx, MultiState* dev_st, MultiState* host_st, Body body,
+                    Update update, bool with_update)
 {
   if (getenv("MFE_CG_EAGER") != nullptr) {
     for (;;) {
@@ -1379,7 +1411,8 @@ mfe_status run_loop(mfe_ctx* ctx, MultiState* dev_st, MultiState* host_st, Body 
                                         cudaMemcpyDeviceToHost, ctx->stream));
       MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
       if (!host_st->cont) return MFE_OK;
-      MFE_TRY(body((cudaGraphConditionalHandle)0, 0));
+      MFE_TRY(body((cudaGraphConditionalHandle)0, (cudaGraphConditionalHandle)0, 0));
+      if (with_update) MFE_TRY(update((cudaGraphConditionalHandle)0, 0));
     }
   }
   cudaStream_t run_stream = ctx->stream, s = ctx->own_stream;
@@ -1410,13 +1443,53 @@ mfe_status run_loop(mfe_ctx* ctx, MultiState* dev_st, MultiState* host_st, Body 
     if (e == cudaSuccess) e = cudaGraphAddNode(&cnode, g, &nodes[0], nullptr, 1, cp);
     if (e == cudaSuccess) {
       cudaGraph_t body_graph = cp->conditional.phGraph_out[0];
-      e = cudaStreamBeginCaptureToGraph(s, body_graph, nullptr, nullptr, 0,
-                                        cudaStreamCaptureModeRelaxed);
+      cudaGraphConditionalHandle hu = 0;
+      if (with_update) e = cudaGraphConditionalHandleCreate(&hu, body_graph, 0, 0);
+      if (e == cudaSuccess)
+        e = cudaStreamBeginCaptureToGraph(s, body_graph, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeRelaxed);
+      cudaGraphNode_t leaf[4];
+      size_t nleaf = 0;
       if (e == cudaSuccess) {
-        st = body(h, 1);
+        st = body(h, hu, 1);
+        cudaError_t e1 = cudaSuccess;
+        if (with_update) {
+          cudaStreamCaptureStatus cs;
+          const cudaGraphNode_t* deps = nullptr;
+          size_t nd = 0;
+          e1 = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+          if (e1 == cudaSuccess && nd >= 1 && nd <= 4) {
+            for (size_t i = 0; i < nd; ++i) leaf[i] = deps[i];
+            nleaf = nd;
+          } else if (e1 == cudaSuccess) {
+            e1 = cudaErrorUnknown;
+          }
+        }
         cudaGraph_t tmp;
         const cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+        if (e == cudaSuccess) e = e1;
         if (e == cudaSuccess) e = e2;
+      }
+      if (with_update && e == cudaSuccess && st == MFE_OK) {
+        alignas(cudaGraphNodeParams) unsigned char up_buf[sizeof(cudaGraphNodeParams)];
+        memset(up_buf, 0, sizeof(up_buf));
+        cudaGraphNodeParams* up = reinterpret_cast<cudaGraphNodeParams*>(up_buf);
+        up->type = cudaGraphNodeTypeConditional;
+        up->conditional.handle = hu;
+        up->conditional.type = cudaGraphCondTypeIf;
+        up->conditional.size = 1;
+        cudaGraphNode_t unode;
+        e = cudaGraphAddNode(&unode, body_graph, leaf, nullptr, nleaf, up);
+        if (e == cudaSuccess) {
+          e = cudaStreamBeginCaptureToGraph(s, up->conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                            cudaStreamCaptureModeRelaxed);
+          if (e == cudaSuccess) {
+            st = update(h, 1);
+            cudaGraph_t tmp;
+            const cudaError_t e2 = cudaStreamEndCapture(s, &tmp);
+            if (e == cudaSuccess) e = e2;
+          }
+        }
       }
     }
     ctx->stream = run_stream;
@@ -1597,15 +1670,24 @@ mfe_status cg_multi(mfe_ctx* ctx, const mfe_csr* A64_in, int nrhs, const double*
       W.st32_grid = st32_grid;
       W.st32_zc = st32_zc;
     }
-    MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
-      return multi_iter_mixed(ctx, A32, A64, nrhs, B, X, W, h, in_graph);
-    }));
+    MFE_TRY(run_loop(
+        ctx, dst, hs,
+        [&](cudaGraphConditionalHandle h, cudaGraphConditionalHandle hu, int in_graph) {
+          return multi_iter_mixed(ctx, A32, A64, nrhs, W, h, hu, in_graph);
+        },
+        [&](cudaGraphConditionalHandle h, int in_graph) {
+          return multi_update_mixed(ctx, A64, nrhs, B, X, W, h, in_graph);
+        },
+        true));
   } else {
     MultiBufs<double> W{static_cast<double*>(r), static_cast<double*>(p),
                         static_cast<double*>(Ap), nullptr, dst, partials, tickets, err};
-    MFE_TRY(run_loop(ctx, dst, hs, [&](cudaGraphConditionalHandle h, int in_graph) {
-      return multi_iter_f64(ctx, A64, nrhs, X, W, h, in_graph);
-    }));
+    MFE_TRY(run_loop(
+        ctx, dst, hs,
+        [&](cudaGraphConditionalHandle h, cudaGraphConditionalHandle, int in_graph) {
+          return multi_iter_f64(ctx, A64, nrhs, X, W, h, in_graph);
+        },
+        [&](cudaGraphConditionalHandle, int) { return MFE_OK; }, false));
   }
   unsigned* herr = reinterpret_cast<unsigned*>(reinterpret_cast<unsigned char*>(hs) + sizeof(MultiState));
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, dst, sizeof(MultiState), cudaMemcpyDeviceToHost, ctx->stream));
