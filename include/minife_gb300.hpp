@@ -12,12 +12,18 @@
 //   dot, waxpby, fused_waxpby  ref/src/Vector_functions.hpp:127-226
 //   impose_dirichlet     ref/src/SparseMatrix_functions.hpp:434-480
 //   cg_solve             ref/src/cg_solve.hpp:69-229
+//   Box, simple_mesh_description (bc_rows_0 / bc_rows_1)
+//                        ref/utils/Box.hpp, ref/src/simple_mesh_description.hpp:39-224
+//   generate_matrix_structure  ref/src/generate_matrix_structure.hpp:47-149
+//   assemble_FE_data, perform_element_loop
+//                        ref/src/assemble_FE_data.hpp:38-73, perform_element_loop.hpp:40-104
 //
 // The containers stay in host std::vectors like the reference's; each call
 // copies its operands to the device, runs the library's CUDA kernels and
 // copies results back (cg_solve does this once for the whole solve).  Only
 // Scalar = double, LocalOrdinal = GlobalOrdinal = int -- the reference's
-// default build (ref/src/Makefile:3-6) -- is supported.
+// default build (ref/src/Makefile:3-6) -- is supported, on one rank (the
+// local box is the global box).
 #pragma once
 
 #include <cmath>
@@ -79,7 +85,7 @@ class Context {
     mfe_status s = mfe_ctx_create(0, &ctx_);
     if (s != MFE_OK) throw Error(s, "mfe_ctx_create(0)");
   }
-  static constexpr int kSlots = 8;
+  static constexpr int kSlots = 12;
   mfe_ctx* ctx_ = nullptr;
   void* ptr_[kSlots] = {};
   size_t cap_[kSlots] = {};
@@ -138,7 +144,8 @@ struct Vector {
 };
 
 namespace detail {
-enum { SLOT_RO = 0, SLOT_COLS, SLOT_VALS, SLOT_X, SLOT_Y, SLOT_W, SLOT_ROWS };
+enum { SLOT_RO = 0, SLOT_COLS, SLOT_VALS, SLOT_X, SLOT_Y, SLOT_W, SLOT_ROWS, SLOT_X2, SLOT_Y2,
+       SLOT_W2 };
 
 inline void h2d(void* d, const void* h, size_t bytes)
 {
@@ -238,13 +245,27 @@ void waxpby(double alpha, const VectorType& x, double beta, const VectorType& y,
   detail::d2h(w.coefs.data(), dw, 8 * n);
 }
 
+// fused_waxpby (Vector_functions.hpp:154-185): both updates in one pass
 template <typename VectorType>
 void fused_waxpby(double alpha, const VectorType& x, double beta, const VectorType& y,
                   VectorType& w, double alpha2, const VectorType& x2, double beta2,
                   const VectorType& y2, VectorType& w2)
 {
-  waxpby(alpha, x, beta, y, w);
-  waxpby(alpha2, x2, beta2, y2, w2);
+  Context& c = Context::get();
+  const size_t n = x.coefs.size();
+  double* d[6];
+  const int slots[6] = {detail::SLOT_X, detail::SLOT_Y, detail::SLOT_W,
+                        detail::SLOT_X2, detail::SLOT_Y2, detail::SLOT_W2};
+  for (int i = 0; i < 6; ++i) d[i] = static_cast<double*>(c.buf(slots[i], 8 * n + 16));
+  detail::h2d(d[0], x.coefs.data(), 8 * n);
+  detail::h2d(d[1], y.coefs.data(), 8 * n);
+  detail::h2d(d[3], x2.coefs.data(), 8 * n);
+  detail::h2d(d[4], y2.coefs.data(), 8 * n);
+  c.check(mfe_fused_waxpby(c.h(), (int64_t)n, alpha, d[0], beta, d[1], d[2], alpha2, d[3], beta2,
+                           d[4], d[5]),
+          "mfe_fused_waxpby");
+  detail::d2h(w.coefs.data(), d[2], 8 * n);
+  detail::d2h(w2.coefs.data(), d[5], 8 * n);
 }
 
 // impose_dirichlet (SparseMatrix_functions.hpp:434-480)
@@ -264,6 +285,135 @@ void impose_dirichlet(double prescribed_value, MatrixType& A, VectorType& b, int
           "mfe_impose_dirichlet");
   detail::d2h(A.packed_coefs.data(), m.vals, 8 * A.packed_coefs.size());
   detail::d2h(b.coefs.data(), db, 8 * n);
+}
+
+// ---- the assembly side, one rank ----
+
+// Box (ref/utils/Box.hpp): three [lo, hi) element ranges, box[d][0..1]
+struct Box {
+  int ranges[6];
+  int* operator[](int xyz) { return &ranges[xyz * 2]; }
+  const int* operator[](int xyz) const { return &ranges[xyz * 2]; }
+};
+
+// simple_mesh_description (simple_mesh_description.hpp:39-224) for one rank:
+// the global box and the two Dirichlet row sets -- bc_rows_0 (faces x = 0,
+// y = 0, z = 0, y = 1, z = 1) and bc_rows_1 (face x = 1) -- from the
+// library (mfe_box_bc_rows).  The local box must be the global box.
+template <typename GlobalOrdinal>
+class simple_mesh_description {
+ public:
+  simple_mesh_description(const Box& global_box_in, const Box& local_box_in)
+      : global_box(global_box_in), local_box(local_box_in)
+  {
+    for (int d = 0; d < 3; ++d)
+      if (global_box[d][0] != 0 || local_box[d][0] != global_box[d][0] ||
+          local_box[d][1] != global_box[d][1] || global_box[d][1] < 1)
+        throw Error(MFE_NOT_SUPPORTED, "simple_mesh_description: one rank, boxes from 0");
+    Context& c = Context::get();
+    const int nx = global_box[0][1], ny = global_box[1][1], nz = global_box[2][1];
+    for (int which = 0; which < 2; ++which) {
+      int64_t cnt = 0;
+      c.check(mfe_box_bc_rows(c.h(), nx, ny, nz, which, nullptr, &cnt), "mfe_box_bc_rows");
+      std::vector<int32_t> rows((size_t)cnt);
+      if (cnt > 0) {
+        int32_t* dr = static_cast<int32_t*>(c.buf(detail::SLOT_ROWS, 4 * (size_t)cnt + 16));
+        c.check(mfe_box_bc_rows(c.h(), nx, ny, nz, which, dr, &cnt), "mfe_box_bc_rows");
+        detail::d2h(rows.data(), dr, 4 * (size_t)cnt);
+      }
+      std::set<GlobalOrdinal>& dst = which == 0 ? bc_rows_0 : bc_rows_1;
+      dst.insert(rows.begin(), rows.end());
+    }
+  }
+  Box global_box;
+  Box local_box;
+  std::set<GlobalOrdinal> bc_rows_0;
+  std::set<GlobalOrdinal> bc_rows_1;
+};
+
+namespace detail {
+// the device CSR of the mesh's box in the shim's buffers (structure only,
+// or with the element loop's values and b)
+inline mfe_csr box_csr(int nx, int ny, int nz)
+{
+  Context& c = Context::get();
+  int64_t n = 0, nnz = 0;
+  c.check(mfe_box_dims(nx, ny, nz, &n, &nnz), "mfe_box_dims");
+  mfe_csr m;
+  std::memset(&m, 0, sizeof(m));
+  m.nrows = n;
+  m.ncols = n;
+  m.nnz = nnz;
+  m.dtype = MFE_F64;
+  m.row_offsets = static_cast<int32_t*>(c.buf(SLOT_RO, 4 * (size_t)(n + 1)));
+  m.cols = static_cast<int32_t*>(c.buf(SLOT_COLS, 4 * (size_t)(nnz + 4)));
+  m.vals = c.buf(SLOT_VALS, 8 * (size_t)(nnz + 4));
+  return m;
+}
+
+template <typename M>
+void download(const mfe_csr& m, M& A, bool structure)
+{
+  if (structure) {
+    A.rows.resize((size_t)m.nrows);
+    for (int64_t i = 0; i < m.nrows; ++i) A.rows[(size_t)i] = (int)i;
+    A.row_offsets.resize((size_t)m.nrows + 1);
+    A.packed_cols.resize((size_t)m.nnz);
+    d2h(A.row_offsets.data(), m.row_offsets, 4 * (size_t)(m.nrows + 1));
+    d2h(A.packed_cols.data(), m.cols, 4 * (size_t)m.nnz);
+    A.has_local_indices = true;
+    A.num_cols = (int)m.nrows;
+  }
+  A.packed_coefs.resize((size_t)m.nnz);
+  d2h(A.packed_coefs.data(), m.vals, 8 * (size_t)m.nnz);
+}
+}  // namespace detail
+
+// generate_matrix_structure (generate_matrix_structure.hpp:47-149,
+// MatrixInitOp.hpp:127-156): rows, row offsets and ascending 27-point
+// columns of the mesh's box, coefficients zero.  Returns 0.
+template <typename GlobalOrdinal, typename MatrixType>
+int generate_matrix_structure(const simple_mesh_description<GlobalOrdinal>& mesh, MatrixType& A)
+{
+  Context& c = Context::get();
+  const int nx = mesh.global_box[0][1], ny = mesh.global_box[1][1], nz = mesh.global_box[2][1];
+  mfe_csr m = detail::box_csr(nx, ny, nz);
+  c.check(mfe_generate_structure(c.h(), nx, ny, nz, &m), "mfe_generate_structure");
+  detail::download(m, A, true);
+  return 0;
+}
+
+// perform_element_loop (perform_element_loop.hpp:40-104) over the whole
+// box: every element's diffusion matrix and source vector summed into A
+// (whose structure generate_matrix_structure made) and b, in element
+// order; params is accepted for signature compatibility.
+template <typename GlobalOrdinal, typename MatrixType, typename VectorType, typename Params>
+void perform_element_loop(const simple_mesh_description<GlobalOrdinal>& mesh, const Box& box,
+                          MatrixType& A, VectorType& b, Params& /*params*/)
+{
+  for (int d = 0; d < 3; ++d)
+    if (box[d][0] != mesh.local_box[d][0] || box[d][1] != mesh.local_box[d][1])
+      throw Error(MFE_NOT_SUPPORTED, "perform_element_loop: the element box is the local box");
+  Context& c = Context::get();
+  const int nx = mesh.global_box[0][1], ny = mesh.global_box[1][1], nz = mesh.global_box[2][1];
+  mfe_csr m = detail::box_csr(nx, ny, nz);
+  if (A.row_offsets.size() != (size_t)m.nrows + 1 || A.packed_cols.size() != (size_t)m.nnz)
+    throw Error(MFE_BAD_ARG, "perform_element_loop: A lacks the box's structure");
+  double* db = static_cast<double*>(c.buf(detail::SLOT_X, 8 * (size_t)m.nrows + 16));
+  c.check(mfe_assemble(c.h(), nx, ny, nz, nullptr, &m, db, 0), "mfe_assemble");
+  detail::download(m, A, false);
+  b.coefs.resize((size_t)m.nrows);
+  detail::d2h(b.coefs.data(), db, 8 * (size_t)m.nrows);
+}
+
+// assemble_FE_data (assemble_FE_data.hpp:38-73): the element loop over the
+// local box; the Dirichlet conditions follow with impose_dirichlet, as in
+// the reference's driver (driver.hpp:214-218)
+template <typename GlobalOrdinal, typename MatrixType, typename VectorType, typename Params>
+void assemble_FE_data(const simple_mesh_description<GlobalOrdinal>& mesh, MatrixType& A,
+                      VectorType& b, Params& params)
+{
+  perform_element_loop(mesh, mesh.local_box, A, b, params);
 }
 
 // cg_solve (cg_solve.hpp:69-229).  The Matvec argument is accepted for

@@ -122,6 +122,16 @@ def test_cpp_shim_matches_oracle(tmp_path):
     for a in vals:  # same summation order as the shim program
         s += a
     assert v["vals_sum"] == s
+    # the mesh's Dirichlet sets (faces x=0, y=0, z=0, y=1, z=1; face x=1)
+    Nx, Ny, Nz = 11, 10, 9
+    n0 = sum(1 for iz in range(Nz) for iy in range(Ny) for ix in range(Nx)
+             if ix == 0 or iy == 0 or iz == 0 or iy == Ny - 1 or iz == Nz - 1)
+    assert int(v["bc_rows_0"]) == n0 and int(v["bc_rows_1"]) == Ny * Nz
+    xw = 1.0 / (1.0 + np.arange(ro.size - 1))
+    yw = O.matvec(ro, cols, vals, xw)
+    assert v["fused_waxpby_diff"] == 0.0
+    w2 = 1.5 * yw + 0.25 * xw
+    assert abs(v["fused_waxpby_sum2"] - w2 @ w2) <= 1e-12 * (w2 @ w2)
     x = 1.0 / (1.0 + np.arange(ro.size - 1))
     y = O.matvec(ro, cols, vals, x)
     assert abs(v["matvec_dot"] - O.dot(x, y)) <= 1e-13 * abs(O.dot(np.abs(x), np.abs(y)))
