@@ -220,21 +220,7 @@ mfe_status mfe_synchronize(mfe_ctx* ctx)
   if (!ctx) return MFE_BAD_ARG;
   MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   // error word of the standalone SpMV/SpMM launches since the last call
-  auto it = ctx->ws.find("spmv.err");
-  if (it != ctx->ws.end() && it->second.ptr) {
-    unsigned h = 0;
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&h, it->second.ptr, sizeof(unsigned),
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (h) {
-      MFE_CUDA_TRY(ctx, cudaMemsetAsync(it->second.ptr, 0, sizeof(unsigned), ctx->stream));
-      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      return fail(ctx, MFE_TIMEOUT,
-                  (h & 1u) ? "a matrix-vector kernel gave up a bounded wait"
-                           : "a matrix-vector kernel met a tile larger than its stage");
-    }
-  }
-  return MFE_OK;
+  return take_spmv_error(ctx);
 }
 
 const char* mfe_last_error_string(const mfe_ctx* ctx)
@@ -275,21 +261,7 @@ mfe_status mfe_memcpy_d2h(mfe_ctx* ctx, void* dst, const void* src, size_t bytes
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   // error word of the standalone SpMV/SpMM launches since the last call
-  auto it = ctx->ws.find("spmv.err");
-  if (it != ctx->ws.end() && it->second.ptr) {
-    unsigned h = 0;
-    MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&h, it->second.ptr, sizeof(unsigned),
-                                      cudaMemcpyDeviceToHost, ctx->stream));
-    MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    if (h) {
-      MFE_CUDA_TRY(ctx, cudaMemsetAsync(it->second.ptr, 0, sizeof(unsigned), ctx->stream));
-      MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-      return fail(ctx, MFE_TIMEOUT,
-                  (h & 1u) ? "a matrix-vector kernel gave up a bounded wait"
-                           : "a matrix-vector kernel met a tile larger than its stage");
-    }
-  }
-  return MFE_OK;
+  return take_spmv_error(ctx);
 }
 
 mfe_status mfe_csr_alloc(mfe_ctx* ctx, int64_t nrows, int64_t nnz, mfe_dtype dtype, mfe_csr* out)

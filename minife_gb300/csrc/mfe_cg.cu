@@ -671,6 +671,8 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
       MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hn, rb.scalars + 4, sizeof(double), cudaMemcpyDeviceToHost,
                                         ctx->stream));
       MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+      // this product reports its bounded waits in the context's SpMV word
+      MFE_TRY(take_spmv_error(ctx));
     }
     const double rr = hn[0];
     true_resid = std::sqrt(std::max(rr, 0.0));

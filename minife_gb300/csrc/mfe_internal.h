@@ -52,6 +52,10 @@ mfe_status cuda_fail(mfe_ctx* ctx, cudaError_t e, const char* where);
 // Check the last launch; returns MFE_OK or MFE_CUDA_ERR.
 mfe_status check_launch(mfe_ctx* ctx, const char* where);
 
+// Read and clear the error word of the SpMV/SpMM launches that carry no
+// solver state (ERR_WAIT_TIMEOUT / ERR_TILE_OVERFLOW): MFE_TIMEOUT if set.
+mfe_status take_spmv_error(mfe_ctx* ctx);
+
 // Named workspace buffer of at least `bytes` (contents undefined when grown).
 void* workspace(mfe_ctx* ctx, const char* name, size_t bytes);
 // Pinned host scratch of at least `bytes`.

@@ -334,6 +334,8 @@ mfe_status cg_jacobi(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
   release();
   MFE_CUDA_TRY(ctx, cudaMemcpyAsync(hs, st, sizeof(PcgState), cudaMemcpyDeviceToHost, ctx->stream));
   MFE_CUDA_TRY(ctx, cudaEventRecord(ctx->ev1, ctx->stream));
+  // the PCG's products report their bounded waits in the context's SpMV word
+  MFE_TRY(take_spmv_error(ctx));
   MFE_CUDA_TRY(ctx, cudaEventSynchronize(ctx->ev1));
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);

@@ -527,4 +527,20 @@ mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, 
   return check_launch(ctx, "k_spmm");
 }
 
+mfe_status take_spmv_error(mfe_ctx* ctx)
+{
+  auto it = ctx->ws.find("spmv.err");
+  if (it == ctx->ws.end() || !it->second.ptr) return MFE_OK;
+  unsigned h = 0;
+  MFE_CUDA_TRY(ctx, cudaMemcpyAsync(&h, it->second.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost,
+                                    ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  if (!h) return MFE_OK;
+  MFE_CUDA_TRY(ctx, cudaMemsetAsync(it->second.ptr, 0, sizeof(unsigned), ctx->stream));
+  MFE_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return fail(ctx, MFE_TIMEOUT,
+              (h & 1u) ? "a matrix-vector kernel gave up a bounded wait"
+                       : "a matrix-vector kernel met a tile larger than its stage");
+}
+
 }  // namespace mfe

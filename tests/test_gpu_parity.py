@@ -491,6 +491,25 @@ def test_bounded_wait_timeout_reports_and_recovers():
         res = M.cg_solve(A, b, x, max_iter=500, tol=1e-10, tol_mode="relative", f64_operator=op)
         assert res.status == 0 and abs(res.num_iters - it) <= 1
         assert np.linalg.norm(host(x) - xo) <= 1e-9 * np.linalg.norm(xo)
+    # the host drop-in call's speculative start (the final residual with the
+    # CSR values is its first box product) and the Jacobi PCG (its products
+    # report through the context's SpMV word)
+    xh = np.zeros(ro.size - 1)
+    M.inject_wait_timeout(20_000_000)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.cg_solve_host(ro, cols, vals, bo, xh, max_iter=500, tol=1e-10, tol_mode="relative")
+    assert ei.value.status == 6
+    xh = np.zeros(ro.size - 1)
+    res = M.cg_solve_host(ro, cols, vals, bo, xh, max_iter=500, tol=1e-10, tol_mode="relative")
+    assert res.status == 0 and np.linalg.norm(xh - xo) <= 1e-9 * np.linalg.norm(xo)
+    x = torch.zeros_like(b)
+    M.inject_wait_timeout(20_000_000)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.cg_solve(A, b, x, max_iter=5, tol=1e-10, tol_mode="relative", precond="jacobi")
+    assert ei.value.status == 6
+    x.zero_()
+    res = M.cg_solve(A, b, x, max_iter=500, tol=1e-10, tol_mode="relative", precond="jacobi")
+    assert res.status == 0 and np.linalg.norm(host(x) - xo) <= 1e-8 * np.linalg.norm(xo)
     xr = torch.randn(A.nrows, dtype=torch.float64, device=DEV)
     y = torch.empty_like(xr)
     M.inject_wait_timeout(20_000_000)
