@@ -523,6 +523,8 @@ mfe_status cg_mixed(mfe_ctx* ctx, const mfe_csr* A64_in, const double* b, double
   float ms = 0.f;
   cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
   if (hs->err) return fail(ctx, MFE_TIMEOUT, "a bounded device wait gave up during mixed CG");
+  // the FP64 residual products report their bounded waits in the context's word
+  MFE_TRY(take_spmv_error(ctx));
   res->num_iters = hs->k;
   res->normr = hs->normr_true;
   res->normr0 = hs->normr0;

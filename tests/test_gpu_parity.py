@@ -510,6 +510,15 @@ def test_bounded_wait_timeout_reports_and_recovers():
     x.zero_()
     res = M.cg_solve(A, b, x, max_iter=500, tol=1e-10, tol_mode="relative", precond="jacobi")
     assert res.status == 0 and np.linalg.norm(host(x) - xo) <= 1e-8 * np.linalg.norm(xo)
+    # the mixed solver (its FP64 residual products)
+    x = torch.zeros_like(b)
+    M.inject_wait_timeout(20_000_000)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.cg_solve(A, b, x, max_iter=5, tol=1e-10, tol_mode="relative", precision="mixed")
+    assert ei.value.status == 6
+    x.zero_()
+    res = M.cg_solve(A, b, x, max_iter=2000, tol=1e-10, tol_mode="relative", precision="mixed")
+    assert res.status == 0 and np.linalg.norm(host(x) - xo) <= 1e-8 * np.linalg.norm(xo)
     xr = torch.randn(A.nrows, dtype=torch.float64, device=DEV)
     y = torch.empty_like(xr)
     M.inject_wait_timeout(20_000_000)
