@@ -32,7 +32,8 @@ The per-rank arithmetic comes from an operations object -- prepare(A)
 (which sets ``xext``, the owned entries followed by the externals),
 empty(n), copy_owned(v, xext), matvec(xext, out), dot(u, v), waxpby(a, u,
 b, v, w) (w = a u + b v), pack(xext, i) (neighbour i's send buffer, on the
-host) and put(xext, off, values): ``DeviceOps`` runs it on the rank's GPU
+host), put(xext, off, values) and, optionally, finish() (raises if the
+device reported an error during the solve): ``DeviceOps`` runs it on the rank's GPU
 with the library's kernels (generic CSR matvec, dot, waxpby, gather),
 staging the halo through host memory for the transport; tests run the
 same logic on CPU ranks (gloo) with operations of their own.
@@ -379,6 +380,9 @@ def cg_solve(A: LocalMatrix, b, x, ops, comm, max_iter: int = 200,
         ops.waxpby(1.0, r, -alpha, Ap, r)
         num_iters = k
         k += 1
+    finish = getattr(ops, "finish", None)
+    if finish is not None:
+        finish()
     return num_iters, normr, normr0
 
 
@@ -392,6 +396,11 @@ class DeviceOps:
         import torch
         self.torch = torch
         self.dev = torch.device("cuda", device)
+
+    def finish(self):
+        """The context's error word of the solve's products (bounded waits):
+        MiniFEError (MFE_TIMEOUT) if one gave up."""
+        self.M.default_context().synchronize()
 
     def prepare(self, A: LocalMatrix):
         import minife_gb300 as M
