@@ -1024,9 +1024,7 @@ mfe_status mfe_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y)
   if (E->nrows > 0 && (!x || !y)) return fail(ctx, MFE_BAD_ARG, "null vector");
   MFE_TRY(set_device(ctx));
   if (E->nrows == 0) return MFE_OK;
-  mfe_csr V;
-  MFE_TRY(ell_view(ctx, E, &V));
-  return launch_spmv(ctx, &V, x, y, nullptr, nullptr, nullptr);
+  return launch_spmv_ell(ctx, E, x, y, nullptr, nullptr, nullptr);
 }
 
 mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, double* x,
@@ -1054,7 +1052,7 @@ mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, dou
   if (!S.cols || !S.vals) return fail(ctx, MFE_OOM, "sliced ELL workspace allocation failed");
   MFE_TRY(launch_ell_to_sell(ctx, E, &S));
   memset(result, 0, sizeof(*result));
-  const mfe_status st = cg_solve_sell(ctx, &V, &S, b, x, &o, result);
+  const mfe_status st = cg_solve_sell(ctx, &V, &S, b, x, &o, result, E);
   result->status = st;
   return st;
 }

@@ -475,7 +475,7 @@ static mfe_status build_graph(mfe_ctx* ctx, const mfe_csr* A, double* x, const C
 // ---------------------------------------------------------------------------
 static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, double* x,
                          const mfe_cg_opts* o, mfe_cg_result* res, const CgSpec* spec,
-                         const mfe_sell* sell = nullptr)
+                         const mfe_sell* sell = nullptr, const mfe_ell* ell = nullptr)
 {
   const int64_t n = A_in->nrows;
   mfe_csr A = *A_in;
@@ -538,7 +538,8 @@ static mfe_status cg_f64(mfe_ctx* ctx, const mfe_csr* A_in, const double* b, dou
     sink.partials = rb.partials;
     sink.ticket = rb.tickets;
     sink.out = rb.scalars;
-    MFE_TRY(launch_spmv(ctx, &A, x, B.r, &sink, b, B.st));
+    if (ell) MFE_TRY(launch_spmv_ell(ctx, ell, x, B.r, &sink, b, B.st));
+    else MFE_TRY(launch_spmv(ctx, &A, x, B.r, &sink, b, B.st));
     csr_products = 1;
   }
   // A CSR that is not a box matrix: the iterations' products run on a
@@ -727,11 +728,11 @@ mfe_status cg_solve_impl(mfe_ctx* ctx, const mfe_csr* A, const double* b, double
 }
 
 mfe_status cg_solve_sell(mfe_ctx* ctx, const mfe_csr* V, const mfe_sell* S, const double* b,
-                         double* x, const mfe_cg_opts* opts, mfe_cg_result* res)
+                         double* x, const mfe_cg_opts* opts, mfe_cg_result* res, const mfe_ell* E)
 {
   if (opts->precond != 0 || opts->precision != MFE_PREC_F64)
     return fail(ctx, MFE_BAD_ARG, "the sliced ELL CG is FP64 without preconditioner");
-  return cg_f64(ctx, V, b, x, opts, res, nullptr, S);
+  return cg_f64(ctx, V, b, x, opts, res, nullptr, S, E);
 }
 
 mfe_status cg_solve_spec(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,

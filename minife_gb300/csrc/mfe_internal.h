@@ -94,6 +94,11 @@ mfe_status ensure_max_row_len(mfe_ctx* ctx, const mfe_csr* A, int* max_len);
 mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
                        const DotSink* sink, const double* resid_b, void* cg_state);
 mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y);
+// y = E x or r = b - E x with r.r for the row-major ELL matrix (rows of up
+// to 64 entries and 16-byte aligned arrays on the warp-staged kernel; other
+// matrices, and products with x.y, through its CSR view)
+mfe_status launch_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y,
+                           const DotSink* sink, const double* resid_b, void* cg_state);
 
 // ---- box-structured SpMV (mfe_spmv_box.cu) ----
 // True when A carries box dimensions consistent with its sizes (the caller
@@ -266,9 +271,11 @@ constexpr mfe_status kSpecFailed = (mfe_status)1000;
 mfe_status cg_solve_spec(mfe_ctx* ctx, const mfe_csr* A, const double* b, double* x,
                          const mfe_cg_opts* opts, mfe_cg_result* res, const CgSpec* spec);
 // FP64 CG (no preconditioner) whose iterations' products run on the sliced
-// ELL copy S of the matrix V (an ELL view); the residuals use V
+// ELL copy S of the matrix V (an ELL view); the initial residual uses the
+// row-major ELL E itself when given, else V
 mfe_status cg_solve_sell(mfe_ctx* ctx, const mfe_csr* V, const mfe_sell* S, const double* b,
-                         double* x, const mfe_cg_opts* opts, mfe_cg_result* res);
+                         double* x, const mfe_cg_opts* opts, mfe_cg_result* res,
+                         const mfe_ell* E = nullptr);
 void cg_graph_destroy(mfe_cg_graph* g);
 
 }  // namespace mfe

@@ -22,6 +22,7 @@
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
+#include <cstring>
 
 #include "mfe_cgstate.cuh"
 #include "mfe_common.cuh"
@@ -263,6 +264,242 @@ __global__ void __launch_bounds__(ROWS) k_spmv_tiled(SpmvParams<T> P)
   }
 }
 
+// Warp-staged products: a warp per group of 32 rows, whose nonzeros are
+// contiguous in both layouts below (CSR: ro[32g] .. ro[32g+32]; the
+// reference's ELLMatrix: 32 g K .. 32 (g+1) K, short rows padded).  Lane 0
+// stages a group's values and columns with two 1-D bulk copies (TMA) into the
+// warp's own ring of kStgStages shared-memory stages, each with its mbarrier
+// (no block barrier in the loop), and every lane sums its own row from shared
+// memory with row_dot.  With rows of 27 entries an FP64 stage is 10.5 KB and
+// ten warps per SM each keep their next group in flight, where the tiled
+// kernel's 128-row tiles hold two blocks per SM behind block barriers: the
+// 256^3 FP64 product takes 1.42 ms against 2.09 ms through the tiled kernel
+// (FP32 rows, half the bytes per stage, stay on the tiled kernel: 0.715
+// against 0.75-0.80 ms).
+constexpr int kStgWarps = 2;    // warps per block
+constexpr int kStgStages = 2;   // stages per warp
+constexpr int kStgMaxLen = 32;  // longer rows: the warp-per-row kernel
+
+// Stage capacity (elements) for a group of 32 rows of at most max_len
+// entries: ELL groups start aligned and hold exactly 32 K; CSR groups carry
+// up to 3 elements of alignment slack at each end.  A multiple of 4, so the
+// column part of a stage starts 16-byte aligned.
+__host__ __device__ constexpr int stg_cap(int max_len, bool ell)
+{
+  return ell ? 32 * max_len : ((32 * max_len + 8) + 3) & ~3;
+}
+
+// CSR rows of at most max_len entries.  A stage starts on the 16-byte
+// boundaries at or below its group's first nonzero, and the ragged end of
+// the arrays arrives by plain loads, as in the tiled kernel.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kStgWarps * 32) k_spmv_staged(SpmvParams<T> P, int max_len)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar[kStgWarps][kStgStages];
+  __shared__ double red[32];
+  constexpr int VA = 16 / sizeof(T);  // values per 16 bytes
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const int cap = stg_cap(max_len, false);
+  const size_t vbytes = (size_t)cap * sizeof(T);
+  const size_t sbytes = vbytes + (size_t)cap * sizeof(int32_t);
+  unsigned char* wbase = smem + (size_t)w * kStgStages * sbytes;
+  const int64_t ngroups = (P.n + 31) / 32;
+  const int64_t nw = (int64_t)gridDim.x * kStgWarps;
+  const int64_t g0 = (int64_t)blockIdx.x * kStgWarps + w;
+  if (lane == 0) {
+    for (int s = 0; s < kStgStages; ++s) mbar_init(&bar[w][s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // lane 0: nonzeros [a, e) of one group into stage s
+  auto issue = [&](int64_t a, int64_t e, int s) {
+    const int64_t av = a & ~(int64_t)(VA - 1);
+    const int64_t ac = a & ~(int64_t)3;
+    int64_t bv = min((e + VA - 1) & ~(int64_t)(VA - 1), P.nnz & ~(int64_t)(VA - 1));
+    int64_t bc = min((e + 3) & ~(int64_t)3, P.nnz & ~(int64_t)3);
+    if (bv < av) bv = av;
+    if (bc < ac) bc = ac;
+    if (max(bv, e) - av > cap || max(bc, e) - ac > cap) {
+      // cannot happen when every row has <= the max_len the host passed;
+      // record it and stage nothing
+      atomicOr(P.err, ERR_TILE_OVERFLOW);
+      mbar_arrive_expect_tx(&bar[w][s], 0);
+      return;
+    }
+    T* dv = reinterpret_cast<T*>(wbase + (size_t)s * sbytes);
+    int32_t* dc = reinterpret_cast<int32_t*>(wbase + (size_t)s * sbytes + vbytes);
+    // ragged tail past the last 16-byte boundary of the arrays: plain loads
+    for (int64_t k = bv; k < e; ++k) dv[k - av] = P.vals[k];
+    for (int64_t k = bc; k < e; ++k) dc[k - ac] = P.cols[k];
+    fence_proxy_async_smem();
+    const unsigned bytes_v = (unsigned)((bv - av) * sizeof(T));
+    const unsigned bytes_c = (unsigned)((bc - ac) * sizeof(int32_t));
+    mbar_arrive_expect_tx(&bar[w][s], bytes_v + bytes_c);
+    if (bytes_v) bulk_g2s(dv, P.vals + av, bytes_v, &bar[w][s]);
+    if (bytes_c) bulk_g2s(dc, P.cols + ac, bytes_c, &bar[w][s]);
+  };
+
+  if (lane == 0)
+    for (int s = 0; s < kStgStages; ++s) {
+      const int64_t g = g0 + (int64_t)s * nw;
+      if (g < ngroups) issue(__ldg(&P.ro[g * 32]), __ldg(&P.ro[min(P.n, g * 32 + 32)]), s);
+    }
+  double dacc = 0.0;
+  bool ok = true;
+  int it = 0;
+  for (int64_t g = g0; g < ngroups; g += nw, ++it) {
+    const int s = it % kStgStages;
+    const int64_t r = g * 32 + lane;
+    const int64_t gn = g + (int64_t)kStgStages * nw;  // the group stage s takes next
+    // the group's and this lane's row bounds, and lane 0's bounds of the
+    // next group, loaded before the wait so their latency overlaps it (the
+    // next copy then starts as soon as the lanes are done)
+    const int32_t a = __ldg(&P.ro[g * 32]);
+    int32_t ra = 0, rb = 0;
+    if (r < P.n) {
+      ra = __ldg(&P.ro[r]);
+      rb = __ldg(&P.ro[r + 1]);
+    }
+    int64_t na = 0, ne = 0;
+    if (lane == 0 && gn < ngroups) {
+      na = __ldg(&P.ro[gn * 32]);
+      ne = __ldg(&P.ro[min(P.n, gn * 32 + 32)]);
+    }
+    ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[w][s], (unsigned)((it / kStgStages) & 1)));
+    if (!ok) break;
+    if (r < P.n) {
+      const T* rv = reinterpret_cast<const T*>(wbase + (size_t)s * sbytes) + (ra - (a & ~(VA - 1)));
+      const int32_t* rc =
+          reinterpret_cast<const int32_t*>(wbase + (size_t)s * sbytes + vbytes) + (ra - (a & ~3));
+      const T sum = row_dot<T, 27>(rv, rc, rb - ra, P.x);
+      if (MODE == SPMV_RESID) {
+        const double rr = P.b[r] - (double)sum;
+        P.y[r] = (T)rr;
+        dacc = fma(rr, rr, dacc);
+      } else {
+        P.y[r] = sum;
+        if (MODE == SPMV_DOT) dacc = fma((double)sum, (double)__ldg(&P.x[r]), dacc);
+      }
+    }
+    __syncwarp();  // every lane is done reading stage s
+    if (lane == 0 && gn < ngroups) issue(na, ne, s);
+  }
+  if (!ok) {
+    if (lane == 0) {
+      atomicOr(P.err, ERR_WAIT_TIMEOUT);
+      // drain: give each stage with a copy issued a bounded chance to land
+      // before the block exits
+      for (int j = it; j < it + kStgStages; ++j)
+        if (g0 + (int64_t)j * nw < ngroups)
+          mbar_wait_bounded(&bar[w][j % kStgStages], (unsigned)((j / kStgStages) & 1));
+    }
+    __syncwarp();
+  }
+  // every warp reaches the block reduction, also after a timeout
+  if (MODE != SPMV_PLAIN) {
+    const double bt = block_sum(dacc, red);
+    double total;
+    if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0)
+      spmv_epilogue<MODE>(total, P.cg, P.dot_out);
+  }
+}
+
+// The reference's row-major ELL, K entries per row (K <= kStgMaxLen): group
+// g's entries start at 32 g K, 16-byte aligned in both arrays, and row lane
+// sits at lane K of its stage.  The stage size is computed from K here (not
+// read from the parameter block), which lets the compiler fold each lane's
+// stage addresses and keep a row's loads in flight together: 1.04 ms for the
+// 256^3 product against 1.13 ms with the size read from P.  MODE: plain or
+// the CG's initial residual.
+template <typename T, int MODE>
+__global__ void __launch_bounds__(kStgWarps * 32) k_spmv_ell(SpmvParams<T> P, int K)
+{
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint64_t bar[kStgWarps][kStgStages];
+  __shared__ double red[32];
+  constexpr int VA = 16 / sizeof(T);
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const size_t sbytes = (size_t)32 * K * (sizeof(T) + sizeof(int32_t));
+  const size_t vbytes = (size_t)32 * K * sizeof(T);
+  unsigned char* wbase = smem + (size_t)w * kStgStages * sbytes;
+  const int64_t ngroups = (P.n + 31) / 32;
+  const int64_t nw = (int64_t)gridDim.x * kStgWarps;
+  const int64_t g0 = (int64_t)blockIdx.x * kStgWarps + w;
+  if (lane == 0) {
+    for (int s = 0; s < kStgStages; ++s) mbar_init(&bar[w][s], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+
+  // lane 0: group g into stage s; the ragged end past the last 16-byte
+  // boundary of the matrix (last group only) by plain loads
+  auto issue = [&](int64_t g, int s) {
+    const int64_t a = g * 32 * K;
+    const int64_t e = min(P.n, g * 32 + 32) * K;
+    const int64_t bv = max(a, e & ~(int64_t)(VA - 1));
+    const int64_t bc = max(a, e & ~(int64_t)3);
+    T* dv = reinterpret_cast<T*>(wbase + (size_t)s * sbytes);
+    int32_t* dc = reinterpret_cast<int32_t*>(wbase + (size_t)s * sbytes + vbytes);
+    for (int64_t k = bv; k < e; ++k) dv[k - a] = P.vals[k];
+    for (int64_t k = bc; k < e; ++k) dc[k - a] = P.cols[k];
+    fence_proxy_async_smem();
+    const unsigned bytes_v = (unsigned)((bv - a) * sizeof(T));
+    const unsigned bytes_c = (unsigned)((bc - a) * sizeof(int32_t));
+    mbar_arrive_expect_tx(&bar[w][s], bytes_v + bytes_c);
+    if (bytes_v) bulk_g2s(dv, P.vals + a, bytes_v, &bar[w][s]);
+    if (bytes_c) bulk_g2s(dc, P.cols + a, bytes_c, &bar[w][s]);
+  };
+  if (lane == 0)
+    for (int s = 0; s < kStgStages; ++s) {
+      const int64_t g = g0 + (int64_t)s * nw;
+      if (g < ngroups) issue(g, s);
+    }
+  double dacc = 0.0;
+  bool ok = true;
+  int it = 0;
+  for (int64_t g = g0; g < ngroups; g += nw, ++it) {
+    const int s = it % kStgStages;
+    ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[w][s], (unsigned)((it / kStgStages) & 1)));
+    if (!ok) break;
+    const int64_t r = g * 32 + lane;
+    if (r < P.n) {
+      const T* rv = reinterpret_cast<const T*>(wbase + (size_t)s * sbytes) + (size_t)lane * K;
+      const int32_t* rc =
+          reinterpret_cast<const int32_t*>(wbase + (size_t)s * sbytes + vbytes) + (size_t)lane * K;
+      const T sum = row_dot<T, 27>(rv, rc, K, P.x);
+      if (MODE == SPMV_RESID) {
+        const double rr = P.b[r] - (double)sum;
+        P.y[r] = (T)rr;
+        dacc = fma(rr, rr, dacc);
+      } else {
+        P.y[r] = sum;
+      }
+    }
+    __syncwarp();  // every lane is done reading stage s
+    const int64_t gn = g + (int64_t)kStgStages * nw;
+    if (lane == 0 && gn < ngroups) issue(gn, s);
+  }
+  if (!ok) {
+    if (lane == 0) {
+      atomicOr(P.err, ERR_WAIT_TIMEOUT);
+      for (int j = it; j < it + kStgStages; ++j)
+        if (g0 + (int64_t)j * nw < ngroups)
+          mbar_wait_bounded(&bar[w][j % kStgStages], (unsigned)((j / kStgStages) & 1));
+    }
+    __syncwarp();
+  }
+  if (MODE == SPMV_RESID) {
+    const double bt = block_sum(dacc, red);
+    double total;
+    if (grid_reduce_last(bt, P.partials, P.ticket, red, &total) && threadIdx.x == 0)
+      spmv_epilogue<MODE>(total, P.cg, P.dot_out);
+  }
+}
+
 // Warp-per-row fallback for long rows (shuffle-reduced).
 template <typename T, int MODE>
 __global__ void __launch_bounds__(256) k_spmv_warp(SpmvParams<T> P)
@@ -407,8 +644,50 @@ static int tiled_ctas_per_sm(size_t smem)
   return std::max(1, per_sm);
 }
 
+// ---- warp-staged kernels ----
+template <typename T>
+static size_t staged_smem(int max_len, bool ell)
+{
+  return (size_t)kStgWarps * kStgStages * stg_cap(max_len, ell) * (sizeof(T) + sizeof(int32_t));
+}
+
+template <typename T>
+static int staged_grid(mfe_ctx* ctx, int64_t nrows, int max_len, bool ell)
+{
+  const size_t smem = staged_smem<T>(max_len, ell);
+  const int per_sm = std::max(1, std::min(16, (int)((227 * 1024) / (smem + 1024))));
+  return (int)std::max<int64_t>(1, std::min<int64_t>(ceil_div(ceil_div(nrows, (int64_t)32), (int64_t)kStgWarps),
+                                                     (int64_t)ctx->sm_count * per_sm));
+}
+
+// shared-memory opt-in for the longest rows, once per device and kernel (a
+// function attribute: set before any stream capture launches the kernel)
+static mfe_status staged_configure(mfe_ctx* ctx, const void* kernel, size_t smem, bool* configured)
+{
+  const int dev = ctx->device;
+  if (dev >= 0 && dev < 64 && configured[dev]) return MFE_OK;
+  MFE_CUDA_TRY(ctx, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  if (dev >= 0 && dev < 64) configured[dev] = true;
+  return MFE_OK;
+}
+
+// P filled but for cap; rows of at most max_len <= kStgMaxLen entries
+template <typename T, int MODE>
+static mfe_status launch_staged(mfe_ctx* ctx, SpmvParams<T>& P, int max_len)
+{
+  static bool configured[64] = {};
+  MFE_TRY(staged_configure(ctx, (const void*)k_spmv_staged<T, MODE>,
+                           staged_smem<T>(kStgMaxLen, false), configured));
+  P.cap = stg_cap(max_len, false);
+  k_spmv_staged<T, MODE><<<staged_grid<T>(ctx, P.n, max_len, false), kStgWarps * 32,
+                           staged_smem<T>(max_len, false), ctx->stream>>>(P, max_len);
+  return check_launch(ctx, "k_spmv_staged");
+}
+
 int spmv_grid(mfe_ctx* ctx, const mfe_csr* A)
 {
+  if (A->dtype == MFE_F64 && A->max_row_len > 0 && A->max_row_len <= kStgMaxLen)
+    return staged_grid<double>(ctx, A->nrows, A->max_row_len, false);
   const int rows = tile_rows();
   const int64_t ntiles = ceil_div(A->nrows, rows);
   const int max_len = A->max_row_len > 0 ? A->max_row_len : kMaxTileRowLen;
@@ -461,6 +740,9 @@ static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, con
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
   if (A->nrows == 0) return MFE_OK;
+  if constexpr (sizeof(T) == 8)
+    if (max_len <= kStgMaxLen && aligned16(A->vals) && aligned16(A->cols))
+      return launch_staged<T, MODE>(ctx, P, max_len);
   if (max_len <= kMaxTileRowLen && aligned16(A->vals) && aligned16(A->cols)) {
     MFE_CUDA_TRY(ctx, configure_tiled(ctx->device));
     const size_t smem = tiled_smem<T>(rows, std::max(max_len, 1));
@@ -504,6 +786,63 @@ mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
     if (resid_b) return fail(ctx, MFE_NOT_SUPPORTED, "FP32 residual SpMV is not provided");
     if (sink) return launch_t<float, SPMV_DOT>(ctx, A, xf, yf, sink, nullptr, cg, max_len);
     return launch_t<float, SPMV_PLAIN>(ctx, A, xf, yf, nullptr, nullptr, cg, max_len);
+  }
+  return fail(ctx, MFE_BAD_ARG, "unknown matrix dtype");
+}
+
+template <typename T, int MODE>
+static mfe_status launch_ell_t(mfe_ctx* ctx, const mfe_ell* E, const T* x, T* y, const DotSink* sink,
+                               const double* b, CgState* cg)
+{
+  static bool configured[64] = {};
+  MFE_TRY(staged_configure(ctx, (const void*)k_spmv_ell<T, MODE>, staged_smem<T>(kStgMaxLen, true),
+                           configured));
+  SpmvParams<T> P;
+  memset(&P, 0, sizeof(P));
+  P.n = E->nrows;
+  P.nnz = E->nrows * (int64_t)E->ncols_per_row;
+  P.cols = E->cols;
+  P.vals = static_cast<const T*>(E->vals);
+  P.x = x;
+  P.y = y;
+  P.b = b;
+  P.cap = stg_cap(E->ncols_per_row, true);
+  P.partials = sink ? sink->partials : nullptr;
+  P.ticket = sink ? sink->ticket : nullptr;
+  P.dot_out = sink ? sink->out : nullptr;
+  P.cg = cg;
+  P.err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
+  if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
+  if (cg) P.err = &cg->err;
+  const int K = E->ncols_per_row;
+  k_spmv_ell<T, MODE><<<staged_grid<T>(ctx, P.n, K, true), kStgWarps * 32, staged_smem<T>(K, true),
+                        ctx->stream>>>(P, K);
+  return check_launch(ctx, "k_spmv_ell");
+}
+
+mfe_status launch_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y,
+                           const DotSink* sink, const double* resid_b, void* cg_state)
+{
+  if (E->nrows == 0) return MFE_OK;
+  // products with x.y (no caller on the ELL) also take the CSR view
+  const bool dot_only = sink != nullptr && resid_b == nullptr;
+  if (E->ncols_per_row > kStgMaxLen || !aligned16(E->vals) || !aligned16(E->cols) || dot_only) {
+    mfe_csr V;
+    MFE_TRY(ell_view(ctx, E, &V));
+    return launch_spmv(ctx, &V, x, y, sink, resid_b, cg_state);
+  }
+  CgState* cg = static_cast<CgState*>(cg_state);
+  if (E->dtype == MFE_F64) {
+    const double* xd = static_cast<const double*>(x);
+    double* yd = static_cast<double*>(y);
+    if (resid_b) return launch_ell_t<double, SPMV_RESID>(ctx, E, xd, yd, sink, resid_b, cg);
+    return launch_ell_t<double, SPMV_PLAIN>(ctx, E, xd, yd, nullptr, nullptr, cg);
+  }
+  if (E->dtype == MFE_F32) {
+    const float* xf = static_cast<const float*>(x);
+    float* yf = static_cast<float*>(y);
+    if (resid_b) return fail(ctx, MFE_NOT_SUPPORTED, "FP32 residual SpMV is not provided");
+    return launch_ell_t<float, SPMV_PLAIN>(ctx, E, xf, yf, nullptr, nullptr, cg);
   }
   return fail(ctx, MFE_BAD_ARG, "unknown matrix dtype");
 }

@@ -115,3 +115,58 @@ def test_ell_cg_relative_and_jacobi():
                                   M.ctypes.byref(o), M.ctypes.byref(r))
     assert st == 0
     assert np.linalg.norm(xj.cpu().numpy() - xo) <= 1e-8 * np.linalg.norm(xo)
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("n,K", [(1, 27), (31, 27), (33, 8), (1000, 27), (4099, 27), (4099, 28),
+                                 (777, 1), (2049, 64), (513, 65)])
+def test_ell_matvec_shapes(n, K, dtype):
+    """The row-major ELL product on random rows (columns anywhere, a quarter
+    of the entries padding: column 0, value 0) for partial 32-row groups,
+    odd and even K, K = 64 (the largest on the warp-staged kernel) and 65
+    (through the CSR view), against an FP64 numpy product within the
+    reordering bound of the two partial sums per row."""
+    rng = np.random.default_rng(n * 131 + K)
+    c = rng.integers(0, n, size=(n, K)).astype(np.int32)
+    v = rng.standard_normal((n, K))
+    pad = rng.random((n, K)) < 0.25
+    c[pad] = 0
+    v[pad] = 0.0
+    if dtype == torch.float32:
+        v = v.astype(np.float32).astype(np.float64)
+    x = rng.standard_normal(n)
+    if dtype == torch.float32:
+        x = x.astype(np.float32).astype(np.float64)
+    yo = (v * x[c]).sum(axis=1)
+    u = 2.0 ** -53 if dtype == torch.float64 else 2.0 ** -24
+    bound = (K + 4) * u * (np.abs(v) * np.abs(x[c])).sum(axis=1) + 1e-300
+    E = M.ELLMatrix(torch.from_numpy(c.ravel()).cuda(), torch.from_numpy(v.ravel()).to("cuda", dtype), K)
+    xd = torch.from_numpy(x).to("cuda", dtype)
+    y = torch.full((n,), float("nan"), dtype=dtype, device="cuda")
+    M.matvec_ell(E, xd, y)
+    assert np.all(np.abs(y.cpu().double().numpy() - yo) <= bound)
+
+
+def test_ell_matvec_unaligned_arrays():
+    """Arrays that do not start on a 16-byte boundary take the CSR view and
+    give the same result."""
+    n, K = 1000, 27
+    rng = np.random.default_rng(5)
+    c = rng.integers(0, n, size=n * K).astype(np.int32)
+    v = rng.standard_normal(n * K)
+    x = rng.standard_normal(n)
+    cb = torch.zeros(n * K + 1, dtype=torch.int32, device="cuda")
+    vb = torch.zeros(n * K + 1, dtype=torch.float64, device="cuda")
+    cb[1:] = torch.from_numpy(c).cuda()
+    vb[1:] = torch.from_numpy(v).cuda()
+    E1 = M.ELLMatrix(cb[1:], vb[1:], K)
+    E0 = M.ELLMatrix(torch.from_numpy(c).cuda(), torch.from_numpy(v).cuda(), K)
+    xd = torch.from_numpy(x).cuda()
+    y1 = torch.empty(n, dtype=torch.float64, device="cuda")
+    y0 = torch.empty_like(y1)
+    M.matvec_ell(E1, xd, y1)
+    M.matvec_ell(E0, xd, y0)
+    yo = (v.reshape(n, K) * x[c.reshape(n, K)]).sum(axis=1)
+    bound = (K + 4) * 2.0 ** -53 * (np.abs(v.reshape(n, K)) * np.abs(x[c.reshape(n, K)])).sum(axis=1)
+    assert np.all(np.abs(y1.cpu().numpy() - yo) <= bound)
+    assert np.all(np.abs(y0.cpu().numpy() - yo) <= bound)
