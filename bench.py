@@ -843,7 +843,8 @@ def run_probe(args):
     """Small fixed workloads for profiler captures (ncu): 'spmv' = the box
     system at --dims^3, three FP64 and three FP32 matvecs; 'st64' = the
     system and three products with its verified FP64 stencil; 'sell' = the
-    system's ELL layout and sliced copy, three products with each; 'cgfull' = the
+    system's ELL layout, its sliced copy and the CSR without box dimensions,
+    three products with each; 'cgfull' = the
     system, one whole FP64 solve to 1e-8 (--op) and the analytic check; 'cg' = the system
     and a 4-iteration CG solve; 'multi' = the system and a 6-iteration
     mixed-precision solve of 32 right-hand sides (reliable update every 3);
@@ -885,15 +886,19 @@ def run_probe(args):
         for _ in range(3):
             M.matvec_stencil64(S, x, y)
     elif args.probe == "sell":
-        # the reference's ELL layout, its sliced copy, three products with each
+        # the reference's ELL layout, its sliced copy and the CSR without its
+        # box dimensions (the generic kernel), three products with each
         x = torch.randn(A.nrows, dtype=torch.float64, device="cuda")
         y = torch.empty_like(x)
         E = M.ELLMatrix.from_csr(A)
         S = M.SELLMatrix.from_ell(E)
+        G = M.CSRMatrix(A.row_offsets, A.packed_cols, A.packed_coefs)
         for _ in range(3):
             M.matvec_ell(E, x, y)
         for _ in range(3):
             M.matvec_sell(S, x, y)
+        for _ in range(3):
+            M.matvec(G, x, y)
     elif args.probe == "spmv":
         x = torch.randn(A.nrows, dtype=torch.float64, device="cuda")
         y = torch.empty_like(x)

@@ -15,10 +15,15 @@
 //     overlap the current tile's FMAs;
 //   - x is gathered through the read-only path (27-point rows touch three
 //     x-planes, which stay L1/L2 resident).
+// Two forms of that scheme: FP64 rows go through the warp-staged kernel (a
+// warp per 32-row group with its own ring of stages and mbarriers, no block
+// barrier), FP32 rows through the tiled kernel (a block per 128-row tile).
+// The reference's row-major ELLMatrix has its own warp-staged kernel, whose
+// groups start aligned.
 // Epilogues: plain y = A x; y = A x with x.y (matvec_and_dot); and the CG
 // residual r = b - A x with r.r.  Dots accumulate in FP64 and reduce
 // deterministically (fixed grid, last block sums the block partials in order).
-// Matrices with rows longer than kMaxTileRowLen use a warp-per-row kernel.
+// Matrices with rows longer than 32 entries use a warp-per-row kernel.
 #include <algorithm>
 #include <cstdio>
 #include <cstdlib>
