@@ -496,8 +496,9 @@ mfe_status mfe_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E);
 mfe_status mfe_spmv_ell(mfe_ctx* ctx, const mfe_ell* E, const void* x, void* y);
 /* cg_solve with the ELL matvec (FP64; opts as for mfe_cg_solve).  Without
  * preconditioner the iterations' products run on a sliced copy of E
- * (mfe_sell, made once per call in context workspace); the initial and
- * final residuals use E itself. */
+ * (mfe_sell, made once per call in context workspace); the initial residual
+ * r = b - A x0 uses E itself, and the reported final residual is the
+ * recursive one, as cg_solve's (ref/src/cg_solve.hpp:152-163). */
 mfe_status mfe_cg_solve_ell(mfe_ctx* ctx, const mfe_ell* E, const double* b, double* x,
                             const mfe_cg_opts* opts, mfe_cg_result* result);
 

@@ -135,12 +135,15 @@ def test_long_rows_fallback():
     assert np.allclose(host(y), yo, rtol=1e-13, atol=1e-13)
 
 
-def test_ragged_generic_csr_tiled():
-    """Short ragged rows (<= 32) with odd nnz exercise the tiled kernel's
-    unaligned starts and array tail."""
-    rng = np.random.default_rng(4)
-    n = 3001
-    lens = rng.integers(0, 33, size=n)
+@pytest.mark.parametrize("n,seed", [(3001, 4), (33, 6), (31, 7), (2, 9)])
+def test_ragged_generic_csr_tiled(n, seed):
+    """Short ragged rows (<= 32 entries, some empty) with an odd nonzero
+    count: the FP64 warp-staged kernel's group starts off the 16-byte
+    boundaries and its plain-load tail of the arrays, and the FP32 tiled
+    kernel's; plain products and products with x.y, against the oracle
+    within the reordering bound."""
+    rng = np.random.default_rng(seed)
+    lens = rng.integers(0, min(33, n + 1), size=n)
     ro = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
     if ro[-1] % 2 == 0:
         lens[-1] = max(lens[-1] - 1, 0) if lens[-1] else 1
@@ -149,9 +152,24 @@ def test_ragged_generic_csr_tiled():
     vals = rng.standard_normal(cols.size)
     A = M.CSRMatrix(cuda(ro), cuda(cols), cuda(vals))
     x = rng.standard_normal(n)
-    y = torch.empty(n, dtype=torch.float64, device=DEV)
+    yo = O.matvec(ro, cols, vals, x)
+    bound = 36 * 2.0 ** -53 * O.matvec(ro, cols, np.abs(vals), np.abs(x)) + 1e-300
+    y = torch.full((n,), float("nan"), dtype=torch.float64, device=DEV)
     M.matvec(A, cuda(x), y)
-    assert np.allclose(host(y), O.matvec(ro, cols, vals, x), rtol=1e-13, atol=1e-13)
+    assert np.all(np.abs(host(y) - yo) <= bound)
+    y.fill_(float("nan"))
+    d = M.matvec_and_dot(A, cuda(x), y)
+    assert np.all(np.abs(host(y) - yo) <= bound)
+    assert abs(d - float(x @ yo)) <= 1e-12 * float(np.abs(x) @ np.abs(yo)) + 1e-300
+    v32 = vals.astype(np.float32)
+    x32 = x.astype(np.float32)
+    A32 = M.CSRMatrix(cuda(ro), cuda(cols), torch.from_numpy(v32).to(DEV))
+    y32 = torch.full((n,), float("nan"), dtype=torch.float32, device=DEV)
+    M.matvec(A32, torch.from_numpy(x32).to(DEV), y32)
+    yo32 = O.matvec(ro, cols, v32.astype(np.float64), x32.astype(np.float64))
+    b32 = 36 * 2.0 ** -24 * O.matvec(ro, cols, np.abs(v32.astype(np.float64)),
+                                     np.abs(x32.astype(np.float64))) + 1e-30
+    assert np.all(np.abs(host(y32).astype(np.float64) - yo32) <= b32)
 
 
 def test_cg_generic_csr_sliced_copy():
