@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(ROWS) k_spmv_tiled(SpmvParams<T> P)
 // memory with row_dot.  With rows of 27 entries an FP64 stage is 10.5 KB and
 // ten warps per SM each keep their next group in flight, where the tiled
 // kernel's 128-row tiles hold two blocks per SM behind block barriers: the
-// 256^3 FP64 product takes 1.42 ms against 2.09 ms through the tiled kernel
+// 256^3 FP64 product takes 1.14 ms against 2.09 ms through the tiled kernel
 // (FP32 rows, half the bytes per stage, stay on the tiled kernel: 0.715
 // against 0.75-0.80 ms).
 constexpr int kStgWarps = 2;    // warps per block
@@ -299,7 +299,7 @@ __host__ __device__ constexpr int stg_cap(int max_len, bool ell)
 // the arrays arrives by plain loads, as in the tiled kernel.
 // Five blocks per SM is the occupancy shared memory allows for 27-entry rows;
 // stating it (any minimum does) lets ptxas keep a row's gathers in flight at
-// 72 registers instead of 40: 1.155 against 1.40 ms for the 256^3 product
+// 72 registers instead of 40: 1.14-1.16 against 1.40 ms for the 256^3 product
 template <typename T, int MODE>
 __global__ void __launch_bounds__(kStgWarps * 32, 5) k_spmv_staged(SpmvParams<T> P, int max_len)
 {
