@@ -65,12 +65,24 @@ struct St64Params {
   CgState* cg;
 };
 
+// CTAs per SM of the grid (three fit at the 76 registers ptxas picks with no
+// minimum in the launch bounds): two give z runs half as
+// long again, i.e. fewer halo planes recomputed, and still enough warps to
+// keep the FP64 pipe fed -- measured at 256^3: 0.4842 ms per product against
+// 0.4893 with three and 0.4853 with one.  (Runs of 16-byte loads of the
+// window, masked afterwards, measured 0.517-0.66 ms: the load path is not
+// what bounds the kernel.)  The kernel's launch bounds state the same two
+// blocks, which lets ptxas use the registers the grid leaves free (110
+// instead of 76): 0.4796 against 0.4817 ms per product, 0.2859 against
+// 0.2867 s for the 256^3 CG, on one box in two interleaved rounds.
+constexpr int kSt64CtasPerSm = 2;
+
 // KP adjacent positions per thread (2 or 4): the window of a line is
 // x~[p0 - 1 .. p0 + KP], KP + 2 values; a plane's class sums cost KP + 2
 // additions (lines y - 1 and y + 1) plus 2 KP (sx, sxy), i.e. 3 + 2 / KP per
 // row.  DOT: accumulate p.Ap (the CG's SpMV) or not (a plain product).
 template <int KP, bool DOT>
-__global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64Params P)
+__global__ void __launch_bounds__(kT64, kSt64CtasPerSm) k_spmv_st64(const __grid_constant__ St64Params P)
 {
   constexpr int W = KP + 2;  // window length per line
   __shared__ double red[32];
@@ -249,13 +261,6 @@ __global__ void __launch_bounds__(kT64) k_spmv_st64(const __grid_constant__ St64
 // against 0.493 ms with two (and no difference between the read-only and the
 // L1-cached load paths)
 constexpr int kKP = 4;
-// CTAs per SM of the grid (3 fit: 74 registers): two give z runs half as
-// long again, i.e. fewer halo planes recomputed, and still enough warps to
-// keep the FP64 pipe fed -- measured at 256^3: 0.4842 ms per product against
-// 0.4893 with three and 0.4853 with one.  (Runs of 16-byte loads of the
-// window, masked afterwards, measured 0.517-0.66 ms: the load path is not
-// what bounds the kernel.)
-constexpr int kSt64CtasPerSm = 2;
 
 template <bool DOT>
 mfe_status st64_launch(mfe_ctx* ctx, St64Params& P)
