@@ -132,8 +132,11 @@ __device__ __forceinline__ void spmv_epilogue(double total, CgState* cg, double*
   }
 }
 
+// A minimum of two blocks per SM in the launch bounds (shared memory allows
+// three or four) lets ptxas keep a row's gathers in flight at 96 registers
+// instead of 32-40: the 256^3 FP32 product 0.638 against 0.714 ms
 template <typename T, int ROWS, int S, int MODE>
-__global__ void __launch_bounds__(ROWS) k_spmv_tiled(SpmvParams<T> P)
+__global__ void __launch_bounds__(ROWS, 2) k_spmv_tiled(SpmvParams<T> P)
 {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar[S];
@@ -279,8 +282,9 @@ __global__ void __launch_bounds__(ROWS) k_spmv_tiled(SpmvParams<T> P)
 // ten warps per SM each keep their next group in flight, where the tiled
 // kernel's 128-row tiles hold two blocks per SM behind block barriers: the
 // 256^3 FP64 product takes 1.14 ms against 2.09 ms through the tiled kernel
-// (FP32 rows, half the bytes per stage, stay on the tiled kernel: 0.715
-// against 0.75-0.80 ms).
+// (FP32 rows, half the bytes per stage, stay on the tiled kernel: 0.638
+// ms, where the staged form took 0.75-0.80 ms before either kernel stated
+// its blocks per SM).
 constexpr int kStgWarps = 2;    // warps per block
 constexpr int kStgStages = 2;   // stages per warp
 constexpr int kStgMaxLen = 32;  // longer rows: the warp-per-row kernel
@@ -422,8 +426,17 @@ __global__ void __launch_bounds__(kStgWarps * 32, 5) k_spmv_staged(SpmvParams<T>
 // stage addresses and keep a row's loads in flight together: 1.04 ms for the
 // 256^3 product against 1.13 ms with the size read from P.  MODE: plain or
 // the CG's initial residual.
+// FP32 rows also name the five blocks per SM in the launch bounds (122
+// registers: 0.579 against 0.595 ms at 256^3); FP64 rows name none (96
+// registers; five blocks: 104 registers and 1.058 against 1.040 ms)
+template <typename T>
+constexpr int ell_min_blocks()
+{
+  return sizeof(T) == 4 ? 5 : 0;
+}
+
 template <typename T, int MODE>
-__global__ void __launch_bounds__(kStgWarps * 32) k_spmv_ell(SpmvParams<T> P, int K)
+__global__ void __launch_bounds__(kStgWarps * 32, ell_min_blocks<T>()) k_spmv_ell(SpmvParams<T> P, int K)
 {
   extern __shared__ __align__(128) unsigned char smem[];
   __shared__ uint64_t bar[kStgWarps][kStgStages];
