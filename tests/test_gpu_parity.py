@@ -119,8 +119,8 @@ def test_matvec_fp32():
 
 
 def test_long_rows_fallback():
-    """A CSR with rows longer than the tiled kernel's limit takes the
-    warp-per-row kernel."""
+    """A CSR with rows longer than 32 entries (the staged and tiled kernels'
+    limit) takes the warp-per-row kernel."""
     rng = np.random.default_rng(3)
     n = 500
     lens = rng.integers(0, 80, size=n)
