@@ -181,7 +181,8 @@ mfe_status mfe_stencil64_from_csr(mfe_ctx* ctx, const mfe_csr* A, mfe_stencil64*
 mfe_status mfe_spmv_stencil64(mfe_ctx* ctx, const mfe_stencil64* S, const double* x, double* y);
 
 /* matvec_and_dot (ref/src/SparseMatrix_functions.hpp:491-536): y = A x and
- * *result = x . y (double, host), accumulated in FP64. */
+ * *result = x . y (double, host), accumulated in FP64.  Blocks for the
+ * scalar; returns MFE_TIMEOUT if the product gave up a bounded wait. */
 mfe_status mfe_matvec_and_dot(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
                               double* result);
 
@@ -238,11 +239,13 @@ mfe_status mfe_dot_f32(mfe_ctx* ctx, int64_t n, const float* x, const float* y,
                        double* result);
 
 /* Fault injection for tests of the bounded-wait error path; no counterpart
- * in the reference.  The next box-structured SpMV launched on ctx outside a
- * graph capture issues none of its shared-memory copies, so its consumers'
- * bounded waits run out after wait_ns nanoseconds (1 ms .. 2 s) with no copy
- * in flight; the call that launched it returns MFE_TIMEOUT (a solve) or
- * mfe_synchronize does (mfe_spmv).  The context stays usable. */
+ * in the reference.  The next SpMV with a shared-memory staging ring (the
+ * box-structured kernel, or the warp-staged kernels of an FP64 CSR with rows
+ * of at most 32 entries and of the ELL matrix) launched on ctx outside a
+ * graph capture issues none of its copies, so its bounded waits run out
+ * after wait_ns nanoseconds (1 ms .. 2 s) with no copy in flight; the call
+ * that launched it returns MFE_TIMEOUT (a solve) or mfe_synchronize does
+ * (mfe_spmv, mfe_spmv_ell).  The context stays usable. */
 mfe_status mfe_inject_wait_timeout(mfe_ctx* ctx, int64_t wait_ns);
 
 /* ------------------------------------------------------------------ */

@@ -463,7 +463,10 @@ mfe_status mfe_matvec_and_dot(mfe_ctx* ctx, const mfe_csr* A, const void* x, voi
   sink.ticket = ticket;
   sink.out = d;
   MFE_TRY(launch_spmv(ctx, A, x, y, &sink, nullptr, nullptr));
-  return read_scalar(ctx, d, result);
+  MFE_TRY(read_scalar(ctx, d, result));
+  // the call blocks for the scalar anyway: a bounded wait of the product that
+  // gave up is reported here, not at the next mfe_synchronize
+  return take_spmv_error(ctx);
 }
 
 mfe_status mfe_dot(mfe_ctx* ctx, int64_t n, const double* x, const double* y, double* result)

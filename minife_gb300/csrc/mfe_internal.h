@@ -31,8 +31,9 @@ struct mfe_ctx {
   std::vector<double> history;
   mfe_csr f32_copy{};
   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
-  // mfe_inject_wait_timeout: the next box-structured SpMV launched outside a
-  // graph capture withholds its copies; its waits give up after this long
+  // mfe_inject_wait_timeout: the next SpMV with a staging ring (the box
+  // kernel, the warp-staged CSR and ELL kernels) launched outside a graph
+  // capture withholds its copies; its waits give up after this long
   uint64_t inject_wait_ns = 0;
   // launch shape of the multi-RHS stencil SpMM (mfe_multi_set_tuning): z
   // steps per work item, 0 = the default
@@ -94,6 +95,9 @@ mfe_status ensure_max_row_len(mfe_ctx* ctx, const mfe_csr* A, int* max_len);
 mfe_status launch_spmv(mfe_ctx* ctx, const mfe_csr* A, const void* x, void* y,
                        const DotSink* sink, const double* resid_b, void* cg_state);
 mfe_status launch_spmm(mfe_ctx* ctx, const mfe_csr* A, int nrhs, const void* X, void* Y);
+// the pending mfe_inject_wait_timeout for a launch that runs now (0: none);
+// consumes it
+mfe_status take_wait_injection(mfe_ctx* ctx, uint64_t* withhold_ns);
 // y = E x or r = b - E x with r.r for the row-major ELL matrix (rows of up
 // to 64 entries and 16-byte aligned arrays on the warp-staged kernel; other
 // matrices, and products with x.y, through its CSR view)

@@ -57,6 +57,9 @@ struct SpmvParams {
   double* dot_out;  // used when cg == nullptr
   CgState* cg;      // CG bookkeeping in the last block (nullable)
   unsigned* err;
+  // fault injection (mfe_inject_wait_timeout), warp-staged kernels: nonzero =
+  // no copy is issued and the bounded waits give up after this many ns
+  uint64_t withhold_ns;
 };
 
 // Row sum with one FMA per nonzero.  Rows of up to LMAX entries run the same
@@ -354,11 +357,12 @@ __global__ void __launch_bounds__(kStgWarps * 32, 5) k_spmv_staged(SpmvParams<T>
     if (bytes_c) bulk_g2s(dc, P.cols + ac, bytes_c, &bar[w][s]);
   };
 
-  if (lane == 0)
+  if (lane == 0 && P.withhold_ns == 0)
     for (int s = 0; s < kStgStages; ++s) {
       const int64_t g = g0 + (int64_t)s * nw;
       if (g < ngroups) issue(__ldg(&P.ro[g * 32]), __ldg(&P.ro[min(P.n, g * 32 + 32)]), s);
     }
+  const uint64_t wait_ns = P.withhold_ns ? P.withhold_ns : kWaitLimitNs;
   double dacc = 0.0;
   bool ok = true;
   int it = 0;
@@ -380,7 +384,7 @@ __global__ void __launch_bounds__(kStgWarps * 32, 5) k_spmv_staged(SpmvParams<T>
       na = __ldg(&P.ro[gn * 32]);
       ne = __ldg(&P.ro[min(P.n, gn * 32 + 32)]);
     }
-    ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[w][s], (unsigned)((it / kStgStages) & 1)));
+    ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[w][s], (unsigned)((it / kStgStages) & 1), wait_ns));
     if (!ok) break;
     if (r < P.n) {
       const T* rv = reinterpret_cast<const T*>(wbase + (size_t)s * sbytes) + (ra - (a & ~(VA - 1)));
@@ -403,9 +407,9 @@ __global__ void __launch_bounds__(kStgWarps * 32, 5) k_spmv_staged(SpmvParams<T>
     if (lane == 0) {
       atomicOr(P.err, ERR_WAIT_TIMEOUT);
       // drain: give each stage with a copy issued a bounded chance to land
-      // before the block exits
+      // before the block exits (an injected fault issued none)
       for (int j = it; j < it + kStgStages; ++j)
-        if (g0 + (int64_t)j * nw < ngroups)
+        if (P.withhold_ns == 0 && g0 + (int64_t)j * nw < ngroups)
           mbar_wait_bounded(&bar[w][j % kStgStages], (unsigned)((j / kStgStages) & 1));
     }
     __syncwarp();
@@ -474,17 +478,18 @@ __global__ void __launch_bounds__(kStgWarps * 32, ell_min_blocks<T>()) k_spmv_el
     if (bytes_v) bulk_g2s(dv, P.vals + a, bytes_v, &bar[w][s]);
     if (bytes_c) bulk_g2s(dc, P.cols + a, bytes_c, &bar[w][s]);
   };
-  if (lane == 0)
+  if (lane == 0 && P.withhold_ns == 0)
     for (int s = 0; s < kStgStages; ++s) {
       const int64_t g = g0 + (int64_t)s * nw;
       if (g < ngroups) issue(g, s);
     }
+  const uint64_t wait_ns = P.withhold_ns ? P.withhold_ns : kWaitLimitNs;
   double dacc = 0.0;
   bool ok = true;
   int it = 0;
   for (int64_t g = g0; g < ngroups; g += nw, ++it) {
     const int s = it % kStgStages;
-    ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[w][s], (unsigned)((it / kStgStages) & 1)));
+    ok = __all_sync(0xffffffffu, mbar_wait_bounded(&bar[w][s], (unsigned)((it / kStgStages) & 1), wait_ns));
     if (!ok) break;
     const int64_t r = g * 32 + lane;
     if (r < P.n) {
@@ -508,7 +513,7 @@ __global__ void __launch_bounds__(kStgWarps * 32, ell_min_blocks<T>()) k_spmv_el
     if (lane == 0) {
       atomicOr(P.err, ERR_WAIT_TIMEOUT);
       for (int j = it; j < it + kStgStages; ++j)
-        if (g0 + (int64_t)j * nw < ngroups)
+        if (P.withhold_ns == 0 && g0 + (int64_t)j * nw < ngroups)
           mbar_wait_bounded(&bar[w][j % kStgStages], (unsigned)((j / kStgStages) & 1));
     }
     __syncwarp();
@@ -663,6 +668,21 @@ static int tiled_ctas_per_sm(size_t smem)
 }
 
 // ---- warp-staged kernels ----
+mfe_status take_wait_injection(mfe_ctx* ctx, uint64_t* withhold_ns)
+{
+  *withhold_ns = 0;
+  if (!ctx->inject_wait_ns) return MFE_OK;
+  // one-shot, and only for a launch that runs now (not one being captured
+  // into a graph, which would replay it)
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  MFE_CUDA_TRY(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
+  if (cs == cudaStreamCaptureStatusNone) {
+    *withhold_ns = ctx->inject_wait_ns;
+    ctx->inject_wait_ns = 0;
+  }
+  return MFE_OK;
+}
+
 template <typename T>
 static size_t staged_smem(int max_len, bool ell)
 {
@@ -697,6 +717,7 @@ static mfe_status launch_staged(mfe_ctx* ctx, SpmvParams<T>& P, int max_len)
   MFE_TRY(staged_configure(ctx, (const void*)k_spmv_staged<T, MODE>,
                            staged_smem<T>(kStgMaxLen, false), configured));
   P.cap = stg_cap(max_len, false);
+  MFE_TRY(take_wait_injection(ctx, &P.withhold_ns));
   k_spmv_staged<T, MODE><<<staged_grid<T>(ctx, P.n, max_len, false), kStgWarps * 32,
                            staged_smem<T>(max_len, false), ctx->stream>>>(P, max_len);
   return check_launch(ctx, "k_spmv_staged");
@@ -754,6 +775,7 @@ static mfe_status launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y, con
   P.ticket = sink ? sink->ticket : nullptr;
   P.dot_out = sink ? sink->out : nullptr;
   P.cg = cg;
+  P.withhold_ns = 0;
   P.err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
@@ -833,6 +855,7 @@ static mfe_status launch_ell_t(mfe_ctx* ctx, const mfe_ell* E, const T* x, T* y,
   P.err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
+  MFE_TRY(take_wait_injection(ctx, &P.withhold_ns));
   const int K = E->ncols_per_row;
   k_spmv_ell<T, MODE><<<staged_grid<T>(ctx, P.n, K, true), kStgWarps * 32, staged_smem<T>(K, true),
                         ctx->stream>>>(P, K);

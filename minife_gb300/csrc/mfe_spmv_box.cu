@@ -495,17 +495,7 @@ static mfe_status box_launch_t(mfe_ctx* ctx, const mfe_csr* A, const T* x, T* y,
   P.err = static_cast<unsigned*>(workspace(ctx, "spmv.err", sizeof(unsigned)));
   if (!P.err) return fail(ctx, MFE_OOM, "workspace allocation failed");
   if (cg) P.err = &cg->err;
-  P.withhold_ns = 0;
-  if (ctx->inject_wait_ns) {
-    // one-shot, and only for a launch that runs now (not one being captured
-    // into a graph, which would replay it)
-    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
-    MFE_CUDA_TRY(ctx, cudaStreamIsCapturing(ctx->stream, &cs));
-    if (cs == cudaStreamCaptureStatusNone) {
-      P.withhold_ns = ctx->inject_wait_ns;
-      ctx->inject_wait_ns = 0;
-    }
-  }
+  MFE_TRY(take_wait_injection(ctx, &P.withhold_ns));
   MFE_CUDA_TRY(ctx, box_configure(ctx->device));
   const size_t smem = box_smem<T>(sh.rows, sh.stages);
   const int64_t ntiles = ceil_div(A->nrows, sh.rows);

@@ -550,6 +550,87 @@ def test_bounded_wait_timeout_reports_and_recovers():
     assert np.allclose(host(y), yo, rtol=1e-13, atol=1e-13 * np.abs(yo).max())
 
 
+def _banded_spd(n=4099, h=8):
+    """A symmetric, diagonally dominant banded CSR (rows of 9 to 17 entries)
+    that no box layout check accepts."""
+    ro = [0]
+    cols, vals = [], []
+    for i in range(n):
+        for j in range(max(0, i - h), min(n, i + h + 1)):
+            cols.append(j)
+            vals.append(20.0 if i == j else -1.0 - 0.01 * ((i + j) % 7))
+        ro.append(len(cols))
+    return np.array(ro, np.int32), np.array(cols, np.int32), np.array(vals, np.float64)
+
+
+def test_bounded_wait_timeout_staged_kernels():
+    """The injected fault on the warp-staged kernels (a generic FP64 CSR, the
+    ELL matrix): lane 0 of every warp issues no copy, the waits give up after
+    20 ms with nothing in flight, and the error reaches the caller -- at
+    mfe_synchronize for a matvec, from the call itself for matvec_and_dot and
+    the solves (the initial residual is the staged product) -- after which
+    the same context computes normally."""
+    ctx = M.default_context()
+    ro, cols, vals = _banded_spd()
+    n = ro.size - 1
+    G = M.CSRMatrix(cuda(ro), cuda(cols), cuda(vals))
+    xr = np.random.default_rng(11).standard_normal(n)
+    yo = O.matvec(ro, cols, vals, xr)
+    tol = 1e-13 * np.abs(yo).max()
+    y = torch.empty(n, dtype=torch.float64, device=DEV)
+    M.inject_wait_timeout(20_000_000)
+    M.matvec(G, cuda(xr), y)
+    with pytest.raises(M.MiniFEError) as ei:
+        ctx.synchronize()
+    assert ei.value.status == 6
+    M.matvec(G, cuda(xr), y)
+    ctx.synchronize()
+    assert np.allclose(host(y), yo, rtol=1e-13, atol=tol)
+    M.inject_wait_timeout(20_000_000)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.matvec_and_dot(G, cuda(xr), y)
+    assert ei.value.status == 6
+    d = M.matvec_and_dot(G, cuda(xr), y)
+    assert abs(d - float(xr @ yo)) <= 1e-12 * float(np.abs(xr) @ np.abs(yo))
+    # the generic CG: its r = b - A x0 is the first staged product
+    b = np.random.default_rng(12).standard_normal(n)
+    x = torch.zeros(n, dtype=torch.float64, device=DEV)
+    M.inject_wait_timeout(20_000_000)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.cg_solve(G, cuda(b), x, max_iter=5, tol=1e-10, tol_mode="relative")
+    assert ei.value.status == 6
+    x.zero_()
+    res = M.cg_solve(G, cuda(b), x, max_iter=500, tol=1e-10, tol_mode="relative")
+    xo, it, nr, st = O.cg_solve(ro, cols, vals, b, max_iter=500, tol=1e-10, tol_mode=1)
+    assert res.status == 0 and abs(res.num_iters - it) <= 1
+    assert np.linalg.norm(host(x) - xo) <= 1e-11 * np.linalg.norm(xo)
+    # the ELL matrix of a box system: its matvec and its CG's initial residual
+    A, bb = M.build_system(8, 8, 8)
+    ro8, cols8, vals8, bo8 = O.build_system(8, 8, 8)
+    E = M.ELLMatrix.from_csr(A)
+    x8 = np.random.default_rng(13).standard_normal(A.nrows)
+    y8 = torch.empty(A.nrows, dtype=torch.float64, device=DEV)
+    M.inject_wait_timeout(20_000_000)
+    M.matvec_ell(E, cuda(x8), y8)
+    with pytest.raises(M.MiniFEError) as ei:
+        ctx.synchronize()
+    assert ei.value.status == 6
+    M.matvec_ell(E, cuda(x8), y8)
+    ctx.synchronize()
+    y8o = O.matvec(ro8, cols8, vals8, x8)
+    assert np.allclose(host(y8), y8o, rtol=1e-13, atol=1e-13 * np.abs(y8o).max())
+    xe = torch.zeros_like(bb)
+    M.inject_wait_timeout(20_000_000)
+    with pytest.raises(M.MiniFEError) as ei:
+        M.cg_solve_ell(E, bb, xe, max_iter=5, tol=1e-10, tol_mode="relative")
+    assert ei.value.status == 6
+    xe.zero_()
+    res = M.cg_solve_ell(E, bb, xe, max_iter=500, tol=1e-10, tol_mode="relative")
+    xo8, it8, _, _ = O.cg_solve(ro8, cols8, vals8, bo8, max_iter=500, tol=1e-10, tol_mode=1)
+    assert res.status == 0 and abs(res.num_iters - it8) <= 1
+    assert np.linalg.norm(host(xe) - xo8) <= 1e-11 * np.linalg.norm(xo8)
+
+
 @pytest.mark.parametrize("dims", [(4, 4, 4), (9, 5, 7), (30, 30, 30), (64, 33, 17)])
 def test_matvec_stencil64(dims):
     """The verified FP64 stencil operator row by row against the oracle's
