@@ -31,28 +31,45 @@ namespace mfe {
 
 namespace {
 
+// CSR -> row-major ELL, a warp per group of 32 rows: the group's output is
+// one contiguous range of 32 K entries (and its input one contiguous CSR
+// range), so lane l writes entries l, l + 32, ... of the range -- coalesced,
+// where a thread per row writes 27 entries 216 bytes apart -- reading each
+// row's bounds from shared memory.  Rows longer than K set *too_long (the
+// call then fails; their first K entries are written).
+constexpr int kCeW = 8;  // warps per block
 template <typename T>
-__global__ void k_csr_to_ell(int64_t n, int K, const int32_t* __restrict__ ro,
-                             const int32_t* __restrict__ cols, const T* __restrict__ vals,
-                             int32_t* __restrict__ ecols, T* __restrict__ evals, unsigned* too_long)
+__global__ void __launch_bounds__(kCeW * 32)
+    k_csr_to_ell(int64_t n, int K, const int32_t* __restrict__ ro, const int32_t* __restrict__ cols,
+                 const T* __restrict__ vals, int32_t* __restrict__ ecols, T* __restrict__ evals,
+                 unsigned* too_long)
 {
-  for (int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; r < n;
-       r += (int64_t)gridDim.x * blockDim.x) {
-    const int32_t a = ro[r], len = ro[r + 1] - a;
-    if (len > K) {
-      atomicOr(too_long, 1u);
-      continue;
+  __shared__ int32_t s_a[kCeW][32], s_len[kCeW][32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int64_t ngroups = (n + 31) / 32;
+  for (int64_t g = (int64_t)blockIdx.x * kCeW + w; g < ngroups; g += (int64_t)gridDim.x * kCeW) {
+    const int64_t r0 = g * 32;
+    const int rows = (int)min((int64_t)32, n - r0);
+    int32_t a = 0, len = 0;
+    if (lane < rows) {
+      a = __ldg(&ro[r0 + lane]);
+      len = __ldg(&ro[r0 + lane + 1]) - a;
     }
-    int32_t* c = ecols + r * K;
-    T* v = evals + r * K;
-    for (int k = 0; k < len; ++k) {
-      c[k] = cols[a + k];
-      v[k] = vals[a + k];
+    if (__any_sync(0xffffffffu, len > K) && lane == 0) atomicOr(too_long, 1u);
+    s_a[w][lane] = a;
+    s_len[w][lane] = min(len, K);
+    __syncwarp();
+    const int total = rows * K;
+    int32_t* c = ecols + r0 * K;
+    T* v = evals + r0 * K;
+    for (int e = lane; e < total; e += 32) {
+      const int row = e / K, k = e - row * K;
+      const bool in = k < s_len[w][row];
+      const int64_t src = (int64_t)s_a[w][row] + k;
+      c[e] = in ? __ldg(&cols[src]) : 0;
+      v[e] = in ? __ldg(&vals[src]) : T(0);
     }
-    for (int k = len; k < K; ++k) {
-      c[k] = 0;
-      v[k] = T(0);
-    }
+    __syncwarp();  // s_a / s_len are rewritten for the next group
   }
 }
 
@@ -247,13 +264,15 @@ mfe_status launch_csr_to_ell(mfe_ctx* ctx, const mfe_csr* A, mfe_ell* E)
   unsigned* flag = static_cast<unsigned*>(workspace(ctx, "ell.flag", sizeof(unsigned)));
   if (!flag) return fail(ctx, MFE_OOM, "workspace allocation failed");
   MFE_CUDA_TRY(ctx, cudaMemsetAsync(flag, 0, sizeof(unsigned), ctx->stream));
-  const int g = grid_for(ctx, A->nrows);
+  const int g = (int)std::max<int64_t>(
+      1, std::min<int64_t>(ceil_div(ceil_div(A->nrows, (int64_t)32), (int64_t)kCeW),
+                           (int64_t)ctx->sm_count * 8));
   if (A->dtype == MFE_F64)
-    k_csr_to_ell<double><<<g, 256, 0, ctx->stream>>>(
+    k_csr_to_ell<double><<<g, kCeW * 32, 0, ctx->stream>>>(
         A->nrows, E->ncols_per_row, A->row_offsets, A->cols, static_cast<const double*>(A->vals),
         E->cols, static_cast<double*>(E->vals), flag);
   else
-    k_csr_to_ell<float><<<g, 256, 0, ctx->stream>>>(
+    k_csr_to_ell<float><<<g, kCeW * 32, 0, ctx->stream>>>(
         A->nrows, E->ncols_per_row, A->row_offsets, A->cols, static_cast<const float*>(A->vals),
         E->cols, static_cast<float*>(E->vals), flag);
   MFE_TRY(check_launch(ctx, "k_csr_to_ell"));

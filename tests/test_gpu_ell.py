@@ -49,6 +49,19 @@ def test_ell_conversion_matvec_cg(dims):
     assert np.abs(xg.cpu().numpy() - xo).max() <= 1e-12
 
 
+@pytest.mark.parametrize("K", [27, 30, 64])
+def test_ell_conversion_padding(K):
+    """The conversion with more columns per row than the longest row (every
+    row padded with column 0, value 0) on 210 rows (a partial 32-row group),
+    bit for bit against numpy."""
+    A, b = M.build_system(4, 5, 6)
+    E = M.ELLMatrix.from_csr(A, K)
+    ro, cols, vals, bo = O.build_system(4, 5, 6)
+    ec, ev = np_ell(ro, cols, vals, K)
+    assert np.array_equal(E.cols.cpu().numpy(), ec)
+    assert np.array_equal(E.coefs.cpu().numpy(), ev)
+
+
 def test_ell_rejects_short_rows():
     A, b = M.build_system(5, 5, 5)
     with pytest.raises(M.MiniFEError) as ei:
