@@ -92,13 +92,16 @@ constexpr int kSellT = 256;     // threads per block
 // one block per slice at a time: the slice's rows [r0, r0 + 32) are one
 // contiguous row-major range of the ELL arrays; kSellKC of its columns at a
 // time go through shared memory, read coalesced along the rows and written
-// coalesced along the slice's column-major order
+// coalesced along the slice's column-major order.  Shared rows are kSellLD =
+// kSellKC + 1 long: the write-out reads one column of 32 rows, which at an
+// even stride would put all 32 lanes on one bank
+constexpr int kSellLD = kSellKC + 1;
 __global__ void __launch_bounds__(kSellT)
     k_ell_to_sell(int64_t n, int K, const int32_t* __restrict__ ec, const double* __restrict__ ev,
                   int32_t* __restrict__ sc, double* __restrict__ sv)
 {
-  __shared__ double tv[kSellRows * kSellKC];
-  __shared__ int32_t tc[kSellRows * kSellKC];
+  __shared__ double tv[kSellRows * kSellLD];
+  __shared__ int32_t tc[kSellRows * kSellLD];
   const int64_t nslices = (n + kSellRows - 1) / kSellRows;
   for (int64_t sl = blockIdx.x; sl < nslices; sl += gridDim.x) {
     const int64_t r0 = sl * kSellRows;
@@ -109,15 +112,15 @@ __global__ void __launch_bounds__(kSellT)
         const int lr = i / kc, k = i - lr * kc;
         const bool in = lr < rows;
         const int64_t e = (r0 + lr) * K + k0 + k;
-        tv[lr * kSellKC + k] = in ? ev[e] : 0.0;
-        tc[lr * kSellKC + k] = in ? ec[e] : 0;
+        tv[lr * kSellLD + k] = in ? ev[e] : 0.0;
+        tc[lr * kSellLD + k] = in ? ec[e] : 0;
       }
       __syncthreads();
       for (int i = threadIdx.x; i < kSellRows * kc; i += kSellT) {
         const int k = i / kSellRows, lr = i - k * kSellRows;
         const int64_t o = (sl * K + k0 + k) * kSellRows + lr;
-        sv[o] = tv[lr * kSellKC + k];
-        sc[o] = tc[lr * kSellKC + k];
+        sv[o] = tv[lr * kSellLD + k];
+        sc[o] = tc[lr * kSellLD + k];
       }
       __syncthreads();
     }
