@@ -539,8 +539,9 @@ def bench_next_rows(args, world, stream, A, b):
     (ELLMatrix: 27 entries per row, the reference's padded layout) -- its
     conversion from the CSR, its matvec against the bytes it moves (every
     padded entry's value and column, x and y once) and the FP64 CG with it to
-    1e-8 relative -- and the Jacobi-preconditioned CG to 1e-8 relative on the
-    CSR.  CUDA events, warm-up first."""
+    1e-8 relative -- the Jacobi-preconditioned CG to 1e-8 relative on the
+    CSR, and a CSR that is not a box matrix: its FP64 CG to 1e-8 and its
+    matvec against the bytes it moves.  CUDA events, warm-up first."""
     import torch
     import minife_gb300 as M
     n = A.nrows
@@ -608,7 +609,12 @@ def bench_next_rows(args, world, stream, A, b):
         return M.cg_solve(G, b, xs, max_iter=5000, tol=TOL, tol_mode="relative")
 
     t_gen, r_gen = ev_time(gen_solve, 1)
-    del xs, G, gcols, gvals
+    # the same CSR's matvec: the warp-staged kernel (rows of <= 32 entries)
+    xg = torch.randn(n, dtype=torch.float64, device="cuda")
+    yg = torch.empty_like(xg)
+    t_gmv, _ = ev_time(lambda: M.matvec(G, xg, yg), 10)
+    gen_bytes = A.nnz * (8 + 4) + n * 20
+    del xs, G, gcols, gvals, xg, yg
     torch.cuda.empty_cache()
     return {
         "ell": {"conversion_s": t_conv, "cg_s": t_ell, "iterations": r_ell.num_iters,
@@ -628,7 +634,11 @@ def bench_next_rows(args, world, stream, A, b):
         "generic_csr_cg": {"value": t_gen, "unit": "s", "iterations": r_gen.num_iters,
                            "final_rel_resid": r_gen.final_resid / r_gen.normr0,
                            "what": "FP64 CG on a CSR that is not a box matrix (one row's "
-                                   "columns rotated): the iterations on its sliced copy"},
+                                   "columns rotated): the iterations on its sliced copy",
+                           "spmv": {"ms": t_gmv * 1e3, "bytes": gen_bytes,
+                                    "achieved_gbs": gen_bytes / t_gmv / 1e9, "peak_gbs": peak,
+                                    "frac": gen_bytes / t_gmv / 1e9 / peak,
+                                    "kernel": "k_spmv_staged (a warp per 32-row group)"}},
     }
 
 
