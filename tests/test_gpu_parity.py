@@ -172,6 +172,31 @@ def test_ragged_generic_csr_tiled(n, seed):
     assert np.all(np.abs(host(y32).astype(np.float64) - yo32) <= b32)
 
 
+def test_generic_csr_unaligned_arrays():
+    """Columns and values that do not start on a 16-byte boundary (slices of
+    larger tensors) cannot be staged by bulk copies: the product takes the
+    warp-per-row kernel and matches the oracle, plain and with x.y."""
+    rng = np.random.default_rng(21)
+    n = 2049
+    lens = rng.integers(1, 28, size=n)
+    ro = np.concatenate([[0], np.cumsum(lens)]).astype(np.int32)
+    cols = np.concatenate([np.sort(rng.choice(n, size=l, replace=False)) for l in lens]).astype(np.int32)
+    vals = rng.standard_normal(cols.size)
+    cb = torch.zeros(cols.size + 1, dtype=torch.int32, device=DEV)
+    vb = torch.zeros(cols.size + 1, dtype=torch.float64, device=DEV)
+    cb[1:] = cuda(cols)
+    vb[1:] = cuda(vals)
+    A = M.CSRMatrix(cuda(ro), cb[1:], vb[1:])
+    x = rng.standard_normal(n)
+    yo = O.matvec(ro, cols, vals, x)
+    bound = 36 * 2.0 ** -53 * O.matvec(ro, cols, np.abs(vals), np.abs(x)) + 1e-300
+    y = torch.full((n,), float("nan"), dtype=torch.float64, device=DEV)
+    M.matvec(A, cuda(x), y)
+    assert np.all(np.abs(host(y) - yo) <= bound)
+    d = M.matvec_and_dot(A, cuda(x), y)
+    assert abs(d - float(x @ yo)) <= 1e-12 * float(np.abs(x) @ np.abs(yo))
+
+
 def test_cg_generic_csr_sliced_copy():
     """A CSR that is not a box matrix (symmetric banded, diagonally dominant,
     rows of 9 to 17 entries, 4,099 rows: a partial last slice): the FP64 CG
