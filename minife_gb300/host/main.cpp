@@ -20,7 +20,12 @@
 // reference's MINIFE_KERNELS timing loops instead of the CG solve), dump (1:
 // the reference's MINIFE_DEBUG files A_prebc.mtx, b_prebc.vec, A.mtx, b.vec,
 // A_local.mtx, b_local.vec, x.vec, each with the ".1.0" suffix), precond
-// (none | jacobi: diagonal-preconditioned CG).
+// (none | jacobi: diagonal-preconditioned CG), matrix (csr | ell: the
+// reference built with MINIFE_ELL_MATRIX, driver.hpp:172-176 -- the
+// assembled system held as its ELLMatrix, 27 entries per row, which the
+// report counts as the matrix's nonzeros and the matvecs and CG run on).
+// The dump files are written from the CSR form, whose rows are the ELL
+// rows without their padding.
 #include <sys/utsname.h>
 #include <unistd.h>
 
@@ -93,7 +98,7 @@ void check(mfe_ctx* ctx, mfe_status s, const char* what)
 struct Params {
   int nx, ny, nz, verify_solution, mv_overlap_comm_comp, numthreads, kernels, dump;
   float load_imbalance;
-  std::string name, precision, precond;
+  std::string name, precision, precond, matrix;
   int max_iters, refine_k, max_refine;
   double abs_tol, rel_tol, inner_tol;
 };
@@ -135,6 +140,11 @@ int main(int argc, char** argv)
   p.kernels = parse_parameter<int>(as, "kernels", 0);
   p.dump = parse_parameter<int>(as, "dump", 0);
   p.precond = parse_parameter<std::string>(as, "precond", "none");
+  p.matrix = parse_parameter<std::string>(as, "matrix", "csr");
+  if (p.matrix != "csr" && p.matrix != "ell") {
+    std::cerr << "miniFE.x: matrix must be csr or ell" << std::endl;
+    return 2;
+  }
 
   // print_params=1 on the command line: print the parsed parameters and stop
   // (no GPU needed); an input_file replaces the other arguments, as in the
@@ -145,7 +155,7 @@ int main(int argc, char** argv)
               << p.load_imbalance << "\nprecision " << p.precision << "\nmax_iters "
               << p.max_iters << "\nabs_tol " << p.abs_tol << "\nrel_tol " << p.rel_tol
               << "\nrefine_k " << p.refine_k << "\ninner_tol " << p.inner_tol << "\nmax_refine "
-              << p.max_refine << std::endl;
+              << p.max_refine << "\nmatrix " << p.matrix << std::endl;
     return 0;
   }
 
@@ -261,6 +271,28 @@ int main(int argc, char** argv)
     check(ctx, mfe_write_vector(ctx, nrows, b, 0, "b_local.vec"), "mfe_write_vector");
   }
 
+  // matrix=ell: the assembled system as the reference's ELLMatrix (27
+  // entries per row, padding column 0 / value 0), converted on the device
+  const bool ell = p.matrix == "ell";
+  mfe_ell E;
+  std::memset(&E, 0, sizeof(E));
+  double t_ell = 0;
+  if (ell) {
+    t0 = now();
+    E.ncols_per_row = 27;
+    check(ctx, mfe_device_alloc(ctx, 4 * (size_t)nrows * 27, (void**)&E.cols), "mfe_device_alloc");
+    check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows * 27, &E.vals), "mfe_device_alloc");
+    check(ctx, mfe_csr_to_ell(ctx, &A, &E), "mfe_csr_to_ell");
+    check(ctx, mfe_synchronize(ctx), "mfe_synchronize");
+    t_ell = now() - t0;
+  }
+  // the matrix's nonzeros as the reference counts them (num_nonzeros():
+  // every stored entry, ELLMatrix.hpp / CSRMatrix.hpp)
+  const int64_t nnz_rep = ell ? nrows * 27 : nnz;
+  auto spmv = [&](const double* xin, double* yout) {
+    return ell ? mfe_spmv_ell(ctx, &E, xin, yout) : mfe_spmv(ctx, &A, xin, yout);
+  };
+
   doc.add("Matrix structure generation", "")->add("Mat-struc-gen Time", gen_structure);
   doc.add("FE assembly", "")->add("FE assembly Time", fe_assembly);
 
@@ -268,20 +300,20 @@ int main(int argc, char** argv)
   {
     auto* ma = doc.add("Matrix attributes", "");
     ma->add("Global Nrows", (size_t)nrows);
-    ma->add("Global NNZ", (size_t)nnz);
+    ma->add("Global NNZ", (size_t)nnz_rep);
     const double invGB = 1.0 / (1024 * 1024 * 1024);
     double memGB = invGB * nrows * sizeof(int);
     memGB += invGB * nrows * sizeof(int);
-    memGB += invGB * nnz * sizeof(int);
-    memGB += invGB * nnz * sizeof(double);
+    memGB += invGB * nnz_rep * sizeof(int);
+    memGB += invGB * nnz_rep * sizeof(double);
     ma->add("Global Memory (GB)", memGB);
     ma->add("Pll Memory Overhead (MB)", 0);
     ma->add("Rows per proc MIN", (size_t)nrows);
     ma->add("Rows per proc MAX", (size_t)nrows);
     ma->add("Rows per proc AVG", (double)nrows);
-    ma->add("NNZ per proc MIN", (size_t)nnz);
-    ma->add("NNZ per proc MAX", (size_t)nnz);
-    ma->add("NNZ per proc AVG", (double)nnz);
+    ma->add("NNZ per proc MIN", (size_t)nnz_rep);
+    ma->add("NNZ per proc MAX", (size_t)nnz_rep);
+    ma->add("NNZ per proc AVG", (double)nnz_rep);
   }
 
   int verify_result = 0;
@@ -305,7 +337,7 @@ int main(int argc, char** argv)
     check(ctx, mfe_synchronize(ctx), "sync");
     const double t_wax = now() - s0;
     s0 = now();
-    for (int i = 0; i < iters; ++i) check(ctx, mfe_spmv(ctx, &A, pv, x), "mfe_spmv");
+    for (int i = 0; i < iters; ++i) check(ctx, spmv(pv, x), "matvec");
     check(ctx, mfe_synchronize(ctx), "sync");
     const double t_mv = now() - s0;
     s0 = now();
@@ -325,7 +357,7 @@ int main(int argc, char** argv)
     kt->add("Final Resid Norm", xdotp);
     // one of each operation per iteration (driver.hpp:337-342)
     const double global_nrows = (double)p.nx * p.ny * p.nz;
-    const double mv_flops = (double)nnz * 2.0 * iters;
+    const double mv_flops = (double)nnz_rep * 2.0 * iters;
     const double dot_flops = global_nrows * 2.0 * iters;
     const double waxpy_flops = global_nrows * 3.0 * iters;
     auto add_rate = [&](const char* key, double f, double t) {
@@ -342,7 +374,11 @@ int main(int argc, char** argv)
     kt->add("MATVEC Flops", mv_flops);
     add_rate("MATVEC Mflops", mv_flops, t_mv);
     auto* gpu = doc.add("GB300", "");
-    gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) * iters / t_mv * 1e-9);
+    gpu->add("matrix", ell ? "ELL" : "CSR");
+    if (ell)
+      gpu->add("MATVEC GB/s (values + columns + x + y)", (12.0 * nnz_rep + 16.0 * nrows) * iters / t_mv * 1e-9);
+    else
+      gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) * iters / t_mv * 1e-9);
     gpu->add("DOT GB/s (host-synchronous calls)", 16.0 * nrows * iters / t_dot * 1e-9);
     gpu->add("WAXPY GB/s", 24.0 * nrows * iters / t_wax * 1e-9);
   } else {
@@ -364,7 +400,7 @@ int main(int argc, char** argv)
     o.max_refine = p.max_refine;
     std::cout << "Starting CG solver ... " << std::endl;
     mfe_cg_result r;
-    const mfe_status st = mfe_cg_solve(ctx, &A, b, x, &o, &r);
+    const mfe_status st = ell ? mfe_cg_solve_ell(ctx, &E, b, x, &o, &r) : mfe_cg_solve(ctx, &A, b, x, &o, &r);
     if (st == MFE_BREAKDOWN) std::cerr << "miniFE::cg_solve ERROR, numerical breakdown!" << std::endl;
     else if (st != MFE_OK && st != MFE_MAXITER) check(ctx, st, "mfe_cg_solve");
     std::cout << "Initial Residual = " << r.normr0 << std::endl;
@@ -391,10 +427,10 @@ int main(int argc, char** argv)
       check(ctx, mfe_device_alloc(ctx, 8 * (size_t)nrows, (void**)&w), "mfe_device_alloc");
       double d = 0;
       const int reps = 5;
-      check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+      check(ctx, spmv(x, w), "matvec");
       check(ctx, mfe_synchronize(ctx), "sync");
       double s0 = now();
-      for (int i = 0; i < reps; ++i) check(ctx, mfe_spmv(ctx, &A, x, w), "mfe_spmv");
+      for (int i = 0; i < reps; ++i) check(ctx, spmv(x, w), "matvec");
       check(ctx, mfe_synchronize(ctx), "sync");
       t_mv = (now() - s0) / reps;
       s0 = now();
@@ -415,7 +451,7 @@ int main(int argc, char** argv)
     cg->add("Iterations", it);
     cg->add("Final Resid Norm", r.normr);
     const double global_nrows = (double)p.nx * p.ny * p.nz;
-    double mv_flops = (double)nnz * 2.0 * (it + 1);
+    double mv_flops = (double)nnz_rep * 2.0 * (it + 1);
     double dot_flops = global_nrows * 2.0 * (2 * it);
     double waxpy_flops = global_nrows * 3.0 * (3 * it + 2);
     const double tw = t_wax * (3 * it + 2), td = t_dot * (2 * it), tm = t_mv * (it + 1);
@@ -456,13 +492,23 @@ int main(int argc, char** argv)
                                      ? "FP32 stencil (verified)"
                                      : (r.inner_operator == MFE_INNER_VALUES ? "FP32 values" : "other"));
     gpu->add("op times", "standalone kernels scaled by operation counts");
-    gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) / t_mv * 1e-9);
+    gpu->add("matrix", ell ? "ELL" : "CSR");
+    if (ell) {
+      gpu->add("ELL conversion Time", t_ell);
+      gpu->add("MATVEC GB/s (values + columns + x + y)", (12.0 * nnz_rep + 16.0 * nrows) / t_mv * 1e-9);
+    } else {
+      gpu->add("MATVEC GB/s (values + x + y)", (8.0 * nnz + 16.0 * nrows) / t_mv * 1e-9);
+    }
     if (p.verify_solution > 0) gpu->add("verification", verify_result == 0 ? "passed" : "failed");
   }
 
   if (p.dump && !p.kernels) check(ctx, mfe_write_vector(ctx, nrows, x, 0, "x.vec"), "mfe_write_vector");
   mfe_device_free(ctx, b);
   mfe_device_free(ctx, x);
+  if (ell) {
+    mfe_device_free(ctx, E.cols);
+    mfe_device_free(ctx, E.vals);
+  }
   mfe_csr_free(ctx, &A);
   mfe_ctx_destroy(ctx);
   doc.add("Total Program Time", now() - t_program);

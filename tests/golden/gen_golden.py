@@ -8,6 +8,10 @@ Writes:
   tests/golden/minife_golden.npz   full arrays for small boxes
   tests/golden/golden_hashes.json  sha256 of every array for larger boxes
 
+With --ell it only writes tests/golden/ref_ell_nx10.json (also written by the
+full run): the report of the reference built with MINIFE_ELL_MATRIX at
+nx=10 (oracle/_ref/miniFE_ell.x).
+
 With --big N (run separately: the serial reference takes about 7 minutes at
 N = 256) it instead runs the N^3 box to a 1e-8 relative residual and writes
   tests/golden/golden_<N>.json     sha256 of every array, iteration count,
@@ -129,7 +133,43 @@ def big_case(n, workdir=None):
     print("wrote golden_%d.json and x%d_strided.npy (%d iterations)" % (n, n, meta["num_iters"]))
 
 
+def ell_report():
+    """The reference built with MINIFE_ELL_MATRIX (oracle/_ref/miniFE_ell.x)
+    at nx=10 with verify_solution=1: the report's values that the ELL layout
+    changes or must keep (Matrix attributes, the CG's iterations and final
+    residual, the flop counts) and its verification line, to
+    tests/golden/ref_ell_nx10.json."""
+    exe = os.path.join(ROOT, "oracle", "_ref", "miniFE_ell.x")
+    if not os.path.exists(exe):
+        sys.exit("build the reference first: make -C oracle ref REF=$REF")
+    with tempfile.TemporaryDirectory() as tmp:
+        run = subprocess.run([exe, "nx=10", "verify_solution=1"], cwd=tmp, capture_output=True,
+                             text=True, check=True)
+        yml = [f for f in os.listdir(tmp) if f.endswith(".yaml")][0]
+        section, vals = None, {}
+        for line in open(os.path.join(tmp, yml)):
+            if ":" not in line:
+                continue
+            indent = len(line) - len(line.lstrip(" "))
+            key, _, val = line.strip().partition(":")
+            if indent == 0:
+                section = key
+            elif section in ("Matrix attributes", "CG solve") and indent == 2 and val.strip():
+                vals["%s/%s" % (section, key)] = val.strip()
+    keep = ["Matrix attributes/Global Nrows", "Matrix attributes/Global NNZ",
+            "Matrix attributes/Global Memory (GB)", "Matrix attributes/NNZ per proc MAX",
+            "CG solve/Iterations", "CG solve/Final Resid Norm", "CG solve/MATVEC Flops",
+            "CG solve/DOT Flops", "CG solve/WAXPY Flops"]
+    out = {k: vals[k] for k in keep}
+    out["verified"] = "solution matches analytic solution" in run.stdout
+    with open(os.path.join(HERE, "ref_ell_nx10.json"), "w") as f:
+        json.dump(out, f, indent=1, sort_keys=True)
+    print("wrote ref_ell_nx10.json")
+
+
 def main():
+    if "--ell" in sys.argv:
+        return ell_report()
     if "--big" in sys.argv:
         if not os.path.exists(HARNESS):
             sys.exit("build the reference harness first: make -C oracle ref REF=$REF")
@@ -192,6 +232,7 @@ def main():
                         "dump"], cwd=tmp, check=True)
         for name in ("A_prebc.mtx", "b_prebc.vec", "A.mtx", "b.vec", "x.vec"):
             shutil.copy(os.path.join(tmp, name + ".1.0"), os.path.join(ddir, name + ".1.0"))
+    ell_report()
     np.savez_compressed(os.path.join(HERE, "minife_golden.npz"), **out)
     with open(os.path.join(HERE, "golden_hashes.json"), "w") as f:
         json.dump(hashes, f, indent=1, sort_keys=True)

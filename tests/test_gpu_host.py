@@ -61,6 +61,38 @@ def test_minife_x_reference_run(tmp_path):
     assert int(yaml_value(yml, "Global NNZ")) == 29791
 
 
+def test_minife_x_ell_matrix(tmp_path):
+    """./miniFE.x nx=10 verify_solution=1 matrix=ell against the reference
+    built with MINIFE_ELL_MATRIX (tests/golden/ref_ell_nx10.json, written by
+    that build): the same key tree, the ELL's padded nonzeros (27 per row) in
+    Matrix attributes and in the matvec flop count, the reference's
+    iterations and an absolute DBL_EPSILON stop, the analytic check passed.
+    Then kernels=1 times the ELL matvec."""
+    import json
+    ref = json.load(open(os.path.join(ROOT, "tests", "golden", "ref_ell_nx10.json")))
+    r, yml = run_driver(tmp_path, "nx=10", "verify_solution=1", "matrix=ell")
+    assert r.returncode == 0, r.stdout + r.stderr
+    assert ref["verified"] and "solution matches analytic solution" in r.stdout
+    keys = [k for k in open(os.path.join(ROOT, "tests", "golden", "ref_yaml_keys.txt")).read().split("\n") if k]
+    missing = [k for k in keys if k not in yaml_keys(yml)]
+    assert not missing, missing
+    for k in ("Global Nrows", "Global NNZ", "NNZ per proc MAX"):
+        assert yaml_value(yml, k) == ref["Matrix attributes/" + k], k
+    assert abs(float(yaml_value(yml, "Global Memory (GB)")) -
+               float(ref["Matrix attributes/Global Memory (GB)"])) <= 1e-9
+    it = int(yaml_value(yml, "Iterations"))
+    assert abs(it - int(ref["CG solve/Iterations"])) <= 1
+    assert float(yaml_value(yml, "Final Resid Norm")) <= 2.220446049250313e-16
+    # the report prints six significant digits
+    assert abs(float(yaml_value(yml, "MATVEC Flops")) / (35937 * 2.0 * (it + 1)) - 1) <= 1e-5
+    assert yaml_value(yml, "matrix") == "ELL"
+    kdir = tmp_path / "kernels"
+    kdir.mkdir()
+    r2, yml2 = run_driver(kdir, "nx=10", "matrix=ell", "kernels=1")
+    assert r2.returncode == 0, r2.stdout + r2.stderr
+    assert abs(float(yaml_value(yml2, "MATVEC Flops")) / (35937 * 2.0 * 500) - 1) <= 1e-5
+
+
 def test_minife_x_mixed_relative(tmp_path):
     r, yml = run_driver(tmp_path, "-nx", "24", "-ny", "20", "-nz", "16", "precision=mixed",
                         "rel_tol=1e-8", "max_iters=3000", "verify_solution=1", "name=mx")
