@@ -6,6 +6,8 @@
 // host code compiles against the GB300 implementation unchanged:
 //
 //   CSRMatrix<S,LO,GO>   ref/src/CSRMatrix.hpp:43-129   (same fields)
+//   ELLMatrix<S,LO,GO>   ref/src/ELLMatrix.hpp:41-130   (same fields; the
+//                        reference built with MINIFE_ELL_MATRIX)
 //   Vector<S,LO,GO>      ref/src/Vector.hpp:36-61       (same fields)
 //   matvec_std<M,V>      ref/src/SparseMatrix_functions.hpp:545-578
 //   matvec_and_dot       ref/src/SparseMatrix_functions.hpp:491-536
@@ -26,6 +28,7 @@
 // local box is the global box).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstring>
 #include <set>
@@ -131,6 +134,51 @@ struct CSRMatrix {
   }
 };
 
+// ELLMatrix: num_cols_per_row entries per row, row-major, each row's
+// columns ascending and then padding with column 0, value 0
+// (MatrixInitOp<ELLMatrix>, MatrixInitOp.hpp:160-220)
+template <typename Scalar, typename LocalOrdinal, typename GlobalOrdinal>
+struct ELLMatrix {
+  static_assert(std::is_same<Scalar, double>::value && std::is_same<LocalOrdinal, int>::value &&
+                    std::is_same<GlobalOrdinal, int>::value,
+                "minife_gb300 supports ELLMatrix<double,int,int>");
+  typedef Scalar ScalarType;
+  typedef LocalOrdinal LocalOrdinalType;
+  typedef GlobalOrdinal GlobalOrdinalType;
+
+  bool has_local_indices = false;
+  std::vector<GlobalOrdinal> rows;
+  std::vector<GlobalOrdinal> cols;
+  std::vector<Scalar> coefs;
+  LocalOrdinal num_cols = 0;
+  LocalOrdinal num_cols_per_row = 0;
+
+  size_t num_nonzeros() const { return rows.size() * (size_t)num_cols_per_row; }
+  void reserve_space(unsigned nrows, unsigned ncols_per_row)
+  {
+    rows.resize(nrows);
+    cols.resize((size_t)nrows * ncols_per_row);
+    coefs.resize((size_t)nrows * ncols_per_row);
+    num_cols_per_row = (LocalOrdinal)ncols_per_row;
+  }
+  // one rank: rows[i] == i.  The row's length ends at its last entry with a
+  // nonzero column, as the reference's (ELLMatrix.hpp:122-128): the padding
+  // after it has column 0
+  void get_row_pointers(GlobalOrdinal row, size_t& row_length, GlobalOrdinal*& cols_ptr,
+                        Scalar*& coefs_ptr)
+  {
+    if (row < 0 || (size_t)row >= rows.size()) {
+      row_length = 0;
+      return;
+    }
+    cols_ptr = &cols[(size_t)row * num_cols_per_row];
+    coefs_ptr = &coefs[(size_t)row * num_cols_per_row];
+    int idx = num_cols_per_row - 1;
+    while (idx >= 0 && cols_ptr[idx] == 0) --idx;
+    row_length = (size_t)(idx + 1);
+  }
+};
+
 template <typename Scalar, typename LocalOrdinal, typename GlobalOrdinal>
 struct Vector {
   typedef Scalar ScalarType;
@@ -176,6 +224,50 @@ mfe_csr upload(const M& A)
   h2d(m.vals, A.packed_coefs.data(), 8 * (size_t)m.nnz);
   return m;
 }
+
+template <typename S, typename LO, typename GO>
+mfe_ell upload_ell(const ELLMatrix<S, LO, GO>& A)
+{
+  Context& c = Context::get();
+  mfe_ell e;
+  std::memset(&e, 0, sizeof(e));
+  e.nrows = (int64_t)A.rows.size();
+  e.ncols_per_row = A.num_cols_per_row;
+  e.dtype = MFE_F64;
+  const size_t ne = A.rows.size() * (size_t)A.num_cols_per_row;
+  e.cols = static_cast<int32_t*>(c.buf(SLOT_COLS, 4 * ne + 16));
+  e.vals = c.buf(SLOT_VALS, 8 * ne + 16);
+  h2d(e.cols, A.cols.data(), 4 * ne);
+  h2d(e.vals, A.coefs.data(), 8 * ne);
+  return e;
+}
+
+// an ELL matrix's device CSR (from mfe_csr m) converted in the shim's ELL
+// buffers and copied into A: columns when structure, always the values
+template <typename S, typename LO, typename GO>
+void download_ell(const mfe_csr& m, ELLMatrix<S, LO, GO>& A, bool structure)
+{
+  Context& c = Context::get();
+  const int K = 27;
+  const size_t ne = (size_t)m.nrows * K;
+  mfe_ell e;
+  std::memset(&e, 0, sizeof(e));
+  e.ncols_per_row = K;
+  e.cols = static_cast<int32_t*>(c.buf(SLOT_X2, 4 * ne + 16));
+  e.vals = c.buf(SLOT_Y2, 8 * ne + 16);
+  c.check(mfe_csr_to_ell(c.h(), &m, &e), "mfe_csr_to_ell");
+  if (structure) {
+    A.rows.resize((size_t)m.nrows);
+    for (int64_t i = 0; i < m.nrows; ++i) A.rows[(size_t)i] = (int)i;
+    A.cols.resize(ne);
+    d2h(A.cols.data(), e.cols, 4 * ne);
+    A.num_cols_per_row = K;
+    A.has_local_indices = true;
+    A.num_cols = (int)m.nrows;
+  }
+  A.coefs.resize(ne);
+  d2h(A.coefs.data(), e.vals, 8 * ne);
+}
 }  // namespace detail
 
 // matvec_std<CSR>: y = A x (SparseMatrix_functions.hpp:548-577)
@@ -190,6 +282,23 @@ struct matvec_std {
     double* dy = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
     detail::h2d(dx, x.coefs.data(), 8 * n);
     c.check(mfe_spmv(c.h(), &m, dx, dy), "mfe_spmv");
+    detail::d2h(y.coefs.data(), dy, 8 * n);
+  }
+};
+
+// matvec_std<ELLMatrix> (SparseMatrix_functions.hpp:579-611): every stored
+// entry, the padding adding 0 * x[0]
+template <typename S, typename LO, typename GO, typename VectorType>
+struct matvec_std<ELLMatrix<S, LO, GO>, VectorType> {
+  void operator()(ELLMatrix<S, LO, GO>& A, VectorType& x, VectorType& y)
+  {
+    Context& c = Context::get();
+    mfe_ell e = detail::upload_ell(A);
+    const size_t n = A.rows.size();
+    double* dx = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+    double* dy = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
+    detail::h2d(dx, x.coefs.data(), 8 * n);
+    c.check(mfe_spmv_ell(c.h(), &e, dx, dy), "mfe_spmv_ell");
     detail::d2h(y.coefs.data(), dy, 8 * n);
   }
 };
@@ -285,6 +394,33 @@ void impose_dirichlet(double prescribed_value, MatrixType& A, VectorType& b, int
           "mfe_impose_dirichlet");
   detail::d2h(A.packed_coefs.data(), m.vals, 8 * A.packed_coefs.size());
   detail::d2h(b.coefs.data(), db, 8 * n);
+}
+
+// impose_dirichlet for the ELLMatrix: the rows as get_row_pointers gives
+// them (the padding left out) go through the same device kernel as a CSR,
+// and the values come back into the ELL rows
+template <typename S, typename LO, typename GO, typename VectorType>
+void impose_dirichlet(double prescribed_value, ELLMatrix<S, LO, GO>& A, VectorType& b,
+                      int global_nx, int global_ny, int global_nz, const std::set<int>& bc_rows)
+{
+  CSRMatrix<S, LO, GO> C;
+  const size_t n = A.rows.size();
+  C.rows = A.rows;
+  C.row_offsets.assign(n + 1, 0);
+  std::vector<size_t> len(n);
+  for (size_t r = 0; r < n; ++r) {
+    GO* cp = nullptr;
+    S* vp = nullptr;
+    A.get_row_pointers((GO)r, len[r], cp, vp);
+    C.row_offsets[r + 1] = C.row_offsets[r] + (LO)len[r];
+    C.packed_cols.insert(C.packed_cols.end(), cp, cp + len[r]);
+    C.packed_coefs.insert(C.packed_coefs.end(), vp, vp + len[r]);
+  }
+  impose_dirichlet(prescribed_value, C, b, global_nx, global_ny, global_nz, bc_rows);
+  const size_t K = (size_t)A.num_cols_per_row;
+  for (size_t r = 0; r < n; ++r)
+    std::copy(C.packed_coefs.begin() + C.row_offsets[r], C.packed_coefs.begin() + C.row_offsets[r + 1],
+              A.coefs.begin() + r * K);
 }
 
 // ---- the assembly side, one rank ----
@@ -383,6 +519,20 @@ int generate_matrix_structure(const simple_mesh_description<GlobalOrdinal>& mesh
   return 0;
 }
 
+// generate_matrix_structure for the ELLMatrix (MatrixInitOp.hpp:160-220):
+// 27 entries per row, each row's columns ascending, then column 0 padding
+template <typename GlobalOrdinal, typename S, typename LO, typename GO>
+int generate_matrix_structure(const simple_mesh_description<GlobalOrdinal>& mesh,
+                              ELLMatrix<S, LO, GO>& A)
+{
+  Context& c = Context::get();
+  const int nx = mesh.global_box[0][1], ny = mesh.global_box[1][1], nz = mesh.global_box[2][1];
+  mfe_csr m = detail::box_csr(nx, ny, nz);
+  c.check(mfe_generate_structure(c.h(), nx, ny, nz, &m), "mfe_generate_structure");
+  detail::download_ell(m, A, true);
+  return 0;
+}
+
 // perform_element_loop (perform_element_loop.hpp:40-104) over the whole
 // box: every element's diffusion matrix and source vector summed into A
 // (whose structure generate_matrix_structure made) and b, in element
@@ -402,6 +552,30 @@ void perform_element_loop(const simple_mesh_description<GlobalOrdinal>& mesh, co
   double* db = static_cast<double*>(c.buf(detail::SLOT_X, 8 * (size_t)m.nrows + 16));
   c.check(mfe_assemble(c.h(), nx, ny, nz, nullptr, &m, db, 0), "mfe_assemble");
   detail::download(m, A, false);
+  b.coefs.resize((size_t)m.nrows);
+  detail::d2h(b.coefs.data(), db, 8 * (size_t)m.nrows);
+}
+
+// perform_element_loop for the ELLMatrix: the same element sums, held in the
+// ELL rows (A's structure from generate_matrix_structure)
+template <typename GlobalOrdinal, typename S, typename LO, typename GO, typename VectorType,
+          typename Params>
+void perform_element_loop(const simple_mesh_description<GlobalOrdinal>& mesh, const Box& box,
+                          ELLMatrix<S, LO, GO>& A, VectorType& b, Params& /*params*/)
+{
+  for (int d = 0; d < 3; ++d)
+    if (box[d][0] != mesh.local_box[d][0] || box[d][1] != mesh.local_box[d][1])
+      throw Error(MFE_NOT_SUPPORTED, "perform_element_loop: the element box is the local box");
+  Context& c = Context::get();
+  const int nx = mesh.global_box[0][1], ny = mesh.global_box[1][1], nz = mesh.global_box[2][1];
+  mfe_csr m = detail::box_csr(nx, ny, nz);
+  if (A.rows.size() != (size_t)m.nrows || A.num_cols_per_row != 27 ||
+      A.cols.size() != (size_t)m.nrows * 27)
+    throw Error(MFE_BAD_ARG, "perform_element_loop: A lacks the box's ELL structure");
+  c.check(mfe_generate_structure(c.h(), nx, ny, nz, &m), "mfe_generate_structure");
+  double* db = static_cast<double*>(c.buf(detail::SLOT_X, 8 * (size_t)m.nrows + 16));
+  c.check(mfe_assemble(c.h(), nx, ny, nz, nullptr, &m, db, 0), "mfe_assemble");
+  detail::download_ell(m, A, false);
   b.coefs.resize((size_t)m.nrows);
   detail::d2h(b.coefs.data(), db, 8 * (size_t)m.nrows);
 }
@@ -438,6 +612,38 @@ void cg_solve(OperatorType& A, const VectorType& b, VectorType& x, Matvec /*matv
   } else if (s != MFE_OK && s != MFE_MAXITER) {
     c.check(s, "mfe_cg_solve_host");
   }
+  num_iters = r.num_iters;
+  normr = r.normr;
+  if (my_cg_times)
+    for (int t = 0; t < NUM_TIMERS; ++t) my_cg_times[t] = r.times[t];
+}
+
+// cg_solve with the ELLMatrix (the reference built with MINIFE_ELL_MATRIX):
+// the library's ELL CG (mfe_cg_solve_ell)
+template <typename S, typename LO, typename GO, typename VectorType, typename Matvec>
+void cg_solve(ELLMatrix<S, LO, GO>& A, const VectorType& b, VectorType& x, Matvec /*matvec*/,
+              LO max_iter, double& tolerance, LO& num_iters, double& normr,
+              timer_type* my_cg_times)
+{
+  Context& c = Context::get();
+  mfe_ell e = detail::upload_ell(A);
+  const size_t n = A.rows.size();
+  double* db = static_cast<double*>(c.buf(detail::SLOT_X, 8 * n + 16));
+  double* dx = static_cast<double*>(c.buf(detail::SLOT_Y, 8 * n + 16));
+  detail::h2d(db, b.coefs.data(), 8 * n);
+  detail::h2d(dx, x.coefs.data(), 8 * n);
+  mfe_cg_opts o;
+  mfe_cg_opts_default(&o);
+  o.max_iter = max_iter;
+  o.tol = tolerance;
+  mfe_cg_result r;
+  const mfe_status s = mfe_cg_solve_ell(c.h(), &e, db, dx, &o, &r);
+  if (s == MFE_BREAKDOWN) {
+    // the reference reports breakdown on std::cerr and returns (cg_solve.hpp:188)
+  } else if (s != MFE_OK && s != MFE_MAXITER) {
+    c.check(s, "mfe_cg_solve_ell");
+  }
+  detail::d2h(x.coefs.data(), dx, 8 * n);
   num_iters = r.num_iters;
   normr = r.normr;
   if (my_cg_times)

@@ -3,7 +3,9 @@
 // generate_matrix_structure, assemble_FE_data and the two impose_dirichlet
 // calls on the reference's CSRMatrix / Vector types in host memory, then
 // matvec, dot, waxpby, fused_waxpby and cg_solve with the reference's
-// signatures.  Prints "key value" lines for tests/test_gpu_host.py.
+// signatures; then the same sequence on the ELLMatrix type (the reference
+// built with MINIFE_ELL_MATRIX), compared with the CSR run.  Prints "key
+// value" lines for tests/test_gpu_host.py.
 #include <cstdio>
 #include <algorithm>
 #include <cmath>
@@ -60,5 +62,46 @@ int main(int argc, char** argv)
   for (double v : x.coefs) xs += v;
   std::printf("num_iters %d\nnormr %.17g\nx_sum %.17g\ntotal_time %.6g\n", num_iters, normr, xs,
               times[TOTAL]);
+
+  // the ELL build: structure, element loop, both Dirichlet passes, then the
+  // rows (padding left out) against the CSR's, a matvec and the solve
+  typedef ELLMatrix<double, int, int> Ell;
+  Ell E;
+  generate_matrix_structure(mesh, E);
+  Vec be(0, (int)n), xe(0, (int)n);
+  assemble_FE_data(mesh, E, be, params);
+  impose_dirichlet(0.0, E, be, nx, ny, nz, mesh.bc_rows_0);
+  impose_dirichlet(1.0, E, be, nx, ny, nz, mesh.bc_rows_1);
+  int same = E.num_cols_per_row == 27 && E.num_nonzeros() == (size_t)n * 27;
+  for (int64_t r = 0; r < n && same; ++r) {
+    size_t len = 0, clen = 0;
+    int *ec = nullptr, *cc = nullptr;
+    double *ev = nullptr, *cv = nullptr;
+    E.get_row_pointers((int)r, len, ec, ev);
+    A.get_row_pointers((int)r, clen, cc, cv);
+    same = len == clen;
+    for (size_t k = 0; k < len && same; ++k) same = ec[k] == cc[k] && ev[k] == cv[k];
+    for (size_t k = len; k < 27 && same; ++k) same = ec[k] == 0 && ev[k] == 0.0;
+  }
+  for (int64_t i = 0; i < n && same; ++i) same = be.coefs[i] == b.coefs[i];
+  std::printf("ell_same_as_csr %d\n", same);
+  for (int64_t i = 0; i < n; ++i) xe.coefs[i] = 1.0 / (1.0 + i);
+  Vec ye(0, (int)n);
+  matvec(E, xe, ye);
+  matvec(A, xe, y);
+  double md = 0;
+  for (int64_t i = 0; i < n; ++i) md = std::max(md, std::fabs(ye.coefs[i] - y.coefs[i]));
+  std::printf("ell_matvec_diff %.17g\n", md);
+  for (int64_t i = 0; i < n; ++i) xe.coefs[i] = 0.0;
+  int ell_iters = 0;
+  double ell_normr = 0, tol2 = 2.220446049250313e-16;
+  cg_solve(E, be, xe, matvec_std<Ell, Vec>(), 200, tol2, ell_iters, ell_normr, times);
+  double xd = 0, xm = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    xd = std::max(xd, std::fabs(xe.coefs[i] - x.coefs[i]));
+    xm = std::max(xm, std::fabs(x.coefs[i]));
+  }
+  std::printf("ell_num_iters %d\nell_normr %.17g\nell_x_rel_diff %.17g\n", ell_iters, ell_normr,
+              xd / xm);
   return 0;
 }

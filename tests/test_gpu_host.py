@@ -170,3 +170,11 @@ def test_cpp_shim_matches_oracle(tmp_path):
     xo, it, nr, st = O.cg_solve(ro, cols, vals, b)
     assert abs(int(v["num_iters"]) - it) <= 2
     assert abs(v["x_sum"] - xo.sum()) <= 1e-11 * np.abs(xo).sum()
+    # the ELLMatrix run: rows (padding left out) and b bit for bit the CSR's,
+    # the same matvec (the padding adds exact zeros), the CG of the
+    # reference's ELL build within one iteration and rounding of the CSR's
+    assert int(v["ell_same_as_csr"]) == 1
+    assert v["ell_matvec_diff"] == 0.0
+    assert abs(int(v["ell_num_iters"]) - int(v["num_iters"])) <= 1
+    assert v["ell_normr"] <= 2.220446049250313e-16
+    assert v["ell_x_rel_diff"] <= 1e-12
