@@ -13,6 +13,8 @@
 //   matvec_and_dot       ref/src/SparseMatrix_functions.hpp:491-536
 //   dot, waxpby, fused_waxpby  ref/src/Vector_functions.hpp:127-226
 //   impose_dirichlet     ref/src/SparseMatrix_functions.hpp:434-480
+//   write_matrix, write_vector  SparseMatrix_functions.hpp:98-140,
+//                        Vector_functions.hpp:49-82 (MINIFE_DEBUG dumps)
 //   cg_solve             ref/src/cg_solve.hpp:69-229
 //   Box, simple_mesh_description (bc_rows_0 / bc_rows_1)
 //                        ref/utils/Box.hpp, ref/src/simple_mesh_description.hpp:39-224
@@ -31,6 +33,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <fstream>
 #include <set>
 #include <stdexcept>
 #include <string>
@@ -421,6 +424,37 @@ void impose_dirichlet(double prescribed_value, ELLMatrix<S, LO, GO>& A, VectorTy
   for (size_t r = 0; r < n; ++r)
     std::copy(C.packed_coefs.begin() + C.row_offsets[r], C.packed_coefs.begin() + C.row_offsets[r + 1],
               A.coefs.begin() + r * K);
+}
+
+// write_matrix / write_vector (SparseMatrix_functions.hpp:98-140,
+// Vector_functions.hpp:49-82; MINIFE_DEBUG), one rank: "<filename>.1.0"
+// holding "nrows nnz" (nnz = num_nonzeros(), the ELL's padded count) and one
+// "row col coef" line per entry of each row as get_row_pointers gives it, or
+// "n" and one "index coef" line per entry; the default std::ostream number
+// format.  The containers are on the host, so these only format them.
+template <typename MatrixType>
+void write_matrix(const std::string& filename, MatrixType& mat)
+{
+  std::ofstream ofs((filename + ".1.0").c_str());
+  if (!ofs) throw Error(MFE_BAD_ARG, "write_matrix: cannot open " + filename + ".1.0");
+  ofs << mat.rows.size() << " " << mat.num_nonzeros() << std::endl;
+  for (size_t i = 0; i < mat.rows.size(); ++i) {
+    size_t len = 0;
+    typename MatrixType::GlobalOrdinalType* cols = nullptr;
+    typename MatrixType::ScalarType* coefs = nullptr;
+    mat.get_row_pointers(mat.rows[i], len, cols, coefs);
+    for (size_t j = 0; j < len; ++j) ofs << mat.rows[i] << " " << cols[j] << " " << coefs[j] << std::endl;
+  }
+}
+
+template <typename VectorType>
+void write_vector(const std::string& filename, const VectorType& vec)
+{
+  std::ofstream ofs((filename + ".1.0").c_str());
+  if (!ofs) throw Error(MFE_BAD_ARG, "write_vector: cannot open " + filename + ".1.0");
+  ofs << vec.local_size << std::endl;
+  for (size_t i = 0; i < (size_t)vec.local_size; ++i)
+    ofs << vec.startIndex + (typename VectorType::GlobalOrdinalType)i << " " << vec.coefs[i] << std::endl;
 }
 
 // ---- the assembly side, one rank ----

@@ -11,6 +11,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <set>
+#include <string>
 #include <vector>
 
 #include "minife_gb300.hpp"
@@ -33,6 +34,12 @@ int main(int argc, char** argv)
   assemble_FE_data(mesh, A, b, params);
   impose_dirichlet(0.0, A, b, nx, ny, nz, mesh.bc_rows_0);
   impose_dirichlet(1.0, A, b, nx, ny, nz, mesh.bc_rows_1);
+  // a fourth argument "dump": the reference's MINIFE_DEBUG files of the system
+  const bool dump = argc > 4 && std::string(argv[4]) == "dump";
+  if (dump) {
+    write_matrix("A.mtx", A);
+    write_vector("b.vec", b);
+  }
   std::printf("bc_rows_0 %zu\nbc_rows_1 %zu\n", mesh.bc_rows_0.size(), mesh.bc_rows_1.size());
   A.has_local_indices = true;
   A.num_cols = (int)n;
@@ -72,6 +79,7 @@ int main(int argc, char** argv)
   assemble_FE_data(mesh, E, be, params);
   impose_dirichlet(0.0, E, be, nx, ny, nz, mesh.bc_rows_0);
   impose_dirichlet(1.0, E, be, nx, ny, nz, mesh.bc_rows_1);
+  if (dump) write_matrix("A_ell.mtx", E);
   int same = E.num_cols_per_row == 27 && E.num_nonzeros() == (size_t)n * 27;
   for (int64_t r = 0; r < n && same; ++r) {
     size_t len = 0, clen = 0;

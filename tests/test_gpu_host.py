@@ -139,6 +139,31 @@ def test_minife_x_dump_files_match_reference(tmp_path):
     assert np.allclose(xs, xo, rtol=1e-5, atol=1e-12)
 
 
+def test_cpp_shim_dump_files(tmp_path):
+    """The shim's write_matrix / write_vector on the 2x3x2 box after both
+    Dirichlet passes: byte for byte the files the reference itself wrote
+    (tests/golden/dumps_2x3x2).  The ELLMatrix's file is the same rows under
+    the header the reference's ELL build writes, its padded nonzero count
+    (36 rows x 27)."""
+    exe = os.path.join(tmp_path, "shim_solve")
+    from minife_gb300 import build
+    build.build()
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "shim_solve.cpp"), "-L",
+                    os.path.join(ROOT, "minife_gb300"), "-lminife_gb300",
+                    "-Wl,-rpath," + os.path.join(ROOT, "minife_gb300"), "-o", exe], check=True)
+    subprocess.run([exe, "2", "3", "2", "dump"], cwd=tmp_path, capture_output=True, text=True,
+                   check=True)
+    gold = os.path.join(ROOT, "tests", "golden", "dumps_2x3x2")
+    for name in ("A.mtx.1.0", "b.vec.1.0"):
+        assert open(os.path.join(tmp_path, name), "rb").read() == \
+            open(os.path.join(gold, name), "rb").read(), name
+    ell = open(os.path.join(tmp_path, "A_ell.mtx.1.0")).read().split("\n")
+    csr = open(os.path.join(gold, "A.mtx.1.0")).read().split("\n")
+    assert ell[0] == "36 %d" % (36 * 27)
+    assert ell[1:] == csr[1:]
+
+
 def test_cpp_shim_matches_oracle(tmp_path):
     exe = os.path.join(tmp_path, "shim_solve")
     from minife_gb300 import build
